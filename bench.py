@@ -1,0 +1,308 @@
+#!/usr/bin/env python3
+"""Benchmark of the GPU path tracer on the 1M-triangle GGX + IBL scene.
+
+Workload (one "step"): a full render of the ~1.03M-triangle scene (512 x 512
+height field displaced by 6-octave improved Perlin noise + 64 geodesic
+spheres of 8000 triangles, GGX conductors and dielectrics, a seeded 512 x 256
+log-normal environment with a 2-degree sun of radiance 5e4) at 1024 x 1024,
+64 samples per pixel, max depth 10.  The scene is synthetic and seeded.
+
+* value      - path samples/s with the scene resident in HBM; device time of
+               the render measured with CUDA events on the launching stream.
+* e2e        - the same metric through the C ABI with host buffers: each step
+               copies the scene from pinned host memory to the device
+               (slrgpu_scene_reupload), renders and reads the film back.
+* roofline   - the dominant kernel's algorithmic bytes per launch (48 B per
+               closest-hit query: 32 B ray in, 16 B hit out; 36 B per any-hit
+               query; 792 B per shaded bounce) over its average launch time.
+* cpu_baseline - the reference renderer (the CPU oracle built from the
+               reference's own sources) on a bounded sample of the same scene.
+
+``--impl reference`` times the reference renderer alone (rank 0) on a
+bounded sample of the same workload.  Under torchrun each rank renders its
+own replica (weak scaling; path samples are independent, no collective).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WIDTH = HEIGHT = 1024
+SPP = 64
+MAX_DEPTH = 10
+METRIC = "path samples/s"
+WORKLOAD = ("ggx_ibl_1m: 1,034,242-triangle height field (512x512, 6-octave improved Perlin, amplitude 0.2) "
+            "+ 64 geodesic spheres (8000 triangles, scale log-uniform 0.05-0.3), GGX conductors/dielectrics "
+            "(alpha 0.05-0.6, anisotropy 0-0.8, eta 1.3-1.7), 512x256 log-normal IBL + 2-degree sun (5e4), "
+            "1024x1024, 64 spp, max depth 10, seed 0")
+
+# Algorithmic bytes per unit (per closest-hit query, per any-hit query, per
+# shaded bounce, per path sample for the film).
+BYTES_EXTEND = 48
+BYTES_SHADOW = 36
+BYTES_SHADE = 792
+BYTES_FILM = 256
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """Samples nvidia-smi SM clocks and throttle reasons while running."""
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def cpu_baseline(desc, threads: int, seconds_target: float = 12.0):
+    """Reference renderer on a bounded sample: full-resolution frames at 1 spp
+    until about seconds_target of CPU work (scene build excluded)."""
+    from oracle import oracle as O
+    t0 = time.time()
+    ref = O.RefScene(desc)
+    build_s = time.time() - t0
+    total_samples, total_s, frames = 0, 0.0, 0
+    while total_s < seconds_target and frames < 16:
+        _, s = ref.render(WIDTH, HEIGHT, 1, MAX_DEPTH, seed=frames, threads=threads)
+        total_samples += WIDTH * HEIGHT
+        total_s += s
+        frames += 1
+    return {"value": total_samples / total_s, "unit": METRIC, "cores": threads, "kind": "reference",
+            "sample": f"{frames} frame(s) of the same scene at {WIDTH}x{HEIGHT}, 1 spp, max depth {MAX_DEPTH} "
+                      f"({total_samples} path samples, {total_s:.1f} s; SBVH build {build_s:.1f} s excluded)"}
+
+
+def run_reference(args):
+    world, rank, _ = dist_setup()
+    if rank != 0:
+        return 0
+    from oracle import oracle as O
+    from slr_gb300 import scenes
+    threads = os.cpu_count() or 1
+    desc = scenes.heightfield_scene(seed=0)
+    ref = O.RefScene(desc)
+    times = []
+    for i in range(args.warmup + args.steps):
+        _, s = ref.render(WIDTH, HEIGHT, 1, MAX_DEPTH, seed=i, threads=threads)
+        if i >= args.warmup:
+            times.append(s)
+    per_step = WIDTH * HEIGHT
+    value = per_step * len(times) / sum(times)
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded procedural scene)",
+            "config": {"workload": WORKLOAD, "step": f"{WIDTH}x{HEIGHT} at 1 spp (bounded sample of the 64-spp frame)"},
+            "cpu_baseline": {"value": value, "unit": METRIC, "cores": threads, "kind": "reference",
+                             "sample": f"{args.steps} frames at {WIDTH}x{HEIGHT}, 1 spp, max depth {MAX_DEPTH}"},
+            "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--spp", type=int, default=SPP)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import numpy as np
+    import torch
+    from slr_gb300 import api, scenes
+
+    world, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    spp = args.spp
+    desc = scenes.heightfield_scene(seed=0)
+    ctx = api.Context(local)
+    t0 = time.time()
+    scene = api.Scene(desc, context=ctx)
+    build_s = time.time() - t0
+    st = scene.bvh_stats
+    seed_base = 1000 * rank
+    l2_flush = torch.empty(256 * 1024 * 1024, dtype=torch.float32, device="cuda")
+
+    film_dev = torch.empty((HEIGHT, WIDTH, 16), dtype=torch.float32, device="cuda")
+    for i in range(args.warmup):
+        scene.render(WIDTH, HEIGHT, spp, MAX_DEPTH, seed=seed_base + i, film=film_dev)
+    torch.cuda.synchronize()
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    step_ms, launches = [], 0
+    kern_ms = [0.0] * 5
+    kern_n = [0] * 5
+    ext_rays = sh_rays = dropped = 0
+    for i in range(args.steps):
+        l2_flush.zero_()
+        barrier()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        _, rs = scene.render(WIDTH, HEIGHT, spp, MAX_DEPTH, seed=seed_base + 100 + i, film=film_dev,
+                             flags=api.FLAG_PROFILE_KERNELS)
+        e1.record()
+        torch.cuda.synchronize()
+        barrier()
+        step_ms.append(e0.elapsed_time(e1))
+        launches += rs.kernel_launches
+        for k in range(5):
+            kern_ms[k] += rs.kernel_ms[k]
+            kern_n[k] += rs.kernel_count[k]
+        ext_rays += rs.extension_rays
+        sh_rays += rs.shadow_rays
+        dropped += rs.dropped_samples
+    clk = clocks.stop()
+    total_ms = sum(step_ms)
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([total_ms], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    samples_per_step = WIDTH * HEIGHT * spp
+    value = samples_per_step * args.steps * world / (total_ms * 1e-3)
+
+    # End to end through the C ABI with host buffers.
+    film_host = torch.empty((HEIGHT, WIDTH, 16), dtype=torch.float32, pin_memory=True)
+    film_np = film_host.numpy()
+    e2e_ms, h2d = [], 0
+    for i in range(max(1, args.steps)):
+        barrier()
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        h2d = scene.reupload()
+        scene.render(WIDTH, HEIGHT, spp, MAX_DEPTH, seed=seed_base + 200 + i, film=film_np)
+        torch.cuda.synchronize()
+        e2e_ms.append(1e3 * (time.perf_counter() - t1))
+    e2e_total = sum(e2e_ms)
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([e2e_total], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_total = float(t.item())
+    e2e_value = samples_per_step * len(e2e_ms) * world / (e2e_total * 1e-3)
+
+    # Roofline of the dominant kernel.
+    names = api.KERNEL_CLASSES
+    dom = max(range(5), key=lambda k: kern_ms[k])
+    units = {1: (ext_rays, BYTES_EXTEND), 3: (sh_rays, BYTES_SHADOW), 2: (ext_rays, BYTES_SHADE),
+             0: (samples_per_step * args.steps, 64), 4: (samples_per_step * args.steps, BYTES_FILM)}
+    n_units, per_unit = units[dom]
+    bytes_per_launch = n_units * per_unit / max(1, kern_n[dom])
+    avg_launch_s = kern_ms[dom] * 1e-3 / max(1, kern_n[dom])
+    achieved = bytes_per_launch / avg_launch_s / 1e9
+    peak, peak_kind = load_peaks()
+    roofline = {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "peak_source": peak_kind, "traffic": None,
+                "bytes_per_unit": per_unit, "units_per_launch": n_units / max(1, kern_n[dom]),
+                "avg_launch_ms": avg_launch_s * 1e3,
+                "kernel_share": {names[k]: kern_ms[k] / max(1e-9, sum(kern_ms)) for k in range(5)}}
+    line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
+            "config": {"workload": WORKLOAD, "width": WIDTH, "height": HEIGHT, "spp": spp, "max_depth": MAX_DEPTH,
+                       "triangles": st.num_triangles, "sbvh_fragments": st.num_fragments,
+                       "bvh_width": st.width, "parallelism": f"replicas x{world}",
+                       "l2": "path state (GBs) exceeds L2; 1 GiB buffer written between timed steps",
+                       "scene_build_s": round(build_s, 2)},
+            "rays_per_s": (ext_rays + sh_rays) * world / (total_ms * 1e-3),
+            "dropped_samples": dropped,
+            "gpu_launches": launches,
+            "roofline": roofline,
+            "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": WIDTH * HEIGHT * 16 * 4, "ms_per_step": e2e_total / len(e2e_ms)},
+            "clocks": clk}
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(desc, os.cpu_count() or 1)
+    if rank == 0:
+        print(json.dumps(line))
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

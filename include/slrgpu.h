@@ -1,0 +1,210 @@
+/*
+ * slrgpu.h - C ABI of the GB300 path tracer (drop-in for SLR's PTRenderer and
+ * VolumetricPTRenderer).
+ *
+ * Plain C: opaque 64-bit handles, plain pointers and sizes, int status codes
+ * (0 = success, negative = error; slrgpu_last_error() returns the message of
+ * the calling thread's last failure).  Arrays passed in are copied before the
+ * call returns; the caller keeps ownership.  One context per GPU; calls on
+ * different scenes may come from different threads.
+ *
+ * The entry points replace the reference's C++ interfaces as follows (paths
+ * are relative to the reference project):
+ *   scene construction  - libSLR/Scene/Scene.h:31-36 (Scene(root), build),
+ *                         libSLR/Scene/TriangleMeshNode.h:37-73,
+ *                         libSLR/Scene/node.h:125-141 (InfiniteSphereNode),
+ *                         libSLR/Scene/medium_nodes.h:33-48 (DensityGridMediumNode),
+ *                         libSLR/Scene/camera_nodes.h:16-54
+ *   spectra             - libSLR/BasicTypes/spectrum_types.h:90-190
+ *                         (Regular/Irregular/UpsampledContinuousSpectrum)
+ *   materials           - libSLR/SurfaceMaterial/basic_surface_materials.h:20-57,
+ *                         microfacet_surface_materials.h:21-37,
+ *                         libSLR/Core/surface_material.h:55-69 (EmitterSurfaceMaterial)
+ *   rendering           - libSLR/Core/renderer.h:15-19 (Renderer::render),
+ *                         libSLR/Renderer/PTRenderer.h:42-43,
+ *                         libSLR/Renderer/VolumetricPTRenderer.h:43-44
+ *   film                - libSLR/Core/ImageSensor.h:47-48 (pixel(x, y))
+ *   ray queries         - libSLR/Core/accelerator.h:16-30 (intersect / testVisibility)
+ */
+#ifndef SLRGPU_H
+#define SLRGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SLRGPU_OK 0
+#define SLRGPU_ERR_INVALID_ARGUMENT (-1)
+#define SLRGPU_ERR_INVALID_HANDLE   (-2)
+#define SLRGPU_ERR_CUDA             (-3)
+#define SLRGPU_ERR_OUT_OF_MEMORY    (-4)
+#define SLRGPU_ERR_NOT_COMMITTED    (-5)
+#define SLRGPU_ERR_STATE            (-6)
+#define SLRGPU_ERR_TIMEOUT          (-7)
+
+typedef uint64_t slrgpu_handle;
+
+/* Spectrum types (libSLR/BasicTypes/spectrum_base.h:34-38). */
+#define SLRGPU_SPECTRUM_REFLECTANCE 0
+#define SLRGPU_SPECTRUM_LIGHT_SOURCE 1
+#define SLRGPU_SPECTRUM_INDEX_OF_REFRACTION 2
+
+typedef struct slrgpu_bvh_stats {
+    uint32_t num_triangles;   /* input primitives */
+    uint32_t num_fragments;   /* SBVH leaf references after spatial splits */
+    uint32_t depth;           /* binary SBVH depth */
+    uint32_t num_binary_nodes;
+    uint32_t num_wide_nodes;  /* after collapse to the wide layout */
+    uint32_t width;           /* children per wide node (4 or 8) */
+    float sah_cost;           /* SAH cost as printed at SBVH.h:415 */
+    float build_seconds;
+} slrgpu_bvh_stats;
+
+typedef struct slrgpu_settings {
+    uint32_t width, height;       /* film size in pixels */
+    uint32_t spp;                 /* samples per pixel */
+    uint32_t max_depth;           /* scattering vertices with NEE + BSDF sampling */
+    uint32_t seed;                /* RNG seed (RenderSettingItem::RNGSeed) */
+    uint32_t volumetric;          /* 0: PTRenderer, 1: VolumetricPTRenderer */
+    uint32_t samples_per_wave;    /* 0: automatic; paths in flight = W*H*this */
+    uint32_t flags;               /* SLRGPU_FLAG_* */
+} slrgpu_settings;
+
+/* settings.flags: record CUDA events around every launch and report the
+ * device time per kernel class in slrgpu_render_stats.kernel_ms. */
+#define SLRGPU_FLAG_PROFILE_KERNELS 1u
+
+/* Kernel classes of the wavefront (index into kernel_ms / kernel_count). */
+#define SLRGPU_KERNEL_RAYGEN 0
+#define SLRGPU_KERNEL_EXTEND 1
+#define SLRGPU_KERNEL_SHADE 2
+#define SLRGPU_KERNEL_SHADOW 3
+#define SLRGPU_KERNEL_ACCUMULATE 4
+#define SLRGPU_KERNEL_CLASSES 8
+
+typedef struct slrgpu_render_stats {
+    double seconds;               /* wall time of the call */
+    double kernel_seconds;        /* device time of the render kernels */
+    uint64_t path_samples;        /* W*H*spp */
+    uint64_t extension_rays;      /* closest-hit queries traced */
+    uint64_t shadow_rays;         /* any-hit queries traced */
+    uint64_t dropped_samples;     /* non-finite contributions dropped */
+    uint64_t kernel_launches;
+    double kernel_ms[SLRGPU_KERNEL_CLASSES];      /* with SLRGPU_FLAG_PROFILE_KERNELS */
+    uint64_t kernel_count[SLRGPU_KERNEL_CLASSES];
+} slrgpu_render_stats;
+
+/* Context ------------------------------------------------------------- */
+int slrgpu_context_create(int device, slrgpu_handle* ctx);
+int slrgpu_context_destroy(slrgpu_handle ctx);
+const char* slrgpu_last_error(void);
+int slrgpu_version(void);
+
+/* Scene --------------------------------------------------------------- */
+int slrgpu_scene_create(slrgpu_handle ctx, slrgpu_handle* scene);
+int slrgpu_scene_destroy(slrgpu_handle scene);
+
+/* Spectra: each returns a scene-local spectrum id in *id. */
+int slrgpu_spectrum_rgb(slrgpu_handle scene, int spectrum_type, float r, float g, float b, int* id);
+int slrgpu_spectrum_regular(slrgpu_handle scene, float min_wl, float max_wl,
+                            const float* values, uint32_t num_values, int* id);
+int slrgpu_spectrum_irregular(slrgpu_handle scene, const float* wavelengths, const float* values,
+                              uint32_t num_values, int* id);
+
+/* Materials: each returns a scene-local material id in *id. */
+int slrgpu_material_matte(slrgpu_handle scene, int reflectance, int* id);
+int slrgpu_material_specular_reflection(slrgpu_handle scene, int coeff, int eta, int k, int* id);
+int slrgpu_material_specular_scattering(slrgpu_handle scene, int coeff, int eta_ext, int eta_int, int* id);
+int slrgpu_material_microfacet_reflection(slrgpu_handle scene, int eta, int k,
+                                          float alpha_x, float alpha_y, int* id);
+int slrgpu_material_microfacet_scattering(slrgpu_handle scene, int eta_ext, int eta_int,
+                                          float alpha_x, float alpha_y, int* id);
+int slrgpu_material_emitter(slrgpu_handle scene, int base_material, int emittance, int* id);
+
+/* Geometry: world-space vertices (positions/normals/tangents xyz, uvs uv),
+ * triangles as vertex index triples. */
+int slrgpu_scene_add_mesh(slrgpu_handle scene, const float* positions, const float* normals,
+                          const float* tangents, const float* uvs, uint32_t num_vertices,
+                          const uint32_t* indices, uint32_t num_triangles, int material);
+
+/* Image-based environment: width*height linear RGBA texels as IEEE binary16
+ * bit patterns; emitted radiance is texel * scale. */
+int slrgpu_environment_ibl(slrgpu_handle scene, const uint16_t* rgba_half, uint32_t width,
+                           uint32_t height, float scale);
+
+/* Heterogeneous medium over an axis-aligned box: density[nz][ny][nx]
+ * multiplies the sigma_s / sigma_e spectra; Henyey-Greenstein phase g. */
+int slrgpu_medium_density_grid(slrgpu_handle scene, const float* bounds_min, const float* bounds_max,
+                               int sigma_s, int sigma_e, const float* density, uint32_t nx,
+                               uint32_t ny, uint32_t nz, float hg_g);
+
+/* Cameras: cam_to_world is a row-major 4x4 matrix. */
+int slrgpu_camera_perspective(slrgpu_handle scene, const float* cam_to_world, float sensitivity,
+                              float aspect, float fov_y, float lens_radius, float img_plane_dist,
+                              float obj_plane_dist);
+int slrgpu_camera_equirect(slrgpu_handle scene, const float* cam_to_world, float sensitivity,
+                           float phi_angle, float theta_angle);
+
+/* Builds the SBVH, collapses it to the wide layout and uploads the scene to
+ * device memory.  stats may be NULL. */
+int slrgpu_scene_commit(slrgpu_handle scene, slrgpu_bvh_stats* stats);
+
+/* Copies every device array of a committed scene again from its pinned host
+ * mirror (stream-ordered before the next render); *bytes receives the bytes
+ * copied.  This is the host-to-device part of an end-to-end render in which
+ * the scene lives on the host. */
+int slrgpu_scene_reupload(slrgpu_handle scene, uint64_t* bytes);
+
+/* Rendering ----------------------------------------------------------- */
+/* Blocking render.  film receives width*height*16 floats: per pixel (row
+ * major) the 16-bin spectral sum over all samples, the value the reference's
+ * ImageSensor::pixel(x, y) returns after PTRenderer::render.  film is a
+ * host pointer, or a device pointer when film_on_device is nonzero. */
+int slrgpu_render(slrgpu_handle scene, const slrgpu_settings* settings, float* film,
+                  int film_on_device, slrgpu_render_stats* stats);
+
+/* Ray queries on the committed scene (device pointers).  rays: n x 8 floats
+ * (org.xyz, tmin, dir.xyz, tmax).  Closest hit fills prim (0xffffffff on
+ * miss), t, b1, b2 (Moller-Trumbore barycentrics); any hit fills prim with 1
+ * (occluded) or 0.  stream is a cudaStream_t or NULL. */
+int slrgpu_trace(slrgpu_handle scene, const float* rays, uint32_t n, int any_hit, uint32_t* prim,
+                 float* t, float* b1, float* b2, void* stream);
+
+/* BSDF queries on the GPU at fixed inputs (the reference's BSDF::sample /
+ * evaluate / evaluatePDF, directional_distribution_functions.h:295-349, on
+ * LambertianBRDF, SpecularBRDF, SpecularBSDF, MicrofacetBRDF, MicrofacetBSDF;
+ * kind 0..4 in that order).  spec0..2: 16 values each (R | coeff, eta, k |
+ * coeff, etaExt, etaInt | eta, k | etaExt, etaInt).  Per query 16 floats:
+ * dir.xyz, gnormal.xyz, wavelength index, adjoint (0), uComponent, uDir0,
+ * uDir1, eval dir.xyz, 0, 0.  Per result 40 floats: sampled fs[16], sampled
+ * dir.xyz, sampled pdf, sampled direction type, evaluated fs[16], evaluated
+ * pdf, 0, 0.  Host arrays. */
+int slrgpu_bsdf_query(int kind, const float* spec0, const float* spec1, const float* spec2, float alpha_x,
+                      float alpha_y, const float* queries, uint32_t n, float* out);
+
+/* Diagnostics (host side, no GPU needed) ------------------------------ */
+/* Builds the SBVH and the other host tables without uploading
+ * (the part of SurfaceObjectAggregate's constructor, surface_object.cpp:373-399,
+ * and Scene::build, Scene.cpp:17-38, that runs on the CPU). */
+int slrgpu_scene_build_host(slrgpu_handle scene, slrgpu_bvh_stats* stats);
+/* Binary SBVH node dump (SBVH.h:21-43 node fields): per node boxes[6]
+ * (min xyz, max xyz) and words[5] (c0, c1, first leaf, leaf count,
+ * split axis or 0xffffffff for leaves); leaf_prims[num_fragments]. */
+int slrgpu_scene_sbvh_dump(slrgpu_handle scene, float* boxes, uint32_t* words, uint32_t* leaf_prims);
+/* Host evaluation of a spectrum at num_sets x 16 wavelengths
+ * (ContinuousSpectrum::evaluate, spectrum_types.h:72-80). */
+int slrgpu_spectrum_evaluate(slrgpu_handle scene, int id, const float* lambdas, uint32_t num_sets, float* out);
+/* Environment importance map (image_textures.cpp:142-195,
+ * distributions.cpp:215-281): row pdf [map_h][map_w], row cdf
+ * [map_h][map_w + 1], top pdf [map_h], top cdf [map_h + 1], and per texel
+ * (adjacency bits, s, t, scale) of its upsampled spectrum. */
+int slrgpu_environment_tables(slrgpu_handle scene, uint32_t* map_w, uint32_t* map_h, float* row_pdf, float* row_cdf,
+                              float* top_pdf, float* top_cdf, float* texel_params);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SLRGPU_H */

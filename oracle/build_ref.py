@@ -1,0 +1,211 @@
+#!/usr/bin/env python3
+"""Build the reference renderer (SLR's ``libSLR``) as the CPU oracle.
+
+TEST INFRASTRUCTURE ONLY.  Nothing in the product (``slr_gb300``) imports,
+links or executes anything under ``oracle/``.  Only ``tests/``,
+``__graft_entry__.smoke()`` and the CPU-baseline leg of ``bench.py`` use it,
+and only as the checker / the timed CPU baseline.
+
+Recipe
+------
+1. When the reference sources are present (``$SLR_REFERENCE`` or the default
+   checkout path), the ``libSLR`` sources are copied into ``oracle/_ref/src``
+   and the build-only patches below are applied to that copy.  The reference
+   tree itself is never written.  ``oracle/_ref`` is git-ignored.
+2. Every translation unit is compiled with g++/gcc (no cmake, no external
+   libraries) into ``oracle/_ref/obj`` and linked, together with the oracle
+   driver ``oracle/ref_driver.cpp`` and the no-op progress reporter
+   ``oracle/progress_reporter_noop.cpp``, into ``oracle/_ref/libslr_ref.so``.
+
+On a machine without the reference checkout (the GPU host) step 1 is skipped
+and the patched copy that travelled with the working tree is compiled.
+
+Build-only patches (all applied to the copy):
+
+* P1 ``libSLR/defines.h:106``: the Linux branch of ``SLR_memalign`` expands to
+  an undeclared identifier; Linux is routed to the ``posix_memalign`` branch.
+* P2 ``-include cstring``: ``Core/distributions.cpp:103,123,199`` use
+  ``std::memcpy`` without including ``<cstring>``.
+* P3 ``BasicTypes/spectrum_types.cpp:922-936``: the explicit specialisations
+  of the static CMF members are declarations only; ``{}`` makes them
+  definitions so the library links.
+* P4 ``Core/surface_object.cpp:18`` and ``Core/medium_object.cpp:18`` include
+  the SSE-only ``Accelerator/QBVH.h`` that nothing on the active path uses;
+  the include is dropped so the library builds on aarch64 too.
+* P5 ``-ffp-contract=off``: x86-64 and aarch64 then round every operation the
+  same way (no fused multiply-add), so golden dumps agree across hosts.
+* P6 max depth: ``Renderer/PTRenderer.cpp:172`` caps a path at 100 vertices
+  and ``Renderer/VolumetricPTRenderer.cpp:185`` has no cap.  Both now stop
+  after ``slr_oracle_max_depth`` scattering vertices (a global the driver
+  sets), which is the ``maxDepth`` the GPU renderer implements.
+* P7 ``Core/ProgressReporter.cpp`` is replaced by a no-op implementation (the
+  stock one blocks up to 250 ms per progressive pass and can hang on a racy
+  counter, ``Core/ProgressReporter.cpp:74-81,101-104``), and the progressive
+  ``saveImage`` calls inside the render loops (``PTRenderer.cpp:84``,
+  ``VolumetricPTRenderer.cpp:84``) are disabled so rendering writes no BMPs.
+"""
+from __future__ import annotations
+
+import argparse
+import concurrent.futures as cf
+import os
+import platform
+import shutil
+import subprocess
+import sys
+from pathlib import Path
+
+HERE = Path(__file__).resolve().parent
+REF_OUT = HERE / "_ref"
+SRC_COPY = REF_OUT / "src" / "libSLR"
+OBJ_DIR = REF_OUT / "obj"
+LIB = REF_OUT / "libslr_ref.so"
+DEFAULT_REFERENCE = "/root/reference"
+
+# Files excluded from the reference's own build (libSLR/CMakeLists.txt:45-51).
+EXCLUDED = {
+    "MemoryAllocators/StackAllocator.cpp", "MemoryAllocators/StackAllocator.h",
+    "MemoryAllocators/MSpaceAllocator.cpp", "MemoryAllocators/MSpaceAllocator.h",
+    "MemoryAllocators/dlmalloc.c", "MemoryAllocators/dlmalloc.h",
+    "Renderer/AMCMCPPMRenderer.cpp", "Renderer/AMCMCPPMRenderer.h",
+}
+SOURCE_DIRS = ["", "External", "External/AnalyticSkyDomeRadiance", "MemoryAllocators",
+               "BasicTypes", "Core", "RNG", "SurfaceShape", "MediumDistribution", "BSDF",
+               "EDF", "PhaseFunction", "Texture", "SurfaceMaterial", "MediumMaterial",
+               "Accelerator", "Camera", "Scene", "Renderer", "Helper"]
+
+
+def _reference_root() -> Path | None:
+    root = Path(os.environ.get("SLR_REFERENCE", DEFAULT_REFERENCE))
+    return root if (root / "libSLR" / "defines.h").is_file() else None
+
+
+def _replace_once(text: str, old: str, new: str, what: str) -> str:
+    if text.count(old) < 1:
+        raise RuntimeError(f"patch site not found: {what}")
+    return text.replace(old, new)
+
+
+def copy_and_patch(ref_root: Path) -> None:
+    src = ref_root / "libSLR"
+    if SRC_COPY.exists():
+        shutil.rmtree(SRC_COPY)
+    for d in SOURCE_DIRS:
+        sdir = src / d
+        if not sdir.is_dir():
+            continue
+        for f in sorted(sdir.iterdir()):
+            if not f.is_file() or f.suffix not in (".h", ".hpp", ".cpp", ".c"):
+                continue
+            rel = f.relative_to(src).as_posix()
+            if rel in EXCLUDED:
+                continue
+            dst = SRC_COPY / rel
+            dst.parent.mkdir(parents=True, exist_ok=True)
+            shutil.copyfile(f, dst)
+
+    def patch(rel: str, fn) -> None:
+        p = SRC_COPY / rel
+        t = p.read_text(encoding="utf-8-sig")
+        p.write_text(fn(t), encoding="utf-8")
+
+    # P1
+    patch("defines.h", lambda t: _replace_once(
+        t, "#elif defined(SLR_Platform_OS_X) || defined(SLR_Platform_OpenBSD)\ninline void* SLR_memalign",
+        "#elif defined(SLR_Platform_OS_X) || defined(SLR_Platform_OpenBSD) || defined(SLR_Platform_Linux)\ninline void* SLR_memalign",
+        "P1 memalign"))
+    # P3
+    def p3(t: str) -> str:
+        for real in ("float", "double"):
+            for m in ("xbar", "ybar", "zbar"):
+                t = _replace_once(t, f"DiscretizedSpectrumTemplate<{real}, NumStrataForStorage>::{m};",
+                                  f"DiscretizedSpectrumTemplate<{real}, NumStrataForStorage>::{m}{{}};", "P3 " + m)
+            t = _replace_once(t, f"DiscretizedSpectrumTemplate<{real}, NumStrataForStorage>::integralCMF;",
+                              f"DiscretizedSpectrumTemplate<{real}, NumStrataForStorage>::integralCMF{{}};", "P3 integralCMF")
+        return t
+    patch("BasicTypes/spectrum_types.cpp", p3)
+    # P4
+    for rel in ("Core/surface_object.cpp", "Core/medium_object.cpp"):
+        patch(rel, lambda t: _replace_once(t, '#include "../Accelerator/QBVH.h"', "", "P4 QBVH include"))
+    # P6 + P7 (saveImage)
+    decl = "extern \"C\" unsigned int slr_oracle_max_depth;\n"
+    def p6_pt(t: str) -> str:
+        t = _replace_once(t, "if (pathLength >= 100)", "if (pathLength > slr_oracle_max_depth)", "P6 PT")
+        t = _replace_once(t, "sensor->saveImage(filename,", "if (0) sensor->saveImage(filename,", "P7 PT")
+        return t.replace("namespace SLR {", decl + "namespace SLR {", 1)
+    patch("Renderer/PTRenderer.cpp", p6_pt)
+    def p6_vpt(t: str) -> str:
+        t = _replace_once(t, "            ++pathLength;\n",
+                          "            ++pathLength;\n            if (pathLength > slr_oracle_max_depth)\n                break;\n",
+                          "P6 VolPT")
+        t = _replace_once(t, "sensor->saveImage(filename,", "if (0) sensor->saveImage(filename,", "P7 VolPT")
+        return t.replace("namespace SLR {", decl + "namespace SLR {", 1)
+    patch("Renderer/VolumetricPTRenderer.cpp", p6_vpt)
+    # P7: the stock reporter is replaced by oracle/progress_reporter_noop.cpp
+    (SRC_COPY / "Core" / "ProgressReporter.cpp").unlink()
+    (REF_OUT / "src" / "PATCHED").write_text("P1 P2 P3 P4 P5 P6 P7\n")
+
+
+def _compile(cmd: list[str]) -> tuple[list[str], int, str]:
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    return cmd, r.returncode, r.stderr
+
+
+def build(jobs: int | None = None, force: bool = False, verbose: bool = False) -> Path:
+    ref_root = _reference_root()
+    if ref_root is not None and (force or not (REF_OUT / "src" / "PATCHED").is_file()):
+        copy_and_patch(ref_root)
+    if not (REF_OUT / "src" / "PATCHED").is_file():
+        raise RuntimeError("reference sources unavailable: neither the reference checkout nor "
+                           "oracle/_ref/src is present")
+    OBJ_DIR.mkdir(parents=True, exist_ok=True)
+    common = ["-O2", "-fPIC", "-ffp-contract=off", "-w", "-pthread", f"-I{SRC_COPY}"]
+    cxx = ["g++", "-std=gnu++11", "-include", "cstring", "-include", "cmath"] + common
+    cc = ["gcc"] + common
+    units: list[tuple[Path, list[str]]] = []
+    for f in sorted(SRC_COPY.rglob("*")):
+        if f.suffix == ".cpp":
+            units.append((f, cxx))
+        elif f.suffix == ".c":
+            units.append((f, cc))
+    units.append((HERE / "progress_reporter_noop.cpp", cxx))
+    units.append((HERE / "ref_driver.cpp", ["g++", "-std=gnu++14", "-include", "cstring", "-include", "cmath"] + common))
+    objs, cmds = [], []
+    for f, tool in units:
+        rel = f.relative_to(SRC_COPY) if SRC_COPY in f.parents else Path("oracle") / f.name
+        o = OBJ_DIR / (rel.as_posix().replace("/", "__") + ".o")
+        objs.append(o)
+        if o.is_file() and o.stat().st_mtime >= f.stat().st_mtime and not force:
+            continue
+        cmds.append(tool + ["-c", str(f), "-o", str(o)])
+    jobs = jobs or os.cpu_count() or 4
+    failed = []
+    with cf.ThreadPoolExecutor(max_workers=jobs) as ex:
+        for cmd, rc, err in ex.map(_compile, cmds):
+            if rc != 0:
+                failed.append((cmd, err))
+            elif verbose:
+                print(" ".join(cmd[-3:]))
+    if failed:
+        cmd, err = failed[0]
+        raise RuntimeError(f"oracle compile failed ({len(failed)} units): {' '.join(cmd)}\n{err[-4000:]}")
+    link = ["g++", "-shared", "-pthread", "-o", str(LIB)] + [str(o) for o in objs]
+    r = subprocess.run(link, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"oracle link failed:\n{r.stderr[-4000:]}")
+    return LIB
+
+
+def main() -> int:
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--force", action="store_true")
+    ap.add_argument("-j", type=int, default=None)
+    ap.add_argument("-v", action="store_true")
+    a = ap.parse_args()
+    lib = build(jobs=a.j, force=a.force, verbose=a.v)
+    print(f"built {lib} ({platform.machine()})")
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

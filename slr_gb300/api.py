@@ -1,0 +1,401 @@
+"""Python mirror of the reference renderer's interface over the C ABI.
+
+The classes follow SLR's names and argument meaning so that code written
+against the reference reads the same:
+
+* :class:`RenderSettings` - the typed settings map of libSLR/Core/RenderSettings.h:15-43
+  (NumThreads, ImageWidth, ImageHeight, TimeStart, TimeEnd, Brightness, RNGSeed).
+* :class:`Scene` - a committed scene (libSLR/Scene/Scene.h:17-52) built from a
+  :class:`~slr_gb300.scene_desc.SceneDesc`.
+* :class:`PathTracingRenderer` / :class:`VolumetricPathTracingRenderer` -
+  ``render(scene, settings)`` like SLR::Renderer::render
+  (libSLR/Core/renderer.h:15-19), returning the 16-bin film that
+  ImageSensor::pixel(x, y) exposes (per pixel the sum over all samples).
+
+Everything runs in the CUDA library ``slr_gb300/lib/libslrgpu.so``; there is
+no CPU fallback: the classes raise when the library or a GPU is missing.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import enum
+import re
+from pathlib import Path
+
+import numpy as np
+
+from .scene_desc import SceneDesc
+
+PKG = Path(__file__).resolve().parent
+LIB_PATH = PKG / "lib" / "libslrgpu.so"
+HEADER = PKG.parent / "include" / "slrgpu.h"
+
+_lib = None
+
+
+class SlrGpuError(RuntimeError):
+    pass
+
+
+class BvhStats(C.Structure):
+    _fields_ = [("num_triangles", C.c_uint32), ("num_fragments", C.c_uint32), ("depth", C.c_uint32),
+                ("num_binary_nodes", C.c_uint32), ("num_wide_nodes", C.c_uint32), ("width", C.c_uint32),
+                ("sah_cost", C.c_float), ("build_seconds", C.c_float)]
+
+
+class Settings(C.Structure):
+    _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("spp", C.c_uint32), ("max_depth", C.c_uint32),
+                ("seed", C.c_uint32), ("volumetric", C.c_uint32), ("samples_per_wave", C.c_uint32),
+                ("flags", C.c_uint32)]
+
+
+KERNEL_CLASSES = ["raygen", "extend", "shade", "shadow", "accumulate"]
+FLAG_PROFILE_KERNELS = 1
+
+
+class RenderStats(C.Structure):
+    _fields_ = [("seconds", C.c_double), ("kernel_seconds", C.c_double), ("path_samples", C.c_uint64),
+                ("extension_rays", C.c_uint64), ("shadow_rays", C.c_uint64), ("dropped_samples", C.c_uint64),
+                ("kernel_launches", C.c_uint64), ("kernel_ms", C.c_double * 8), ("kernel_count", C.c_uint64 * 8)]
+
+    def as_dict(self):
+        d = {k: getattr(self, k) for k, _ in self._fields_ if k not in ("kernel_ms", "kernel_count")}
+        d["kernel_ms"] = {n: self.kernel_ms[i] for i, n in enumerate(KERNEL_CLASSES)}
+        d["kernel_count"] = {n: self.kernel_count[i] for i, n in enumerate(KERNEL_CLASSES)}
+        return d
+
+
+def header_symbols() -> list[str]:
+    """Every function the C ABI header declares."""
+    text = HEADER.read_text()
+    return sorted(set(re.findall(r"^\s*(?:int|const char\*|void)\s+(slrgpu_\w+)\s*\(", text, re.M)))
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.is_file():
+            raise SlrGpuError(f"CUDA extension not built: {LIB_PATH} (run __graft_entry__.build())")
+        L = C.CDLL(str(LIB_PATH))
+        H, I, U, F, P = C.c_uint64, C.c_int, C.c_uint32, C.c_float, C.c_void_p
+        fp, up, ip, hp = C.POINTER(C.c_float), C.POINTER(C.c_uint32), C.POINTER(C.c_int), C.POINTER(C.c_uint64)
+        u16p = C.POINTER(C.c_uint16)
+        sig = {
+            "slrgpu_last_error": (C.c_char_p, []),
+            "slrgpu_version": (I, []),
+            "slrgpu_context_create": (I, [I, hp]),
+            "slrgpu_context_destroy": (I, [H]),
+            "slrgpu_scene_create": (I, [H, hp]),
+            "slrgpu_scene_destroy": (I, [H]),
+            "slrgpu_spectrum_rgb": (I, [H, I, F, F, F, ip]),
+            "slrgpu_spectrum_regular": (I, [H, F, F, fp, U, ip]),
+            "slrgpu_spectrum_irregular": (I, [H, fp, fp, U, ip]),
+            "slrgpu_material_matte": (I, [H, I, ip]),
+            "slrgpu_material_specular_reflection": (I, [H, I, I, I, ip]),
+            "slrgpu_material_specular_scattering": (I, [H, I, I, I, ip]),
+            "slrgpu_material_microfacet_reflection": (I, [H, I, I, F, F, ip]),
+            "slrgpu_material_microfacet_scattering": (I, [H, I, I, F, F, ip]),
+            "slrgpu_material_emitter": (I, [H, I, I, ip]),
+            "slrgpu_scene_add_mesh": (I, [H, fp, fp, fp, fp, U, up, U, I]),
+            "slrgpu_environment_ibl": (I, [H, u16p, U, U, F]),
+            "slrgpu_medium_density_grid": (I, [H, fp, fp, I, I, fp, U, U, U, F]),
+            "slrgpu_camera_perspective": (I, [H, fp, F, F, F, F, F, F]),
+            "slrgpu_camera_equirect": (I, [H, fp, F, F, F]),
+            "slrgpu_scene_commit": (I, [H, C.POINTER(BvhStats)]),
+            "slrgpu_scene_build_host": (I, [H, C.POINTER(BvhStats)]),
+            "slrgpu_render": (I, [H, C.POINTER(Settings), P, I, C.POINTER(RenderStats)]),
+            "slrgpu_trace": (I, [H, P, U, I, P, P, P, P, P]),
+            "slrgpu_scene_sbvh_dump": (I, [H, fp, up, up]),
+            "slrgpu_spectrum_evaluate": (I, [H, I, fp, U, fp]),
+            "slrgpu_environment_tables": (I, [H, up, up, fp, fp, fp, fp, fp]),
+            "slrgpu_bsdf_query": (I, [I, fp, fp, fp, F, F, fp, U, fp]),
+            "slrgpu_scene_reupload": (I, [H, C.POINTER(C.c_uint64)]),
+        }
+        for name, (res, args) in sig.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def check(rc: int) -> None:
+    if rc != 0:
+        raise SlrGpuError(f"slrgpu error {rc}: {lib().slrgpu_last_error().decode()}")
+
+
+def _fp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+def _up(a):
+    return a.ctypes.data_as(C.POINTER(C.c_uint32))
+
+
+class RenderSettingItem(enum.Enum):
+    NumThreads = 0
+    ImageWidth = 1
+    ImageHeight = 2
+    TimeStart = 3
+    TimeEnd = 4
+    Brightness = 5
+    RNGSeed = 6
+
+
+class RenderSettings:
+    """Typed key/value settings (libSLR/Core/RenderSettings.h:24-43)."""
+
+    def __init__(self, **items):
+        self._items = {}
+        for k, v in items.items():
+            self.addItem(RenderSettingItem[k], v)
+
+    def addItem(self, item: RenderSettingItem, value) -> None:
+        self._items[item] = value
+
+    def get(self, item: RenderSettingItem, default=None):
+        return self._items.get(item, default)
+
+
+class Context:
+    """One GPU (device index); owns path-state and film buffers."""
+
+    def __init__(self, device: int = 0):
+        h = C.c_uint64()
+        check(lib().slrgpu_context_create(device, C.byref(h)))
+        self.handle = h.value
+
+    def close(self):
+        if getattr(self, "handle", 0):
+            lib().slrgpu_context_destroy(self.handle)
+            self.handle = 0
+
+
+_default_ctx = None
+
+
+def default_context() -> Context:
+    global _default_ctx
+    if _default_ctx is None:
+        _default_ctx = Context(0)
+    return _default_ctx
+
+
+class Scene:
+    """A scene on the device built from a SceneDesc (tee of the reference's
+    node-API construction: same spectra, materials, meshes, environment,
+    camera)."""
+
+    def __init__(self, desc: SceneDesc, context: Context | None = None, commit: bool = True,
+                 host_only: bool = False):
+        L = lib()
+        self.desc = desc
+        self.context = None if host_only else (context or default_context())
+        h = C.c_uint64()
+        check(L.slrgpu_scene_create(0 if host_only else self.context.handle, C.byref(h)))
+        self.handle = h.value
+        self._keep = []
+        sid = []
+        out = C.c_int()
+        for sp in desc.spectra:
+            if sp.kind == "rgb":
+                check(L.slrgpu_spectrum_rgb(self.handle, sp.sp_type, *sp.rgb, C.byref(out)))
+            elif sp.kind == "regular":
+                v = np.ascontiguousarray(sp.values, np.float32)
+                check(L.slrgpu_spectrum_regular(self.handle, sp.min_wl, sp.max_wl, _fp(v), len(v), C.byref(out)))
+            else:
+                w = np.ascontiguousarray(sp.wavelengths, np.float32)
+                v = np.ascontiguousarray(sp.values, np.float32)
+                check(L.slrgpu_spectrum_irregular(self.handle, _fp(w), _fp(v), len(v), C.byref(out)))
+            sid.append(out.value)
+        mid = []
+        for m in desc.materials:
+            s = [sid[i] for i in m.spectra]
+            if m.kind == "matte":
+                check(L.slrgpu_material_matte(self.handle, s[0], C.byref(out)))
+            elif m.kind == "specular_reflection":
+                check(L.slrgpu_material_specular_reflection(self.handle, *s, C.byref(out)))
+            elif m.kind == "specular_scattering":
+                check(L.slrgpu_material_specular_scattering(self.handle, *s, C.byref(out)))
+            elif m.kind == "microfacet_reflection":
+                check(L.slrgpu_material_microfacet_reflection(self.handle, s[0], s[1], m.alpha_x, m.alpha_y,
+                                                              C.byref(out)))
+            elif m.kind == "microfacet_scattering":
+                check(L.slrgpu_material_microfacet_scattering(self.handle, s[0], s[1], m.alpha_x, m.alpha_y,
+                                                              C.byref(out)))
+            elif m.kind == "emitter":
+                check(L.slrgpu_material_emitter(self.handle, mid[m.base], s[0], C.byref(out)))
+            else:
+                raise ValueError(m.kind)
+            mid.append(out.value)
+        for mesh in desc.meshes:
+            p = np.ascontiguousarray(mesh.positions, np.float32)
+            n = np.ascontiguousarray(mesh.normals, np.float32)
+            t = np.ascontiguousarray(mesh.tangents, np.float32)
+            uv = np.ascontiguousarray(mesh.uvs, np.float32)
+            idx = np.ascontiguousarray(mesh.indices, np.uint32)
+            check(L.slrgpu_scene_add_mesh(self.handle, _fp(p), _fp(n), _fp(t), _fp(uv), len(p), _up(idx), len(idx),
+                                          mid[mesh.material]))
+        if desc.environment is not None:
+            img = np.ascontiguousarray(desc.environment.rgba_half, np.float16).view(np.uint16)
+            check(L.slrgpu_environment_ibl(self.handle, img.ctypes.data_as(C.POINTER(C.c_uint16)), img.shape[1],
+                                           img.shape[0], desc.environment.scale))
+        if desc.medium is not None:
+            md = desc.medium
+            bmin = np.asarray(md.bounds_min, np.float32)
+            bmax = np.asarray(md.bounds_max, np.float32)
+            dens = np.ascontiguousarray(md.density, np.float32)
+            nz, ny, nx = dens.shape
+            check(L.slrgpu_medium_density_grid(self.handle, _fp(bmin), _fp(bmax), sid[md.sigma_s], sid[md.sigma_e],
+                                               _fp(dens), nx, ny, nz, md.hg_g))
+        cam = desc.camera
+        if cam is not None:
+            m = np.ascontiguousarray(cam.cam_to_world, np.float32)
+            if cam.kind == "perspective":
+                check(L.slrgpu_camera_perspective(self.handle, _fp(m), cam.sensitivity, cam.aspect, cam.fov_y,
+                                                  cam.lens_radius, cam.img_plane_dist, cam.obj_plane_dist))
+            else:
+                check(L.slrgpu_camera_equirect(self.handle, _fp(m), cam.sensitivity, cam.phi_angle, cam.theta_angle))
+        self.spectrum_ids = sid
+        self.material_ids = mid
+        self.bvh_stats = None
+        if host_only:
+            st = BvhStats()
+            check(L.slrgpu_scene_build_host(self.handle, C.byref(st)))
+            self.bvh_stats = st
+        elif commit:
+            self.commit()
+
+    def commit(self) -> BvhStats:
+        st = BvhStats()
+        check(lib().slrgpu_scene_commit(self.handle, C.byref(st)))
+        self.bvh_stats = st
+        return st
+
+    def close(self):
+        if getattr(self, "handle", 0):
+            lib().slrgpu_scene_destroy(self.handle)
+            self.handle = 0
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- rendering / queries ------------------------------------------------
+    def reupload(self) -> int:
+        """Copies the scene's device arrays again from their pinned host
+        mirrors; returns the bytes copied."""
+        b = C.c_uint64()
+        check(lib().slrgpu_scene_reupload(self.handle, C.byref(b)))
+        return b.value
+
+    def render(self, width: int, height: int, spp: int, max_depth: int, seed: int = 0, volumetric: bool = False,
+               samples_per_wave: int = 0, film=None, flags: int = 0):
+        """Returns (film (h, w, 16) float32 sum over samples, RenderStats).
+        ``film`` may be a preallocated host numpy array or a CUDA tensor."""
+        s = Settings(width, height, spp, max_depth, seed, int(volumetric), samples_per_wave, flags)
+        st = RenderStats()
+        on_device = 0
+        if film is None:
+            film = np.zeros((height, width, 16), np.float32)
+            ptr = film.ctypes.data
+        elif isinstance(film, np.ndarray):
+            ptr = film.ctypes.data
+        else:  # torch CUDA tensor
+            on_device = 1
+            ptr = film.data_ptr()
+        check(lib().slrgpu_render(self.handle, C.byref(s), C.c_void_p(ptr), on_device, C.byref(st)))
+        return film, st
+
+    def trace(self, rays_dev, any_hit: bool = False):
+        """rays_dev: torch CUDA float32 tensor (n, 8).  Returns torch tensors
+        (prim, t, b1, b2) on the same device (any hit: prim only)."""
+        import torch
+        n = rays_dev.shape[0]
+        prim = torch.empty(n, dtype=torch.int32, device=rays_dev.device)
+        if any_hit:
+            t = b1 = b2 = None
+            ptrs = [None, None, None]
+        else:
+            t = torch.empty(n, dtype=torch.float32, device=rays_dev.device)
+            b1 = torch.empty_like(t)
+            b2 = torch.empty_like(t)
+            ptrs = [t.data_ptr(), b1.data_ptr(), b2.data_ptr()]
+        stream = torch.cuda.current_stream(rays_dev.device).cuda_stream
+        check(lib().slrgpu_trace(self.handle, C.c_void_p(rays_dev.data_ptr()), n, int(any_hit),
+                                 C.c_void_p(prim.data_ptr()), *(C.c_void_p(p) if p else None for p in ptrs),
+                                 C.c_void_p(stream)))
+        return prim, t, b1, b2
+
+    # -- host diagnostics -------------------------------------------------
+    def sbvh_dump(self):
+        st = self.bvh_stats
+        boxes = np.zeros((st.num_binary_nodes, 6), np.float32)
+        words = np.zeros((st.num_binary_nodes, 5), np.uint32)
+        leaves = np.zeros(st.num_fragments, np.uint32)
+        check(lib().slrgpu_scene_sbvh_dump(self.handle, _fp(boxes), _up(words), _up(leaves)))
+        return boxes, words, leaves
+
+    def spectrum_evaluate(self, spectrum_index: int, lambdas: np.ndarray) -> np.ndarray:
+        lam = np.ascontiguousarray(lambdas, np.float32).reshape(-1, 16)
+        out = np.zeros_like(lam)
+        check(lib().slrgpu_spectrum_evaluate(self.handle, self.spectrum_ids[spectrum_index], _fp(lam), len(lam),
+                                             _fp(out)))
+        return out
+
+    def environment_tables(self):
+        env = self.desc.environment
+        h, w = env.rgba_half.shape[:2]
+        mw, mh = w // 4, h // 4
+        row_pdf = np.zeros((mh, mw), np.float32)
+        row_cdf = np.zeros((mh, mw + 1), np.float32)
+        top_pdf = np.zeros(mh, np.float32)
+        top_cdf = np.zeros(mh + 1, np.float32)
+        texels = np.zeros((h, w, 4), np.float32)
+        a, b = C.c_uint32(), C.c_uint32()
+        check(lib().slrgpu_environment_tables(self.handle, C.byref(a), C.byref(b), _fp(row_pdf), _fp(row_cdf),
+                                              _fp(top_pdf), _fp(top_cdf), _fp(texels)))
+        return {"row_pdf": row_pdf, "row_cdf": row_cdf, "top_pdf": top_pdf, "top_cdf": top_cdf, "texels": texels}
+
+
+BSDF_KINDS = {"lambert": 0, "specular_brdf": 1, "specular_bsdf": 2, "ggx_brdf": 3, "ggx_bsdf": 4}
+
+
+def bsdf_query(kind: str, spec0, spec1=None, spec2=None, ax=0.0, ay=0.0, queries=None) -> np.ndarray:
+    """Evaluates a BSDF on the GPU at fixed (query, sample) tuples; the
+    16-float query and 40-float result layouts of slrgpu_bsdf_query."""
+    s0 = np.ascontiguousarray(spec0, np.float32)
+    s1 = np.ascontiguousarray(spec1 if spec1 is not None else spec0, np.float32)
+    s2 = np.ascontiguousarray(spec2 if spec2 is not None else spec0, np.float32)
+    q = np.ascontiguousarray(queries, np.float32).reshape(-1, 16)
+    out = np.zeros((len(q), 40), np.float32)
+    check(lib().slrgpu_bsdf_query(BSDF_KINDS[kind], _fp(s0), _fp(s1), _fp(s2), ax, ay, _fp(q), len(q), _fp(out)))
+    return out
+
+
+class PathTracingRenderer:
+    """Drop-in for SLR::PTRenderer(spp) (libSLR/Renderer/PTRenderer.h:42-43)
+    with the max-depth parameter the GPU path adds."""
+
+    volumetric = False
+
+    def __init__(self, spp: int, max_depth: int = 100):
+        self.spp = int(spp)
+        self.max_depth = int(max_depth)
+
+    def render(self, scene: Scene, settings: RenderSettings):
+        w = int(settings.get(RenderSettingItem.ImageWidth))
+        h = int(settings.get(RenderSettingItem.ImageHeight))
+        seed = int(settings.get(RenderSettingItem.RNGSeed, 0)) & 0xffffffff
+        film, stats = scene.render(w, h, self.spp, self.max_depth, seed=seed, volumetric=self.volumetric)
+        self.last_stats = stats
+        return film
+
+
+class VolumetricPathTracingRenderer(PathTracingRenderer):
+    """Drop-in for SLR::VolumetricPTRenderer(spp)
+    (libSLR/Renderer/VolumetricPTRenderer.h:43-44)."""
+
+    volumetric = True

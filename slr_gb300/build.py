@@ -1,0 +1,86 @@
+"""Builds the CUDA extension ``slr_gb300/lib/libslrgpu.so`` for sm_103a.
+
+Host C++ is compiled with g++ (-ffp-contract=off: the SBVH build, spectral
+upsampling and environment tables must round exactly like the reference), the
+kernels with nvcc for ``arch=compute_103a,code=sm_103a``; the translation
+units compile in parallel and are linked by nvcc into one shared library
+with a C ABI (include/slrgpu.h).
+"""
+from __future__ import annotations
+
+import concurrent.futures as cf
+import os
+import shutil
+import subprocess
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+CSRC = PKG / "csrc"
+BUILD = PKG / "_build"
+LIB_DIR = PKG / "lib"
+LIB = LIB_DIR / "libslrgpu.so"
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+HOST_SOURCES = ["scene_host.cpp", "capi.cpp"]
+CUDA_SOURCES = ["render.cu"]
+
+
+def _cuda_home() -> Path:
+    for c in (os.environ.get("CUDA_HOME"), "/usr/local/cuda"):
+        if c and (Path(c) / "bin" / "nvcc").exists():
+            return Path(c)
+    nvcc = shutil.which("nvcc")
+    if nvcc:
+        return Path(nvcc).resolve().parent.parent
+    raise RuntimeError("nvcc not found")
+
+
+def _run(cmd):
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    return cmd, r.returncode, r.stdout + r.stderr
+
+
+def build(verbose: bool = False, force: bool = False, extra_nvcc: list[str] | None = None) -> Path:
+    cuda = _cuda_home()
+    nvcc = str(cuda / "bin" / "nvcc")
+    BUILD.mkdir(exist_ok=True)
+    LIB_DIR.mkdir(exist_ok=True)
+    inc = [f"-I{cuda / 'include'}", f"-I{CSRC}"]
+    deps = sorted(CSRC.glob("*.h")) + sorted(CSRC.glob("*.cuh")) + sorted(CSRC.glob("*.inc")) + \
+        [PKG.parent / "include" / "slrgpu.h"]
+    newest_dep = max(p.stat().st_mtime for p in deps)
+    jobs = []
+    objs = []
+    for src in HOST_SOURCES:
+        o = BUILD / (src + ".o")
+        objs.append(o)
+        s = CSRC / src
+        if force or not o.exists() or o.stat().st_mtime < max(s.stat().st_mtime, newest_dep):
+            jobs.append(["g++", "-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-unused-function",
+                         *inc, "-c", str(s), "-o", str(o)])
+    for src in CUDA_SOURCES:
+        o = BUILD / (src + ".o")
+        objs.append(o)
+        s = CSRC / src
+        if force or not o.exists() or o.stat().st_mtime < max(s.stat().st_mtime, newest_dep):
+            jobs.append([nvcc, "-std=c++17", "-O3", "-lineinfo", *ARCH, "-Xcompiler", "-fPIC",
+                         "-Xcompiler", "-ffp-contract=off", "-Xptxas", "-v", *(extra_nvcc or []),
+                         *inc, "-c", str(s), "-o", str(o)])
+    with cf.ThreadPoolExecutor(max_workers=max(1, len(jobs))) as ex:
+        for cmd, rc, out in ex.map(_run, jobs):
+            if rc != 0:
+                raise RuntimeError(f"compile failed: {' '.join(cmd)}\n{out[-6000:]}")
+            if verbose:
+                print(out)
+    if jobs or not LIB.exists():
+        cmd = [nvcc, "-shared", *ARCH, "-o", str(LIB), *[str(o) for o in objs], "-lcudart_static", "-lrt",
+               "-lpthread", "-ldl"]
+        _, rc, out = _run(cmd)
+        if rc != 0:
+            raise RuntimeError(f"link failed: {' '.join(cmd)}\n{out[-6000:]}")
+    return LIB
+
+
+if __name__ == "__main__":
+    import sys
+    print(build(verbose="-v" in sys.argv, force="--force" in sys.argv))

@@ -1,0 +1,425 @@
+// BSDFs on the device: Lambert, specular reflection / scattering, GGX
+// microfacet reflection / scattering with visible-normal sampling, and the
+// shading-normal correction of the reference's BSDF wrapper
+// (libSLR/Core/directional_distribution_functions.h:295-349).  Non-adjoint
+// queries with the "All" direction filter, which is what the path tracers use.
+#pragma once
+#include "device_common.cuh"
+
+namespace slrgpu {
+
+// DirectionType bits (directional_distribution_functions.h:18-50).
+constexpr uint32_t kDirLowFreq = 1u << 0;
+constexpr uint32_t kDirHighFreq = 1u << 1;
+constexpr uint32_t kDirDelta0D = 1u << 2;
+constexpr uint32_t kDirDelta1D = 1u << 3;
+constexpr uint32_t kDirReflection = 1u << 4;
+constexpr uint32_t kDirTransmission = 1u << 5;
+constexpr uint32_t kDirDispersive = 1u << 6;
+constexpr uint32_t kDirNonDelta = kDirLowFreq | kDirHighFreq;
+constexpr uint32_t kDirDelta = kDirDelta0D | kDirDelta1D;
+
+__device__ __forceinline__ bool dirIsDelta(uint32_t t) { return (t & kDirDelta) && !(t & kDirNonDelta); }
+
+struct Bsdf {
+    uint32_t kind;
+    Spec a, b, c;          // see MaterialKind
+    float ax, ay;
+    bool dispersive;       // SpecularBSDF built while no wavelength is selected
+};
+
+struct BsdfQuery {
+    V3 dir;                // outgoing direction in the shading frame
+    V3 gn;                 // geometric normal in the shading frame
+    int wl;                // selected wavelength index
+};
+
+struct BsdfSample {
+    V3 dir;
+    float pdf;
+    uint32_t type;
+};
+
+__device__ __forceinline__ bool bsdfHasNonDelta(uint32_t kind) {
+    return kind == kMatMatte || kind == kMatGGXReflection || kind == kMatGGXScattering;
+}
+
+// ---- sampling helpers (distributions.cpp:59-91, distributions.h:30-73) ----
+__device__ __forceinline__ void concentricSampleDisk(float u0, float u1, float* dx, float* dy) {
+    float r, theta;
+    float sx = 2 * u0 - 1;
+    float sy = 2 * u1 - 1;
+    if (sx == 0 && sy == 0) { *dx = 0; *dy = 0; return; }
+    if (sx >= -sy) {
+        if (sx > sy) { r = sx; theta = sy / sx; }
+        else { r = sy; theta = 2 - sx / sy; }
+    } else {
+        if (sx > sy) { r = -sy; theta = 6 + sx / sy; }
+        else { r = -sx; theta = 4 + sy / sx; }
+    }
+    theta *= 0.785398163397448309616f;
+    float s, c;
+    sincosf(theta, &s, &c);
+    *dx = r * c;
+    *dy = r * s;
+}
+
+__device__ __forceinline__ V3 cosineSampleHemisphere(float u0, float u1) {
+    float x, y;
+    concentricSampleDisk(u0, u1, &x, &y);
+    return V3{x, y, sqrtf(fmaxf(0.0f, 1.0f - x * x - y * y))};
+}
+
+// ---- Fresnel (directional_distribution_functions.cpp:118-211) ----
+__device__ __forceinline__ float fresnelConductor1(float eta, float k, float cosEnter) {
+    cosEnter = fabsf(cosEnter);
+    float c2 = cosEnter * cosEnter;
+    float twoEtaCos = 2.0f * eta * cosEnter;
+    float tmpF = eta * eta + k * k;
+    float tmp = tmpF * c2;
+    float rparl2 = (tmp - twoEtaCos + 1) / (tmp + twoEtaCos + 1);
+    float rperp2 = (tmpF - twoEtaCos + c2) / (tmpF + twoEtaCos + c2);
+    return (rparl2 + rperp2) * 0.5f;
+}
+
+__device__ __forceinline__ float fresnelEvalF(float etaEnter, float etaExit, float cosEnter, float cosExit) {
+    float rparl = ((etaExit * cosEnter) - (etaEnter * cosExit)) / ((etaExit * cosEnter) + (etaEnter * cosExit));
+    float rperp = ((etaEnter * cosEnter) - (etaExit * cosExit)) / ((etaEnter * cosEnter) + (etaExit * cosExit));
+    return (rparl * rparl + rperp * rperp) * 0.5f;
+}
+
+__device__ __forceinline__ float fresnelDielectric1(float etaExt, float etaInt, float cosEnter) {
+    cosEnter = fminf(fmaxf(cosEnter, -1.0f), 1.0f);
+    bool entering = cosEnter > 0.0f;
+    float eEnter = entering ? etaExt : etaInt;
+    float eExit = entering ? etaInt : etaExt;
+    float sinExit = eEnter / eExit * sqrtf(fmaxf(0.0f, 1.0f - cosEnter * cosEnter));
+    cosEnter = fabsf(cosEnter);
+    if (sinExit >= 1.0f) return 1.0f;
+    float cosExit = sqrtf(fmaxf(0.0f, 1.0f - sinExit * sinExit));
+    return fresnelEvalF(eEnter, eExit, cosEnter, cosExit);
+}
+
+__device__ __forceinline__ void fresnelConductor(const Spec &eta, const Spec &k, float cosEnter, Spec &out) {
+#pragma unroll
+    for (int i = 0; i < kNumLambda; ++i) out.v[i] = fresnelConductor1(eta.v[i], k.v[i], cosEnter);
+}
+
+__device__ __forceinline__ void fresnelDielectric(const Spec &etaExt, const Spec &etaInt, float cosEnter, Spec &out) {
+#pragma unroll
+    for (int i = 0; i < kNumLambda; ++i) out.v[i] = fresnelDielectric1(etaExt.v[i], etaInt.v[i], cosEnter);
+}
+
+// ---- GGX (directional_distribution_functions.cpp:247-315) ----
+__device__ __forceinline__ float ggxD(float ax, float ay, V3 m) {
+    if (m.z <= 0) return 0.0f;
+    float temp = m.x * m.x / (ax * ax) + m.y * m.y / (ay * ay) + m.z * m.z;
+    return 1.0f / (kPiF * ax * ay * temp * temp);
+}
+
+__device__ __forceinline__ float ggxG1(float ax, float ay, V3 v, V3 m) {
+    float chi = (dot(v, m) / v.z) > 0 ? 1.0f : 0.0f;
+    float tan2 = (v.x * v.x * ax * ax + v.y * v.y * ay * ay) / (v.z * v.z);
+    return chi * 2 / (1 + sqrtf(1 + tan2));
+}
+
+__device__ __forceinline__ float ggxPdf(float ax, float ay, V3 v, V3 m) {
+    return ggxG1(ax, ay, v, m) * absDot(v, m) * ggxD(ax, ay, m) / fabsf(v.z);
+}
+
+// Visible-normal sampling (Heitz 2017, "A Simpler and Exact Sampling Routine
+// for the GGX Distribution of Visible Normals").
+__device__ __forceinline__ float ggxSample(float ax, float ay, V3 v, float u0, float u1, V3* m, float* pdf) {
+    V3 sv = normalize(V3{ax * v.x, ay * v.y, v.z});
+    float dist2D = sqrtf(sv.x * sv.x + sv.y * sv.y);
+    float rec = 1.0f / dist2D;
+    V3 T1 = (sv.z < 0.9999f) ? V3{sv.y * rec, -sv.x * rec, 0} : V3{1, 0, 0};
+    V3 T2 = V3{T1.y * sv.z, -T1.x * sv.z, dist2D};
+    float a = 1.0f / (1.0f + sv.z);
+    float r = sqrtf(u0);
+    float phi = kPiF * ((u1 < a) ? u1 / a : 1 + (u1 - a) / (1.0f - a));
+    float sp, cp;
+    sincosf(phi, &sp, &cp);
+    float P1 = r * cp;
+    float P2 = r * sp * ((u1 < a) ? 1.0f : sv.z);
+    V3 mm = P1 * T1 + P2 * T2 + sqrtf(1.0f - P1 * P1 - P2 * P2) * sv;
+    mm = normalize(V3{ax * mm.x, ay * mm.y, mm.z});
+    *m = mm;
+    float D = ggxD(ax, ay, mm);
+    *pdf = ggxG1(ax, ay, v, mm) * absDot(v, mm) * D / fabsf(v.z);
+    return D;
+}
+
+// ---- per-BSDF internals ----
+__device__ __forceinline__ void specScale(const Spec &a, float s, Spec &out) {
+#pragma unroll
+    for (int i = 0; i < kNumLambda; ++i) out.v[i] = a.v[i] * s;
+}
+
+// Returns fs (without the shading-normal correction); res->pdf == 0 on failure.
+__device__ __noinline__ void bsdfSampleInternal(const Bsdf &B, const BsdfQuery &q, float uc, float u0, float u1,
+                                               BsdfSample* res, Spec &fs) {
+    res->pdf = 0.0f;
+    res->type = 0;
+    res->dir = V3{0, 0, 1};
+    fs = specConst(0.0f);
+    switch (B.kind) {
+    case kMatMatte: {  // basic_bsdfs.cpp:13-27
+        V3 d = cosineSampleHemisphere(u0, u1);
+        res->pdf = d.z * kInvPiF;
+        res->type = kDirReflection | kDirLowFreq;
+        d.z *= q.dir.z > 0 ? 1.0f : -1.0f;
+        res->dir = d;
+        specScale(B.a, 1.0f / kPiF, fs);
+        return;
+    }
+    case kMatSpecularReflection: {  // basic_bsdfs.cpp:62-72
+        res->dir = V3{-q.dir.x, -q.dir.y, q.dir.z};
+        res->pdf = 1.0f;
+        res->type = kDirReflection | kDirDelta0D;
+        Spec F;
+        fresnelConductor(B.b, B.c, q.dir.z, F);
+        float r = 1.0f / fabsf(q.dir.z);
+#pragma unroll
+        for (int i = 0; i < kNumLambda; ++i) fs.v[i] = (B.a.v[i] * F.v[i]) * r;
+        return;
+    }
+    case kMatSpecularScattering: {  // basic_bsdfs.cpp:99-150
+        Spec F;
+        fresnelDielectric(B.b, B.c, q.dir.z, F);
+        float reflectProb = importance(F, q.wl);
+        if (uc < reflectProb) {
+            if (q.dir.z == 0.0f) return;
+            res->dir = V3{-q.dir.x, -q.dir.y, q.dir.z};
+            res->pdf = reflectProb;
+            res->type = kDirReflection | kDirDelta0D;
+            float r = 1.0f / fabsf(q.dir.z);
+#pragma unroll
+            for (int i = 0; i < kNumLambda; ++i) fs.v[i] = (B.a.v[i] * F.v[i]) * r;
+            return;
+        }
+        bool entering = q.dir.z > 0.0f;
+        float eExtW = specAt(B.b, q.wl), eIntW = specAt(B.c, q.wl);
+        float eEnter = entering ? eExtW : eIntW;
+        float eExit = entering ? eIntW : eExtW;
+        float sinEnter2 = 1.0f - q.dir.z * q.dir.z;
+        float rrEta = eEnter / eExit;
+        float sinExit2 = rrEta * rrEta * sinEnter2;
+        if (sinExit2 >= 1.0f) return;
+        float cosExit = sqrtf(fmaxf(0.0f, 1.0f - sinExit2));
+        if (entering) cosExit = -cosExit;
+        res->dir = V3{rrEta * -q.dir.x, rrEta * -q.dir.y, cosExit};
+        res->pdf = 1.0f - reflectProb;
+        res->type = kDirTransmission | kDirDelta0D | (B.dispersive ? kDirDispersive : 0u);
+        float val = specAt(B.a, q.wl) * (1.0f - specAt(F, q.wl));
+        val *= (eEnter * eEnter) / (eExit * eExit);
+        float r = 1.0f / fabsf(cosExit);
+#pragma unroll
+        for (int i = 0; i < kNumLambda; ++i) fs.v[i] = (i == q.wl) ? val * r : 0.0f;
+        return;
+    }
+    case kMatGGXReflection: {  // microfacet_bsdfs.cpp:11-40
+        bool entering = q.dir.z >= 0.0f;
+        float sign = entering ? 1.0f : -1.0f;
+        V3 m;
+        float mPdf;
+        float D = ggxSample(B.ax, B.ay, sign * q.dir, u0, u1, &m, &mPdf);
+        float dotHV = dot(q.dir, m);
+        if (dotHV * sign <= 0) return;
+        V3 d = (2 * dotHV) * m - q.dir;
+        if (d.z * q.dir.z <= 0) return;
+        float common = 1.0f / (4 * dotHV * sign);
+        res->dir = d;
+        res->pdf = common * mPdf;
+        res->type = kDirReflection | kDirHighFreq;
+        Spec F;
+        fresnelConductor(B.a, B.b, dotHV, F);
+        float G = ggxG1(B.ax, B.ay, q.dir, m) * ggxG1(B.ax, B.ay, d, m);
+        float r = 1.0f / (4 * q.dir.z * d.z);
+#pragma unroll
+        for (int i = 0; i < kNumLambda; ++i) fs.v[i] = ((F.v[i] * D) * G) * r;
+        return;
+    }
+    case kMatGGXScattering: {  // microfacet_bsdfs.cpp:116-215
+        bool entering = q.dir.z >= 0.0f;
+        float sign = entering ? 1.0f : -1.0f;
+        V3 m;
+        float mPdf;
+        float D = ggxSample(B.ax, B.ay, sign * q.dir, u0, u1, &m, &mPdf);
+        float dotHV = dot(q.dir, m);
+        if (dotHV * sign <= 0 || isnan(D)) return;
+        Spec F;
+        fresnelDielectric(B.a, B.b, dotHV, F);
+        float reflectProb = importance(F, q.wl);
+        if (uc < reflectProb) {
+            V3 d = (2 * dotHV) * m - q.dir;
+            if (d.z * q.dir.z <= 0) return;
+            float common = reflectProb / (4 * dotHV * sign);
+            res->dir = d;
+            res->pdf = common * mPdf;
+            res->type = kDirReflection | kDirHighFreq;
+            float G = ggxG1(B.ax, B.ay, q.dir, m) * ggxG1(B.ax, B.ay, d, m);
+            float r = 1.0f / (4 * q.dir.z * d.z);
+#pragma unroll
+            for (int i = 0; i < kNumLambda; ++i) fs.v[i] = ((F.v[i] * D) * G) * r;
+            return;
+        }
+        float eExtW = specAt(B.a, q.wl), eIntW = specAt(B.b, q.wl);
+        float eEnterW = entering ? eExtW : eIntW;
+        float eExitW = entering ? eIntW : eExtW;
+        float recRelIOR = eEnterW / eExitW;
+        float innerRoot = 1 + recRelIOR * recRelIOR * (dotHV * dotHV - 1);
+        if (innerRoot < 0) return;
+        V3 d = (recRelIOR * dotHV - sign * sqrtf(innerRoot)) * m - recRelIOR * q.dir;
+        if (d.z * q.dir.z >= 0) return;
+        float dotHL = dot(d, m);
+        float den = eEnterW * dotHV + eExitW * dotHL;
+        float common = (1 - reflectProb) / (den * den);
+        res->dir = d;
+        res->pdf = common * mPdf * eExitW * eExitW * fabsf(dotHL);
+        res->type = kDirTransmission | kDirHighFreq;
+        float r = 1.0f / fabsf(q.dir.z * d.z);
+#pragma unroll
+        for (int i = 0; i < kNumLambda; ++i) {
+            float eEnter = entering ? B.a.v[i] : B.b.v[i];
+            float eExit = entering ? B.b.v[i] : B.a.v[i];
+            V3 mw = normalize(-(eEnter * q.dir + eExit * d));
+            float dHV = dot(q.dir, mw), dHL = dot(d, mw);
+            float Fw = fresnelDielectric1(B.a.v[i], B.b.v[i], dHV);
+            float Gw = ggxG1(B.ax, B.ay, q.dir, mw) * ggxG1(B.ax, B.ay, d, mw);
+            float Dw = ggxD(B.ax, B.ay, mw);
+            float dd = eEnter * dHV + eExit * dHL;
+            float val = fabsf(dHV * dHL) * (1 - Fw) * Gw * Dw / (dd * dd);
+            fs.v[i] = (val * r) * (eEnter * eEnter);
+        }
+        return;
+    }
+    default:
+        return;
+    }
+}
+
+__device__ __noinline__ void bsdfEvalInternal(const Bsdf &B, const BsdfQuery &q, V3 dir, Spec &fs) {
+    fs = specConst(0.0f);
+    switch (B.kind) {
+    case kMatMatte:
+        if (q.dir.z * dir.z <= 0.0f) return;
+        specScale(B.a, 1.0f / kPiF, fs);
+        return;
+    case kMatGGXReflection: {
+        if (dir.z * q.dir.z <= 0) return;
+        float sign = q.dir.z >= 0.0f ? 1.0f : -1.0f;
+        V3 m = sign * normalize(q.dir + dir);
+        float dotHV = dot(q.dir, m);
+        float D = ggxD(B.ax, B.ay, m);
+        Spec F;
+        fresnelConductor(B.a, B.b, dotHV, F);
+        float G = ggxG1(B.ax, B.ay, q.dir, m) * ggxG1(B.ax, B.ay, dir, m);
+        float r = 1.0f / (4 * q.dir.z * dir.z);
+#pragma unroll
+        for (int i = 0; i < kNumLambda; ++i) fs.v[i] = ((F.v[i] * D) * G) * r;
+        return;
+    }
+    case kMatGGXScattering: {  // microfacet_bsdfs.cpp:217-263
+        bool entering = q.dir.z >= 0.0f;
+        float sign = entering ? 1.0f : -1.0f;
+        float dNVNL = dir.z * q.dir.z;
+        if (dNVNL > 0) {
+            V3 m = sign * normalize(q.dir + dir);
+            float dotHV = dot(q.dir, m);
+            float D = ggxD(B.ax, B.ay, m);
+            Spec F;
+            fresnelDielectric(B.a, B.b, dotHV, F);
+            float G = ggxG1(B.ax, B.ay, q.dir, m) * ggxG1(B.ax, B.ay, dir, m);
+            float r = 1.0f / (4 * dNVNL);
+#pragma unroll
+            for (int i = 0; i < kNumLambda; ++i) fs.v[i] = ((F.v[i] * D) * G) * r;
+        } else if (dNVNL < 0) {
+            float r = 1.0f / fabsf(dNVNL);
+#pragma unroll
+            for (int i = 0; i < kNumLambda; ++i) {
+                float eEnter = entering ? B.a.v[i] : B.b.v[i];
+                float eExit = entering ? B.b.v[i] : B.a.v[i];
+                V3 mw = normalize(-(eEnter * q.dir + eExit * dir));
+                float dHV = dot(q.dir, mw), dHL = dot(dir, mw);
+                float Fw = fresnelDielectric1(B.a.v[i], B.b.v[i], dHV);
+                float Gw = ggxG1(B.ax, B.ay, q.dir, mw) * ggxG1(B.ax, B.ay, dir, mw);
+                float Dw = ggxD(B.ax, B.ay, mw);
+                float dd = eEnter * dHV + eExit * dHL;
+                float val = fabsf(dHV * dHL) * (1 - Fw) * Gw * Dw / (dd * dd);
+                fs.v[i] = (val * r) * (eEnter * eEnter);
+            }
+        }
+        return;
+    }
+    default:  // delta BSDFs evaluate to zero
+        return;
+    }
+}
+
+__device__ __noinline__ float bsdfPdfInternal(const Bsdf &B, const BsdfQuery &q, V3 dir) {
+    switch (B.kind) {
+    case kMatMatte:
+        if (q.dir.z * dir.z <= 0.0f) return 0.0f;
+        return fabsf(dir.z) * kInvPiF;
+    case kMatGGXReflection: {
+        if (dir.z * q.dir.z <= 0) return 0.0f;
+        float sign = q.dir.z >= 0.0f ? 1.0f : -1.0f;
+        V3 m = sign * normalize(q.dir + dir);
+        float dotHV = dot(q.dir, m);
+        if (dotHV * sign <= 0) return 0.0f;
+        float mPdf = ggxPdf(B.ax, B.ay, sign * q.dir, m);
+        float common = 1.0f / (4 * dotHV * sign);
+        return common * mPdf;
+    }
+    case kMatGGXScattering: {  // microfacet_bsdfs.cpp:265-318
+        bool entering = q.dir.z >= 0.0f;
+        float sign = entering ? 1.0f : -1.0f;
+        float dNVNL = dir.z * q.dir.z;
+        if (dNVNL == 0) return 0.0f;
+        float eExtW = specAt(B.a, q.wl), eIntW = specAt(B.b, q.wl);
+        float eEnterW = entering ? eExtW : eIntW;
+        float eExitW = entering ? eIntW : eExtW;
+        V3 m = dNVNL > 0 ? sign * normalize(q.dir + dir) : normalize(-(eEnterW * q.dir + eExitW * dir));
+        float dotHV = dot(q.dir, m);
+        if (dotHV * sign <= 0) return 0.0f;
+        float mPdf = ggxPdf(B.ax, B.ay, sign * q.dir, m);
+        Spec F;
+        fresnelDielectric(B.a, B.b, dotHV, F);
+        float reflectProb = importance(F, q.wl);
+        if (dNVNL > 0) {
+            float common = reflectProb / (4 * dotHV * sign);
+            return common * mPdf;
+        }
+        float dotHL = dot(dir, m);
+        float den = eEnterW * dotHV + eExitW * dotHL;
+        float common = (1 - reflectProb) / (den * den);
+        return common * mPdf * eExitW * eExitW * fabsf(dotHL);
+    }
+    default:
+        return 0.0f;
+    }
+}
+
+// ---- the BSDF wrapper: shading-normal correction |d.z / dot(d, n_g)| ----
+__device__ __forceinline__ void bsdfSample(const Bsdf &B, const BsdfQuery &q, float uc, float u0, float u1,
+                                           BsdfSample* res, Spec &fs) {
+    bsdfSampleInternal(B, q, uc, u0, u1, res, fs);
+    if (res->pdf == 0.0f) return;
+    float sn = fabsf(res->dir.z / dot(res->dir, q.gn));
+#pragma unroll
+    for (int i = 0; i < kNumLambda; ++i) fs.v[i] *= sn;
+}
+
+__device__ __forceinline__ void bsdfEval(const Bsdf &B, const BsdfQuery &q, V3 dir, Spec &fs) {
+    bsdfEvalInternal(B, q, dir, fs);
+    float sn = fabsf(dir.z / dot(dir, q.gn));
+#pragma unroll
+    for (int i = 0; i < kNumLambda; ++i) fs.v[i] *= sn;
+}
+
+__device__ __forceinline__ float bsdfPdf(const Bsdf &B, const BsdfQuery &q, V3 dir) {
+    return bsdfPdfInternal(B, q, dir);
+}
+
+}  // namespace slrgpu

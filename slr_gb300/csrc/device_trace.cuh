@@ -1,0 +1,198 @@
+// Closest-hit and any-hit traversal of the 4-wide BVH.
+//
+// The box and triangle tests repeat the reference's arithmetic exactly (no
+// fused multiply-add): the slab test of BoundingBox3D::intersect
+// (libSLR/BasicTypes/BoundingBox3D.h:100-116) on the SBVH's own boxes, and
+// the Moller-Trumbore test of TriangleSurfaceShape::intersect
+// (libSLR/SurfaceShape/TriangleSurfaceShape.cpp:205-257), including its
+// inclusive [tmin, tmax] acceptance.  The wide nodes only skip the SBVH's
+// intermediate boxes, which contain their children's boxes, so every
+// triangle the reference would test is still tested.
+#pragma once
+#include "device_common.cuh"
+
+namespace slrgpu {
+
+struct Hit {
+    float t, b1, b2;
+    uint32_t prim;
+};
+
+constexpr uint32_t kNoHit = 0xffffffffu;
+constexpr int kTraceStack = 96;
+
+// Moller-Trumbore; returns true and t/b1/b2 when the triangle is hit within [tmin, tmax].
+__device__ __forceinline__ bool mtIntersect(const TriFrag &f, V3 org, V3 dir, float tmin, float tmax,
+                                            float* tOut, float* b1Out, float* b2Out) {
+    V3 e1 = V3{f.e1x, f.e1y, f.e1z};
+    V3 e2 = V3{f.e2x, f.e2y, f.e2z};
+    V3 p = rn_cross(dir, e2);
+    float det = rn_dot(e1, p);
+    if (det == 0.0f) return false;
+    float invDet = __fdiv_rn(1.0f, det);
+    V3 d = rn_sub(org, V3{f.v0x, f.v0y, f.v0z});
+    float b1 = __fmul_rn(rn_dot(d, p), invDet);
+    if (b1 < 0.0f || b1 > 1.0f) return false;
+    V3 q = rn_cross(d, e1);
+    float b2 = __fmul_rn(rn_dot(dir, q), invDet);
+    if (b2 < 0.0f || __fadd_rn(b1, b2) > 1.0f) return false;
+    float tt = __fmul_rn(rn_dot(e2, q), invDet);
+    if (tt < tmin || tt > tmax) return false;
+    *tOut = tt;
+    *b1Out = b1;
+    *b2Out = b2;
+    return true;
+}
+
+// Slab test; returns the entry distance (dist0) or +inf when rejected.
+__device__ __forceinline__ float slabTest(float lox, float hix, float loy, float hiy, float loz, float hiz,
+                                          V3 org, V3 inv, float tmin, float tmax) {
+    float d0 = tmin, d1 = tmax;
+    float tn = __fmul_rn(__fsub_rn(lox, org.x), inv.x), tf = __fmul_rn(__fsub_rn(hix, org.x), inv.x);
+    if (tn > tf) { float s = tn; tn = tf; tf = s; }
+    d0 = tn > d0 ? tn : d0;
+    d1 = tf < d1 ? tf : d1;
+    tn = __fmul_rn(__fsub_rn(loy, org.y), inv.y); tf = __fmul_rn(__fsub_rn(hiy, org.y), inv.y);
+    if (tn > tf) { float s = tn; tn = tf; tf = s; }
+    d0 = tn > d0 ? tn : d0;
+    d1 = tf < d1 ? tf : d1;
+    tn = __fmul_rn(__fsub_rn(loz, org.z), inv.z); tf = __fmul_rn(__fsub_rn(hiz, org.z), inv.z);
+    if (tn > tf) { float s = tn; tn = tf; tf = s; }
+    d0 = tn > d0 ? tn : d0;
+    d1 = tf < d1 ? tf : d1;
+    return (d0 > d1) ? __int_as_float(0x7f800000) : d0;
+}
+
+struct StackEntry {
+    uint32_t node;
+    float tnear;
+};
+
+// Box test of the 4 children of a node; returns the hit mask and entry distances.
+__device__ __forceinline__ uint32_t testChildren(const BvhNode4* __restrict__ nodes, uint32_t ni, V3 org, V3 inv,
+                                                 float tmin, float tmax, float tn[4], uint32_t ch[4]) {
+    const float4* np = reinterpret_cast<const float4*>(nodes + ni);
+    float4 lx = __ldg(np + 0), hx = __ldg(np + 1), ly = __ldg(np + 2), hy = __ldg(np + 3);
+    float4 lz = __ldg(np + 4), hz = __ldg(np + 5);
+    uint4 c = __ldg(reinterpret_cast<const uint4*>(np + 6));
+    ch[0] = c.x; ch[1] = c.y; ch[2] = c.z; ch[3] = c.w;
+    uint32_t mask = 0;
+    float lxa[4] = {lx.x, lx.y, lx.z, lx.w}, hxa[4] = {hx.x, hx.y, hx.z, hx.w};
+    float lya[4] = {ly.x, ly.y, ly.z, ly.w}, hya[4] = {hy.x, hy.y, hy.z, hy.w};
+    float lza[4] = {lz.x, lz.y, lz.z, lz.w}, hza[4] = {hz.x, hz.y, hz.z, hz.w};
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        tn[k] = slabTest(lxa[k], hxa[k], lya[k], hya[k], lza[k], hza[k], org, inv, tmin, tmax);
+        if (ch[k] != kChildEmpty && tn[k] != __int_as_float(0x7f800000)) mask |= 1u << k;
+    }
+    return mask;
+}
+
+__device__ __forceinline__ TriFrag loadFrag(const TriFrag* __restrict__ frags, uint32_t i) {
+    const float4* p = reinterpret_cast<const float4*>(frags + i);
+    float4 a = __ldg(p), b = __ldg(p + 1), c = __ldg(p + 2);
+    TriFrag f;
+    f.v0x = a.x; f.v0y = a.y; f.v0z = a.z; f.prim = __float_as_uint(a.w);
+    f.e1x = b.x; f.e1y = b.y; f.e1z = b.z; f.pad0 = 0;
+    f.e2x = c.x; f.e2y = c.y; f.e2z = c.z; f.pad1 = 0;
+    return f;
+}
+
+// Closest hit over [tmin, tmax].  Returns false on stack overflow (the hit
+// found so far is still reported).
+__device__ __forceinline__ bool traceClosest(const DevScene &sc, V3 org, V3 dir, float tmin, float tmax, Hit* hit) {
+    hit->prim = kNoHit;
+    hit->t = __int_as_float(0x7f800000);
+    hit->b1 = hit->b2 = 0.0f;
+    V3 inv = V3{__fdiv_rn(1.0f, dir.x), __fdiv_rn(1.0f, dir.y), __fdiv_rn(1.0f, dir.z)};
+    StackEntry stack[kTraceStack];
+    int sp = 0;
+    uint32_t cur = 0;
+    bool ok = true;
+    if (sc.numPrims == 0) return true;
+    for (;;) {
+        if (!(cur & kLeafBit)) {
+            float tn[4];
+            uint32_t ch[4];
+            uint32_t mask = testChildren(sc.nodes, cur, org, inv, tmin, tmax, tn, ch);
+            // Order hit children near to far; visit the nearest next and push the rest.
+            uint32_t order[4];
+            int n = 0;
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+                if (mask & (1u << k)) order[n++] = k;
+            // insertion sort by tn (n <= 4)
+            for (int a = 1; a < n; ++a) {
+                uint32_t x = order[a];
+                int b = a - 1;
+                while (b >= 0 && tn[order[b]] > tn[x]) { order[b + 1] = order[b]; --b; }
+                order[b + 1] = x;
+            }
+            if (n == 0) goto pop;
+            for (int k = n - 1; k >= 1; --k) {
+                if (sp < kTraceStack) stack[sp++] = StackEntry{ch[order[k]], tn[order[k]]};
+                else ok = false;
+            }
+            cur = ch[order[0]];
+            continue;
+        } else {
+            uint32_t first = cur & kLeafFirstMask;
+            uint32_t count = ((cur >> kLeafCountShift) & 0x1f) + 1;
+            for (uint32_t i = 0; i < count; ++i) {
+                TriFrag f = loadFrag(sc.frags, first + i);
+                float t, b1, b2;
+                if (mtIntersect(f, org, dir, tmin, tmax, &t, &b1, &b2)) {
+                    tmax = t;
+                    hit->t = t;
+                    hit->b1 = b1;
+                    hit->b2 = b2;
+                    hit->prim = f.prim;
+                }
+            }
+        }
+    pop:
+        for (;;) {
+            if (sp == 0) return ok;
+            StackEntry e = stack[--sp];
+            if (e.tnear <= tmax) { cur = e.node; break; }
+        }
+    }
+}
+
+// Any hit over [tmin, tmax]: true when the segment is occluded.
+__device__ __forceinline__ bool traceAny(const DevScene &sc, V3 org, V3 dir, float tmin, float tmax) {
+    if (sc.numPrims == 0) return false;
+    V3 inv = V3{__fdiv_rn(1.0f, dir.x), __fdiv_rn(1.0f, dir.y), __fdiv_rn(1.0f, dir.z)};
+    uint32_t stack[kTraceStack];
+    int sp = 0;
+    uint32_t cur = 0;
+    for (;;) {
+        if (!(cur & kLeafBit)) {
+            float tn[4];
+            uint32_t ch[4];
+            uint32_t mask = testChildren(sc.nodes, cur, org, inv, tmin, tmax, tn, ch);
+            bool have = false;
+            uint32_t next = 0;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                if (mask & (1u << k)) {
+                    if (!have) { next = ch[k]; have = true; }
+                    else if (sp < kTraceStack) stack[sp++] = ch[k];
+                }
+            }
+            if (have) { cur = next; continue; }
+        } else {
+            uint32_t first = cur & kLeafFirstMask;
+            uint32_t count = ((cur >> kLeafCountShift) & 0x1f) + 1;
+            for (uint32_t i = 0; i < count; ++i) {
+                TriFrag f = loadFrag(sc.frags, first + i);
+                float t, b1, b2;
+                if (mtIntersect(f, org, dir, tmin, tmax, &t, &b1, &b2)) return true;
+            }
+        }
+        if (sp == 0) return false;
+        cur = stack[--sp];
+    }
+}
+
+}  // namespace slrgpu

@@ -1,0 +1,1005 @@
+// Wavefront path tracer (PTRenderer semantics) on the GPU.
+//
+// One wave = S samples of every pixel; each path is one thread slot in SoA
+// state arrays.  Per bounce: extend (closest hit) -> shade (emission with
+// MIS, Russian roulette, next-event estimation, BSDF sampling) -> shadow (any
+// hit) over compacted queues; after the last bounce the wave's paths are
+// added to the 16-bin film with compensated summation.  The estimator is the
+// reference's PTRenderer::Job::contribution (libSLR/Renderer/PTRenderer.cpp:146-276)
+// and Job::kernel (:103-144); only the random numbers differ (counter-based).
+#include "render_api.h"
+
+#include <algorithm>
+#include <chrono>
+#include <cstdio>
+#include <cstring>
+
+#include "device_bsdf.cuh"
+#include "device_trace.cuh"
+
+namespace slrgpu {
+
+#define CUDA_TRY(x)                                                                 \
+    do {                                                                            \
+        cudaError_t e_ = (x);                                                       \
+        if (e_ != cudaSuccess) {                                                    \
+            setError(std::string(#x) + ": " + cudaGetErrorString(e_));             \
+            return SLRGPU_ERR_CUDA;                                                 \
+        }                                                                           \
+    } while (0)
+
+// ---------------------------------------------------------------------------
+// Path state (structure of arrays, N = paths per wave)
+// ---------------------------------------------------------------------------
+struct WaveState {
+    float4* rayOrg;      // xyz, tmin
+    float4* rayDir;      // xyz, tmax
+    float4* hit;         // t, b1, b2, prim bits
+    float* alpha;        // [16][N]
+    float* L;            // [16][N]
+    uint32_t* info;      // bits 0-3 selected lambda, 4 wavelength selected, 5 previous delta, 8-15 depth
+    float* wlOffset;
+    float* prevPdf;
+    float* initY;
+    float* camWeight;
+    uint32_t* rngCounter;
+    float4* shOrg;
+    float4* shDir;
+    float* shContrib;    // [16][N]
+    uint32_t* queue[2];
+    uint32_t* shadowQueue;
+    uint32_t* counters;  // [3 * (maxDepth + 2)]
+    unsigned long long* stats;  // 0 extension rays, 1 shadow rays, 2 dropped samples
+    uint32_t N;
+};
+
+struct WaveParams {
+    uint32_t width, height, numPixels;
+    uint32_t samplesInWave;   // S
+    uint32_t sampleBase;      // first sample index of the wave
+    uint32_t numPaths;
+    uint32_t maxDepth;
+    uint32_t seed;
+};
+
+constexpr uint32_t kInfoSelMask = 0xfu;
+constexpr uint32_t kInfoWlSelected = 1u << 4;
+constexpr uint32_t kInfoPrevDelta = 1u << 5;
+constexpr int kInfoDepthShift = 8;
+
+__device__ __forceinline__ void loadSpec(const float* base, uint32_t N, uint32_t p, Spec &s) {
+#pragma unroll
+    for (int i = 0; i < kNumLambda; ++i) s.v[i] = base[(size_t)i * N + p];
+}
+__device__ __forceinline__ void storeSpec(float* base, uint32_t N, uint32_t p, const Spec &s) {
+#pragma unroll
+    for (int i = 0; i < kNumLambda; ++i) base[(size_t)i * N + p] = s.v[i];
+}
+__device__ __forceinline__ void addSpec(float* base, uint32_t N, uint32_t p, const Spec &s) {
+#pragma unroll
+    for (int i = 0; i < kNumLambda; ++i) base[(size_t)i * N + p] += s.v[i];
+}
+
+// Warp-aggregated queue push.
+__device__ __forceinline__ void queuePush(uint32_t* queue, uint32_t* count, uint32_t value, bool pred) {
+    unsigned mask = __ballot_sync(__activemask(), pred);
+    if (!pred) return;
+    int leader = __ffs(mask) - 1;
+    int lane = threadIdx.x & 31;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(count, (uint32_t)__popc(mask));
+    base = __shfl_sync(mask, base, leader);
+    queue[base + __popc(mask & ((1u << lane) - 1))] = value;
+}
+
+__device__ __forceinline__ uint64_t sampleIndexOf(const WaveParams &wp, uint32_t p) {
+    uint32_t s = p / wp.numPixels;
+    uint32_t pixel = p - s * wp.numPixels;
+    return (uint64_t)(wp.sampleBase + s) * wp.numPixels + pixel;
+}
+
+// ---------------------------------------------------------------------------
+// Camera
+// ---------------------------------------------------------------------------
+// Thin-lens perspective camera (PerspectiveCamera.cpp:31-83) and
+// equirectangular camera (EquirectangularCamera.cpp:25-69): ray and the
+// sample weight We0 We1 cos / (areaPDF dirPDF).
+__device__ __forceinline__ void cameraRay(const DevCamera &c, float lu0, float lu1, float px, float py,
+                                          V3* org, V3* dir, float* weight) {
+    V3 ex = V3{c.ex[0], c.ex[1], c.ex[2]}, ey = V3{c.ey[0], c.ey[1], c.ey[2]}, ez = V3{c.ez[0], c.ez[1], c.ez[2]};
+    Frame fr{ex, ey, ez};
+    if (c.kind == 0) {
+        float lx, ly;
+        concentricSampleDisk(lu0, lu1, &lx, &ly);
+        V3 orgLocal = V3{c.lensRadius * lx, c.lensRadius * ly, 0.0f};
+        *org = V3{c.org[0], c.org[1], c.org[2]} + orgLocal.x * ex + orgLocal.y * ey;
+        V3 pFocus = V3{c.opWidth * (0.5f - px), c.opHeight * (0.5f - py), c.objPlaneDist};
+        V3 dl = normalize(pFocus - orgLocal);
+        float dirPDF = c.imgPlaneDist * c.imgPlaneDist / ((dl.z * dl.z * dl.z) * c.imgPlaneArea);
+        float areaPDF = c.lensRadius > 0.0f ? 1.0f / (kPiF * c.lensRadius * c.lensRadius) : 1.0f;
+        *dir = fr.fromLocal(dl);
+        float cosT = absDot(*dir, ez);
+        *weight = cosT / (areaPDF * dirPDF);
+    } else {
+        *org = V3{c.org[0], c.org[1], c.org[2]};
+        float phi = c.phiAngle * (px - 0.5f);
+        float theta = 0.5f * kPiF + c.thetaAngle * (py - 0.5f);
+        float sp, cp, st, ct;
+        sincosf(phi, &sp, &cp);
+        sincosf(theta, &st, &ct);
+        V3 dl = V3{-sp * st, ct, cp * st};
+        float dirPDF = 1.0f / (c.phiAngle * c.thetaAngle * st);
+        *dir = fr.fromLocal(dl);
+        *weight = 1.0f / dirPDF;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Environment
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void toPolarYUp(V3 d, float* theta, float* phi) {
+    *theta = acosf(fminf(fmaxf(d.y, -1.0f), 1.0f));
+    const float twoPi = 6.28318530717958647692f;
+    *phi = fmodf(atan2f(-d.x, d.z) + twoPi, twoPi);
+}
+
+// Emitted radiance of the environment at texture coordinate (tu, tv):
+// (pi * texel * scale) * (1 / pi) (IBLEmitterSurfaceProperty.cpp:16-18, IBLEDF.cpp:18-21).
+__device__ __forceinline__ void envRadiance(const DevScene &sc, float tu, float tv, const float lambdas[kNumLambda],
+                                            Spec &Le) {
+    float u = fmodf(tu, 1.0f), v = fmodf(tv, 1.0f);
+    u += u < 0 ? 1.0f : 0.0f;
+    v += v < 0 ? 1.0f : 0.0f;
+    uint32_t px = min((uint32_t)(sc.envWidth * u), sc.envWidth - 1);
+    uint32_t py = min((uint32_t)(sc.envHeight * v), sc.envHeight - 1);
+    EnvTexel tx = sc.envTexels[(size_t)py * sc.envWidth + px];
+    evalUpsampled(sc.upsSpectra, tx.adj, tx.s, tx.t, tx.scale, lambdas, Le);
+#pragma unroll
+    for (int i = 0; i < kNumLambda; ++i) Le.v[i] = ((Le.v[i] * kPiF) * sc.envScale) * kInvPiF;
+}
+
+// RegularConstantContinuousDistribution1D::sample (distributions.cpp:205-214).
+__device__ __forceinline__ uint32_t prevPow2(uint32_t x) {
+    x |= x >> 1; x |= x >> 2; x |= x >> 4; x |= x >> 8; x |= x >> 16;
+    return x - (x >> 1);
+}
+__device__ __forceinline__ float sample1D(const float* pdf, const float* cdf, uint32_t n, float u, float* outPdf) {
+    int idx = (int)n;
+    for (int d = (int)prevPow2(n); d > 0; d >>= 1)
+        if (idx - d > 0 && cdf[idx - d] >= u) idx -= d;
+    --idx;
+    *outPdf = pdf[idx];
+    float t = (u - cdf[idx]) / (cdf[idx + 1] - cdf[idx]);
+    return (idx + t) / n;
+}
+
+__device__ __forceinline__ float envUVPdf(const DevScene &sc, float d0, float d1) {
+    uint32_t row = min((uint32_t)(sc.envMapH * d1), sc.envMapH - 1);
+    float top = sc.envTopPDF[min((int)(d1 * sc.envMapH), (int)sc.envMapH - 1)];
+    return top * sc.envRowPDF[(size_t)row * sc.envMapW + min((int)(d0 * sc.envMapW), (int)sc.envMapW - 1)];
+}
+
+// Area pdf of the environment at (phi, theta) (surface_object.cpp:281-286).
+__device__ __forceinline__ float envAreaPdf(const DevScene &sc, float phi, float theta) {
+    const float twoPi = 6.28318530717958647692f;
+    float uvPdf = envUVPdf(sc, phi / twoPi, theta / kPiF);
+    return uvPdf / (2.0f * kPiF * kPiF * sinf(theta));
+}
+
+// ---------------------------------------------------------------------------
+// Material -> BSDF (SurfaceMaterial::getBSDF)
+// ---------------------------------------------------------------------------
+__device__ __noinline__ void makeBsdf(const DevScene &sc, const DevMaterial &m, const float lambdas[kNumLambda],
+                                      bool wlSelected, Bsdf &B) {
+    B.kind = m.kind;
+    B.ax = m.alphaX;
+    B.ay = m.alphaY;
+    B.dispersive = !wlSelected;
+    switch (m.kind) {
+    case kMatMatte:
+        evalSpectrum(sc, m.spec[0], lambdas, B.a);
+        break;
+    case kMatSpecularReflection:
+    case kMatSpecularScattering:
+        evalSpectrum(sc, m.spec[0], lambdas, B.a);
+        evalSpectrum(sc, m.spec[1], lambdas, B.b);
+        evalSpectrum(sc, m.spec[2], lambdas, B.c);
+        break;
+    case kMatGGXReflection:
+    case kMatGGXScattering:
+        evalSpectrum(sc, m.spec[0], lambdas, B.a);
+        evalSpectrum(sc, m.spec[1], lambdas, B.b);
+        break;
+    default:
+        break;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Kernels
+// ---------------------------------------------------------------------------
+__global__ void kRaygen(DevScene sc, WaveState ws, WaveParams wp) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) ws.counters[0] = wp.numPaths;
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < wp.numPaths; p += gridDim.x * blockDim.x) {
+        uint32_t s = p / wp.numPixels;
+        uint32_t pixel = p - s * wp.numPixels;
+        uint32_t ix = pixel % wp.width, iy = pixel / wp.width;
+        Rng rng{pathKey(wp.seed, (uint64_t)(wp.sampleBase + s) * wp.numPixels + pixel), 0};
+        // Draw order of Job::kernel: time, pixel (2), wavelength offset,
+        // wavelength selection, lens (2) (PTRenderer.cpp:108-116).
+        (void)rng.next();
+        float pxf = ix + rng.next();
+        float pyf = iy + rng.next();
+        float wlOff = rng.next();
+        float uSel = rng.next();
+        float lu0 = rng.next(), lu1 = rng.next();
+        uint32_t sel = min((uint32_t)(kNumLambda * uSel), (uint32_t)(kNumLambda - 1));
+        const float selectWLPDF = kNumLambda / (kWavelengthHigh - kWavelengthLow);
+        V3 org, dir;
+        float w;
+        cameraRay(sc.camera, lu0, lu1, pxf / wp.width, pyf / wp.height, &org, &dir, &w);
+        ws.camWeight[p] = w / selectWLPDF;
+        ws.rayOrg[p] = make_float4(org.x, org.y, org.z, 0.0f);
+        ws.rayDir[p] = make_float4(dir.x, dir.y, dir.z, __int_as_float(0x7f800000));
+        ws.wlOffset[p] = wlOff;
+        ws.info[p] = sel;
+        ws.rngCounter[p] = rng.counter;
+        Spec one = specConst(1.0f);
+        ws.initY[p] = importance(one, (int)sel);
+        ws.prevPdf[p] = 0.0f;
+#pragma unroll
+        for (int i = 0; i < kNumLambda; ++i) {
+            ws.alpha[(size_t)i * ws.N + p] = 1.0f;
+            ws.L[(size_t)i * ws.N + p] = 0.0f;
+        }
+        ws.queue[0][p] = p;
+    }
+}
+
+__global__ void kExtend(DevScene sc, WaveState ws, const uint32_t* __restrict__ queue, const uint32_t* __restrict__ count) {
+    const uint32_t n = *count;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        uint32_t p = queue[i];
+        float4 o = ws.rayOrg[p], d = ws.rayDir[p];
+        Hit h;
+        traceClosest(sc, V3{o.x, o.y, o.z}, V3{d.x, d.y, d.z}, o.w, d.w, &h);
+        ws.hit[p] = make_float4(h.t, h.b1, h.b2, __uint_as_float(h.prim));
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&ws.stats[0], (unsigned long long)n);
+}
+
+__global__ void kShadow(DevScene sc, WaveState ws, const uint32_t* __restrict__ queue, const uint32_t* __restrict__ count) {
+    const uint32_t n = *count;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        uint32_t p = queue[i];
+        float4 o = ws.shOrg[p], d = ws.shDir[p];
+        if (!traceAny(sc, V3{o.x, o.y, o.z}, V3{d.x, d.y, d.z}, o.w, d.w)) {
+#pragma unroll
+            for (int k = 0; k < kNumLambda; ++k)
+                ws.L[(size_t)k * ws.N + p] += ws.shContrib[(size_t)k * ws.N + p];
+        }
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&ws.stats[1], (unsigned long long)n);
+}
+
+struct SurfPoint {
+    V3 p;
+    Frame frame;
+    V3 gn;
+};
+
+// Surface point of a hit (TriangleSurfaceShape.cpp:301-346): interpolated
+// shading normal, tangent made orthogonal to it, geometric normal.
+__device__ __forceinline__ void surfacePoint(const DevScene &sc, const DevPrim &pr, V3 org, V3 dir, float t, float mb1,
+                                             float mb2, SurfPoint &sp) {
+    sp.p = org + dir * t;
+    float b0 = 1.0f - mb1 - mb2;
+    float b1 = mb1;
+    float b2 = 1.0f - b0 - b1;
+    float4 n0 = sc.vnrm[pr.v0], n1 = sc.vnrm[pr.v1], n2 = sc.vnrm[pr.v2];
+    float4 t0 = sc.vtan[pr.v0], t1 = sc.vtan[pr.v1], t2 = sc.vtan[pr.v2];
+    V3 z = normalize(b0 * V3{n0.x, n0.y, n0.z} + b1 * V3{n1.x, n1.y, n1.z} + b2 * V3{n2.x, n2.y, n2.z});
+    V3 x = b0 * V3{t0.x, t0.y, t0.z} + b1 * V3{t1.x, t1.y, t1.z} + b2 * V3{t2.x, t2.y, t2.z};
+    float dnt = dot(z, x);
+    x = normalize(x - dnt * z);
+    sp.frame = Frame{x, cross(z, x), z};
+    sp.gn = V3{pr.ngx, pr.ngy, pr.ngz};
+}
+
+// Light selection (Scene::selectSurfaceLight, Scene.cpp:137-155).  Returns
+// -1 for the environment, else the light index; *prob = selection probability.
+__device__ __forceinline__ int selectLight(const DevScene &sc, float u, float* prob) {
+    auto surf = [&](float uu, float* pr) -> int {
+        int idx = (int)sc.numLights;
+        for (int d = (int)prevPow2(sc.numLights); d > 0; d >>= 1)
+            if (idx - d > 0 && sc.lightCDF[idx - d] >= uu) idx -= d;
+        --idx;
+        *pr = sc.lightPMF[idx];
+        return idx;
+    };
+    if (sc.envPresent) {
+        float sumImps = sc.surfImportance + sc.envImportance;
+        float su = sumImps * u;
+        if (su < sc.surfImportance) {
+            float uu = u / (sc.surfImportance / sumImps);
+            int idx = surf(uu, prob);
+            *prob *= sc.surfImportance / sumImps;
+            return idx;
+        }
+        *prob = 1.0f * (sc.envImportance / sumImps);
+        return -1;
+    }
+    return surf(u, prob);
+}
+
+__global__ void __launch_bounds__(256) kShade(DevScene sc, WaveState ws, WaveParams wp,
+                                              const uint32_t* __restrict__ inQueue, const uint32_t* __restrict__ inCount,
+                                              uint32_t* outQueue, uint32_t* outCount, uint32_t* shQueue, uint32_t* shCount) {
+    const uint32_t n = *inCount;
+    const uint32_t N = ws.N;
+    const float inf = __int_as_float(0x7f800000);
+    const float twoPi = 6.28318530717958647692f;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+        const uint32_t i = base + threadIdx.x;
+        bool active = i < n;
+        bool extend = false, shadow = false;
+        uint32_t p = active ? inQueue[i] : 0;
+        if (active) {
+            uint32_t info = ws.info[p];
+            const int sel = (int)(info & kInfoSelMask);
+            bool wlSelected = (info & kInfoWlSelected) != 0;
+            const bool prevDelta = (info & kInfoPrevDelta) != 0;
+            uint32_t depth = info >> kInfoDepthShift;
+            const float wlOff = ws.wlOffset[p];
+            float lambdas[kNumLambda];
+#pragma unroll
+            for (int k = 0; k < kNumLambda; ++k) lambdas[k] = lambdaAt(k, wlOff);
+            Rng rng{pathKey(wp.seed, sampleIndexOf(wp, p)), ws.rngCounter[p]};
+            float4 ro = ws.rayOrg[p], rd = ws.rayDir[p];
+            V3 org = V3{ro.x, ro.y, ro.z}, dir = V3{rd.x, rd.y, rd.z};
+            float4 hv = ws.hit[p];
+            uint32_t prim = __float_as_uint(hv.w);
+            Spec alpha;
+            loadSpec(ws.alpha, N, p, alpha);
+            bool alive = true;
+
+            if (prim == kNoHit) {
+                // Environment (Scene.cpp:57-62): always "hit" for unbounded rays.
+                if (sc.envPresent) {
+                    float theta, phi;
+                    toPolarYUp(dir, &theta, &phi);
+                    Spec Le;
+                    envRadiance(sc, phi / twoPi, theta / kPiF, lambdas, Le);
+                    float mis = 1.0f;
+                    if (depth > 0 && !prevDelta) {
+                        float lightProb = sc.envImportance / (sc.surfImportance + sc.envImportance);
+                        float lightPdf = lightProb * envAreaPdf(sc, phi, theta) * 1.0f / absDot(dir, -dir);
+                        float bp = ws.prevPdf[p];
+                        mis = (bp * bp) / (lightPdf * lightPdf + bp * bp);
+                    }
+                    Spec add;
+#pragma unroll
+                    for (int k = 0; k < kNumLambda; ++k) add.v[k] = alpha.v[k] * Le.v[k] * mis;
+                    addSpec(ws.L, N, p, add);
+                }
+                alive = false;
+            } else {
+                const DevPrim pr = sc.prims[prim];
+                SurfPoint sp;
+                surfacePoint(sc, pr, org, dir, hv.x, hv.y, hv.z, sp);
+                const DevMaterial mat = sc.materials[pr.material];
+                V3 dirOut = sp.frame.toLocal(-dir);
+                // Emission on hit (PTRenderer.cpp:162-166, :240-263).
+                if (mat.emit >= 0) {
+                    Spec M;
+                    evalSpectrum(sc, mat.emit, lambdas, M);
+                    float edf = dirOut.z > 0.0f ? kInvPiF : 0.0f;
+                    float mis = 1.0f;
+                    if (depth > 0 && !prevDelta) {
+                        float lightProb = (sc.surfImportance / (sc.surfImportance + sc.envImportance)) * sc.lightPMF[0];
+                        float dist2 = sqLength(sp.p - org);
+                        float lightPdf = lightProb * pr.invArea * dist2 / absDot(dir, sp.gn);
+                        float bp = ws.prevPdf[p];
+                        mis = (bp * bp) / (lightPdf * lightPdf + bp * bp);
+                    }
+                    Spec add;
+#pragma unroll
+                    for (int k = 0; k < kNumLambda; ++k) add.v[k] = alpha.v[k] * (M.v[k] * edf) * mis;
+                    addSpec(ws.L, N, p, add);
+                }
+                // Russian roulette (PTRenderer.cpp:266-272).
+                if (depth > 0) {
+                    float cp = fminf(importance(alpha, sel) / ws.initY[p], 1.0f);
+                    if (rng.next() < cp) {
+                        float r = 1.0f / cp;
+#pragma unroll
+                        for (int k = 0; k < kNumLambda; ++k) alpha.v[k] *= r;
+                    } else {
+                        alive = false;
+                    }
+                }
+                if (alive) {
+                    ++depth;
+                    if (depth > wp.maxDepth) alive = false;
+                }
+                if (alive) {
+                    Bsdf B;
+                    makeBsdf(sc, mat, lambdas, wlSelected, B);
+                    BsdfQuery q{dirOut, sp.frame.toLocal(sp.gn), sel};
+                    // Next-event estimation (PTRenderer.cpp:179-218).
+                    if (bsdfHasNonDelta(B.kind) && (sc.numLights > 0 || sc.envPresent)) {
+                        float lightProb;
+                        int li = selectLight(sc, rng.next(), &lightProb);
+                        float lu0 = rng.next(), lu1 = rng.next();
+                        V3 lp, lgn;
+                        Spec M;
+                        float areaPdf;
+                        bool atInf = false;
+                        float edfVal = 0.0f;
+                        V3 shadowDir;
+                        float dist2;
+                        if (li >= 0) {
+                            const DevPrim lpr = sc.prims[sc.lightPrims[li]];
+                            float su = sqrtf(lu0);
+                            float b0 = 1.0f - su, b1 = lu1 * su, b2 = 1.0f - b0 - b1;
+                            float4 p0 = sc.vpos[lpr.v0], p1 = sc.vpos[lpr.v1], p2 = sc.vpos[lpr.v2];
+                            V3 P0 = V3{p0.x, p0.y, p0.z}, P1 = V3{p1.x, p1.y, p1.z}, P2 = V3{p2.x, p2.y, p2.z};
+                            lp = b0 * P0 + b1 * P1 + b2 * P2;
+                            float4 n0 = sc.vnrm[lpr.v0], n1 = sc.vnrm[lpr.v1], n2 = sc.vnrm[lpr.v2];
+                            V3 lz = normalize(b0 * V3{n0.x, n0.y, n0.z} + b1 * V3{n1.x, n1.y, n1.z} + b2 * V3{n2.x, n2.y, n2.z});
+                            lgn = V3{lpr.ngx, lpr.ngy, lpr.ngz};
+                            areaPdf = lpr.invArea;
+                            evalSpectrum(sc, sc.materials[lpr.material].emit, lambdas, M);
+                            V3 diff = lp - sp.p;
+                            dist2 = sqLength(diff);
+                            shadowDir = diff * (1.0f / sqrtf(dist2));
+                            edfVal = dot(lz, -shadowDir) > 0.0f ? kInvPiF : 0.0f;
+                        } else {
+                            float uvPdf, topPdf;
+                            float d1 = sample1D(sc.envTopPDF, sc.envTopCDF, sc.envMapH, lu1, &topPdf);
+                            uint32_t row = min((uint32_t)(sc.envMapH * d1), sc.envMapH - 1);
+                            float d0 = sample1D(sc.envRowPDF + (size_t)row * sc.envMapW,
+                                                sc.envRowCDF + (size_t)row * (sc.envMapW + 1), sc.envMapW, lu0, &uvPdf);
+                            uvPdf *= topPdf;
+                            float phi = d0 * twoPi, theta = d1 * kPiF;
+                            float sph, cph, sth, cth;
+                            sincosf(phi, &sph, &cph);
+                            sincosf(theta, &sth, &cth);
+                            lp = V3{-sph * sth, cth, cph * sth};
+                            lgn = -lp;
+                            atInf = true;
+                            areaPdf = uvPdf / (2.0f * kPiF * kPiF * sth);
+                            envRadiance(sc, phi / twoPi, theta / kPiF, lambdas, M);
+                            // M already includes the IBL EDF's 1/pi; edf factor 1.
+                            edfVal = 1.0f;
+                            shadowDir = normalize(lp);
+                            dist2 = 1.0f;
+                        }
+                        float cosShading = absDot(shadowDir, sp.gn);
+                        float cosLight = absDot(shadowDir, lgn);
+                        if (cosShading * cosLight > 0) {
+                            float lightPdf = lightProb * areaPdf;
+                            V3 sdl = sp.frame.toLocal(shadowDir);
+                            Spec fs;
+                            bsdfEval(B, q, sdl, fs);
+                            float bsdfPdfV = bsdfPdf(B, q, sdl) * cosLight / dist2;
+                            float mis = 1.0f;
+                            if (!isinf(areaPdf))
+                                mis = (lightPdf * lightPdf) / (lightPdf * lightPdf + bsdfPdfV * bsdfPdfV);
+                            float G = cosShading * cosLight / dist2;
+                            float scale = G * mis / lightPdf;
+                            Spec c;
+                            bool nz = false;
+#pragma unroll
+                            for (int k = 0; k < kNumLambda; ++k) {
+                                c.v[k] = ((alpha.v[k] * (M.v[k] * edfVal)) * fs.v[k]) * scale;
+                                nz |= c.v[k] != 0.0f;
+                            }
+                            if (nz) {
+                                storeSpec(ws.shContrib, N, p, c);
+                                float tmax;
+                                V3 sdir;
+                                if (atInf) {
+                                    sdir = shadowDir;
+                                    tmax = 3.402823466e+38f;
+                                } else {
+                                    V3 dd = lp - sp.p;
+                                    float dist = length(dd);
+                                    sdir = dd * (1.0f / dist);
+                                    tmax = dist * (1 - kRayEpsilon);
+                                }
+                                ws.shOrg[p] = make_float4(sp.p.x, sp.p.y, sp.p.z, kRayEpsilon);
+                                ws.shDir[p] = make_float4(sdir.x, sdir.y, sdir.z, tmax);
+                                shadow = true;
+                            }
+                        }
+                    }
+                    // BSDF sampling (PTRenderer.cpp:220-236).
+                    float uc = rng.next(), u0 = rng.next(), u1 = rng.next();
+                    BsdfSample bs;
+                    Spec fs;
+                    bsdfSample(B, q, uc, u0, u1, &bs, fs);
+                    if (bs.pdf == 0.0f || specIsZero(fs)) {
+                        alive = false;
+                    } else {
+                        if ((bs.type & kDirDispersive) && !wlSelected) {
+                            bs.pdf /= kNumLambda;
+                            wlSelected = true;
+                        }
+                        float cg = absDot(bs.dir, q.gn);
+                        float r = 1.0f / bs.pdf;
+#pragma unroll
+                        for (int k = 0; k < kNumLambda; ++k) alpha.v[k] *= (fs.v[k] * cg) * r;
+                        V3 nd = sp.frame.fromLocal(bs.dir);
+                        ws.rayOrg[p] = make_float4(sp.p.x, sp.p.y, sp.p.z, kRayEpsilon);
+                        ws.rayDir[p] = make_float4(nd.x, nd.y, nd.z, inf);
+                        ws.prevPdf[p] = bs.pdf;
+                        info = (uint32_t)sel | (wlSelected ? kInfoWlSelected : 0u) |
+                               (dirIsDelta(bs.type) ? kInfoPrevDelta : 0u) | (depth << kInfoDepthShift);
+                        ws.info[p] = info;
+                        storeSpec(ws.alpha, N, p, alpha);
+                        extend = true;
+                    }
+                }
+            }
+            ws.rngCounter[p] = rng.counter;
+        }
+        queuePush(shQueue, shCount, p, active && shadow);
+        queuePush(outQueue, outCount, p, active && extend);
+    }
+}
+
+// Adds the wave's paths to the film: C = L * weight, dropped when not finite
+// (PTRenderer.cpp:129-138); binning and compensated sum of
+// SpectrumStorage::add (spectrum_types.h:716-739, CompensatedSum.h:16-33).
+__global__ void kAccumulate(WaveState ws, WaveParams wp, float* filmSum, float* filmComp) {
+    const float recBinWidth = kNumLambda / (kWavelengthHigh - kWavelengthLow);
+    const uint32_t P = wp.numPixels;
+    unsigned long long dropped = 0;
+    for (uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x; pix < P; pix += gridDim.x * blockDim.x) {
+        float sum[kNumLambda], comp[kNumLambda];
+#pragma unroll
+        for (int b = 0; b < kNumLambda; ++b) {
+            sum[b] = filmSum[(size_t)b * P + pix];
+            comp[b] = filmComp[(size_t)b * P + pix];
+        }
+        for (uint32_t s = 0; s < wp.samplesInWave; ++s) {
+            uint32_t p = s * P + pix;
+            float w = ws.camWeight[p];
+            float c[kNumLambda];
+            bool finite = true;
+#pragma unroll
+            for (int k = 0; k < kNumLambda; ++k) {
+                c[k] = ws.L[(size_t)k * ws.N + p] * w;
+                finite &= isfinite(c[k]);
+            }
+            if (!finite) { ++dropped; continue; }
+            float wlOff = ws.wlOffset[p];
+            float addend[kNumLambda];
+#pragma unroll
+            for (int b = 0; b < kNumLambda; ++b) addend[b] = 0.0f;
+#pragma unroll
+            for (int k = 0; k < kNumLambda; ++k) {
+                float lam = lambdaAt(k, wlOff);
+                float f = __fmul_rn(__fdiv_rn(__fsub_rn(lam, kWavelengthLow), kWavelengthHigh - kWavelengthLow), (float)kNumLambda);
+                uint32_t bin = min((uint32_t)f, (uint32_t)(kNumLambda - 1));
+#pragma unroll
+                for (int b = 0; b < kNumLambda; ++b)
+                    if (b == (int)bin) addend[b] += c[k] * recBinWidth;
+            }
+#pragma unroll
+            for (int b = 0; b < kNumLambda; ++b) {
+                float cin = __fsub_rn(addend[b], comp[b]);
+                float st = __fadd_rn(sum[b], cin);
+                comp[b] = __fsub_rn(__fsub_rn(st, sum[b]), cin);
+                sum[b] = st;
+            }
+        }
+#pragma unroll
+        for (int b = 0; b < kNumLambda; ++b) {
+            filmSum[(size_t)b * P + pix] = sum[b];
+            filmComp[(size_t)b * P + pix] = comp[b];
+        }
+    }
+    if (dropped) atomicAdd(&ws.stats[2], dropped);
+}
+
+// Film layout conversion [16][P] -> [P][16].
+__global__ void kFilmToPixelMajor(const float* __restrict__ src, float* __restrict__ dst, uint32_t P) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < P * kNumLambda; i += gridDim.x * blockDim.x) {
+        uint32_t pix = i / kNumLambda, b = i % kNumLambda;
+        dst[i] = src[(size_t)b * P + pix];
+    }
+}
+
+__global__ void kTrace(DevScene sc, const float* __restrict__ rays, uint32_t n, int anyHit, uint32_t* prim, float* t,
+                       float* b1, float* b2) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float4* r = reinterpret_cast<const float4*>(rays) + 2 * (size_t)i;
+        float4 o = r[0], d = r[1];
+        if (anyHit) {
+            prim[i] = traceAny(sc, V3{o.x, o.y, o.z}, V3{d.x, d.y, d.z}, o.w, d.w) ? 1u : 0u;
+        } else {
+            Hit h;
+            traceClosest(sc, V3{o.x, o.y, o.z}, V3{d.x, d.y, d.z}, o.w, d.w, &h);
+            prim[i] = h.prim;
+            if (t) t[i] = h.t;
+            if (b1) b1[i] = h.b1;
+            if (b2) b2[i] = h.b2;
+        }
+    }
+}
+
+// BSDF queries at fixed inputs (16 floats in, 40 out per query; the layout of
+// slrgpu_bsdf_query in include/slrgpu.h).
+__global__ void kBsdfQuery(Bsdf B, const float* __restrict__ q, uint32_t n, float* __restrict__ o) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float* qi = q + 16 * (size_t)i;
+        float* oi = o + 40 * (size_t)i;
+        BsdfQuery bq{V3{qi[0], qi[1], qi[2]}, V3{qi[3], qi[4], qi[5]}, (int)qi[6]};
+        BsdfSample bs;
+        Spec fs;
+        bsdfSample(B, bq, qi[8], qi[9], qi[10], &bs, fs);
+#pragma unroll
+        for (int k = 0; k < kNumLambda; ++k) oi[k] = bs.pdf == 0.0f ? 0.0f : fs.v[k];
+        oi[16] = bs.dir.x; oi[17] = bs.dir.y; oi[18] = bs.dir.z;
+        oi[19] = bs.pdf;
+        oi[20] = (float)bs.type;
+        V3 ed = V3{qi[11], qi[12], qi[13]};
+        Spec fe;
+        bsdfEval(B, bq, ed, fe);
+#pragma unroll
+        for (int k = 0; k < kNumLambda; ++k) oi[21 + k] = fe.v[k];
+        oi[37] = bsdfPdf(B, bq, ed);
+        oi[38] = 0.0f;
+        oi[39] = 0.0f;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Host side
+// ---------------------------------------------------------------------------
+namespace {
+// Each scene array gets a device allocation and a pinned host mirror; the
+// mirror is what slrgpu_scene_reupload copies from.
+template <typename T>
+int upload(DeviceBuffers &db, const std::vector<T> &v, const T** out) {
+    *out = nullptr;
+    if (v.empty()) return SLRGPU_OK;
+    const size_t bytes = v.size() * sizeof(T);
+    void* p = nullptr;
+    void* h = nullptr;
+    CUDA_TRY(cudaMalloc(&p, bytes));
+    db.allocs.push_back(p);
+    CUDA_TRY(cudaMallocHost(&h, bytes));
+    db.pinned.push_back(h);
+    db.sizes.push_back(bytes);
+    std::memcpy(h, v.data(), bytes);
+    CUDA_TRY(cudaMemcpy(p, h, bytes, cudaMemcpyHostToDevice));
+    *out = (const T*)p;
+    return SLRGPU_OK;
+}
+
+template <typename T>
+T* allocDev(std::vector<void*> &allocs, size_t n, cudaError_t* err) {
+    void* p = nullptr;
+    *err = cudaMalloc(&p, n * sizeof(T) + 16);
+    if (*err != cudaSuccess) return nullptr;
+    allocs.push_back(p);
+    return (T*)p;
+}
+}  // namespace
+
+void DeviceBuffers::release() {
+    for (void* p : allocs) cudaFree(p);
+    for (void* p : pinned) cudaFreeHost(p);
+    allocs.clear();
+    pinned.clear();
+    sizes.clear();
+}
+
+int reuploadScene(DeviceScene* ds, uint64_t* bytes, cudaStream_t stream) {
+    uint64_t total = 0;
+    for (size_t i = 0; i < ds->buffers.allocs.size(); ++i) {
+        CUDA_TRY(cudaMemcpyAsync(ds->buffers.allocs[i], ds->buffers.pinned[i], ds->buffers.sizes[i],
+                                 cudaMemcpyHostToDevice, stream));
+        total += ds->buffers.sizes[i];
+    }
+    if (bytes) *bytes = total;
+    return SLRGPU_OK;
+}
+
+int uploadScene(const HostScene &hs, const BuiltScene &bs, DeviceScene* ds) {
+    ds->buffers.release();
+    DevScene &sc = ds->sc;
+    std::memset(&sc, 0, sizeof(sc));
+    DeviceBuffers &db = ds->buffers;
+    int rc;
+#define UP(vec, field) if ((rc = upload(db, vec, &sc.field)) != SLRGPU_OK) return rc
+    UP(bs.wide.nodes, nodes);
+    UP(bs.wide.frags, frags);
+    UP(bs.prims, prims);
+    UP(bs.vpos, vpos);
+    UP(bs.vnrm, vnrm);
+    UP(bs.vtan, vtan);
+    UP(hs.materials, materials);
+    UP(hs.spectra, spectra);
+    UP(hs.specValues, specValues);
+    std::vector<float> ups(upsSpectra(), upsSpectra() + (size_t)upsNumPoints() * kUpsNumSamples);
+    UP(ups, upsSpectra);
+    UP(bs.lightPrims, lightPrims);
+    UP(bs.lightCDF, lightCDF);
+    UP(bs.lightPMF, lightPMF);
+    if (hs.envPresent) {
+        UP(bs.env.texels, envTexels);
+        UP(bs.env.rowPDF, envRowPDF);
+        UP(bs.env.rowCDF, envRowCDF);
+        UP(bs.env.topPDF, envTopPDF);
+        UP(bs.env.topCDF, envTopCDF);
+    }
+#undef UP
+    sc.numPrims = (uint32_t)bs.prims.size();
+    sc.numNodes = (uint32_t)bs.wide.nodes.size();
+    sc.numLights = (uint32_t)bs.lightPrims.size();
+    sc.surfImportance = (float)bs.lightPrims.size();
+    sc.envPresent = hs.envPresent ? 1u : 0u;
+    sc.envImportance = hs.envPresent ? 1.0f : 0.0f;
+    sc.envWidth = bs.env.width;
+    sc.envHeight = bs.env.height;
+    sc.envScale = bs.env.scale;
+    sc.envMapW = bs.env.mapW;
+    sc.envMapH = bs.env.mapH;
+    sc.worldRadius = bs.worldRadius;
+    sc.worldDiscArea = bs.worldDiscArea;
+    for (int k = 0; k < 3; ++k) sc.worldCenter[k] = bs.worldCenter[k];
+    sc.camera = bs.camera;
+    return SLRGPU_OK;
+}
+
+int RenderEngine::ensure(uint32_t N, uint32_t maxDepth) {
+    if (N <= capacity && maxDepth <= depthCapacity && ws) return SLRGPU_OK;
+    release();
+    cudaError_t e;
+    WaveState* w = new WaveState();
+    std::memset(w, 0, sizeof(*w));
+    w->N = N;
+    w->rayOrg = allocDev<float4>(allocs, N, &e); if (!w->rayOrg) goto fail;
+    w->rayDir = allocDev<float4>(allocs, N, &e); if (!w->rayDir) goto fail;
+    w->hit = allocDev<float4>(allocs, N, &e); if (!w->hit) goto fail;
+    w->alpha = allocDev<float>(allocs, (size_t)N * kNumLambda, &e); if (!w->alpha) goto fail;
+    w->L = allocDev<float>(allocs, (size_t)N * kNumLambda, &e); if (!w->L) goto fail;
+    w->info = allocDev<uint32_t>(allocs, N, &e); if (!w->info) goto fail;
+    w->wlOffset = allocDev<float>(allocs, N, &e); if (!w->wlOffset) goto fail;
+    w->prevPdf = allocDev<float>(allocs, N, &e); if (!w->prevPdf) goto fail;
+    w->initY = allocDev<float>(allocs, N, &e); if (!w->initY) goto fail;
+    w->camWeight = allocDev<float>(allocs, N, &e); if (!w->camWeight) goto fail;
+    w->rngCounter = allocDev<uint32_t>(allocs, N, &e); if (!w->rngCounter) goto fail;
+    w->shOrg = allocDev<float4>(allocs, N, &e); if (!w->shOrg) goto fail;
+    w->shDir = allocDev<float4>(allocs, N, &e); if (!w->shDir) goto fail;
+    w->shContrib = allocDev<float>(allocs, (size_t)N * kNumLambda, &e); if (!w->shContrib) goto fail;
+    w->queue[0] = allocDev<uint32_t>(allocs, N, &e); if (!w->queue[0]) goto fail;
+    w->queue[1] = allocDev<uint32_t>(allocs, N, &e); if (!w->queue[1]) goto fail;
+    w->shadowQueue = allocDev<uint32_t>(allocs, N, &e); if (!w->shadowQueue) goto fail;
+    w->counters = allocDev<uint32_t>(allocs, 3 * (size_t)(maxDepth + 2), &e); if (!w->counters) goto fail;
+    w->stats = allocDev<unsigned long long>(allocs, 4, &e); if (!w->stats) goto fail;
+    ws = w;
+    capacity = N;
+    depthCapacity = maxDepth;
+    return SLRGPU_OK;
+fail:
+    delete w;
+    release();
+    setError(std::string("path state allocation failed: ") + cudaGetErrorString(e));
+    return SLRGPU_ERR_OUT_OF_MEMORY;
+}
+
+void RenderEngine::release() {
+    for (void* p : allocs) cudaFree(p);
+    allocs.clear();
+    delete ws;
+    ws = nullptr;
+    capacity = 0;
+    depthCapacity = 0;
+    if (filmSum) { cudaFree(filmSum); filmSum = nullptr; }
+    if (filmComp) { cudaFree(filmComp); filmComp = nullptr; }
+    if (filmOut) { cudaFree(filmOut); filmOut = nullptr; }
+    filmPixels = 0;
+}
+
+static int gridFor(const void* kernel, int block) {
+    int dev = 0, sms = 0, perSM = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, kernel, block, 0);
+    return std::max(1, sms * std::max(1, perSM));
+}
+
+int RenderEngine::render(const DeviceScene &ds, const slrgpu_settings &s, float* film, bool filmOnDevice,
+                         slrgpu_render_stats* stats, cudaStream_t stream) {
+    auto t0 = std::chrono::steady_clock::now();
+    if (s.width == 0 || s.height == 0 || s.spp == 0) {
+        setError("width, height and spp must be positive");
+        return SLRGPU_ERR_INVALID_ARGUMENT;
+    }
+    if (s.max_depth > 1000) {
+        setError("max_depth must be <= 1000");
+        return SLRGPU_ERR_INVALID_ARGUMENT;
+    }
+    const uint32_t P = s.width * s.height;
+    uint32_t S = s.samples_per_wave;
+    if (S == 0) S = std::max(1u, std::min(s.spp, (uint32_t)((4u << 20) / std::max(1u, P))));
+    S = std::min(S, s.spp);
+    const uint64_t Nwant = (uint64_t)S * P;
+    if (Nwant > 0x7fffffffull) {
+        setError("paths per wave exceed 2^31");
+        return SLRGPU_ERR_INVALID_ARGUMENT;
+    }
+    int rc = ensure((uint32_t)Nwant, s.max_depth);
+    if (rc != SLRGPU_OK) return rc;
+    if (filmPixels < P) {
+        if (filmSum) cudaFree(filmSum);
+        if (filmComp) cudaFree(filmComp);
+        if (filmOut) cudaFree(filmOut);
+        filmSum = filmComp = filmOut = nullptr;
+        CUDA_TRY(cudaMalloc(&filmSum, (size_t)P * kNumLambda * sizeof(float)));
+        CUDA_TRY(cudaMalloc(&filmComp, (size_t)P * kNumLambda * sizeof(float)));
+        CUDA_TRY(cudaMalloc(&filmOut, (size_t)P * kNumLambda * sizeof(float)));
+        filmPixels = P;
+    }
+    WaveState w = *ws;
+    CUDA_TRY(cudaMemsetAsync(filmSum, 0, (size_t)P * kNumLambda * sizeof(float), stream));
+    CUDA_TRY(cudaMemsetAsync(filmComp, 0, (size_t)P * kNumLambda * sizeof(float), stream));
+    CUDA_TRY(cudaMemsetAsync(w.stats, 0, 4 * sizeof(unsigned long long), stream));
+    const int block = 256;
+    static int gRaygen = 0, gExtend = 0, gShade = 0, gShadow = 0, gAcc = 0;
+    if (!gRaygen) {
+        gRaygen = gridFor((const void*)kRaygen, block);
+        gExtend = gridFor((const void*)kExtend, block);
+        gShade = gridFor((const void*)kShade, block);
+        gShadow = gridFor((const void*)kShadow, block);
+        gAcc = gridFor((const void*)kAccumulate, block);
+    }
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, stream);
+    uint64_t launches = 0;
+    const uint32_t D = s.max_depth;
+    // Optional per-launch events for the per-kernel device times.
+    const bool profile = (s.flags & SLRGPU_FLAG_PROFILE_KERNELS) != 0;
+    struct Mark { int cls; size_t ev; };
+    std::vector<Mark> marks;
+    size_t evUsed = 0;
+    auto nextEvent = [&]() -> cudaEvent_t {
+        if (evUsed == eventPool.size()) {
+            cudaEvent_t e;
+            cudaEventCreate(&e);
+            eventPool.push_back(e);
+        }
+        return eventPool[evUsed++];
+    };
+    auto begin = [&](int cls) {
+        if (!profile) return;
+        marks.push_back(Mark{cls, evUsed});
+        cudaEventRecord(nextEvent(), stream);
+    };
+    auto end = [&]() {
+        if (!profile) return;
+        cudaEventRecord(nextEvent(), stream);
+    };
+    for (uint32_t base = 0; base < s.spp; base += S) {
+        WaveParams wp;
+        wp.width = s.width;
+        wp.height = s.height;
+        wp.numPixels = P;
+        wp.samplesInWave = std::min(S, s.spp - base);
+        wp.sampleBase = base;
+        wp.numPaths = wp.samplesInWave * P;
+        wp.maxDepth = D;
+        wp.seed = s.seed;
+        CUDA_TRY(cudaMemsetAsync(w.counters, 0, 3 * (size_t)(D + 2) * sizeof(uint32_t), stream));
+        begin(SLRGPU_KERNEL_RAYGEN);
+        kRaygen<<<gRaygen, block, 0, stream>>>(ds.sc, w, wp);
+        end();
+        ++launches;
+        for (uint32_t b = 0; b <= D; ++b) {
+            uint32_t* inCount = w.counters + b;
+            uint32_t* outCount = w.counters + b + 1;
+            uint32_t* shCount = w.counters + (D + 2) + b;
+            begin(SLRGPU_KERNEL_EXTEND);
+            kExtend<<<gExtend, block, 0, stream>>>(ds.sc, w, w.queue[b & 1], inCount);
+            end();
+            begin(SLRGPU_KERNEL_SHADE);
+            kShade<<<gShade, block, 0, stream>>>(ds.sc, w, wp, w.queue[b & 1], inCount, w.queue[(b + 1) & 1],
+                                                 outCount, w.shadowQueue, shCount);
+            end();
+            begin(SLRGPU_KERNEL_SHADOW);
+            kShadow<<<gShadow, block, 0, stream>>>(ds.sc, w, w.shadowQueue, shCount);
+            end();
+            launches += 3;
+        }
+        begin(SLRGPU_KERNEL_ACCUMULATE);
+        kAccumulate<<<gAcc, block, 0, stream>>>(w, wp, filmSum, filmComp);
+        end();
+        ++launches;
+    }
+    CUDA_TRY(cudaGetLastError());
+    float* dst = filmOnDevice ? film : filmOut;
+    kFilmToPixelMajor<<<gAcc, block, 0, stream>>>(filmSum, dst, P);
+    ++launches;
+    cudaEventRecord(e1, stream);
+    if (!filmOnDevice)
+        CUDA_TRY(cudaMemcpyAsync(film, filmOut, (size_t)P * kNumLambda * sizeof(float), cudaMemcpyDeviceToHost, stream));
+    unsigned long long hstats[4] = {0, 0, 0, 0};
+    CUDA_TRY(cudaMemcpyAsync(hstats, w.stats, sizeof(hstats), cudaMemcpyDeviceToHost, stream));
+    CUDA_TRY(cudaStreamSynchronize(stream));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (stats) {
+        std::memset(stats, 0, sizeof(*stats));
+        for (const Mark &m : marks) {
+            float kms = 0;
+            cudaEventElapsedTime(&kms, eventPool[m.ev], eventPool[m.ev + 1]);
+            stats->kernel_ms[m.cls] += kms;
+            stats->kernel_count[m.cls] += 1;
+        }
+        stats->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        stats->kernel_seconds = ms * 1e-3;
+        stats->path_samples = (uint64_t)P * s.spp;
+        stats->extension_rays = hstats[0];
+        stats->shadow_rays = hstats[1];
+        stats->dropped_samples = hstats[2];
+        stats->kernel_launches = launches;
+    }
+    return SLRGPU_OK;
+}
+
+int bsdfQuery(int kind, const float* s0, const float* s1, const float* s2, float ax, float ay, const float* queries,
+              uint32_t n, float* out) {
+    Bsdf B;
+    std::memset(&B, 0, sizeof(B));
+    static const uint32_t kinds[5] = {kMatMatte, kMatSpecularReflection, kMatSpecularScattering, kMatGGXReflection,
+                                      kMatGGXScattering};
+    if (kind < 0 || kind > 4) {
+        setError("unknown BSDF kind");
+        return SLRGPU_ERR_INVALID_ARGUMENT;
+    }
+    B.kind = kinds[kind];
+    for (int i = 0; i < kNumLambda; ++i) {
+        B.a.v[i] = s0[i];
+        B.b.v[i] = s1 ? s1[i] : s0[i];
+        B.c.v[i] = s2 ? s2[i] : s0[i];
+    }
+    B.ax = ax;
+    B.ay = ay;
+    B.dispersive = true;
+    if (n == 0) return SLRGPU_OK;
+    float *dq = nullptr, *dout = nullptr;
+    CUDA_TRY(cudaMalloc(&dq, (size_t)n * 16 * sizeof(float)));
+    cudaError_t e = cudaMalloc(&dout, (size_t)n * 40 * sizeof(float));
+    if (e != cudaSuccess) { cudaFree(dq); setError(cudaGetErrorString(e)); return SLRGPU_ERR_CUDA; }
+    e = cudaMemcpy(dq, queries, (size_t)n * 16 * sizeof(float), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        kBsdfQuery<<<std::min<uint32_t>((n + 255) / 256, 4096), 256>>>(B, dq, n, dout);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(out, dout, (size_t)n * 40 * sizeof(float), cudaMemcpyDeviceToHost);
+    cudaFree(dq);
+    cudaFree(dout);
+    if (e != cudaSuccess) { setError(cudaGetErrorString(e)); return SLRGPU_ERR_CUDA; }
+    return SLRGPU_OK;
+}
+
+int traceRays(const DeviceScene &ds, const float* rays, uint32_t n, int anyHit, uint32_t* prim, float* t, float* b1,
+              float* b2, cudaStream_t stream) {
+    if (n == 0) return SLRGPU_OK;
+    static int grid = 0;
+    if (!grid) grid = gridFor((const void*)kTrace, 256);
+    kTrace<<<grid, 256, 0, stream>>>(ds.sc, rays, n, anyHit, prim, t, b1, b2);
+    CUDA_TRY(cudaGetLastError());
+    return SLRGPU_OK;
+}
+
+}  // namespace slrgpu

@@ -1,0 +1,57 @@
+// Internal interface between the C ABI (capi.cpp) and the CUDA side (render.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/slrgpu.h"
+#include "scene_host.h"
+#include "slrgpu_types.h"
+
+namespace slrgpu {
+
+void setError(const std::string &msg);
+
+struct DeviceBuffers {
+    std::vector<void*> allocs;   // device arrays
+    std::vector<void*> pinned;   // pinned host mirrors of the same arrays
+    std::vector<size_t> sizes;
+    void release();
+    ~DeviceBuffers() { release(); }
+};
+
+struct DeviceScene {
+    DevScene sc;
+    DeviceBuffers buffers;
+};
+
+struct WaveState;
+
+// Per-context path state and film buffers, grown on demand.
+struct RenderEngine {
+    WaveState* ws = nullptr;
+    std::vector<void*> allocs;
+    uint32_t capacity = 0;
+    uint32_t depthCapacity = 0;
+    float* filmSum = nullptr;
+    float* filmComp = nullptr;
+    float* filmOut = nullptr;
+    uint32_t filmPixels = 0;
+    std::vector<cudaEvent_t> eventPool;
+
+    int ensure(uint32_t paths, uint32_t maxDepth);
+    void release();
+    int render(const DeviceScene &ds, const slrgpu_settings &s, float* film, bool filmOnDevice,
+               slrgpu_render_stats* stats, cudaStream_t stream);
+    ~RenderEngine() { release(); }
+};
+
+int uploadScene(const HostScene &hs, const BuiltScene &bs, DeviceScene* ds);
+int reuploadScene(DeviceScene* ds, uint64_t* bytes, cudaStream_t stream);
+int bsdfQuery(int kind, const float* s0, const float* s1, const float* s2, float ax, float ay, const float* queries,
+              uint32_t n, float* out);
+int traceRays(const DeviceScene &ds, const float* rays, uint32_t n, int anyHit, uint32_t* prim, float* t, float* b1,
+              float* b2, cudaStream_t stream);
+
+}  // namespace slrgpu

@@ -1,0 +1,43 @@
+"""C ABI: the library loads without a GPU, exports every declared symbol and
+rejects bad arguments with error codes (no compute calls)."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+
+def test_exports_every_header_symbol(gpu_lib):
+    L = gpu_lib.lib()
+    syms = gpu_lib.header_symbols()
+    assert len(syms) >= 25
+    missing = [s for s in syms if not hasattr(L, s)]
+    assert not missing, missing
+
+
+def test_invalid_handles_and_arguments(gpu_lib):
+    L = gpu_lib.lib()
+    assert L.slrgpu_scene_destroy(12345) == -2
+    assert b"invalid" in L.slrgpu_last_error()
+    h = C.c_uint64()
+    assert L.slrgpu_scene_create(0, C.byref(h)) == 0
+    out = C.c_int()
+    assert L.slrgpu_material_matte(h.value, 3, C.byref(out)) == -1          # no such spectrum
+    assert L.slrgpu_spectrum_rgb(h.value, 7, 1, 1, 1, C.byref(out)) == -1   # bad spectrum type
+    assert L.slrgpu_spectrum_rgb(h.value, 0, 0.5, 0.5, 0.5, C.byref(out)) == 0
+    assert L.slrgpu_material_matte(h.value, out.value, C.byref(out)) == 0
+    p = np.zeros((3, 3), np.float32)
+    idx = np.array([[0, 1, 5]], np.uint32)                                 # index out of range
+    fp = p.ctypes.data_as(C.POINTER(C.c_float))
+    assert L.slrgpu_scene_add_mesh(h.value, fp, fp, fp, None, 3, idx.ctypes.data_as(C.POINTER(C.c_uint32)), 1,
+                                   0) == -1
+    # rendering an uncommitted scene is refused before any device work
+    st = gpu_lib.Settings(8, 8, 1, 1, 0, 0, 0, 0)
+    film = np.zeros(8 * 8 * 16, np.float32)
+    assert L.slrgpu_render(h.value, C.byref(st), C.c_void_p(film.ctypes.data), 0, None) == -5
+    assert L.slrgpu_scene_destroy(h.value) == 0
+
+
+def test_host_build_of_empty_scene(gpu_lib):
+    from slr_gb300.scene_desc import SceneDesc
+    s = gpu_lib.Scene(SceneDesc(), host_only=True)
+    assert s.bvh_stats.num_triangles == 0

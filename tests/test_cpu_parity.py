@@ -1,0 +1,80 @@
+"""Host-side parity with the reference (no GPU): the SBVH build, RGB spectral
+upsampling, sampled spectra and the environment importance tables must be
+bit-identical to the reference's on the same inputs; the numpy restatement of
+the triangle test is pinned against the reference accelerator."""
+import numpy as np
+import pytest
+
+from slr_gb300 import scenes
+from slr_gb300.scene_desc import LIGHT_SOURCE, REFLECTANCE, SceneDesc
+from tests import helpers
+
+
+def _sbvh_equal(gpu_lib, oracle_lib, desc):
+    g = gpu_lib.Scene(desc, host_only=True)
+    r = oracle_lib.RefScene(desc, build=False)
+    rs = r.sbvh_stats()
+    st = g.bvh_stats
+    assert (st.num_fragments, st.depth, st.num_binary_nodes) == (rs["fragments"], rs["depth"], rs["nodes"])
+    assert np.float32(st.sah_cost) == np.float32(rs["cost"])
+    gb, gw, gl = g.sbvh_dump()
+    rb, rw, rl = r.sbvh_dump()
+    np.testing.assert_array_equal(gb.view(np.uint32), rb.view(np.uint32))
+    np.testing.assert_array_equal(gw, rw)
+    np.testing.assert_array_equal(gl, rl)
+    return st
+
+
+def test_sbvh_box_scene(gpu_lib, oracle_lib):
+    _sbvh_equal(gpu_lib, oracle_lib, scenes.box_scene())
+
+
+@pytest.mark.parametrize("n,seed", [(1, 0), (2, 1), (500, 2), (4000, 3)])
+def test_sbvh_triangle_soup(gpu_lib, oracle_lib, n, seed):
+    st = _sbvh_equal(gpu_lib, oracle_lib, helpers.triangle_soup(n, seed))
+    if n >= 500:
+        assert st.num_fragments > n  # spatial splits were exercised
+
+
+def test_sbvh_heightfield(gpu_lib, oracle_lib):
+    d = scenes.heightfield_scene(grid=48, spheres=4, sphere_freq=4, env_size=(16, 8))
+    _sbvh_equal(gpu_lib, oracle_lib, d)
+
+
+def test_upsampled_and_tabulated_spectra(gpu_lib, oracle_lib):
+    # RGB spectra of type IndexOfRefraction are not compared: the reference's
+    # constructor (spectrum_types.cpp:482-520) converts only Reflectance and
+    # LightSource colours and leaves XYZ uninitialised otherwise.
+    rng = np.random.default_rng(5)
+    d = SceneDesc()
+    for k in range(60):
+        d.spectrum_rgb([REFLECTANCE, LIGHT_SOURCE][k % 2], *rng.random(3) * (1 + 20 * (k % 2 == 1)))
+    d.spectrum_rgb(REFLECTANCE, 0, 0, 0)
+    d.spectrum_rgb(LIGHT_SOURCE, 1, 0, 0)
+    d.spectrum_rgb(REFLECTANCE, 0, 0, 1)
+    d.spectrum_regular(rng.random(95) + 0.5, 360, 830)
+    d.spectrum_regular(rng.random(7) + 1.0, 400, 700)
+    wl = np.sort(rng.uniform(350, 850, 12)).astype(np.float32)
+    d.spectrum_irregular(wl, rng.random(12))
+    d.material("matte", (0,))
+    g = gpu_lib.Scene(d, host_only=True)
+    r = oracle_lib.RefScene(d, build=False)
+    offs = rng.random(200).astype(np.float32)
+    lam = (360.0 + 470.0 * (np.arange(16)[None, :] + offs[:, None]) / 16).astype(np.float32)
+    lam = np.concatenate([lam, rng.uniform(300, 900, (50, 16)).astype(np.float32)])
+    for i in range(len(d.spectra)):
+        a = g.spectrum_evaluate(i, lam)
+        b = r.spectrum_eval(i, lam)
+        np.testing.assert_array_equal(a.view(np.uint32), b.view(np.uint32), err_msg=f"spectrum {i}")
+
+
+def test_restated_triangle_test_pinned(oracle_lib):
+    d = helpers.triangle_soup(300, 9)
+    rays = helpers.random_rays(d, 3000, seed=4)
+    ref = oracle_lib.RefScene(d, build=False)
+    rp, rt, _, _ = ref.trace(rays)
+    from oracle.restate import brute_force_closest
+    bp, bt = brute_force_closest(d.triangle_arrays(), rays)
+    np.testing.assert_array_equal(bt.view(np.uint32), rt.view(np.uint32))
+    res = helpers.compare_hits(d, rays, bp, bt, rp, rt)
+    assert res["mismatch"] == 0, res
