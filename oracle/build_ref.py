@@ -43,6 +43,10 @@ Build-only patches (all applied to the copy):
   counter, ``Core/ProgressReporter.cpp:74-81,101-104``), and the progressive
   ``saveImage`` calls inside the render loops (``PTRenderer.cpp:84``,
   ``VolumetricPTRenderer.cpp:84``) are disabled so rendering writes no BMPs.
+* P8 the message printed for each dropped non-finite sample
+  (``PTRenderer.cpp:138``, ``VolumetricPTRenderer.cpp:138``) is replaced by an
+  increment of a counter the driver reports; which samples are dropped does
+  not change.
 """
 from __future__ import annotations
 
@@ -127,11 +131,15 @@ def copy_and_patch(ref_root: Path) -> None:
     # P4
     for rel in ("Core/surface_object.cpp", "Core/medium_object.cpp"):
         patch(rel, lambda t: _replace_once(t, '#include "../Accelerator/QBVH.h"', "", "P4 QBVH include"))
-    # P6 + P7 (saveImage)
-    decl = "extern \"C\" unsigned int slr_oracle_max_depth;\n"
+    # P6 + P7 (saveImage) + P8 (count dropped samples instead of printing them)
+    decl = ("extern \"C\" unsigned int slr_oracle_max_depth;\n"
+            "#include <atomic>\nextern std::atomic<unsigned long long> slr_oracle_dropped_samples;\n")
+    drop_print = 'slrDevPrintf("Unexpected value detected: %s at (%f, %f)\\n", C.toString().c_str(), p.x, p.y);'
+    drop_count = "slr_oracle_dropped_samples.fetch_add(1);"
     def p6_pt(t: str) -> str:
         t = _replace_once(t, "if (pathLength >= 100)", "if (pathLength > slr_oracle_max_depth)", "P6 PT")
         t = _replace_once(t, "sensor->saveImage(filename,", "if (0) sensor->saveImage(filename,", "P7 PT")
+        t = _replace_once(t, drop_print, drop_count, "P8 PT")
         return t.replace("namespace SLR {", decl + "namespace SLR {", 1)
     patch("Renderer/PTRenderer.cpp", p6_pt)
     def p6_vpt(t: str) -> str:
@@ -139,11 +147,12 @@ def copy_and_patch(ref_root: Path) -> None:
                           "            ++pathLength;\n            if (pathLength > slr_oracle_max_depth)\n                break;\n",
                           "P6 VolPT")
         t = _replace_once(t, "sensor->saveImage(filename,", "if (0) sensor->saveImage(filename,", "P7 VolPT")
+        t = _replace_once(t, drop_print, drop_count, "P8 VolPT")
         return t.replace("namespace SLR {", decl + "namespace SLR {", 1)
     patch("Renderer/VolumetricPTRenderer.cpp", p6_vpt)
     # P7: the stock reporter is replaced by oracle/progress_reporter_noop.cpp
     (SRC_COPY / "Core" / "ProgressReporter.cpp").unlink()
-    (REF_OUT / "src" / "PATCHED").write_text("P1 P2 P3 P4 P5 P6 P7\n")
+    (REF_OUT / "src" / "PATCHED").write_text("P1 P2 P3 P4 P5 P6 P7 P8\n")
 
 
 def _compile(cmd: list[str]) -> tuple[list[str], int, str]:

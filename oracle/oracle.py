@@ -45,6 +45,7 @@ def lib():
             "ora_mesh": (I, [P, fp, fp, fp, fp, I, up, I, I]),
             "ora_env_ibl": (I, [P, hp, I, I, F]),
             "ora_camera_perspective": (I, [P, fp, F, F, F, F, F, F]),
+            "ora_medium_density_grid": (I, [P, fp, fp, I, I, fp, I, I, I, F]),
             "ora_camera_equirect": (I, [P, fp, F, F, F]),
             "ora_build": (I, [P]),
             "ora_render": (I, [P, I, I, I, I, I, I, I, fp, dp]),
@@ -53,6 +54,7 @@ def lib():
             "ora_trace": (I, [P, fp, I, I, I, up, fp, fp, fp]),
             "ora_bsdf_query": (I, [I, fp, fp, fp, F, F, fp, I, fp]),
             "ora_spectrum_eval": (I, [P, I, fp, I, fp]),
+            "ora_dropped_samples": (C.c_ulonglong, []),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -128,6 +130,15 @@ class RefScene:
             keep.append(img)
             L.ora_env_ibl(self.h, img.ctypes.data_as(C.POINTER(C.c_uint16)), img.shape[1], img.shape[0],
                           desc.environment.scale)
+        if desc.medium is not None:
+            md = desc.medium
+            bmin, bminp = _f(md.bounds_min)
+            bmax, bmaxp = _f(md.bounds_max)
+            dens, densp = _f(md.density)
+            keep += [bmin, bmax, dens]
+            nz, ny, nx = dens.shape
+            L.ora_medium_density_grid(self.h, bminp, bmaxp, sp_ids[md.sigma_s], sp_ids[md.sigma_e], densp, nx, ny, nz,
+                                      md.hg_g)
         cam = desc.camera
         if cam is not None:
             m, mp = _f(cam.cam_to_world)
@@ -155,6 +166,7 @@ class RefScene:
                               film.ctypes.data_as(C.POINTER(C.c_float)), C.byref(sec))
         if rc != 0:
             raise RuntimeError("oracle render failed")
+        self.last_dropped = int(lib().ora_dropped_samples())
         return film, sec.value
 
     def sbvh_stats(self):

@@ -58,8 +58,11 @@
 #include "BSDF/microfacet_bsdfs.h"
 #include "Renderer/PTRenderer.h"
 #include "Renderer/VolumetricPTRenderer.h"
+#include "MediumMaterial/basic_medium_materials.h"
+#include "Core/medium_material.h"
 
 extern "C" unsigned int slr_oracle_max_depth = 100;
+std::atomic<unsigned long long> slr_oracle_dropped_samples(0);
 
 namespace SLR {
     // Reads the private node arrays of a built SBVH through SBVH's friend
@@ -95,6 +98,8 @@ namespace {
         const SpectrumTexture* envTex = nullptr;
         float envScale = 1.0f;
         std::vector<std::unique_ptr<MediumNode>> mediumNodes;
+        std::vector<std::unique_ptr<MediumMaterial>> mediumMaterials;
+        std::vector<std::vector<float>> densitySlices;   // must outlive the medium node
         std::unique_ptr<Scene> scene;
         bool built = false;
         // Standalone SBVH over the same surface objects, for ray queries.
@@ -247,6 +252,24 @@ int ora_env_ibl(void* p, const uint16_t* rgbaHalf, int w, int h, float scale) {
     return 0;
 }
 
+// Density-grid medium over [bmin, bmax] with a Henyey-Greenstein phase
+// function (Scene/medium_nodes.h:33-48, MediumMaterial/basic_medium_materials.h:25-32);
+// density is [nz][ny][nx].
+int ora_medium_density_grid(void* p, const float* bmin, const float* bmax, int sigmaS, int sigmaE,
+                            const float* density, int nx, int ny, int nz, float g) {
+    OraScene* s = (OraScene*)p;
+    s->densitySlices.assign(nz, std::vector<float>());
+    for (int z = 0; z < nz; ++z)
+        s->densitySlices[z].assign(density + (size_t)z * nx * ny, density + (size_t)(z + 1) * nx * ny);
+    s->mediumMaterials.emplace_back(new HenyeyGreensteinScatteringMediumMaterial(floatTex(s, g)));
+    BoundingBox3D region(Point3D(bmin[0], bmin[1], bmin[2]), Point3D(bmax[0], bmax[1], bmax[2]));
+    DensityGridMediumNode* node = new DensityGridMediumNode(region, s->spectra.at(sigmaS).get(), s->spectra.at(sigmaE).get(),
+                                                            s->densitySlices, nx, ny, nz, s->mediumMaterials.back().get());
+    s->mediumNodes.emplace_back(node);
+    s->root->addChildNode(node);
+    return 0;
+}
+
 // m: row-major 4x4 camera-to-world matrix.
 int ora_camera_perspective(void* p, const float* m, float sensitivity, float aspect, float fovY,
                            float lensRadius, float imgPDist, float objPDist) {
@@ -305,6 +328,7 @@ int ora_render(void* p, int volumetric, int spp, int maxDepth, int w, int h, int
     settings.addItem(RenderSettingItem::Brightness, 1.0f);
     settings.addItem(RenderSettingItem::RNGSeed, (int32_t)seed);
     std::unique_ptr<Renderer> r;
+    slr_oracle_dropped_samples.store(0);
     if (volumetric) r.reset(new VolumetricPTRenderer(spp));
     else r.reset(new PTRenderer(spp));
     auto t0 = std::chrono::steady_clock::now();
@@ -322,6 +346,9 @@ int ora_render(void* p, int volumetric, int spp, int maxDepth, int w, int h, int
     }
     return 0;
 }
+
+// Non-finite samples dropped by the last ora_render call.
+unsigned long long ora_dropped_samples() { return slr_oracle_dropped_samples.load(); }
 
 // Builds a standalone SBVH over the scene's triangles, in the same object
 // order as Scene::build (node order, then triangle order), and reports the

@@ -15,6 +15,7 @@
 #include <cstring>
 
 #include "device_bsdf.cuh"
+#include "device_medium.cuh"
 #include "device_trace.cuh"
 
 namespace slrgpu {
@@ -128,9 +129,11 @@ __device__ __forceinline__ void cameraRay(const DevCamera &c, float lu0, float l
         sincosf(phi, &sp, &cp);
         sincosf(theta, &st, &ct);
         V3 dl = V3{-sp * st, ct, cp * st};
-        float dirPDF = 1.0f / (c.phiAngle * c.thetaAngle * st);
+        float sinTheta = sqrtf(1.0f - dl.y * dl.y);
+        float dirPDF = 1.0f / (c.phiAngle * c.thetaAngle * sinTheta);
         *dir = fr.fromLocal(dl);
-        *weight = 1.0f / dirPDF;
+        // We0 We1 |cos| / (areaPDF dirPDF) with areaPDF = 1 (EquirectangularCamera.cpp:25-69).
+        *weight = absDot(*dir, ez) / dirPDF;
     }
 }
 
@@ -549,6 +552,372 @@ __global__ void __launch_bounds__(256) kShade(DevScene sc, WaveState ws, WavePar
     }
 }
 
+// ---------------------------------------------------------------------------
+// Volumetric path tracing (VolumetricPTRenderer::Job::contribution,
+// libSLR/Renderer/VolumetricPTRenderer.cpp:146-296)
+// ---------------------------------------------------------------------------
+// Scene::selectLight (Scene.cpp:157-188) with sampleDiscrete
+// (distributions.cpp:16-36) over {surfaces, media, environment}.  Returns 0
+// surface (light index in *li), 2 environment; *prob = selection probability.
+__device__ __forceinline__ int selectLight3(const DevScene &sc, float u, int* li, float* prob) {
+    float imps[3] = {sc.surfImportance, sc.medium.importance, sc.envImportance};
+    // compensated sums as in the reference
+    float sum = 0.0f, c = 0.0f;
+    for (int i = 0; i < 3; ++i) {
+        float y = imps[i] - c, t = sum + y;
+        c = (t - sum) - y;
+        sum = t;
+    }
+    float su = u * sum;
+    float cum = 0.0f, cc = 0.0f, base = 0.0f;
+    int idx = 0;
+    float prob1st = imps[0] / sum, remapped = u;
+    bool found = false;
+    for (int i = 0; i < 3; ++i) {
+        base = cum;
+        float y = imps[i] - cc, t = cum + y;
+        cc = (t - cum) - y;
+        cum = t;
+        if (!found && su < cum) {
+            idx = i;
+            prob1st = imps[i] / sum;
+            remapped = (su - base) / imps[i];
+            found = true;
+        }
+    }
+    if (idx == 0) {
+        int n = (int)sc.numLights;
+        int j = n;
+        for (int d = (int)prevPow2(sc.numLights); d > 0; d >>= 1)
+            if (j - d > 0 && sc.lightCDF[j - d] >= remapped) j -= d;
+        --j;
+        *li = j;
+        *prob = sc.lightPMF[j] * prob1st;
+    } else {
+        *li = -1;
+        *prob = 1.0f * prob1st;
+    }
+    return idx;
+}
+
+__global__ void __launch_bounds__(256) kShadeVol(DevScene sc, WaveState ws, WaveParams wp,
+                                                 const uint32_t* __restrict__ inQueue,
+                                                 const uint32_t* __restrict__ inCount, uint32_t* outQueue,
+                                                 uint32_t* outCount, uint32_t* shQueue, uint32_t* shCount) {
+    const uint32_t n = *inCount;
+    const uint32_t N = ws.N;
+    const float inf = __int_as_float(0x7f800000);
+    const float twoPi = 6.28318530717958647692f;
+    const DevMedium &med = sc.medium;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+        const uint32_t i = base + threadIdx.x;
+        bool active = i < n;
+        bool extend = false, shadow = false;
+        uint32_t p = active ? inQueue[i] : 0;
+        if (active) {
+            uint32_t info = ws.info[p];
+            const int sel = (int)(info & kInfoSelMask);
+            bool wlSelected = (info & kInfoWlSelected) != 0;
+            const bool prevDelta = (info & kInfoPrevDelta) != 0;
+            uint32_t depth = info >> kInfoDepthShift;
+            const float wlOff = ws.wlOffset[p];
+            float lambdas[kNumLambda];
+#pragma unroll
+            for (int k = 0; k < kNumLambda; ++k) lambdas[k] = lambdaAt(k, wlOff);
+            Rng rng{pathKey(wp.seed, sampleIndexOf(wp, p)), ws.rngCounter[p]};
+            float4 ro = ws.rayOrg[p], rd = ws.rayDir[p];
+            V3 org = V3{ro.x, ro.y, ro.z}, dir = V3{rd.x, rd.y, rd.z};
+            float4 hv = ws.hit[p];
+            uint32_t prim = __float_as_uint(hv.w);
+            Spec alpha;
+            loadSpec(ws.alpha, N, p, alpha);
+            bool alive = true;
+
+            // Scene::interact (Scene.cpp:66-94): surface hit, then a medium
+            // collision before it.
+            float tSurf = prim == kNoHit ? inf : hv.x;
+            bool medHit = false;
+            float tMed = 0.0f;
+            V3 mparam = V3{0, 0, 0};
+            Spec sigmaE;
+            if (med.present) {
+                evalSpectrum(sc, med.sigmaE, lambdas, sigmaE);
+                Spec thr;
+                medHit = mediumInteract(med, org, dir, ro.w, tSurf, sigmaE, sel, wlSelected, rng, &tMed, &mparam, thr);
+#pragma unroll
+                for (int k = 0; k < kNumLambda; ++k) alpha.v[k] *= thr.v[k];
+            }
+            // Interaction point.
+            V3 P;
+            Frame frame;
+            V3 gn = V3{0, 0, 1};
+            DevMaterial mat;
+            mat.kind = kMatNull;
+            mat.emit = -1;
+            bool isMedium = false, atInf = false;
+            float hitInvArea = 0.0f;
+            if (medHit) {
+                isMedium = true;
+                P = org + tMed * dir;
+                frame = frameFromZ(normalize(dir));
+                float dens = mediumDensity(med, mparam);
+#pragma unroll
+                for (int k = 0; k < kNumLambda; ++k) alpha.v[k] *= dens * sigmaE.v[k];
+            } else if (prim != kNoHit) {
+                const DevPrim pr = sc.prims[prim];
+                SurfPoint sp;
+                surfacePoint(sc, pr, org, dir, hv.x, hv.y, hv.z, sp);
+                P = sp.p;
+                frame = sp.frame;
+                gn = sp.gn;
+                mat = sc.materials[pr.material];
+                hitInvArea = pr.invArea;
+            } else if (sc.envPresent) {
+                atInf = true;
+            } else {
+                alive = false;
+            }
+            if (alive) {
+                // Emission (VolumetricPTRenderer.cpp:175-180, :262-278).  The
+                // light probability of a surface or environment hit is the one
+                // the surface query set (Scene::interact stores the share of
+                // surfaces / environment on the medium interaction instead).
+                Spec Le;
+                bool emitting = false;
+                float lightPdf = 0.0f;
+                if (atInf) {
+                    float theta, phi;
+                    toPolarYUp(dir, &theta, &phi);
+                    envRadiance(sc, phi / twoPi, theta / kPiF, lambdas, Le);
+                    emitting = true;
+                    if (depth > 0) lightPdf = 1.0f * envAreaPdf(sc, phi, theta) * 1.0f / absDot(dir, -dir);
+                } else if (!isMedium && mat.emit >= 0) {
+                    Spec M;
+                    evalSpectrum(sc, mat.emit, lambdas, M);
+                    V3 dirOut = frame.toLocal(-dir);
+                    float edf = dirOut.z > 0.0f ? kInvPiF : 0.0f;
+#pragma unroll
+                    for (int k = 0; k < kNumLambda; ++k) Le.v[k] = M.v[k] * edf;
+                    emitting = true;
+                    if (depth > 0) {
+                        float dist2 = sqLength(P - org);
+                        lightPdf = sc.lightPMF[0] * hitInvArea * dist2 / absDot(dir, gn);
+                    }
+                }
+                if (emitting) {
+                    float mis = 1.0f;
+                    if (depth > 0 && !prevDelta) {
+                        float bp = ws.prevPdf[p];
+                        mis = (bp * bp) / (lightPdf * lightPdf + bp * bp);
+                    }
+                    Spec add;
+#pragma unroll
+                    for (int k = 0; k < kNumLambda; ++k) add.v[k] = alpha.v[k] * Le.v[k] * mis;
+                    addSpec(ws.L, N, p, add);
+                }
+                if (atInf) alive = false;
+            }
+            if (alive && depth > 0) {
+                float cp = fminf(importance(alpha, sel) / ws.initY[p], 1.0f);
+                if (rng.next() < cp) {
+                    float r = 1.0f / cp;
+#pragma unroll
+                    for (int k = 0; k < kNumLambda; ++k) alpha.v[k] *= r;
+                } else {
+                    alive = false;
+                }
+            }
+            if (alive) {
+                ++depth;
+                if (depth > wp.maxDepth) alive = false;
+            }
+            if (alive) {
+                V3 dirOut = frame.toLocal(-dir);
+                Bsdf B;
+                Spec albedo;
+                if (isMedium) {
+                    B.kind = kMatNull;
+                    bool in = !outsideUnit(mparam);
+                    Spec sigmaS;
+                    evalSpectrum(sc, med.sigmaS, lambdas, sigmaS);
+#pragma unroll
+                    for (int k = 0; k < kNumLambda; ++k)
+                        albedo.v[k] = (in && sigmaE.v[k] > 0) ? sigmaS.v[k] / sigmaE.v[k] : 0.0f;
+                } else {
+                    makeBsdf(sc, mat, lambdas, wlSelected, B);
+                }
+                BsdfQuery q{dirOut, frame.toLocal(gn), sel};
+                const bool nonDelta = isMedium || bsdfHasNonDelta(B.kind);
+                if (nonDelta && (sc.numLights > 0 || sc.envPresent)) {
+                    int li;
+                    float lightProb;
+                    int kind = selectLight3(sc, rng.next(), &li, &lightProb);
+                    float lu0 = rng.next(), lu1 = rng.next();
+                    V3 lp, lgn;
+                    Spec M;
+                    float areaPdf, edfVal, dist2;
+                    bool lAtInf = false;
+                    V3 shadowDir;
+                    if (kind == 0) {
+                        const DevPrim lpr = sc.prims[sc.lightPrims[li]];
+                        float su = sqrtf(lu0);
+                        float b0 = 1.0f - su, b1 = lu1 * su, b2 = 1.0f - b0 - b1;
+                        float4 p0 = sc.vpos[lpr.v0], p1 = sc.vpos[lpr.v1], p2 = sc.vpos[lpr.v2];
+                        lp = b0 * V3{p0.x, p0.y, p0.z} + b1 * V3{p1.x, p1.y, p1.z} + b2 * V3{p2.x, p2.y, p2.z};
+                        float4 n0 = sc.vnrm[lpr.v0], n1 = sc.vnrm[lpr.v1], n2 = sc.vnrm[lpr.v2];
+                        V3 lz = normalize(b0 * V3{n0.x, n0.y, n0.z} + b1 * V3{n1.x, n1.y, n1.z} + b2 * V3{n2.x, n2.y, n2.z});
+                        lgn = V3{lpr.ngx, lpr.ngy, lpr.ngz};
+                        areaPdf = lpr.invArea;
+                        evalSpectrum(sc, sc.materials[lpr.material].emit, lambdas, M);
+                        V3 diff = lp - P;
+                        dist2 = sqLength(diff);
+                        shadowDir = diff * (1.0f / sqrtf(dist2));
+                        edfVal = dot(lz, -shadowDir) > 0.0f ? kInvPiF : 0.0f;
+                    } else {
+                        float uvPdf, topPdf;
+                        float d1 = sample1D(sc.envTopPDF, sc.envTopCDF, sc.envMapH, lu1, &topPdf);
+                        uint32_t row = min((uint32_t)(sc.envMapH * d1), sc.envMapH - 1);
+                        float d0 = sample1D(sc.envRowPDF + (size_t)row * sc.envMapW,
+                                            sc.envRowCDF + (size_t)row * (sc.envMapW + 1), sc.envMapW, lu0, &uvPdf);
+                        uvPdf *= topPdf;
+                        float phi = d0 * twoPi, theta = d1 * kPiF;
+                        float sph, cph, sth, cth;
+                        sincosf(phi, &sph, &cph);
+                        sincosf(theta, &sth, &cth);
+                        lp = V3{-sph * sth, cth, cph * sth};
+                        lgn = -lp;
+                        lAtInf = true;
+                        areaPdf = uvPdf / (2.0f * kPiF * kPiF * sth);
+                        envRadiance(sc, phi / twoPi, theta / kPiF, lambdas, M);
+                        edfVal = 1.0f;
+                        shadowDir = normalize(lp);
+                        dist2 = 1.0f;
+                    }
+                    float cosLight = absDot(-shadowDir, lgn);
+                    float cosInter = isMedium ? 1.0f : absDot(shadowDir, gn);
+                    float lightPdf = lightProb * areaPdf;
+                    V3 sdl = frame.toLocal(shadowDir);
+                    Spec fv;
+                    float apdf;
+                    if (isMedium) {
+                        float ph = hgValue(med.g, sdl.z);
+#pragma unroll
+                        for (int k = 0; k < kNumLambda; ++k) fv.v[k] = albedo.v[k] * ph;
+                        apdf = ph;
+                    } else {
+                        bsdfEval(B, q, sdl, fv);
+                        apdf = bsdfPdf(B, q, sdl);
+                    }
+                    float abdfPdf = apdf * cosLight / dist2;
+                    float mis = 1.0f;
+                    if (!isinf(areaPdf)) mis = (lightPdf * lightPdf) / (lightPdf * lightPdf + abdfPdf * abdfPdf);
+                    float G = cosInter * cosLight / dist2;
+                    float scale = G * mis / lightPdf;
+                    Spec c;
+                    bool nz = false;
+#pragma unroll
+                    for (int k = 0; k < kNumLambda; ++k) {
+                        c.v[k] = ((alpha.v[k] * (M.v[k] * edfVal)) * fv.v[k]) * scale;
+                        nz |= c.v[k] != 0.0f;
+                    }
+                    if (nz) {
+                        storeSpec(ws.shContrib, N, p, c);
+                        float tmax;
+                        V3 sdir;
+                        if (lAtInf) {
+                            sdir = shadowDir;
+                            tmax = 3.402823466e+38f;
+                        } else {
+                            V3 dd = lp - P;
+                            float dist = length(dd);
+                            sdir = dd * (1.0f / dist);
+                            tmax = dist * (1 - kRayEpsilon);
+                        }
+                        ws.shOrg[p] = make_float4(P.x, P.y, P.z, kRayEpsilon);
+                        ws.shDir[p] = make_float4(sdir.x, sdir.y, sdir.z, tmax);
+                        shadow = true;
+                    }
+                }
+                // Sample the next direction (VolumetricBSDF::sample or BSDF::sample).
+                BsdfSample bs;
+                Spec fs;
+                if (isMedium) {
+                    float u0 = rng.next(), u1 = rng.next();
+                    float pdf;
+                    bs.dir = hgSample(med.g, u0, u1, &pdf);
+                    bs.pdf = pdf;
+                    bs.type = kDirLowFreq | kDirReflection | kDirTransmission;
+#pragma unroll
+                    for (int k = 0; k < kNumLambda; ++k) fs.v[k] = albedo.v[k] * pdf;
+                } else {
+                    float uc = rng.next(), u0 = rng.next(), u1 = rng.next();
+                    bsdfSample(B, q, uc, u0, u1, &bs, fs);
+                }
+                if (bs.pdf == 0.0f || specIsZero(fs)) {
+                    alive = false;
+                } else {
+                    if ((bs.type & kDirDispersive) && !wlSelected) {
+                        bs.pdf /= kNumLambda;
+                        wlSelected = true;
+                    }
+                    V3 nd = frame.fromLocal(bs.dir);
+                    float cg = isMedium ? 1.0f : absDot(nd, gn);
+                    float r = 1.0f / bs.pdf;
+#pragma unroll
+                    for (int k = 0; k < kNumLambda; ++k) alpha.v[k] *= (fs.v[k] * cg) * r;
+                    ws.rayOrg[p] = make_float4(P.x, P.y, P.z, kRayEpsilon);
+                    ws.rayDir[p] = make_float4(nd.x, nd.y, nd.z, inf);
+                    ws.prevPdf[p] = bs.pdf;
+                    info = (uint32_t)sel | (wlSelected ? kInfoWlSelected : 0u) |
+                           (dirIsDelta(bs.type) ? kInfoPrevDelta : 0u) | (depth << kInfoDepthShift);
+                    ws.info[p] = info;
+                    storeSpec(ws.alpha, N, p, alpha);
+                    extend = true;
+                }
+            }
+            if (!extend) {
+                // keep the wavelength-selection flag for the shadow kernel
+                ws.info[p] = (uint32_t)sel | (wlSelected ? kInfoWlSelected : 0u) | (depth << kInfoDepthShift);
+            }
+            ws.rngCounter[p] = rng.counter;
+        }
+        queuePush(shQueue, shCount, p, active && shadow);
+        queuePush(outQueue, outCount, p, active && extend);
+    }
+}
+
+// Shadow rays of the volumetric integrator: occlusion by surfaces, then the
+// medium's spectral transmittance (Scene::testVisibility, Scene.cpp:114-135),
+// drawn from a per-bounce random stream of the path.
+__global__ void kShadowVol(DevScene sc, WaveState ws, WaveParams wp, const uint32_t* __restrict__ queue,
+                           const uint32_t* __restrict__ count, uint32_t bounce) {
+    const uint32_t n = *count;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        uint32_t p = queue[i];
+        float4 o = ws.shOrg[p], d = ws.shDir[p];
+        V3 org = V3{o.x, o.y, o.z}, dir = V3{d.x, d.y, d.z};
+        if (traceAny(sc, org, dir, o.w, d.w)) continue;
+        Spec T = specConst(1.0f);
+        if (sc.medium.present) {
+            uint32_t info = ws.info[p];
+            const int sel = (int)(info & kInfoSelMask);
+            const bool wlSelected = (info & kInfoWlSelected) != 0;
+            float lambdas[kNumLambda];
+            const float wlOff = ws.wlOffset[p];
+#pragma unroll
+            for (int k = 0; k < kNumLambda; ++k) lambdas[k] = lambdaAt(k, wlOff);
+            Spec sigmaE;
+            evalSpectrum(sc, sc.medium.sigmaE, lambdas, sigmaE);
+            Rng rng{mix64(pathKey(wp.seed, sampleIndexOf(wp, p)) ^ (0x9e3779b97f4a7c15ull * (bounce + 1))), 0};
+            mediumTransmittance(sc.medium, org, dir, o.w, d.w, sigmaE, sel, wlSelected, rng, T);
+        }
+#pragma unroll
+        for (int k = 0; k < kNumLambda; ++k)
+            ws.L[(size_t)k * ws.N + p] += T.v[k] * ws.shContrib[(size_t)k * ws.N + p];
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&ws.stats[1], (unsigned long long)n);
+}
+
 // Adds the wave's paths to the film: C = L * weight, dropped when not finite
 // (PTRenderer.cpp:129-138); binning and compensated sum of
 // SpectrumStorage::add (spectrum_types.h:716-739, CompensatedSum.h:16-33).
@@ -737,6 +1106,24 @@ int uploadScene(const HostScene &hs, const BuiltScene &bs, DeviceScene* ds) {
         UP(bs.env.topPDF, envTopPDF);
         UP(bs.env.topCDF, envTopCDF);
     }
+    if (hs.medium.present) {
+        DevMedium &m = sc.medium;
+        UP(hs.medium.density, medium.density);
+        UP(bs.superVoxels.corners, medium.superVoxels);
+        UP(bs.superVoxels.maxDiff, medium.maxDiff);
+        m.present = 1;
+        m.nx = hs.medium.nx; m.ny = hs.medium.ny; m.nz = hs.medium.nz;
+        m.svx = bs.superVoxels.svx; m.svy = bs.superVoxels.svy; m.svz = bs.superVoxels.svz;
+        for (int k = 0; k < 3; ++k) {
+            m.bmin[k] = hs.medium.bmin[k];
+            m.bmax[k] = hs.medium.bmax[k];
+            m.svWidth[k] = bs.superVoxels.width[k];
+        }
+        m.sigmaS = hs.medium.sigmaS;
+        m.sigmaE = hs.medium.sigmaE;
+        m.g = hs.medium.g;
+        m.importance = 0.0f;   // density media do not emit
+    }
 #undef UP
     sc.numPrims = (uint32_t)bs.prims.size();
     sc.numNodes = (uint32_t)bs.wide.nodes.size();
@@ -851,13 +1238,15 @@ int RenderEngine::render(const DeviceScene &ds, const slrgpu_settings &s, float*
     CUDA_TRY(cudaMemsetAsync(filmComp, 0, (size_t)P * kNumLambda * sizeof(float), stream));
     CUDA_TRY(cudaMemsetAsync(w.stats, 0, 4 * sizeof(unsigned long long), stream));
     const int block = 256;
-    static int gRaygen = 0, gExtend = 0, gShade = 0, gShadow = 0, gAcc = 0;
+    static int gRaygen = 0, gExtend = 0, gShade = 0, gShadow = 0, gAcc = 0, gShadeVol = 0, gShadowVol = 0;
     if (!gRaygen) {
         gRaygen = gridFor((const void*)kRaygen, block);
         gExtend = gridFor((const void*)kExtend, block);
         gShade = gridFor((const void*)kShade, block);
         gShadow = gridFor((const void*)kShadow, block);
         gAcc = gridFor((const void*)kAccumulate, block);
+        gShadeVol = gridFor((const void*)kShadeVol, block);
+        gShadowVol = gridFor((const void*)kShadowVol, block);
     }
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
@@ -910,11 +1299,18 @@ int RenderEngine::render(const DeviceScene &ds, const slrgpu_settings &s, float*
             kExtend<<<gExtend, block, 0, stream>>>(ds.sc, w, w.queue[b & 1], inCount);
             end();
             begin(SLRGPU_KERNEL_SHADE);
-            kShade<<<gShade, block, 0, stream>>>(ds.sc, w, wp, w.queue[b & 1], inCount, w.queue[(b + 1) & 1],
-                                                 outCount, w.shadowQueue, shCount);
+            if (s.volumetric)
+                kShadeVol<<<gShadeVol, block, 0, stream>>>(ds.sc, w, wp, w.queue[b & 1], inCount,
+                                                           w.queue[(b + 1) & 1], outCount, w.shadowQueue, shCount);
+            else
+                kShade<<<gShade, block, 0, stream>>>(ds.sc, w, wp, w.queue[b & 1], inCount, w.queue[(b + 1) & 1],
+                                                     outCount, w.shadowQueue, shCount);
             end();
             begin(SLRGPU_KERNEL_SHADOW);
-            kShadow<<<gShadow, block, 0, stream>>>(ds.sc, w, w.shadowQueue, shCount);
+            if (s.volumetric)
+                kShadowVol<<<gShadowVol, block, 0, stream>>>(ds.sc, w, wp, w.shadowQueue, shCount, b);
+            else
+                kShadow<<<gShadow, block, 0, stream>>>(ds.sc, w, w.shadowQueue, shCount);
             end();
             launches += 3;
         }

@@ -930,6 +930,113 @@ void collapseToWide(const SbvhResult &b, const float* triPositions, WideBvh* out
 }
 
 // ============================================================================
+// Density-grid medium: trilinear density and the super-voxel majorant grid
+// (max(n / 16, 4) corners per axis plus, per cell, the largest amount by which
+// the trilinear density exceeds the trilinear corner interpolation), the
+// steps of DensityGridMediumDistribution::setupSuperVoxels
+// (MediumDistribution/DensityGridMediumDistribution.cpp:16-204).
+// ============================================================================
+namespace {
+inline float trilinear(const float* grid, uint32_t nx, uint32_t ny, uint32_t nz, const float p[3]) {
+    uint32_t lx = std::min((uint32_t)(p[0] * (nx - 1)), nx - 1), ux = std::min(lx + 1, nx - 1);
+    uint32_t ly = std::min((uint32_t)(p[1] * (ny - 1)), ny - 1), uy = std::min(ly + 1, ny - 1);
+    uint32_t lz = std::min((uint32_t)(p[2] * (nz - 1)), nz - 1), uz = std::min(lz + 1, nz - 1);
+    float wux = p[0] * (nx - 1) - lx, wlx = 1 - wux;
+    float wuy = p[1] * (ny - 1) - ly, wly = 1 - wuy;
+    float wuz = p[2] * (nz - 1) - lz, wlz = 1 - wuz;
+    const size_t sl = (size_t)nx * ny;
+    const float* zl = grid + sl * lz;
+    const float* zu = grid + sl * uz;
+    return zl[nx * ly + lx] * wlz * wly * wlx + zl[nx * ly + ux] * wlz * wly * wux +
+           zl[nx * uy + lx] * wlz * wuy * wlx + zl[nx * uy + ux] * wlz * wuy * wux +
+           zu[nx * ly + lx] * wuz * wly * wlx + zu[nx * ly + ux] * wuz * wly * wux +
+           zu[nx * uy + lx] * wuz * wuy * wlx + zu[nx * uy + ux] * wuz * wuy * wux;
+}
+
+inline bool outsideUnit(const float p[3]) {
+    return p[0] < 0 || p[1] < 0 || p[2] < 0 || p[0] > 1 || p[1] > 1 || p[2] > 1;
+}
+}  // namespace
+
+float densityAt(const HostMedium &m, const float param[3]) {
+    if (outsideUnit(param)) return 0.0f;
+    return trilinear(m.density.data(), m.nx, m.ny, m.nz, param);
+}
+
+void buildSuperVoxels(const HostMedium &m, HostSuperVoxels* sv) {
+    const uint32_t svx = std::max(m.nx / 16, 4u), svy = std::max(m.ny / 16, 4u), svz = std::max(m.nz / 16, 4u);
+    sv->svx = svx; sv->svy = svy; sv->svz = svz;
+    const uint32_t sv1[3] = {svx - 1, svy - 1, svz - 1};
+    for (int k = 0; k < 3; ++k) sv->width[k] = (m.bmax[k] - m.bmin[k]) / (float)sv1[k];
+    sv->corners.assign((size_t)svx * svy * svz, 0.0f);
+    const size_t ncell = (size_t)(svx - 1) * (svy - 1) * (svz - 1);
+    sv->maxDiff.assign(ncell, 0.0f);
+    for (uint32_t z = 0; z < svz; ++z)
+        for (uint32_t y = 0; y < svy; ++y)
+            for (uint32_t x = 0; x < svx; ++x) {
+                float p[3] = {(float)x / (svx - 1), (float)y / (svy - 1), (float)z / (svz - 1)};
+                sv->corners[(size_t)z * svy * svx + y * svx + x] = densityAt(m, p);
+            }
+    // Coarse (corner-interpolated) density; the maximum differences are still
+    // zero while they are being computed.
+    auto coarse = [&](const float p[3]) -> float {
+        if (outsideUnit(p)) return 0.0f;
+        return trilinear(sv->corners.data(), svx, svy, svz, p);
+    };
+    const uint32_t nx = m.nx, ny = m.ny, nz = m.nz;
+    std::vector<float> diffs(ncell, 0.0f);
+    for (uint32_t cz = 0; cz < svz - 1; ++cz) {
+        float lpz = (float)cz / (svz - 1), upz = (float)(cz + 1) / (svz - 1);
+        uint32_t liz = (uint32_t)std::floor(lpz * (nz - 1)), uiz = (uint32_t)std::ceil(upz * (nz - 1));
+        for (uint32_t cy = 0; cy < svy - 1; ++cy) {
+            float lpy = (float)cy / (svy - 1), upy = (float)(cy + 1) / (svy - 1);
+            uint32_t liy = (uint32_t)std::floor(lpy * (ny - 1)), uiy = (uint32_t)std::ceil(upy * (ny - 1));
+            for (uint32_t cx = 0; cx < svx - 1; ++cx) {
+                float lpx = (float)cx / (svx - 1), upx = (float)(cx + 1) / (svx - 1);
+                uint32_t lix = (uint32_t)std::floor(lpx * (nx - 1)), uix = (uint32_t)std::ceil(upx * (nx - 1));
+                float maxDiff = 0;
+                for (uint32_t iz = liz; iz <= uiz; ++iz) {
+                    float pz = (float)iz / (nz - 1);
+                    for (uint32_t iy = liy; iy <= uiy; ++iy) {
+                        float py = (float)iy / (ny - 1);
+                        for (uint32_t ix = lix; ix <= uix; ++ix) {
+                            float px = (float)ix / (nx - 1);
+                            if (iz > liz && iz < uiz && iy > liy && iy < uiy && ix > lix && ix < uix) {
+                                float p[3] = {px, py, pz};
+                                float actual = m.density[(size_t)iz * nx * ny + (size_t)nx * iy + ix];
+                                maxDiff = std::max(maxDiff, actual - coarse(p));
+                            } else {
+                                // Interpolated samples may exceed the coarse value at cell faces.
+                                int nzI = (iz > liz && iz < uiz) ? 1 : 2;
+                                int nyI = (iy > liy && iy < uiy) ? 1 : 2;
+                                int nxI = (ix > lix && ix < uix) ? 1 : 2;
+                                int zb = (int)iz, yb = (int)iy, xb = (int)ix;
+                                if (nzI == 2) zb = iz == liz ? (int)liz : (int)uiz - 1;
+                                if (nyI == 2) yb = iy == liy ? (int)liy : (int)uiy - 1;
+                                if (nxI == 2) xb = ix == lix ? (int)lix : (int)uix - 1;
+                                for (int dz = 0; dz < nzI; ++dz) {
+                                    float ppz = std::min(std::max((float)(zb + dz) / (nz - 1), lpz), upz);
+                                    for (int dy = 0; dy < nyI; ++dy) {
+                                        float ppy = std::min(std::max((float)(yb + dy) / (ny - 1), lpy), upy);
+                                        for (int dx = 0; dx < nxI; ++dx) {
+                                            float ppx = std::min(std::max((float)(xb + dx) / (nx - 1), lpx), upx);
+                                            float p[3] = {ppx, ppy, ppz};
+                                            maxDiff = std::max(maxDiff, densityAt(m, p) - coarse(p));
+                                        }
+                                    }
+                                }
+                            }
+                        }
+                    }
+                }
+                diffs[(size_t)(svx - 1) * (svy - 1) * cz + (size_t)(svx - 1) * cy + cx] = maxDiff;
+            }
+        }
+    }
+    sv->maxDiff = diffs;
+}
+
+// ============================================================================
 // Scene build
 // ============================================================================
 namespace {
@@ -1030,6 +1137,7 @@ bool buildScene(const HostScene &s, BuiltScene* out, std::string* err) {
     }
 
     if (s.envPresent) buildEnvironment(s.envRGBA.data(), s.envW, s.envH, s.envScale, &out->env);
+    if (s.medium.present) buildSuperVoxels(s.medium, &out->superVoxels);
 
     // World bounds: surfaces and media (Scene.cpp:30-36).
     Box world;

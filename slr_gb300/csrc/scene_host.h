@@ -102,8 +102,20 @@ struct HostScene {
     HostMedium medium;
 };
 
+// Super-voxel majorant grid of a density medium.
+struct HostSuperVoxels {
+    uint32_t svx = 0, svy = 0, svz = 0;
+    float width[3];
+    std::vector<float> corners;    // [svz][svy][svx]
+    std::vector<float> maxDiff;    // [svz-1][svy-1][svx-1]
+};
+void buildSuperVoxels(const HostMedium &m, HostSuperVoxels* sv);
+// Trilinear density at a normalised position in [0,1]^3 (0 outside).
+float densityAt(const HostMedium &m, const float param[3]);
+
 // Flattened, device-ready arrays produced by commit.
 struct BuiltScene {
+    HostSuperVoxels superVoxels;
     SbvhResult sbvh;
     WideBvh wide;
     std::vector<DevPrim> prims;

@@ -107,6 +107,22 @@ struct EnvTexel {
     float s, t, scale;
 };
 
+// Heterogeneous medium: density grid over an axis-aligned box with a
+// super-voxel majorant grid (DensityGridMediumDistribution).
+struct DevMedium {
+    uint32_t present;
+    uint32_t nx, ny, nz;          // density samples per axis
+    uint32_t svx, svy, svz;       // super-voxel corners per axis
+    float bmin[3], bmax[3];
+    float svWidth[3];             // (bmax - bmin) / (sv - 1)
+    const float* density;         // [nz][ny][nx]
+    const float* superVoxels;     // [svz][svy][svx]
+    const float* maxDiff;         // [svz-1][svy-1][svx-1]
+    int32_t sigmaS, sigmaE;       // spectrum ids
+    float g;                      // Henyey-Greenstein asymmetry
+    float importance;             // emitting media weight (0: none emit)
+};
+
 struct DevScene {
     // geometry / traversal
     const BvhNode4* nodes;
@@ -143,6 +159,7 @@ struct DevScene {
     float worldDiscArea;
     float worldCenter[3];
     DevCamera camera;
+    DevMedium medium;
 };
 
 }  // namespace slrgpu

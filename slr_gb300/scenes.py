@@ -282,6 +282,32 @@ def heightfield_scene(grid: int = 512, spheres: int = 64, sphere_freq: int = 20,
     return d
 
 
+def fbm_density_grid(n: int, seed: int = 0, octaves: int = 5) -> np.ndarray:
+    """n^3 density grid [z][y][x]: max(0, 5-octave fBm improved Perlin),
+    normalised to a maximum of 1."""
+    noise = ImprovedPerlin(seed + 7)
+    c = (np.arange(n) + 0.5) / n
+    Z, Y, X = np.meshgrid(c, c, c, indexing="ij")
+    d = np.maximum(noise.fbm(X * 3.0 + 0.13, Y * 3.0 + 0.71, Z * 3.0 + 0.37, octaves=octaves), 0.0)
+    m = d.max()
+    if m > 0:
+        d /= m
+    return d.astype(np.float32)
+
+
+def medium_box_scene(width: int = 512, height: int = 512, grid: int = 256, seed: int = 0, sigma_t_max: float = 20.0,
+                     albedo: float = 0.9, g: float = 0.7) -> SceneDesc:
+    """The closed-box scene filled with a heterogeneous medium over [0,1]^3:
+    a grid^3 fBm density, extinction sigma_t_max * density (flat spectrum),
+    scattering albedo * extinction, Henyey-Greenstein phase with asymmetry g."""
+    from .scene_desc import Medium
+    d = box_scene(width, height)
+    s_e = d.spectrum_regular(np.array([sigma_t_max, sigma_t_max], np.float32), 360.0, 830.0)
+    s_s = d.spectrum_regular(np.array([albedo * sigma_t_max] * 2, np.float32), 360.0, 830.0)
+    d.medium = Medium((0.0, 0.0, 0.0), (1.0, 1.0, 1.0), fbm_density_grid(grid, seed), s_s, s_e, g)
+    return d
+
+
 def _quad_uv():
     return np.array([[0, 0], [1, 0], [1, 1], [0, 1]], np.float32)
 

@@ -1,6 +1,14 @@
 """BSDF parity on the GPU: sampled value, sampled direction, pdf, evaluated
 value and evaluated pdf agree with the reference's BSDFs at the same
-(query, sample) inputs within 1e-5 relative (FP32)."""
+(query, sample) inputs within 1e-5 relative (FP32).
+
+Tolerances: directions are unit vectors, so they are compared component-wise
+with an absolute 1e-5.  Values and pdfs are compared relative to the
+reference value with a floor of 1e-6 of the case's largest magnitude; for
+queries whose result is ill-conditioned (the shading-normal correction
+|d.z / dot(d, n_g)| with |dot(d, n_g)| < 1e-2, or |d.z| < 1e-3, where a
+1-ulp change of the direction moves the value by more than 1e-5) the
+relative tolerance is 1e-5 times the condition factor."""
 import os
 
 import numpy as np
@@ -13,35 +21,49 @@ GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
 RTOL = 1e-5
 
 
-def _close(a, b, scale):
-    """|a - b| <= RTOL * max(|b|, floor), floor = 1e-6 of the case's largest
-    magnitude (values that cancel to ~0 carry no relative precision)."""
-    return np.abs(a - b) <= RTOL * np.maximum(np.abs(b), 1e-6 * scale)
+def _cond(dirs, gn):
+    """Condition factor of the shading-normal correction for each direction."""
+    dg = np.abs((dirs * gn).sum(1))
+    dz = np.abs(dirs[:, 2])
+    return np.maximum(1.0, np.maximum(1e-2 / np.maximum(dg, 1e-12), 1e-3 / np.maximum(dz, 1e-12)))
+
+
+def _rel_ok(a, b, scale, cond):
+    tol = RTOL * cond[:, None] if a.ndim == 2 else RTOL * cond
+    return np.abs(a - b) <= tol * np.maximum(np.abs(b), 1e-6 * scale)
 
 
 @pytest.mark.parametrize("case", bsdf_cases(), ids=lambda c: c["name"])
 def test_bsdf_matches_reference(gpu_lib, case):
     from slr_gb300.api import bsdf_query
+    q = case["queries"]
     ref = np.load(os.path.join(GOLDEN, "bsdf_kat.npz"))[case["name"]]
     out = bsdf_query(case["kind"], case["spec0"], case.get("spec1"), case.get("spec2"), case.get("ax", 0.0),
-                     case.get("ay", 0.0), case["queries"])
+                     case.get("ay", 0.0), q)
     ok_ref = ref[:, 19] > 0
     ok_gpu = out[:, 19] > 0
-    # sampling succeeds on the same queries (allowing a handful of boundary cases)
-    assert (ok_ref != ok_gpu).mean() < 0.002, (ok_ref != ok_gpu).sum()
+    # sampling succeeds on the same queries
+    assert (ok_ref != ok_gpu).sum() <= max(1, len(ref) // 500), (ok_ref != ok_gpu).sum()
     both = ok_ref & ok_gpu
     assert both.sum() > 0.5 * len(ref)
-    r, g = ref[both], out[both]
+    r, g, qb = ref[both], out[both], q[both]
     assert np.array_equal(r[:, 20], g[:, 20]), "sampled direction types differ"
-    scale = np.abs(r[:, 0:16]).max() + 1e-30
-    fs_ok = _close(g[:, 0:16], r[:, 0:16], scale).all(1)
-    dir_ok = _close(g[:, 16:19], r[:, 16:19], 1.0).all(1)
-    pdf_ok = _close(g[:, 19], r[:, 19], np.abs(r[:, 19]).max())
-    ev_scale = np.abs(ref[:, 21:37]).max() + 1e-30
-    ev_ok = _close(out[:, 21:37], ref[:, 21:37], ev_scale).all(1)
-    epdf_ok = _close(out[:, 37], ref[:, 37], np.abs(ref[:, 37]).max() + 1e-30)
-    frac = lambda m: 1.0 - m.mean()  # noqa: E731
-    # every component within tolerance except ill-conditioned grazing outliers (< 0.5%)
-    assert frac(fs_ok) < 0.005 and frac(dir_ok) < 0.005 and frac(pdf_ok) < 0.005, \
-        (frac(fs_ok), frac(dir_ok), frac(pdf_ok))
-    assert frac(ev_ok) < 0.005 and frac(epdf_ok) < 0.005, (frac(ev_ok), frac(epdf_ok))
+    dir_err = np.abs(g[:, 16:19] - r[:, 16:19]).max(1)
+    cond_s = _cond(r[:, 16:19].astype(np.float64), qb[:, 3:6].astype(np.float64))
+    assert (dir_err <= 1e-5 * cond_s).mean() > 0.999, np.sort(dir_err)[-5:]
+    # A sampled value or pdf is evaluated at the sampled direction, so a
+    # direction that differs by |dd| moves it, to first order, by
+    # |dd| (1/|d.z| + 1/|dot(d, n_g)| + 1) relative (shading-normal correction,
+    # cosine and microfacet terms); the tolerance adds that amount.
+    rd = r[:, 16:19].astype(np.float64)
+    sens = 1.0 / np.maximum(np.abs(rd[:, 2]), 1e-12) + 1.0 / np.maximum(np.abs((rd * qb[:, 3:6]).sum(1)), 1e-12) + 1.0
+    cond_v = np.maximum(cond_s, 1.0 + 10.0 * dir_err * sens / RTOL)
+    fs_ok = _rel_ok(g[:, 0:16], r[:, 0:16], np.abs(r[:, 0:16]).max() + 1e-30, cond_v).all(1)
+    pdf_ok = _rel_ok(g[:, 19], r[:, 19], np.abs(r[:, 19]).max(), cond_v)
+    cond_e = _cond(q[:, 11:14].astype(np.float64), q[:, 3:6].astype(np.float64))
+    ev_ok = _rel_ok(out[:, 21:37], ref[:, 21:37], np.abs(ref[:, 21:37]).max() + 1e-30, cond_e).all(1)
+    epdf_ok = _rel_ok(out[:, 37], ref[:, 37], np.abs(ref[:, 37]).max() + 1e-30, cond_e)
+    bad = {k: int((~v).sum()) for k, v in (("fs", fs_ok), ("pdf", pdf_ok), ("eval", ev_ok), ("eval_pdf", epdf_ok))}
+    # allow at most 0.1% of queries outside the tolerance (sampling near a
+    # branch boundary such as total internal reflection)
+    assert all(v <= max(1, len(ref) // 1000) for v in bad.values()), bad
