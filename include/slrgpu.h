@@ -165,6 +165,35 @@ int slrgpu_scene_reupload(slrgpu_handle scene, uint64_t* bytes);
 int slrgpu_render(slrgpu_handle scene, const slrgpu_settings* settings, float* film,
                   int film_on_device, slrgpu_render_stats* stats);
 
+/* Render that allocates nothing.  It has no counterpart in the reference.
+ *
+ * For callers that cannot call cudaMalloc while they run: a real-time loop
+ * with a fixed device-memory budget, a host application that owns the GPU's
+ * allocator, or an embedding runtime that forbids allocation after start-up.
+ * slrgpu_render needs per-context path-state buffers that it allocates (and
+ * grows) on demand; this variant keeps the path state, queues, counters and
+ * film sums in one fixed file-scope device array of
+ * slrgpu_render_noalloc_scratch_bytes() bytes (about 27 MiB), which every GPU
+ * that loads the library holds until the process exits.
+ *
+ * Limits: width * height <= 65536 and max_depth <= 64 (settings beyond them
+ * are rejected with SLRGPU_ERR_INVALID_ARGUMENT and a message); each wave
+ * holds width * height * samples_per_wave <= 65536 paths (0 picks the
+ * largest).  film_device receives width*height*16 floats in the layout of
+ * slrgpu_render.  The call is stream-ordered on `stream` (a cudaStream_t, or
+ * NULL for the legacy default stream) and returns without waiting; the caller
+ * synchronizes before reading the film.  The scene's own arrays were
+ * allocated by slrgpu_scene_commit.
+ *
+ * The first call on a device, with that device current, looks up the device
+ * address of the scratch array; make that first call before any stream
+ * capture.  Every call shares the one array and clears what must start at
+ * zero, so calls that overlap on the GPU (concurrent streams or threads)
+ * race: serialize them.  With the same settings and samples_per_wave the
+ * film equals slrgpu_render's. */
+int slrgpu_render_noalloc(slrgpu_handle scene, const slrgpu_settings* settings, float* film_device, void* stream);
+uint64_t slrgpu_render_noalloc_scratch_bytes(void);
+
 /* Ray queries on the committed scene (device pointers).  rays: n x 8 floats
  * (org.xyz, tmin, dir.xyz, tmax).  Closest hit fills prim (0xffffffff on
  * miss), t, b1, b2 (Moller-Trumbore barycentrics); any hit fills prim with 1

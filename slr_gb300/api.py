@@ -68,7 +68,7 @@ class RenderStats(C.Structure):
 def header_symbols() -> list[str]:
     """Every function the C ABI header declares."""
     text = HEADER.read_text()
-    return sorted(set(re.findall(r"^\s*(?:int|const char\*|void)\s+(slrgpu_\w+)\s*\(", text, re.M)))
+    return sorted(set(re.findall(r"^\s*(?:int|const char\*|void|uint64_t)\s+(slrgpu_\w+)\s*\(", text, re.M)))
 
 
 def lib():
@@ -110,6 +110,8 @@ def lib():
             "slrgpu_environment_tables": (I, [H, up, up, fp, fp, fp, fp, fp]),
             "slrgpu_bsdf_query": (I, [I, fp, fp, fp, F, F, fp, U, fp]),
             "slrgpu_scene_reupload": (I, [H, C.POINTER(C.c_uint64)]),
+            "slrgpu_render_noalloc": (I, [H, C.POINTER(Settings), P, P]),
+            "slrgpu_render_noalloc_scratch_bytes": (C.c_uint64, []),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)

@@ -395,6 +395,21 @@ int slrgpu_render(slrgpu_handle scene, const slrgpu_settings* settings, float* f
     return s->ctx->engine.render(s->dev, *settings, film, film_on_device != 0, stats, 0);
 }
 
+int slrgpu_render_noalloc(slrgpu_handle scene, const slrgpu_settings* settings, float* film_device, void* stream) {
+    const bool mutating = false;
+    GET_SCENE(s, scene);
+    if (!settings || !film_device) return fail(SLRGPU_ERR_INVALID_ARGUMENT, "settings and film must not be NULL");
+    if (!s->committed) return fail(SLRGPU_ERR_NOT_COMMITTED, "scene not committed");
+    if (!s->host.cameraPresent) return fail(SLRGPU_ERR_STATE, "scene has no camera");
+    if (settings->volumetric && !s->host.medium.present)
+        return fail(SLRGPU_ERR_INVALID_ARGUMENT, "volumetric render of a scene without medium");
+    cudaError_t e = cudaSetDevice(s->ctx->device);
+    if (e != cudaSuccess) return fail(SLRGPU_ERR_CUDA, cudaGetErrorString(e));
+    return renderNoAlloc(s->dev, *settings, film_device, (cudaStream_t)stream);
+}
+
+uint64_t slrgpu_render_noalloc_scratch_bytes(void) { return (uint64_t)noAllocScratchBytes(); }
+
 int slrgpu_trace(slrgpu_handle scene, const float* rays, uint32_t n, int any_hit, uint32_t* prim, float* t, float* b1,
                  float* b2, void* stream) {
     const bool mutating = false;

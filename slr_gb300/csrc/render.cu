@@ -13,6 +13,7 @@
 #include <chrono>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 
 #include "device_bsdf.cuh"
 #include "device_medium.cuh"
@@ -1349,6 +1350,177 @@ int RenderEngine::render(const DeviceScene &ds, const slrgpu_settings &s, float*
         stats->dropped_samples = hstats[2];
         stats->kernel_launches = launches;
     }
+    return SLRGPU_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Allocation-free render (slrgpu_render_noalloc)
+//
+// For callers that may not allocate device memory once they are running: a
+// real-time loop that owns a fixed memory budget, a host that hands the GPU
+// to the renderer only between its own allocations, or an embedding runtime
+// whose allocator forbids cudaMalloc after start-up.  The path state, queues, counters and the film sums live in
+// one file-scope device array of a fixed size, which every GPU that loads this
+// library keeps until the process exits.  Limits: width * height * samples
+// per wave <= kNoAllocMaxPaths and max_depth <= kNoAllocMaxDepth.
+// ---------------------------------------------------------------------------
+constexpr uint32_t kNoAllocMaxPaths = 65536;
+constexpr uint32_t kNoAllocMaxDepth = 64;
+
+constexpr size_t naAlign(size_t x) { return (x + 255) & ~(size_t)255; }
+constexpr size_t kNaRayOrg = 0;
+constexpr size_t kNaRayDir = naAlign(kNaRayOrg + 16ull * kNoAllocMaxPaths);
+constexpr size_t kNaHit = naAlign(kNaRayDir + 16ull * kNoAllocMaxPaths);
+constexpr size_t kNaAlpha = naAlign(kNaHit + 16ull * kNoAllocMaxPaths);
+constexpr size_t kNaL = naAlign(kNaAlpha + 4ull * kNumLambda * kNoAllocMaxPaths);
+constexpr size_t kNaInfo = naAlign(kNaL + 4ull * kNumLambda * kNoAllocMaxPaths);
+constexpr size_t kNaWlOffset = naAlign(kNaInfo + 4ull * kNoAllocMaxPaths);
+constexpr size_t kNaPrevPdf = naAlign(kNaWlOffset + 4ull * kNoAllocMaxPaths);
+constexpr size_t kNaInitY = naAlign(kNaPrevPdf + 4ull * kNoAllocMaxPaths);
+constexpr size_t kNaCamWeight = naAlign(kNaInitY + 4ull * kNoAllocMaxPaths);
+constexpr size_t kNaRngCounter = naAlign(kNaCamWeight + 4ull * kNoAllocMaxPaths);
+constexpr size_t kNaShOrg = naAlign(kNaRngCounter + 4ull * kNoAllocMaxPaths);
+constexpr size_t kNaShDir = naAlign(kNaShOrg + 16ull * kNoAllocMaxPaths);
+constexpr size_t kNaShContrib = naAlign(kNaShDir + 16ull * kNoAllocMaxPaths);
+constexpr size_t kNaQueue0 = naAlign(kNaShContrib + 4ull * kNumLambda * kNoAllocMaxPaths);
+constexpr size_t kNaQueue1 = naAlign(kNaQueue0 + 4ull * kNoAllocMaxPaths);
+constexpr size_t kNaShQueue = naAlign(kNaQueue1 + 4ull * kNoAllocMaxPaths);
+constexpr size_t kNaCounters = naAlign(kNaShQueue + 4ull * kNoAllocMaxPaths);
+constexpr size_t kNaStats = naAlign(kNaCounters + 4ull * 3 * (kNoAllocMaxDepth + 2));
+constexpr size_t kNaFilmSum = naAlign(kNaStats + 8ull * 4);
+constexpr size_t kNaFilmComp = naAlign(kNaFilmSum + 4ull * kNumLambda * kNoAllocMaxPaths);
+constexpr size_t kNoAllocScratchBytes = naAlign(kNaFilmComp + 4ull * kNumLambda * kNoAllocMaxPaths);
+
+static __device__ __align__(256) unsigned char g_noallocScratch[kNoAllocScratchBytes];
+
+namespace {
+std::mutex g_noallocMu;
+void* g_noallocAddr[64] = {};   // device address of g_noallocScratch, per device
+}  // namespace
+
+size_t noAllocScratchBytes() { return kNoAllocScratchBytes; }
+
+int renderNoAlloc(const DeviceScene &ds, const slrgpu_settings &s, float* film, cudaStream_t stream) {
+    if (!film) {
+        setError("film must be a device pointer");
+        return SLRGPU_ERR_INVALID_ARGUMENT;
+    }
+    const uint64_t P = (uint64_t)s.width * s.height;
+    if (s.width == 0 || s.height == 0 || s.spp == 0) {
+        setError("width, height and spp must be positive");
+        return SLRGPU_ERR_INVALID_ARGUMENT;
+    }
+    if (P > kNoAllocMaxPaths) {
+        setError("slrgpu_render_noalloc: width * height exceeds the fixed scratch limit of 65536 pixels");
+        return SLRGPU_ERR_INVALID_ARGUMENT;
+    }
+    if (s.max_depth > kNoAllocMaxDepth) {
+        setError("slrgpu_render_noalloc: max_depth exceeds the fixed scratch limit of 64");
+        return SLRGPU_ERR_INVALID_ARGUMENT;
+    }
+    uint32_t S = s.samples_per_wave ? s.samples_per_wave : (uint32_t)(kNoAllocMaxPaths / P);
+    S = std::min(S, s.spp);
+    if ((uint64_t)S * P > kNoAllocMaxPaths) {
+        setError("slrgpu_render_noalloc: width * height * samples_per_wave exceeds the fixed scratch limit of 65536 paths");
+        return SLRGPU_ERR_INVALID_ARGUMENT;
+    }
+    int dev = 0;
+    CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) {
+        setError("device index out of range for the scratch table");
+        return SLRGPU_ERR_INVALID_ARGUMENT;
+    }
+    unsigned char* base = nullptr;
+    {
+        // First call on this device (with it current): resolve the device
+        // address of the scratch array.  The host-side symbol is only a
+        // stand-in and must never be handed to a kernel.
+        std::lock_guard<std::mutex> lock(g_noallocMu);
+        if (!g_noallocAddr[dev]) {
+            void* ptr = nullptr;
+            cudaError_t e = cudaGetSymbolAddress(&ptr, g_noallocScratch);
+            if (e != cudaSuccess || !ptr) {
+                setError(std::string("cudaGetSymbolAddress failed: ") + cudaGetErrorString(e));
+                return SLRGPU_ERR_CUDA;
+            }
+            g_noallocAddr[dev] = ptr;
+        }
+        base = (unsigned char*)g_noallocAddr[dev];
+    }
+    const int block = 256;
+    static int gRaygen = 0, gExtend = 0, gShade = 0, gShadow = 0, gAcc = 0, gShadeVol = 0, gShadowVol = 0;
+    {
+        std::lock_guard<std::mutex> lock(g_noallocMu);
+        if (!gRaygen) {
+            gExtend = gridFor((const void*)kExtend, block);
+            gShade = gridFor((const void*)kShade, block);
+            gShadow = gridFor((const void*)kShadow, block);
+            gAcc = gridFor((const void*)kAccumulate, block);
+            gShadeVol = gridFor((const void*)kShadeVol, block);
+            gShadowVol = gridFor((const void*)kShadowVol, block);
+            gRaygen = gridFor((const void*)kRaygen, block);
+        }
+    }
+    WaveState w;
+    std::memset(&w, 0, sizeof(w));
+    w.N = (uint32_t)(S * P);
+    w.rayOrg = (float4*)(base + kNaRayOrg);
+    w.rayDir = (float4*)(base + kNaRayDir);
+    w.hit = (float4*)(base + kNaHit);
+    w.alpha = (float*)(base + kNaAlpha);
+    w.L = (float*)(base + kNaL);
+    w.info = (uint32_t*)(base + kNaInfo);
+    w.wlOffset = (float*)(base + kNaWlOffset);
+    w.prevPdf = (float*)(base + kNaPrevPdf);
+    w.initY = (float*)(base + kNaInitY);
+    w.camWeight = (float*)(base + kNaCamWeight);
+    w.rngCounter = (uint32_t*)(base + kNaRngCounter);
+    w.shOrg = (float4*)(base + kNaShOrg);
+    w.shDir = (float4*)(base + kNaShDir);
+    w.shContrib = (float*)(base + kNaShContrib);
+    w.queue[0] = (uint32_t*)(base + kNaQueue0);
+    w.queue[1] = (uint32_t*)(base + kNaQueue1);
+    w.shadowQueue = (uint32_t*)(base + kNaShQueue);
+    w.counters = (uint32_t*)(base + kNaCounters);
+    w.stats = (unsigned long long*)(base + kNaStats);
+    float* filmSum = (float*)(base + kNaFilmSum);
+    float* filmComp = (float*)(base + kNaFilmComp);
+    // The array keeps the previous call's contents: clear the accumulators.
+    CUDA_TRY(cudaMemsetAsync(filmSum, 0, (size_t)P * kNumLambda * sizeof(float), stream));
+    CUDA_TRY(cudaMemsetAsync(filmComp, 0, (size_t)P * kNumLambda * sizeof(float), stream));
+    CUDA_TRY(cudaMemsetAsync(w.stats, 0, 4 * sizeof(unsigned long long), stream));
+    const uint32_t D = s.max_depth;
+    for (uint32_t sb = 0; sb < s.spp; sb += S) {
+        WaveParams wp;
+        wp.width = s.width;
+        wp.height = s.height;
+        wp.numPixels = (uint32_t)P;
+        wp.samplesInWave = std::min(S, s.spp - sb);
+        wp.sampleBase = sb;
+        wp.numPaths = wp.samplesInWave * (uint32_t)P;
+        wp.maxDepth = D;
+        wp.seed = s.seed;
+        CUDA_TRY(cudaMemsetAsync(w.counters, 0, 3 * (size_t)(D + 2) * sizeof(uint32_t), stream));
+        kRaygen<<<gRaygen, block, 0, stream>>>(ds.sc, w, wp);
+        for (uint32_t b = 0; b <= D; ++b) {
+            uint32_t* inCount = w.counters + b;
+            uint32_t* outCount = w.counters + b + 1;
+            uint32_t* shCount = w.counters + (D + 2) + b;
+            kExtend<<<gExtend, block, 0, stream>>>(ds.sc, w, w.queue[b & 1], inCount);
+            if (s.volumetric) {
+                kShadeVol<<<gShadeVol, block, 0, stream>>>(ds.sc, w, wp, w.queue[b & 1], inCount,
+                                                           w.queue[(b + 1) & 1], outCount, w.shadowQueue, shCount);
+                kShadowVol<<<gShadowVol, block, 0, stream>>>(ds.sc, w, wp, w.shadowQueue, shCount, b);
+            } else {
+                kShade<<<gShade, block, 0, stream>>>(ds.sc, w, wp, w.queue[b & 1], inCount, w.queue[(b + 1) & 1],
+                                                     outCount, w.shadowQueue, shCount);
+                kShadow<<<gShadow, block, 0, stream>>>(ds.sc, w, w.shadowQueue, shCount);
+            }
+        }
+        kAccumulate<<<gAcc, block, 0, stream>>>(w, wp, filmSum, filmComp);
+    }
+    kFilmToPixelMajor<<<gAcc, block, 0, stream>>>(filmSum, film, (uint32_t)P);
+    CUDA_TRY(cudaGetLastError());
     return SLRGPU_OK;
 }
 

@@ -49,6 +49,9 @@ struct RenderEngine {
 
 int uploadScene(const HostScene &hs, const BuiltScene &bs, DeviceScene* ds);
 int reuploadScene(DeviceScene* ds, uint64_t* bytes, cudaStream_t stream);
+// Render with all scratch in a fixed device array (no allocation).
+int renderNoAlloc(const DeviceScene &ds, const slrgpu_settings &s, float* film, cudaStream_t stream);
+size_t noAllocScratchBytes();
 int bsdfQuery(int kind, const float* s0, const float* s1, const float* s2, float ax, float ay, const float* queries,
               uint32_t n, float* out);
 int traceRays(const DeviceScene &ds, const float* rays, uint32_t n, int anyHit, uint32_t* prim, float* t, float* b1,
