@@ -160,8 +160,12 @@ int slrgpu_scene_reupload(slrgpu_handle scene, uint64_t* bytes);
 /* Rendering ----------------------------------------------------------- */
 /* Blocking render.  film receives width*height*16 floats: per pixel (row
  * major) the 16-bin spectral sum over all samples, the value the reference's
- * ImageSensor::pixel(x, y) returns after PTRenderer::render.  film is a
- * host pointer, or a device pointer when film_on_device is nonzero. */
+ * ImageSensor::pixel(x, y) returns after PTRenderer::render.  As in the
+ * reference, the sensor is sampled in whole 8 x 8 tiles: when width or height
+ * is not a multiple of 8, the samples of the overhanging tile positions land
+ * in the last column / row (PTRenderer.cpp:104-110, ImageSensor.cpp:125-130),
+ * and stats->path_samples counts them.  film is a host pointer, or a device
+ * pointer when film_on_device is nonzero. */
 int slrgpu_render(slrgpu_handle scene, const slrgpu_settings* settings, float* film,
                   int film_on_device, slrgpu_render_stats* stats);
 
@@ -176,10 +180,11 @@ int slrgpu_render(slrgpu_handle scene, const slrgpu_settings* settings, float* f
  * slrgpu_render_noalloc_scratch_bytes() bytes (about 27 MiB), which every GPU
  * that loads the library holds until the process exits.
  *
- * Limits: width * height <= 65536 and max_depth <= 64 (settings beyond them
- * are rejected with SLRGPU_ERR_INVALID_ARGUMENT and a message); each wave
- * holds width * height * samples_per_wave <= 65536 paths (0 picks the
- * largest).  film_device receives width*height*16 floats in the layout of
+ * Limits: the sample grid, width and height each rounded up to a multiple
+ * of 8 (the reference samples its sensor in whole 8 x 8 tiles), holds <= 65536
+ * positions, and max_depth <= 64 (settings beyond them are rejected with
+ * SLRGPU_ERR_INVALID_ARGUMENT and a message); each wave holds grid positions *
+ * samples_per_wave <= 65536 paths (0 picks the largest).  film_device receives width*height*16 floats in the layout of
  * slrgpu_render.  The call is stream-ordered on `stream` (a cudaStream_t, or
  * NULL for the legacy default stream) and returns without waiting; the caller
  * synchronizes before reading the film.  The scene's own arrays were
@@ -212,6 +217,23 @@ int slrgpu_trace(slrgpu_handle scene, const float* rays, uint32_t n, int any_hit
  * pdf, 0, 0.  Host arrays. */
 int slrgpu_bsdf_query(int kind, const float* spec0, const float* spec1, const float* spec2, float alpha_x,
                       float alpha_y, const float* queries, uint32_t n, float* out);
+
+/* Medium queries on the GPU on segments inside the committed scene's
+ * density-grid medium, with the free-path sampler replaying given 32-bit
+ * values as uniforms (value >> 9 as the mantissa, as the reference's
+ * RandomNumberGenerator::getFloat0cTo1o; 0x80000000 once a query's values run
+ * out).  mode 0: DensityGridMediumDistribution::interact
+ * (DensityGridMediumDistribution.cpp:402-575), 1: ::evaluateTransmittance
+ * (:577-744), 2: ::evaluateExtinctionCoefficient at the normalised position
+ * rays[0..2] (:756-759); 3 and 4: MediumObjectAggregate::interact /
+ * ::evaluateTransmittance (medium_object.cpp:287-402), which walk the
+ * medium's boundary crossings, on segments anywhere.  rays: n x 8 (org.xyz, dist_min, dir.xyz, dist_max);
+ * lambdas: n x 16 wavelengths; sel: n (selected index, | 0x100 when the
+ * wavelength is already selected); vals: n x num_vals; out: n x 24 (hit,
+ * distance, normalised position xyz, values drawn, spectrum[16], 0, 0).
+ * Host arrays. */
+int slrgpu_medium_query(slrgpu_handle scene, int mode, uint32_t n, const float* rays, const float* lambdas,
+                        const int* sel, const uint32_t* vals, uint32_t num_vals, float* out);
 
 /* Diagnostics (host side, no GPU needed) ------------------------------ */
 /* Builds the SBVH and the other host tables without uploading

@@ -55,6 +55,7 @@ def lib():
             "ora_bsdf_query": (I, [I, fp, fp, fp, F, F, fp, I, fp]),
             "ora_spectrum_eval": (I, [P, I, fp, I, fp]),
             "ora_dropped_samples": (C.c_ulonglong, []),
+            "ora_medium_query": (I, [P, I, I, fp, fp, C.POINTER(C.c_int), up, I, fp]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -204,6 +205,23 @@ class RefScene:
         out = np.zeros_like(lam)
         lib().ora_spectrum_eval(self.h, self.spectrum_ids[spectrum_index], lp, len(lam),
                                 out.ctypes.data_as(C.POINTER(C.c_float)))
+        return out
+
+    def medium_query(self, mode: int, rays: np.ndarray, lambdas: np.ndarray, sel: np.ndarray,
+                     vals: np.ndarray) -> np.ndarray:
+        """DensityGridMediumDistribution interact (0) / evaluateTransmittance
+        (1) / evaluateExtinctionCoefficient (2) with the free-path sampler
+        replaying `vals` (see ora_medium_query in ref_driver.cpp for the
+        layouts); returns n x 24 floats."""
+        r, rp = _f(rays.reshape(-1, 8))
+        lam, lp = _f(lambdas.reshape(-1, 16))
+        sl = np.ascontiguousarray(sel, np.int32)
+        v, vp = _u(vals.reshape(len(r), -1))
+        out = np.zeros((len(r), 24), np.float32)
+        rc = lib().ora_medium_query(self.h, int(mode), len(r), rp, lp, sl.ctypes.data_as(C.POINTER(C.c_int)), vp,
+                                    v.shape[1], out.ctypes.data_as(C.POINTER(C.c_float)))
+        if rc != 0:
+            raise RuntimeError("scene has no medium")
         return out
 
 

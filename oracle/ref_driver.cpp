@@ -49,6 +49,7 @@
 #include "Scene/TriangleMeshNode.h"
 #include "Scene/camera_nodes.h"
 #include "Scene/medium_nodes.h"
+#include "MediumDistribution/DensityGridMediumDistribution.h"
 #include "Texture/constant_textures.h"
 #include "Texture/image_textures.h"
 #include "SurfaceMaterial/basic_surface_materials.h"
@@ -60,6 +61,7 @@
 #include "Renderer/VolumetricPTRenderer.h"
 #include "MediumMaterial/basic_medium_materials.h"
 #include "Core/medium_material.h"
+#include "Core/medium_object.h"
 
 extern "C" unsigned int slr_oracle_max_depth = 100;
 std::atomic<unsigned long long> slr_oracle_dropped_samples(0);
@@ -100,6 +102,12 @@ namespace {
         std::vector<std::unique_ptr<MediumNode>> mediumNodes;
         std::vector<std::unique_ptr<MediumMaterial>> mediumMaterials;
         std::vector<std::vector<float>> densitySlices;   // must outlive the medium node
+        // The medium's distribution again, standalone, for medium queries.
+        int medSigmaS = -1, medSigmaE = -1, medN[3] = {0, 0, 0};
+        float medBmin[3], medBmax[3];
+        std::unique_ptr<DensityGridMediumDistribution> medDist;
+        std::unique_ptr<SingleMediumObject> medObj;
+        std::unique_ptr<MediumObjectAggregate> medAgg;
         std::unique_ptr<Scene> scene;
         bool built = false;
         // Standalone SBVH over the same surface objects, for ray queries.
@@ -267,6 +275,10 @@ int ora_medium_density_grid(void* p, const float* bmin, const float* bmax, int s
                                                             s->densitySlices, nx, ny, nz, s->mediumMaterials.back().get());
     s->mediumNodes.emplace_back(node);
     s->root->addChildNode(node);
+    s->medSigmaS = sigmaS;
+    s->medSigmaE = sigmaE;
+    s->medN[0] = nx; s->medN[1] = ny; s->medN[2] = nz;
+    for (int i = 0; i < 3; ++i) { s->medBmin[i] = bmin[i]; s->medBmax[i] = bmax[i]; }
     return 0;
 }
 
@@ -472,6 +484,124 @@ int ora_bsdf_query(int kind, const float* spec0, const float* spec1, const float
         for (int k = 0; k < 16; ++k) oi[21 + k] = fe[k];
         oi[37] = bsdf->evaluatePDF(query, ed);
         oi[38] = 0.0f; oi[39] = 0.0f;
+    }
+    return 0;
+}
+
+}  // extern "C"
+
+namespace {
+// An RNG that replays a given stream of 32-bit values (then 0x80000000), so
+// that the medium routines draw exactly the uniforms a test hands them; it
+// stands in for the XORShift generator behind FreePathSampler
+// (Core/light_path_sampler.h:55-61).
+class ReplayRNG : public XORShiftRNG {
+public:
+    const uint32_t* vals = nullptr;
+    uint32_t n = 0, used = 0;
+    uint32_t getUInt() override {
+        uint32_t v = used < n ? vals[used] : 0x80000000u;
+        ++used;
+        return v;
+    }
+};
+
+class ReplayPathSampler : public LightPathSampler {
+public:
+    ReplayRNG rng;
+    AlphaTestSampler alphaSampler;
+    FreePathSampler freeSampler;
+    ReplayPathSampler() : alphaSampler(rng), freeSampler(rng) { }
+    float f() { return rng.getFloat0cTo1o(); }
+    float getTimeSample(float b, float e) override { float v = f(); return b * (1 - v) + e * v; }
+    PixelPosition getPixelPositionSample(uint32_t x, uint32_t y) override { float a = f(); return PixelPosition(x + a, y + f()); }
+    float getWavelengthSample() override { return f(); }
+    float getWLSelectionSample() override { return f(); }
+    LensPosSample getLensPosSample() override { float a = f(); return LensPosSample(a, f()); }
+    IDFSample getIDFSample() override { float a = f(); return IDFSample(a, f()); }
+    BSDFSample getBSDFSample() override { float a = f(), b = f(); return BSDFSample(a, b, f()); }
+    PFSample getPFSample() override { float a = f(); return PFSample(a, f()); }
+    AlphaTestSampler &getAlphaTestSampler() override { return alphaSampler; }
+    FreePathSampler &getFreePathSampler() override { return freeSampler; }
+    float getPathTerminationSample() override { return f(); }
+    float getLightSelectionSample() override { return f(); }
+    SurfaceLightPosSample getSurfaceLightPosSample() override { float a = f(); return SurfaceLightPosSample(a, f()); }
+    VolumetricLightPosSample getVolumetricLightPosSample() override { float a = f(), b = f(); return VolumetricLightPosSample(a, b, f()); }
+    EDFSample getEDFSample() override { float a = f(), b = f(); return EDFSample(a, b, f()); }
+};
+}  // namespace
+
+extern "C" {
+
+// Medium queries on one segment inside the density-grid medium, with the
+// free-path sampler replaying given uniforms.  mode 0:
+// DensityGridMediumDistribution::interact (DensityGridMediumDistribution.cpp:402-575),
+// mode 1: ::evaluateTransmittance (:577-744), mode 2: the extinction
+// coefficient at a normalised position (rays[0..2]) (:756-759); modes 3 and
+// 4: interact / evaluateTransmittance of the medium aggregate
+// (Core/medium_object.cpp:287-402), which walks the medium's boundary
+// crossings, on any segment.
+// rays: n x 8 (org.xyz, distMin, dir.xyz, distMax); lambdas: n x 16;
+// sel: n (selected index | 0x100 if the wavelength is already selected);
+// vals: n x nvals uint32; out: n x 24 (hit, dist, param.xyz, values used,
+// spectrum[16], 0, 0).
+int ora_medium_query(void* p, int mode, int n, const float* rays, const float* lambdas, const int* sel,
+                     const uint32_t* vals, int nvals, float* out) {
+    OraScene* s = (OraScene*)p;
+    if (s->medSigmaE < 0) return -1;
+    if (!s->medDist) {
+        BoundingBox3D region(Point3D(s->medBmin[0], s->medBmin[1], s->medBmin[2]),
+                             Point3D(s->medBmax[0], s->medBmax[1], s->medBmax[2]));
+        s->medDist.reset(new DensityGridMediumDistribution(region, s->spectra.at(s->medSigmaS).get(),
+                                                           s->spectra.at(s->medSigmaE).get(), s->densitySlices,
+                                                           s->medN[0], s->medN[1], s->medN[2]));
+    }
+    if (!s->medAgg) {
+        s->medObj.reset(new SingleMediumObject(s->medDist.get(), s->mediumMaterials.back().get()));
+        std::vector<MediumObject*> objs{s->medObj.get()};
+        s->medAgg.reset(new MediumObjectAggregate(objs));
+    }
+    const DensityGridMediumDistribution* md = s->medDist.get();
+    const MediumObjectAggregate* agg = s->medAgg.get();
+    for (int i = 0; i < n; ++i) {
+        const float* r = rays + 8 * (size_t)i;
+        float* o = out + 24 * (size_t)i;
+        std::memset(o, 0, 24 * sizeof(float));
+        WavelengthSamples wls(lambdas + 16 * (size_t)i);
+        wls.selectedLambdaIndex = (uint16_t)(sel[i] & 0xff);
+        wls.flags = (sel[i] & 0x100) ? WavelengthSamples::WavelengthIsSelected : 0;
+        ReplayPathSampler ps;
+        ps.rng.vals = vals + (size_t)nvals * i;
+        ps.rng.n = (uint32_t)nvals;
+        Ray ray(Point3D(r[0], r[1], r[2]), Vector3D(r[4], r[5], r[6]), 0.0f);
+        RaySegment seg(r[3], r[7]);
+        SampledSpectrum v;
+        bool single = false;
+        if (mode == 0) {
+            MediumInteraction mi;
+            bool hit = md->interact(ray, seg, wls, ps, &mi, &v, &single);
+            o[0] = hit ? 1.0f : 0.0f;
+            if (hit) {
+                o[1] = mi.getDistance();
+                mi.getMediumParameter(&o[2], &o[3], &o[4]);
+            }
+        } else if (mode == 1) {
+            v = md->evaluateTransmittance(ray, seg, wls, ps, &single);
+        } else if (mode == 3) {
+            MediumInteraction mi;
+            bool hit = agg->interact(ray, seg, wls, ps, &mi, &v, &single);
+            o[0] = hit ? 1.0f : 0.0f;
+            if (hit) {
+                o[1] = mi.getDistance();
+                mi.getMediumParameter(&o[2], &o[3], &o[4]);
+            }
+        } else if (mode == 4) {
+            v = agg->evaluateTransmittance(ray, seg, wls, ps, &single);
+        } else {
+            v = md->evaluateExtinctionCoefficient(Point3D(r[0], r[1], r[2]), wls);
+        }
+        o[5] = (float)ps.rng.used;
+        for (int k = 0; k < 16; ++k) o[6 + k] = v[k];
     }
     return 0;
 }

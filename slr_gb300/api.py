@@ -112,6 +112,7 @@ def lib():
             "slrgpu_scene_reupload": (I, [H, C.POINTER(C.c_uint64)]),
             "slrgpu_render_noalloc": (I, [H, C.POINTER(Settings), P, P]),
             "slrgpu_render_noalloc_scratch_bytes": (C.c_uint64, []),
+            "slrgpu_medium_query": (I, [H, I, U, fp, fp, ip, up, U, fp]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -345,6 +346,20 @@ class Scene:
         out = np.zeros_like(lam)
         check(lib().slrgpu_spectrum_evaluate(self.handle, self.spectrum_ids[spectrum_index], _fp(lam), len(lam),
                                              _fp(out)))
+        return out
+
+    def medium_query(self, mode: int, rays: np.ndarray, lambdas: np.ndarray, sel: np.ndarray,
+                     vals: np.ndarray) -> np.ndarray:
+        """GPU medium queries with replayed uniforms (slrgpu_medium_query):
+        mode 0 free-path sampling, 1 transmittance, 2 extinction coefficient;
+        returns n x 24 floats."""
+        r = np.ascontiguousarray(rays, np.float32).reshape(-1, 8)
+        lam = np.ascontiguousarray(lambdas, np.float32).reshape(-1, 16)
+        sl = np.ascontiguousarray(sel, np.int32)
+        v = np.ascontiguousarray(vals, np.uint32).reshape(len(r), -1)
+        out = np.zeros((len(r), 24), np.float32)
+        check(lib().slrgpu_medium_query(self.handle, int(mode), len(r), _fp(r), _fp(lam),
+                                        sl.ctypes.data_as(C.POINTER(C.c_int)), _up(v), v.shape[1], _fp(out)))
         return out
 
     def environment_tables(self):

@@ -427,6 +427,18 @@ int slrgpu_bsdf_query(int kind, const float* spec0, const float* spec1, const fl
     return bsdfQuery(kind, spec0, spec1, spec2, alpha_x, alpha_y, queries, n, out);
 }
 
+int slrgpu_medium_query(slrgpu_handle scene, int mode, uint32_t n, const float* rays, const float* lambdas,
+                        const int* sel, const uint32_t* vals, uint32_t num_vals, float* out) {
+    const bool mutating = false;
+    GET_SCENE(s, scene);
+    if (!s->committed) return fail(SLRGPU_ERR_NOT_COMMITTED, "scene not committed");
+    if (n > 0 && (!rays || !lambdas || !sel || !out || (num_vals > 0 && !vals)))
+        return fail(SLRGPU_ERR_INVALID_ARGUMENT, "NULL argument");
+    cudaError_t e = cudaSetDevice(s->ctx->device);
+    if (e != cudaSuccess) return fail(SLRGPU_ERR_CUDA, cudaGetErrorString(e));
+    return mediumQuery(s->dev, mode, n, rays, lambdas, sel, vals, num_vals, out);
+}
+
 // ---- host-side diagnostics ----------------------------------------------------
 int slrgpu_scene_sbvh_dump(slrgpu_handle scene, float* boxes, uint32_t* words, uint32_t* leaf_prims) {
     const bool mutating = false;

@@ -38,6 +38,21 @@ __device__ __forceinline__ V3 rn_cross(V3 a, V3 b) {
               __fsub_rn(__fmul_rn(a.x, b.y), __fmul_rn(a.y, b.x))};
 }
 __device__ __forceinline__ V3 rn_sub(V3 a, V3 b) { return V3{__fsub_rn(a.x, b.x), __fsub_rn(a.y, b.y), __fsub_rn(a.z, b.z)}; }
+// org + dir * t, each product and sum rounded on its own.  Points on a light
+// (hit points, sampled light positions) must round as the reference does:
+// whether a point on an emitter lands exactly in the emitter's plane decides
+// whether next-event estimation from it divides zero by zero, and a fused
+// multiply-add lands there more often.
+__device__ __forceinline__ V3 rn_ray_point(V3 org, V3 dir, float t) {
+    return V3{__fadd_rn(org.x, __fmul_rn(dir.x, t)), __fadd_rn(org.y, __fmul_rn(dir.y, t)),
+              __fadd_rn(org.z, __fmul_rn(dir.z, t))};
+}
+// b0 * p0 + b1 * p1 + b2 * p2, left to right, without contraction.
+__device__ __forceinline__ V3 rn_bary(float b0, V3 p0, float b1, V3 p1, float b2, V3 p2) {
+    return V3{__fadd_rn(__fadd_rn(__fmul_rn(b0, p0.x), __fmul_rn(b1, p1.x)), __fmul_rn(b2, p2.x)),
+              __fadd_rn(__fadd_rn(__fmul_rn(b0, p0.y), __fmul_rn(b1, p1.y)), __fmul_rn(b2, p2.y)),
+              __fadd_rn(__fadd_rn(__fmul_rn(b0, p0.z), __fmul_rn(b1, p1.z)), __fmul_rn(b2, p2.z))};
+}
 
 struct Frame {
     V3 x, y, z;

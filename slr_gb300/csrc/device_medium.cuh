@@ -216,8 +216,9 @@ __device__ __noinline__ bool svTraverse(const DevMedium &m, V3 org, V3 dir, floa
 // estimator.  Returns true on a real collision at *tHit (param = normalised
 // position).  thr receives the medium throughput (already divided by the
 // extinction coefficient at the collision).
+template <class R>
 __device__ __noinline__ bool mediumInteractSegment(const DevMedium &m, V3 org, V3 dir, float dmin, float dmax,
-                                                   const Spec &sigmaE, int sel, bool wlSelected, Rng &rng,
+                                                   const Spec &sigmaE, int sel, bool wlSelected, R &rng,
                                                    float* tHit, V3* param, Spec &thr) {
     SvSetup s;
     svSetup(m, org, dir, dmin, s);
@@ -279,8 +280,9 @@ __device__ __noinline__ bool mediumInteractSegment(const DevMedium &m, V3 org, V
 
 // Ratio-tracking transmittance with Russian roulette below 0.1
 // (DensityGridMediumDistribution.cpp:577-744).
+template <class R>
 __device__ __noinline__ void mediumTransmittanceSegment(const DevMedium &m, V3 org, V3 dir, float dmin, float dmax,
-                                                        const Spec &sigmaE, int sel, bool wlSelected, Rng &rng,
+                                                        const Spec &sigmaE, int sel, bool wlSelected, R &rng,
                                                         Spec &T) {
     SvSetup s;
     svSetup(m, org, dir, dmin, s);
@@ -313,8 +315,9 @@ __device__ __noinline__ void mediumTransmittanceSegment(const DevMedium &m, V3 o
 
 // MediumObjectAggregate::interact for one medium (medium_object.cpp:287-348):
 // walks boundary crossings of the medium box within [dmin, dmax).
+template <class R>
 __device__ __forceinline__ bool mediumInteract(const DevMedium &m, V3 org, V3 dir, float dmin, float dmax,
-                                               const Spec &sigmaE, int sel, bool wlSelected, Rng &rng, float* tHit,
+                                               const Spec &sigmaE, int sel, bool wlSelected, R &rng, float* tHit,
                                                V3* param, Spec &thr) {
     thr = specConst(1.0f);
     float rmin = dmin;
@@ -346,8 +349,9 @@ __device__ __forceinline__ bool mediumInteract(const DevMedium &m, V3 org, V3 di
 }
 
 // MediumObjectAggregate::evaluateTransmittance for one medium (:350-402).
+template <class R>
 __device__ __forceinline__ void mediumTransmittance(const DevMedium &m, V3 org, V3 dir, float dmin, float dmax,
-                                                    const Spec &sigmaE, int sel, bool wlSelected, Rng &rng, Spec &T) {
+                                                    const Spec &sigmaE, int sel, bool wlSelected, R &rng, Spec &T) {
     T = specConst(1.0f);
     float rmin = dmin;
     bool inside = mediumContains(m, org + rmin * dir);

@@ -55,8 +55,20 @@ struct WaveState {
     uint32_t N;
 };
 
+// The reference's renderers sample the sensor in whole 8x8 tiles
+// (ImageSensor.cpp:13-14, :42-43; PTRenderer.cpp:104-110), also where a tile
+// hangs over the image's right or bottom edge; ImageSensor::add
+// (ImageSensor.cpp:125-130) clamps those samples into the last column / row.
+// A wave therefore traces every position of the tile-padded sample grid.
+constexpr uint32_t kSensorTile = 8;
+__host__ __device__ __forceinline__ uint32_t padToTile(uint32_t n) {
+    return (n + kSensorTile - 1) / kSensorTile * kSensorTile;
+}
+
 struct WaveParams {
-    uint32_t width, height, numPixels;
+    uint32_t width, height;   // image
+    uint32_t gridW, gridH;    // tile-padded sample grid
+    uint32_t numPixels;       // gridW * gridH sample positions per sample index
     uint32_t samplesInWave;   // S
     uint32_t sampleBase;      // first sample index of the wave
     uint32_t numPaths;
@@ -227,7 +239,7 @@ __global__ void kRaygen(DevScene sc, WaveState ws, WaveParams wp) {
     for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < wp.numPaths; p += gridDim.x * blockDim.x) {
         uint32_t s = p / wp.numPixels;
         uint32_t pixel = p - s * wp.numPixels;
-        uint32_t ix = pixel % wp.width, iy = pixel / wp.width;
+        uint32_t ix = pixel % wp.gridW, iy = pixel / wp.gridW;
         Rng rng{pathKey(wp.seed, (uint64_t)(wp.sampleBase + s) * wp.numPixels + pixel), 0};
         // Draw order of Job::kernel: time, pixel (2), wavelength offset,
         // wavelength selection, lens (2) (PTRenderer.cpp:108-116).
@@ -296,7 +308,7 @@ struct SurfPoint {
 // shading normal, tangent made orthogonal to it, geometric normal.
 __device__ __forceinline__ void surfacePoint(const DevScene &sc, const DevPrim &pr, V3 org, V3 dir, float t, float mb1,
                                              float mb2, SurfPoint &sp) {
-    sp.p = org + dir * t;
+    sp.p = rn_ray_point(org, dir, t);   // TriangleSurfaceShape.cpp:250
     float b0 = 1.0f - mb1 - mb2;
     float b1 = mb1;
     float b2 = 1.0f - b0 - b1;
@@ -448,7 +460,7 @@ __global__ void __launch_bounds__(256) kShade(DevScene sc, WaveState ws, WavePar
                             float b0 = 1.0f - su, b1 = lu1 * su, b2 = 1.0f - b0 - b1;
                             float4 p0 = sc.vpos[lpr.v0], p1 = sc.vpos[lpr.v1], p2 = sc.vpos[lpr.v2];
                             V3 P0 = V3{p0.x, p0.y, p0.z}, P1 = V3{p1.x, p1.y, p1.z}, P2 = V3{p2.x, p2.y, p2.z};
-                            lp = b0 * P0 + b1 * P1 + b2 * P2;
+                            lp = rn_bary(b0, P0, b1, P1, b2, P2);
                             float4 n0 = sc.vnrm[lpr.v0], n1 = sc.vnrm[lpr.v1], n2 = sc.vnrm[lpr.v2];
                             V3 lz = normalize(b0 * V3{n0.x, n0.y, n0.z} + b1 * V3{n1.x, n1.y, n1.z} + b2 * V3{n2.x, n2.y, n2.z});
                             lgn = V3{lpr.ngx, lpr.ngy, lpr.ngz};
@@ -659,7 +671,7 @@ __global__ void __launch_bounds__(256) kShadeVol(DevScene sc, WaveState ws, Wave
             float hitInvArea = 0.0f;
             if (medHit) {
                 isMedium = true;
-                P = org + tMed * dir;
+                P = rn_ray_point(org, dir, tMed);
                 frame = frameFromZ(normalize(dir));
                 float dens = mediumDensity(med, mparam);
 #pragma unroll
@@ -764,7 +776,7 @@ __global__ void __launch_bounds__(256) kShadeVol(DevScene sc, WaveState ws, Wave
                         float su = sqrtf(lu0);
                         float b0 = 1.0f - su, b1 = lu1 * su, b2 = 1.0f - b0 - b1;
                         float4 p0 = sc.vpos[lpr.v0], p1 = sc.vpos[lpr.v1], p2 = sc.vpos[lpr.v2];
-                        lp = b0 * V3{p0.x, p0.y, p0.z} + b1 * V3{p1.x, p1.y, p1.z} + b2 * V3{p2.x, p2.y, p2.z};
+                        lp = rn_bary(b0, V3{p0.x, p0.y, p0.z}, b1, V3{p1.x, p1.y, p1.z}, b2, V3{p2.x, p2.y, p2.z});
                         float4 n0 = sc.vnrm[lpr.v0], n1 = sc.vnrm[lpr.v1], n2 = sc.vnrm[lpr.v2];
                         V3 lz = normalize(b0 * V3{n0.x, n0.y, n0.z} + b1 * V3{n1.x, n1.y, n1.z} + b2 * V3{n2.x, n2.y, n2.z});
                         lgn = V3{lpr.ngx, lpr.ngy, lpr.ngz};
@@ -924,7 +936,7 @@ __global__ void kShadowVol(DevScene sc, WaveState ws, WaveParams wp, const uint3
 // SpectrumStorage::add (spectrum_types.h:716-739, CompensatedSum.h:16-33).
 __global__ void kAccumulate(WaveState ws, WaveParams wp, float* filmSum, float* filmComp) {
     const float recBinWidth = kNumLambda / (kWavelengthHigh - kWavelengthLow);
-    const uint32_t P = wp.numPixels;
+    const uint32_t P = wp.width * wp.height;
     unsigned long long dropped = 0;
     for (uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x; pix < P; pix += gridDim.x * blockDim.x) {
         float sum[kNumLambda], comp[kNumLambda];
@@ -933,8 +945,15 @@ __global__ void kAccumulate(WaveState ws, WaveParams wp, float* filmSum, float* 
             sum[b] = filmSum[(size_t)b * P + pix];
             comp[b] = filmComp[(size_t)b * P + pix];
         }
-        for (uint32_t s = 0; s < wp.samplesInWave; ++s) {
-            uint32_t p = s * P + pix;
+        // Grid positions clamped into this pixel: itself, plus the overhang
+        // of the last column / row.
+        const uint32_t x = pix % wp.width, y = pix / wp.width;
+        const uint32_t xEnd = x + 1 == wp.width ? wp.gridW : x + 1;
+        const uint32_t yEnd = y + 1 == wp.height ? wp.gridH : y + 1;
+        for (uint32_t s = 0; s < wp.samplesInWave; ++s)
+        for (uint32_t gy = y; gy < yEnd; ++gy)
+        for (uint32_t gx = x; gx < xEnd; ++gx) {
+            const uint32_t p = s * wp.numPixels + gy * wp.gridW + gx;
             float w = ws.camWeight[p];
             float c[kNumLambda];
             bool finite = true;
@@ -1002,6 +1021,82 @@ __global__ void kTrace(DevScene sc, const float* __restrict__ rays, uint32_t n, 
 
 // BSDF queries at fixed inputs (16 floats in, 40 out per query; the layout of
 // slrgpu_bsdf_query in include/slrgpu.h).
+// Replays a given stream of 32-bit values as uniforms (then 0x80000000), with
+// the reference's 23-bit conversion, so that medium queries draw exactly the
+// uniforms a test hands them.
+struct ReplayRng {
+    const uint32_t* vals;
+    uint32_t n;
+    uint32_t counter;
+    __device__ float next() {
+        uint32_t v = counter < n ? vals[counter] : 0x80000000u;
+        ++counter;
+        return __uint_as_float((v >> 9) | 0x3f800000u) - 1.0f;
+    }
+};
+
+// One medium query per thread: on a segment inside the medium, mode 0
+// free-path sampling (DensityGridMediumDistribution::interact), 1
+// transmittance (::evaluateTransmittance), 2 extinction coefficient at a
+// normalised position (::evaluateExtinctionCoefficient); on any segment, 3
+// and 4 the same through the boundary walk of MediumObjectAggregate.
+// Layouts as slrgpu_medium_query.
+__global__ void kMediumQuery(DevScene sc, int mode, uint32_t n, const float* __restrict__ rays,
+                             const float* __restrict__ lambdasIn, const int* __restrict__ selIn,
+                             const uint32_t* __restrict__ vals, uint32_t nvals, float* __restrict__ out) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float* r = rays + 8 * (size_t)i;
+        float* o = out + 24 * (size_t)i;
+        float lambdas[kNumLambda];
+#pragma unroll
+        for (int k = 0; k < kNumLambda; ++k) lambdas[k] = lambdasIn[16 * (size_t)i + k];
+        const int sel = selIn[i] & 0xff;
+        const bool wlSelected = (selIn[i] & 0x100) != 0;
+        Spec sigmaE;
+        evalSpectrum(sc, sc.medium.sigmaE, lambdas, sigmaE);
+        ReplayRng rng{vals + (size_t)nvals * i, nvals, 0};
+        V3 org = V3{r[0], r[1], r[2]}, dir = V3{r[4], r[5], r[6]};
+        Spec v = specConst(0.0f);
+        float hit = 0.0f, dist = 0.0f;
+        V3 param = V3{0.0f, 0.0f, 0.0f};
+        if (mode == 0) {
+            float t;
+            V3 pr;
+            if (mediumInteractSegment(sc.medium, org, dir, r[3], r[7], sigmaE, sel, wlSelected, rng, &t, &pr, v)) {
+                hit = 1.0f;
+                dist = t;
+                param = pr;
+            }
+        } else if (mode == 1) {
+            mediumTransmittanceSegment(sc.medium, org, dir, r[3], r[7], sigmaE, sel, wlSelected, rng, v);
+        } else if (mode == 3) {
+            float t;
+            V3 pr;
+            if (mediumInteract(sc.medium, org, dir, r[3], r[7], sigmaE, sel, wlSelected, rng, &t, &pr, v)) {
+                hit = 1.0f;
+                dist = t;
+                param = pr;
+            }
+        } else if (mode == 4) {
+            mediumTransmittance(sc.medium, org, dir, r[3], r[7], sigmaE, sel, wlSelected, rng, v);
+        } else {
+            float d = mediumDensity(sc.medium, org);
+#pragma unroll
+            for (int k = 0; k < kNumLambda; ++k) v.v[k] = d * sigmaE.v[k];
+        }
+        o[0] = hit;
+        o[1] = dist;
+        o[2] = param.x;
+        o[3] = param.y;
+        o[4] = param.z;
+        o[5] = (float)rng.counter;
+#pragma unroll
+        for (int k = 0; k < kNumLambda; ++k) o[6 + k] = v.v[k];
+        o[22] = 0.0f;
+        o[23] = 0.0f;
+    }
+}
+
 __global__ void kBsdfQuery(Bsdf B, const float* __restrict__ q, uint32_t n, float* __restrict__ o) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const float* qi = q + 16 * (size_t)i;
@@ -1202,6 +1297,127 @@ static int gridFor(const void* kernel, int block) {
     return std::max(1, sms * std::max(1, perSM));
 }
 
+// Persistent grid sizes (resident blocks per SM x SMs) of the wave kernels,
+// computed once per process.
+struct WaveGrids {
+    int raygen, extend, shade, shadow, accumulate, shadeVol, shadowVol;
+};
+static const WaveGrids &waveGrids(int block) {
+    static WaveGrids g;
+    static std::once_flag once;
+    std::call_once(once, [&]() {
+        g.raygen = gridFor((const void*)kRaygen, block);
+        g.extend = gridFor((const void*)kExtend, block);
+        g.shade = gridFor((const void*)kShade, block);
+        g.shadow = gridFor((const void*)kShadow, block);
+        g.accumulate = gridFor((const void*)kAccumulate, block);
+        g.shadeVol = gridFor((const void*)kShadeVol, block);
+        g.shadowVol = gridFor((const void*)kShadowVol, block);
+    });
+    return g;
+}
+
+// Optional per-launch timing of the wave kernels by kernel class.
+struct LaunchMarks {
+    std::vector<cudaEvent_t>* pool = nullptr;   // null: no timing
+    cudaStream_t stream = 0;
+    struct Mark { int cls; size_t ev; };
+    std::vector<Mark> marks;
+    size_t used = 0;
+    cudaEvent_t next() {
+        if (used == pool->size()) {
+            cudaEvent_t e;
+            cudaEventCreate(&e);
+            pool->push_back(e);
+        }
+        return (*pool)[used++];
+    }
+    void begin(int cls) {
+        if (!pool) return;
+        marks.push_back(Mark{cls, used});
+        cudaEventRecord(next(), stream);
+    }
+    void end() {
+        if (pool) cudaEventRecord(next(), stream);
+    }
+};
+
+// Sample grid and wave size of a render: every position of the tile-padded
+// grid is one path per sample index; a wave holds S sample indices.
+struct WavePlan {
+    uint32_t gridW, gridH, gridPositions, filmPixels, S;
+};
+static WavePlan planWaves(const slrgpu_settings &s, uint32_t autoPaths) {
+    WavePlan pl;
+    pl.gridW = padToTile(s.width);
+    pl.gridH = padToTile(s.height);
+    pl.gridPositions = pl.gridW * pl.gridH;
+    pl.filmPixels = s.width * s.height;
+    uint32_t S = s.samples_per_wave;
+    if (S == 0) S = std::max(1u, autoPaths / pl.gridPositions);
+    pl.S = std::min(S, s.spp);
+    return pl;
+}
+
+// The wave loop shared by slrgpu_render and slrgpu_render_noalloc: per wave,
+// camera rays for S samples of every grid position, then per bounce
+// extension, shading and shadow kernels over the queues, then the film.
+// Stream-ordered; counters, queues and path state live in w.  Returns the
+// number of kernel launches.
+static uint64_t runWaves(const DeviceScene &ds, const slrgpu_settings &s, const WavePlan &pl, const WaveState &w,
+                         float* filmSum, float* filmComp, cudaStream_t stream, LaunchMarks &lm) {
+    const int block = 256;
+    const WaveGrids &g = waveGrids(block);
+    const uint32_t D = s.max_depth;
+    uint64_t launches = 0;
+    for (uint32_t base = 0; base < s.spp; base += pl.S) {
+        WaveParams wp;
+        wp.width = s.width;
+        wp.height = s.height;
+        wp.gridW = pl.gridW;
+        wp.gridH = pl.gridH;
+        wp.numPixels = pl.gridPositions;
+        wp.samplesInWave = std::min(pl.S, s.spp - base);
+        wp.sampleBase = base;
+        wp.numPaths = wp.samplesInWave * pl.gridPositions;
+        wp.maxDepth = D;
+        wp.seed = s.seed;
+        cudaMemsetAsync(w.counters, 0, 3 * (size_t)(D + 2) * sizeof(uint32_t), stream);
+        lm.begin(SLRGPU_KERNEL_RAYGEN);
+        kRaygen<<<g.raygen, block, 0, stream>>>(ds.sc, w, wp);
+        lm.end();
+        ++launches;
+        for (uint32_t b = 0; b <= D; ++b) {
+            uint32_t* inCount = w.counters + b;
+            uint32_t* outCount = w.counters + b + 1;
+            uint32_t* shCount = w.counters + (D + 2) + b;
+            lm.begin(SLRGPU_KERNEL_EXTEND);
+            kExtend<<<g.extend, block, 0, stream>>>(ds.sc, w, w.queue[b & 1], inCount);
+            lm.end();
+            lm.begin(SLRGPU_KERNEL_SHADE);
+            if (s.volumetric)
+                kShadeVol<<<g.shadeVol, block, 0, stream>>>(ds.sc, w, wp, w.queue[b & 1], inCount,
+                                                            w.queue[(b + 1) & 1], outCount, w.shadowQueue, shCount);
+            else
+                kShade<<<g.shade, block, 0, stream>>>(ds.sc, w, wp, w.queue[b & 1], inCount, w.queue[(b + 1) & 1],
+                                                      outCount, w.shadowQueue, shCount);
+            lm.end();
+            lm.begin(SLRGPU_KERNEL_SHADOW);
+            if (s.volumetric)
+                kShadowVol<<<g.shadowVol, block, 0, stream>>>(ds.sc, w, wp, w.shadowQueue, shCount, b);
+            else
+                kShadow<<<g.shadow, block, 0, stream>>>(ds.sc, w, w.shadowQueue, shCount);
+            lm.end();
+            launches += 3;
+        }
+        lm.begin(SLRGPU_KERNEL_ACCUMULATE);
+        kAccumulate<<<g.accumulate, block, 0, stream>>>(w, wp, filmSum, filmComp);
+        lm.end();
+        ++launches;
+    }
+    return launches;
+}
+
 int RenderEngine::render(const DeviceScene &ds, const slrgpu_settings &s, float* film, bool filmOnDevice,
                          slrgpu_render_stats* stats, cudaStream_t stream) {
     auto t0 = std::chrono::steady_clock::now();
@@ -1213,11 +1429,13 @@ int RenderEngine::render(const DeviceScene &ds, const slrgpu_settings &s, float*
         setError("max_depth must be <= 1000");
         return SLRGPU_ERR_INVALID_ARGUMENT;
     }
-    const uint32_t P = s.width * s.height;
-    uint32_t S = s.samples_per_wave;
-    if (S == 0) S = std::max(1u, std::min(s.spp, (uint32_t)((4u << 20) / std::max(1u, P))));
-    S = std::min(S, s.spp);
-    const uint64_t Nwant = (uint64_t)S * P;
+    if ((uint64_t)padToTile(s.width) * padToTile(s.height) > 0x7fffffffull) {
+        setError("image too large");
+        return SLRGPU_ERR_INVALID_ARGUMENT;
+    }
+    const WavePlan pl = planWaves(s, 4u << 20);
+    const uint32_t P = pl.filmPixels;
+    const uint64_t Nwant = (uint64_t)pl.S * pl.gridPositions;
     if (Nwant > 0x7fffffffull) {
         setError("paths per wave exceed 2^31");
         return SLRGPU_ERR_INVALID_ARGUMENT;
@@ -1238,91 +1456,17 @@ int RenderEngine::render(const DeviceScene &ds, const slrgpu_settings &s, float*
     CUDA_TRY(cudaMemsetAsync(filmSum, 0, (size_t)P * kNumLambda * sizeof(float), stream));
     CUDA_TRY(cudaMemsetAsync(filmComp, 0, (size_t)P * kNumLambda * sizeof(float), stream));
     CUDA_TRY(cudaMemsetAsync(w.stats, 0, 4 * sizeof(unsigned long long), stream));
-    const int block = 256;
-    static int gRaygen = 0, gExtend = 0, gShade = 0, gShadow = 0, gAcc = 0, gShadeVol = 0, gShadowVol = 0;
-    if (!gRaygen) {
-        gRaygen = gridFor((const void*)kRaygen, block);
-        gExtend = gridFor((const void*)kExtend, block);
-        gShade = gridFor((const void*)kShade, block);
-        gShadow = gridFor((const void*)kShadow, block);
-        gAcc = gridFor((const void*)kAccumulate, block);
-        gShadeVol = gridFor((const void*)kShadeVol, block);
-        gShadowVol = gridFor((const void*)kShadowVol, block);
-    }
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     cudaEventRecord(e0, stream);
-    uint64_t launches = 0;
-    const uint32_t D = s.max_depth;
-    // Optional per-launch events for the per-kernel device times.
-    const bool profile = (s.flags & SLRGPU_FLAG_PROFILE_KERNELS) != 0;
-    struct Mark { int cls; size_t ev; };
-    std::vector<Mark> marks;
-    size_t evUsed = 0;
-    auto nextEvent = [&]() -> cudaEvent_t {
-        if (evUsed == eventPool.size()) {
-            cudaEvent_t e;
-            cudaEventCreate(&e);
-            eventPool.push_back(e);
-        }
-        return eventPool[evUsed++];
-    };
-    auto begin = [&](int cls) {
-        if (!profile) return;
-        marks.push_back(Mark{cls, evUsed});
-        cudaEventRecord(nextEvent(), stream);
-    };
-    auto end = [&]() {
-        if (!profile) return;
-        cudaEventRecord(nextEvent(), stream);
-    };
-    for (uint32_t base = 0; base < s.spp; base += S) {
-        WaveParams wp;
-        wp.width = s.width;
-        wp.height = s.height;
-        wp.numPixels = P;
-        wp.samplesInWave = std::min(S, s.spp - base);
-        wp.sampleBase = base;
-        wp.numPaths = wp.samplesInWave * P;
-        wp.maxDepth = D;
-        wp.seed = s.seed;
-        CUDA_TRY(cudaMemsetAsync(w.counters, 0, 3 * (size_t)(D + 2) * sizeof(uint32_t), stream));
-        begin(SLRGPU_KERNEL_RAYGEN);
-        kRaygen<<<gRaygen, block, 0, stream>>>(ds.sc, w, wp);
-        end();
-        ++launches;
-        for (uint32_t b = 0; b <= D; ++b) {
-            uint32_t* inCount = w.counters + b;
-            uint32_t* outCount = w.counters + b + 1;
-            uint32_t* shCount = w.counters + (D + 2) + b;
-            begin(SLRGPU_KERNEL_EXTEND);
-            kExtend<<<gExtend, block, 0, stream>>>(ds.sc, w, w.queue[b & 1], inCount);
-            end();
-            begin(SLRGPU_KERNEL_SHADE);
-            if (s.volumetric)
-                kShadeVol<<<gShadeVol, block, 0, stream>>>(ds.sc, w, wp, w.queue[b & 1], inCount,
-                                                           w.queue[(b + 1) & 1], outCount, w.shadowQueue, shCount);
-            else
-                kShade<<<gShade, block, 0, stream>>>(ds.sc, w, wp, w.queue[b & 1], inCount, w.queue[(b + 1) & 1],
-                                                     outCount, w.shadowQueue, shCount);
-            end();
-            begin(SLRGPU_KERNEL_SHADOW);
-            if (s.volumetric)
-                kShadowVol<<<gShadowVol, block, 0, stream>>>(ds.sc, w, wp, w.shadowQueue, shCount, b);
-            else
-                kShadow<<<gShadow, block, 0, stream>>>(ds.sc, w, w.shadowQueue, shCount);
-            end();
-            launches += 3;
-        }
-        begin(SLRGPU_KERNEL_ACCUMULATE);
-        kAccumulate<<<gAcc, block, 0, stream>>>(w, wp, filmSum, filmComp);
-        end();
-        ++launches;
-    }
+    LaunchMarks lm;
+    lm.stream = stream;
+    if (s.flags & SLRGPU_FLAG_PROFILE_KERNELS) lm.pool = &eventPool;
+    uint64_t launches = runWaves(ds, s, pl, w, filmSum, filmComp, stream, lm);
     CUDA_TRY(cudaGetLastError());
     float* dst = filmOnDevice ? film : filmOut;
-    kFilmToPixelMajor<<<gAcc, block, 0, stream>>>(filmSum, dst, P);
+    kFilmToPixelMajor<<<waveGrids(256).accumulate, 256, 0, stream>>>(filmSum, dst, P);
     ++launches;
     cudaEventRecord(e1, stream);
     if (!filmOnDevice)
@@ -1336,7 +1480,7 @@ int RenderEngine::render(const DeviceScene &ds, const slrgpu_settings &s, float*
     cudaEventDestroy(e1);
     if (stats) {
         std::memset(stats, 0, sizeof(*stats));
-        for (const Mark &m : marks) {
+        for (const LaunchMarks::Mark &m : lm.marks) {
             float kms = 0;
             cudaEventElapsedTime(&kms, eventPool[m.ev], eventPool[m.ev + 1]);
             stats->kernel_ms[m.cls] += kms;
@@ -1344,7 +1488,7 @@ int RenderEngine::render(const DeviceScene &ds, const slrgpu_settings &s, float*
         }
         stats->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
         stats->kernel_seconds = ms * 1e-3;
-        stats->path_samples = (uint64_t)P * s.spp;
+        stats->path_samples = (uint64_t)pl.gridPositions * s.spp;
         stats->extension_rays = hstats[0];
         stats->shadow_rays = hstats[1];
         stats->dropped_samples = hstats[2];
@@ -1359,10 +1503,12 @@ int RenderEngine::render(const DeviceScene &ds, const slrgpu_settings &s, float*
 // For callers that may not allocate device memory once they are running: a
 // real-time loop that owns a fixed memory budget, a host that hands the GPU
 // to the renderer only between its own allocations, or an embedding runtime
-// whose allocator forbids cudaMalloc after start-up.  The path state, queues, counters and the film sums live in
-// one file-scope device array of a fixed size, which every GPU that loads this
-// library keeps until the process exits.  Limits: width * height * samples
-// per wave <= kNoAllocMaxPaths and max_depth <= kNoAllocMaxDepth.
+// whose allocator forbids cudaMalloc after start-up.  The path state, queues,
+// counters and the film sums live in one file-scope device array of a fixed
+// size, which every GPU that loads this library keeps until the process
+// exits.  Limits: the tile-padded sample grid (width and height rounded up to
+// multiples of 8) times the samples per wave <= kNoAllocMaxPaths, and
+// max_depth <= kNoAllocMaxDepth.
 // ---------------------------------------------------------------------------
 constexpr uint32_t kNoAllocMaxPaths = 65536;
 constexpr uint32_t kNoAllocMaxDepth = 64;
@@ -1405,25 +1551,26 @@ int renderNoAlloc(const DeviceScene &ds, const slrgpu_settings &s, float* film, 
         setError("film must be a device pointer");
         return SLRGPU_ERR_INVALID_ARGUMENT;
     }
-    const uint64_t P = (uint64_t)s.width * s.height;
     if (s.width == 0 || s.height == 0 || s.spp == 0) {
         setError("width, height and spp must be positive");
         return SLRGPU_ERR_INVALID_ARGUMENT;
     }
-    if (P > kNoAllocMaxPaths) {
-        setError("slrgpu_render_noalloc: width * height exceeds the fixed scratch limit of 65536 pixels");
+    if ((uint64_t)padToTile(s.width) * padToTile(s.height) > kNoAllocMaxPaths) {
+        setError("slrgpu_render_noalloc: the sample grid (width and height rounded up to multiples of 8) exceeds "
+                 "the fixed scratch limit of 65536 pixels");
         return SLRGPU_ERR_INVALID_ARGUMENT;
     }
     if (s.max_depth > kNoAllocMaxDepth) {
         setError("slrgpu_render_noalloc: max_depth exceeds the fixed scratch limit of 64");
         return SLRGPU_ERR_INVALID_ARGUMENT;
     }
-    uint32_t S = s.samples_per_wave ? s.samples_per_wave : (uint32_t)(kNoAllocMaxPaths / P);
-    S = std::min(S, s.spp);
-    if ((uint64_t)S * P > kNoAllocMaxPaths) {
-        setError("slrgpu_render_noalloc: width * height * samples_per_wave exceeds the fixed scratch limit of 65536 paths");
+    const WavePlan pl = planWaves(s, kNoAllocMaxPaths);
+    if ((uint64_t)pl.S * pl.gridPositions > kNoAllocMaxPaths) {
+        setError("slrgpu_render_noalloc: sample grid * samples_per_wave exceeds the fixed scratch limit of 65536 "
+                 "paths");
         return SLRGPU_ERR_INVALID_ARGUMENT;
     }
+    const uint32_t P = pl.filmPixels;
     int dev = 0;
     CUDA_TRY(cudaGetDevice(&dev));
     if (dev < 0 || dev >= 64) {
@@ -1447,23 +1594,9 @@ int renderNoAlloc(const DeviceScene &ds, const slrgpu_settings &s, float* film, 
         }
         base = (unsigned char*)g_noallocAddr[dev];
     }
-    const int block = 256;
-    static int gRaygen = 0, gExtend = 0, gShade = 0, gShadow = 0, gAcc = 0, gShadeVol = 0, gShadowVol = 0;
-    {
-        std::lock_guard<std::mutex> lock(g_noallocMu);
-        if (!gRaygen) {
-            gExtend = gridFor((const void*)kExtend, block);
-            gShade = gridFor((const void*)kShade, block);
-            gShadow = gridFor((const void*)kShadow, block);
-            gAcc = gridFor((const void*)kAccumulate, block);
-            gShadeVol = gridFor((const void*)kShadeVol, block);
-            gShadowVol = gridFor((const void*)kShadowVol, block);
-            gRaygen = gridFor((const void*)kRaygen, block);
-        }
-    }
     WaveState w;
     std::memset(&w, 0, sizeof(w));
-    w.N = (uint32_t)(S * P);
+    w.N = pl.S * pl.gridPositions;
     w.rayOrg = (float4*)(base + kNaRayOrg);
     w.rayDir = (float4*)(base + kNaRayDir);
     w.hit = (float4*)(base + kNaHit);
@@ -1485,41 +1618,14 @@ int renderNoAlloc(const DeviceScene &ds, const slrgpu_settings &s, float* film, 
     w.stats = (unsigned long long*)(base + kNaStats);
     float* filmSum = (float*)(base + kNaFilmSum);
     float* filmComp = (float*)(base + kNaFilmComp);
-    // The array keeps the previous call's contents: clear the accumulators.
+    // The array keeps the previous call's contents: clear the accumulators
+    // (the wave loop clears the queue counters of every wave itself).
     CUDA_TRY(cudaMemsetAsync(filmSum, 0, (size_t)P * kNumLambda * sizeof(float), stream));
     CUDA_TRY(cudaMemsetAsync(filmComp, 0, (size_t)P * kNumLambda * sizeof(float), stream));
     CUDA_TRY(cudaMemsetAsync(w.stats, 0, 4 * sizeof(unsigned long long), stream));
-    const uint32_t D = s.max_depth;
-    for (uint32_t sb = 0; sb < s.spp; sb += S) {
-        WaveParams wp;
-        wp.width = s.width;
-        wp.height = s.height;
-        wp.numPixels = (uint32_t)P;
-        wp.samplesInWave = std::min(S, s.spp - sb);
-        wp.sampleBase = sb;
-        wp.numPaths = wp.samplesInWave * (uint32_t)P;
-        wp.maxDepth = D;
-        wp.seed = s.seed;
-        CUDA_TRY(cudaMemsetAsync(w.counters, 0, 3 * (size_t)(D + 2) * sizeof(uint32_t), stream));
-        kRaygen<<<gRaygen, block, 0, stream>>>(ds.sc, w, wp);
-        for (uint32_t b = 0; b <= D; ++b) {
-            uint32_t* inCount = w.counters + b;
-            uint32_t* outCount = w.counters + b + 1;
-            uint32_t* shCount = w.counters + (D + 2) + b;
-            kExtend<<<gExtend, block, 0, stream>>>(ds.sc, w, w.queue[b & 1], inCount);
-            if (s.volumetric) {
-                kShadeVol<<<gShadeVol, block, 0, stream>>>(ds.sc, w, wp, w.queue[b & 1], inCount,
-                                                           w.queue[(b + 1) & 1], outCount, w.shadowQueue, shCount);
-                kShadowVol<<<gShadowVol, block, 0, stream>>>(ds.sc, w, wp, w.shadowQueue, shCount, b);
-            } else {
-                kShade<<<gShade, block, 0, stream>>>(ds.sc, w, wp, w.queue[b & 1], inCount, w.queue[(b + 1) & 1],
-                                                     outCount, w.shadowQueue, shCount);
-                kShadow<<<gShadow, block, 0, stream>>>(ds.sc, w, w.shadowQueue, shCount);
-            }
-        }
-        kAccumulate<<<gAcc, block, 0, stream>>>(w, wp, filmSum, filmComp);
-    }
-    kFilmToPixelMajor<<<gAcc, block, 0, stream>>>(filmSum, film, (uint32_t)P);
+    LaunchMarks lm;
+    runWaves(ds, s, pl, w, filmSum, filmComp, stream, lm);
+    kFilmToPixelMajor<<<waveGrids(256).accumulate, 256, 0, stream>>>(filmSum, film, P);
     CUDA_TRY(cudaGetLastError());
     return SLRGPU_OK;
 }
@@ -1557,6 +1663,45 @@ int bsdfQuery(int kind, const float* s0, const float* s1, const float* s2, float
     cudaFree(dq);
     cudaFree(dout);
     if (e != cudaSuccess) { setError(cudaGetErrorString(e)); return SLRGPU_ERR_CUDA; }
+    return SLRGPU_OK;
+}
+
+int mediumQuery(const DeviceScene &ds, int mode, uint32_t n, const float* rays, const float* lambdas, const int* sel,
+                const uint32_t* vals, uint32_t nvals, float* out) {
+    if (!ds.sc.medium.present) {
+        setError("the scene has no medium");
+        return SLRGPU_ERR_STATE;
+    }
+    if (mode < 0 || mode > 4) {
+        setError("medium query mode must be 0 to 4");
+        return SLRGPU_ERR_INVALID_ARGUMENT;
+    }
+    if (n == 0) return SLRGPU_OK;
+    const size_t bRays = (size_t)n * 8 * sizeof(float), bLam = (size_t)n * 16 * sizeof(float);
+    const size_t bSel = (size_t)n * sizeof(int), bVals = (size_t)n * nvals * sizeof(uint32_t);
+    const size_t bOut = (size_t)n * 24 * sizeof(float);
+    unsigned char* d = nullptr;
+    CUDA_TRY(cudaMalloc(&d, bRays + bLam + bSel + bVals + bOut + 64));
+    float* dRays = (float*)d;
+    float* dLam = (float*)(d + bRays);
+    int* dSel = (int*)(d + bRays + bLam);
+    uint32_t* dVals = (uint32_t*)(d + bRays + bLam + bSel);
+    float* dOut = (float*)(d + bRays + bLam + bSel + bVals);
+    cudaError_t e = cudaMemcpy(dRays, rays, bRays, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(dLam, lambdas, bLam, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(dSel, sel, bSel, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && bVals) e = cudaMemcpy(dVals, vals, bVals, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        kMediumQuery<<<std::min<uint32_t>((n + 127) / 128, 4096), 128>>>(ds.sc, mode, n, dRays, dLam, dSel, dVals,
+                                                                         nvals, dOut);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(out, dOut, bOut, cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess) {
+        setError(cudaGetErrorString(e));
+        return SLRGPU_ERR_CUDA;
+    }
     return SLRGPU_OK;
 }
 

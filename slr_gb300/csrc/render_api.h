@@ -54,6 +54,8 @@ int renderNoAlloc(const DeviceScene &ds, const slrgpu_settings &s, float* film, 
 size_t noAllocScratchBytes();
 int bsdfQuery(int kind, const float* s0, const float* s1, const float* s2, float ax, float ay, const float* queries,
               uint32_t n, float* out);
+int mediumQuery(const DeviceScene &ds, int mode, uint32_t n, const float* rays, const float* lambdas, const int* sel,
+                const uint32_t* vals, uint32_t nvals, float* out);
 int traceRays(const DeviceScene &ds, const float* rays, uint32_t n, int anyHit, uint32_t* prim, float* t, float* b1,
               float* b2, cudaStream_t stream);
 

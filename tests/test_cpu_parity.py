@@ -2,6 +2,8 @@
 upsampling, sampled spectra and the environment importance tables must be
 bit-identical to the reference's on the same inputs; the numpy restatement of
 the triangle test is pinned against the reference accelerator."""
+import os
+
 import numpy as np
 import pytest
 
@@ -78,3 +80,27 @@ def test_restated_triangle_test_pinned(oracle_lib):
     np.testing.assert_array_equal(bt.view(np.uint32), rt.view(np.uint32))
     res = helpers.compare_hits(d, rays, bp, bt, rp, rt)
     assert res["mismatch"] == 0, res
+
+
+def test_microfacet_bsdf_restatement_matches_golden():
+    """The float64 restatement of MicrofacetBSDF used for the BSDF test's
+    condition numbers reproduces the reference's golden values (FP32, so
+    agreement is to FP32 rounding where well conditioned)."""
+    from tests.bsdf_cases import bsdf_cases
+    from tests.bsdf_conditioning import condition, microfacet_bsdf
+    golden = np.load(os.path.join(os.path.dirname(__file__), "golden", "bsdf_kat.npz"))
+    for c in bsdf_cases():
+        if c["kind"] != "ggx_bsdf":
+            continue
+        q = c["queries"].astype(np.float64)
+        ref = golden[c["name"]]
+        wo, gn, wi, wl = q[:, 0:3], q[:, 3:6], q[:, 11:14], q[:, 6].astype(int)
+        fs, pdf = microfacet_bsdf(wo, wi, wl, c["spec0"], c["spec1"], c["ax"], c["ay"])
+        fs = fs * np.abs(wi[:, 2] / (wi * gn).sum(1))[:, None]      # shading-normal correction
+        kappa = condition(wo, wi, wl, c["spec0"], c["spec1"], c["ax"], c["ay"])
+        tol = np.maximum(1e-5, 6e-6 * kappa)
+        rf, rp = ref[:, 21:37], ref[:, 37]
+        assert ((fs == 0) == (rf == 0)).all() and ((pdf == 0) == (rp == 0)).all()
+        ok_f = (np.abs(fs - rf) <= tol[:, None] * np.abs(rf) + 1e-30).all(1)
+        ok_p = np.abs(pdf - rp) <= tol * np.abs(rp) + 1e-30
+        assert ok_f.mean() > 0.998 and ok_p.mean() > 0.998, (ok_f.mean(), ok_p.mean())

@@ -15,6 +15,7 @@ import numpy as np
 import pytest
 
 from tests.bsdf_cases import bsdf_cases
+from tests.bsdf_conditioning import condition
 
 pytestmark = pytest.mark.gpu
 GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
@@ -58,9 +59,20 @@ def test_bsdf_matches_reference(gpu_lib, case):
     rd = r[:, 16:19].astype(np.float64)
     sens = 1.0 / np.maximum(np.abs(rd[:, 2]), 1e-12) + 1.0 / np.maximum(np.abs((rd * qb[:, 3:6]).sum(1)), 1e-12) + 1.0
     cond_v = np.maximum(cond_s, 1.0 + 10.0 * dir_err * sens / RTOL)
+    cond_e = _cond(q[:, 11:14].astype(np.float64), q[:, 3:6].astype(np.float64))
+    if case["kind"] == "ggx_bsdf":
+        # Near total internal reflection the dielectric microfacet value and
+        # pdf are ill-conditioned in FP32 (1 - F cancels): widen by the
+        # condition number per unit relative change of the directions, times
+        # FP32 input rounding (6e-8) and a factor 100 for the rounding of the
+        # ~50 operations in between.
+        args = (case["spec0"], case["spec1"], case["ax"], case["ay"])
+        k_s = condition(qb[:, 0:3], rd, qb[:, 6].astype(int), *args)
+        k_e = condition(q[:, 0:3], q[:, 11:14], q[:, 6].astype(int), *args)
+        cond_v = np.maximum(cond_v, 6e-6 * k_s / RTOL)
+        cond_e = np.maximum(cond_e, 6e-6 * k_e / RTOL)
     fs_ok = _rel_ok(g[:, 0:16], r[:, 0:16], np.abs(r[:, 0:16]).max() + 1e-30, cond_v).all(1)
     pdf_ok = _rel_ok(g[:, 19], r[:, 19], np.abs(r[:, 19]).max(), cond_v)
-    cond_e = _cond(q[:, 11:14].astype(np.float64), q[:, 3:6].astype(np.float64))
     ev_ok = _rel_ok(out[:, 21:37], ref[:, 21:37], np.abs(ref[:, 21:37]).max() + 1e-30, cond_e).all(1)
     epdf_ok = _rel_ok(out[:, 37], ref[:, 37], np.abs(ref[:, 37]).max() + 1e-30, cond_e)
     bad = {k: int((~v).sum()) for k, v in (("fs", fs_ok), ("pdf", pdf_ok), ("eval", ev_ok), ("eval_pdf", epdf_ok))}

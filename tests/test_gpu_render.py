@@ -23,17 +23,23 @@ def gpu_batches(gpu_lib, desc, w, h, spp, depth, batches, seed0=50000):
         dropped += st.dropped_samples
         means.append(film.astype(np.float64) / spp)
     m = np.stack(means)
-    return m.mean(0), m.var(0, ddof=1), dropped
+    return m.mean(0), m.var(0, ddof=1), dropped, m.reshape(batches, -1).sum(1)
 
 
-def check_statistical_parity(mg, vg, kg, mr, vr, kr, frac_limit=0.015):
+def check_statistical_parity(mg, vg, kg, mr, vr, kr, frac_limit=0.015, tg=None, tr=None):
+    """tg, tr: per-batch image sums, when known; the image-wide test then
+    uses their spread, which includes the correlation between the bins of one
+    pixel (one path adds to all 16 wavelength bins)."""
     se = np.sqrt(vg / kg + vr / kr)
     diff = mg - mr
     zero = se == 0
     assert np.all(np.abs(diff[zero]) < 1e-6), "deterministic-zero bins differ"
     z = np.abs(diff[~zero]) / se[~zero]
     frac = float((z > 3).mean())
-    gz = diff.sum() / np.sqrt((vg / kg).sum() + (vr / kr).sum())
+    if tg is not None and tr is not None:
+        gz = (tg.mean() - tr.mean()) / np.sqrt(tg.var(ddof=1) / len(tg) + tr.var(ddof=1) / len(tr))
+    else:
+        gz = diff.sum() / np.sqrt((vg / kg).sum() + (vr / kr).sum())
     assert frac < frac_limit, f"{frac:.4f} of bins beyond 3 sigma"
     assert abs(gz) < 4.0, f"image-wide sum differs by {gz:.2f} sigma"
     return frac, gz
@@ -42,9 +48,23 @@ def check_statistical_parity(mg, vg, kg, mr, vr, kr, frac_limit=0.015):
 def test_box_scene_matches_reference(gpu_lib):
     g = np.load(os.path.join(GOLDEN, "box_render_32.npz"))
     desc = scenes.box_scene(32, 32)
-    mg, vg, dropped = gpu_batches(gpu_lib, desc, 32, 32, int(g["spp"]), int(g["max_depth"]), 192)
+    mg, vg, dropped, _ = gpu_batches(gpu_lib, desc, 32, 32, int(g["spp"]), int(g["max_depth"]), 192)
     frac, gz = check_statistical_parity(mg, vg, 192, g["mean"], g["var"], int(g["batches"]))
     assert dropped == 0
+
+
+def test_ragged_image_matches_reference(gpu_lib, oracle_lib):
+    """21 x 13 pixels: neither side a multiple of the reference's 8 x 8 sensor
+    tiles, so the last column and row also collect the samples of the
+    overhanging tile positions, as ImageSensor::add clamps them there."""
+    w, h = 21, 13
+    desc = scenes.heightfield_scene(grid=24, spheres=5, sphere_freq=3, env_size=(64, 32), width=w, height=h)
+    spp, depth, kr, kg = 8, 3, 64, 192
+    ref = oracle_lib.RefScene(desc)
+    rm = np.stack([ref.render(w, h, spp, depth, seed=700 + k, threads=os.cpu_count())[0].astype(np.float64) / spp
+                   for k in range(kr)])
+    mg, vg, _, tg = gpu_batches(gpu_lib, desc, w, h, spp, depth, kg)
+    check_statistical_parity(mg, vg, kg, rm.mean(0), rm.var(0, ddof=1), kr, tg=tg, tr=rm.reshape(kr, -1).sum(1))
 
 
 def test_ggx_ibl_scene_matches_reference(gpu_lib, oracle_lib):
@@ -59,8 +79,9 @@ def test_ggx_ibl_scene_matches_reference(gpu_lib, oracle_lib):
         film, _ = ref.render(w, h, spp, depth, seed=100 + k, threads=os.cpu_count())
         means.append(film.astype(np.float64) / spp)
     rm = np.stack(means)
-    mg, vg, _ = gpu_batches(gpu_lib, desc, w, h, spp, depth, kg)
-    check_statistical_parity(mg, vg, kg, rm.mean(0), rm.var(0, ddof=1), kr, frac_limit=0.02)
+    mg, vg, _, tg = gpu_batches(gpu_lib, desc, w, h, spp, depth, kg)
+    check_statistical_parity(mg, vg, kg, rm.mean(0), rm.var(0, ddof=1), kr, frac_limit=0.02, tg=tg,
+                             tr=rm.reshape(kr, -1).sum(1))
 
 
 def test_volumetric_box_matches_reference(gpu_lib, oracle_lib):
@@ -86,8 +107,10 @@ def test_volumetric_box_matches_reference(gpu_lib, oracle_lib):
         gdrop += st.dropped_samples
         gmeans.append(film.astype(np.float64) / spp)
     gm = np.stack(gmeans)
-    check_statistical_parity(gm.mean(0), gm.var(0, ddof=1), kg, rm.mean(0), rm.var(0, ddof=1), kr, frac_limit=0.02)
-    nr, ng = kr * w * h * spp, kg * w * h * spp
+    check_statistical_parity(gm.mean(0), gm.var(0, ddof=1), kg, rm.mean(0), rm.var(0, ddof=1), kr, frac_limit=0.02,
+                             tg=gm.reshape(kg, -1).sum(1), tr=rm.reshape(kr, -1).sum(1))
+    grid = ((w + 7) // 8 * 8) * ((h + 7) // 8 * 8)     # sample positions, whole 8 x 8 tiles
+    nr, ng = kr * grid * spp, kg * grid * spp
     pr, pg = rdrop / nr, gdrop / ng
     pooled = (rdrop + gdrop) / (nr + ng)
     se = np.sqrt(pooled * (1 - pooled) * (1 / nr + 1 / ng)) + 1e-12
