@@ -18,6 +18,10 @@ log-normal environment with a 2-degree sun of radiance 5e4) at 1024 x 1024,
 * cpu_baseline - the reference renderer (the CPU oracle built from the
                reference's own sources) on a bounded sample of the same scene.
 
+``--workload small`` runs the same scene recipe at a size for profiler
+captures (256 x 256 height field, 16 spheres, 512 x 512 pixels, 4 spp); it is
+not a benchmark line.
+
 ``--impl reference`` times the reference renderer alone (rank 0) on a
 bounded sample of the same workload.  Under torchrun each rank renders its
 own replica (weak scaling; path samples are independent, no collective).
@@ -174,8 +178,16 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--spp", type=int, default=SPP)
+    ap.add_argument("--spp", type=int, default=None)
+    ap.add_argument("--workload", default="ggx_ibl_1m", choices=["ggx_ibl_1m", "small"])
     args = ap.parse_args()
+    global WIDTH, HEIGHT, WORKLOAD
+    if args.workload == "small":
+        WIDTH = HEIGHT = 512
+        WORKLOAD = "small: 256x256 height field + 16 spheres (freq 12), 256x128 IBL, 512x512, max depth 10"
+        args.no_cpu_baseline = True
+    if args.spp is None:
+        args.spp = 4 if args.workload == "small" else SPP
     if args.impl == "reference":
         return run_reference(args)
 
@@ -195,7 +207,11 @@ def main():
             dist.barrier()
 
     spp = args.spp
-    desc = scenes.heightfield_scene(seed=0)
+    if args.workload == "small":
+        desc = scenes.heightfield_scene(grid=256, spheres=16, sphere_freq=12, env_size=(256, 128), width=WIDTH,
+                                        height=HEIGHT, seed=0)
+    else:
+        desc = scenes.heightfield_scene(seed=0)
     ctx = api.Context(local)
     t0 = time.time()
     scene = api.Scene(desc, context=ctx)

@@ -68,7 +68,9 @@ typedef struct slrgpu_settings {
     uint32_t max_depth;           /* scattering vertices with NEE + BSDF sampling */
     uint32_t seed;                /* RNG seed (RenderSettingItem::RNGSeed) */
     uint32_t volumetric;          /* 0: PTRenderer, 1: VolumetricPTRenderer */
-    uint32_t samples_per_wave;    /* 0: automatic; paths in flight = W*H*this */
+    uint32_t samples_per_wave;    /* 0: automatic; paths in flight = this times
+                                     the sample grid (W and H rounded up to
+                                     multiples of 8) */
     uint32_t flags;               /* SLRGPU_FLAG_* */
 } slrgpu_settings;
 
@@ -87,7 +89,7 @@ typedef struct slrgpu_settings {
 typedef struct slrgpu_render_stats {
     double seconds;               /* wall time of the call */
     double kernel_seconds;        /* device time of the render kernels */
-    uint64_t path_samples;        /* W*H*spp */
+    uint64_t path_samples;        /* sample grid positions * spp */
     uint64_t extension_rays;      /* closest-hit queries traced */
     uint64_t shadow_rays;         /* any-hit queries traced */
     uint64_t dropped_samples;     /* non-finite contributions dropped */
@@ -177,7 +179,7 @@ int slrgpu_render(slrgpu_handle scene, const slrgpu_settings* settings, float* f
  * slrgpu_render needs per-context path-state buffers that it allocates (and
  * grows) on demand; this variant keeps the path state, queues, counters and
  * film sums in one fixed file-scope device array of
- * slrgpu_render_noalloc_scratch_bytes() bytes (about 27 MiB), which every GPU
+ * slrgpu_render_noalloc_scratch_bytes() bytes (about 29 MiB), which every GPU
  * that loads the library holds until the process exits.
  *
  * Limits: the sample grid, width and height each rounded up to a multiple

@@ -156,14 +156,20 @@ __device__ __forceinline__ void specScale(const Spec &a, float s, Spec &out) {
     for (int i = 0; i < kNumLambda; ++i) out.v[i] = a.v[i] * s;
 }
 
+// The BSDF bodies are templates over the material kind: K >= 0 fixes the
+// kind at compile time (the switch folds to one case inside a kernel that
+// shades a single material), K < 0 dispatches on B.kind at run time.
+
 // Returns fs (without the shading-normal correction); res->pdf == 0 on failure.
-__device__ __noinline__ void bsdfSampleInternal(const Bsdf &B, const BsdfQuery &q, float uc, float u0, float u1,
+template <int K>
+__device__ __forceinline__ void bsdfSampleBody(const Bsdf &B, const BsdfQuery &q, float uc, float u0, float u1,
                                                BsdfSample* res, Spec &fs) {
     res->pdf = 0.0f;
     res->type = 0;
     res->dir = V3{0, 0, 1};
     fs = specConst(0.0f);
-    switch (B.kind) {
+    const uint32_t kind = K < 0 ? B.kind : (uint32_t)K;
+    switch (kind) {
     case kMatMatte: {  // basic_bsdfs.cpp:13-27
         V3 d = cosineSampleHemisphere(u0, u1);
         res->pdf = d.z * kInvPiF;
@@ -299,9 +305,11 @@ __device__ __noinline__ void bsdfSampleInternal(const Bsdf &B, const BsdfQuery &
     }
 }
 
-__device__ __noinline__ void bsdfEvalInternal(const Bsdf &B, const BsdfQuery &q, V3 dir, Spec &fs) {
+template <int K>
+__device__ __forceinline__ void bsdfEvalBody(const Bsdf &B, const BsdfQuery &q, V3 dir, Spec &fs) {
     fs = specConst(0.0f);
-    switch (B.kind) {
+    const uint32_t kind = K < 0 ? B.kind : (uint32_t)K;
+    switch (kind) {
     case kMatMatte:
         if (q.dir.z * dir.z <= 0.0f) return;
         specScale(B.a, 1.0f / kPiF, fs);
@@ -357,8 +365,10 @@ __device__ __noinline__ void bsdfEvalInternal(const Bsdf &B, const BsdfQuery &q,
     }
 }
 
-__device__ __noinline__ float bsdfPdfInternal(const Bsdf &B, const BsdfQuery &q, V3 dir) {
-    switch (B.kind) {
+template <int K>
+__device__ __forceinline__ float bsdfPdfBody(const Bsdf &B, const BsdfQuery &q, V3 dir) {
+    const uint32_t kind = K < 0 ? B.kind : (uint32_t)K;
+    switch (kind) {
     case kMatMatte:
         if (q.dir.z * dir.z <= 0.0f) return 0.0f;
         return fabsf(dir.z) * kInvPiF;
@@ -401,25 +411,45 @@ __device__ __noinline__ float bsdfPdfInternal(const Bsdf &B, const BsdfQuery &q,
     }
 }
 
+// Run-time dispatch, kept out of line so that kernels shading any material
+// carry one copy of every BSDF.
+__device__ __noinline__ void bsdfSampleInternal(const Bsdf &B, const BsdfQuery &q, float uc, float u0, float u1,
+                                                BsdfSample* res, Spec &fs) {
+    bsdfSampleBody<-1>(B, q, uc, u0, u1, res, fs);
+}
+__device__ __noinline__ void bsdfEvalInternal(const Bsdf &B, const BsdfQuery &q, V3 dir, Spec &fs) {
+    bsdfEvalBody<-1>(B, q, dir, fs);
+}
+__device__ __noinline__ float bsdfPdfInternal(const Bsdf &B, const BsdfQuery &q, V3 dir) {
+    return bsdfPdfBody<-1>(B, q, dir);
+}
+
 // ---- the BSDF wrapper: shading-normal correction |d.z / dot(d, n_g)| ----
+// K < 0: any material (run-time dispatch); K >= 0: that material kind only.
+template <int K = -1>
 __device__ __forceinline__ void bsdfSample(const Bsdf &B, const BsdfQuery &q, float uc, float u0, float u1,
                                            BsdfSample* res, Spec &fs) {
-    bsdfSampleInternal(B, q, uc, u0, u1, res, fs);
+    if (K < 0) bsdfSampleInternal(B, q, uc, u0, u1, res, fs);
+    else bsdfSampleBody<K>(B, q, uc, u0, u1, res, fs);
     if (res->pdf == 0.0f) return;
     float sn = fabsf(res->dir.z / dot(res->dir, q.gn));
 #pragma unroll
     for (int i = 0; i < kNumLambda; ++i) fs.v[i] *= sn;
 }
 
+template <int K = -1>
 __device__ __forceinline__ void bsdfEval(const Bsdf &B, const BsdfQuery &q, V3 dir, Spec &fs) {
-    bsdfEvalInternal(B, q, dir, fs);
+    if (K < 0) bsdfEvalInternal(B, q, dir, fs);
+    else bsdfEvalBody<K>(B, q, dir, fs);
     float sn = fabsf(dir.z / dot(dir, q.gn));
 #pragma unroll
     for (int i = 0; i < kNumLambda; ++i) fs.v[i] *= sn;
 }
 
+template <int K = -1>
 __device__ __forceinline__ float bsdfPdf(const Bsdf &B, const BsdfQuery &q, V3 dir) {
-    return bsdfPdfInternal(B, q, dir);
+    if (K < 0) return bsdfPdfInternal(B, q, dir);
+    return bsdfPdfBody<K>(B, q, dir);
 }
 
 }  // namespace slrgpu

@@ -50,7 +50,8 @@ struct WaveState {
     float* shContrib;    // [16][N]
     uint32_t* queue[2];
     uint32_t* shadowQueue;
-    uint32_t* counters;  // [3 * (maxDepth + 2)]
+    uint32_t* classQueue;  // [kNumShadeClasses][N]: paths of one bounce sorted by shading class
+    uint32_t* counters;    // [kCtrStride * (maxDepth + 2)], see kCtr*
     unsigned long long* stats;  // 0 extension rays, 1 shadow rays, 2 dropped samples
     uint32_t N;
 };
@@ -75,6 +76,14 @@ struct WaveParams {
     uint32_t maxDepth;
     uint32_t seed;
 };
+
+// Per-bounce counter block: [0, kNumShadeClasses) paths per shading class,
+// kCtrExt paths in the extension queue of the bounce, kCtrShadow shadow rays.
+constexpr int kNumShadeClasses = 6;   // the five material kinds + environment / miss
+constexpr int kClassMiss = 5;
+constexpr int kCtrStride = 8;
+constexpr int kCtrExt = 6;
+constexpr int kCtrShadow = 7;
 
 constexpr uint32_t kInfoSelMask = 0xfu;
 constexpr uint32_t kInfoWlSelected = 1u << 4;
@@ -235,7 +244,7 @@ __device__ __noinline__ void makeBsdf(const DevScene &sc, const DevMaterial &m, 
 // Kernels
 // ---------------------------------------------------------------------------
 __global__ void kRaygen(DevScene sc, WaveState ws, WaveParams wp) {
-    if (blockIdx.x == 0 && threadIdx.x == 0) ws.counters[0] = wp.numPaths;
+    if (blockIdx.x == 0 && threadIdx.x == 0) ws.counters[kCtrExt] = wp.numPaths;
     for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < wp.numPaths; p += gridDim.x * blockDim.x) {
         uint32_t s = p / wp.numPixels;
         uint32_t pixel = p - s * wp.numPixels;
@@ -348,9 +357,90 @@ __device__ __forceinline__ int selectLight(const DevScene &sc, float u, float* p
     return surf(u, prob);
 }
 
-__global__ void __launch_bounds__(256) kShade(DevScene sc, WaveState ws, WaveParams wp,
-                                              const uint32_t* __restrict__ inQueue, const uint32_t* __restrict__ inCount,
-                                              uint32_t* outQueue, uint32_t* outCount, uint32_t* shQueue, uint32_t* shCount) {
+// ---------------------------------------------------------------------------
+// Material-sorted surface shading.  The extension kernel sorts every path of
+// a bounce into one queue per shading class (material kind, or environment
+// for rays that hit nothing); one kernel per class then shades its queue with
+// that material's BSDF compiled in alone, which keeps each kernel's code
+// small (instruction-cache resident) and its warps free of material
+// divergence.  Emission with MIS, Russian roulette, next-event estimation and
+// BSDF sampling follow PTRenderer::Job::contribution (PTRenderer.cpp:145-277).
+// ---------------------------------------------------------------------------
+__global__ void kExtendSort(DevScene sc, WaveState ws, const uint32_t* __restrict__ queue,
+                            const uint32_t* __restrict__ count, uint32_t* classCounts) {
+    const uint32_t n = *count;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+        const uint32_t i = base + threadIdx.x;
+        const bool active = i < n;
+        int cls = -1;
+        uint32_t p = 0;
+        if (active) {
+            p = queue[i];
+            float4 o = ws.rayOrg[p], d = ws.rayDir[p];
+            Hit h;
+            traceClosest(sc, V3{o.x, o.y, o.z}, V3{d.x, d.y, d.z}, o.w, d.w, &h);
+            ws.hit[p] = make_float4(h.t, h.b1, h.b2, __uint_as_float(h.prim));
+            cls = h.prim == kNoHit ? kClassMiss : (int)sc.materials[sc.prims[h.prim].material].kind;
+        }
+#pragma unroll
+        for (int c = 0; c < kNumShadeClasses; ++c)
+            queuePush(ws.classQueue + (size_t)c * ws.N, classCounts + c, p, cls == c);
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&ws.stats[0], (unsigned long long)n);
+}
+
+// Paths whose ray left the scene: environment emission (with MIS after a
+// non-delta bounce), then the path ends (PTRenderer.cpp:150-152, :234-263).
+__global__ void kShadeMiss(DevScene sc, WaveState ws, const uint32_t* __restrict__ queue,
+                           const uint32_t* __restrict__ count) {
+    const uint32_t n = *count;
+    if (!sc.envPresent) return;
+    const float twoPi = 6.28318530717958647692f;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t p = queue[i];
+        const uint32_t info = ws.info[p];
+        const uint32_t depth = info >> kInfoDepthShift;
+        const bool prevDelta = (info & kInfoPrevDelta) != 0;
+        const float wlOff = ws.wlOffset[p];
+        float lambdas[kNumLambda];
+#pragma unroll
+        for (int k = 0; k < kNumLambda; ++k) lambdas[k] = lambdaAt(k, wlOff);
+        float4 rd = ws.rayDir[p];
+        V3 dir = V3{rd.x, rd.y, rd.z};
+        float theta, phi;
+        toPolarYUp(dir, &theta, &phi);
+        Spec Le;
+        envRadiance(sc, phi / twoPi, theta / kPiF, lambdas, Le);
+        float mis = 1.0f;
+        if (depth > 0 && !prevDelta) {
+            float lightProb = sc.envImportance / (sc.surfImportance + sc.envImportance);
+            float lightPdf = lightProb * envAreaPdf(sc, phi, theta) * 1.0f / absDot(dir, -dir);
+            float bp = ws.prevPdf[p];
+            mis = (bp * bp) / (lightPdf * lightPdf + bp * bp);
+        }
+#pragma unroll
+        for (int k = 0; k < kNumLambda; ++k)
+            ws.L[(size_t)k * ws.N + p] += ws.alpha[(size_t)k * ws.N + p] * Le.v[k] * mis;
+    }
+}
+
+template <int K>
+__device__ __forceinline__ void makeBsdfK(const DevScene &sc, const DevMaterial &m, const float lambdas[kNumLambda],
+                                          bool wlSelected, Bsdf &B) {
+    B.kind = (uint32_t)K;
+    B.ax = m.alphaX;
+    B.ay = m.alphaY;
+    B.dispersive = !wlSelected;
+    evalSpectrum(sc, m.spec[0], lambdas, B.a);
+    if (K != kMatMatte) evalSpectrum(sc, m.spec[1], lambdas, B.b);
+    if (K == kMatSpecularReflection || K == kMatSpecularScattering) evalSpectrum(sc, m.spec[2], lambdas, B.c);
+}
+
+template <int K>
+__global__ void __launch_bounds__(256) kShadeSurf(DevScene sc, WaveState ws, WaveParams wp,
+                                                  const uint32_t* __restrict__ inQueue,
+                                                  const uint32_t* __restrict__ inCount, uint32_t* outQueue,
+                                                  uint32_t* outCount, uint32_t* shQueue, uint32_t* shCount) {
     const uint32_t n = *inCount;
     const uint32_t N = ws.N;
     const float inf = __int_as_float(0x7f800000);
@@ -374,188 +464,160 @@ __global__ void __launch_bounds__(256) kShade(DevScene sc, WaveState ws, WavePar
             float4 ro = ws.rayOrg[p], rd = ws.rayDir[p];
             V3 org = V3{ro.x, ro.y, ro.z}, dir = V3{rd.x, rd.y, rd.z};
             float4 hv = ws.hit[p];
-            uint32_t prim = __float_as_uint(hv.w);
+            const DevPrim pr = sc.prims[__float_as_uint(hv.w)];
             Spec alpha;
             loadSpec(ws.alpha, N, p, alpha);
             bool alive = true;
-
-            if (prim == kNoHit) {
-                // Environment (Scene.cpp:57-62): always "hit" for unbounded rays.
-                if (sc.envPresent) {
-                    float theta, phi;
-                    toPolarYUp(dir, &theta, &phi);
-                    Spec Le;
-                    envRadiance(sc, phi / twoPi, theta / kPiF, lambdas, Le);
-                    float mis = 1.0f;
-                    if (depth > 0 && !prevDelta) {
-                        float lightProb = sc.envImportance / (sc.surfImportance + sc.envImportance);
-                        float lightPdf = lightProb * envAreaPdf(sc, phi, theta) * 1.0f / absDot(dir, -dir);
-                        float bp = ws.prevPdf[p];
-                        mis = (bp * bp) / (lightPdf * lightPdf + bp * bp);
-                    }
-                    Spec add;
-#pragma unroll
-                    for (int k = 0; k < kNumLambda; ++k) add.v[k] = alpha.v[k] * Le.v[k] * mis;
-                    addSpec(ws.L, N, p, add);
+            SurfPoint sp;
+            surfacePoint(sc, pr, org, dir, hv.x, hv.y, hv.z, sp);
+            const DevMaterial mat = sc.materials[pr.material];
+            V3 dirOut = sp.frame.toLocal(-dir);
+            // Emission on hit (PTRenderer.cpp:162-166, :240-263).
+            if (mat.emit >= 0) {
+                Spec M;
+                evalSpectrum(sc, mat.emit, lambdas, M);
+                float edf = dirOut.z > 0.0f ? kInvPiF : 0.0f;
+                float mis = 1.0f;
+                if (depth > 0 && !prevDelta) {
+                    float lightProb = (sc.surfImportance / (sc.surfImportance + sc.envImportance)) * sc.lightPMF[0];
+                    float dist2 = sqLength(sp.p - org);
+                    float lightPdf = lightProb * pr.invArea * dist2 / absDot(dir, sp.gn);
+                    float bp = ws.prevPdf[p];
+                    mis = (bp * bp) / (lightPdf * lightPdf + bp * bp);
                 }
-                alive = false;
-            } else {
-                const DevPrim pr = sc.prims[prim];
-                SurfPoint sp;
-                surfacePoint(sc, pr, org, dir, hv.x, hv.y, hv.z, sp);
-                const DevMaterial mat = sc.materials[pr.material];
-                V3 dirOut = sp.frame.toLocal(-dir);
-                // Emission on hit (PTRenderer.cpp:162-166, :240-263).
-                if (mat.emit >= 0) {
+                Spec add;
+#pragma unroll
+                for (int k = 0; k < kNumLambda; ++k) add.v[k] = alpha.v[k] * (M.v[k] * edf) * mis;
+                addSpec(ws.L, N, p, add);
+            }
+            // Russian roulette (PTRenderer.cpp:266-272).
+            if (depth > 0) {
+                float cp = fminf(importance(alpha, sel) / ws.initY[p], 1.0f);
+                if (rng.next() < cp) {
+                    float r = 1.0f / cp;
+#pragma unroll
+                    for (int k = 0; k < kNumLambda; ++k) alpha.v[k] *= r;
+                } else {
+                    alive = false;
+                }
+            }
+            if (alive) {
+                ++depth;
+                if (depth > wp.maxDepth) alive = false;
+            }
+            if (alive) {
+                Bsdf B;
+                makeBsdfK<K>(sc, mat, lambdas, wlSelected, B);
+                BsdfQuery q{dirOut, sp.frame.toLocal(sp.gn), sel};
+                // Next-event estimation (PTRenderer.cpp:179-218).
+                if (bsdfHasNonDelta(K) && (sc.numLights > 0 || sc.envPresent)) {
+                    float lightProb;
+                    int li = selectLight(sc, rng.next(), &lightProb);
+                    float lu0 = rng.next(), lu1 = rng.next();
+                    V3 lp, lgn;
                     Spec M;
-                    evalSpectrum(sc, mat.emit, lambdas, M);
-                    float edf = dirOut.z > 0.0f ? kInvPiF : 0.0f;
-                    float mis = 1.0f;
-                    if (depth > 0 && !prevDelta) {
-                        float lightProb = (sc.surfImportance / (sc.surfImportance + sc.envImportance)) * sc.lightPMF[0];
-                        float dist2 = sqLength(sp.p - org);
-                        float lightPdf = lightProb * pr.invArea * dist2 / absDot(dir, sp.gn);
-                        float bp = ws.prevPdf[p];
-                        mis = (bp * bp) / (lightPdf * lightPdf + bp * bp);
-                    }
-                    Spec add;
-#pragma unroll
-                    for (int k = 0; k < kNumLambda; ++k) add.v[k] = alpha.v[k] * (M.v[k] * edf) * mis;
-                    addSpec(ws.L, N, p, add);
-                }
-                // Russian roulette (PTRenderer.cpp:266-272).
-                if (depth > 0) {
-                    float cp = fminf(importance(alpha, sel) / ws.initY[p], 1.0f);
-                    if (rng.next() < cp) {
-                        float r = 1.0f / cp;
-#pragma unroll
-                        for (int k = 0; k < kNumLambda; ++k) alpha.v[k] *= r;
+                    float areaPdf, edfVal, dist2;
+                    bool atInf = false;
+                    V3 shadowDir;
+                    if (li >= 0) {
+                        const DevPrim lpr = sc.prims[sc.lightPrims[li]];
+                        float su = sqrtf(lu0);
+                        float b0 = 1.0f - su, b1 = lu1 * su, b2 = 1.0f - b0 - b1;
+                        float4 p0 = sc.vpos[lpr.v0], p1 = sc.vpos[lpr.v1], p2 = sc.vpos[lpr.v2];
+                        lp = rn_bary(b0, V3{p0.x, p0.y, p0.z}, b1, V3{p1.x, p1.y, p1.z}, b2, V3{p2.x, p2.y, p2.z});
+                        float4 n0 = sc.vnrm[lpr.v0], n1 = sc.vnrm[lpr.v1], n2 = sc.vnrm[lpr.v2];
+                        V3 lz = normalize(b0 * V3{n0.x, n0.y, n0.z} + b1 * V3{n1.x, n1.y, n1.z} + b2 * V3{n2.x, n2.y, n2.z});
+                        lgn = V3{lpr.ngx, lpr.ngy, lpr.ngz};
+                        areaPdf = lpr.invArea;
+                        evalSpectrum(sc, sc.materials[lpr.material].emit, lambdas, M);
+                        V3 diff = lp - sp.p;
+                        dist2 = sqLength(diff);
+                        shadowDir = diff * (1.0f / sqrtf(dist2));
+                        edfVal = dot(lz, -shadowDir) > 0.0f ? kInvPiF : 0.0f;
                     } else {
-                        alive = false;
+                        float uvPdf, topPdf;
+                        float d1 = sample1D(sc.envTopPDF, sc.envTopCDF, sc.envMapH, lu1, &topPdf);
+                        uint32_t row = min((uint32_t)(sc.envMapH * d1), sc.envMapH - 1);
+                        float d0 = sample1D(sc.envRowPDF + (size_t)row * sc.envMapW,
+                                            sc.envRowCDF + (size_t)row * (sc.envMapW + 1), sc.envMapW, lu0, &uvPdf);
+                        uvPdf *= topPdf;
+                        float phi = d0 * twoPi, theta = d1 * kPiF;
+                        float sph, cph, sth, cth;
+                        sincosf(phi, &sph, &cph);
+                        sincosf(theta, &sth, &cth);
+                        lp = V3{-sph * sth, cth, cph * sth};
+                        lgn = -lp;
+                        atInf = true;
+                        areaPdf = uvPdf / (2.0f * kPiF * kPiF * sth);
+                        envRadiance(sc, phi / twoPi, theta / kPiF, lambdas, M);
+                        edfVal = 1.0f;
+                        shadowDir = normalize(lp);
+                        dist2 = 1.0f;
+                    }
+                    float cosShading = absDot(shadowDir, sp.gn);
+                    float cosLight = absDot(shadowDir, lgn);
+                    if (cosShading * cosLight > 0) {
+                        float lightPdf = lightProb * areaPdf;
+                        V3 sdl = sp.frame.toLocal(shadowDir);
+                        Spec fs;
+                        bsdfEval<K>(B, q, sdl, fs);
+                        float bsdfPdfV = bsdfPdf<K>(B, q, sdl) * cosLight / dist2;
+                        float mis = 1.0f;
+                        if (!isinf(areaPdf))
+                            mis = (lightPdf * lightPdf) / (lightPdf * lightPdf + bsdfPdfV * bsdfPdfV);
+                        float G = cosShading * cosLight / dist2;
+                        float scale = G * mis / lightPdf;
+                        Spec c;
+                        bool nz = false;
+#pragma unroll
+                        for (int k = 0; k < kNumLambda; ++k) {
+                            c.v[k] = ((alpha.v[k] * (M.v[k] * edfVal)) * fs.v[k]) * scale;
+                            nz |= c.v[k] != 0.0f;
+                        }
+                        if (nz) {
+                            storeSpec(ws.shContrib, N, p, c);
+                            float tmax;
+                            V3 sdir;
+                            if (atInf) {
+                                sdir = shadowDir;
+                                tmax = 3.402823466e+38f;
+                            } else {
+                                V3 dd = lp - sp.p;
+                                float dist = length(dd);
+                                sdir = dd * (1.0f / dist);
+                                tmax = dist * (1 - kRayEpsilon);
+                            }
+                            ws.shOrg[p] = make_float4(sp.p.x, sp.p.y, sp.p.z, kRayEpsilon);
+                            ws.shDir[p] = make_float4(sdir.x, sdir.y, sdir.z, tmax);
+                            shadow = true;
+                        }
                     }
                 }
-                if (alive) {
-                    ++depth;
-                    if (depth > wp.maxDepth) alive = false;
-                }
-                if (alive) {
-                    Bsdf B;
-                    makeBsdf(sc, mat, lambdas, wlSelected, B);
-                    BsdfQuery q{dirOut, sp.frame.toLocal(sp.gn), sel};
-                    // Next-event estimation (PTRenderer.cpp:179-218).
-                    if (bsdfHasNonDelta(B.kind) && (sc.numLights > 0 || sc.envPresent)) {
-                        float lightProb;
-                        int li = selectLight(sc, rng.next(), &lightProb);
-                        float lu0 = rng.next(), lu1 = rng.next();
-                        V3 lp, lgn;
-                        Spec M;
-                        float areaPdf;
-                        bool atInf = false;
-                        float edfVal = 0.0f;
-                        V3 shadowDir;
-                        float dist2;
-                        if (li >= 0) {
-                            const DevPrim lpr = sc.prims[sc.lightPrims[li]];
-                            float su = sqrtf(lu0);
-                            float b0 = 1.0f - su, b1 = lu1 * su, b2 = 1.0f - b0 - b1;
-                            float4 p0 = sc.vpos[lpr.v0], p1 = sc.vpos[lpr.v1], p2 = sc.vpos[lpr.v2];
-                            V3 P0 = V3{p0.x, p0.y, p0.z}, P1 = V3{p1.x, p1.y, p1.z}, P2 = V3{p2.x, p2.y, p2.z};
-                            lp = rn_bary(b0, P0, b1, P1, b2, P2);
-                            float4 n0 = sc.vnrm[lpr.v0], n1 = sc.vnrm[lpr.v1], n2 = sc.vnrm[lpr.v2];
-                            V3 lz = normalize(b0 * V3{n0.x, n0.y, n0.z} + b1 * V3{n1.x, n1.y, n1.z} + b2 * V3{n2.x, n2.y, n2.z});
-                            lgn = V3{lpr.ngx, lpr.ngy, lpr.ngz};
-                            areaPdf = lpr.invArea;
-                            evalSpectrum(sc, sc.materials[lpr.material].emit, lambdas, M);
-                            V3 diff = lp - sp.p;
-                            dist2 = sqLength(diff);
-                            shadowDir = diff * (1.0f / sqrtf(dist2));
-                            edfVal = dot(lz, -shadowDir) > 0.0f ? kInvPiF : 0.0f;
-                        } else {
-                            float uvPdf, topPdf;
-                            float d1 = sample1D(sc.envTopPDF, sc.envTopCDF, sc.envMapH, lu1, &topPdf);
-                            uint32_t row = min((uint32_t)(sc.envMapH * d1), sc.envMapH - 1);
-                            float d0 = sample1D(sc.envRowPDF + (size_t)row * sc.envMapW,
-                                                sc.envRowCDF + (size_t)row * (sc.envMapW + 1), sc.envMapW, lu0, &uvPdf);
-                            uvPdf *= topPdf;
-                            float phi = d0 * twoPi, theta = d1 * kPiF;
-                            float sph, cph, sth, cth;
-                            sincosf(phi, &sph, &cph);
-                            sincosf(theta, &sth, &cth);
-                            lp = V3{-sph * sth, cth, cph * sth};
-                            lgn = -lp;
-                            atInf = true;
-                            areaPdf = uvPdf / (2.0f * kPiF * kPiF * sth);
-                            envRadiance(sc, phi / twoPi, theta / kPiF, lambdas, M);
-                            // M already includes the IBL EDF's 1/pi; edf factor 1.
-                            edfVal = 1.0f;
-                            shadowDir = normalize(lp);
-                            dist2 = 1.0f;
-                        }
-                        float cosShading = absDot(shadowDir, sp.gn);
-                        float cosLight = absDot(shadowDir, lgn);
-                        if (cosShading * cosLight > 0) {
-                            float lightPdf = lightProb * areaPdf;
-                            V3 sdl = sp.frame.toLocal(shadowDir);
-                            Spec fs;
-                            bsdfEval(B, q, sdl, fs);
-                            float bsdfPdfV = bsdfPdf(B, q, sdl) * cosLight / dist2;
-                            float mis = 1.0f;
-                            if (!isinf(areaPdf))
-                                mis = (lightPdf * lightPdf) / (lightPdf * lightPdf + bsdfPdfV * bsdfPdfV);
-                            float G = cosShading * cosLight / dist2;
-                            float scale = G * mis / lightPdf;
-                            Spec c;
-                            bool nz = false;
-#pragma unroll
-                            for (int k = 0; k < kNumLambda; ++k) {
-                                c.v[k] = ((alpha.v[k] * (M.v[k] * edfVal)) * fs.v[k]) * scale;
-                                nz |= c.v[k] != 0.0f;
-                            }
-                            if (nz) {
-                                storeSpec(ws.shContrib, N, p, c);
-                                float tmax;
-                                V3 sdir;
-                                if (atInf) {
-                                    sdir = shadowDir;
-                                    tmax = 3.402823466e+38f;
-                                } else {
-                                    V3 dd = lp - sp.p;
-                                    float dist = length(dd);
-                                    sdir = dd * (1.0f / dist);
-                                    tmax = dist * (1 - kRayEpsilon);
-                                }
-                                ws.shOrg[p] = make_float4(sp.p.x, sp.p.y, sp.p.z, kRayEpsilon);
-                                ws.shDir[p] = make_float4(sdir.x, sdir.y, sdir.z, tmax);
-                                shadow = true;
-                            }
-                        }
+                // BSDF sampling (PTRenderer.cpp:220-236).
+                float uc = rng.next(), u0 = rng.next(), u1 = rng.next();
+                BsdfSample bs;
+                Spec fs;
+                bsdfSample<K>(B, q, uc, u0, u1, &bs, fs);
+                if (bs.pdf == 0.0f || specIsZero(fs)) {
+                    alive = false;
+                } else {
+                    if ((bs.type & kDirDispersive) && !wlSelected) {
+                        bs.pdf /= kNumLambda;
+                        wlSelected = true;
                     }
-                    // BSDF sampling (PTRenderer.cpp:220-236).
-                    float uc = rng.next(), u0 = rng.next(), u1 = rng.next();
-                    BsdfSample bs;
-                    Spec fs;
-                    bsdfSample(B, q, uc, u0, u1, &bs, fs);
-                    if (bs.pdf == 0.0f || specIsZero(fs)) {
-                        alive = false;
-                    } else {
-                        if ((bs.type & kDirDispersive) && !wlSelected) {
-                            bs.pdf /= kNumLambda;
-                            wlSelected = true;
-                        }
-                        float cg = absDot(bs.dir, q.gn);
-                        float r = 1.0f / bs.pdf;
+                    float cg = absDot(bs.dir, q.gn);
+                    float r = 1.0f / bs.pdf;
 #pragma unroll
-                        for (int k = 0; k < kNumLambda; ++k) alpha.v[k] *= (fs.v[k] * cg) * r;
-                        V3 nd = sp.frame.fromLocal(bs.dir);
-                        ws.rayOrg[p] = make_float4(sp.p.x, sp.p.y, sp.p.z, kRayEpsilon);
-                        ws.rayDir[p] = make_float4(nd.x, nd.y, nd.z, inf);
-                        ws.prevPdf[p] = bs.pdf;
-                        info = (uint32_t)sel | (wlSelected ? kInfoWlSelected : 0u) |
-                               (dirIsDelta(bs.type) ? kInfoPrevDelta : 0u) | (depth << kInfoDepthShift);
-                        ws.info[p] = info;
-                        storeSpec(ws.alpha, N, p, alpha);
-                        extend = true;
-                    }
+                    for (int k = 0; k < kNumLambda; ++k) alpha.v[k] *= (fs.v[k] * cg) * r;
+                    V3 nd = sp.frame.fromLocal(bs.dir);
+                    ws.rayOrg[p] = make_float4(sp.p.x, sp.p.y, sp.p.z, kRayEpsilon);
+                    ws.rayDir[p] = make_float4(nd.x, nd.y, nd.z, inf);
+                    ws.prevPdf[p] = bs.pdf;
+                    info = (uint32_t)sel | (wlSelected ? kInfoWlSelected : 0u) |
+                           (dirIsDelta(bs.type) ? kInfoPrevDelta : 0u) | (depth << kInfoDepthShift);
+                    ws.info[p] = info;
+                    storeSpec(ws.alpha, N, p, alpha);
+                    extend = true;
                 }
             }
             ws.rngCounter[p] = rng.counter;
@@ -1188,6 +1250,9 @@ int uploadScene(const HostScene &hs, const BuiltScene &bs, DeviceScene* ds) {
     UP(bs.vnrm, vnrm);
     UP(bs.vtan, vtan);
     UP(hs.materials, materials);
+    ds->kindMask = 0;
+    for (const DevMaterial &m : hs.materials)
+        if (m.kind < kMatNull) ds->kindMask |= 1u << m.kind;
     UP(hs.spectra, spectra);
     UP(hs.specValues, specValues);
     std::vector<float> ups(upsSpectra(), upsSpectra() + (size_t)upsNumPoints() * kUpsNumSamples);
@@ -1263,7 +1328,8 @@ int RenderEngine::ensure(uint32_t N, uint32_t maxDepth) {
     w->queue[0] = allocDev<uint32_t>(allocs, N, &e); if (!w->queue[0]) goto fail;
     w->queue[1] = allocDev<uint32_t>(allocs, N, &e); if (!w->queue[1]) goto fail;
     w->shadowQueue = allocDev<uint32_t>(allocs, N, &e); if (!w->shadowQueue) goto fail;
-    w->counters = allocDev<uint32_t>(allocs, 3 * (size_t)(maxDepth + 2), &e); if (!w->counters) goto fail;
+    w->classQueue = allocDev<uint32_t>(allocs, (size_t)N * kNumShadeClasses, &e); if (!w->classQueue) goto fail;
+    w->counters = allocDev<uint32_t>(allocs, (size_t)kCtrStride * (maxDepth + 2), &e); if (!w->counters) goto fail;
     w->stats = allocDev<unsigned long long>(allocs, 4, &e); if (!w->stats) goto fail;
     ws = w;
     capacity = N;
@@ -1300,7 +1366,8 @@ static int gridFor(const void* kernel, int block) {
 // Persistent grid sizes (resident blocks per SM x SMs) of the wave kernels,
 // computed once per process.
 struct WaveGrids {
-    int raygen, extend, shade, shadow, accumulate, shadeVol, shadowVol;
+    int raygen, extend, shadow, accumulate, shadeVol, shadowVol, extendSort, shadeMiss;
+    int shadeSurf[kNumShadeClasses - 1];
 };
 static const WaveGrids &waveGrids(int block) {
     static WaveGrids g;
@@ -1308,11 +1375,17 @@ static const WaveGrids &waveGrids(int block) {
     std::call_once(once, [&]() {
         g.raygen = gridFor((const void*)kRaygen, block);
         g.extend = gridFor((const void*)kExtend, block);
-        g.shade = gridFor((const void*)kShade, block);
         g.shadow = gridFor((const void*)kShadow, block);
         g.accumulate = gridFor((const void*)kAccumulate, block);
         g.shadeVol = gridFor((const void*)kShadeVol, block);
         g.shadowVol = gridFor((const void*)kShadowVol, block);
+        g.extendSort = gridFor((const void*)kExtendSort, block);
+        g.shadeMiss = gridFor((const void*)kShadeMiss, block);
+        g.shadeSurf[kMatMatte] = gridFor((const void*)kShadeSurf<kMatMatte>, block);
+        g.shadeSurf[kMatSpecularReflection] = gridFor((const void*)kShadeSurf<kMatSpecularReflection>, block);
+        g.shadeSurf[kMatSpecularScattering] = gridFor((const void*)kShadeSurf<kMatSpecularScattering>, block);
+        g.shadeSurf[kMatGGXReflection] = gridFor((const void*)kShadeSurf<kMatGGXReflection>, block);
+        g.shadeSurf[kMatGGXScattering] = gridFor((const void*)kShadeSurf<kMatGGXScattering>, block);
     });
     return g;
 }
@@ -1382,33 +1455,76 @@ static uint64_t runWaves(const DeviceScene &ds, const slrgpu_settings &s, const 
         wp.numPaths = wp.samplesInWave * pl.gridPositions;
         wp.maxDepth = D;
         wp.seed = s.seed;
-        cudaMemsetAsync(w.counters, 0, 3 * (size_t)(D + 2) * sizeof(uint32_t), stream);
+        cudaMemsetAsync(w.counters, 0, (size_t)kCtrStride * (D + 2) * sizeof(uint32_t), stream);
         lm.begin(SLRGPU_KERNEL_RAYGEN);
         kRaygen<<<g.raygen, block, 0, stream>>>(ds.sc, w, wp);
         lm.end();
         ++launches;
         for (uint32_t b = 0; b <= D; ++b) {
-            uint32_t* inCount = w.counters + b;
-            uint32_t* outCount = w.counters + b + 1;
-            uint32_t* shCount = w.counters + (D + 2) + b;
+            uint32_t* ctr = w.counters + (size_t)kCtrStride * b;
+            uint32_t* next = ctr + kCtrStride;
+            uint32_t* inQueue = w.queue[b & 1];
+            uint32_t* outQueue = w.queue[(b + 1) & 1];
+            if (s.volumetric) {
+                lm.begin(SLRGPU_KERNEL_EXTEND);
+                kExtend<<<g.extend, block, 0, stream>>>(ds.sc, w, inQueue, ctr + kCtrExt);
+                lm.end();
+                lm.begin(SLRGPU_KERNEL_SHADE);
+                kShadeVol<<<g.shadeVol, block, 0, stream>>>(ds.sc, w, wp, inQueue, ctr + kCtrExt, outQueue,
+                                                            next + kCtrExt, w.shadowQueue, ctr + kCtrShadow);
+                lm.end();
+                lm.begin(SLRGPU_KERNEL_SHADOW);
+                kShadowVol<<<g.shadowVol, block, 0, stream>>>(ds.sc, w, wp, w.shadowQueue, ctr + kCtrShadow, b);
+                lm.end();
+                launches += 3;
+                continue;
+            }
+            // Closest hits, sorted into one queue per shading class.
             lm.begin(SLRGPU_KERNEL_EXTEND);
-            kExtend<<<g.extend, block, 0, stream>>>(ds.sc, w, w.queue[b & 1], inCount);
+            kExtendSort<<<g.extendSort, block, 0, stream>>>(ds.sc, w, inQueue, ctr + kCtrExt, ctr);
             lm.end();
-            lm.begin(SLRGPU_KERNEL_SHADE);
-            if (s.volumetric)
-                kShadeVol<<<g.shadeVol, block, 0, stream>>>(ds.sc, w, wp, w.queue[b & 1], inCount,
-                                                            w.queue[(b + 1) & 1], outCount, w.shadowQueue, shCount);
-            else
-                kShade<<<g.shade, block, 0, stream>>>(ds.sc, w, wp, w.queue[b & 1], inCount, w.queue[(b + 1) & 1],
-                                                      outCount, w.shadowQueue, shCount);
-            lm.end();
+            ++launches;
+            if (ds.sc.envPresent) {
+                lm.begin(SLRGPU_KERNEL_SHADE);
+                kShadeMiss<<<g.shadeMiss, block, 0, stream>>>(ds.sc, w, w.classQueue + (size_t)kClassMiss * w.N,
+                                                              ctr + kClassMiss);
+                lm.end();
+                ++launches;
+            }
+            // One kernel per material kind present in the scene.
+            for (int k = 0; k < kNumShadeClasses - 1; ++k) {
+                if (!(ds.kindMask & (1u << k))) continue;
+                const uint32_t* cq = w.classQueue + (size_t)k * w.N;
+                lm.begin(SLRGPU_KERNEL_SHADE);
+                switch (k) {
+                case kMatMatte:
+                    kShadeSurf<kMatMatte><<<g.shadeSurf[k], block, 0, stream>>>(
+                        ds.sc, w, wp, cq, ctr + k, outQueue, next + kCtrExt, w.shadowQueue, ctr + kCtrShadow);
+                    break;
+                case kMatSpecularReflection:
+                    kShadeSurf<kMatSpecularReflection><<<g.shadeSurf[k], block, 0, stream>>>(
+                        ds.sc, w, wp, cq, ctr + k, outQueue, next + kCtrExt, w.shadowQueue, ctr + kCtrShadow);
+                    break;
+                case kMatSpecularScattering:
+                    kShadeSurf<kMatSpecularScattering><<<g.shadeSurf[k], block, 0, stream>>>(
+                        ds.sc, w, wp, cq, ctr + k, outQueue, next + kCtrExt, w.shadowQueue, ctr + kCtrShadow);
+                    break;
+                case kMatGGXReflection:
+                    kShadeSurf<kMatGGXReflection><<<g.shadeSurf[k], block, 0, stream>>>(
+                        ds.sc, w, wp, cq, ctr + k, outQueue, next + kCtrExt, w.shadowQueue, ctr + kCtrShadow);
+                    break;
+                default:
+                    kShadeSurf<kMatGGXScattering><<<g.shadeSurf[k], block, 0, stream>>>(
+                        ds.sc, w, wp, cq, ctr + k, outQueue, next + kCtrExt, w.shadowQueue, ctr + kCtrShadow);
+                    break;
+                }
+                lm.end();
+                ++launches;
+            }
             lm.begin(SLRGPU_KERNEL_SHADOW);
-            if (s.volumetric)
-                kShadowVol<<<g.shadowVol, block, 0, stream>>>(ds.sc, w, wp, w.shadowQueue, shCount, b);
-            else
-                kShadow<<<g.shadow, block, 0, stream>>>(ds.sc, w, w.shadowQueue, shCount);
+            kShadow<<<g.shadow, block, 0, stream>>>(ds.sc, w, w.shadowQueue, ctr + kCtrShadow);
             lm.end();
-            launches += 3;
+            ++launches;
         }
         lm.begin(SLRGPU_KERNEL_ACCUMULATE);
         kAccumulate<<<g.accumulate, block, 0, stream>>>(w, wp, filmSum, filmComp);
@@ -1531,8 +1647,9 @@ constexpr size_t kNaShContrib = naAlign(kNaShDir + 16ull * kNoAllocMaxPaths);
 constexpr size_t kNaQueue0 = naAlign(kNaShContrib + 4ull * kNumLambda * kNoAllocMaxPaths);
 constexpr size_t kNaQueue1 = naAlign(kNaQueue0 + 4ull * kNoAllocMaxPaths);
 constexpr size_t kNaShQueue = naAlign(kNaQueue1 + 4ull * kNoAllocMaxPaths);
-constexpr size_t kNaCounters = naAlign(kNaShQueue + 4ull * kNoAllocMaxPaths);
-constexpr size_t kNaStats = naAlign(kNaCounters + 4ull * 3 * (kNoAllocMaxDepth + 2));
+constexpr size_t kNaClassQueue = naAlign(kNaShQueue + 4ull * kNoAllocMaxPaths);
+constexpr size_t kNaCounters = naAlign(kNaClassQueue + 4ull * kNumShadeClasses * kNoAllocMaxPaths);
+constexpr size_t kNaStats = naAlign(kNaCounters + 4ull * kCtrStride * (kNoAllocMaxDepth + 2));
 constexpr size_t kNaFilmSum = naAlign(kNaStats + 8ull * 4);
 constexpr size_t kNaFilmComp = naAlign(kNaFilmSum + 4ull * kNumLambda * kNoAllocMaxPaths);
 constexpr size_t kNoAllocScratchBytes = naAlign(kNaFilmComp + 4ull * kNumLambda * kNoAllocMaxPaths);
@@ -1614,6 +1731,7 @@ int renderNoAlloc(const DeviceScene &ds, const slrgpu_settings &s, float* film, 
     w.queue[0] = (uint32_t*)(base + kNaQueue0);
     w.queue[1] = (uint32_t*)(base + kNaQueue1);
     w.shadowQueue = (uint32_t*)(base + kNaShQueue);
+    w.classQueue = (uint32_t*)(base + kNaClassQueue);
     w.counters = (uint32_t*)(base + kNaCounters);
     w.stats = (unsigned long long*)(base + kNaStats);
     float* filmSum = (float*)(base + kNaFilmSum);

@@ -24,6 +24,7 @@ struct DeviceBuffers {
 struct DeviceScene {
     DevScene sc;
     DeviceBuffers buffers;
+    uint32_t kindMask = 0;   // bit k: some material of kind k (MaterialKind) exists
 };
 
 struct WaveState;
