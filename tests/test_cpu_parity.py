@@ -104,3 +104,10 @@ def test_microfacet_bsdf_restatement_matches_golden():
         ok_f = (np.abs(fs - rf) <= tol[:, None] * np.abs(rf) + 1e-30).all(1)
         ok_p = np.abs(pdf - rp) <= tol * np.abs(rp) + 1e-30
         assert ok_f.mean() > 0.998 and ok_p.mean() > 0.998, (ok_f.mean(), ok_p.mean())
+
+
+def test_sbvh_full_ggx_scene(gpu_lib, oracle_lib):
+    """The benchmark's 1,034,242-triangle scene: the whole SBVH (every node's
+    box and words, every leaf reference) equals the reference's."""
+    st = _sbvh_equal(gpu_lib, oracle_lib, scenes.heightfield_scene(seed=0))
+    assert st.num_triangles == 1034242
