@@ -201,6 +201,70 @@ int slrgpu_render(slrgpu_handle scene, const slrgpu_settings* settings, float* f
 int slrgpu_render_noalloc(slrgpu_handle scene, const slrgpu_settings* settings, float* film_device, void* stream);
 uint64_t slrgpu_render_noalloc_scratch_bytes(void);
 
+/* Serving ------------------------------------------------------------- *
+ * No counterpart in the reference, whose renderers take one blocking render
+ * call at a time.  A server renders queued requests (any committed scene of
+ * its context, any resolution, spp and max depth) with continuous batching:
+ * requests are admitted oldest first while their films fit the HBM budget;
+ * in SLRGPU_SERVER_BATCHED mode each wave of launches carries the next
+ * samples of several admitted requests of one scene (up to 32), and waves of
+ * different scenes run concurrently on separate streams and path-state
+ * slots; requests that arrive while others are on the GPU join the next
+ * wave.  SLRGPU_SERVER_PLAIN renders one request at a time, like
+ * slrgpu_render.  A request's film is bit-identical in both modes and to
+ * slrgpu_render with the same settings: its random numbers depend only on
+ * (seed, sample, pixel) and its samples are accumulated in order.  A scene
+ * cannot be destroyed while it has unfinished requests. */
+#define SLRGPU_SERVER_PLAIN 0u
+#define SLRGPU_SERVER_BATCHED 1u
+
+#define SLRGPU_REQUEST_QUEUED 0
+#define SLRGPU_REQUEST_RUNNING 1
+#define SLRGPU_REQUEST_DONE 2
+
+typedef struct slrgpu_server_config {
+    uint32_t mode;              /* SLRGPU_SERVER_PLAIN or SLRGPU_SERVER_BATCHED */
+    uint32_t slots;             /* path-state slots = waves in flight; 0: 4 (plain: 1) */
+    uint32_t paths_per_slot;    /* 0: 4 Mi paths (about 2 GB per slot) */
+    uint32_t max_depth;         /* largest max_depth accepted; 0: 64 */
+    uint64_t hbm_budget_bytes;  /* device bytes for admitted requests' films; 0: 150 GB */
+} slrgpu_server_config;
+
+typedef struct slrgpu_request_info {
+    int32_t status;             /* SLRGPU_REQUEST_* or a negative error code */
+    uint32_t spp_done;
+    double submit_seconds;      /* since the server's creation */
+    double start_seconds;       /* admission */
+    double done_seconds;
+    uint64_t path_samples;      /* sample grid positions * spp done */
+    uint64_t dropped_samples;
+} slrgpu_request_info;
+
+typedef struct slrgpu_server_stats {
+    uint64_t requests_done;
+    uint64_t path_samples_done;
+    uint64_t waves;
+    uint64_t kernel_launches;
+    uint64_t bytes_in_use;      /* films of admitted requests */
+    uint32_t queued, active;
+    double first_start_seconds;
+    double last_done_seconds;
+} slrgpu_server_stats;
+
+int slrgpu_server_create(slrgpu_handle ctx, const slrgpu_server_config* config, slrgpu_handle* server);
+/* Finishes the waves on the GPU; queued requests end with an error status. */
+int slrgpu_server_destroy(slrgpu_handle server);
+int slrgpu_server_submit(slrgpu_handle server, slrgpu_handle scene, const slrgpu_settings* settings,
+                         uint64_t* request);
+int slrgpu_server_poll(slrgpu_handle server, uint64_t request, slrgpu_request_info* info);
+/* Blocks until the request is done (timeout_seconds < 0: no limit;
+ * SLRGPU_ERR_TIMEOUT otherwise), copies its film (width*height*16 floats,
+ * the layout of slrgpu_render; film may be NULL) to host memory and
+ * releases the request. */
+int slrgpu_server_wait(slrgpu_handle server, uint64_t request, float* film, slrgpu_request_info* info,
+                       double timeout_seconds);
+int slrgpu_server_get_stats(slrgpu_handle server, slrgpu_server_stats* stats);
+
 /* Ray queries on the committed scene (device pointers).  rays: n x 8 floats
  * (org.xyz, tmin, dir.xyz, tmax).  Closest hit fills prim (0xffffffff on
  * miss), t, b1, b2 (Moller-Trumbore barycentrics); any hit fills prim with 1

@@ -65,6 +65,33 @@ class RenderStats(C.Structure):
         return d
 
 
+class ServerConfig(C.Structure):
+    _fields_ = [("mode", C.c_uint32), ("slots", C.c_uint32), ("paths_per_slot", C.c_uint32),
+                ("max_depth", C.c_uint32), ("hbm_budget_bytes", C.c_uint64)]
+
+
+class RequestInfo(C.Structure):
+    _fields_ = [("status", C.c_int32), ("spp_done", C.c_uint32), ("submit_seconds", C.c_double),
+                ("start_seconds", C.c_double), ("done_seconds", C.c_double), ("path_samples", C.c_uint64),
+                ("dropped_samples", C.c_uint64)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("requests_done", C.c_uint64), ("path_samples_done", C.c_uint64), ("waves", C.c_uint64),
+                ("kernel_launches", C.c_uint64), ("bytes_in_use", C.c_uint64), ("queued", C.c_uint32),
+                ("active", C.c_uint32), ("first_start_seconds", C.c_double), ("last_done_seconds", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+SERVER_PLAIN, SERVER_BATCHED = 0, 1
+REQUEST_QUEUED, REQUEST_RUNNING, REQUEST_DONE = 0, 1, 2
+
+
 def header_symbols() -> list[str]:
     """Every function the C ABI header declares."""
     text = HEADER.read_text()
@@ -113,6 +140,12 @@ def lib():
             "slrgpu_render_noalloc": (I, [H, C.POINTER(Settings), P, P]),
             "slrgpu_render_noalloc_scratch_bytes": (C.c_uint64, []),
             "slrgpu_medium_query": (I, [H, I, U, fp, fp, ip, up, U, fp]),
+            "slrgpu_server_create": (I, [H, C.POINTER(ServerConfig), hp]),
+            "slrgpu_server_destroy": (I, [H]),
+            "slrgpu_server_submit": (I, [H, H, C.POINTER(Settings), hp]),
+            "slrgpu_server_poll": (I, [H, C.c_uint64, C.POINTER(RequestInfo)]),
+            "slrgpu_server_wait": (I, [H, C.c_uint64, fp, C.POINTER(RequestInfo), C.c_double]),
+            "slrgpu_server_get_stats": (I, [H, C.POINTER(ServerStats)]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -390,6 +423,57 @@ def bsdf_query(kind: str, spec0, spec1=None, spec2=None, ax=0.0, ay=0.0, queries
     out = np.zeros((len(q), 40), np.float32)
     check(lib().slrgpu_bsdf_query(BSDF_KINDS[kind], _fp(s0), _fp(s1), _fp(s2), ax, ay, _fp(q), len(q), _fp(out)))
     return out
+
+
+class Server:
+    """Serving loop with continuous batching (slrgpu_server_*): submit render
+    requests of any committed scene of the context; wait() returns the film,
+    bit-identical to Scene.render with the same settings."""
+
+    def __init__(self, context: Context | None = None, mode: int = SERVER_BATCHED, slots: int = 0,
+                 paths_per_slot: int = 0, max_depth: int = 0, hbm_budget_bytes: int = 0):
+        self.context = context or default_context()
+        cfg = ServerConfig(mode, slots, paths_per_slot, max_depth, hbm_budget_bytes)
+        h = C.c_uint64()
+        check(lib().slrgpu_server_create(self.context.handle, C.byref(cfg), C.byref(h)))
+        self.handle = h.value
+        self._shapes = {}
+
+    def submit(self, scene: "Scene", width: int, height: int, spp: int, max_depth: int, seed: int = 0,
+               volumetric: bool = False) -> int:
+        s = Settings(width, height, spp, max_depth, seed & 0xffffffff, int(volumetric), 0, 0)
+        rid = C.c_uint64()
+        check(lib().slrgpu_server_submit(self.handle, scene.handle, C.byref(s), C.byref(rid)))
+        self._shapes[rid.value] = (height, width)
+        return rid.value
+
+    def poll(self, request: int) -> RequestInfo:
+        info = RequestInfo()
+        check(lib().slrgpu_server_poll(self.handle, request, C.byref(info)))
+        return info
+
+    def wait(self, request: int, timeout: float = -1.0):
+        h, w = self._shapes.pop(request)
+        film = np.zeros((h, w, 16), np.float32)
+        info = RequestInfo()
+        check(lib().slrgpu_server_wait(self.handle, request, _fp(film), C.byref(info), float(timeout)))
+        return film, info
+
+    def stats(self) -> ServerStats:
+        st = ServerStats()
+        check(lib().slrgpu_server_get_stats(self.handle, C.byref(st)))
+        return st
+
+    def close(self):
+        if getattr(self, "handle", 0):
+            lib().slrgpu_server_destroy(self.handle)
+            self.handle = 0
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class PathTracingRenderer:

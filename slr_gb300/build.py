@@ -21,7 +21,7 @@ LIB_DIR = PKG / "lib"
 LIB = LIB_DIR / "libslrgpu.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-HOST_SOURCES = ["scene_host.cpp", "capi.cpp"]
+HOST_SOURCES = ["scene_host.cpp", "capi.cpp", "server.cpp"]
 CUDA_SOURCES = ["render.cu"]
 
 

@@ -1,6 +1,7 @@
 // C ABI of the GPU path tracer (declared in include/slrgpu.h).
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <cstring>
@@ -12,6 +13,7 @@
 #include "../../include/slrgpu.h"
 #include "render_api.h"
 #include "scene_host.h"
+#include "server.h"
 
 namespace slrgpu {
 
@@ -31,12 +33,25 @@ struct Scene {
     bool hostBuilt = false;
     DeviceScene dev;
     bool committed = false;
+    std::atomic<int> inFlight{0};   // unfinished server requests
     std::mutex mu;
+};
+
+struct ServerRec {
+    Context* ctx = nullptr;
+    std::unique_ptr<Server> server;
 };
 
 std::mutex g_registryMu;
 std::unordered_map<uint64_t, std::unique_ptr<Context>> g_contexts;
 std::unordered_map<uint64_t, std::unique_ptr<Scene>> g_scenes;
+std::unordered_map<uint64_t, std::unique_ptr<ServerRec>> g_servers;
+
+ServerRec* findServer(slrgpu_handle h) {
+    std::lock_guard<std::mutex> lock(g_registryMu);
+    auto it = g_servers.find(h);
+    return it == g_servers.end() ? nullptr : it->second.get();
+}
 
 Context* findContext(slrgpu_handle h) {
     std::lock_guard<std::mutex> lock(g_registryMu);
@@ -131,6 +146,8 @@ int slrgpu_context_destroy(slrgpu_handle ctx) {
         if (it == g_contexts.end()) return fail(SLRGPU_ERR_INVALID_HANDLE, "invalid context handle");
         for (auto &kv : g_scenes)
             if (kv.second->ctx == it->second.get()) return fail(SLRGPU_ERR_STATE, "context still has scenes");
+        for (auto &kv : g_servers)
+            if (kv.second->ctx == it->second.get()) return fail(SLRGPU_ERR_STATE, "context still has servers");
         c = std::move(it->second);
         g_contexts.erase(it);
     }
@@ -161,6 +178,7 @@ int slrgpu_scene_destroy(slrgpu_handle scene) {
         std::lock_guard<std::mutex> lock(g_registryMu);
         auto it = g_scenes.find(scene);
         if (it == g_scenes.end()) return fail(SLRGPU_ERR_INVALID_HANDLE, "invalid scene handle");
+        if (it->second->inFlight.load() > 0) return fail(SLRGPU_ERR_STATE, "scene has unfinished server requests");
         s = std::move(it->second);
         g_scenes.erase(it);
     }
@@ -437,6 +455,75 @@ int slrgpu_medium_query(slrgpu_handle scene, int mode, uint32_t n, const float* 
     cudaError_t e = cudaSetDevice(s->ctx->device);
     if (e != cudaSuccess) return fail(SLRGPU_ERR_CUDA, cudaGetErrorString(e));
     return mediumQuery(s->dev, mode, n, rays, lambdas, sel, vals, num_vals, out);
+}
+
+// ---- serving -------------------------------------------------------------------
+int slrgpu_server_create(slrgpu_handle ctx, const slrgpu_server_config* config, slrgpu_handle* server) {
+    if (!server) return fail(SLRGPU_ERR_INVALID_ARGUMENT, "server is NULL");
+    Context* c = findContext(ctx);
+    if (!c) return fail(SLRGPU_ERR_INVALID_HANDLE, "invalid context handle");
+    slrgpu_server_config cfg;
+    std::memset(&cfg, 0, sizeof(cfg));
+    if (config) cfg = *config;
+    std::unique_ptr<ServerRec> rec(new ServerRec());
+    rec->ctx = c;
+    rec->server.reset(new Server(c->device, cfg));
+    int rc = rec->server->init();
+    if (rc != SLRGPU_OK) return rc;
+    uint64_t h = (uint64_t)(uintptr_t)rec.get();
+    std::lock_guard<std::mutex> lock(g_registryMu);
+    g_servers[h] = std::move(rec);
+    *server = h;
+    return SLRGPU_OK;
+}
+
+int slrgpu_server_destroy(slrgpu_handle server) {
+    std::unique_ptr<ServerRec> rec;
+    {
+        std::lock_guard<std::mutex> lock(g_registryMu);
+        auto it = g_servers.find(server);
+        if (it == g_servers.end()) return fail(SLRGPU_ERR_INVALID_HANDLE, "invalid server handle");
+        rec = std::move(it->second);
+        g_servers.erase(it);
+    }
+    rec->server.reset();
+    return SLRGPU_OK;
+}
+
+int slrgpu_server_submit(slrgpu_handle server, slrgpu_handle scene, const slrgpu_settings* settings,
+                         uint64_t* request) {
+    ServerRec* rec = findServer(server);
+    if (!rec) return fail(SLRGPU_ERR_INVALID_HANDLE, "invalid server handle");
+    if (!settings || !request) return fail(SLRGPU_ERR_INVALID_ARGUMENT, "settings and request must not be NULL");
+    const bool mutating = false;
+    GET_SCENE(s, scene);
+    if (!s->committed) return fail(SLRGPU_ERR_NOT_COMMITTED, "scene not committed");
+    if (s->ctx != rec->ctx) return fail(SLRGPU_ERR_INVALID_ARGUMENT, "scene belongs to another context");
+    if (!s->host.cameraPresent) return fail(SLRGPU_ERR_STATE, "scene has no camera");
+    if (settings->volumetric && !s->host.medium.present)
+        return fail(SLRGPU_ERR_INVALID_ARGUMENT, "volumetric render of a scene without medium");
+    return rec->server->submit(&s->dev, &s->inFlight, *settings, request);
+}
+
+int slrgpu_server_poll(slrgpu_handle server, uint64_t request, slrgpu_request_info* info) {
+    ServerRec* rec = findServer(server);
+    if (!rec) return fail(SLRGPU_ERR_INVALID_HANDLE, "invalid server handle");
+    return rec->server->poll(request, info);
+}
+
+int slrgpu_server_wait(slrgpu_handle server, uint64_t request, float* film, slrgpu_request_info* info,
+                       double timeout_seconds) {
+    ServerRec* rec = findServer(server);
+    if (!rec) return fail(SLRGPU_ERR_INVALID_HANDLE, "invalid server handle");
+    return rec->server->wait(request, film, info, timeout_seconds);
+}
+
+int slrgpu_server_get_stats(slrgpu_handle server, slrgpu_server_stats* stats) {
+    ServerRec* rec = findServer(server);
+    if (!rec) return fail(SLRGPU_ERR_INVALID_HANDLE, "invalid server handle");
+    if (!stats) return fail(SLRGPU_ERR_INVALID_ARGUMENT, "stats is NULL");
+    rec->server->stats(stats);
+    return SLRGPU_OK;
 }
 
 // ---- host-side diagnostics ----------------------------------------------------

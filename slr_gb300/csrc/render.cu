@@ -45,6 +45,7 @@ struct WaveState {
     float* initY;
     float* camWeight;
     uint32_t* rngCounter;
+    uint2* rngKey;       // counter-RNG key of the path (seed, sample index, grid position)
     float4* shOrg;
     float4* shDir;
     float* shContrib;    // [16][N]
@@ -66,15 +67,30 @@ __host__ __device__ __forceinline__ uint32_t padToTile(uint32_t n) {
     return (n + kSensorTile - 1) / kSensorTile * kSensorTile;
 }
 
-struct WaveParams {
+// One request's share of a wave: `samples` consecutive sample indices from
+// `sampleBase`, each over every position of the request's tile-padded grid,
+// as the paths [pathBegin, pathBegin + samples * gridPositions).  A path's
+// random numbers depend only on (seed, sample index, grid position), so a
+// request renders the same alone or in a wave shared with others.
+struct WaveSegment {
+    uint32_t pathBegin;
     uint32_t width, height;   // image
     uint32_t gridW, gridH;    // tile-padded sample grid
-    uint32_t numPixels;       // gridW * gridH sample positions per sample index
-    uint32_t samplesInWave;   // S
-    uint32_t sampleBase;      // first sample index of the wave
-    uint32_t numPaths;
-    uint32_t maxDepth;
+    uint32_t gridPositions;   // gridW * gridH
+    uint32_t sampleBase, samples;
     uint32_t seed;
+    uint32_t filmBegin;       // first pixel of the request in the wave's film enumeration
+    float* filmSum;           // [16][width * height], Kahan sum and compensation
+    float* filmComp;
+    unsigned long long* dropped;   // non-finite samples of the request
+};
+constexpr int kMaxWaveSegments = 32;
+struct WaveParams {
+    uint32_t numSegments;
+    uint32_t numPaths;        // sum of samples * gridPositions
+    uint32_t filmPixels;      // sum of width * height
+    uint32_t pad;
+    WaveSegment seg[kMaxWaveSegments];
 };
 
 // Per-bounce counter block: [0, kNumShadeClasses) paths per shading class,
@@ -115,10 +131,9 @@ __device__ __forceinline__ void queuePush(uint32_t* queue, uint32_t* count, uint
     queue[base + __popc(mask & ((1u << lane) - 1))] = value;
 }
 
-__device__ __forceinline__ uint64_t sampleIndexOf(const WaveParams &wp, uint32_t p) {
-    uint32_t s = p / wp.numPixels;
-    uint32_t pixel = p - s * wp.numPixels;
-    return (uint64_t)(wp.sampleBase + s) * wp.numPixels + pixel;
+__device__ __forceinline__ uint64_t loadKey(const WaveState &ws, uint32_t p) {
+    uint2 k = ws.rngKey[p];
+    return ((uint64_t)k.y << 32) | k.x;
 }
 
 // ---------------------------------------------------------------------------
@@ -243,13 +258,19 @@ __device__ __noinline__ void makeBsdf(const DevScene &sc, const DevMaterial &m, 
 // ---------------------------------------------------------------------------
 // Kernels
 // ---------------------------------------------------------------------------
-__global__ void kRaygen(DevScene sc, WaveState ws, WaveParams wp) {
+__global__ void kRaygen(DevScene sc, WaveState ws, const __grid_constant__ WaveParams wp) {
     if (blockIdx.x == 0 && threadIdx.x == 0) ws.counters[kCtrExt] = wp.numPaths;
     for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < wp.numPaths; p += gridDim.x * blockDim.x) {
-        uint32_t s = p / wp.numPixels;
-        uint32_t pixel = p - s * wp.numPixels;
-        uint32_t ix = pixel % wp.gridW, iy = pixel / wp.gridW;
-        Rng rng{pathKey(wp.seed, (uint64_t)(wp.sampleBase + s) * wp.numPixels + pixel), 0};
+        uint32_t k = 0;
+        while (k + 1 < wp.numSegments && p >= wp.seg[k + 1].pathBegin) ++k;
+        const WaveSegment &sg = wp.seg[k];
+        const uint32_t q = p - sg.pathBegin;
+        uint32_t s = q / sg.gridPositions;
+        uint32_t pixel = q - s * sg.gridPositions;
+        uint32_t ix = pixel % sg.gridW, iy = pixel / sg.gridW;
+        const uint64_t key = pathKey(sg.seed, (uint64_t)(sg.sampleBase + s) * sg.gridPositions + pixel);
+        ws.rngKey[p] = make_uint2((uint32_t)key, (uint32_t)(key >> 32));
+        Rng rng{key, 0};
         // Draw order of Job::kernel: time, pixel (2), wavelength offset,
         // wavelength selection, lens (2) (PTRenderer.cpp:108-116).
         (void)rng.next();
@@ -262,7 +283,7 @@ __global__ void kRaygen(DevScene sc, WaveState ws, WaveParams wp) {
         const float selectWLPDF = kNumLambda / (kWavelengthHigh - kWavelengthLow);
         V3 org, dir;
         float w;
-        cameraRay(sc.camera, lu0, lu1, pxf / wp.width, pyf / wp.height, &org, &dir, &w);
+        cameraRay(sc.camera, lu0, lu1, pxf / sg.width, pyf / sg.height, &org, &dir, &w);
         ws.camWeight[p] = w / selectWLPDF;
         ws.rayOrg[p] = make_float4(org.x, org.y, org.z, 0.0f);
         ws.rayDir[p] = make_float4(dir.x, dir.y, dir.z, __int_as_float(0x7f800000));
@@ -437,7 +458,7 @@ __device__ __forceinline__ void makeBsdfK(const DevScene &sc, const DevMaterial 
 }
 
 template <int K>
-__global__ void __launch_bounds__(256) kShadeSurf(DevScene sc, WaveState ws, WaveParams wp,
+__global__ void __launch_bounds__(256) kShadeSurf(DevScene sc, WaveState ws, uint32_t maxDepth,
                                                   const uint32_t* __restrict__ inQueue,
                                                   const uint32_t* __restrict__ inCount, uint32_t* outQueue,
                                                   uint32_t* outCount, uint32_t* shQueue, uint32_t* shCount) {
@@ -460,7 +481,7 @@ __global__ void __launch_bounds__(256) kShadeSurf(DevScene sc, WaveState ws, Wav
             float lambdas[kNumLambda];
 #pragma unroll
             for (int k = 0; k < kNumLambda; ++k) lambdas[k] = lambdaAt(k, wlOff);
-            Rng rng{pathKey(wp.seed, sampleIndexOf(wp, p)), ws.rngCounter[p]};
+            Rng rng{loadKey(ws, p), ws.rngCounter[p]};
             float4 ro = ws.rayOrg[p], rd = ws.rayDir[p];
             V3 org = V3{ro.x, ro.y, ro.z}, dir = V3{rd.x, rd.y, rd.z};
             float4 hv = ws.hit[p];
@@ -503,7 +524,7 @@ __global__ void __launch_bounds__(256) kShadeSurf(DevScene sc, WaveState ws, Wav
             }
             if (alive) {
                 ++depth;
-                if (depth > wp.maxDepth) alive = false;
+                if (depth > maxDepth) alive = false;
             }
             if (alive) {
                 Bsdf B;
@@ -675,7 +696,7 @@ __device__ __forceinline__ int selectLight3(const DevScene &sc, float u, int* li
     return idx;
 }
 
-__global__ void __launch_bounds__(256) kShadeVol(DevScene sc, WaveState ws, WaveParams wp,
+__global__ void __launch_bounds__(256) kShadeVol(DevScene sc, WaveState ws, uint32_t maxDepth,
                                                  const uint32_t* __restrict__ inQueue,
                                                  const uint32_t* __restrict__ inCount, uint32_t* outQueue,
                                                  uint32_t* outCount, uint32_t* shQueue, uint32_t* shCount) {
@@ -699,7 +720,7 @@ __global__ void __launch_bounds__(256) kShadeVol(DevScene sc, WaveState ws, Wave
             float lambdas[kNumLambda];
 #pragma unroll
             for (int k = 0; k < kNumLambda; ++k) lambdas[k] = lambdaAt(k, wlOff);
-            Rng rng{pathKey(wp.seed, sampleIndexOf(wp, p)), ws.rngCounter[p]};
+            Rng rng{loadKey(ws, p), ws.rngCounter[p]};
             float4 ro = ws.rayOrg[p], rd = ws.rayDir[p];
             V3 org = V3{ro.x, ro.y, ro.z}, dir = V3{rd.x, rd.y, rd.z};
             float4 hv = ws.hit[p];
@@ -804,7 +825,7 @@ __global__ void __launch_bounds__(256) kShadeVol(DevScene sc, WaveState ws, Wave
             }
             if (alive) {
                 ++depth;
-                if (depth > wp.maxDepth) alive = false;
+                if (depth > maxDepth) alive = false;
             }
             if (alive) {
                 V3 dirOut = frame.toLocal(-dir);
@@ -964,7 +985,7 @@ __global__ void __launch_bounds__(256) kShadeVol(DevScene sc, WaveState ws, Wave
 // Shadow rays of the volumetric integrator: occlusion by surfaces, then the
 // medium's spectral transmittance (Scene::testVisibility, Scene.cpp:114-135),
 // drawn from a per-bounce random stream of the path.
-__global__ void kShadowVol(DevScene sc, WaveState ws, WaveParams wp, const uint32_t* __restrict__ queue,
+__global__ void kShadowVol(DevScene sc, WaveState ws, const uint32_t* __restrict__ queue,
                            const uint32_t* __restrict__ count, uint32_t bounce) {
     const uint32_t n = *count;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -983,7 +1004,7 @@ __global__ void kShadowVol(DevScene sc, WaveState ws, WaveParams wp, const uint3
             for (int k = 0; k < kNumLambda; ++k) lambdas[k] = lambdaAt(k, wlOff);
             Spec sigmaE;
             evalSpectrum(sc, sc.medium.sigmaE, lambdas, sigmaE);
-            Rng rng{mix64(pathKey(wp.seed, sampleIndexOf(wp, p)) ^ (0x9e3779b97f4a7c15ull * (bounce + 1))), 0};
+            Rng rng{mix64(loadKey(ws, p) ^ (0x9e3779b97f4a7c15ull * (bounce + 1))), 0};
             mediumTransmittance(sc.medium, org, dir, o.w, d.w, sigmaE, sel, wlSelected, rng, T);
         }
 #pragma unroll
@@ -996,33 +1017,37 @@ __global__ void kShadowVol(DevScene sc, WaveState ws, WaveParams wp, const uint3
 // Adds the wave's paths to the film: C = L * weight, dropped when not finite
 // (PTRenderer.cpp:129-138); binning and compensated sum of
 // SpectrumStorage::add (spectrum_types.h:716-739, CompensatedSum.h:16-33).
-__global__ void kAccumulate(WaveState ws, WaveParams wp, float* filmSum, float* filmComp) {
+__global__ void kAccumulate(WaveState ws, const __grid_constant__ WaveParams wp) {
     const float recBinWidth = kNumLambda / (kWavelengthHigh - kWavelengthLow);
-    const uint32_t P = wp.width * wp.height;
-    unsigned long long dropped = 0;
-    for (uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x; pix < P; pix += gridDim.x * blockDim.x) {
+    for (uint32_t fp = blockIdx.x * blockDim.x + threadIdx.x; fp < wp.filmPixels; fp += gridDim.x * blockDim.x) {
+        uint32_t k = 0;
+        while (k + 1 < wp.numSegments && fp >= wp.seg[k + 1].filmBegin) ++k;
+        const WaveSegment &sg = wp.seg[k];
+        const uint32_t P = sg.width * sg.height;
+        const uint32_t pix = fp - sg.filmBegin;
         float sum[kNumLambda], comp[kNumLambda];
 #pragma unroll
         for (int b = 0; b < kNumLambda; ++b) {
-            sum[b] = filmSum[(size_t)b * P + pix];
-            comp[b] = filmComp[(size_t)b * P + pix];
+            sum[b] = sg.filmSum[(size_t)b * P + pix];
+            comp[b] = sg.filmComp[(size_t)b * P + pix];
         }
+        unsigned long long dropped = 0;
         // Grid positions clamped into this pixel: itself, plus the overhang
         // of the last column / row.
-        const uint32_t x = pix % wp.width, y = pix / wp.width;
-        const uint32_t xEnd = x + 1 == wp.width ? wp.gridW : x + 1;
-        const uint32_t yEnd = y + 1 == wp.height ? wp.gridH : y + 1;
-        for (uint32_t s = 0; s < wp.samplesInWave; ++s)
+        const uint32_t x = pix % sg.width, y = pix / sg.width;
+        const uint32_t xEnd = x + 1 == sg.width ? sg.gridW : x + 1;
+        const uint32_t yEnd = y + 1 == sg.height ? sg.gridH : y + 1;
+        for (uint32_t s = 0; s < sg.samples; ++s)
         for (uint32_t gy = y; gy < yEnd; ++gy)
         for (uint32_t gx = x; gx < xEnd; ++gx) {
-            const uint32_t p = s * wp.numPixels + gy * wp.gridW + gx;
+            const uint32_t p = sg.pathBegin + s * sg.gridPositions + gy * sg.gridW + gx;
             float w = ws.camWeight[p];
             float c[kNumLambda];
             bool finite = true;
 #pragma unroll
-            for (int k = 0; k < kNumLambda; ++k) {
-                c[k] = ws.L[(size_t)k * ws.N + p] * w;
-                finite &= isfinite(c[k]);
+            for (int i = 0; i < kNumLambda; ++i) {
+                c[i] = ws.L[(size_t)i * ws.N + p] * w;
+                finite &= isfinite(c[i]);
             }
             if (!finite) { ++dropped; continue; }
             float wlOff = ws.wlOffset[p];
@@ -1030,13 +1055,13 @@ __global__ void kAccumulate(WaveState ws, WaveParams wp, float* filmSum, float* 
 #pragma unroll
             for (int b = 0; b < kNumLambda; ++b) addend[b] = 0.0f;
 #pragma unroll
-            for (int k = 0; k < kNumLambda; ++k) {
-                float lam = lambdaAt(k, wlOff);
+            for (int i = 0; i < kNumLambda; ++i) {
+                float lam = lambdaAt(i, wlOff);
                 float f = __fmul_rn(__fdiv_rn(__fsub_rn(lam, kWavelengthLow), kWavelengthHigh - kWavelengthLow), (float)kNumLambda);
                 uint32_t bin = min((uint32_t)f, (uint32_t)(kNumLambda - 1));
 #pragma unroll
                 for (int b = 0; b < kNumLambda; ++b)
-                    if (b == (int)bin) addend[b] += c[k] * recBinWidth;
+                    if (b == (int)bin) addend[b] += c[i] * recBinWidth;
             }
 #pragma unroll
             for (int b = 0; b < kNumLambda; ++b) {
@@ -1048,11 +1073,14 @@ __global__ void kAccumulate(WaveState ws, WaveParams wp, float* filmSum, float* 
         }
 #pragma unroll
         for (int b = 0; b < kNumLambda; ++b) {
-            filmSum[(size_t)b * P + pix] = sum[b];
-            filmComp[(size_t)b * P + pix] = comp[b];
+            sg.filmSum[(size_t)b * P + pix] = sum[b];
+            sg.filmComp[(size_t)b * P + pix] = comp[b];
+        }
+        if (dropped) {
+            atomicAdd(&ws.stats[2], dropped);
+            if (sg.dropped) atomicAdd(sg.dropped, dropped);
         }
     }
-    if (dropped) atomicAdd(&ws.stats[2], dropped);
 }
 
 // Film layout conversion [16][P] -> [P][16].
@@ -1322,6 +1350,7 @@ int RenderEngine::ensure(uint32_t N, uint32_t maxDepth) {
     w->initY = allocDev<float>(allocs, N, &e); if (!w->initY) goto fail;
     w->camWeight = allocDev<float>(allocs, N, &e); if (!w->camWeight) goto fail;
     w->rngCounter = allocDev<uint32_t>(allocs, N, &e); if (!w->rngCounter) goto fail;
+    w->rngKey = allocDev<uint2>(allocs, N, &e); if (!w->rngKey) goto fail;
     w->shOrg = allocDev<float4>(allocs, N, &e); if (!w->shOrg) goto fail;
     w->shDir = allocDev<float4>(allocs, N, &e); if (!w->shDir) goto fail;
     w->shContrib = allocDev<float>(allocs, (size_t)N * kNumLambda, &e); if (!w->shContrib) goto fail;
@@ -1432,104 +1461,119 @@ static WavePlan planWaves(const slrgpu_settings &s, uint32_t autoPaths) {
     return pl;
 }
 
-// The wave loop shared by slrgpu_render and slrgpu_render_noalloc: per wave,
-// camera rays for S samples of every grid position, then per bounce
-// extension, shading and shadow kernels over the queues, then the film.
-// Stream-ordered; counters, queues and path state live in w.  Returns the
-// number of kernel launches.
-static uint64_t runWaves(const DeviceScene &ds, const slrgpu_settings &s, const WavePlan &pl, const WaveState &w,
-                         float* filmSum, float* filmComp, cudaStream_t stream, LaunchMarks &lm) {
+// One wave: camera rays for every path of the wave's segments, then per
+// bounce the extension, shading and shadow kernels over the device-side
+// queues, then the film update of every segment.  Stream-ordered; counters,
+// queues and path state live in w.  Returns the number of kernel launches.
+static uint64_t runWave(const DeviceScene &ds, const WaveState &w, const WaveParams &wp, uint32_t D, bool volumetric,
+                        cudaStream_t stream, LaunchMarks &lm) {
     const int block = 256;
     const WaveGrids &g = waveGrids(block);
-    const uint32_t D = s.max_depth;
     uint64_t launches = 0;
-    for (uint32_t base = 0; base < s.spp; base += pl.S) {
-        WaveParams wp;
-        wp.width = s.width;
-        wp.height = s.height;
-        wp.gridW = pl.gridW;
-        wp.gridH = pl.gridH;
-        wp.numPixels = pl.gridPositions;
-        wp.samplesInWave = std::min(pl.S, s.spp - base);
-        wp.sampleBase = base;
-        wp.numPaths = wp.samplesInWave * pl.gridPositions;
-        wp.maxDepth = D;
-        wp.seed = s.seed;
-        cudaMemsetAsync(w.counters, 0, (size_t)kCtrStride * (D + 2) * sizeof(uint32_t), stream);
-        lm.begin(SLRGPU_KERNEL_RAYGEN);
-        kRaygen<<<g.raygen, block, 0, stream>>>(ds.sc, w, wp);
+    cudaMemsetAsync(w.counters, 0, (size_t)kCtrStride * (D + 2) * sizeof(uint32_t), stream);
+    lm.begin(SLRGPU_KERNEL_RAYGEN);
+    kRaygen<<<g.raygen, block, 0, stream>>>(ds.sc, w, wp);
+    lm.end();
+    ++launches;
+    for (uint32_t b = 0; b <= D; ++b) {
+        uint32_t* ctr = w.counters + (size_t)kCtrStride * b;
+        uint32_t* next = ctr + kCtrStride;
+        uint32_t* inQueue = w.queue[b & 1];
+        uint32_t* outQueue = w.queue[(b + 1) & 1];
+        if (volumetric) {
+            lm.begin(SLRGPU_KERNEL_EXTEND);
+            kExtend<<<g.extend, block, 0, stream>>>(ds.sc, w, inQueue, ctr + kCtrExt);
+            lm.end();
+            lm.begin(SLRGPU_KERNEL_SHADE);
+            kShadeVol<<<g.shadeVol, block, 0, stream>>>(ds.sc, w, D, inQueue, ctr + kCtrExt, outQueue,
+                                                        next + kCtrExt, w.shadowQueue, ctr + kCtrShadow);
+            lm.end();
+            lm.begin(SLRGPU_KERNEL_SHADOW);
+            kShadowVol<<<g.shadowVol, block, 0, stream>>>(ds.sc, w, w.shadowQueue, ctr + kCtrShadow, b);
+            lm.end();
+            launches += 3;
+            continue;
+        }
+        // Closest hits, sorted into one queue per shading class.
+        lm.begin(SLRGPU_KERNEL_EXTEND);
+        kExtendSort<<<g.extendSort, block, 0, stream>>>(ds.sc, w, inQueue, ctr + kCtrExt, ctr);
         lm.end();
         ++launches;
-        for (uint32_t b = 0; b <= D; ++b) {
-            uint32_t* ctr = w.counters + (size_t)kCtrStride * b;
-            uint32_t* next = ctr + kCtrStride;
-            uint32_t* inQueue = w.queue[b & 1];
-            uint32_t* outQueue = w.queue[(b + 1) & 1];
-            if (s.volumetric) {
-                lm.begin(SLRGPU_KERNEL_EXTEND);
-                kExtend<<<g.extend, block, 0, stream>>>(ds.sc, w, inQueue, ctr + kCtrExt);
-                lm.end();
-                lm.begin(SLRGPU_KERNEL_SHADE);
-                kShadeVol<<<g.shadeVol, block, 0, stream>>>(ds.sc, w, wp, inQueue, ctr + kCtrExt, outQueue,
-                                                            next + kCtrExt, w.shadowQueue, ctr + kCtrShadow);
-                lm.end();
-                lm.begin(SLRGPU_KERNEL_SHADOW);
-                kShadowVol<<<g.shadowVol, block, 0, stream>>>(ds.sc, w, wp, w.shadowQueue, ctr + kCtrShadow, b);
-                lm.end();
-                launches += 3;
-                continue;
-            }
-            // Closest hits, sorted into one queue per shading class.
-            lm.begin(SLRGPU_KERNEL_EXTEND);
-            kExtendSort<<<g.extendSort, block, 0, stream>>>(ds.sc, w, inQueue, ctr + kCtrExt, ctr);
-            lm.end();
-            ++launches;
-            if (ds.sc.envPresent) {
-                lm.begin(SLRGPU_KERNEL_SHADE);
-                kShadeMiss<<<g.shadeMiss, block, 0, stream>>>(ds.sc, w, w.classQueue + (size_t)kClassMiss * w.N,
-                                                              ctr + kClassMiss);
-                lm.end();
-                ++launches;
-            }
-            // One kernel per material kind present in the scene.
-            for (int k = 0; k < kNumShadeClasses - 1; ++k) {
-                if (!(ds.kindMask & (1u << k))) continue;
-                const uint32_t* cq = w.classQueue + (size_t)k * w.N;
-                lm.begin(SLRGPU_KERNEL_SHADE);
-                switch (k) {
-                case kMatMatte:
-                    kShadeSurf<kMatMatte><<<g.shadeSurf[k], block, 0, stream>>>(
-                        ds.sc, w, wp, cq, ctr + k, outQueue, next + kCtrExt, w.shadowQueue, ctr + kCtrShadow);
-                    break;
-                case kMatSpecularReflection:
-                    kShadeSurf<kMatSpecularReflection><<<g.shadeSurf[k], block, 0, stream>>>(
-                        ds.sc, w, wp, cq, ctr + k, outQueue, next + kCtrExt, w.shadowQueue, ctr + kCtrShadow);
-                    break;
-                case kMatSpecularScattering:
-                    kShadeSurf<kMatSpecularScattering><<<g.shadeSurf[k], block, 0, stream>>>(
-                        ds.sc, w, wp, cq, ctr + k, outQueue, next + kCtrExt, w.shadowQueue, ctr + kCtrShadow);
-                    break;
-                case kMatGGXReflection:
-                    kShadeSurf<kMatGGXReflection><<<g.shadeSurf[k], block, 0, stream>>>(
-                        ds.sc, w, wp, cq, ctr + k, outQueue, next + kCtrExt, w.shadowQueue, ctr + kCtrShadow);
-                    break;
-                default:
-                    kShadeSurf<kMatGGXScattering><<<g.shadeSurf[k], block, 0, stream>>>(
-                        ds.sc, w, wp, cq, ctr + k, outQueue, next + kCtrExt, w.shadowQueue, ctr + kCtrShadow);
-                    break;
-                }
-                lm.end();
-                ++launches;
-            }
-            lm.begin(SLRGPU_KERNEL_SHADOW);
-            kShadow<<<g.shadow, block, 0, stream>>>(ds.sc, w, w.shadowQueue, ctr + kCtrShadow);
+        if (ds.sc.envPresent) {
+            lm.begin(SLRGPU_KERNEL_SHADE);
+            kShadeMiss<<<g.shadeMiss, block, 0, stream>>>(ds.sc, w, w.classQueue + (size_t)kClassMiss * w.N,
+                                                          ctr + kClassMiss);
             lm.end();
             ++launches;
         }
-        lm.begin(SLRGPU_KERNEL_ACCUMULATE);
-        kAccumulate<<<g.accumulate, block, 0, stream>>>(w, wp, filmSum, filmComp);
+        // One kernel per material kind present in the scene.
+        for (int k = 0; k < kNumShadeClasses - 1; ++k) {
+            if (!(ds.kindMask & (1u << k))) continue;
+            const uint32_t* cq = w.classQueue + (size_t)k * w.N;
+            lm.begin(SLRGPU_KERNEL_SHADE);
+            switch (k) {
+            case kMatMatte:
+                kShadeSurf<kMatMatte><<<g.shadeSurf[k], block, 0, stream>>>(
+                    ds.sc, w, D, cq, ctr + k, outQueue, next + kCtrExt, w.shadowQueue, ctr + kCtrShadow);
+                break;
+            case kMatSpecularReflection:
+                kShadeSurf<kMatSpecularReflection><<<g.shadeSurf[k], block, 0, stream>>>(
+                    ds.sc, w, D, cq, ctr + k, outQueue, next + kCtrExt, w.shadowQueue, ctr + kCtrShadow);
+                break;
+            case kMatSpecularScattering:
+                kShadeSurf<kMatSpecularScattering><<<g.shadeSurf[k], block, 0, stream>>>(
+                    ds.sc, w, D, cq, ctr + k, outQueue, next + kCtrExt, w.shadowQueue, ctr + kCtrShadow);
+                break;
+            case kMatGGXReflection:
+                kShadeSurf<kMatGGXReflection><<<g.shadeSurf[k], block, 0, stream>>>(
+                    ds.sc, w, D, cq, ctr + k, outQueue, next + kCtrExt, w.shadowQueue, ctr + kCtrShadow);
+                break;
+            default:
+                kShadeSurf<kMatGGXScattering><<<g.shadeSurf[k], block, 0, stream>>>(
+                    ds.sc, w, D, cq, ctr + k, outQueue, next + kCtrExt, w.shadowQueue, ctr + kCtrShadow);
+                break;
+            }
+            lm.end();
+            ++launches;
+        }
+        lm.begin(SLRGPU_KERNEL_SHADOW);
+        kShadow<<<g.shadow, block, 0, stream>>>(ds.sc, w, w.shadowQueue, ctr + kCtrShadow);
         lm.end();
         ++launches;
+    }
+    lm.begin(SLRGPU_KERNEL_ACCUMULATE);
+    kAccumulate<<<g.accumulate, block, 0, stream>>>(w, wp);
+    lm.end();
+    ++launches;
+    return launches;
+}
+
+// The wave loop of one render (slrgpu_render, slrgpu_render_noalloc): waves
+// of pl.S sample indices over the whole sample grid, one segment each.
+static uint64_t runWaves(const DeviceScene &ds, const slrgpu_settings &s, const WavePlan &pl, const WaveState &w,
+                         float* filmSum, float* filmComp, cudaStream_t stream, LaunchMarks &lm) {
+    uint64_t launches = 0;
+    for (uint32_t base = 0; base < s.spp; base += pl.S) {
+        WaveParams wp;
+        std::memset(&wp, 0, sizeof(wp));
+        WaveSegment &sg = wp.seg[0];
+        sg.pathBegin = 0;
+        sg.width = s.width;
+        sg.height = s.height;
+        sg.gridW = pl.gridW;
+        sg.gridH = pl.gridH;
+        sg.gridPositions = pl.gridPositions;
+        sg.sampleBase = base;
+        sg.samples = std::min(pl.S, s.spp - base);
+        sg.seed = s.seed;
+        sg.filmBegin = 0;
+        sg.filmSum = filmSum;
+        sg.filmComp = filmComp;
+        sg.dropped = nullptr;
+        wp.numSegments = 1;
+        wp.numPaths = sg.samples * pl.gridPositions;
+        wp.filmPixels = s.width * s.height;
+        launches += runWave(ds, w, wp, s.max_depth, s.volumetric != 0, stream, lm);
     }
     return launches;
 }
@@ -1641,7 +1685,8 @@ constexpr size_t kNaPrevPdf = naAlign(kNaWlOffset + 4ull * kNoAllocMaxPaths);
 constexpr size_t kNaInitY = naAlign(kNaPrevPdf + 4ull * kNoAllocMaxPaths);
 constexpr size_t kNaCamWeight = naAlign(kNaInitY + 4ull * kNoAllocMaxPaths);
 constexpr size_t kNaRngCounter = naAlign(kNaCamWeight + 4ull * kNoAllocMaxPaths);
-constexpr size_t kNaShOrg = naAlign(kNaRngCounter + 4ull * kNoAllocMaxPaths);
+constexpr size_t kNaRngKey = naAlign(kNaRngCounter + 4ull * kNoAllocMaxPaths);
+constexpr size_t kNaShOrg = naAlign(kNaRngKey + 8ull * kNoAllocMaxPaths);
 constexpr size_t kNaShDir = naAlign(kNaShOrg + 16ull * kNoAllocMaxPaths);
 constexpr size_t kNaShContrib = naAlign(kNaShDir + 16ull * kNoAllocMaxPaths);
 constexpr size_t kNaQueue0 = naAlign(kNaShContrib + 4ull * kNumLambda * kNoAllocMaxPaths);
@@ -1725,6 +1770,7 @@ int renderNoAlloc(const DeviceScene &ds, const slrgpu_settings &s, float* film, 
     w.initY = (float*)(base + kNaInitY);
     w.camWeight = (float*)(base + kNaCamWeight);
     w.rngCounter = (uint32_t*)(base + kNaRngCounter);
+    w.rngKey = (uint2*)(base + kNaRngKey);
     w.shOrg = (float4*)(base + kNaShOrg);
     w.shDir = (float4*)(base + kNaShDir);
     w.shContrib = (float*)(base + kNaShContrib);
@@ -1744,6 +1790,82 @@ int renderNoAlloc(const DeviceScene &ds, const slrgpu_settings &s, float* film, 
     LaunchMarks lm;
     runWaves(ds, s, pl, w, filmSum, filmComp, stream, lm);
     kFilmToPixelMajor<<<waveGrids(256).accumulate, 256, 0, stream>>>(filmSum, film, P);
+    CUDA_TRY(cudaGetLastError());
+    return SLRGPU_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Wave slots for the serving loop: path state for up to `paths` paths and
+// waves whose segments come from several requests of one scene.
+// ---------------------------------------------------------------------------
+struct WaveSlot {
+    RenderEngine engine;   // path state only; films belong to the requests
+};
+
+WaveSlot* waveSlotCreate(uint32_t paths, uint32_t maxDepth, std::string* err) {
+    WaveSlot* slot = new WaveSlot();
+    if (slot->engine.ensure(paths, maxDepth) != SLRGPU_OK) {
+        if (err) *err = "wave slot allocation failed";
+        delete slot;
+        return nullptr;
+    }
+    return slot;
+}
+
+void waveSlotDestroy(WaveSlot* slot) { delete slot; }
+
+uint32_t waveSlotCapacity(const WaveSlot* slot) { return slot->engine.capacity; }
+
+uint32_t sampleGridPositions(uint32_t width, uint32_t height) { return padToTile(width) * padToTile(height); }
+
+int launchWave(const DeviceScene &ds, WaveSlot* slot, const SegmentDesc* segs, int numSegs, uint32_t maxDepth,
+               bool volumetric, cudaStream_t stream, uint64_t* launches) {
+    if (numSegs <= 0 || numSegs > kMaxWaveSegments) {
+        setError("a wave holds 1 to 32 segments");
+        return SLRGPU_ERR_INVALID_ARGUMENT;
+    }
+    if (maxDepth > slot->engine.depthCapacity) {
+        setError("max_depth exceeds the wave slot's counter capacity");
+        return SLRGPU_ERR_INVALID_ARGUMENT;
+    }
+    WaveParams wp;
+    std::memset(&wp, 0, sizeof(wp));
+    uint64_t paths = 0, pixels = 0;
+    for (int i = 0; i < numSegs; ++i) {
+        const SegmentDesc &d = segs[i];
+        WaveSegment &sg = wp.seg[i];
+        sg.pathBegin = (uint32_t)paths;
+        sg.width = d.width;
+        sg.height = d.height;
+        sg.gridW = padToTile(d.width);
+        sg.gridH = padToTile(d.height);
+        sg.gridPositions = sg.gridW * sg.gridH;
+        sg.sampleBase = d.sampleBase;
+        sg.samples = d.samples;
+        sg.seed = d.seed;
+        sg.filmBegin = (uint32_t)pixels;
+        sg.filmSum = d.filmSum;
+        sg.filmComp = d.filmComp;
+        sg.dropped = d.dropped;
+        paths += (uint64_t)sg.samples * sg.gridPositions;
+        pixels += (uint64_t)d.width * d.height;
+    }
+    if (paths > slot->engine.capacity || pixels > 0x7fffffffull) {
+        setError("wave larger than the slot");
+        return SLRGPU_ERR_INVALID_ARGUMENT;
+    }
+    wp.numSegments = (uint32_t)numSegs;
+    wp.numPaths = (uint32_t)paths;
+    wp.filmPixels = (uint32_t)pixels;
+    LaunchMarks lm;
+    uint64_t n = runWave(ds, *slot->engine.ws, wp, maxDepth, volumetric, stream, lm);
+    if (launches) *launches += n;
+    CUDA_TRY(cudaGetLastError());
+    return SLRGPU_OK;
+}
+
+int launchFilmToPixelMajor(const float* filmSum, float* out, uint32_t pixels, cudaStream_t stream) {
+    kFilmToPixelMajor<<<waveGrids(256).accumulate, 256, 0, stream>>>(filmSum, out, pixels);
     CUDA_TRY(cudaGetLastError());
     return SLRGPU_OK;
 }

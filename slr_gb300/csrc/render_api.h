@@ -48,6 +48,25 @@ struct RenderEngine {
     ~RenderEngine() { release(); }
 };
 
+// Wave slots (serving): path state for up to `paths` paths in flight.
+struct WaveSlot;
+// One request's share of a wave: samples [sampleBase, sampleBase + samples)
+// over its whole tile-padded sample grid, accumulated into its film
+// (16-bin planes of width * height floats, sum and compensation).
+struct SegmentDesc {
+    uint32_t width, height, sampleBase, samples, seed;
+    float* filmSum;
+    float* filmComp;
+    unsigned long long* dropped;   // device counter, or null
+};
+WaveSlot* waveSlotCreate(uint32_t paths, uint32_t maxDepth, std::string* err);
+void waveSlotDestroy(WaveSlot* slot);
+uint32_t waveSlotCapacity(const WaveSlot* slot);
+uint32_t sampleGridPositions(uint32_t width, uint32_t height);
+int launchWave(const DeviceScene &ds, WaveSlot* slot, const SegmentDesc* segs, int numSegs, uint32_t maxDepth,
+               bool volumetric, cudaStream_t stream, uint64_t* launches);
+int launchFilmToPixelMajor(const float* filmSum, float* out, uint32_t pixels, cudaStream_t stream);
+
 int uploadScene(const HostScene &hs, const BuiltScene &bs, DeviceScene* ds);
 int reuploadScene(DeviceScene* ds, uint64_t* bytes, cudaStream_t stream);
 // Render with all scratch in a fixed device array (no allocation).

@@ -1,0 +1,133 @@
+"""Serving loop (slrgpu_server_*): continuous batching of render requests of
+several scenes, resolutions, sample counts and both integrators.
+
+Each request's film must be bit-identical to a standalone slrgpu_render with
+the same settings, in the plain and in the batched mode: its random numbers
+depend only on (seed, sample, pixel) and its samples are accumulated in
+order, whichever waves they travel in.  The slot size here is small (64 Ki
+paths), so requests are split over many waves and packed together with
+others."""
+import time
+
+import numpy as np
+import pytest
+
+from slr_gb300 import scenes
+
+pytestmark = pytest.mark.gpu
+
+# (scene index, width, height, spp, max depth, seed, volumetric)
+REQUESTS = [
+    (0, 64, 64, 16, 8, 1, False),
+    (1, 48, 48, 4, 8, 2, False),
+    (0, 21, 13, 64, 8, 3, False),      # ragged: overhanging 8x8 tiles
+    (2, 32, 32, 8, 8, 4, True),        # volumetric
+    (1, 128, 64, 4, 8, 5, False),
+    (0, 64, 64, 4, 3, 6, False),       # another max depth: its own waves
+    (2, 20, 20, 16, 8, 7, True),
+    (1, 48, 48, 16, 8, 8, False),
+]
+
+
+@pytest.fixture(scope="module")
+def served_scenes(gpu_lib):
+    ctx = gpu_lib.default_context()
+    box = gpu_lib.Scene(scenes.box_scene(64, 64), context=ctx)
+    ggx = gpu_lib.Scene(scenes.heightfield_scene(grid=32, spheres=4, sphere_freq=4, env_size=(32, 16), width=48,
+                                                 height=48), context=ctx)
+    vol = gpu_lib.Scene(scenes.medium_box_scene(32, 32, grid=16), context=ctx)
+    return ctx, [box, ggx, vol]
+
+
+@pytest.fixture(scope="module")
+def standalone(served_scenes):
+    _, scs = served_scenes
+    out = []
+    for i, w, h, spp, d, seed, vol in REQUESTS:
+        film, _ = scs[i].render(w, h, spp, d, seed=seed, volumetric=vol)
+        out.append(film)
+    return out
+
+
+@pytest.mark.parametrize("mode", ["plain", "batched"])
+def test_served_films_equal_standalone(gpu_lib, served_scenes, standalone, mode):
+    ctx, scs = served_scenes
+    m = gpu_lib.SERVER_PLAIN if mode == "plain" else gpu_lib.SERVER_BATCHED
+    srv = gpu_lib.Server(ctx, mode=m, paths_per_slot=1 << 16, max_depth=16)
+    try:
+        ids = [srv.submit(scs[i], w, h, spp, d, seed=seed, volumetric=vol)
+               for i, w, h, spp, d, seed, vol in REQUESTS]
+        for rid, ref, req in zip(ids, standalone, REQUESTS):
+            film, info = srv.wait(rid, timeout=120)
+            assert info.status == gpu_lib.REQUEST_DONE
+            assert info.spp_done == req[3]
+            assert np.array_equal(film, ref), f"request {req} differs from its standalone render"
+            assert info.submit_seconds <= info.start_seconds <= info.done_seconds
+        st = srv.stats()
+        assert st.requests_done == len(REQUESTS) and st.queued == 0 and st.active == 0
+        if m == gpu_lib.SERVER_BATCHED:
+            # packing: fewer waves than the requests would need one by one
+            singles = sum(-(-spp // max(1, (1 << 16) // (((w + 7) // 8 * 8) * ((h + 7) // 8 * 8))))
+                          for _, w, h, spp, _, _, _ in REQUESTS)
+            assert st.waves < singles
+    finally:
+        srv.close()
+
+
+def test_requests_arriving_while_others_run(gpu_lib, served_scenes, standalone):
+    """Continuous batching: later submissions join while earlier requests are
+    on the GPU; every film still equals its standalone render."""
+    ctx, scs = served_scenes
+    srv = gpu_lib.Server(ctx, mode=gpu_lib.SERVER_BATCHED, paths_per_slot=1 << 16, max_depth=16)
+    try:
+        ids = []
+        for k, (i, w, h, spp, d, seed, vol) in enumerate(REQUESTS):
+            ids.append(srv.submit(scs[i], w, h, spp, d, seed=seed, volumetric=vol))
+            if k % 2 == 1:
+                time.sleep(0.002)
+        for rid, ref in zip(ids, standalone):
+            film, info = srv.wait(rid, timeout=120)
+            assert np.array_equal(film, ref)
+    finally:
+        srv.close()
+
+
+def test_admission_respects_the_budget(gpu_lib, served_scenes, standalone):
+    """A budget that holds one film at a time still serves every request,
+    in order, and never has more than one film admitted."""
+    ctx, scs = served_scenes
+    biggest = max(w * h for _, w, h, *_ in REQUESTS)
+    budget = 3 * biggest * 16 * 4              # sum + compensation + output planes of one film
+    srv = gpu_lib.Server(ctx, mode=gpu_lib.SERVER_BATCHED, paths_per_slot=1 << 16, max_depth=16,
+                         hbm_budget_bytes=budget)
+    try:
+        ids = [srv.submit(scs[i], w, h, spp, d, seed=seed, volumetric=vol)
+               for i, w, h, spp, d, seed, vol in REQUESTS]
+        peak = 0
+        done = []
+        for rid, ref in zip(ids, standalone):
+            while srv.poll(rid).status not in (gpu_lib.REQUEST_DONE,) and srv.poll(rid).status >= 0:
+                peak = max(peak, srv.stats().bytes_in_use)
+                time.sleep(0.0005)
+            film, info = srv.wait(rid, timeout=120)
+            assert np.array_equal(film, ref)
+            done.append(info.done_seconds)
+        assert peak <= budget
+    finally:
+        srv.close()
+
+
+def test_server_rejects_bad_requests(gpu_lib, served_scenes):
+    ctx, scs = served_scenes
+    srv = gpu_lib.Server(ctx, mode=gpu_lib.SERVER_BATCHED, paths_per_slot=1 << 12, max_depth=16)
+    try:
+        with pytest.raises(gpu_lib.SlrGpuError):
+            srv.submit(scs[0], 0, 8, 1, 4)                      # empty image
+        with pytest.raises(gpu_lib.SlrGpuError):
+            srv.submit(scs[0], 8, 8, 1, 17)                     # deeper than the server allows
+        with pytest.raises(gpu_lib.SlrGpuError):
+            srv.submit(scs[0], 128, 128, 1, 4)                  # one sample exceeds the slot
+        with pytest.raises(gpu_lib.SlrGpuError):
+            srv.submit(scs[0], 8, 8, 1, 4, volumetric=True)     # no medium in this scene
+    finally:
+        srv.close()
