@@ -22,6 +22,11 @@ log-normal environment with a 2-degree sun of radiance 5e4) at 1024 x 1024,
 captures (256 x 256 height field, 16 spheres, 512 x 512 pixels, 4 spp); it is
 not a benchmark line.
 
+``--workload serving`` runs the serving stream (512 requests, Poisson
+arrivals at 20/s, 8 scenes of 1k-2M triangles, half with a medium) through
+the plain and the batched server, as a burst and at the arrival times, and
+prints throughput and p50/p99 latency of both.
+
 ``--impl reference`` times the reference renderer alone (rank 0) on a
 bounded sample of the same workload.  Under torchrun each rank renders its
 own replica (weak scaling; path samples are independent, no collective).
@@ -171,6 +176,89 @@ def run_reference(args):
     return 0
 
 
+def serving_requests(n: int, rate: float, seed: int, num_scenes: int):
+    """The serving stream: n requests with Poisson arrivals (mean `rate`/s),
+    scene uniform over the serving scenes, resolution uniform over
+    {64, 128, 256, 512}^2, spp uniform over {4, 16, 64}, max depth 8."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    t = np.cumsum(rng.exponential(1.0 / rate, n))
+    t -= t[0]
+    res = rng.choice([64, 128, 256, 512], n)
+    spp = rng.choice([4, 16, 64], n)
+    sc = rng.integers(0, num_scenes, n)
+    return [dict(t=float(t[i]), scene=int(sc[i]), res=int(res[i]), spp=int(spp[i]), depth=8, seed=7000 + i)
+            for i in range(n)]
+
+
+def run_serving(args):
+    """Serving stream: plain (one request at a time) vs batched (continuous
+    batching), open loop at the Poisson arrival times and as a burst."""
+    import numpy as np
+    from slr_gb300 import api, scenes
+    t0 = time.time()
+    descs = scenes.serving_scenes(seed=0)
+    gen_s = time.time() - t0
+    ctx = api.Context(0)
+    t0 = time.time()
+    scs = [api.Scene(d, context=ctx) for d in descs]
+    build_s = time.time() - t0
+    reqs = serving_requests(args.requests, 20.0, 0, len(scs))
+    grid = lambda r: ((r["res"] + 7) // 8 * 8) ** 2  # noqa: E731
+    total_samples = sum(grid(r) * r["spp"] for r in reqs)
+
+    def run(mode, open_loop):
+        srv = api.Server(ctx, mode=mode, max_depth=8)
+        # warm-up: one small request per scene
+        for k, sc in enumerate(scs):
+            srv.wait(srv.submit(sc, 64, 64, 1, 8, seed=k, volumetric=descs[k].medium is not None))
+        ids, sub = [], []
+        start = time.perf_counter()
+        for r in reqs:
+            if open_loop:
+                delay = start + r["t"] - time.perf_counter()
+                if delay > 0:
+                    time.sleep(delay)
+            sub.append(time.perf_counter())
+            ids.append(srv.submit(scs[r["scene"]], r["res"], r["res"], r["spp"], r["depth"], seed=r["seed"],
+                                  volumetric=descs[r["scene"]].medium is not None))
+        lat, films = [], {}
+        for k, rid in enumerate(ids):
+            film, info = srv.wait(rid)
+            lat.append((info.done_seconds - info.submit_seconds) * 1e3)
+            if k % 64 == 0:
+                films[k] = film
+        end = time.perf_counter()
+        st = srv.stats().as_dict()
+        srv.close()
+        lat = np.array(lat)
+        return {"path_samples_per_s": total_samples / (end - start), "seconds": end - start,
+                "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                "mean_ms": float(lat.mean()), "waves": st["waves"], "kernel_launches": st["kernel_launches"]}, films
+
+    out = {}
+    films_by_mode = {}
+    for name, mode in (("plain", api.SERVER_PLAIN), ("batched", api.SERVER_BATCHED)):
+        burst, films_by_mode[name] = run(mode, open_loop=False)
+        poisson, _ = run(mode, open_loop=True)
+        out[name] = {"burst": burst, "poisson": poisson}
+    same = all(np.array_equal(films_by_mode["plain"][k], films_by_mode["batched"][k]) for k in films_by_mode["plain"])
+    line = {"metric": "path samples/s (serving stream, batched)", "value": out["batched"]["burst"]["path_samples_per_s"],
+            "unit": "path samples/s", "n_gpus": 1, "higher_is_better": True, "dtype": "f32",
+            "data": "synthetic (seeded procedural scenes and request stream)",
+            "config": {"workload": f"serving: {args.requests} requests, Poisson 20/s, 8 scenes "
+                                   f"{[sum(len(m.indices) for m in d.meshes) for d in descs]} triangles "
+                                   "(odd ones with a 256^3 fBm medium, volumetric PT), res {64..512}^2, "
+                                   "spp {4,16,64}, max depth 8", "hbm_budget_gb": 150,
+                       "scene_generation_s": round(gen_s, 1), "scene_build_s": round(build_s, 1)},
+            "batched_over_plain_burst": out["batched"]["burst"]["path_samples_per_s"] /
+                                        out["plain"]["burst"]["path_samples_per_s"],
+            "plain": out["plain"], "batched": out["batched"],
+            "films_identical_across_modes": bool(same), "total_path_samples": total_samples}
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -179,8 +267,11 @@ def main():
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--spp", type=int, default=None)
-    ap.add_argument("--workload", default="ggx_ibl_1m", choices=["ggx_ibl_1m", "small"])
+    ap.add_argument("--workload", default="ggx_ibl_1m", choices=["ggx_ibl_1m", "small", "serving"])
+    ap.add_argument("--requests", type=int, default=512)
     args = ap.parse_args()
+    if args.workload == "serving":
+        return run_serving(args)
     global WIDTH, HEIGHT, WORKLOAD
     if args.workload == "small":
         WIDTH = HEIGHT = 512

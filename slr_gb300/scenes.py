@@ -316,3 +316,29 @@ def _tangent_for(nrm: np.ndarray) -> np.ndarray:
     a = np.where(np.abs(nrm[:, :1]) < 0.9, np.array([[1.0, 0, 0]], np.float32), np.array([[0, 0, 1.0]], np.float32))
     t = a - (a * nrm).sum(1, keepdims=True) * nrm
     return (t / np.linalg.norm(t, axis=1, keepdims=True)).astype(np.float32)
+
+
+def serving_scenes(seed: int = 0, count: int = 8, min_tris: int = 1000, max_tris: int = 2_000_000):
+    """The serving workload's scenes: `count` height-field + sphere scenes
+    built as heightfield_scene, with triangle counts log-spaced from min_tris
+    to max_tris (half in the height field, half in 8 geodesic spheres); every
+    second scene also carries the volumetric benchmark's medium (a 256^3 fBm
+    density grid, sigma_t max 20, albedo 0.9, Henyey-Greenstein g = 0.7) as a
+    fog layer over the terrain, y in [-0.25, 0.15]; the media share one
+    density grid.  Square images."""
+    from .scene_desc import Medium
+    out = []
+    density = None
+    for k, n in enumerate(np.geomspace(min_tris, max_tris, count)):
+        f = max(1, int(round(math.sqrt(n * 0.5 / (8 * 20)))))
+        g = max(4, int(round(math.sqrt(n * 0.5 / 2))) + 1)
+        d = heightfield_scene(grid=g, spheres=8, sphere_freq=f, env_size=(512, 256), width=512, height=512,
+                              seed=seed + 17 * k)
+        if k % 2 == 1:
+            s_e = d.spectrum_regular(np.array([20.0, 20.0], np.float32), 360.0, 830.0)
+            s_s = d.spectrum_regular(np.array([18.0, 18.0], np.float32), 360.0, 830.0)
+            if density is None:
+                density = fbm_density_grid(256, seed)
+            d.medium = Medium((-1.0, -0.25, -1.0), (1.0, 0.15, 1.0), density, s_s, s_e, 0.7)
+        out.append(d)
+    return out
