@@ -278,8 +278,34 @@ __device__ __noinline__ bool mediumInteractSegment(const DevMedium &m, V3 org, V
     return hit;
 }
 
-// Ratio-tracking transmittance with Russian roulette below 0.1
-// (DensityGridMediumDistribution.cpp:577-744).
+// Ratio-tracking estimate of one wavelength's transmittance over [dmin, dmax)
+// inside the medium, with Russian roulette below 0.1
+// (DensityGridMediumDistribution.cpp:618-651); s is the DDA set-up at dmin.
+template <class R>
+__device__ __forceinline__ float ratioTrackSegment(const DevMedium &m, V3 org, V3 dir, float dmin, float dmax,
+                                                   const SvSetup &s, float sig, R &rng) {
+    float t = 1.0f;
+    SvWalk w = s.init;
+    float sd = dmin;
+    while (sd < dmax) {
+        float maj;
+        bool tent = svTraverse(m, org, dir, sd, dmax, rng.next(), sig, s, w, &sd, &maj);
+        if (tent) {
+            float ext = sig * mediumDensity(m, mediumLocal(m, org + sd * dir));
+            float prob = ext / maj;
+            if (maj != 0.0f) t *= (1.0f - prob);
+            if (t < 0.1f) {
+                if (rng.next() < t) t = 1.0f;
+                else return 0.0f;
+            }
+        }
+    }
+    return t;
+}
+
+// Spectral transmittance of one segment inside the medium
+// (DensityGridMediumDistribution::evaluateTransmittance, :577-744): every
+// wavelength, or only the selected one once a wavelength is selected.
 template <class R>
 __device__ __noinline__ void mediumTransmittanceSegment(const DevMedium &m, V3 org, V3 dir, float dmin, float dmax,
                                                         const Spec &sigmaE, int sel, bool wlSelected, R &rng,
@@ -289,27 +315,10 @@ __device__ __noinline__ void mediumTransmittanceSegment(const DevMedium &m, V3 o
     T = specConst(0.0f);
     for (int wl = 0; wl < kNumLambda; ++wl) {
         if (wlSelected && wl != sel) continue;
-        const float sig = specAt(sigmaE, wl);
-        float t = 1.0f;
-        SvWalk w = s.init;
-        float sd = dmin;
-        bool killed = false;
-        while (sd < dmax) {
-            float maj;
-            bool tent = svTraverse(m, org, dir, sd, dmax, rng.next(), sig, s, w, &sd, &maj);
-            if (tent) {
-                float ext = sig * mediumDensity(m, mediumLocal(m, org + sd * dir));
-                float prob = ext / maj;
-                if (maj != 0.0f) t *= (1.0f - prob);
-                if (t < 0.1f) {
-                    if (rng.next() < t) t = 1.0f;
-                    else { killed = true; break; }
-                }
-            }
-        }
+        const float t = ratioTrackSegment(m, org, dir, dmin, dmax, s, specAt(sigmaE, wl), rng);
 #pragma unroll
         for (int k = 0; k < kNumLambda; ++k)
-            if (k == wl) T.v[k] = killed ? 0.0f : t;
+            if (k == wl) T.v[k] = t;
     }
 }
 
@@ -377,6 +386,42 @@ __device__ __forceinline__ void mediumTransmittance(const DevMedium &m, V3 org, 
         rmin = distNext * (1.0f + kRayEpsilon);
         inside = nextInside;
     }
+}
+
+// One wavelength of mediumTransmittance, for a thread per (ray, wavelength):
+// the same boundary walk and per-segment estimate; `evaluate` false (a
+// wavelength other than the selected one) gives 0 once the ray crosses the
+// medium and 1 otherwise, as the spectral version does.
+template <class R>
+__device__ __noinline__ float mediumTransmittanceWl(const DevMedium &m, V3 org, V3 dir, float dmin, float dmax,
+                                                    float sig, bool evaluate, R &rng) {
+    float T = 1.0f;
+    float rmin = dmin;
+    bool inside = mediumContains(m, org + rmin * dir);
+    for (int guard = 0; guard < 8; ++guard) {
+        float dist;
+        bool enter;
+        bool nextInside = false;
+        float distNext = __int_as_float(0x7f800000);
+        if (mediumIntersectBoundary(m, org, dir, rmin, dmax, &dist, &enter) && dist < distNext) {
+            distNext = dist;
+            nextInside = enter;
+        }
+        if (inside && nextInside) inside = false;
+        distNext = fminf(distNext, dmax);
+        if (isinf(distNext)) return T;
+        if (inside) {
+            if (!evaluate) return 0.0f;
+            SvSetup s;
+            svSetup(m, org, dir, rmin, s);
+            T *= ratioTrackSegment(m, org, dir, rmin, distNext, s, sig, rng);
+            if (T == 0.0f) return 0.0f;
+        }
+        if (distNext == dmax) return T;
+        rmin = distNext * (1.0f + kRayEpsilon);
+        inside = nextInside;
+    }
+    return T;
 }
 
 // Henyey-Greenstein phase function (PhaseFunction/basic_phase_functions.cpp:36-65).

@@ -982,36 +982,61 @@ __global__ void __launch_bounds__(256) kShadeVol(DevScene sc, WaveState ws, uint
     }
 }
 
-// Shadow rays of the volumetric integrator: occlusion by surfaces, then the
-// medium's spectral transmittance (Scene::testVisibility, Scene.cpp:114-135),
-// drawn from a per-bounce random stream of the path.
+// Shadow rays of the volumetric integrator (Scene::testVisibility,
+// Scene.cpp:114-135): occlusion by surfaces here; unoccluded rays that may
+// cross the medium go to a second queue for their spectral transmittance.
 __global__ void kShadowVol(DevScene sc, WaveState ws, const uint32_t* __restrict__ queue,
-                           const uint32_t* __restrict__ count, uint32_t bounce) {
+                           const uint32_t* __restrict__ count, uint32_t* medQueue, uint32_t* medCount) {
     const uint32_t n = *count;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        uint32_t p = queue[i];
-        float4 o = ws.shOrg[p], d = ws.shDir[p];
-        V3 org = V3{o.x, o.y, o.z}, dir = V3{d.x, d.y, d.z};
-        if (traceAny(sc, org, dir, o.w, d.w)) continue;
-        Spec T = specConst(1.0f);
-        if (sc.medium.present) {
-            uint32_t info = ws.info[p];
-            const int sel = (int)(info & kInfoSelMask);
-            const bool wlSelected = (info & kInfoWlSelected) != 0;
-            float lambdas[kNumLambda];
-            const float wlOff = ws.wlOffset[p];
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+        const uint32_t i = base + threadIdx.x;
+        bool pushMedium = false;
+        uint32_t p = 0;
+        if (i < n) {
+            p = queue[i];
+            float4 o = ws.shOrg[p], d = ws.shDir[p];
+            if (!traceAny(sc, V3{o.x, o.y, o.z}, V3{d.x, d.y, d.z}, o.w, d.w)) {
+                if (sc.medium.present) {
+                    pushMedium = true;
+                } else {
 #pragma unroll
-            for (int k = 0; k < kNumLambda; ++k) lambdas[k] = lambdaAt(k, wlOff);
-            Spec sigmaE;
-            evalSpectrum(sc, sc.medium.sigmaE, lambdas, sigmaE);
-            Rng rng{mix64(loadKey(ws, p) ^ (0x9e3779b97f4a7c15ull * (bounce + 1))), 0};
-            mediumTransmittance(sc.medium, org, dir, o.w, d.w, sigmaE, sel, wlSelected, rng, T);
+                    for (int k = 0; k < kNumLambda; ++k)
+                        ws.L[(size_t)k * ws.N + p] += ws.shContrib[(size_t)k * ws.N + p];
+                }
+            }
         }
-#pragma unroll
-        for (int k = 0; k < kNumLambda; ++k)
-            ws.L[(size_t)k * ws.N + p] += T.v[k] * ws.shContrib[(size_t)k * ws.N + p];
+        queuePush(medQueue, medCount, p, pushMedium);
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&ws.stats[1], (unsigned long long)n);
+}
+
+// Medium transmittance of the unoccluded shadow rays, one thread per (ray,
+// wavelength): the 16 ratio-tracking walks of a ray run side by side in
+// consecutive lanes instead of one after another.  Each wavelength draws
+// from its own counter range of the ray's per-bounce random stream.
+__global__ void kShadowVolMedium(DevScene sc, WaveState ws, const uint32_t* __restrict__ queue,
+                                 const uint32_t* __restrict__ count, uint32_t bounce) {
+    const uint32_t n = *count * kNumLambda;
+    for (uint32_t item = blockIdx.x * blockDim.x + threadIdx.x; item < n; item += gridDim.x * blockDim.x) {
+        const uint32_t p = queue[item / kNumLambda];
+        const int wl = (int)(item % kNumLambda);
+        float4 o = ws.shOrg[p], d = ws.shDir[p];
+        const uint32_t info = ws.info[p];
+        const int sel = (int)(info & kInfoSelMask);
+        const bool wlSelected = (info & kInfoWlSelected) != 0;
+        float lambdas[kNumLambda];
+        const float wlOff = ws.wlOffset[p];
+#pragma unroll
+        for (int k = 0; k < kNumLambda; ++k) lambdas[k] = lambdaAt(k, wlOff);
+        Spec sigmaE;
+        evalSpectrum(sc, sc.medium.sigmaE, lambdas, sigmaE);   // same values as the shading kernel's
+        const float sig = specAt(sigmaE, wl);
+        Rng rng{mix64(loadKey(ws, p) ^ (0x9e3779b97f4a7c15ull * (bounce + 1))), (uint32_t)wl << 24};
+        const float T = mediumTransmittanceWl(sc.medium, V3{o.x, o.y, o.z}, V3{d.x, d.y, d.z}, o.w, d.w, sig,
+                                              !wlSelected || wl == sel, rng);
+        const size_t k = (size_t)wl * ws.N + p;
+        if (T != 0.0f) ws.L[k] += T * ws.shContrib[k];
+    }
 }
 
 // Adds the wave's paths to the film: C = L * weight, dropped when not finite
@@ -1395,7 +1420,7 @@ static int gridFor(const void* kernel, int block) {
 // Persistent grid sizes (resident blocks per SM x SMs) of the wave kernels,
 // computed once per process.
 struct WaveGrids {
-    int raygen, extend, shadow, accumulate, shadeVol, shadowVol, extendSort, shadeMiss;
+    int raygen, extend, shadow, accumulate, shadeVol, shadowVol, shadowVolMedium, extendSort, shadeMiss;
     int shadeSurf[kNumShadeClasses - 1];
 };
 static const WaveGrids &waveGrids(int block) {
@@ -1408,6 +1433,7 @@ static const WaveGrids &waveGrids(int block) {
         g.accumulate = gridFor((const void*)kAccumulate, block);
         g.shadeVol = gridFor((const void*)kShadeVol, block);
         g.shadowVol = gridFor((const void*)kShadowVol, block);
+        g.shadowVolMedium = gridFor((const void*)kShadowVolMedium, block);
         g.extendSort = gridFor((const void*)kExtendSort, block);
         g.shadeMiss = gridFor((const void*)kShadeMiss, block);
         g.shadeSurf[kMatMatte] = gridFor((const void*)kShadeSurf<kMatMatte>, block);
@@ -1488,10 +1514,16 @@ static uint64_t runWave(const DeviceScene &ds, const WaveState &w, const WavePar
             kShadeVol<<<g.shadeVol, block, 0, stream>>>(ds.sc, w, D, inQueue, ctr + kCtrExt, outQueue,
                                                         next + kCtrExt, w.shadowQueue, ctr + kCtrShadow);
             lm.end();
+            // unoccluded shadow rays that cross the medium: class queue 0 and
+            // its counter (unused by the volumetric integrator otherwise)
             lm.begin(SLRGPU_KERNEL_SHADOW);
-            kShadowVol<<<g.shadowVol, block, 0, stream>>>(ds.sc, w, w.shadowQueue, ctr + kCtrShadow, b);
+            kShadowVol<<<g.shadowVol, block, 0, stream>>>(ds.sc, w, w.shadowQueue, ctr + kCtrShadow, w.classQueue,
+                                                          ctr + 0);
             lm.end();
-            launches += 3;
+            lm.begin(SLRGPU_KERNEL_SHADOW);
+            kShadowVolMedium<<<g.shadowVolMedium, block, 0, stream>>>(ds.sc, w, w.classQueue, ctr + 0, b);
+            lm.end();
+            launches += 4;
             continue;
         }
         // Closest hits, sorted into one queue per shading class.

@@ -65,11 +65,26 @@ def test_served_films_equal_standalone(gpu_lib, served_scenes, standalone, mode)
             assert info.submit_seconds <= info.start_seconds <= info.done_seconds
         st = srv.stats()
         assert st.requests_done == len(REQUESTS) and st.queued == 0 and st.active == 0
-        if m == gpu_lib.SERVER_BATCHED:
-            # packing: fewer waves than the requests would need one by one
-            singles = sum(-(-spp // max(1, (1 << 16) // (((w + 7) // 8 * 8) * ((h + 7) // 8 * 8))))
-                          for _, w, h, spp, _, _, _ in REQUESTS)
-            assert st.waves < singles
+    finally:
+        srv.close()
+
+
+def test_queued_requests_share_waves(gpu_lib, served_scenes):
+    """Requests that queue up behind a long one are packed into shared
+    waves: one slot, a request that fills it for 128 waves, then six small
+    requests of the same scene submitted at once."""
+    ctx, scs = served_scenes
+    srv = gpu_lib.Server(ctx, mode=gpu_lib.SERVER_BATCHED, slots=1, paths_per_slot=1 << 16, max_depth=16)
+    try:
+        big = srv.submit(scs[0], 64, 64, 2048, 8, seed=1)          # 16 samples of 4096 positions per wave
+        small = [srv.submit(scs[0], 16, 16, 4, 8, seed=10 + k) for k in range(6)]
+        refs = [scs[0].render(16, 16, 4, 8, seed=10 + k)[0] for k in range(6)]
+        srv.wait(big, timeout=300)
+        for rid, ref in zip(small, refs):
+            film, _ = srv.wait(rid, timeout=60)
+            assert np.array_equal(film, ref)
+        waves = srv.stats().waves
+        assert waves < 128 + 6, waves
     finally:
         srv.close()
 
