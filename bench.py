@@ -48,6 +48,7 @@ sys.path.insert(0, ROOT)
 WIDTH = HEIGHT = 1024
 SPP = 64
 MAX_DEPTH = 10
+VOLUMETRIC = False
 METRIC = "path samples/s"
 WORKLOAD = ("ggx_ibl_1m: 1,034,242-triangle height field (512x512, 6-octave improved Perlin, amplitude 0.2) "
             "+ 64 geodesic spheres (8000 triangles, scale log-uniform 0.05-0.3), GGX conductors/dielectrics "
@@ -139,7 +140,7 @@ def cpu_baseline(desc, threads: int, seconds_target: float = 12.0):
     build_s = time.time() - t0
     total_samples, total_s, frames = 0, 0.0, 0
     while total_s < seconds_target and frames < 16:
-        _, s = ref.render(WIDTH, HEIGHT, 1, MAX_DEPTH, seed=frames, threads=threads)
+        _, s = ref.render(WIDTH, HEIGHT, 1, MAX_DEPTH, seed=frames, threads=threads, volumetric=VOLUMETRIC)
         total_samples += WIDTH * HEIGHT
         total_s += s
         frames += 1
@@ -155,11 +156,11 @@ def run_reference(args):
     from oracle import oracle as O
     from slr_gb300 import scenes
     threads = os.cpu_count() or 1
-    desc = scenes.heightfield_scene(seed=0)
+    desc = WORKLOADS[args.workload]["scene"]()
     ref = O.RefScene(desc)
     times = []
     for i in range(args.warmup + args.steps):
-        _, s = ref.render(WIDTH, HEIGHT, 1, MAX_DEPTH, seed=i, threads=threads)
+        _, s = ref.render(WIDTH, HEIGHT, 1, MAX_DEPTH, seed=i, threads=threads, volumetric=VOLUMETRIC)
         if i >= args.warmup:
             times.append(s)
     per_step = WIDTH * HEIGHT
@@ -168,7 +169,7 @@ def run_reference(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded procedural scene)",
-            "config": {"workload": WORKLOAD, "step": f"{WIDTH}x{HEIGHT} at 1 spp (bounded sample of the 64-spp frame)"},
+            "config": {"workload": WORKLOAD, "step": f"{WIDTH}x{HEIGHT} at 1 spp (bounded sample of the {SPP}-spp frame)"},
             "cpu_baseline": {"value": value, "unit": METRIC, "cores": threads, "kind": "reference",
                              "sample": f"{args.steps} frames at {WIDTH}x{HEIGHT}, 1 spp, max depth {MAX_DEPTH}"},
             "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -259,7 +260,138 @@ def run_serving(args):
     return 0
 
 
+def run_traversal(args):
+    """Traversal microbenchmark on the 1M-triangle scene's BVH: 16,777,216
+    coherent primary rays (4096x4096 pinhole, pixel centres) and 16,777,216
+    incoherent rays (origins uniform over the surface area, directions
+    uniform on the sphere, t_max uniform in [0.1, 10]); closest-hit and
+    any-hit queries.  Primitive ids and t are checked against the reference
+    accelerator on a 65,536-ray sample of each set."""
+    import numpy as np
+    import torch
+    from slr_gb300 import api, scenes
+    from oracle import oracle as O
+    desc = scenes.heightfield_scene(seed=0)
+    scene = api.Scene(desc)
+    n_side = 4096
+    n = n_side * n_side
+    dev = torch.device("cuda")
+    g = torch.Generator(device=dev)
+    g.manual_seed(0)
+    # coherent: pinhole through pixel centres, the scene camera's frame
+    cam = desc.camera
+    m = torch.tensor(cam.cam_to_world, dtype=torch.float64, device=dev)
+    th = np.tan(cam.fov_y / 2)
+    ij = torch.arange(n_side, dtype=torch.float64, device=dev) + 0.5
+    y, x = torch.meshgrid(ij, ij, indexing="ij")
+    lx = (0.5 - x / n_side) * 2 * th * cam.aspect      # mirrored image x (PerspectiveCamera)
+    ly = (0.5 - y / n_side) * 2 * th
+    dl = torch.stack([lx, ly, torch.ones_like(lx)], -1).reshape(-1, 3)
+    dw = dl @ m[:3, :3].T
+    dw = dw / dw.norm(dim=1, keepdim=True)
+    coherent = torch.zeros((n, 8), dtype=torch.float32, device=dev)
+    coherent[:, 0:3] = m[:3, 3].float()
+    coherent[:, 4:7] = dw.float()
+    coherent[:, 7] = float("inf")
+    # incoherent: area-weighted surface points, uniform directions
+    tris = torch.tensor(desc.triangle_arrays(), dtype=torch.float32, device=dev)
+    area = 0.5 * torch.linalg.cross(tris[:, 1] - tris[:, 0], tris[:, 2] - tris[:, 0]).norm(dim=1)
+    pick = torch.multinomial(area, n, replacement=True, generator=g)
+    u0 = torch.rand(n, device=dev, generator=g)
+    u1 = torch.rand(n, device=dev, generator=g)
+    su = u0.sqrt()
+    b0, b1 = 1 - su, u1 * su
+    t = tris[pick]
+    org = b0[:, None] * t[:, 0] + b1[:, None] * t[:, 1] + (1 - b0 - b1)[:, None] * t[:, 2]
+    z = torch.rand(n, device=dev, generator=g) * 2 - 1
+    phi = torch.rand(n, device=dev, generator=g) * 2 * np.pi
+    sz = (1 - z * z).clamp_min(0).sqrt()
+    incoherent = torch.zeros((n, 8), dtype=torch.float32, device=dev)
+    incoherent[:, 0:3] = org
+    incoherent[:, 3] = 1e-4
+    incoherent[:, 4] = sz * torch.cos(phi)
+    incoherent[:, 5] = sz * torch.sin(phi)
+    incoherent[:, 6] = z
+    incoherent[:, 7] = 0.1 + 9.9 * torch.rand(n, device=dev, generator=g)
+    del tris, pick, t, org
+    torch.cuda.synchronize()
+    results = {}
+    ref = O.RefScene(desc, build=False)
+    check_n = 65536
+    for name, rays in (("coherent", coherent), ("incoherent", incoherent)):
+        for kind in ("closest", "any"):
+            anyhit = kind == "any"
+            for _ in range(args.warmup):
+                scene.trace(rays, anyhit)
+            torch.cuda.synchronize()
+            times = []
+            for _ in range(args.steps):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                prim, tt, _, _ = scene.trace(rays, anyhit)
+                e1.record()
+                torch.cuda.synchronize()
+                times.append(e0.elapsed_time(e1) * 1e-3)
+            # parity on a sample against the reference accelerator
+            sub = rays[:: n // check_n][:check_n].cpu().numpy()
+            rp, rt, _, _ = ref.trace(sub, anyhit=anyhit, threads=os.cpu_count())
+            gp = prim[:: n // check_n][:check_n].cpu().numpy()
+            if anyhit:
+                mism = int((gp.astype(bool) != rp).sum())
+                t_ok = True
+            else:
+                gt = tt[:: n // check_n][:check_n].cpu().numpy()
+                mism = int((gp.astype(np.uint32) != rp).sum())
+                hit = rp != 0xffffffff
+                t_ok = bool(np.all(np.abs(gt[hit] - rt[hit]) <= 1e-6 * np.abs(rt[hit])))
+            results[f"{name}_{kind}"] = {"rays_per_s": n / (sum(times) / len(times)), "ms": 1e3 * sum(times) / len(times),
+                                         "sample_id_mismatches": mism, "sample_t_within_1e-6": t_ok}
+    # CPU baseline: the reference accelerator on 1M incoherent closest-hit rays
+    sub = incoherent[: 1 << 20].cpu().numpy()
+    t0 = time.perf_counter()
+    ref.trace(sub, anyhit=False, threads=os.cpu_count())
+    cpu_s = time.perf_counter() - t0
+    total_rays = 4 * n
+    total_s = sum(r["ms"] for r in results.values()) * 1e-3
+    line = {"metric": "rays/s", "value": total_rays / total_s, "unit": "rays/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "higher_is_better": True, "dtype": "f32", "data": "synthetic (seeded rays)",
+            "config": {"workload": "traversal: 1,034,242-triangle scene, 4-wide BVH from the SBVH; 4096x4096 coherent "
+                                   "primary rays and 16,777,216 incoherent rays, closest and any hit",
+                       "l2": "rays (512 MB per set) exceed L2"},
+            "sets": results,
+            "cpu_baseline": {"value": (1 << 20) / cpu_s, "unit": "rays/s", "cores": os.cpu_count(), "kind": "reference",
+                             "sample": "1,048,576 incoherent closest-hit rays through the reference SBVH"}}
+    print(json.dumps(line))
+    return 0
+
+
+def _workloads():
+    from slr_gb300 import scenes
+    return {
+        "ggx_ibl_1m": dict(width=1024, height=1024, spp=64, depth=10, volumetric=False, text=WORKLOAD,
+                           scene=lambda: scenes.heightfield_scene(seed=0)),
+        "small": dict(width=512, height=512, spp=4, depth=10, volumetric=False,
+                      text="small: 256x256 height field + 16 spheres (freq 12), 256x128 IBL, 512x512, max depth 10",
+                      scene=lambda: scenes.heightfield_scene(grid=256, spheres=16, sphere_freq=12, env_size=(256, 128),
+                                                             width=512, height=512, seed=0)),
+        "box": dict(width=256, height=256, spp=16, depth=8, volumetric=False,
+                    text="box_pt: closed box of 10 triangles + 2 rotated boxes, Lambert walls, 0.25x0.25 ceiling "
+                         "light of radiance 15, pinhole, 256x256, 16 spp, max depth 8, seed 0",
+                    scene=lambda: scenes.box_scene(256, 256)),
+        "volumetric": dict(width=512, height=512, spp=64, depth=32, volumetric=True,
+                           text="volumetric_box: the box filled with a 256^3 fBm density grid (sigma_t max 20, "
+                                "albedo 0.9, Henyey-Greenstein g 0.7, 16^3 super voxels), VolumetricPTRenderer, "
+                                "512x512, 64 spp, max depth 32",
+                           scene=lambda: scenes.medium_box_scene(512, 512, grid=256)),
+    }
+
+
+WORKLOADS = None
+
+
 def main():
+    global WORKLOADS
+    WORKLOADS = _workloads()
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=3)
@@ -267,19 +399,27 @@ def main():
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--spp", type=int, default=None)
-    ap.add_argument("--workload", default="ggx_ibl_1m", choices=["ggx_ibl_1m", "small", "serving"])
+    ap.add_argument("--workload", default="ggx_ibl_1m",
+                    choices=["ggx_ibl_1m", "small", "box", "volumetric", "serving", "traversal"])
     ap.add_argument("--requests", type=int, default=512)
     args = ap.parse_args()
     if args.workload == "serving":
         return run_serving(args)
-    global WIDTH, HEIGHT, WORKLOAD
+    if args.workload == "traversal":
+        return run_traversal(args)
+    global WIDTH, HEIGHT, WORKLOAD, SPP, MAX_DEPTH, VOLUMETRIC
+    wl = WORKLOADS[args.workload]
+    WIDTH, HEIGHT, SPP, MAX_DEPTH, VOLUMETRIC, WORKLOAD = (wl["width"], wl["height"], wl["spp"], wl["depth"],
+                                                           wl["volumetric"], wl["text"])
     if args.workload == "small":
-        WIDTH = HEIGHT = 512
-        WORKLOAD = "small: 256x256 height field + 16 spheres (freq 12), 256x128 IBL, 512x512, max depth 10"
         args.no_cpu_baseline = True
     if args.spp is None:
-        args.spp = 4 if args.workload == "small" else SPP
+        args.spp = SPP
     if args.impl == "reference":
+        if args.workload in ("serving", "traversal"):
+            print(json.dumps({"impl": "reference", "unavailable": "the reference has no serving loop; its "
+                              "traversal is timed by --workload traversal's cpu_baseline"}))
+            return 0
         return run_reference(args)
 
     import numpy as np
@@ -298,11 +438,7 @@ def main():
             dist.barrier()
 
     spp = args.spp
-    if args.workload == "small":
-        desc = scenes.heightfield_scene(grid=256, spheres=16, sphere_freq=12, env_size=(256, 128), width=WIDTH,
-                                        height=HEIGHT, seed=0)
-    else:
-        desc = scenes.heightfield_scene(seed=0)
+    desc = wl["scene"]()
     ctx = api.Context(local)
     t0 = time.time()
     scene = api.Scene(desc, context=ctx)
@@ -313,7 +449,7 @@ def main():
 
     film_dev = torch.empty((HEIGHT, WIDTH, 16), dtype=torch.float32, device="cuda")
     for i in range(args.warmup):
-        scene.render(WIDTH, HEIGHT, spp, MAX_DEPTH, seed=seed_base + i, film=film_dev)
+        scene.render(WIDTH, HEIGHT, spp, MAX_DEPTH, seed=seed_base + i, film=film_dev, volumetric=VOLUMETRIC)
     torch.cuda.synchronize()
 
     clocks = ClockSampler(local)
@@ -329,7 +465,7 @@ def main():
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()
         _, rs = scene.render(WIDTH, HEIGHT, spp, MAX_DEPTH, seed=seed_base + 100 + i, film=film_dev,
-                             flags=api.FLAG_PROFILE_KERNELS)
+                             flags=api.FLAG_PROFILE_KERNELS, volumetric=VOLUMETRIC)
         e1.record()
         torch.cuda.synchronize()
         barrier()
@@ -360,7 +496,7 @@ def main():
         torch.cuda.synchronize()
         t1 = time.perf_counter()
         h2d = scene.reupload()
-        scene.render(WIDTH, HEIGHT, spp, MAX_DEPTH, seed=seed_base + 200 + i, film=film_np)
+        scene.render(WIDTH, HEIGHT, spp, MAX_DEPTH, seed=seed_base + 200 + i, film=film_np, volumetric=VOLUMETRIC)
         torch.cuda.synchronize()
         e2e_ms.append(1e3 * (time.perf_counter() - t1))
     e2e_total = sum(e2e_ms)

@@ -72,6 +72,10 @@ typedef struct slrgpu_settings {
                                      the sample grid (W and H rounded up to
                                      multiples of 8) */
     uint32_t flags;               /* SLRGPU_FLAG_* */
+    uint32_t sample_base;         /* index of the first sample: renders of disjoint
+                                     ranges [sample_base, sample_base + spp) of one
+                                     image (e.g. one per GPU) sum to the film of
+                                     the whole range */
 } slrgpu_settings;
 
 /* settings.flags: record CUDA events around every launch and report the
@@ -264,6 +268,23 @@ int slrgpu_server_poll(slrgpu_handle server, uint64_t request, slrgpu_request_in
 int slrgpu_server_wait(slrgpu_handle server, uint64_t request, float* film, slrgpu_request_info* info,
                        double timeout_seconds);
 int slrgpu_server_get_stats(slrgpu_handle server, slrgpu_server_stats* stats);
+
+/* Film output --------------------------------------------------------- *
+ * ImageSensor::saveImage (libSLR/Core/ImageSensor.cpp:139-195) on the GPU: the
+ * film (width*height*16 floats, the layout slrgpu_render writes) times
+ * scale x sensitivity (an infinite sensitivity counts as 1) -> XYZ with the
+ * CIE 1931 2-degree colour matching functions integrated over the 16 bins ->
+ * sRGB -> 1 - exp(-x) -> sRGB gamma -> 8 bits.  pixels (optional) receives
+ * the BMP pixel array: bottom-up rows of B, G, R bytes, each row padded to a
+ * multiple of 4 bytes with zeros ((3*width + width%4) * height bytes); path
+ * (optional) receives a 24-bit BMP file laid out as the reference's
+ * (Helper/bmp_exporter.cpp:15-53). */
+int slrgpu_film_to_bmp(const float* film, uint32_t width, uint32_t height, int film_on_device, float scale,
+                       float sensitivity, uint8_t* pixels, const char* path);
+/* The 16 film bins of the colour matching functions (x[16], y[16], z[16])
+ * and their y integral (DiscretizedSpectrumTemplate::initialize,
+ * spectrum_types.cpp:945-995).  Host only. */
+int slrgpu_film_cmf(float* bins, float* integral);
 
 /* Ray queries on the committed scene (device pointers).  rays: n x 8 floats
  * (org.xyz, tmin, dir.xyz, tmax).  Closest hit fills prim (0xffffffff on

@@ -56,6 +56,8 @@ def lib():
             "ora_spectrum_eval": (I, [P, I, fp, I, fp]),
             "ora_dropped_samples": (C.c_ulonglong, []),
             "ora_medium_query": (I, [P, I, I, fp, fp, C.POINTER(C.c_int), up, I, fp]),
+            "ora_film_bmp": (I, [fp, I, I, F, F, C.c_char_p]),
+            "ora_film_cmf": (I, [fp, fp]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -241,3 +243,19 @@ def bsdf_query(kind: str, spec0, spec1=None, spec2=None, ax=0.0, ay=0.0, queries
     if rc != 0:
         raise ValueError(kind)
     return out
+
+
+def film_bmp(film: np.ndarray, scale: float, sensitivity: float, path: str) -> None:
+    """Writes the film (h, w, 16) as a BMP with the reference's
+    ImageSensor::saveImage."""
+    f, fp = _f(np.ascontiguousarray(film, np.float32).reshape(-1))
+    h, w = film.shape[:2]
+    lib().ora_film_bmp(fp, w, h, float(scale), float(sensitivity), path.encode())
+
+
+def film_cmf():
+    """(bins (48,), integral) of the reference's discretised CMF."""
+    bins = np.zeros(48, np.float32)
+    integ = np.zeros(1, np.float32)
+    lib().ora_film_cmf(bins.ctypes.data_as(C.POINTER(C.c_float)), integ.ctypes.data_as(C.POINTER(C.c_float)))
+    return bins, float(integ[0])

@@ -606,6 +606,37 @@ int ora_medium_query(void* p, int mode, int n, const float* rays, const float* l
     return 0;
 }
 
+// Film output through the reference's own ImageSensor::saveImage
+// (Core/ImageSensor.cpp:139-195): the film (width*height*16 floats, row
+// major) is written into a sensor of the given sensitivity, then saved.
+int ora_film_bmp(const float* film, int w, int h, float scale, float sensitivity, const char* path) {
+    std::call_once(g_colorInit, []() { initializeColorSystem(); });
+    ImageSensor sensor(sensitivity);
+    sensor.init((uint32_t)w, (uint32_t)h);
+    for (int y = 0; y < h; ++y)
+        for (int x = 0; x < w; ++x)
+        {
+            CompensatedSum<DiscretizedSpectrum> &v = sensor.pixel((uint32_t)x, (uint32_t)y).getValue();
+            v.result = DiscretizedSpectrum(film + 16 * ((size_t)y * w + x));
+            v.comp = DiscretizedSpectrum(0.0f);
+        }
+    sensor.saveImage(path, scale);
+    return 0;
+}
+
+// The discretised colour matching functions of the film
+// (DiscretizedSpectrumTemplate::initialize): x[16], y[16], z[16], integral.
+int ora_film_cmf(float* bins, float* integral) {
+    std::call_once(g_colorInit, []() { initializeColorSystem(); });
+    for (int i = 0; i < 16; ++i) {
+        bins[i] = DiscretizedSpectrum::xbar[i];
+        bins[16 + i] = DiscretizedSpectrum::ybar[i];
+        bins[32 + i] = DiscretizedSpectrum::zbar[i];
+    }
+    *integral = DiscretizedSpectrum::integralCMF;
+    return 0;
+}
+
 // Spectrum evaluation at explicit wavelength sets (16 per set), for the
 // upsampled / regular / irregular spectrum parity checks.
 int ora_spectrum_eval(void* p, int spectrum, const float* lambdas, int nsets, float* out) {

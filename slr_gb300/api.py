@@ -46,7 +46,7 @@ class BvhStats(C.Structure):
 class Settings(C.Structure):
     _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("spp", C.c_uint32), ("max_depth", C.c_uint32),
                 ("seed", C.c_uint32), ("volumetric", C.c_uint32), ("samples_per_wave", C.c_uint32),
-                ("flags", C.c_uint32)]
+                ("flags", C.c_uint32), ("sample_base", C.c_uint32)]
 
 
 KERNEL_CLASSES = ["raygen", "extend", "shade", "shadow", "accumulate"]
@@ -146,6 +146,8 @@ def lib():
             "slrgpu_server_poll": (I, [H, C.c_uint64, C.POINTER(RequestInfo)]),
             "slrgpu_server_wait": (I, [H, C.c_uint64, fp, C.POINTER(RequestInfo), C.c_double]),
             "slrgpu_server_get_stats": (I, [H, C.POINTER(ServerStats)]),
+            "slrgpu_film_to_bmp": (I, [fp, U, U, I, F, F, C.POINTER(C.c_uint8), C.c_char_p]),
+            "slrgpu_film_cmf": (I, [fp, fp]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -328,10 +330,11 @@ class Scene:
         return b.value
 
     def render(self, width: int, height: int, spp: int, max_depth: int, seed: int = 0, volumetric: bool = False,
-               samples_per_wave: int = 0, film=None, flags: int = 0):
+               samples_per_wave: int = 0, film=None, flags: int = 0, sample_base: int = 0):
         """Returns (film (h, w, 16) float32 sum over samples, RenderStats).
-        ``film`` may be a preallocated host numpy array or a CUDA tensor."""
-        s = Settings(width, height, spp, max_depth, seed, int(volumetric), samples_per_wave, flags)
+        ``film`` may be a preallocated host numpy array or a CUDA tensor;
+        samples [sample_base, sample_base + spp) are rendered."""
+        s = Settings(width, height, spp, max_depth, seed, int(volumetric), samples_per_wave, flags, sample_base)
         st = RenderStats()
         on_device = 0
         if film is None:
@@ -474,6 +477,27 @@ class Server:
             self.close()
         except Exception:
             pass
+
+
+def film_to_bmp(film: np.ndarray, scale: float = 1.0, sensitivity: float = 1.0, path: str | None = None):
+    """ImageSensor::saveImage on the GPU (slrgpu_film_to_bmp): returns the BMP
+    pixel array (bottom-up BGR rows padded to 4 bytes) of an (h, w, 16) film
+    and writes a BMP file when `path` is given."""
+    f = np.ascontiguousarray(film, np.float32)
+    h, w = f.shape[:2]
+    row = 3 * w + w % 4
+    px = np.zeros(row * h, np.uint8)
+    check(lib().slrgpu_film_to_bmp(_fp(f), w, h, 0, float(scale), float(sensitivity),
+                                   px.ctypes.data_as(C.POINTER(C.c_uint8)), path.encode() if path else None))
+    return px.reshape(h, row)
+
+
+def film_cmf():
+    """(x, y, z bins of the colour matching functions (3, 16), y integral)."""
+    bins = np.zeros(48, np.float32)
+    integ = np.zeros(1, np.float32)
+    check(lib().slrgpu_film_cmf(_fp(bins), _fp(integ)))
+    return bins.reshape(3, 16), float(integ[0])
 
 
 class PathTracingRenderer:

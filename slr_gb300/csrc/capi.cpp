@@ -3,12 +3,14 @@
 
 #include <atomic>
 #include <chrono>
+#include <cstdio>
 #include <cmath>
 #include <cstring>
 #include <memory>
 #include <mutex>
 #include <string>
 #include <unordered_map>
+#include <vector>
 
 #include "../../include/slrgpu.h"
 #include "render_api.h"
@@ -523,6 +525,52 @@ int slrgpu_server_get_stats(slrgpu_handle server, slrgpu_server_stats* stats) {
     if (!rec) return fail(SLRGPU_ERR_INVALID_HANDLE, "invalid server handle");
     if (!stats) return fail(SLRGPU_ERR_INVALID_ARGUMENT, "stats is NULL");
     rec->server->stats(stats);
+    return SLRGPU_OK;
+}
+
+// ---- film output ---------------------------------------------------------------
+int slrgpu_film_to_bmp(const float* film, uint32_t width, uint32_t height, int film_on_device, float scale,
+                       float sensitivity, uint8_t* pixels, const char* path) {
+    if (!film) return fail(SLRGPU_ERR_INVALID_ARGUMENT, "film is NULL");
+    if (width == 0 || height == 0) return fail(SLRGPU_ERR_INVALID_ARGUMENT, "width and height must be positive");
+    const uint32_t rowBytes = 3 * width + width % 4;
+    std::vector<uint8_t> buf((size_t)rowBytes * height);
+    int rc = filmToBmp(film, width, height, film_on_device != 0, scale, sensitivity, buf.data());
+    if (rc != SLRGPU_OK) return rc;
+    if (pixels) std::memcpy(pixels, buf.data(), buf.size());
+    if (path) {
+        // 54-byte BITMAPFILEHEADER + BITMAPINFOHEADER, 24 bits, no compression,
+        // 1 pixel per metre (Helper/bmp_exporter.cpp:15-53).
+        uint8_t header[54];
+        std::memset(header, 0, sizeof(header));
+        auto put32 = [&](int off, uint32_t v) { for (int k = 0; k < 4; ++k) header[off + k] = (uint8_t)(v >> (8 * k)); };
+        auto put16 = [&](int off, uint16_t v) { header[off] = (uint8_t)v; header[off + 1] = (uint8_t)(v >> 8); };
+        header[0] = 'B';
+        header[1] = 'M';
+        put32(2, (uint32_t)buf.size() + 54);
+        put32(10, 54);
+        put32(14, 40);
+        put32(18, width);
+        put32(22, height);
+        put16(26, 1);
+        put16(28, 24);
+        put32(30, 0);
+        put32(34, (uint32_t)buf.size());
+        put32(38, 1);
+        put32(42, 1);
+        FILE* fp = std::fopen(path, "wb");
+        if (!fp) return fail(SLRGPU_ERR_INVALID_ARGUMENT, std::string("cannot open ") + path);
+        bool ok = std::fwrite(header, 1, sizeof(header), fp) == sizeof(header) &&
+                  std::fwrite(buf.data(), 1, buf.size(), fp) == buf.size();
+        std::fclose(fp);
+        if (!ok) return fail(SLRGPU_ERR_INVALID_ARGUMENT, std::string("cannot write ") + path);
+    }
+    return SLRGPU_OK;
+}
+
+int slrgpu_film_cmf(float* bins, float* integral) {
+    if (!bins || !integral) return fail(SLRGPU_ERR_INVALID_ARGUMENT, "NULL argument");
+    discretizedCmf(bins, bins + 16, bins + 32, integral);
     return SLRGPU_OK;
 }
 

@@ -10,6 +10,7 @@
 #include "render_api.h"
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cstdio>
 #include <cstring>
@@ -258,7 +259,11 @@ __device__ __noinline__ void makeBsdf(const DevScene &sc, const DevMaterial &m, 
 // ---------------------------------------------------------------------------
 // Kernels
 // ---------------------------------------------------------------------------
-__global__ void kRaygen(DevScene sc, WaveState ws, const __grid_constant__ WaveParams wp) {
+// wpDev: the wave's parameters in device memory (graph-captured waves, whose
+// launch parameters are fixed at capture), or null to use wpArg.
+__global__ void kRaygen(DevScene sc, WaveState ws, const __grid_constant__ WaveParams wpArg,
+                        const WaveParams* __restrict__ wpDev) {
+    const WaveParams &wp = wpDev ? *wpDev : wpArg;
     if (blockIdx.x == 0 && threadIdx.x == 0) ws.counters[kCtrExt] = wp.numPaths;
     for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < wp.numPaths; p += gridDim.x * blockDim.x) {
         uint32_t k = 0;
@@ -1042,7 +1047,9 @@ __global__ void kShadowVolMedium(DevScene sc, WaveState ws, const uint32_t* __re
 // Adds the wave's paths to the film: C = L * weight, dropped when not finite
 // (PTRenderer.cpp:129-138); binning and compensated sum of
 // SpectrumStorage::add (spectrum_types.h:716-739, CompensatedSum.h:16-33).
-__global__ void kAccumulate(WaveState ws, const __grid_constant__ WaveParams wp) {
+__global__ void kAccumulate(WaveState ws, const __grid_constant__ WaveParams wpArg,
+                            const WaveParams* __restrict__ wpDev) {
+    const WaveParams &wp = wpDev ? *wpDev : wpArg;
     const float recBinWidth = kNumLambda / (kWavelengthHigh - kWavelengthLow);
     for (uint32_t fp = blockIdx.x * blockDim.x + threadIdx.x; fp < wp.filmPixels; fp += gridDim.x * blockDim.x) {
         uint32_t k = 0;
@@ -1303,6 +1310,8 @@ int uploadScene(const HostScene &hs, const BuiltScene &bs, DeviceScene* ds) {
     UP(bs.vnrm, vnrm);
     UP(bs.vtan, vtan);
     UP(hs.materials, materials);
+    static std::atomic<uint64_t> nextUid{1};
+    ds->uid = nextUid.fetch_add(1);
     ds->kindMask = 0;
     for (const DevMaterial &m : hs.materials)
         if (m.kind < kMatNull) ds->kindMask |= 1u << m.kind;
@@ -1492,13 +1501,13 @@ static WavePlan planWaves(const slrgpu_settings &s, uint32_t autoPaths) {
 // queues, then the film update of every segment.  Stream-ordered; counters,
 // queues and path state live in w.  Returns the number of kernel launches.
 static uint64_t runWave(const DeviceScene &ds, const WaveState &w, const WaveParams &wp, uint32_t D, bool volumetric,
-                        cudaStream_t stream, LaunchMarks &lm) {
+                        cudaStream_t stream, LaunchMarks &lm, const WaveParams* wpDev = nullptr) {
     const int block = 256;
     const WaveGrids &g = waveGrids(block);
     uint64_t launches = 0;
     cudaMemsetAsync(w.counters, 0, (size_t)kCtrStride * (D + 2) * sizeof(uint32_t), stream);
     lm.begin(SLRGPU_KERNEL_RAYGEN);
-    kRaygen<<<g.raygen, block, 0, stream>>>(ds.sc, w, wp);
+    kRaygen<<<g.raygen, block, 0, stream>>>(ds.sc, w, wp, wpDev);
     lm.end();
     ++launches;
     for (uint32_t b = 0; b <= D; ++b) {
@@ -1574,7 +1583,7 @@ static uint64_t runWave(const DeviceScene &ds, const WaveState &w, const WavePar
         ++launches;
     }
     lm.begin(SLRGPU_KERNEL_ACCUMULATE);
-    kAccumulate<<<g.accumulate, block, 0, stream>>>(w, wp);
+    kAccumulate<<<g.accumulate, block, 0, stream>>>(w, wp, wpDev);
     lm.end();
     ++launches;
     return launches;
@@ -1595,7 +1604,7 @@ static uint64_t runWaves(const DeviceScene &ds, const slrgpu_settings &s, const 
         sg.gridW = pl.gridW;
         sg.gridH = pl.gridH;
         sg.gridPositions = pl.gridPositions;
-        sg.sampleBase = base;
+        sg.sampleBase = s.sample_base + base;
         sg.samples = std::min(pl.S, s.spp - base);
         sg.seed = s.seed;
         sg.filmBegin = 0;
@@ -1827,16 +1836,130 @@ int renderNoAlloc(const DeviceScene &ds, const slrgpu_settings &s, float* film, 
 }
 
 // ---------------------------------------------------------------------------
+// Film output (ImageSensor::saveImage, Core/ImageSensor.cpp:139-195): the 16
+// bins times scale x sensitivity -> XYZ with the discretised colour matching
+// functions -> sRGB (double-precision matrix, spectrum_base.h:68-72) ->
+// clamp at 0 -> 1 - exp(-x) -> sRGB gamma (spectrum_base.cpp:16-21) ->
+// min(255, 256 x value), written as bottom-up BGR rows padded to 4 bytes.
+// The arithmetic is rounded as the reference's host build rounds it (no
+// contraction; the double expressions stay double).
+// ---------------------------------------------------------------------------
+struct FilmColor {
+    float xbar[16], ybar[16], zbar[16];
+    float integral;
+};
+
+__device__ __forceinline__ float srgbGamma(float v) {
+    if ((double)v <= 0.0031308) return (float)__dmul_rn(12.92, (double)v);
+    return (float)__dsub_rn(__dmul_rn(1.055, pow((double)v, 1.0 / 2.4)), 0.055);
+}
+
+__global__ void kFilmToBmp(const float* __restrict__ film, uint32_t w, uint32_t h, float scale, FilmColor fc,
+                           uint8_t* __restrict__ out, uint32_t rowBytes) {
+    const uint32_t P = w * h;
+    for (uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x; pix < P; pix += gridDim.x * blockDim.x) {
+        const uint32_t i = pix / w, j = pix - i * w;
+        float X = 0.0f, Y = 0.0f, Z = 0.0f;
+#pragma unroll
+        for (int b = 0; b < kNumLambda; ++b) {
+            const float v = __fmul_rn(film[(size_t)pix * kNumLambda + b], scale);
+            X = __fadd_rn(X, __fmul_rn(fc.xbar[b], v));
+            Y = __fadd_rn(Y, __fmul_rn(fc.ybar[b], v));
+            Z = __fadd_rn(Z, __fmul_rn(fc.zbar[b], v));
+        }
+        X = __fdiv_rn(X, fc.integral);
+        Y = __fdiv_rn(Y, fc.integral);
+        Z = __fdiv_rn(Z, fc.integral);
+        const double x = X, y = Y, z = Z;
+        float rgb[3];
+        rgb[0] = (float)__dsub_rn(__dsub_rn(__dmul_rn(3.2404542, x), __dmul_rn(1.5371385, y)), __dmul_rn(0.4985314, z));
+        rgb[1] = (float)__dadd_rn(__dadd_rn(__dmul_rn(-0.9692660, x), __dmul_rn(1.8760108, y)), __dmul_rn(0.0415560, z));
+        rgb[2] = (float)__dadd_rn(__dsub_rn(__dmul_rn(0.0556434, x), __dmul_rn(0.2040259, y)), __dmul_rn(1.0572252, z));
+        uint8_t bytes[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            float v = rgb[c] < 0.0f ? 0.0f : rgb[c];
+            v = __fsub_rn(1.0f, expf(-v));
+            const float g = __fmul_rn(256.0f, srgbGamma(v));
+            bytes[c] = (uint8_t)min(255u, (uint32_t)g);
+        }
+        uint8_t* dst = out + (size_t)(h - i - 1) * rowBytes + 3 * j;
+        dst[0] = bytes[2];
+        dst[1] = bytes[1];
+        dst[2] = bytes[0];
+    }
+}
+
+int filmToBmp(const float* film, uint32_t width, uint32_t height, bool filmOnDevice, float scale, float sensitivity,
+              uint8_t* pixels) {
+    if (width == 0 || height == 0) {
+        setError("width and height must be positive");
+        return SLRGPU_ERR_INVALID_ARGUMENT;
+    }
+    FilmColor fc;
+    discretizedCmf(fc.xbar, fc.ybar, fc.zbar, &fc.integral);
+    if (std::isinf(sensitivity)) sensitivity = 1.0f;
+    scale *= sensitivity;
+    const uint32_t rowBytes = 3 * width + width % 4;
+    const size_t filmBytes = (size_t)width * height * kNumLambda * sizeof(float);
+    const size_t outBytes = (size_t)rowBytes * height;
+    float* dfilm = nullptr;
+    uint8_t* dout = nullptr;
+    cudaError_t e = cudaSuccess;
+    if (!filmOnDevice) {
+        e = cudaMalloc(&dfilm, filmBytes);
+        if (e == cudaSuccess) e = cudaMemcpy(dfilm, film, filmBytes, cudaMemcpyHostToDevice);
+    }
+    if (e == cudaSuccess) e = cudaMalloc(&dout, outBytes);
+    if (e == cudaSuccess) e = cudaMemset(dout, 0, outBytes);
+    if (e == cudaSuccess) {
+        kFilmToBmp<<<std::min<uint32_t>((width * height + 255) / 256, 4096), 256>>>(
+            filmOnDevice ? film : dfilm, width, height, scale, fc, dout, rowBytes);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(pixels, dout, outBytes, cudaMemcpyDeviceToHost);
+    if (dfilm) cudaFree(dfilm);
+    if (dout) cudaFree(dout);
+    if (e != cudaSuccess) {
+        setError(cudaGetErrorString(e));
+        return SLRGPU_ERR_CUDA;
+    }
+    return SLRGPU_OK;
+}
+
+// ---------------------------------------------------------------------------
 // Wave slots for the serving loop: path state for up to `paths` paths and
 // waves whose segments come from several requests of one scene.
 // ---------------------------------------------------------------------------
+// A slot captures the launch sequence of a wave (counter reset, ray
+// generation, every bounce's kernels, film update) once per (scene, max
+// depth, integrator) as a CUDA graph and replays it for every later wave of
+// that kind; the wave's segments travel in device memory (copied from pinned
+// staging memory before each replay), so the captured launches never change.
 struct WaveSlot {
     RenderEngine engine;   // path state only; films belong to the requests
+    WaveParams* dParams = nullptr;
+    WaveParams* hParams = nullptr;   // pinned
+    struct Graph {
+        uint64_t sceneUid;
+        uint32_t depth;
+        bool volumetric;
+        cudaGraphExec_t exec;
+        uint64_t launches;
+    };
+    std::vector<Graph> graphs;
+    ~WaveSlot() {
+        for (Graph &g : graphs) cudaGraphExecDestroy(g.exec);
+        if (dParams) cudaFree(dParams);
+        if (hParams) cudaFreeHost(hParams);
+    }
 };
 
 WaveSlot* waveSlotCreate(uint32_t paths, uint32_t maxDepth, std::string* err) {
     WaveSlot* slot = new WaveSlot();
-    if (slot->engine.ensure(paths, maxDepth) != SLRGPU_OK) {
+    if (slot->engine.ensure(paths, maxDepth) != SLRGPU_OK ||
+        cudaMalloc(&slot->dParams, sizeof(WaveParams)) != cudaSuccess ||
+        cudaMallocHost(&slot->hParams, sizeof(WaveParams)) != cudaSuccess) {
         if (err) *err = "wave slot allocation failed";
         delete slot;
         return nullptr;
@@ -1851,7 +1974,7 @@ uint32_t waveSlotCapacity(const WaveSlot* slot) { return slot->engine.capacity; 
 uint32_t sampleGridPositions(uint32_t width, uint32_t height) { return padToTile(width) * padToTile(height); }
 
 int launchWave(const DeviceScene &ds, WaveSlot* slot, const SegmentDesc* segs, int numSegs, uint32_t maxDepth,
-               bool volumetric, cudaStream_t stream, uint64_t* launches) {
+               bool volumetric, cudaStream_t stream, uint64_t* launches, bool useGraph) {
     if (numSegs <= 0 || numSegs > kMaxWaveSegments) {
         setError("a wave holds 1 to 32 segments");
         return SLRGPU_ERR_INVALID_ARGUMENT;
@@ -1889,10 +2012,47 @@ int launchWave(const DeviceScene &ds, WaveSlot* slot, const SegmentDesc* segs, i
     wp.numSegments = (uint32_t)numSegs;
     wp.numPaths = (uint32_t)paths;
     wp.filmPixels = (uint32_t)pixels;
-    LaunchMarks lm;
-    uint64_t n = runWave(ds, *slot->engine.ws, wp, maxDepth, volumetric, stream, lm);
-    if (launches) *launches += n;
-    CUDA_TRY(cudaGetLastError());
+    if (!useGraph) {
+        LaunchMarks lm;
+        uint64_t n = runWave(ds, *slot->engine.ws, wp, maxDepth, volumetric, stream, lm);
+        if (launches) *launches += n;
+        CUDA_TRY(cudaGetLastError());
+        return SLRGPU_OK;
+    }
+    WaveSlot::Graph* graph = nullptr;
+    for (WaveSlot::Graph &g : slot->graphs)
+        if (g.sceneUid == ds.uid && g.depth == maxDepth && g.volumetric == volumetric) graph = &g;
+    if (!graph) {
+        waveGrids(256);   // occupancy queries stay outside the capture
+        // Capture on this stream: the launches read their segments from
+        // slot->dParams, so the by-value parameters are left empty.
+        WaveParams empty;
+        std::memset(&empty, 0, sizeof(empty));
+        LaunchMarks lm;
+        cudaGraph_t g = nullptr;
+        CUDA_TRY(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+        uint64_t n = runWave(ds, *slot->engine.ws, empty, maxDepth, volumetric, stream, lm, slot->dParams);
+        cudaError_t e = cudaStreamEndCapture(stream, &g);
+        if (e != cudaSuccess) {
+            setError(std::string("wave capture failed: ") + cudaGetErrorString(e));
+            return SLRGPU_ERR_CUDA;
+        }
+        cudaGraphExec_t exec = nullptr;
+        e = cudaGraphInstantiate(&exec, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) {
+            setError(std::string("wave graph instantiation failed: ") + cudaGetErrorString(e));
+            return SLRGPU_ERR_CUDA;
+        }
+        slot->graphs.push_back(WaveSlot::Graph{ds.uid, maxDepth, volumetric, exec, n});
+        graph = &slot->graphs.back();
+    }
+    // The previous wave on this slot has completed (the caller waits for it),
+    // so the staging copy is free to overwrite.
+    std::memcpy(slot->hParams, &wp, sizeof(wp));
+    CUDA_TRY(cudaMemcpyAsync(slot->dParams, slot->hParams, sizeof(wp), cudaMemcpyHostToDevice, stream));
+    CUDA_TRY(cudaGraphLaunch(graph->exec, stream));
+    if (launches) *launches += graph->launches;
     return SLRGPU_OK;
 }
 

@@ -25,6 +25,7 @@ struct DeviceScene {
     DevScene sc;
     DeviceBuffers buffers;
     uint32_t kindMask = 0;   // bit k: some material of kind k (MaterialKind) exists
+    uint64_t uid = 0;        // unique per upload (keys captured wave graphs)
 };
 
 struct WaveState;
@@ -63,9 +64,15 @@ WaveSlot* waveSlotCreate(uint32_t paths, uint32_t maxDepth, std::string* err);
 void waveSlotDestroy(WaveSlot* slot);
 uint32_t waveSlotCapacity(const WaveSlot* slot);
 uint32_t sampleGridPositions(uint32_t width, uint32_t height);
+// useGraph: replay the slot's captured graph for this (scene, depth,
+// integrator), capturing it on first use.
 int launchWave(const DeviceScene &ds, WaveSlot* slot, const SegmentDesc* segs, int numSegs, uint32_t maxDepth,
-               bool volumetric, cudaStream_t stream, uint64_t* launches);
+               bool volumetric, cudaStream_t stream, uint64_t* launches, bool useGraph);
 int launchFilmToPixelMajor(const float* filmSum, float* out, uint32_t pixels, cudaStream_t stream);
+
+// Film -> 8-bit sRGB BMP pixel rows (bottom-up BGR, rows padded to 4 bytes).
+int filmToBmp(const float* film, uint32_t width, uint32_t height, bool filmOnDevice, float scale, float sensitivity,
+              uint8_t* pixels);
 
 int uploadScene(const HostScene &hs, const BuiltScene &bs, DeviceScene* ds);
 int reuploadScene(DeviceScene* ds, uint64_t* bytes, cudaStream_t stream);

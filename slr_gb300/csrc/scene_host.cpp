@@ -1194,4 +1194,62 @@ bool buildScene(const HostScene &s, BuiltScene* out, std::string* err) {
     return true;
 }
 
+// ---------------------------------------------------------------------------
+// Film colour: the CIE 1931 2-degree colour matching functions integrated
+// over the 16 film bins (DiscretizedSpectrumTemplate::initialize,
+// BasicTypes/spectrum_types.cpp:945-995), in float and in the same order, so
+// the bins equal the reference's bit for bit.
+// ---------------------------------------------------------------------------
+#include "cmf_table.inc"
+
+void discretizedCmf(float xbar[16], float ybar[16], float zbar[16], float* integral) {
+    const int numSamples = 471, numBins = 16;
+    auto val = [](const unsigned int* bits, int i) {
+        float f;
+        std::memcpy(&f, &bits[i], sizeof(f));
+        return f;
+    };
+    uint32_t sBin = 0;
+    float nextP = float(sBin + 1) / numBins;
+    float xSum = 0, xPrev = val(kCmfXBits, 0);
+    float ySum = 0, yPrev = val(kCmfYBits, 0);
+    float zSum = 0, zPrev = val(kCmfZBits, 0);
+    const float interval = 1;
+    for (int i = 1; i < numSamples; ++i) {
+        float curP = float(i) / (numSamples - 1);
+        float width = interval;
+        float xCur = val(kCmfXBits, i), yCur = val(kCmfYBits, i), zCur = val(kCmfZBits, i);
+        if (curP >= nextP) {
+            width = (curP - nextP) * (830.0f - 360.0f);
+            float t = 1 - width / interval;
+            float xIn = xPrev * (1 - t) + xCur * t;
+            float yIn = yPrev * (1 - t) + yCur * t;
+            float zIn = zPrev * (1 - t) + zCur * t;
+            xSum += (xPrev + xIn) * (interval - width) * 0.5f;
+            ySum += (yPrev + yIn) * (interval - width) * 0.5f;
+            zSum += (zPrev + zIn) * (interval - width) * 0.5f;
+            if (sBin < (uint32_t)numBins) {
+                xbar[sBin] = xSum;
+                ybar[sBin] = ySum;
+                zbar[sBin] = zSum;
+            }
+            xSum = ySum = zSum = 0;
+            xPrev = xIn;
+            yPrev = yIn;
+            zPrev = zIn;
+            ++sBin;
+            nextP = float(sBin + 1) / numBins;
+        }
+        xSum += (xPrev + xCur) * width * 0.5f;
+        ySum += (yPrev + yCur) * width * 0.5f;
+        zSum += (zPrev + zCur) * width * 0.5f;
+        xPrev = xCur;
+        yPrev = yCur;
+        zPrev = zCur;
+    }
+    float sum = 0.0f;
+    for (int i = 0; i < numBins; ++i) sum += ybar[i];
+    *integral = sum;
+}
+
 }  // namespace slrgpu

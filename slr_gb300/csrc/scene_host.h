@@ -130,4 +130,9 @@ struct BuiltScene {
 
 bool buildScene(const HostScene &s, BuiltScene* out, std::string* err);
 
+// The colour matching functions integrated over the 16 film bins and the
+// sum of the y bins (the reference's DiscretizedSpectrum::xbar/ybar/zbar and
+// integralCMF).
+void discretizedCmf(float xbar[16], float ybar[16], float zbar[16], float* integral);
+
 }  // namespace slrgpu

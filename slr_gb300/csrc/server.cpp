@@ -307,7 +307,7 @@ bool Server::launchWaves() {
             SegmentDesc d;
             d.width = r->settings.width;
             d.height = r->settings.height;
-            d.sampleBase = r->samplesIssued;
+            d.sampleBase = r->settings.sample_base + r->samplesIssued;
             d.samples = take;
             d.seed = r->settings.seed;
             d.filmSum = r->filmSum;
@@ -321,7 +321,7 @@ bool Server::launchWaves() {
         if (segs.empty()) break;
         uint64_t n = 0;
         int rc = launchWave(*lead->ds, sl.wave, segs.data(), (int)segs.size(), lead->settings.max_depth,
-                            lead->settings.volumetric != 0, sl.stream, &n);
+                            lead->settings.volumetric != 0, sl.stream, &n, cfg_.mode == SLRGPU_SERVER_BATCHED);
         if (rc != SLRGPU_OK) {
             for (auto &pr : sl.segments) failRequest(pr.first, "wave launch failed");
             sl.segments.clear();

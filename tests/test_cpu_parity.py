@@ -111,3 +111,12 @@ def test_sbvh_full_ggx_scene(gpu_lib, oracle_lib):
     box and words, every leaf reference) equals the reference's."""
     st = _sbvh_equal(gpu_lib, oracle_lib, scenes.heightfield_scene(seed=0))
     assert st.num_triangles == 1034242
+
+
+def test_film_colour_matching_bins_bit_exact(gpu_lib, oracle_lib):
+    """The 16-bin colour matching functions and their integral used to turn
+    films into RGB equal the reference's DiscretizedSpectrum tables."""
+    bins, integ = gpu_lib.film_cmf()
+    rb, ri = oracle_lib.film_cmf()
+    assert np.array_equal(bins.reshape(-1).view(np.uint32), rb.view(np.uint32))
+    assert np.float32(integ).view(np.uint32) == np.float32(ri).view(np.uint32)

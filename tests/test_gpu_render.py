@@ -134,3 +134,15 @@ def test_renderer_interface(gpu_lib):
     film = renderer.render(scene, settings)
     assert film.shape == (16, 16, 16) and film.sum() > 0
     assert renderer.last_stats.path_samples == 16 * 16 * 4
+
+
+def test_sharded_render_sums_to_whole(gpu_lib):
+    """Three ranks' sample ranges (slr_gb300/replicas.py) rendered with
+    sample_base sum to the unsharded film: the same samples, summed in a
+    different grouping (relative difference at float rounding level)."""
+    from slr_gb300.replicas import render_shard
+    s = gpu_lib.Scene(scenes.box_scene(32, 32))
+    whole, _ = s.render(32, 32, 16, 8, seed=5)
+    parts = [render_shard(s, 32, 32, 16, 8, seed=5, world=3, rank=r)[0] for r in range(3)]
+    np.testing.assert_allclose(sum(parts), whole, rtol=2e-5, atol=1e-6)
+    assert not np.array_equal(parts[0], parts[1])
