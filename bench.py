@@ -378,6 +378,10 @@ def _workloads():
                     text="box_pt: closed box of 10 triangles + 2 rotated boxes, Lambert walls, 0.25x0.25 ceiling "
                          "light of radiance 15, pinhole, 256x256, 16 spp, max depth 8, seed 0",
                     scene=lambda: scenes.box_scene(256, 256)),
+        "volumetric_small": dict(width=256, height=256, spp=4, depth=32, volumetric=True,
+                                 text="volumetric_small: the volumetric box with a 128^3 grid, 256x256, 4 spp, "
+                                      "max depth 32 (profiler captures)",
+                                 scene=lambda: scenes.medium_box_scene(256, 256, grid=128)),
         "volumetric": dict(width=512, height=512, spp=64, depth=32, volumetric=True,
                            text="volumetric_box: the box filled with a 256^3 fBm density grid (sigma_t max 20, "
                                 "albedo 0.9, Henyey-Greenstein g 0.7, 16^3 super voxels), VolumetricPTRenderer, "
@@ -400,7 +404,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--spp", type=int, default=None)
     ap.add_argument("--workload", default="ggx_ibl_1m",
-                    choices=["ggx_ibl_1m", "small", "box", "volumetric", "serving", "traversal"])
+                    choices=["ggx_ibl_1m", "small", "box", "volumetric", "volumetric_small", "serving", "traversal"])
     ap.add_argument("--requests", type=int, default=512)
     args = ap.parse_args()
     if args.workload == "serving":
@@ -411,7 +415,7 @@ def main():
     wl = WORKLOADS[args.workload]
     WIDTH, HEIGHT, SPP, MAX_DEPTH, VOLUMETRIC, WORKLOAD = (wl["width"], wl["height"], wl["spp"], wl["depth"],
                                                            wl["volumetric"], wl["text"])
-    if args.workload == "small":
+    if args.workload in ("small", "volumetric_small"):
         args.no_cpu_baseline = True
     if args.spp is None:
         args.spp = SPP

@@ -146,6 +146,13 @@ int slrgpu_medium_density_grid(slrgpu_handle scene, const float* bounds_min, con
                                int sigma_s, int sigma_e, const float* density, uint32_t nx,
                                uint32_t ny, uint32_t nz, float hg_g);
 
+/* The same from the reference's raw density-grid file (the scene-graph
+ * loader's format, libSLRSceneGraph/API.cpp:966-989): uint32 nx, ny, nz, then
+ * nz slices of ny rows of nx float32, native byte order.  A short or
+ * malformed file is an error (SLRGPU_ERR_INVALID_ARGUMENT). */
+int slrgpu_medium_density_grid_file(slrgpu_handle scene, const char* path, const float* bounds_min,
+                                    const float* bounds_max, int sigma_s, int sigma_e, float hg_g);
+
 /* Cameras: cam_to_world is a row-major 4x4 matrix. */
 int slrgpu_camera_perspective(slrgpu_handle scene, const float* cam_to_world, float sensitivity,
                               float aspect, float fov_y, float lens_radius, float img_plane_dist,

@@ -126,6 +126,7 @@ def lib():
             "slrgpu_scene_add_mesh": (I, [H, fp, fp, fp, fp, U, up, U, I]),
             "slrgpu_environment_ibl": (I, [H, u16p, U, U, F]),
             "slrgpu_medium_density_grid": (I, [H, fp, fp, I, I, fp, U, U, U, F]),
+            "slrgpu_medium_density_grid_file": (I, [H, C.c_char_p, fp, fp, I, I, F]),
             "slrgpu_camera_perspective": (I, [H, fp, F, F, F, F, F, F]),
             "slrgpu_camera_equirect": (I, [H, fp, F, F, F]),
             "slrgpu_scene_commit": (I, [H, C.POINTER(BvhStats)]),

@@ -333,6 +333,24 @@ int slrgpu_medium_density_grid(slrgpu_handle scene, const float* bmin, const flo
     return SLRGPU_OK;
 }
 
+int slrgpu_medium_density_grid_file(slrgpu_handle scene, const char* path, const float* bmin, const float* bmax,
+                                    int sigma_s, int sigma_e, float hg_g) {
+    if (!path) return fail(SLRGPU_ERR_INVALID_ARGUMENT, "path is NULL");
+    FILE* fp = std::fopen(path, "rb");
+    if (!fp) return fail(SLRGPU_ERR_INVALID_ARGUMENT, std::string("failed to read density grid file: ") + path);
+    uint32_t n[3] = {0, 0, 0};
+    bool ok = std::fread(n, sizeof(uint32_t), 3, fp) == 3 && n[0] >= 2 && n[1] >= 2 && n[2] >= 2 &&
+              (uint64_t)n[0] * n[1] * n[2] <= (1ull << 32);
+    std::vector<float> density;
+    if (ok) {
+        density.resize((size_t)n[0] * n[1] * n[2]);
+        ok = std::fread(density.data(), sizeof(float), density.size(), fp) == density.size();
+    }
+    std::fclose(fp);
+    if (!ok) return fail(SLRGPU_ERR_INVALID_ARGUMENT, std::string("malformed density grid file: ") + path);
+    return slrgpu_medium_density_grid(scene, bmin, bmax, sigma_s, sigma_e, density.data(), n[0], n[1], n[2], hg_g);
+}
+
 int slrgpu_camera_perspective(slrgpu_handle scene, const float* m, float sensitivity, float aspect, float fov_y,
                               float lens_radius, float img_dist, float obj_dist) {
     const bool mutating = true;

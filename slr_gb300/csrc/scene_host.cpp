@@ -9,6 +9,8 @@
 #include <cmath>
 #include <cstring>
 #include <limits>
+#include <thread>
+#include <vector>
 
 namespace slrgpu {
 
@@ -471,18 +473,19 @@ public:
             m_bounds.unify(m_frags[i].box);
         }
         m_budget = budget;
-        m_depth = 0;
-        uint32_t added = 0;
-        m_overflow = false;
-        build(m_n, 0, m_n, 0, &added);
-        if (m_overflow) {
+        std::vector<Frag> all(m_frags.begin(), m_frags.begin() + m_n);
+        std::vector<Frag>().swap(m_frags);
+        SubTree tree;
+        const int threads = (int)std::max(1u, std::min(64u, std::thread::hardware_concurrency()));
+        subtreeParallel(std::move(all), threads, &tree);
+        if (tree.overflow || tree.leaves.size() > budget) {
             *err = "SBVH fragment budget (5x triangles) exceeded";
             return false;
         }
-        out->nodes = std::move(m_nodes);
-        out->leafPrims = std::move(m_leaves);
-        out->depth = m_depth;
-        out->numFragments = m_n + added;
+        out->nodes = std::move(tree.nodes);
+        out->leafPrims = std::move(tree.leaves);
+        out->depth = tree.depth;
+        out->numFragments = (uint32_t)out->leafPrims.size();
         out->cost = sahCost(out->nodes);
         for (int k = 0; k < 3; ++k) { out->bmin[k] = m_bounds.mn[k]; out->bmax[k] = m_bounds.mx[k]; }
         return true;
@@ -562,142 +565,221 @@ private:
         for (uint32_t i = 0; i < n; ++i) { b0->unifyPoint(isect[i]); b1->unifyPoint(isect[i]); }
     }
 
-    uint32_t build(uint32_t currentSize, uint32_t start, uint32_t end, uint32_t depth, uint32_t* numAdded) {
-        *numAdded = 0;
-        const uint32_t nodeIdx = (uint32_t)m_nodes.size();
-        m_nodes.emplace_back();
-        if (++depth > m_depth) m_depth = depth;
+    // ---- one node's decision (SBVH.h:57-250): leaf, object split or spatial
+    // split, from the node's fragments alone.  The cost sums add fragment
+    // costs of 1 (exact in float for any order) and the boxes are min/max
+    // unions, so the decision does not depend on the fragments' order or on
+    // how the binning is divided between threads.
+    struct Decision {
+        enum Kind { kLeaf, kObject, kSpatial } kind;
+        Box parent;
+        int axis;
+        float pivot;                  // object split
+        uint32_t splitSP;             // spatial split
+        float pMin, pMax, binWidth;
+    };
 
+    struct Bins {
+        static constexpr uint32_t kObjBins = 32, kSBins = 16;
         Box parent, parentCentroid;
         float leafCost = 0.0f;
-        for (uint32_t i = start; i < end; ++i) {
-            parent.unify(m_frags[i].box);
-            float c[3];
-            m_frags[i].box.centroid(c);
-            parentCentroid.unifyPoint(c);
-            leafCost += m_frags[i].cost;
+        Box objBox[kObjBins];
+        float objCost[kObjBins] = {};
+        Box sBox[kSBins];
+        float sEntryCost[kSBins] = {}, sExitCost[kSBins] = {};
+        void merge(const Bins &o, bool obj, bool spatial) {
+            parent.unify(o.parent);
+            parentCentroid.unify(o.parentCentroid);
+            leafCost += o.leafCost;
+            if (obj)
+                for (uint32_t i = 0; i < kObjBins; ++i) { objBox[i].unify(o.objBox[i]); objCost[i] += o.objCost[i]; }
+            if (spatial)
+                for (uint32_t i = 0; i < kSBins; ++i) {
+                    sBox[i].unify(o.sBox[i]);
+                    sEntryCost[i] += o.sEntryCost[i];
+                    sExitCost[i] += o.sExitCost[i];
+                }
         }
+    };
+
+    // Runs fn(lo, hi, partial) over [0, n) on up to `threads` threads and
+    // merges the partial bins in chunk order.
+    template <typename Fn>
+    static void parallelBins(uint32_t n, int threads, Bins* out, bool obj, bool spatial, Fn fn) {
+        const uint32_t kMinChunk = 16384;
+        int t = (int)std::min<uint32_t>((uint32_t)std::max(1, threads), std::max(1u, n / kMinChunk));
+        if (t <= 1) {
+            fn(0u, n, out);
+            return;
+        }
+        std::vector<Bins> part(t);
+        std::vector<std::thread> pool;
+        for (int k = 0; k < t; ++k) {
+            uint32_t lo = (uint32_t)((uint64_t)n * k / t), hi = (uint32_t)((uint64_t)n * (k + 1) / t);
+            pool.emplace_back([&, lo, hi, k]() { fn(lo, hi, &part[k]); });
+        }
+        for (std::thread &th : pool) th.join();
+        for (int k = 0; k < t; ++k) out->merge(part[k], obj, spatial);
+    }
+
+    Decision decide(const Frag* f, uint32_t n, int threads) const {
+        Decision d;
+        Bins bins;
+        parallelBins(n, threads, &bins, false, false, [&](uint32_t lo, uint32_t hi, Bins* b) {
+            for (uint32_t i = lo; i < hi; ++i) {
+                b->parent.unify(f[i].box);
+                float c[3];
+                f[i].box.centroid(c);
+                b->parentCentroid.unifyPoint(c);
+                b->leafCost += f[i].cost;
+            }
+        });
+        const Box parent = bins.parent, parentCentroid = bins.parentCentroid;
+        const float leafCost = bins.leafCost;
+        d.parent = parent;
+        d.kind = Decision::kLeaf;
+        if (n == 1) return d;
         const int axisOP = parentCentroid.widestAxis();
         const int axisSP = parent.widestAxis();
         const float saParent = parent.sa();
         const float pcMin = parentCentroid.mn[axisOP], pcMax = parentCentroid.mx[axisOP];
         const float pMin = parent.mn[axisSP], pMax = parent.mx[axisSP];
-        const uint32_t numObjs = end - start;
-
-        if (numObjs == 1) {
-            makeLeaf(nodeIdx, parent, start, end);
-            return nodeIdx;
-        }
         const float travCost = 1.2f;
+        constexpr uint32_t kObjBins = Bins::kObjBins, kSBins = Bins::kSBins;
 
         // Object binning.
-        constexpr uint32_t kObjBins = 32;
-        Box objBox[kObjBins];
-        float objCost[kObjBins] = {};
         uint32_t splitOP = 0;
         float minCostOP = INFINITY;
         if ((pcMax - pcMin) > 0) {
-            for (uint32_t i = start; i < end; ++i) {
-                const Frag &f = m_frags[i];
-                uint32_t bin = (uint32_t)(kObjBins * ((f.box.center(axisOP) - pcMin) / (pcMax - pcMin)));
-                bin = std::min(bin, kObjBins - 1);
-                objCost[bin] += f.cost;
-                objBox[bin].unify(f.box);
-            }
+            parallelBins(n, threads, &bins, true, false, [&](uint32_t lo, uint32_t hi, Bins* b) {
+                for (uint32_t i = lo; i < hi; ++i) {
+                    uint32_t bin = (uint32_t)(kObjBins * ((f[i].box.center(axisOP) - pcMin) / (pcMax - pcMin)));
+                    bin = std::min(bin, kObjBins - 1);
+                    b->objCost[bin] += f[i].cost;
+                    b->objBox[bin].unify(f[i].box);
+                }
+            });
             for (uint32_t i = 0; i < kObjBins - 1; ++i) {
                 Box b0, b1;
                 float c0 = 0.0f, c1 = 0.0f;
-                for (uint32_t j = 0; j <= i; ++j) { b0.unify(objBox[j]); c0 += objCost[j]; }
-                for (uint32_t j = i + 1; j < kObjBins; ++j) { b1.unify(objBox[j]); c1 += objCost[j]; }
+                for (uint32_t j = 0; j <= i; ++j) { b0.unify(bins.objBox[j]); c0 += bins.objCost[j]; }
+                for (uint32_t j = i + 1; j < kObjBins; ++j) { b1.unify(bins.objBox[j]); c1 += bins.objCost[j]; }
                 float cost = travCost + (b0.sa() * c0 + b1.sa() * c1) / saParent;
                 if (cost < minCostOP) { minCostOP = cost; splitOP = i; }
             }
         }
         Box leftOP, rightOP;
-        for (uint32_t j = 0; j <= splitOP; ++j) leftOP.unify(objBox[j]);
-        for (uint32_t j = splitOP + 1; j < kObjBins; ++j) rightOP.unify(objBox[j]);
+        for (uint32_t j = 0; j <= splitOP; ++j) leftOP.unify(bins.objBox[j]);
+        for (uint32_t j = splitOP + 1; j < kObjBins; ++j) rightOP.unify(bins.objBox[j]);
         Box overlap = intersect(leftOP, rightOP);
         float overlapSA = 0;
         if (overlap.valid()) overlapSA = overlap.sa();
 
         // Spatial binning.
-        constexpr uint32_t kSBins = 16;
         const float binWidth = (parent.mx[axisSP] - parent.mn[axisSP]) / kSBins;
-        Box sBox[kSBins];
-        float sEntryCost[kSBins] = {}, sExitCost[kSBins] = {};
         uint32_t splitSP = 0;
         float minCostSP = INFINITY;
         const float alpha = 1e-5f;
         if (overlapSA / m_bounds.sa() > alpha) {
-            for (uint32_t i = start; i < end; ++i) {
-                const Frag &f = m_frags[i];
-                uint32_t entry = binIndex(f.box.mn[axisSP], pMin, pMax);
-                uint32_t exit = binIndex(f.box.mx[axisSP], pMin, pMax);
-                sEntryCost[entry] += f.cost;
-                sExitCost[exit] += f.cost;
-                for (uint32_t b = entry; b <= exit; ++b) {
-                    float lo = b * binWidth + pMin;
-                    Box chopped = choppedBounds(f.prim, axisSP, lo, lo + binWidth);
-                    sBox[b].unify(intersect(chopped, f.box));
+            parallelBins(n, threads, &bins, false, true, [&](uint32_t lo, uint32_t hi, Bins* b) {
+                for (uint32_t i = lo; i < hi; ++i) {
+                    uint32_t entry = binIndex(f[i].box.mn[axisSP], pMin, pMax);
+                    uint32_t exit = binIndex(f[i].box.mx[axisSP], pMin, pMax);
+                    b->sEntryCost[entry] += f[i].cost;
+                    b->sExitCost[exit] += f[i].cost;
+                    for (uint32_t k = entry; k <= exit; ++k) {
+                        float blo = k * binWidth + pMin;
+                        Box chopped = choppedBounds(f[i].prim, axisSP, blo, blo + binWidth);
+                        b->sBox[k].unify(intersect(chopped, f[i].box));
+                    }
                 }
-            }
+            });
             for (uint32_t i = 0; i < kSBins - 1; ++i) {
                 Box b0, b1;
                 float c0 = 0.0f, c1 = 0.0f;
-                for (uint32_t j = 0; j <= i; ++j) { b0.unify(sBox[j]); c0 += sEntryCost[j]; }
-                for (uint32_t j = i + 1; j < kSBins; ++j) { b1.unify(sBox[j]); c1 += sExitCost[j]; }
+                for (uint32_t j = 0; j <= i; ++j) { b0.unify(bins.sBox[j]); c0 += bins.sEntryCost[j]; }
+                for (uint32_t j = i + 1; j < kSBins; ++j) { b1.unify(bins.sBox[j]); c1 += bins.sExitCost[j]; }
                 float cost = travCost + (b0.sa() * c0 + b1.sa() * c1) / saParent;
                 if (cost < minCostSP) { minCostSP = cost; splitSP = i; }
             }
         }
+        if (leafCost < minCostOP && leafCost < minCostSP) return d;
+        if (minCostOP < minCostSP) {
+            d.kind = Decision::kObject;
+            d.axis = axisOP;
+            d.pivot = pcMin + (pcMax - pcMin) / kObjBins * (splitOP + 1);
+            return d;
+        }
+        d.kind = Decision::kSpatial;
+        d.axis = axisSP;
+        d.splitSP = splitSP;
+        d.pMin = pMin;
+        d.pMax = pMax;
+        d.binWidth = binWidth;
+        return d;
+    }
 
-        if (leafCost < minCostOP && leafCost < minCostSP) {
-            makeLeaf(nodeIdx, parent, start, end);
+    // Object split: partitions [first, last) in place (std::partition, as
+    // SBVH.h:252-257) and returns the split offset (at least 1).
+    static uint32_t objectPartition(Frag* first, Frag* last, const Decision &d) {
+        const int axis = d.axis;
+        const float pivot = d.pivot;
+        Frag* mid = std::partition(first, last, [axis, pivot](const Frag &f) { return f.box.center(axis) < pivot; });
+        return std::max((uint32_t)(mid - first), 1u);
+    }
+
+    // Spatial split (SBVH.h:276-330): fragments straddling the plane become
+    // two, clipped to each side.
+    void spatialSplit(const Frag* f, uint32_t n, const Decision &d, std::vector<Frag>* left,
+                      std::vector<Frag>* right) const {
+        left->reserve(n);
+        right->reserve(n);
+        for (uint32_t i = 0; i < n; ++i) {
+            uint32_t entry = binIndex(f[i].box.mn[d.axis], d.pMin, d.pMax);
+            uint32_t exit = binIndex(f[i].box.mx[d.axis], d.pMin, d.pMax);
+            if (exit <= d.splitSP) {
+                left->push_back(f[i]);
+            } else if (entry > d.splitSP) {
+                right->push_back(f[i]);
+            } else {
+                float splitPos = (d.splitSP + 1) * d.binWidth + d.pMin;
+                Box sl, sr;
+                splitBounds(f[i].prim, d.axis, splitPos, &sl, &sr);
+                if (sl.valid()) left->push_back(Frag{f[i].prim, intersect(sl, f[i].box), f[i].cost});
+                if (sr.valid()) right->push_back(Frag{f[i].prim, intersect(sr, f[i].box), f[i].cost});
+            }
+        }
+    }
+
+    // ---- in-place build of one (small) subtree, as SBVH.h:57-349: nodes in
+    // pre-order, leaf references in the same order.
+    uint32_t build(uint32_t currentSize, uint32_t start, uint32_t end, uint32_t depth, uint32_t* numAdded) {
+        *numAdded = 0;
+        const uint32_t nodeIdx = (uint32_t)m_nodes.size();
+        m_nodes.emplace_back();
+        if (++depth > m_depth) m_depth = depth;
+        const uint32_t numObjs = end - start;
+        const Decision d = decide(m_frags.data() + start, numObjs, 1);
+        if (d.kind == Decision::kLeaf) {
+            makeLeaf(nodeIdx, d.parent, start, end);
             return nodeIdx;
         }
-        if (minCostOP < minCostSP) {
-            float pivot = pcMin + (pcMax - pcMin) / kObjBins * (splitOP + 1);
-            Frag* first = m_frags.data() + start;
-            Frag* mid = std::partition(first, m_frags.data() + end, [axisOP, pivot](const Frag &f) {
-                return f.box.center(axisOP) < pivot;
-            });
-            uint32_t splitIdx = std::max((uint32_t)(mid - first), 1u) + start;
+        if (d.kind == Decision::kObject) {
+            uint32_t splitIdx = objectPartition(m_frags.data() + start, m_frags.data() + end, d) + start;
             uint32_t addL, addR;
             uint32_t c0 = build(currentSize, start, splitIdx, depth, &addL);
             uint32_t c1 = build(currentSize + addL, splitIdx + addL, end + addL, depth, &addR);
-            makeInternal(nodeIdx, parent, c0, c1, axisOP);
+            makeInternal(nodeIdx, d.parent, c0, c1, d.axis);
             *numAdded += addL + addR;
             return nodeIdx;
         }
-
-        // Spatial split: fragments straddling the plane are split in two.
-        uint32_t numLeft = 0, numRight = 0;
-        for (uint32_t j = 0; j <= splitSP; ++j) { (void)j; }
         std::vector<Frag> left, right;
-        left.reserve(numObjs);
-        right.reserve(numObjs);
-        for (uint32_t i = start; i < end; ++i) {
-            const Frag &f = m_frags[i];
-            uint32_t entry = binIndex(f.box.mn[axisSP], pMin, pMax);
-            uint32_t exit = binIndex(f.box.mx[axisSP], pMin, pMax);
-            if (exit <= splitSP) {
-                left.push_back(f);
-            } else if (entry > splitSP) {
-                right.push_back(f);
-            } else {
-                float splitPos = (splitSP + 1) * binWidth + pMin;
-                Box sl, sr;
-                splitBounds(f.prim, axisSP, splitPos, &sl, &sr);
-                if (sl.valid()) left.push_back(Frag{f.prim, intersect(sl, f.box), f.cost});
-                if (sr.valid()) right.push_back(Frag{f.prim, intersect(sr, f.box), f.cost});
-            }
-        }
-        numLeft = (uint32_t)left.size();
-        numRight = (uint32_t)right.size();
+        spatialSplit(m_frags.data() + start, numObjs, d, &left, &right);
+        const uint32_t numLeft = (uint32_t)left.size(), numRight = (uint32_t)right.size();
         *numAdded = (numLeft + numRight) - numObjs;
-        if (currentSize + *numAdded > m_budget) {
+        if (currentSize + *numAdded > (uint32_t)m_frags.size()) {
             m_overflow = true;
-            makeLeaf(nodeIdx, parent, start, end);
+            makeLeaf(nodeIdx, d.parent, start, end);
             *numAdded = 0;
             return nodeIdx;
         }
@@ -709,9 +791,95 @@ private:
         uint32_t addL, addR;
         uint32_t c0 = build(currentSize + *numAdded, start, splitIdx, depth, &addL);
         uint32_t c1 = build(currentSize + *numAdded + addL, splitIdx + addL, end + *numAdded + addL, depth, &addR);
-        makeInternal(nodeIdx, parent, c0, c1, axisSP);
+        makeInternal(nodeIdx, d.parent, c0, c1, d.axis);
         *numAdded += addL + addR;
         return nodeIdx;
+    }
+
+    // ---- parallel build of the top of the tree.  A node's subtree depends
+    // only on its own fragments (in order), so the two children build
+    // concurrently into separate arrays, concatenated afterwards in the
+    // sequential pre-order; the result equals the sequential build's.
+    struct SubTree {
+        std::vector<SbvhNode> nodes;     // pre-order, child / leaf indices local
+        std::vector<uint32_t> leaves;
+        uint32_t depth = 0;
+        bool overflow = false;
+    };
+
+    void subtreeSequential(std::vector<Frag> &&frags, SubTree* out) const {
+        // Fragment headroom grows until the subtree fits (the reference's
+        // decisions never depend on it).
+        for (size_t room = frags.size() * 5 + 64;; room *= 2) {
+            SbvhBuilder local(m_tris, 0);
+            local.m_bounds = m_bounds;
+            local.m_frags = frags;
+            local.m_frags.resize(room);
+            local.m_depth = 0;
+            local.m_overflow = false;
+            uint32_t added = 0;
+            local.build((uint32_t)frags.size(), 0, (uint32_t)frags.size(), 0, &added);
+            if (local.m_overflow && room < ((size_t)1 << 31)) continue;
+            out->nodes = std::move(local.m_nodes);
+            out->leaves = std::move(local.m_leaves);
+            out->depth = local.m_depth;
+            out->overflow = local.m_overflow;
+            return;
+        }
+    }
+
+    static void append(SubTree* dst, const SubTree &src) {
+        const uint32_t nodeBase = (uint32_t)dst->nodes.size(), leafBase = (uint32_t)dst->leaves.size();
+        for (SbvhNode n : src.nodes) {
+            if (n.leaf) {
+                if (n.offset != 0xffffffffu) n.offset += leafBase;
+            } else {
+                n.c0 += nodeBase;
+                n.c1 += nodeBase;
+            }
+            dst->nodes.push_back(n);
+        }
+        dst->leaves.insert(dst->leaves.end(), src.leaves.begin(), src.leaves.end());
+    }
+
+    void subtreeParallel(std::vector<Frag> &&frags, int threads, SubTree* out) const {
+        const uint32_t kSequentialBelow = 1u << 14;
+        const uint32_t n = (uint32_t)frags.size();
+        if (n <= kSequentialBelow || threads <= 1) {
+            subtreeSequential(std::move(frags), out);
+            return;
+        }
+        const Decision d = decide(frags.data(), n, threads);
+        if (d.kind == Decision::kLeaf) {
+            subtreeSequential(std::move(frags), out);
+            return;
+        }
+        std::vector<Frag> left, right;
+        if (d.kind == Decision::kObject) {
+            uint32_t split = objectPartition(frags.data(), frags.data() + n, d);
+            left.assign(frags.begin(), frags.begin() + split);
+            right.assign(frags.begin() + split, frags.end());
+        } else {
+            spatialSplit(frags.data(), n, d, &left, &right);
+        }
+        std::vector<Frag>().swap(frags);
+        SubTree l, r;
+        const int tl = threads / 2, tr = threads - tl;
+        std::thread th([&]() { subtreeParallel(std::move(left), std::max(1, tl), &l); });
+        subtreeParallel(std::move(right), std::max(1, tr), &r);
+        th.join();
+        SbvhNode node{};
+        for (int k = 0; k < 3; ++k) { node.bmin[k] = d.parent.mn[k]; node.bmax[k] = d.parent.mx[k]; }
+        node.axis = (uint32_t)d.axis;
+        node.leaf = 0;
+        out->nodes.clear();
+        out->nodes.push_back(node);
+        out->nodes[0].c0 = 1;
+        out->nodes[0].c1 = 1 + (uint32_t)l.nodes.size();
+        append(out, l);
+        append(out, r);
+        out->depth = 1 + std::max(l.depth, r.depth);
+        out->overflow = l.overflow || r.overflow;
     }
 
     static uint32_t binIndex(float x, float lo, float hi) {

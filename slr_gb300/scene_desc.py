@@ -80,6 +80,26 @@ class Medium:
     hg_g: float = 0.0
 
 
+def write_density_grid(path: str, density: np.ndarray) -> None:
+    """Writes a (nz, ny, nx) float32 grid in the reference's raw density-grid
+    format: uint32 nx, ny, nz, then the slices (libSLRSceneGraph/API.cpp:966-989)."""
+    d = np.ascontiguousarray(density, np.float32)
+    nz, ny, nx = d.shape
+    with open(path, "wb") as f:
+        f.write(np.array([nx, ny, nz], np.uint32).tobytes())
+        f.write(d.tobytes())
+
+
+def read_density_grid(path: str) -> np.ndarray:
+    """Reads the reference's raw density-grid format into a (nz, ny, nx) array."""
+    raw = open(path, "rb").read()
+    nx, ny, nz = np.frombuffer(raw[:12], np.uint32)
+    d = np.frombuffer(raw[12:], np.float32)
+    if d.size != int(nx) * int(ny) * int(nz):
+        raise ValueError(f"malformed density grid file: {path}")
+    return d.reshape(int(nz), int(ny), int(nx))
+
+
 @dataclass
 class SceneDesc:
     spectra: list = field(default_factory=list)

@@ -41,3 +41,33 @@ def test_host_build_of_empty_scene(gpu_lib):
     from slr_gb300.scene_desc import SceneDesc
     s = gpu_lib.Scene(SceneDesc(), host_only=True)
     assert s.bvh_stats.num_triangles == 0
+
+
+def test_density_grid_file_round_trip(tmp_path, gpu_lib):
+    """The reference's raw density-grid format: written and read back by the
+    Python helpers, accepted by slrgpu_medium_density_grid_file (host side
+    only), and a truncated file is rejected."""
+    import ctypes as C
+    from slr_gb300.scene_desc import read_density_grid, write_density_grid
+    rng = np.random.default_rng(0)
+    d = rng.random((5, 4, 3)).astype(np.float32)
+    path = str(tmp_path / "grid.raw")
+    write_density_grid(path, d)
+    assert np.array_equal(read_density_grid(path), d)
+    raw = open(path, "rb").read()
+    assert np.frombuffer(raw[:12], np.uint32).tolist() == [3, 4, 5]
+    L = gpu_lib.lib()
+    h = C.c_uint64()
+    assert L.slrgpu_scene_create(0, C.byref(h)) == 0                      # host-only scene
+    fp = lambda a: a.ctypes.data_as(C.POINTER(C.c_float))  # noqa: E731
+    vals = np.array([2.0, 2.0], np.float32)
+    sid = C.c_int()
+    assert L.slrgpu_spectrum_regular(h.value, 360.0, 830.0, fp(vals), 2, C.byref(sid)) == 0
+    lo = np.zeros(3, np.float32)
+    hi = np.ones(3, np.float32)
+    short = str(tmp_path / "short.raw")
+    open(short, "wb").write(raw[:-4])
+    assert L.slrgpu_medium_density_grid_file(h.value, short.encode(), fp(lo), fp(hi), sid.value, sid.value, 0.3) == -1
+    assert b"malformed" in L.slrgpu_last_error()
+    assert L.slrgpu_medium_density_grid_file(h.value, path.encode(), fp(lo), fp(hi), sid.value, sid.value, 0.3) == 0
+    assert L.slrgpu_scene_destroy(h.value) == 0
