@@ -41,6 +41,9 @@ def _run(cmd):
 
 
 def build(verbose: bool = False, force: bool = False, extra_nvcc: list[str] | None = None) -> Path:
+    # SLRGPU_NVCC_EXTRA: extra nvcc flags, e.g. tuning constants such as
+    # -DSLRGPU_SHADE_MIN_BLOCKS=2 (use force=True when changing them).
+    extra_nvcc = list(extra_nvcc or []) + os.environ.get("SLRGPU_NVCC_EXTRA", "").split()
     cuda = _cuda_home()
     nvcc = str(cuda / "bin" / "nvcc")
     BUILD.mkdir(exist_ok=True)

@@ -285,7 +285,9 @@ __device__ __forceinline__ void bsdfSampleBody(const Bsdf &B, const BsdfQuery &q
         res->pdf = common * mPdf * eExitW * eExitW * fabsf(dotHL);
         res->type = kDirTransmission | kDirHighFreq;
         float r = 1.0f / fabsf(q.dir.z * d.z);
-#pragma unroll
+        // Kept rolled: 16 copies of the refraction half-vector math overflow
+        // the instruction cache of the shading kernel.
+#pragma unroll 1
         for (int i = 0; i < kNumLambda; ++i) {
             float eEnter = entering ? B.a.v[i] : B.b.v[i];
             float eExit = entering ? B.b.v[i] : B.a.v[i];
@@ -344,7 +346,7 @@ __device__ __forceinline__ void bsdfEvalBody(const Bsdf &B, const BsdfQuery &q, 
             for (int i = 0; i < kNumLambda; ++i) fs.v[i] = ((F.v[i] * D) * G) * r;
         } else if (dNVNL < 0) {
             float r = 1.0f / fabsf(dNVNL);
-#pragma unroll
+#pragma unroll 1
             for (int i = 0; i < kNumLambda; ++i) {
                 float eEnter = entering ? B.a.v[i] : B.b.v[i];
                 float eExit = entering ? B.b.v[i] : B.a.v[i];

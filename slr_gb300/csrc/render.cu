@@ -319,7 +319,14 @@ __global__ void kExtend(DevScene sc, WaveState ws, const uint32_t* __restrict__ 
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&ws.stats[0], (unsigned long long)n);
 }
 
-__global__ void kShadow(DevScene sc, WaveState ws, const uint32_t* __restrict__ queue, const uint32_t* __restrict__ count) {
+// Resident blocks per SM the traversal kernels are compiled for; a
+// compile-time tuning constant.
+#ifndef SLRGPU_TRACE_MIN_BLOCKS
+#define SLRGPU_TRACE_MIN_BLOCKS 4
+#endif
+__global__ void __launch_bounds__(256, SLRGPU_TRACE_MIN_BLOCKS) kShadow(DevScene sc, WaveState ws,
+                                                                      const uint32_t* __restrict__ queue,
+                                                                      const uint32_t* __restrict__ count) {
     const uint32_t n = *count;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         uint32_t p = queue[i];
@@ -392,7 +399,8 @@ __device__ __forceinline__ int selectLight(const DevScene &sc, float u, float* p
 // divergence.  Emission with MIS, Russian roulette, next-event estimation and
 // BSDF sampling follow PTRenderer::Job::contribution (PTRenderer.cpp:145-277).
 // ---------------------------------------------------------------------------
-__global__ void kExtendSort(DevScene sc, WaveState ws, const uint32_t* __restrict__ queue,
+__global__ void __launch_bounds__(256, SLRGPU_TRACE_MIN_BLOCKS) kExtendSort(DevScene sc, WaveState ws,
+                                                                          const uint32_t* __restrict__ queue,
                             const uint32_t* __restrict__ count, uint32_t* classCounts) {
     const uint32_t n = *count;
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
@@ -463,7 +471,12 @@ __device__ __forceinline__ void makeBsdfK(const DevScene &sc, const DevMaterial 
 }
 
 template <int K>
-__global__ void __launch_bounds__(256) kShadeSurf(DevScene sc, WaveState ws, uint32_t maxDepth,
+// Resident blocks per SM the shading kernels are compiled for (register cap
+// 65536 / (256 x this)); a compile-time tuning constant.
+#ifndef SLRGPU_SHADE_MIN_BLOCKS
+#define SLRGPU_SHADE_MIN_BLOCKS 3   // 85 registers: +9 % on the 1M-triangle benchmark over 2 (128)
+#endif
+__global__ void __launch_bounds__(256, SLRGPU_SHADE_MIN_BLOCKS) kShadeSurf(DevScene sc, WaveState ws, uint32_t maxDepth,
                                                   const uint32_t* __restrict__ inQueue,
                                                   const uint32_t* __restrict__ inCount, uint32_t* outQueue,
                                                   uint32_t* outCount, uint32_t* shQueue, uint32_t* shCount) {
@@ -701,7 +714,10 @@ __device__ __forceinline__ int selectLight3(const DevScene &sc, float u, int* li
     return idx;
 }
 
-__global__ void __launch_bounds__(256) kShadeVol(DevScene sc, WaveState ws, uint32_t maxDepth,
+#ifndef SLRGPU_SHADEVOL_MIN_BLOCKS
+#define SLRGPU_SHADEVOL_MIN_BLOCKS 3   // measured best on the volumetric benchmark (2, 3 tried)
+#endif
+__global__ void __launch_bounds__(256, SLRGPU_SHADEVOL_MIN_BLOCKS) kShadeVol(DevScene sc, WaveState ws, uint32_t maxDepth,
                                                  const uint32_t* __restrict__ inQueue,
                                                  const uint32_t* __restrict__ inCount, uint32_t* outQueue,
                                                  uint32_t* outCount, uint32_t* shQueue, uint32_t* shCount) {
@@ -1019,7 +1035,11 @@ __global__ void kShadowVol(DevScene sc, WaveState ws, const uint32_t* __restrict
 // wavelength): the 16 ratio-tracking walks of a ray run side by side in
 // consecutive lanes instead of one after another.  Each wavelength draws
 // from its own counter range of the ray's per-bounce random stream.
-__global__ void kShadowVolMedium(DevScene sc, WaveState ws, const uint32_t* __restrict__ queue,
+#ifndef SLRGPU_MEDIUM_MIN_BLOCKS
+#define SLRGPU_MEDIUM_MIN_BLOCKS 4     // 64 registers; measured best of 2, 3, 4
+#endif
+__global__ void __launch_bounds__(256, SLRGPU_MEDIUM_MIN_BLOCKS) kShadowVolMedium(DevScene sc, WaveState ws,
+                                                                                  const uint32_t* __restrict__ queue,
                                  const uint32_t* __restrict__ count, uint32_t bounce) {
     const uint32_t n = *count * kNumLambda;
     for (uint32_t item = blockIdx.x * blockDim.x + threadIdx.x; item < n; item += gridDim.x * blockDim.x) {
