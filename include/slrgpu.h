@@ -81,6 +81,11 @@ typedef struct slrgpu_settings {
 /* settings.flags: record CUDA events around every launch and report the
  * device time per kernel class in slrgpu_render_stats.kernel_ms. */
 #define SLRGPU_FLAG_PROFILE_KERNELS 1u
+/* settings.flags: watertight ray-triangle test (Woop, Benthin, Wald 2013)
+ * instead of the reference's Moller-Trumbore order, which can let a ray
+ * through the shared edge of two triangles; hits then differ from the
+ * reference only for rays within rounding of an edge or vertex. */
+#define SLRGPU_FLAG_WATERTIGHT 2u
 
 /* Kernel classes of the wavefront (index into kernel_ms / kernel_count). */
 #define SLRGPU_KERNEL_RAYGEN 0
@@ -294,9 +299,11 @@ int slrgpu_film_to_bmp(const float* film, uint32_t width, uint32_t height, int f
 int slrgpu_film_cmf(float* bins, float* integral);
 
 /* Ray queries on the committed scene (device pointers).  rays: n x 8 floats
- * (org.xyz, tmin, dir.xyz, tmax).  Closest hit fills prim (0xffffffff on
- * miss), t, b1, b2 (Moller-Trumbore barycentrics); any hit fills prim with 1
- * (occluded) or 0.  stream is a cudaStream_t or NULL. */
+ * (org.xyz, tmin, dir.xyz, tmax).  any_hit bit 0: any hit (prim = 1 when
+ * occluded, else 0), otherwise closest hit filling prim (0xffffffff on miss),
+ * t, b1, b2 (barycentric weights of the second and third vertex); bit 1: the
+ * watertight triangle test instead of the reference's.  stream is a
+ * cudaStream_t or NULL. */
 int slrgpu_trace(slrgpu_handle scene, const float* rays, uint32_t n, int any_hit, uint32_t* prim,
                  float* t, float* b1, float* b2, void* stream);
 

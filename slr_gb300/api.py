@@ -51,6 +51,7 @@ class Settings(C.Structure):
 
 KERNEL_CLASSES = ["raygen", "extend", "shade", "shadow", "accumulate"]
 FLAG_PROFILE_KERNELS = 1
+FLAG_WATERTIGHT = 2
 
 
 class RenderStats(C.Structure):
@@ -349,9 +350,10 @@ class Scene:
         check(lib().slrgpu_render(self.handle, C.byref(s), C.c_void_p(ptr), on_device, C.byref(st)))
         return film, st
 
-    def trace(self, rays_dev, any_hit: bool = False):
+    def trace(self, rays_dev, any_hit: bool = False, watertight: bool = False):
         """rays_dev: torch CUDA float32 tensor (n, 8).  Returns torch tensors
-        (prim, t, b1, b2) on the same device (any hit: prim only)."""
+        (prim, t, b1, b2) on the same device (any hit: prim only); watertight
+        selects the watertight triangle test instead of the reference's."""
         import torch
         n = rays_dev.shape[0]
         prim = torch.empty(n, dtype=torch.int32, device=rays_dev.device)
@@ -364,7 +366,7 @@ class Scene:
             b2 = torch.empty_like(t)
             ptrs = [t.data_ptr(), b1.data_ptr(), b2.data_ptr()]
         stream = torch.cuda.current_stream(rays_dev.device).cuda_stream
-        check(lib().slrgpu_trace(self.handle, C.c_void_p(rays_dev.data_ptr()), n, int(any_hit),
+        check(lib().slrgpu_trace(self.handle, C.c_void_p(rays_dev.data_ptr()), n, int(any_hit) | (2 * int(watertight)),
                                  C.c_void_p(prim.data_ptr()), *(C.c_void_p(p) if p else None for p in ptrs),
                                  C.c_void_p(stream)))
         return prim, t, b1, b2

@@ -9,6 +9,7 @@ with a C ABI (include/slrgpu.h).
 from __future__ import annotations
 
 import concurrent.futures as cf
+import json
 import os
 import shutil
 import subprocess
@@ -40,10 +41,29 @@ def _run(cmd):
     return cmd, r.returncode, r.stdout + r.stderr
 
 
+def tuning_flags() -> list[str]:
+    """nvcc flags of the tuned constants: SLRGPU_NVCC_EXTRA when set (the
+    autotuner's candidates), else slr_gb300/tuning.json (the autotuner's
+    choice), else none (the defaults in the sources)."""
+    if "SLRGPU_NVCC_EXTRA" in os.environ:
+        return os.environ["SLRGPU_NVCC_EXTRA"].split()
+    tuning = PKG / "tuning.json"
+    if not tuning.is_file():
+        return []
+    t = json.loads(tuning.read_text())
+    flags = [f"-D{k}={int(v)}" for k, v in sorted(t.get("knobs", {}).items())]
+    if "wave_paths" in t:
+        flags.append(f"-DSLRGPU_WAVE_PATHS={int(t['wave_paths'])}u")
+    return flags
+
+
 def build(verbose: bool = False, force: bool = False, extra_nvcc: list[str] | None = None) -> Path:
-    # SLRGPU_NVCC_EXTRA: extra nvcc flags, e.g. tuning constants such as
-    # -DSLRGPU_SHADE_MIN_BLOCKS=2 (use force=True when changing them).
-    extra_nvcc = list(extra_nvcc or []) + os.environ.get("SLRGPU_NVCC_EXTRA", "").split()
+    extra_nvcc = list(extra_nvcc or []) + tuning_flags()
+    # rebuild the CUDA objects when the tuned flags change
+    stamp = BUILD / "nvcc_flags"
+    BUILD.mkdir(exist_ok=True)
+    if not stamp.is_file() or stamp.read_text() != " ".join(extra_nvcc):
+        force = True
     cuda = _cuda_home()
     nvcc = str(cuda / "bin" / "nvcc")
     BUILD.mkdir(exist_ok=True)
@@ -75,6 +95,7 @@ def build(verbose: bool = False, force: bool = False, extra_nvcc: list[str] | No
                 raise RuntimeError(f"compile failed: {' '.join(cmd)}\n{out[-6000:]}")
             if verbose:
                 print(out)
+    stamp.write_text(" ".join(extra_nvcc))
     if jobs or not LIB.exists():
         cmd = [nvcc, "-shared", *ARCH, "-o", str(LIB), *[str(o) for o in objs], "-lcudart_static", "-lrt",
                "-lpthread", "-ldl"]

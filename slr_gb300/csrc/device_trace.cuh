@@ -1,13 +1,14 @@
 // Closest-hit and any-hit traversal of the 4-wide BVH.
 //
-// The box and triangle tests repeat the reference's arithmetic exactly (no
-// fused multiply-add): the slab test of BoundingBox3D::intersect
+// By default the box and triangle tests repeat the reference's arithmetic
+// exactly (no fused multiply-add): the slab test of BoundingBox3D::intersect
 // (libSLR/BasicTypes/BoundingBox3D.h:100-116) on the SBVH's own boxes, and
 // the Moller-Trumbore test of TriangleSurfaceShape::intersect
 // (libSLR/SurfaceShape/TriangleSurfaceShape.cpp:205-257), including its
 // inclusive [tmin, tmax] acceptance.  The wide nodes only skip the SBVH's
 // intermediate boxes, which contain their children's boxes, so every
-// triangle the reference would test is still tested.
+// triangle the reference would test is still tested.  With
+// DevScene::watertight the triangle test is the watertight one below.
 #pragma once
 #include "device_common.cuh"
 
@@ -44,20 +45,95 @@ __device__ __forceinline__ bool mtIntersect(const TriFrag &f, V3 org, V3 dir, fl
     return true;
 }
 
+// Watertight ray-triangle test (Woop, Benthin and Wald, "Watertight
+// Ray/Triangle Intersection", JCGT 2013): vertices translated to the ray
+// origin and sheared so the ray runs along +z; the 2-D edge functions are
+// exact in sign for edges shared by two triangles (recomputed in double when
+// one is zero), so a ray never slips between adjacent triangles.  Uses the
+// vertices as given (not v0 + edge).  b1, b2 are the weights of v1 and v2, t
+// is accepted in [tmin, tmax] as the reference's test does.
+struct WtRay {
+    int kx, ky, kz;
+    float sx, sy, sz;
+    V3 org;
+};
+
+__device__ __forceinline__ WtRay wtSetup(V3 org, V3 dir) {
+    const float d[3] = {dir.x, dir.y, dir.z};
+    const float ax = fabsf(dir.x), ay = fabsf(dir.y), az = fabsf(dir.z);
+    int kz = ax > ay ? (ax > az ? 0 : 2) : (ay > az ? 1 : 2);
+    int kx = kz == 2 ? 0 : kz + 1;
+    int ky = kx == 2 ? 0 : kx + 1;
+    float dz = kz == 0 ? d[0] : (kz == 1 ? d[1] : d[2]);
+    if (dz < 0.0f) { int tmp = kx; kx = ky; ky = tmp; }
+    const float dx = kx == 0 ? d[0] : (kx == 1 ? d[1] : d[2]);
+    const float dy = ky == 0 ? d[0] : (ky == 1 ? d[1] : d[2]);
+    WtRay r;
+    r.kx = kx; r.ky = ky; r.kz = kz;
+    r.sx = dx / dz;
+    r.sy = dy / dz;
+    r.sz = 1.0f / dz;
+    r.org = org;
+    return r;
+}
+
+__device__ __forceinline__ float comp(V3 v, int k) { return k == 0 ? v.x : (k == 1 ? v.y : v.z); }
+
+__device__ __forceinline__ bool wtIntersect(const float4* __restrict__ wv, uint32_t i, const WtRay &r, float tmin,
+                                            float tmax, float* tOut, float* b1Out, float* b2Out, uint32_t* prim) {
+    const float4 p0 = __ldg(wv + 3 * (size_t)i), p1 = __ldg(wv + 3 * (size_t)i + 1), p2 = __ldg(wv + 3 * (size_t)i + 2);
+    const V3 A = V3{p0.x, p0.y, p0.z} - r.org, B = V3{p1.x, p1.y, p1.z} - r.org, C = V3{p2.x, p2.y, p2.z} - r.org;
+    const float Az = comp(A, r.kz), Bz = comp(B, r.kz), Cz = comp(C, r.kz);
+    const float Ax = comp(A, r.kx) - r.sx * Az, Ay = comp(A, r.ky) - r.sy * Az;
+    const float Bx = comp(B, r.kx) - r.sx * Bz, By = comp(B, r.ky) - r.sy * Bz;
+    const float Cx = comp(C, r.kx) - r.sx * Cz, Cy = comp(C, r.ky) - r.sy * Cz;
+    // Each product rounded on its own (no fused multiply-add): the edge
+    // function of an edge shared by two triangles must come out exactly
+    // negated in the neighbour, which a contraction would break.
+    float U = __fsub_rn(__fmul_rn(Cx, By), __fmul_rn(Cy, Bx));
+    float V = __fsub_rn(__fmul_rn(Ax, Cy), __fmul_rn(Ay, Cx));
+    float W = __fsub_rn(__fmul_rn(Bx, Ay), __fmul_rn(By, Ax));
+    if (U == 0.0f || V == 0.0f || W == 0.0f) {
+        U = (float)__dsub_rn(__dmul_rn(Cx, By), __dmul_rn(Cy, Bx));
+        V = (float)__dsub_rn(__dmul_rn(Ax, Cy), __dmul_rn(Ay, Cx));
+        W = (float)__dsub_rn(__dmul_rn(Bx, Ay), __dmul_rn(By, Ax));
+    }
+    if ((U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f)) return false;
+    const float det = U + V + W;
+    if (det == 0.0f) return false;
+    const float T = U * (r.sz * Az) + V * (r.sz * Bz) + W * (r.sz * Cz);
+    const float inv = 1.0f / det;
+    const float t = T * inv;
+    if (!(t >= tmin && t <= tmax)) return false;
+    *tOut = t;
+    *b1Out = V * inv;
+    *b2Out = W * inv;
+    *prim = __float_as_uint(p0.w);
+    return true;
+}
+
 // Slab test; returns the entry distance (dist0) or +inf when rejected.
+// `robust` widens each slab's exit distance by 1 + 2 gamma_3 (Ize, "Robust
+// BVH Ray Traversal", JCGT 2013) so that rounding cannot reject a box the
+// ray only grazes at a face, edge or corner; the watertight triangle test
+// needs it, the reference's arithmetic does not have it.
 __device__ __forceinline__ float slabTest(float lox, float hix, float loy, float hiy, float loz, float hiz,
-                                          V3 org, V3 inv, float tmin, float tmax) {
+                                          V3 org, V3 inv, float tmin, float tmax, bool robust = false) {
+    const float widen = robust ? 1.0000008f : 1.0f;
     float d0 = tmin, d1 = tmax;
     float tn = __fmul_rn(__fsub_rn(lox, org.x), inv.x), tf = __fmul_rn(__fsub_rn(hix, org.x), inv.x);
     if (tn > tf) { float s = tn; tn = tf; tf = s; }
+    tf = __fmul_rn(tf, widen);
     d0 = tn > d0 ? tn : d0;
     d1 = tf < d1 ? tf : d1;
     tn = __fmul_rn(__fsub_rn(loy, org.y), inv.y); tf = __fmul_rn(__fsub_rn(hiy, org.y), inv.y);
     if (tn > tf) { float s = tn; tn = tf; tf = s; }
+    tf = __fmul_rn(tf, widen);
     d0 = tn > d0 ? tn : d0;
     d1 = tf < d1 ? tf : d1;
     tn = __fmul_rn(__fsub_rn(loz, org.z), inv.z); tf = __fmul_rn(__fsub_rn(hiz, org.z), inv.z);
     if (tn > tf) { float s = tn; tn = tf; tf = s; }
+    tf = __fmul_rn(tf, widen);
     d0 = tn > d0 ? tn : d0;
     d1 = tf < d1 ? tf : d1;
     return (d0 > d1) ? __int_as_float(0x7f800000) : d0;
@@ -70,7 +146,8 @@ struct StackEntry {
 
 // Box test of the 4 children of a node; returns the hit mask and entry distances.
 __device__ __forceinline__ uint32_t testChildren(const BvhNode4* __restrict__ nodes, uint32_t ni, V3 org, V3 inv,
-                                                 float tmin, float tmax, float tn[4], uint32_t ch[4]) {
+                                                 float tmin, float tmax, float tn[4], uint32_t ch[4],
+                                                 bool robust = false) {
     const float4* np = reinterpret_cast<const float4*>(nodes + ni);
     float4 lx = __ldg(np + 0), hx = __ldg(np + 1), ly = __ldg(np + 2), hy = __ldg(np + 3);
     float4 lz = __ldg(np + 4), hz = __ldg(np + 5);
@@ -82,7 +159,7 @@ __device__ __forceinline__ uint32_t testChildren(const BvhNode4* __restrict__ no
     float lza[4] = {lz.x, lz.y, lz.z, lz.w}, hza[4] = {hz.x, hz.y, hz.z, hz.w};
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
-        tn[k] = slabTest(lxa[k], hxa[k], lya[k], hya[k], lza[k], hza[k], org, inv, tmin, tmax);
+        tn[k] = slabTest(lxa[k], hxa[k], lya[k], hya[k], lza[k], hza[k], org, inv, tmin, tmax, robust);
         if (ch[k] != kChildEmpty && tn[k] != __int_as_float(0x7f800000)) mask |= 1u << k;
     }
     return mask;
@@ -105,6 +182,8 @@ __device__ __forceinline__ bool traceClosest(const DevScene &sc, V3 org, V3 dir,
     hit->t = __int_as_float(0x7f800000);
     hit->b1 = hit->b2 = 0.0f;
     V3 inv = V3{__fdiv_rn(1.0f, dir.x), __fdiv_rn(1.0f, dir.y), __fdiv_rn(1.0f, dir.z)};
+    WtRay wr;
+    if (sc.watertight) wr = wtSetup(org, dir);
     StackEntry stack[kTraceStack];
     int sp = 0;
     uint32_t cur = 0;
@@ -114,7 +193,7 @@ __device__ __forceinline__ bool traceClosest(const DevScene &sc, V3 org, V3 dir,
         if (!(cur & kLeafBit)) {
             float tn[4];
             uint32_t ch[4];
-            uint32_t mask = testChildren(sc.nodes, cur, org, inv, tmin, tmax, tn, ch);
+            uint32_t mask = testChildren(sc.nodes, cur, org, inv, tmin, tmax, tn, ch, sc.watertight != 0);
             // Order hit children near to far; visit the nearest next and push the rest.
             uint32_t order[4];
             int n = 0;
@@ -139,14 +218,22 @@ __device__ __forceinline__ bool traceClosest(const DevScene &sc, V3 org, V3 dir,
             uint32_t first = cur & kLeafFirstMask;
             uint32_t count = ((cur >> kLeafCountShift) & 0x1f) + 1;
             for (uint32_t i = 0; i < count; ++i) {
-                TriFrag f = loadFrag(sc.frags, first + i);
                 float t, b1, b2;
-                if (mtIntersect(f, org, dir, tmin, tmax, &t, &b1, &b2)) {
+                uint32_t prim;
+                bool h;
+                if (sc.watertight) {
+                    h = wtIntersect(sc.wtVerts, first + i, wr, tmin, tmax, &t, &b1, &b2, &prim);
+                } else {
+                    TriFrag f = loadFrag(sc.frags, first + i);
+                    h = mtIntersect(f, org, dir, tmin, tmax, &t, &b1, &b2);
+                    prim = f.prim;
+                }
+                if (h) {
                     tmax = t;
                     hit->t = t;
                     hit->b1 = b1;
                     hit->b2 = b2;
-                    hit->prim = f.prim;
+                    hit->prim = prim;
                 }
             }
         }
@@ -163,6 +250,8 @@ __device__ __forceinline__ bool traceClosest(const DevScene &sc, V3 org, V3 dir,
 __device__ __forceinline__ bool traceAny(const DevScene &sc, V3 org, V3 dir, float tmin, float tmax) {
     if (sc.numPrims == 0) return false;
     V3 inv = V3{__fdiv_rn(1.0f, dir.x), __fdiv_rn(1.0f, dir.y), __fdiv_rn(1.0f, dir.z)};
+    WtRay wr;
+    if (sc.watertight) wr = wtSetup(org, dir);
     uint32_t stack[kTraceStack];
     int sp = 0;
     uint32_t cur = 0;
@@ -170,7 +259,7 @@ __device__ __forceinline__ bool traceAny(const DevScene &sc, V3 org, V3 dir, flo
         if (!(cur & kLeafBit)) {
             float tn[4];
             uint32_t ch[4];
-            uint32_t mask = testChildren(sc.nodes, cur, org, inv, tmin, tmax, tn, ch);
+            uint32_t mask = testChildren(sc.nodes, cur, org, inv, tmin, tmax, tn, ch, sc.watertight != 0);
             bool have = false;
             uint32_t next = 0;
 #pragma unroll
@@ -185,9 +274,14 @@ __device__ __forceinline__ bool traceAny(const DevScene &sc, V3 org, V3 dir, flo
             uint32_t first = cur & kLeafFirstMask;
             uint32_t count = ((cur >> kLeafCountShift) & 0x1f) + 1;
             for (uint32_t i = 0; i < count; ++i) {
-                TriFrag f = loadFrag(sc.frags, first + i);
                 float t, b1, b2;
-                if (mtIntersect(f, org, dir, tmin, tmax, &t, &b1, &b2)) return true;
+                if (sc.watertight) {
+                    uint32_t prim;
+                    if (wtIntersect(sc.wtVerts, first + i, wr, tmin, tmax, &t, &b1, &b2, &prim)) return true;
+                } else {
+                    TriFrag f = loadFrag(sc.frags, first + i);
+                    if (mtIntersect(f, org, dir, tmin, tmax, &t, &b1, &b2)) return true;
+                }
             }
         }
         if (sp == 0) return false;

@@ -1325,6 +1325,20 @@ int uploadScene(const HostScene &hs, const BuiltScene &bs, DeviceScene* ds) {
 #define UP(vec, field) if ((rc = upload(db, vec, &sc.field)) != SLRGPU_OK) return rc
     UP(bs.wide.nodes, nodes);
     UP(bs.wide.frags, frags);
+    {
+        // Vertices of every fragment as given, for the watertight test.
+        std::vector<float4> wv(3 * bs.wide.frags.size());
+        for (size_t i = 0; i < bs.wide.frags.size(); ++i) {
+            const uint32_t prim = bs.wide.frags[i].prim;
+            const DevPrim &pr = bs.prims[prim];
+            const float4 a = bs.vpos[pr.v0], b = bs.vpos[pr.v1], c = bs.vpos[pr.v2];
+            wv[3 * i] = float4{a.x, a.y, a.z, 0.0f};
+            std::memcpy(&wv[3 * i].w, &prim, sizeof(prim));
+            wv[3 * i + 1] = float4{b.x, b.y, b.z, 0.0f};
+            wv[3 * i + 2] = float4{c.x, c.y, c.z, 0.0f};
+        }
+        UP(wv, wtVerts);
+    }
     UP(bs.prims, prims);
     UP(bs.vpos, vpos);
     UP(bs.vnrm, vnrm);
@@ -1501,6 +1515,11 @@ struct LaunchMarks {
 
 // Sample grid and wave size of a render: every position of the tile-padded
 // grid is one path per sample index; a wave holds S sample indices.
+// Paths in flight per wave when samples_per_wave is 0 (a tuned constant).
+#ifndef SLRGPU_WAVE_PATHS
+#define SLRGPU_WAVE_PATHS (4u << 20)
+#endif
+
 struct WavePlan {
     uint32_t gridW, gridH, gridPositions, filmPixels, S;
 };
@@ -1520,8 +1539,11 @@ static WavePlan planWaves(const slrgpu_settings &s, uint32_t autoPaths) {
 // bounce the extension, shading and shadow kernels over the device-side
 // queues, then the film update of every segment.  Stream-ordered; counters,
 // queues and path state live in w.  Returns the number of kernel launches.
-static uint64_t runWave(const DeviceScene &ds, const WaveState &w, const WaveParams &wp, uint32_t D, bool volumetric,
-                        cudaStream_t stream, LaunchMarks &lm, const WaveParams* wpDev = nullptr) {
+static uint64_t runWave(const DeviceScene &ds0, const WaveState &w, const WaveParams &wp, uint32_t D, bool volumetric,
+                        bool watertight, cudaStream_t stream, LaunchMarks &lm, const WaveParams* wpDev = nullptr) {
+    // the scene as the kernels see it, with the triangle test chosen
+    struct { DevScene sc; uint32_t kindMask; } ds{ds0.sc, ds0.kindMask};
+    ds.sc.watertight = watertight ? 1u : 0u;
     const int block = 256;
     const WaveGrids &g = waveGrids(block);
     uint64_t launches = 0;
@@ -1634,7 +1656,8 @@ static uint64_t runWaves(const DeviceScene &ds, const slrgpu_settings &s, const 
         wp.numSegments = 1;
         wp.numPaths = sg.samples * pl.gridPositions;
         wp.filmPixels = s.width * s.height;
-        launches += runWave(ds, w, wp, s.max_depth, s.volumetric != 0, stream, lm);
+        launches += runWave(ds, w, wp, s.max_depth, s.volumetric != 0, (s.flags & SLRGPU_FLAG_WATERTIGHT) != 0,
+                            stream, lm);
     }
     return launches;
 }
@@ -1654,7 +1677,7 @@ int RenderEngine::render(const DeviceScene &ds, const slrgpu_settings &s, float*
         setError("image too large");
         return SLRGPU_ERR_INVALID_ARGUMENT;
     }
-    const WavePlan pl = planWaves(s, 4u << 20);
+    const WavePlan pl = planWaves(s, SLRGPU_WAVE_PATHS);
     const uint32_t P = pl.filmPixels;
     const uint64_t Nwant = (uint64_t)pl.S * pl.gridPositions;
     if (Nwant > 0x7fffffffull) {
@@ -1964,6 +1987,7 @@ struct WaveSlot {
         uint64_t sceneUid;
         uint32_t depth;
         bool volumetric;
+        bool watertight;
         cudaGraphExec_t exec;
         uint64_t launches;
     };
@@ -1994,7 +2018,7 @@ uint32_t waveSlotCapacity(const WaveSlot* slot) { return slot->engine.capacity; 
 uint32_t sampleGridPositions(uint32_t width, uint32_t height) { return padToTile(width) * padToTile(height); }
 
 int launchWave(const DeviceScene &ds, WaveSlot* slot, const SegmentDesc* segs, int numSegs, uint32_t maxDepth,
-               bool volumetric, cudaStream_t stream, uint64_t* launches, bool useGraph) {
+               bool volumetric, bool watertight, cudaStream_t stream, uint64_t* launches, bool useGraph) {
     if (numSegs <= 0 || numSegs > kMaxWaveSegments) {
         setError("a wave holds 1 to 32 segments");
         return SLRGPU_ERR_INVALID_ARGUMENT;
@@ -2034,14 +2058,15 @@ int launchWave(const DeviceScene &ds, WaveSlot* slot, const SegmentDesc* segs, i
     wp.filmPixels = (uint32_t)pixels;
     if (!useGraph) {
         LaunchMarks lm;
-        uint64_t n = runWave(ds, *slot->engine.ws, wp, maxDepth, volumetric, stream, lm);
+        uint64_t n = runWave(ds, *slot->engine.ws, wp, maxDepth, volumetric, watertight, stream, lm);
         if (launches) *launches += n;
         CUDA_TRY(cudaGetLastError());
         return SLRGPU_OK;
     }
     WaveSlot::Graph* graph = nullptr;
     for (WaveSlot::Graph &g : slot->graphs)
-        if (g.sceneUid == ds.uid && g.depth == maxDepth && g.volumetric == volumetric) graph = &g;
+        if (g.sceneUid == ds.uid && g.depth == maxDepth && g.volumetric == volumetric && g.watertight == watertight)
+            graph = &g;
     if (!graph) {
         waveGrids(256);   // occupancy queries stay outside the capture
         // Capture on this stream: the launches read their segments from
@@ -2051,7 +2076,8 @@ int launchWave(const DeviceScene &ds, WaveSlot* slot, const SegmentDesc* segs, i
         LaunchMarks lm;
         cudaGraph_t g = nullptr;
         CUDA_TRY(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
-        uint64_t n = runWave(ds, *slot->engine.ws, empty, maxDepth, volumetric, stream, lm, slot->dParams);
+        uint64_t n = runWave(ds, *slot->engine.ws, empty, maxDepth, volumetric, watertight, stream, lm,
+                             slot->dParams);
         cudaError_t e = cudaStreamEndCapture(stream, &g);
         if (e != cudaSuccess) {
             setError(std::string("wave capture failed: ") + cudaGetErrorString(e));
@@ -2064,7 +2090,7 @@ int launchWave(const DeviceScene &ds, WaveSlot* slot, const SegmentDesc* segs, i
             setError(std::string("wave graph instantiation failed: ") + cudaGetErrorString(e));
             return SLRGPU_ERR_CUDA;
         }
-        slot->graphs.push_back(WaveSlot::Graph{ds.uid, maxDepth, volumetric, exec, n});
+        slot->graphs.push_back(WaveSlot::Graph{ds.uid, maxDepth, volumetric, watertight, exec, n});
         graph = &slot->graphs.back();
     }
     // The previous wave on this slot has completed (the caller waits for it),
@@ -2162,7 +2188,9 @@ int traceRays(const DeviceScene &ds, const float* rays, uint32_t n, int anyHit, 
     if (n == 0) return SLRGPU_OK;
     static int grid = 0;
     if (!grid) grid = gridFor((const void*)kTrace, 256);
-    kTrace<<<grid, 256, 0, stream>>>(ds.sc, rays, n, anyHit, prim, t, b1, b2);
+    DevScene sc = ds.sc;
+    sc.watertight = (anyHit & 2) ? 1u : 0u;
+    kTrace<<<grid, 256, 0, stream>>>(sc, rays, n, anyHit & 1, prim, t, b1, b2);
     CUDA_TRY(cudaGetLastError());
     return SLRGPU_OK;
 }

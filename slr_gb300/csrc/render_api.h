@@ -67,7 +67,7 @@ uint32_t sampleGridPositions(uint32_t width, uint32_t height);
 // useGraph: replay the slot's captured graph for this (scene, depth,
 // integrator), capturing it on first use.
 int launchWave(const DeviceScene &ds, WaveSlot* slot, const SegmentDesc* segs, int numSegs, uint32_t maxDepth,
-               bool volumetric, cudaStream_t stream, uint64_t* launches, bool useGraph);
+               bool volumetric, bool watertight, cudaStream_t stream, uint64_t* launches, bool useGraph);
 int launchFilmToPixelMajor(const float* filmSum, float* out, uint32_t pixels, cudaStream_t stream);
 
 // Film -> 8-bit sRGB BMP pixel rows (bottom-up BGR, rows padded to 4 bytes).

@@ -297,7 +297,8 @@ bool Server::launchWaves() {
             if ((int)segs.size() == kMaxSegmentsPerWave) break;
             if (r->samplesIssued >= r->settings.spp) continue;
             if (r->ds != lead->ds || r->settings.volumetric != lead->settings.volumetric ||
-                r->settings.max_depth != lead->settings.max_depth)
+                r->settings.max_depth != lead->settings.max_depth ||
+                (r->settings.flags & SLRGPU_FLAG_WATERTIGHT) != (lead->settings.flags & SLRGPU_FLAG_WATERTIGHT))
                 continue;
             if (cfg_.mode == SLRGPU_SERVER_PLAIN && r != lead) continue;
             uint64_t room = (cap - paths) / r->gridPositions;
@@ -321,7 +322,8 @@ bool Server::launchWaves() {
         if (segs.empty()) break;
         uint64_t n = 0;
         int rc = launchWave(*lead->ds, sl.wave, segs.data(), (int)segs.size(), lead->settings.max_depth,
-                            lead->settings.volumetric != 0, sl.stream, &n, cfg_.mode == SLRGPU_SERVER_BATCHED);
+                            lead->settings.volumetric != 0, (lead->settings.flags & SLRGPU_FLAG_WATERTIGHT) != 0,
+                            sl.stream, &n, cfg_.mode == SLRGPU_SERVER_BATCHED);
         if (rc != SLRGPU_OK) {
             for (auto &pr : sl.segments) failRequest(pr.first, "wave launch failed");
             sl.segments.clear();

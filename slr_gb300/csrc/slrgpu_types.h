@@ -127,6 +127,8 @@ struct DevScene {
     // geometry / traversal
     const BvhNode4* nodes;
     const TriFrag* frags;
+    const float4* wtVerts;  // per fragment: v0 (w = prim id bits), v1, v2 as given (watertight test)
+    uint32_t watertight;    // 1: watertight triangle test instead of the reference's
     const DevPrim* prims;
     const float4* vpos;     // xyz, u
     const float4* vnrm;     // xyz, v

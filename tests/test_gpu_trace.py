@@ -87,3 +87,81 @@ def test_trace_empty_batch_and_empty_scene(gpu_lib):
     rays = torch.tensor([[0, 0, 0, 0, 0, 0, 1, float("inf")]], device="cuda")
     prim, t, _, _ = e.trace(rays)
     assert int(prim.cpu().numpy().view(np.uint32)[0]) == 0xffffffff
+
+
+def _edge_rays(P, T, origins):
+    """Rays from each origin through every vertex and every edge midpoint of
+    the mesh (P, T): exactly the points a non-watertight test can slip
+    through."""
+    targets = [P]
+    for a, b in ((0, 1), (1, 2), (2, 0)):
+        targets.append(0.5 * (P[T[:, a]] + P[T[:, b]]))
+    targets = np.concatenate(targets)
+    rays = []
+    for o in origins:
+        d = targets - o
+        d /= np.linalg.norm(d, axis=1, keepdims=True)
+        r = np.zeros((len(d), 8), np.float32)
+        r[:, 0:3] = o
+        r[:, 4:7] = d
+        r[:, 7] = np.inf
+        rays.append(r)
+    return np.concatenate(rays)
+
+
+def test_watertight_closed_mesh_has_no_leaks(gpu_lib):
+    """A closed geodesic sphere, rays from inside through every vertex and
+    edge midpoint: the watertight test hits on every ray (the reference's
+    Moller-Trumbore test may let some through; counted, not required)."""
+    import torch
+    from slr_gb300.scene_desc import REFLECTANCE, SceneDesc
+    P, T = scenes.geodesic_sphere(12)          # closed: every edge shared by two triangles
+    P = P.astype(np.float32) * np.float32(0.73)
+    d = SceneDesc()
+    m = d.material("matte", (d.spectrum_rgb(REFLECTANCE, 0.5, 0.5, 0.5),))
+    d.mesh(P, T, m)
+    rng = np.random.default_rng(4)
+    origins = [np.zeros(3)] + list(rng.uniform(-0.3, 0.3, (5, 3)))
+    rays = _edge_rays(P.astype(np.float64), T, origins)
+    s = gpu_lib.Scene(d)
+    r = torch.from_numpy(rays).cuda()
+    wt, _, _, _ = s.trace(r, watertight=True)
+    mt, _, _, _ = s.trace(r)
+    torch.cuda.synchronize()
+    wt = wt.cpu().numpy().view(np.uint32)
+    mt = mt.cpu().numpy().view(np.uint32)
+    assert (wt != 0xffffffff).all(), int((wt == 0xffffffff).sum())
+    assert len(rays) > 20000
+    print("reference-order test misses:", int((mt == 0xffffffff).sum()), "of", len(rays))
+
+
+def test_watertight_agrees_with_reference_away_from_edges(gpu_lib, oracle_lib):
+    """Random rays: the watertight test finds the reference's primitive
+    except where the hit lies within rounding of an edge or vertex (smallest
+    barycentric weight below 1e-5) or at an exact tie."""
+    import torch
+    desc = scenes.heightfield_scene(grid=96, spheres=6, sphere_freq=6, env_size=(16, 8))
+    rays = helpers.random_rays(desc, 60000, seed=31)
+    s = gpu_lib.Scene(desc)
+    r = torch.from_numpy(rays).cuda()
+    prim, t, b1, b2 = s.trace(r, watertight=True)
+    occ, _, _, _ = s.trace(r, any_hit=True, watertight=True)
+    torch.cuda.synchronize()
+    prim = prim.cpu().numpy().view(np.uint32)
+    t = t.cpu().numpy()
+    ref = oracle_lib.RefScene(desc, build=False)
+    rp, rt, rb1, rb2 = ref.trace(rays)
+    ro, _, _, _ = ref.trace(rays, anyhit=True)
+    diff = np.nonzero(prim != rp)[0]
+    wmin = np.minimum(np.minimum(rb1, rb2), 1 - rb1 - rb2)
+    near_edge = (rp[diff] != 0xffffffff) & (wmin[diff] < 1e-5)
+    tie = (prim[diff] != 0xffffffff) & (rp[diff] != 0xffffffff) & (np.abs(t[diff] - rt[diff]) <= 1e-6 * np.abs(rt[diff]))
+    unexplained = diff[~(near_edge | tie)]
+    assert len(unexplained) == 0, (len(diff), unexplained[:10])
+    assert len(diff) <= 1e-3 * len(rays)
+    same = prim == rp
+    hit = same & (rp != 0xffffffff)
+    # same triangle: t from a different formula, equal to float rounding
+    # (relative 1e-5, plus 1e-6 absolute for the hits just past tmin)
+    assert np.all(np.abs(t[hit] - rt[hit]) <= 1e-5 * np.abs(rt[hit]) + 1e-6)
+    assert (occ.cpu().numpy().astype(bool) != ro).mean() <= 1e-3
