@@ -354,6 +354,13 @@ int slrgpu_spectrum_evaluate(slrgpu_handle scene, int id, const float* lambdas, 
  * (adjacency bits, s, t, scale) of its upsampled spectrum. */
 int slrgpu_environment_tables(slrgpu_handle scene, uint32_t* map_w, uint32_t* map_h, float* row_pdf, float* row_cdf,
                               float* top_pdf, float* top_cdf, float* texel_params);
+/* The alias tables the GPU samples lights and the environment with (Vose;
+ * bin i is kept with probability prob[i], else alias[i] is taken), built
+ * from the CDFs above, so they carry the same PMFs: surface lights
+ * (num_lights entries), the environment's rows (map_h) and the bins of each
+ * row (map_h x map_w).  Host only; any output may be NULL. */
+int slrgpu_scene_alias_tables(slrgpu_handle scene, uint32_t* num_lights, float* light_prob, uint32_t* light_alias,
+                              float* top_prob, uint32_t* top_alias, float* row_prob, uint32_t* row_alias);
 
 #ifdef __cplusplus
 }

@@ -150,6 +150,7 @@ def lib():
             "slrgpu_server_get_stats": (I, [H, C.POINTER(ServerStats)]),
             "slrgpu_film_to_bmp": (I, [fp, U, U, I, F, F, C.POINTER(C.c_uint8), C.c_char_p]),
             "slrgpu_film_cmf": (I, [fp, fp]),
+            "slrgpu_scene_alias_tables": (I, [H, up, fp, up, fp, up, fp, up]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -399,6 +400,27 @@ class Scene:
         out = np.zeros((len(r), 24), np.float32)
         check(lib().slrgpu_medium_query(self.handle, int(mode), len(r), _fp(r), _fp(lam),
                                         sl.ctypes.data_as(C.POINTER(C.c_int)), _up(v), v.shape[1], _fp(out)))
+        return out
+
+    def alias_tables(self):
+        """Alias tables of the light and environment sampling (host build):
+        dict of (prob, alias) pairs for 'lights', 'top' (rows), 'rows'."""
+        n = C.c_uint32()
+        check(lib().slrgpu_scene_alias_tables(self.handle, C.byref(n), None, None, None, None, None, None))
+        out = {}
+        lp, la = np.zeros(n.value, np.float32), np.zeros(n.value, np.uint32)
+        args = [_fp(lp), _up(la)]
+        if self.desc.environment is not None:
+            h, w = self.desc.environment.rgba_half.shape[:2]
+            mw, mh = w // 4, h // 4
+            tp, ta = np.zeros(mh, np.float32), np.zeros(mh, np.uint32)
+            rp, ra = np.zeros((mh, mw), np.float32), np.zeros((mh, mw), np.uint32)
+            args += [_fp(tp), _up(ta), _fp(rp), _up(ra)]
+            out["top"], out["rows"] = (tp, ta), (rp, ra)
+        else:
+            args += [None, None, None, None]
+        check(lib().slrgpu_scene_alias_tables(self.handle, None, *args))
+        out["lights"] = (lp, la)
         return out
 
     def environment_tables(self):

@@ -640,4 +640,23 @@ int slrgpu_environment_tables(slrgpu_handle scene, uint32_t* map_w, uint32_t* ma
     return SLRGPU_OK;
 }
 
+int slrgpu_scene_alias_tables(slrgpu_handle scene, uint32_t* num_lights, float* light_prob, uint32_t* light_alias,
+                              float* top_prob, uint32_t* top_alias, float* row_prob, uint32_t* row_alias) {
+    const bool mutating = false;
+    GET_SCENE(s, scene);
+    int rc = ensureHostBuilt(s);
+    if (rc != SLRGPU_OK) return rc;
+    auto split = [](const std::vector<AliasEntry> &t, float* prob, uint32_t* alias) {
+        for (size_t i = 0; i < t.size(); ++i) {
+            if (prob) prob[i] = t[i].prob;
+            if (alias) alias[i] = t[i].alias;
+        }
+    };
+    if (num_lights) *num_lights = (uint32_t)s->built.lightAlias.size();
+    split(s->built.lightAlias, light_prob, light_alias);
+    split(s->built.env.topAlias, top_prob, top_alias);
+    split(s->built.env.rowAlias, row_prob, row_alias);
+    return SLRGPU_OK;
+}
+
 }  // extern "C"

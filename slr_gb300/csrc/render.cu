@@ -204,15 +204,33 @@ __device__ __forceinline__ uint32_t prevPow2(uint32_t x) {
     x |= x >> 1; x |= x >> 2; x |= x >> 4; x |= x >> 8; x |= x >> 16;
     return x - (x >> 1);
 }
-__device__ __forceinline__ float sample1D(const float* pdf, const float* cdf, uint32_t n, float u, float* outPdf) {
-    int idx = (int)n;
-    for (int d = (int)prevPow2(n); d > 0; d >>= 1)
-        if (idx - d > 0 && cdf[idx - d] >= u) idx -= d;
-    --idx;
-    *outPdf = pdf[idx];
-    float t = (u - cdf[idx]) / (cdf[idx + 1] - cdf[idx]);
-    return (idx + t) / n;
+// Alias-table sampling (Vose; O(1) instead of the CDF's binary search) of a
+// piecewise-constant distribution over [0, 1) with n bins: the bin is the
+// alias pick of u, the position inside it the leftover fraction of u
+// rescaled to [0, 1), the density that of the bin.  The tables hold the
+// PMF of the reference's CDFs, so the sampled distribution is the same.
+__device__ __forceinline__ uint32_t aliasPick(const AliasEntry* __restrict__ t, uint32_t n, float u, float* frac) {
+    const float x = u * (float)n;
+    const uint32_t i = min((uint32_t)x, n - 1);
+    const float f = fminf(x - (float)i, 0x1.fffffep-1f);
+    const AliasEntry e = t[i];
+    if (f < e.prob) {
+        *frac = f / e.prob;
+        return i;
+    }
+    *frac = (f - e.prob) / (1.0f - e.prob);
+    return e.alias;
 }
+
+__device__ __forceinline__ float sampleAlias(const AliasEntry* __restrict__ t, const float* __restrict__ pdf, uint32_t n,
+                                             float u, float* outPdf, uint32_t* bin) {
+    float frac;
+    const uint32_t k = aliasPick(t, n, u, &frac);
+    *outPdf = pdf[k];
+    *bin = k;
+    return fminf(((float)k + fminf(frac, 0x1.fffffep-1f)) / (float)n, 0x1.fffffep-1f);
+}
+
 
 __device__ __forceinline__ float envUVPdf(const DevScene &sc, float d0, float d1) {
     uint32_t row = min((uint32_t)(sc.envMapH * d1), sc.envMapH - 1);
@@ -368,10 +386,8 @@ __device__ __forceinline__ void surfacePoint(const DevScene &sc, const DevPrim &
 // -1 for the environment, else the light index; *prob = selection probability.
 __device__ __forceinline__ int selectLight(const DevScene &sc, float u, float* prob) {
     auto surf = [&](float uu, float* pr) -> int {
-        int idx = (int)sc.numLights;
-        for (int d = (int)prevPow2(sc.numLights); d > 0; d >>= 1)
-            if (idx - d > 0 && sc.lightCDF[idx - d] >= uu) idx -= d;
-        --idx;
+        float frac;
+        const int idx = (int)aliasPick(sc.lightAlias, sc.numLights, uu, &frac);
         *pr = sc.lightPMF[idx];
         return idx;
     };
@@ -575,10 +591,10 @@ __global__ void __launch_bounds__(256, SLRGPU_SHADE_MIN_BLOCKS) kShadeSurf(DevSc
                         edfVal = dot(lz, -shadowDir) > 0.0f ? kInvPiF : 0.0f;
                     } else {
                         float uvPdf, topPdf;
-                        float d1 = sample1D(sc.envTopPDF, sc.envTopCDF, sc.envMapH, lu1, &topPdf);
-                        uint32_t row = min((uint32_t)(sc.envMapH * d1), sc.envMapH - 1);
-                        float d0 = sample1D(sc.envRowPDF + (size_t)row * sc.envMapW,
-                                            sc.envRowCDF + (size_t)row * (sc.envMapW + 1), sc.envMapW, lu0, &uvPdf);
+                        uint32_t row, col;
+                        float d1 = sampleAlias(sc.envTopAlias, sc.envTopPDF, sc.envMapH, lu1, &topPdf, &row);
+                        float d0 = sampleAlias(sc.envRowAlias + (size_t)row * sc.envMapW,
+                                               sc.envRowPDF + (size_t)row * sc.envMapW, sc.envMapW, lu0, &uvPdf, &col);
                         uvPdf *= topPdf;
                         float phi = d0 * twoPi, theta = d1 * kPiF;
                         float sph, cph, sth, cth;
@@ -700,11 +716,8 @@ __device__ __forceinline__ int selectLight3(const DevScene &sc, float u, int* li
         }
     }
     if (idx == 0) {
-        int n = (int)sc.numLights;
-        int j = n;
-        for (int d = (int)prevPow2(sc.numLights); d > 0; d >>= 1)
-            if (j - d > 0 && sc.lightCDF[j - d] >= remapped) j -= d;
-        --j;
+        float frac;
+        const int j = (int)aliasPick(sc.lightAlias, sc.numLights, remapped, &frac);
         *li = j;
         *prob = sc.lightPMF[j] * prob1st;
     } else {
@@ -892,10 +905,10 @@ __global__ void __launch_bounds__(256, SLRGPU_SHADEVOL_MIN_BLOCKS) kShadeVol(Dev
                         edfVal = dot(lz, -shadowDir) > 0.0f ? kInvPiF : 0.0f;
                     } else {
                         float uvPdf, topPdf;
-                        float d1 = sample1D(sc.envTopPDF, sc.envTopCDF, sc.envMapH, lu1, &topPdf);
-                        uint32_t row = min((uint32_t)(sc.envMapH * d1), sc.envMapH - 1);
-                        float d0 = sample1D(sc.envRowPDF + (size_t)row * sc.envMapW,
-                                            sc.envRowCDF + (size_t)row * (sc.envMapW + 1), sc.envMapW, lu0, &uvPdf);
+                        uint32_t row, col;
+                        float d1 = sampleAlias(sc.envTopAlias, sc.envTopPDF, sc.envMapH, lu1, &topPdf, &row);
+                        float d0 = sampleAlias(sc.envRowAlias + (size_t)row * sc.envMapW,
+                                               sc.envRowPDF + (size_t)row * sc.envMapW, sc.envMapW, lu0, &uvPdf, &col);
                         uvPdf *= topPdf;
                         float phi = d0 * twoPi, theta = d1 * kPiF;
                         float sph, cph, sth, cth;
@@ -1355,6 +1368,7 @@ int uploadScene(const HostScene &hs, const BuiltScene &bs, DeviceScene* ds) {
     UP(ups, upsSpectra);
     UP(bs.lightPrims, lightPrims);
     UP(bs.lightCDF, lightCDF);
+    UP(bs.lightAlias, lightAlias);
     UP(bs.lightPMF, lightPMF);
     if (hs.envPresent) {
         UP(bs.env.texels, envTexels);
@@ -1362,6 +1376,8 @@ int uploadScene(const HostScene &hs, const BuiltScene &bs, DeviceScene* ds) {
         UP(bs.env.rowCDF, envRowCDF);
         UP(bs.env.topPDF, envTopPDF);
         UP(bs.env.topCDF, envTopCDF);
+        UP(bs.env.rowAlias, envRowAlias);
+        UP(bs.env.topAlias, envTopAlias);
     }
     if (hs.medium.present) {
         DevMedium &m = sc.medium;

@@ -354,6 +354,35 @@ void build1D(const std::vector<float> &vals, float* pdf, float* cdf, float* inte
 }
 }  // namespace
 
+// Vose's alias method in double precision: the bins' probabilities are the
+// CDF's increments (the PMF the CDF inversion samples), scaled to mean 1;
+// bins below 1 take an alias among those above.
+void buildAlias(const float* cdf, uint32_t n, AliasEntry* out) {
+    std::vector<double> q(n);
+    double total = 0.0;
+    for (uint32_t i = 0; i < n; ++i) {
+        q[i] = std::max(0.0, (double)cdf[i + 1] - (double)cdf[i]);
+        total += q[i];
+    }
+    for (uint32_t i = 0; i < n; ++i) q[i] = total > 0 ? q[i] * n / total : 1.0;
+    std::vector<uint32_t> small, large;
+    for (uint32_t i = 0; i < n; ++i) (q[i] < 1.0 ? small : large).push_back(i);
+    for (uint32_t i = 0; i < n; ++i) out[i] = AliasEntry{1.0f, i};
+    while (!small.empty() && !large.empty()) {
+        uint32_t s = small.back(), l = large.back();
+        small.pop_back();
+        out[s] = AliasEntry{(float)q[s], l};
+        q[l] = (q[l] + q[s]) - 1.0;
+        if (q[l] < 1.0) {
+            large.pop_back();
+            small.push_back(l);
+        }
+    }
+    // leftovers (rounding) keep themselves with probability 1
+    for (uint32_t i : large) out[i] = AliasEntry{1.0f, i};
+    for (uint32_t i : small) out[i] = AliasEntry{1.0f, i};
+}
+
 void buildEnvironment(const uint16_t* rgbaHalf, uint32_t w, uint32_t h, float scale, HostEnvironment* env) {
     env->width = w;
     env->height = h;
@@ -400,6 +429,11 @@ void buildEnvironment(const uint16_t* rgbaHalf, uint32_t w, uint32_t h, float sc
     env->topCDF.assign(mapH + 1, 0.0f);
     float topIntegral;
     build1D(env->rowIntegral, env->topPDF.data(), env->topCDF.data(), &topIntegral);
+    env->rowAlias.resize((size_t)mapW * mapH);
+    for (uint32_t y = 0; y < mapH; ++y)
+        buildAlias(&env->rowCDF[(size_t)y * (mapW + 1)], mapW, &env->rowAlias[(size_t)y * mapW]);
+    env->topAlias.resize(mapH);
+    buildAlias(env->topCDF.data(), mapH, env->topAlias.data());
 }
 
 // ============================================================================
@@ -1302,6 +1336,8 @@ bool buildScene(const HostScene &s, BuiltScene* out, std::string* err) {
         Kahan sum;
         for (uint32_t i = 0; i < nl; ++i) { sum.add(out->lightPMF[i]); out->lightCDF[i + 1] = sum.result; }
         for (uint32_t i = 0; i < nl; ++i) { out->lightPMF[i] /= sum.result; out->lightCDF[i + 1] /= sum.result; }
+        out->lightAlias.resize(nl);
+        buildAlias(out->lightCDF.data(), nl, out->lightAlias.data());
     }
 
     if (s.envPresent) buildEnvironment(s.envRGBA.data(), s.envW, s.envH, s.envScale, &out->env);

@@ -65,9 +65,12 @@ struct HostEnvironment {
     std::vector<EnvTexel> texels;          // row-major
     uint32_t mapW = 0, mapH = 0;
     std::vector<float> rowPDF, rowCDF, rowIntegral, topPDF, topCDF;
+    std::vector<AliasEntry> rowAlias, topAlias;
     float integral = 0.0f;
 };
 void buildEnvironment(const uint16_t* rgbaHalf, uint32_t w, uint32_t h, float scale, HostEnvironment* env);
+// Alias table with the PMF cdf[i + 1] - cdf[i] of the n bins of a CDF.
+void buildAlias(const float* cdf, uint32_t n, AliasEntry* out);
 
 // ---- scene ---------------------------------------------------------------------
 struct HostMesh {
@@ -122,6 +125,7 @@ struct BuiltScene {
     std::vector<float4> vpos, vnrm, vtan;
     std::vector<uint32_t> lightPrims;
     std::vector<float> lightCDF, lightPMF;
+    std::vector<AliasEntry> lightAlias;
     HostEnvironment env;
     DevCamera camera;
     float worldCenter[3], worldRadius, worldDiscArea;

@@ -123,6 +123,13 @@ struct DevMedium {
     float importance;             // emitting media weight (0: none emit)
 };
 
+// Alias table entry (Vose): bin i is kept with probability prob, else its
+// alias is taken; built from a CDF, so the bins keep the CDF's PMF.
+struct AliasEntry {
+    float prob;
+    uint32_t alias;
+};
+
 struct DevScene {
     // geometry / traversal
     const BvhNode4* nodes;
@@ -144,6 +151,7 @@ struct DevScene {
     const uint32_t* lightPrims;
     const float* lightCDF;     // numLights + 1
     const float* lightPMF;     // numLights
+    const AliasEntry* lightAlias;   // numLights
     uint32_t numLights;
     float surfImportance;      // SurfaceObjectAggregate::importance()
     float envImportance;       // 1 when an environment is present, else 0
@@ -157,6 +165,8 @@ struct DevScene {
     const float* envRowCDF;    // [mapH][mapW + 1]
     const float* envTopPDF;    // [mapH]
     const float* envTopCDF;    // [mapH + 1]
+    const AliasEntry* envRowAlias;  // [mapH][mapW]
+    const AliasEntry* envTopAlias;  // [mapH]
     float worldRadius;
     float worldDiscArea;
     float worldCenter[3];

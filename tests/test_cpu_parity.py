@@ -120,3 +120,30 @@ def test_film_colour_matching_bins_bit_exact(gpu_lib, oracle_lib):
     rb, ri = oracle_lib.film_cmf()
     assert np.array_equal(bins.reshape(-1).view(np.uint32), rb.view(np.uint32))
     assert np.float32(integ).view(np.uint32) == np.float32(ri).view(np.uint32)
+
+
+def _alias_pmf(prob, alias):
+    n = len(prob)
+    pmf = prob.astype(np.float64) / n
+    np.add.at(pmf, alias, (1.0 - prob.astype(np.float64)) / n)
+    return pmf
+
+
+def test_alias_tables_carry_the_reference_pmfs(gpu_lib):
+    """The GPU samples lights and the environment with alias tables; the
+    probability each table gives every bin equals the PMF of the CDF the
+    reference inverts (bit-identical CDFs are checked above)."""
+    desc = scenes.heightfield_scene(grid=24, spheres=2, sphere_freq=2, env_size=(64, 32))
+    s = gpu_lib.Scene(desc, host_only=True)
+    tabs = s.alias_tables()
+    env = s.environment_tables()
+    np.testing.assert_allclose(_alias_pmf(*tabs["top"]), np.diff(env["top_cdf"].astype(np.float64)), rtol=1e-5,
+                               atol=1e-7)
+    rows_p, rows_a = tabs["rows"]
+    for y in range(rows_p.shape[0]):
+        np.testing.assert_allclose(_alias_pmf(rows_p[y], rows_a[y]), np.diff(env["row_cdf"][y].astype(np.float64)),
+                                   rtol=1e-5, atol=1e-7)
+    box = gpu_lib.Scene(scenes.box_scene(8, 8), host_only=True)
+    lp, la = box.alias_tables()["lights"]
+    assert len(lp) == 2
+    np.testing.assert_allclose(_alias_pmf(lp, la), [0.5, 0.5])
