@@ -22,6 +22,10 @@ log-normal environment with a 2-degree sun of radiance 5e4) at 1024 x 1024,
 captures (256 x 256 height field, 16 spheres, 512 x 512 pixels, 4 spp); it is
 not a benchmark line.
 
+``--workload bpt_box`` renders the box scene with the bidirectional path
+tracer (BPTRenderer semantics, 16 vertices per subpath) at 512 x 512 and
+16 spp; its CPU baseline is the reference's BPTRenderer.
+
 ``--workload serving`` runs the serving stream (512 requests, Poisson
 arrivals at 20/s, 8 scenes of 1k-2M triangles, half with a medium) through
 the plain and the batched server, as a burst and at the arrival times, and
@@ -49,6 +53,7 @@ WIDTH = HEIGHT = 1024
 SPP = 64
 MAX_DEPTH = 10
 VOLUMETRIC = False
+BPT = False
 METRIC = "path samples/s"
 WORKLOAD = ("ggx_ibl_1m: 1,034,242-triangle height field (512x512, 6-octave improved Perlin, amplitude 0.2) "
             "+ 64 geodesic spheres (8000 triangles, scale log-uniform 0.05-0.3), GGX conductors/dielectrics "
@@ -61,6 +66,18 @@ BYTES_EXTEND = 48
 BYTES_SHADOW = 36
 BYTES_SHADE = 792
 BYTES_FILM = 256
+# Bidirectional tracer: per traced subpath vertex (ray 32 B + state 16 B +
+# throughput 64 B in; vertex record 160 B, throughput 64 B, ray and state
+# 48 B, previous vertex's reverse densities 8 B out; closest hit 48 B) and
+# per connection (light vertex 160 B, its predecessor 64 B, two density
+# records per MIS term ~64 B, shadow query 36 B, contribution 64 B).
+BYTES_BPT_BOUNCE = 440
+BYTES_BPT_CONNECT = 390
+
+# DRAM bytes per unit of the dominant kernel class measured by ncu
+# (dram__bytes_read.sum + dram__bytes_write.sum over the class's launches of
+# the same workload, divided by its units): profiles/dram_ggx_ibl_1m.md.
+MEASURED_DRAM_PER_UNIT = {("ggx_ibl_1m", "shade"): 721.7}
 
 
 def load_peaks():
@@ -140,7 +157,11 @@ def cpu_baseline(desc, threads: int, seconds_target: float = 12.0):
     build_s = time.time() - t0
     total_samples, total_s, frames = 0, 0.0, 0
     while total_s < seconds_target and frames < 16:
-        _, s = ref.render(WIDTH, HEIGHT, 1, MAX_DEPTH, seed=frames, threads=threads, volumetric=VOLUMETRIC)
+        if BPT:   # one BPT render per reference sensor
+            ref = O.RefScene(desc) if frames else ref
+            _, s = ref.render_bpt(WIDTH, HEIGHT, 1, MAX_DEPTH, seed=frames, threads=threads)
+        else:
+            _, s = ref.render(WIDTH, HEIGHT, 1, MAX_DEPTH, seed=frames, threads=threads, volumetric=VOLUMETRIC)
         total_samples += WIDTH * HEIGHT
         total_s += s
         frames += 1
@@ -160,7 +181,11 @@ def run_reference(args):
     ref = O.RefScene(desc)
     times = []
     for i in range(args.warmup + args.steps):
-        _, s = ref.render(WIDTH, HEIGHT, 1, MAX_DEPTH, seed=i, threads=threads, volumetric=VOLUMETRIC)
+        if BPT:   # one BPT render per reference sensor
+            ref = O.RefScene(desc) if i else ref
+            _, s = ref.render_bpt(WIDTH, HEIGHT, 1, MAX_DEPTH, seed=i, threads=threads)
+        else:
+            _, s = ref.render(WIDTH, HEIGHT, 1, MAX_DEPTH, seed=i, threads=threads, volumetric=VOLUMETRIC)
         if i >= args.warmup:
             times.append(s)
     per_step = WIDTH * HEIGHT
@@ -378,6 +403,14 @@ def _workloads():
                     text="box_pt: closed box of 10 triangles + 2 rotated boxes, Lambert walls, 0.25x0.25 ceiling "
                          "light of radiance 15, pinhole, 256x256, 16 spp, max depth 8, seed 0",
                     scene=lambda: scenes.box_scene(256, 256)),
+        "bpt_box": dict(width=512, height=512, spp=16, depth=16, volumetric=False, bpt=True,
+                        text="bpt_box: the box scene (Lambert walls and blocks, 0.25x0.25 ceiling light), "
+                             "BPTRenderer, 16 vertices per subpath, 512x512, 16 spp, seed 0",
+                        scene=lambda: scenes.box_scene(512, 512)),
+        "bpt_box_small": dict(width=256, height=256, spp=4, depth=16, volumetric=False, bpt=True,
+                              text="bpt_box_small: the bidirectional box workload at 256x256, 4 spp (profiler "
+                                   "captures)",
+                              scene=lambda: scenes.box_scene(256, 256)),
         "volumetric_small": dict(width=256, height=256, spp=4, depth=32, volumetric=True,
                                  text="volumetric_small: the volumetric box with a 128^3 grid, 256x256, 4 spp, "
                                       "max depth 32 (profiler captures)",
@@ -404,18 +437,20 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--spp", type=int, default=None)
     ap.add_argument("--workload", default="ggx_ibl_1m",
-                    choices=["ggx_ibl_1m", "small", "box", "volumetric", "volumetric_small", "serving", "traversal"])
+                    choices=["ggx_ibl_1m", "small", "box", "bpt_box", "bpt_box_small", "volumetric", "volumetric_small",
+                             "serving", "traversal"])
     ap.add_argument("--requests", type=int, default=512)
     args = ap.parse_args()
     if args.workload == "serving":
         return run_serving(args)
     if args.workload == "traversal":
         return run_traversal(args)
-    global WIDTH, HEIGHT, WORKLOAD, SPP, MAX_DEPTH, VOLUMETRIC
+    global WIDTH, HEIGHT, WORKLOAD, SPP, MAX_DEPTH, VOLUMETRIC, BPT
     wl = WORKLOADS[args.workload]
     WIDTH, HEIGHT, SPP, MAX_DEPTH, VOLUMETRIC, WORKLOAD = (wl["width"], wl["height"], wl["spp"], wl["depth"],
                                                            wl["volumetric"], wl["text"])
-    if args.workload in ("small", "volumetric_small"):
+    BPT = wl.get("bpt", False)
+    if args.workload in ("small", "volumetric_small", "bpt_box_small"):
         args.no_cpu_baseline = True
     if args.spp is None:
         args.spp = SPP
@@ -453,7 +488,7 @@ def main():
 
     film_dev = torch.empty((HEIGHT, WIDTH, 16), dtype=torch.float32, device="cuda")
     for i in range(args.warmup):
-        scene.render(WIDTH, HEIGHT, spp, MAX_DEPTH, seed=seed_base + i, film=film_dev, volumetric=VOLUMETRIC)
+        scene.render(WIDTH, HEIGHT, spp, MAX_DEPTH, seed=seed_base + i, film=film_dev, volumetric=VOLUMETRIC, bpt=BPT)
     torch.cuda.synchronize()
 
     clocks = ClockSampler(local)
@@ -469,7 +504,7 @@ def main():
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()
         _, rs = scene.render(WIDTH, HEIGHT, spp, MAX_DEPTH, seed=seed_base + 100 + i, film=film_dev,
-                             flags=api.FLAG_PROFILE_KERNELS, volumetric=VOLUMETRIC)
+                             flags=api.FLAG_PROFILE_KERNELS, volumetric=VOLUMETRIC, bpt=BPT)
         e1.record()
         torch.cuda.synchronize()
         barrier()
@@ -500,7 +535,8 @@ def main():
         torch.cuda.synchronize()
         t1 = time.perf_counter()
         h2d = scene.reupload()
-        scene.render(WIDTH, HEIGHT, spp, MAX_DEPTH, seed=seed_base + 200 + i, film=film_np, volumetric=VOLUMETRIC)
+        scene.render(WIDTH, HEIGHT, spp, MAX_DEPTH, seed=seed_base + 200 + i, film=film_np, volumetric=VOLUMETRIC,
+                     bpt=BPT)
         torch.cuda.synchronize()
         e2e_ms.append(1e3 * (time.perf_counter() - t1))
     e2e_total = sum(e2e_ms)
@@ -516,6 +552,9 @@ def main():
     dom = max(range(5), key=lambda k: kern_ms[k])
     units = {1: (ext_rays, BYTES_EXTEND), 3: (sh_rays, BYTES_SHADOW), 2: (ext_rays, BYTES_SHADE),
              0: (samples_per_step * args.steps, 64), 4: (samples_per_step * args.steps, BYTES_FILM)}
+    if BPT:
+        units.update({1: (ext_rays, BYTES_BPT_BOUNCE), 3: (sh_rays, BYTES_BPT_CONNECT),
+                      0: (samples_per_step * args.steps, 2 * 160 + 96)})
     n_units, per_unit = units[dom]
     bytes_per_launch = n_units * per_unit / max(1, kern_n[dom])
     avg_launch_s = kern_ms[dom] * 1e-3 / max(1, kern_n[dom])
@@ -526,6 +565,12 @@ def main():
                 "bytes_per_unit": per_unit, "units_per_launch": n_units / max(1, kern_n[dom]),
                 "avg_launch_ms": avg_launch_s * 1e3,
                 "kernel_share": {names[k]: kern_ms[k] / max(1e-9, sum(kern_ms)) for k in range(5)}}
+    measured = MEASURED_DRAM_PER_UNIT.get((args.workload, names[dom]))
+    if measured is not None and not BPT:
+        roofline["traffic"] = measured * n_units / max(1, kern_n[dom])
+        roofline["traffic_source"] = "ncu dram bytes per unit (profiles/dram_ggx_ibl_1m.md) x units per launch"
+    if BPT:   # the bidirectional tracer's kernels behind the classes
+        roofline["kernel"] = {0: "kBptInit", 1: "kBptBounce", 3: "kBptConnect", 4: "kBptAccumulate"}.get(dom, names[dom])
     line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",

@@ -43,6 +43,7 @@ extern "C" {
 #define SLRGPU_ERR_NOT_COMMITTED    (-5)
 #define SLRGPU_ERR_STATE            (-6)
 #define SLRGPU_ERR_TIMEOUT          (-7)
+#define SLRGPU_ERR_UNSUPPORTED      (-8)   /* a valid request this build does not implement */
 
 typedef uint64_t slrgpu_handle;
 
@@ -86,6 +87,15 @@ typedef struct slrgpu_settings {
  * through the shared edge of two triangles; hits then differ from the
  * reference only for rays within rounding of an edge or vertex. */
 #define SLRGPU_FLAG_WATERTIGHT 2u
+/* settings.flags: bidirectional path tracing, BPTRenderer(spp)
+ * (libSLR/Renderer/BPTRenderer.h:117-123, BPTRenderer.cpp:25-431), instead
+ * of PTRenderer.  max_depth (1..63) then caps each subpath at max_depth
+ * vertices after its first (the reference ends subpaths by Russian roulette
+ * only).  Surface lights only: scenes with an environment, and volumetric = 1
+ * (VolumetricBPTRenderer), return SLRGPU_ERR_UNSUPPORTED.  Contributions
+ * through the lens vertex land on the pixel they project to;
+ * slrgpu_render_stats.dropped_samples counts non-finite contributions. */
+#define SLRGPU_FLAG_BPT 4u
 
 /* Kernel classes of the wavefront (index into kernel_ms / kernel_count). */
 #define SLRGPU_KERNEL_RAYGEN 0

@@ -47,6 +47,15 @@ Build-only patches (all applied to the copy):
   (``PTRenderer.cpp:138``, ``VolumetricPTRenderer.cpp:138``) is replaced by an
   increment of a counter the driver reports; which samples are dropped does
   not change.
+* P9 ``Renderer/BPTRenderer.cpp``: a subpath stops after
+  ``slr_oracle_max_depth`` vertices beyond its first (the stock renderer ends
+  subpaths by Russian roulette only; the check sits before the BSDF sample
+  at ``:347``, so the last vertex is still made and connected), the
+  progressive ``saveImage`` (``:84``) is disabled and the message for a
+  dropped non-finite connection (``:265``) becomes a counter increment.
+* P10 ``Renderer/BPTRenderer.cpp:338``: a non-finite implicit-path
+  contribution is dropped and counted instead of being added to the film
+  (where one NaN would spoil the pixel for good).
 """
 from __future__ import annotations
 
@@ -65,6 +74,7 @@ SRC_COPY = REF_OUT / "src" / "libSLR"
 OBJ_DIR = REF_OUT / "obj"
 LIB = REF_OUT / "libslr_ref.so"
 DEFAULT_REFERENCE = "/root/reference"
+PATCH_SET = "P1 P2 P3 P4 P5 P6 P7 P8 P9 P10\n"
 
 # Files excluded from the reference's own build (libSLR/CMakeLists.txt:45-51).
 EXCLUDED = {
@@ -150,9 +160,21 @@ def copy_and_patch(ref_root: Path) -> None:
         t = _replace_once(t, drop_print, drop_count, "P8 VolPT")
         return t.replace("namespace SLR {", decl + "namespace SLR {", 1)
     patch("Renderer/VolumetricPTRenderer.cpp", p6_vpt)
+    def p9_bpt(t: str) -> str:
+        t = _replace_once(t, "            BSDFQueryResult fsResult;\n            SampledSpectrum fs = bsdf->sample(",
+                          "            if (vertices.size() > slr_oracle_max_depth)\n                break;\n"
+                          "            BSDFQueryResult fsResult;\n            SampledSpectrum fs = bsdf->sample(", "P9 BPT cap")
+        t = _replace_once(t, "sensor->saveImage(filename,", "if (0) sensor->saveImage(filename,", "P9 BPT save")
+        t = _replace_once(t, 'slrDevPrintf("Unexpected value detected: %s at (%f, %f)\\n", contribution.toString().c_str(), p.x, p.y);',
+                          "slr_oracle_dropped_samples.fetch_add(1);", "P9 BPT drop")
+        t = _replace_once(t, "                    sensor->add(curPx, curPy, wls, contribution);",
+                          "                    if (contribution.allFinite()) sensor->add(curPx, curPy, wls, contribution);\n"
+                          "                    else slr_oracle_dropped_samples.fetch_add(1);", "P10 BPT implicit")
+        return t.replace("namespace SLR {", decl + "namespace SLR {", 1)
+    patch("Renderer/BPTRenderer.cpp", p9_bpt)
     # P7: the stock reporter is replaced by oracle/progress_reporter_noop.cpp
     (SRC_COPY / "Core" / "ProgressReporter.cpp").unlink()
-    (REF_OUT / "src" / "PATCHED").write_text("P1 P2 P3 P4 P5 P6 P7 P8\n")
+    (REF_OUT / "src" / "PATCHED").write_text(PATCH_SET)
 
 
 def _compile(cmd: list[str]) -> tuple[list[str], int, str]:
@@ -162,7 +184,8 @@ def _compile(cmd: list[str]) -> tuple[list[str], int, str]:
 
 def build(jobs: int | None = None, force: bool = False, verbose: bool = False) -> Path:
     ref_root = _reference_root()
-    if ref_root is not None and (force or not (REF_OUT / "src" / "PATCHED").is_file()):
+    marker = REF_OUT / "src" / "PATCHED"
+    if ref_root is not None and (force or not marker.is_file() or marker.read_text() != PATCH_SET):
         copy_and_patch(ref_root)
     if not (REF_OUT / "src" / "PATCHED").is_file():
         raise RuntimeError("reference sources unavailable: neither the reference checkout nor "

@@ -6,7 +6,8 @@
 // exposes extern "C" entry points so that tests and the CPU-baseline leg of
 // bench.py can run, through ctypes:
 //   * the reference renderers PTRenderer / VolumetricPTRenderer
-//     (libSLR/Renderer/PTRenderer.cpp:26-101) and read back the 16-bin film;
+//     (libSLR/Renderer/PTRenderer.cpp:26-101) and BPTRenderer
+//     (libSLR/Renderer/BPTRenderer.cpp:25-101) and read back the 16-bin film;
 //   * the reference SBVH (libSLR/Accelerator/SBVH.h:380-496) on explicit ray
 //     sets (closest hit and any hit), plus its node dump for build parity;
 //   * the reference BSDFs at fixed queries (libSLR/BSDF/*.cpp).
@@ -59,6 +60,7 @@
 #include "BSDF/microfacet_bsdfs.h"
 #include "Renderer/PTRenderer.h"
 #include "Renderer/VolumetricPTRenderer.h"
+#include "Renderer/BPTRenderer.h"
 #include "MediumMaterial/basic_medium_materials.h"
 #include "Core/medium_material.h"
 #include "Core/medium_object.h"
@@ -110,6 +112,7 @@ namespace {
         std::unique_ptr<MediumObjectAggregate> medAgg;
         std::unique_ptr<Scene> scene;
         bool built = false;
+        bool bptRendered = false;
         // Standalone SBVH over the same surface objects, for ray queries.
         ArenaAllocator rayMem;
         std::vector<SurfaceObject*> rayObjs;
@@ -352,6 +355,47 @@ int ora_render(void* p, int volumetric, int spp, int maxDepth, int w, int h, int
         for (int y = 0; y < h; ++y)
             for (int x = 0; x < w; ++x) {
                 DiscretizedSpectrum v = sensor->pixel(x, y);
+                for (int b = 0; b < 16; ++b)
+                    film[((size_t)y * w + x) * 16 + b] = v[b];
+            }
+    }
+    return 0;
+}
+
+// Renders with BPTRenderer and copies the 16-bin film, main buffer plus the
+// per-thread buffers that collect the light-tracing connections
+// (BPTRenderer.cpp:268-276; ImageSensor::saveImage adds them the same way,
+// ImageSensor.cpp:154-156).  ImageSensor::addSeparatedBuffers
+// (ImageSensor.cpp:54-63) allocates buffers only beyond those it already
+// has, into a new pointer array, so a second BPT render through the same
+// sensor would clear unallocated buffers: one BPT render per scene (-2).
+int ora_render_bpt(void* p, int spp, int maxDepth, int w, int h, int threads, int seed, float* film,
+                   double* seconds) {
+    OraScene* s = (OraScene*)p;
+    if (!s->built || !s->scene->getCamera()) return -1;
+    if (s->bptRendered) return -2;
+    s->bptRendered = true;
+    slr_oracle_max_depth = (unsigned)maxDepth;
+    RenderSettings settings;
+    settings.addItem(RenderSettingItem::NumThreads, (int32_t)threads);
+    settings.addItem(RenderSettingItem::ImageWidth, (int32_t)w);
+    settings.addItem(RenderSettingItem::ImageHeight, (int32_t)h);
+    settings.addItem(RenderSettingItem::TimeStart, 0.0f);
+    settings.addItem(RenderSettingItem::TimeEnd, 0.0f);
+    settings.addItem(RenderSettingItem::Brightness, 1.0f);
+    settings.addItem(RenderSettingItem::RNGSeed, (int32_t)seed);
+    slr_oracle_dropped_samples.store(0);
+    BPTRenderer r(spp);
+    auto t0 = std::chrono::steady_clock::now();
+    r.render(*s->scene, settings);
+    auto t1 = std::chrono::steady_clock::now();
+    if (seconds) *seconds = std::chrono::duration<double>(t1 - t0).count();
+    const ImageSensor* sensor = s->scene->getCamera()->getSensor();
+    if (film) {
+        for (int y = 0; y < h; ++y)
+            for (int x = 0; x < w; ++x) {
+                DiscretizedSpectrum v = sensor->pixel(x, y);
+                for (int t = 0; t < threads; ++t) v += sensor->pixel((uint32_t)t, x, y);
                 for (int b = 0; b < 16; ++b)
                     film[((size_t)y * w + x) * 16 + b] = v[b];
             }

@@ -52,6 +52,7 @@ class Settings(C.Structure):
 KERNEL_CLASSES = ["raygen", "extend", "shade", "shadow", "accumulate"]
 FLAG_PROFILE_KERNELS = 1
 FLAG_WATERTIGHT = 2
+FLAG_BPT = 4
 
 
 class RenderStats(C.Structure):
@@ -333,10 +334,13 @@ class Scene:
         return b.value
 
     def render(self, width: int, height: int, spp: int, max_depth: int, seed: int = 0, volumetric: bool = False,
-               samples_per_wave: int = 0, film=None, flags: int = 0, sample_base: int = 0):
+               samples_per_wave: int = 0, film=None, flags: int = 0, sample_base: int = 0, bpt: bool = False):
         """Returns (film (h, w, 16) float32 sum over samples, RenderStats).
         ``film`` may be a preallocated host numpy array or a CUDA tensor;
-        samples [sample_base, sample_base + spp) are rendered."""
+        samples [sample_base, sample_base + spp) are rendered.  ``bpt``:
+        bidirectional path tracing (max_depth then caps each subpath)."""
+        if bpt:
+            flags |= FLAG_BPT
         s = Settings(width, height, spp, max_depth, seed, int(volumetric), samples_per_wave, flags, sample_base)
         st = RenderStats()
         on_device = 0
@@ -540,6 +544,24 @@ class PathTracingRenderer:
         h = int(settings.get(RenderSettingItem.ImageHeight))
         seed = int(settings.get(RenderSettingItem.RNGSeed, 0)) & 0xffffffff
         film, stats = scene.render(w, h, self.spp, self.max_depth, seed=seed, volumetric=self.volumetric)
+        self.last_stats = stats
+        return film
+
+
+class BidirectionalPathTracingRenderer:
+    """Drop-in for SLR::BPTRenderer(spp) (libSLR/Renderer/BPTRenderer.h:117-123);
+    max_depth caps each subpath at that many vertices beyond its first (the
+    reference ends subpaths by Russian roulette only)."""
+
+    def __init__(self, spp: int, max_depth: int = 32):
+        self.spp = int(spp)
+        self.max_depth = int(max_depth)
+
+    def render(self, scene: Scene, settings: RenderSettings):
+        w = int(settings.get(RenderSettingItem.ImageWidth))
+        h = int(settings.get(RenderSettingItem.ImageHeight))
+        seed = int(settings.get(RenderSettingItem.RNGSeed, 0)) & 0xffffffff
+        film, stats = scene.render(w, h, self.spp, self.max_depth, seed=seed, bpt=True)
         self.last_stats = stats
         return film
 

@@ -23,7 +23,7 @@ LIB = LIB_DIR / "libslrgpu.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 HOST_SOURCES = ["scene_host.cpp", "capi.cpp", "server.cpp"]
-CUDA_SOURCES = ["render.cu"]
+CUDA_SOURCES = ["render.cu", "bpt.cu"]
 
 
 def _cuda_home() -> Path:

@@ -1,0 +1,981 @@
+// Bidirectional path tracing (BPTRenderer semantics) on the GPU.
+//
+// The estimator is the reference's BPTRenderer::Job (libSLR/Renderer/
+// BPTRenderer.cpp:103-431): per sample a light subpath (light vertex, then
+// vertices traced with adjoint BSDFs) and an eye subpath (lens vertex, then
+// vertices traced with radiance BSDFs, adding the implicit paths that hit an
+// emitter), then every connection of an eye vertex with a light vertex,
+// weighted by the power heuristic over all strategies of the same path.
+// Connections through the lens vertex (t = 1) land on another pixel and go
+// to a splat film, the counterpart of the reference's separated sensor
+// buffers (ImageSensor.cpp:132-137).  Only the random numbers differ
+// (counter-based, one stream per subpath).
+//
+// GPU structure, one wave at a time:
+//   kBptInit     one thread per path: pixel and wavelengths, the light vertex
+//                and the lens vertex, the first ray of each subpath;
+//   kBptBounce   per bounce, over the queue of live subpaths (both kinds
+//                mixed): closest hit, vertex creation, implicit emission,
+//                BSDF sampling with reverse densities, Russian roulette;
+//   kBptConnect  one thread per eye vertex: the connections with every light
+//                vertex of its path (shadow ray, MIS weight, contribution);
+//   kBptAccumulate  per pixel: the wave's per-path sums and the splat film
+//                into the compensated 16-bin film.
+// Vertices live in HBM as [depth][subpath] arrays of 64-byte geometry,
+// 32-byte density and 64-byte throughput records.
+#include "render_api.h"
+
+#include <algorithm>
+#include <chrono>
+#include <cstring>
+#include <mutex>
+
+#include "device_bsdf_rev.cuh"
+#include "device_scene.cuh"
+
+namespace slrgpu {
+
+namespace {
+
+// Vertex kinds.
+constexpr uint32_t kVtxLens = 0;
+constexpr uint32_t kVtxLight = 1;
+constexpr uint32_t kVtxSurface = 2;
+// BptPdf::flags
+constexpr uint32_t kVfDelta = 1u;        // reached by a delta distribution (position or direction)
+constexpr uint32_t kVfWlSelected = 2u;   // the subpath's wavelength was selected when the vertex was made
+constexpr int kVfKindShift = 4;         // vertex kind, 2 bits
+constexpr int kVfMatShift = 8;          // material kind of a surface vertex, 4 bits
+
+// Geometry of a vertex (64 B).
+//   surface: pg.w = material index bits; ng.w, nz.w, tx.w = query direction
+//            (toward the previous vertex) z, x, y in the shading frame
+//   lens:    nz.w, tx.w = lens position in the lens frame (x, y)
+struct __align__(16) BptGeom {
+    float4 pg;   // position
+    float4 ng;   // geometric normal
+    float4 nz;   // shading normal
+    float4 tx;   // shading tangent
+};
+
+// Densities of a vertex (32 B), BPTRenderer.h:66-86.
+struct __align__(16) BptPdf {
+    float cosIn;        // |cos| at this vertex toward the previous one
+    float areaPdf;      // area density of this vertex, sampled from the previous one
+    float rrProb;       // Russian roulette probability that led here
+    float revAreaPdf;   // area density of this vertex, sampled from the next one
+    float revRRProb;
+    uint32_t flags;
+    float pad0, pad1;
+};
+
+// Per-subpath state (S = 2N subpaths: light subpaths [0, N), eye [N, 2N)).
+struct BptState {
+    uint32_t N;           // paths per wave
+    uint32_t S;           // 2N
+    uint32_t D;           // vertex capacity per subpath - 1
+    BptGeom* geom;        // [(D + 1) * S]
+    BptPdf* pdf;          // [(D + 1) * S]
+    float4* alpha;        // [(D + 1) * S * 4]
+    float4* bsdfA;        // [(D + 1) * S * 4] first spectrum of a surface vertex's BSDF
+    float4* rayOrg;       // [S] xyz, tmin
+    float4* rayDir;       // [S]
+    float4* alphaPend;    // [S * 4] throughput arriving at the next vertex
+    float4* aux;          // [S] dirPdf, cosLast, rrPend, info bits
+    uint32_t* rngCounter; // [S]
+    uint32_t* numVerts;   // [S]
+    // per path
+    uint2* rngKey;        // [N]
+    float2* pix;          // [N] film position
+    float* wlOffset;      // [N]
+    uint32_t* sel;        // [N]
+    float* L;             // [N][16] contributions at the path's own pixel
+    float* splat;         // [16][pixels] contributions through the lens vertex
+    uint32_t splatPixels;
+    uint32_t* queue[2];   // [S]
+    uint32_t* connQueue;  // [N * (D + 1)] eye vertex indices
+    uint32_t* counters;   // [D + 2] queue sizes per bounce, then the connection count
+    unsigned long long* stats;   // 0 extension rays, 1 shadow rays, 2 dropped contributions
+};
+
+// aux.w info bits
+constexpr uint32_t kAuxDelta = 1u;        // the pending direction was sampled by a delta distribution
+constexpr uint32_t kAuxWlSelected = 2u;
+
+struct BptWave {
+    uint32_t width, height, gridW, gridH, gridPositions;
+    uint32_t sampleBase, samples, seed, numPaths;
+};
+
+constexpr uint32_t kLightStream = 1u << 30;   // counter offset of the light subpath's random numbers
+
+__device__ __forceinline__ uint64_t keyOf(const BptState &st, uint32_t p) {
+    uint2 k = st.rngKey[p];
+    return ((uint64_t)k.y << 32) | k.x;
+}
+__device__ __forceinline__ V3 xyz(float4 v) { return V3{v.x, v.y, v.z}; }
+// std::min(a, b) as the reference evaluates it: b < a ? b : a (a NaN first
+// argument stays NaN, unlike fminf).
+__device__ __forceinline__ float stdMin(float a, float b) { return (b < a) ? b : a; }
+
+__device__ __forceinline__ void storeAlpha(float4* a, size_t i, const Spec &s) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) a[i * 4 + k] = make_float4(s.v[4 * k], s.v[4 * k + 1], s.v[4 * k + 2], s.v[4 * k + 3]);
+}
+__device__ __forceinline__ void loadAlpha(const float4* a, size_t i, Spec &s) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        float4 v = a[i * 4 + k];
+        s.v[4 * k] = v.x; s.v[4 * k + 1] = v.y; s.v[4 * k + 2] = v.z; s.v[4 * k + 3] = v.w;
+    }
+}
+
+__device__ __forceinline__ Frame cameraFrame(const DevCamera &c) {
+    return Frame{V3{c.ex[0], c.ex[1], c.ex[2]}, V3{c.ey[0], c.ey[1], c.ey[2]}, V3{c.ez[0], c.ez[1], c.ez[2]}};
+}
+
+// ---- the camera as a vertex (PerspectiveCamera.cpp:31-107, EquirectangularCamera.cpp:24-109) ----
+// Importance of the lens vertex toward dirIn (lens frame): 1 inside the view, else 0.
+__device__ __forceinline__ bool idfInside(const DevCamera &c, V3 d, float lu, float lv) {
+    if (c.kind == 0) {
+        float s = c.objPlaneDist / d.z;
+        float fx = d.x * s + lu, fy = d.y * s + lv;
+        return fx >= -c.opWidth * 0.5f && fx <= c.opWidth * 0.5f && fy >= -c.opHeight * 0.5f &&
+               fy <= c.opHeight * 0.5f && d.z >= 0;
+    }
+    float theta, phi;
+    toPolarYUp(d, &theta, &phi);
+    if (phi > kPiF) phi -= 2 * kPiF;
+    theta -= 0.5f * kPiF;
+    return phi >= -c.phiAngle * 0.5f && phi < c.phiAngle * 0.5f && theta >= -c.thetaAngle * 0.5f &&
+           theta < c.thetaAngle * 0.5f;
+}
+__device__ __forceinline__ float idfPdf(const DevCamera &c, V3 d, float lu, float lv) {
+    if (!idfInside(c, d, lu, lv)) return 0.0f;
+    if (c.kind == 0) return c.imgPlaneDist * c.imgPlaneDist / ((d.z * d.z * d.z) * c.imgPlaneArea);
+    // EquirectangularIDF::evaluatePDF takes 1 - y^2 for the sine (no root).
+    float sinTheta = 1.0f - d.y * d.y;
+    return 1.0f / (c.phiAngle * c.thetaAngle * sinTheta);
+}
+__device__ __forceinline__ void idfPixel(const DevCamera &c, V3 d, float lu, float lv, uint32_t w, uint32_t h,
+                                         float* px, float* py) {
+    if (c.kind == 0) {
+        float s = c.objPlaneDist / d.z;
+        float fx = d.x * s + lu, fy = d.y * s + lv;
+        *px = w * (0.5f - fx / c.opWidth);
+        *py = h * (0.5f - fy / c.opHeight);
+        return;
+    }
+    float theta, phi;
+    toPolarYUp(d, &theta, &phi);
+    if (phi > kPiF) phi -= 2 * kPiF;
+    theta -= 0.5f * kPiF;
+    *px = (phi / c.phiAngle + 0.5f) * w;
+    *py = (theta / c.thetaAngle + 0.5f) * h;
+}
+
+// ---------------------------------------------------------------------------
+// Kernels
+// ---------------------------------------------------------------------------
+// Job::kernel up to the two subpath generations (BPTRenderer.cpp:107-172).
+__global__ void kBptInit(DevScene sc, BptState st, BptWave wv) {
+    const float selectWLPDF = kNumLambda / (kWavelengthHigh - kWavelengthLow);
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < wv.numPaths; p += gridDim.x * blockDim.x) {
+        const uint32_t s = p / wv.gridPositions;
+        const uint32_t pos = p - s * wv.gridPositions;
+        const uint32_t ix = pos % wv.gridW, iy = pos / wv.gridW;
+        const uint64_t key = pathKey(wv.seed, (uint64_t)(wv.sampleBase + s) * wv.gridPositions + pos);
+        st.rngKey[p] = make_uint2((uint32_t)key, (uint32_t)(key >> 32));
+        Rng er{key, 0};
+        (void)er.next();   // time
+        const float pxf = ix + er.next();
+        const float pyf = iy + er.next();
+        const float wlOff = er.next();
+        const uint32_t sel = min((uint32_t)(kNumLambda * er.next()), (uint32_t)(kNumLambda - 1));
+        st.pix[p] = make_float2(pxf, pyf);
+        st.wlOffset[p] = wlOff;
+        st.sel[p] = sel;
+        float lambdas[kNumLambda];
+#pragma unroll
+        for (int k = 0; k < kNumLambda; ++k) {
+            lambdas[k] = lambdaAt(k, wlOff);
+            st.L[(size_t)p * kNumLambda + k] = 0.0f;
+        }
+
+        // Light subpath: light vertex and its ray (BPTRenderer.cpp:122-149,
+        // surface_object.cpp:65-90, TriangleSurfaceShape.cpp:357-406).
+        {
+            const uint32_t sp = p;
+            Rng lr{key, kLightStream};
+            float lightProb;
+            const int li = selectLight(sc, lr.next(), &lightProb);
+            const float u0 = lr.next(), u1 = lr.next();
+            (void)lr.next();   // EDFSample::uComponent
+            const float e0 = lr.next(), e1 = lr.next();
+            const DevPrim lpr = sc.prims[sc.lightPrims[li < 0 ? 0 : li]];
+            const float su = sqrtf(u0);
+            const float b0 = 1.0f - su, b1 = u1 * su, b2 = 1.0f - b0 - b1;
+            const float4 p0 = sc.vpos[lpr.v0], p1 = sc.vpos[lpr.v1], p2 = sc.vpos[lpr.v2];
+            const V3 lp = rn_bary(b0, xyz(p0), b1, xyz(p1), b2, xyz(p2));
+            const float4 n0 = sc.vnrm[lpr.v0], n1 = sc.vnrm[lpr.v1], n2 = sc.vnrm[lpr.v2];
+            const float4 t0 = sc.vtan[lpr.v0], t1 = sc.vtan[lpr.v1], t2 = sc.vtan[lpr.v2];
+            const V3 z = normalize(b0 * xyz(n0) + b1 * xyz(n1) + b2 * xyz(n2));
+            V3 x = normalize(b0 * xyz(t0) + b1 * xyz(t1) + b2 * xyz(t2));
+            const float dotNT = dot(z, x);
+            if (fabsf(dotNT) >= 0.01f) x = normalize(x - dotNT * z);
+            const Frame fr{x, cross(z, x), z};
+            const V3 gn = V3{lpr.ngx, lpr.ngy, lpr.ngz};
+            Spec Le0;
+            evalSpectrum(sc, sc.materials[lpr.material].emit, lambdas, Le0);
+            const float lightAreaPdf = lightProb * lpr.invArea;
+            Spec a0;
+#pragma unroll
+            for (int k = 0; k < kNumLambda; ++k) a0.v[k] = Le0.v[k] / lightAreaPdf;
+            BptGeom g;
+            g.pg = make_float4(lp.x, lp.y, lp.z, 0.0f);
+            g.ng = make_float4(gn.x, gn.y, gn.z, 0.0f);
+            g.nz = make_float4(z.x, z.y, z.z, 0.0f);
+            g.tx = make_float4(x.x, x.y, x.z, 0.0f);
+            st.geom[sp] = g;
+            BptPdf pd;
+            pd.cosIn = 0.0f;
+            pd.areaPdf = lightAreaPdf;
+            pd.rrProb = 1.0f;
+            pd.revAreaPdf = 0.0f;
+            pd.revRRProb = 0.0f;
+            pd.flags = kVtxLight << kVfKindShift;   // LowFreq position
+            pd.pad0 = pd.pad1 = 0.0f;
+            st.pdf[sp] = pd;
+            storeAlpha(st.alpha, sp, a0);
+            // DiffuseEDF::sample (basic_edfs.cpp:13-18)
+            const V3 dl = cosineSampleHemisphere(e0, e1);
+            const float dirPdf = dl.z * kInvPiF;
+            const V3 dir = fr.fromLocal(dl);
+            const float cosG = absDot(dir, gn);
+            Spec a;
+#pragma unroll
+            for (int k = 0; k < kNumLambda; ++k) a.v[k] = a0.v[k] * kInvPiF * (cosG / dirPdf);
+            storeAlpha(st.alphaPend, sp, a);
+            st.rayOrg[sp] = make_float4(lp.x, lp.y, lp.z, kRayEpsilon);
+            st.rayDir[sp] = make_float4(dir.x, dir.y, dir.z, 0.0f);
+            st.aux[sp] = make_float4(dirPdf, dl.z, 1.0f, __uint_as_float(0u));
+            st.rngCounter[sp] = lr.counter;
+            st.numVerts[sp] = 1;
+            queuePush(st.queue[0], st.counters + 0, sp, dirPdf != 0.0f);
+        }
+
+        // Eye subpath: lens vertex and its ray (BPTRenderer.cpp:151-172, camera.h:49-63).
+        {
+            const uint32_t sp = st.N + p;
+            const DevCamera &c = sc.camera;
+            const Frame fr = cameraFrame(c);
+            const float l0 = er.next(), l1 = er.next();
+            V3 orgLocal = V3{0.0f, 0.0f, 0.0f};
+            float areaPdf = 1.0f;
+            bool deltaPos = true;
+            V3 dl;
+            float dirPdf;
+            const float u = pxf / wv.width, v = pyf / wv.height;
+            if (c.kind == 0) {
+                float lx, ly;
+                concentricSampleDisk(l0, l1, &lx, &ly);
+                orgLocal = V3{c.lensRadius * lx, c.lensRadius * ly, 0.0f};
+                if (c.lensRadius > 0.0f) {
+                    areaPdf = 1.0f / (kPiF * c.lensRadius * c.lensRadius);
+                    deltaPos = false;
+                }
+                V3 pFocus = V3{c.opWidth * (0.5f - u), c.opHeight * (0.5f - v), c.objPlaneDist};
+                dl = normalize(pFocus - orgLocal);
+                dirPdf = c.imgPlaneDist * c.imgPlaneDist / ((dl.z * dl.z * dl.z) * c.imgPlaneArea);
+            } else {
+                float phi = c.phiAngle * (u - 0.5f);
+                float theta = 0.5f * kPiF + c.thetaAngle * (v - 0.5f);
+                float sp_, cp, st_, ct;
+                sincosf(phi, &sp_, &cp);
+                sincosf(theta, &st_, &ct);
+                dl = V3{-sp_ * st_, ct, cp * st_};
+                float sinTheta = sqrtf(1.0f - dl.y * dl.y);
+                dirPdf = 1.0f / (c.phiAngle * c.thetaAngle * sinTheta);
+            }
+            const V3 org = V3{c.org[0], c.org[1], c.org[2]} + orgLocal.x * fr.x + orgLocal.y * fr.y;
+            const float a0 = 1.0f / (areaPdf * selectWLPDF);
+            BptGeom g;
+            g.pg = make_float4(org.x, org.y, org.z, 0.0f);
+            g.ng = make_float4(fr.z.x, fr.z.y, fr.z.z, 0.0f);
+            g.nz = make_float4(fr.z.x, fr.z.y, fr.z.z, orgLocal.x);
+            g.tx = make_float4(fr.x.x, fr.x.y, fr.x.z, orgLocal.y);
+            st.geom[sp] = g;
+            BptPdf pd;
+            pd.cosIn = 0.0f;
+            pd.areaPdf = areaPdf;
+            pd.rrProb = 1.0f;
+            pd.revAreaPdf = 0.0f;
+            pd.revRRProb = 0.0f;
+            pd.flags = (kVtxLens << kVfKindShift) | (deltaPos ? kVfDelta : 0u);
+            pd.pad0 = pd.pad1 = 0.0f;
+            st.pdf[sp] = pd;
+            storeAlpha(st.alpha, sp, specConst(a0));
+            const V3 dir = fr.fromLocal(dl);
+            const float cosG = absDot(dir, fr.z);
+            storeAlpha(st.alphaPend, sp, specConst(a0 * (cosG / dirPdf)));
+            st.rayOrg[sp] = make_float4(org.x, org.y, org.z, 0.0f);
+            st.rayDir[sp] = make_float4(dir.x, dir.y, dir.z, 0.0f);
+            st.aux[sp] = make_float4(dirPdf, dl.z, 1.0f, __uint_as_float(0u));
+            st.rngCounter[sp] = er.counter;
+            st.numVerts[sp] = 1;
+            queuePush(st.queue[0], st.counters + 0, sp, dirPdf != 0.0f);
+            queuePush(st.connQueue, st.counters + st.D + 1, sp, true);   // t = 1
+        }
+    }
+}
+
+// Power-heuristic MIS weight (BPTRenderer.cpp:383-431) over the density
+// records of one eye subpath and one light subpath.
+struct MisSide {
+    const BptPdf* pdf;
+    uint32_t S, sp, n, minN;
+    float e1, r1, e2, r2;   // densities of extending the other subpath by one and two vertices
+};
+__device__ __forceinline__ void kahanAdd(float &sum, float &comp, float v) {
+    float cin = v - comp;
+    float t = sum + cin;
+    comp = (t - sum) - cin;
+    sum = t;
+}
+__device__ void extendAndShorten(const MisSide &m, float &sum, float &comp) {
+    if (m.n <= m.minN) return;
+    const BptPdf end = m.pdf[(size_t)(m.n - 1) * m.S + m.sp];
+    float ratio = m.e1 * m.r1 / (end.areaPdf * end.rrProb);
+    bool sd = (end.flags & kVfDelta) != 0;
+    if (!sd) kahanAdd(sum, comp, ratio * ratio);
+    bool prev = sd;
+    if (m.n - 1 > m.minN) {
+        const BptPdf nv = m.pdf[(size_t)(m.n - 2) * m.S + m.sp];
+        ratio *= m.e2 * m.r2 / (nv.areaPdf * nv.rrProb);
+        sd = (nv.flags & kVfDelta) != 0;
+        if (!sd && !prev) kahanAdd(sum, comp, ratio * ratio);
+        prev = sd;
+        for (int i = (int)m.n - 2; i > (int)m.minN; --i) {
+            const BptPdf v = m.pdf[(size_t)(i - 1) * m.S + m.sp];
+            ratio *= v.revAreaPdf * v.revRRProb / (v.areaPdf * v.rrProb);
+            sd = (v.flags & kVfDelta) != 0;
+            if (!sd && !prev) kahanAdd(sum, comp, ratio * ratio);
+            prev = sd;
+        }
+    }
+}
+__device__ __forceinline__ float misWeight(const MisSide &eye, const MisSide &light) {
+    float sum = 1.0f, comp = 0.0f;
+    extendAndShorten(eye, sum, comp);     // shorten the eye subpath, not down to the lens
+    extendAndShorten(light, sum, comp);   // shorten the light subpath, down to the implicit path
+    return 1.0f / sum;
+}
+
+__device__ __forceinline__ Frame vertexFrame(const BptGeom &g) {
+    V3 z = xyz(g.nz), x = xyz(g.tx);
+    return Frame{x, cross(z, x), z};
+}
+
+// One bounce of every live subpath: generateSubPath's loop body
+// (BPTRenderer.cpp:304-379).  A subpath holds at most D + 1 vertices.
+__global__ void __launch_bounds__(256, 2) kBptBounce(DevScene sc, BptState st, const uint32_t* __restrict__ inQueue,
+                                                     const uint32_t* __restrict__ inCount, uint32_t* outQueue,
+                                                     uint32_t* outCount) {
+    const uint32_t n = *inCount;
+    const float inf = __int_as_float(0x7f800000);
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+        const uint32_t i = base + threadIdx.x;
+        const bool active = i < n;
+        bool extend = false, conn = false;
+        uint32_t sp = active ? inQueue[i] : 0;
+        if (active) {
+            const bool adjoint = sp < st.N;
+            const uint32_t p = adjoint ? sp : sp - st.N;
+            const float4 ro = st.rayOrg[sp], rd = st.rayDir[sp];
+            const V3 org = xyz(ro), dir = xyz(rd);
+            Hit h;
+            traceClosest(sc, org, dir, ro.w, inf, &h);
+            if (h.prim != kNoHit) {
+                const DevPrim pr = sc.prims[h.prim];
+                SurfPoint spt;
+                surfacePoint(sc, pr, org, dir, h.t, h.b1, h.b2, spt);
+                const float4 ax = st.aux[sp];
+                float dirPdf = ax.x, cosLast = ax.y, rrPend = ax.z;
+                uint32_t info = __float_as_uint(ax.w);
+                bool wlSelected = (info & kAuxWlSelected) != 0;
+                const uint32_t k = st.numVerts[sp];   // index of the new vertex
+                const float dist2 = sqLength(spt.p - org);
+                const V3 dirOut = spt.frame.toLocal(-dir);
+                const V3 gnl = spt.frame.toLocal(spt.gn);
+                const float cosOut = absDot(-dir, spt.gn);
+                const float areaPdf = dirPdf * cosOut / dist2;
+                Spec alpha;
+                loadAlpha(st.alphaPend, sp, alpha);
+                const size_t vi = (size_t)k * st.S + sp;
+                BptGeom g;
+                g.pg = make_float4(spt.p.x, spt.p.y, spt.p.z, __uint_as_float(pr.material));
+                g.ng = make_float4(spt.gn.x, spt.gn.y, spt.gn.z, dirOut.z);
+                g.nz = make_float4(spt.frame.z.x, spt.frame.z.y, spt.frame.z.z, dirOut.x);
+                g.tx = make_float4(spt.frame.x.x, spt.frame.x.y, spt.frame.x.z, dirOut.y);
+                st.geom[vi] = g;
+                BptPdf pd;
+                pd.cosIn = cosOut;
+                pd.areaPdf = areaPdf;
+                pd.rrProb = rrPend;
+                pd.revAreaPdf = 0.0f;
+                pd.revRRProb = 0.0f;
+                const DevMaterial mat = sc.materials[pr.material];
+                pd.flags = (kVtxSurface << kVfKindShift) | (mat.kind << kVfMatShift) |
+                           ((info & kAuxDelta) ? kVfDelta : 0u) | (wlSelected ? kVfWlSelected : 0u);
+                pd.pad0 = pd.pad1 = 0.0f;
+                st.pdf[vi] = pd;
+                storeAlpha(st.alpha, vi, alpha);
+                st.numVerts[sp] = k + 1;
+                conn = !adjoint;
+
+                const float wlOff = st.wlOffset[p];
+                const int sel = (int)st.sel[p];
+                float lambdas[kNumLambda];
+#pragma unroll
+                for (int q = 0; q < kNumLambda; ++q) lambdas[q] = lambdaAt(q, wlOff);
+                Bsdf B;
+                makeBsdf(sc, mat, lambdas, wlSelected, B);
+                storeAlpha(st.bsdfA, vi, B.a);   // the connections reuse it (Lambert reflectance)
+                // Implicit path, no light subpath vertex (BPTRenderer.cpp:318-340).
+                if (!adjoint && mat.emit >= 0) {
+                    Spec Le0;
+                    evalSpectrum(sc, mat.emit, lambdas, Le0);
+                    const float Le1 = dirOut.z > 0.0f ? kInvPiF : 0.0f;
+                    // Scene::intersect's light probability: the emitter's share
+                    // of the surface aggregate (all emitting triangles weigh 1).
+                    const float hitLightProb = (sc.surfImportance / (sc.surfImportance + sc.envImportance)) *
+                                               sc.lightPMF[0];
+                    const float e1 = hitLightProb * pr.invArea;
+                    const float e2 = (dirOut.z > 0.0f ? dirOut.z * kInvPiF : 0.0f) * cosLast / dist2;
+                    MisSide eye{st.pdf, st.S, sp, k + 1, 1, e1, 1.0f, e2, 1.0f};
+                    MisSide light{st.pdf, st.S, p, 0, 0, 0.0f, 0.0f, 0.0f, 0.0f};
+                    const float mis = misWeight(eye, light);
+                    if (!isinf(mis) && !isnan(mis)) {
+                        Spec c;
+                        bool finite = true;
+#pragma unroll
+                        for (int q = 0; q < kNumLambda; ++q) {
+                            c.v[q] = ((mis * alpha.v[q]) * Le0.v[q]) * Le1;
+                            if (wlSelected && q == sel) c.v[q] *= kNumLambda;
+                            finite &= isfinite(c.v[q]);
+                        }
+                        if (finite) {
+#pragma unroll
+                            for (int q = 0; q < kNumLambda; ++q)
+                                if (c.v[q] != 0.0f) atomicAdd(&st.L[(size_t)p * kNumLambda + q], c.v[q]);
+                        } else {
+                            atomicAdd(&st.stats[2], 1ull);
+                        }
+                    }
+                }
+                if (k < st.D) {
+                    Rng rng{keyOf(st, p), st.rngCounter[sp]};
+                    RevQuery q{dirOut, gnl, sel, adjoint};
+                    const float uc = rng.next(), u0 = rng.next(), u1 = rng.next();
+                    BsdfSample bs;
+                    Spec fs, revFs;
+                    float revPdf;
+                    bsdfSampleRev(B, q, uc, u0, u1, &bs, fs, &revPdf, revFs);
+                    if (bs.pdf != 0.0f && !specIsZero(fs)) {
+                        if ((bs.type & kDirDispersive) && !wlSelected) wlSelected = true;
+                        const V3 vecIn = spt.frame.fromLocal(bs.dir);
+                        const float cosIn = absDot(vecIn, spt.gn);
+                        Spec weight;
+#pragma unroll
+                        for (int c = 0; c < kNumLambda; ++c) weight.v[c] = fs.v[c] * (cosIn / bs.pdf);
+                        const float rr = stdMin(importance(weight, sel), 1.0f);
+                        if (rng.next() < rr) {
+#pragma unroll
+                            for (int c = 0; c < kNumLambda; ++c) alpha.v[c] *= weight.v[c] / rr;
+                            // reverse densities of the previous vertex
+                            BptPdf* prev = &st.pdf[(size_t)(k - 1) * st.S + sp];
+                            prev->revAreaPdf = revPdf * cosLast / dist2;
+                            Spec rv;
+#pragma unroll
+                            for (int c = 0; c < kNumLambda; ++c) rv.v[c] = revFs.v[c] * cosOut / revPdf;
+                            prev->revRRProb = stdMin(importance(rv, sel), 1.0f);
+                            storeAlpha(st.alphaPend, sp, alpha);
+                            st.rayOrg[sp] = make_float4(spt.p.x, spt.p.y, spt.p.z, kRayEpsilon);
+                            st.rayDir[sp] = make_float4(vecIn.x, vecIn.y, vecIn.z, 0.0f);
+                            info = (dirIsDelta(bs.type) ? kAuxDelta : 0u) | (wlSelected ? kAuxWlSelected : 0u);
+                            st.aux[sp] = make_float4(bs.pdf, cosIn, rr, __uint_as_float(info));
+                            extend = true;
+                        }
+                    }
+                    st.rngCounter[sp] = rng.counter;
+                }
+            }
+        }
+        queuePush(outQueue, outCount, sp, active && extend);
+        queuePush(st.connQueue, st.counters + st.D + 1, sp + (uint32_t)(st.numVerts[sp] - 1) * st.S,
+                  active && conn);
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&st.stats[0], (unsigned long long)n);
+}
+
+// The BSDF of a surface vertex for its connections: Lambert from the
+// reflectance cached at the vertex, other kinds evaluated again.
+__device__ __forceinline__ void vertexBsdf(const DevScene &sc, const BptState &st, size_t vi, uint32_t material,
+                                           uint32_t flags, const float lambdas[kNumLambda], Bsdf &B) {
+    if (((flags >> kVfMatShift) & 0xfu) == kMatMatte) {
+        B.kind = kMatMatte;
+        B.ax = B.ay = 0.0f;
+        B.dispersive = (flags & kVfWlSelected) == 0;
+        loadAlpha(st.bsdfA, vi, B.a);
+    } else {
+        makeBsdf(sc, sc.materials[material], lambdas, (flags & kVfWlSelected) != 0, B);
+    }
+}
+
+// Connections of one eye vertex with every light vertex of its path
+// (BPTRenderer.cpp:174-280).  Contributions to the path's own pixel (t > 1)
+// are summed in registers and added once per eye vertex.
+__global__ void __launch_bounds__(256, 2) kBptConnect(DevScene sc, BptState st, uint32_t width, uint32_t height,
+                                                      const uint32_t* __restrict__ queue,
+                                                      const uint32_t* __restrict__ count) {
+    const uint32_t n = *count;
+    const float recBinWidth = kNumLambda / (kWavelengthHigh - kWavelengthLow);
+    unsigned long long shadowRays = 0;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t evi = queue[i];
+        const uint32_t k = evi / st.S;            // eye vertex index, t = k + 1
+        const uint32_t esp = evi - k * st.S;
+        const uint32_t p = esp - st.N;
+        const uint32_t t = k + 1;
+        const uint32_t nL = st.numVerts[p];
+        const int sel = (int)st.sel[p];
+        const float wlOff = st.wlOffset[p];
+        float lambdas[kNumLambda];
+#pragma unroll
+        for (int q = 0; q < kNumLambda; ++q) lambdas[q] = lambdaAt(q, wlOff);
+        const BptGeom eg = st.geom[evi];
+        const BptPdf ep = st.pdf[evi];
+        const V3 eP = xyz(eg.pg), eN = xyz(eg.ng);
+        const Frame eF = vertexFrame(eg);
+        const bool eLens = (ep.flags >> kVfKindShift) == kVtxLens;
+        Bsdf eB;
+        RevQuery eq{V3{eg.nz.w, eg.tx.w, eg.ng.w}, eF.toLocal(eN), sel, false};
+        if (!eLens) vertexBsdf(sc, st, evi, __float_as_uint(eg.pg.w), ep.flags, lambdas, eB);
+        // the eye vertex before this one (t > 1)
+        V3 e2P{0, 0, 0}, e2N{0, 0, 0};
+        if (t > 1) {
+            const BptGeom g2 = st.geom[evi - st.S];
+            e2P = xyz(g2.pg);
+            e2N = xyz(g2.ng);
+        }
+        Spec eAlpha;
+        loadAlpha(st.alpha, evi, eAlpha);
+        Spec own = specConst(0.0f);
+        for (uint32_t s = 1; s <= nL; ++s) {
+            const size_t lvi = (size_t)(s - 1) * st.S + p;
+            const BptGeom lg = st.geom[lvi];
+            const BptPdf lpd = st.pdf[lvi];
+            const V3 lP = xyz(lg.pg), lN = xyz(lg.ng);
+            const Frame lF = vertexFrame(lg);
+            V3 cv = lP - eP;
+            const float dist2 = sqLength(cv);
+            cv = cv * (1.0f / sqrtf(dist2));
+            const float cosLightEnd = absDot(cv, lN);
+            const float cosEyeEnd = absDot(cv, eN);
+            const float G = cosEyeEnd * cosLightEnd / dist2;
+            // light end: EDF of the light vertex or the adjoint BSDF
+            const V3 lc = lF.toLocal(-cv);
+            Spec lDDF, lRev;
+            float lExt1DirPdf, eExt2DirPdf = 0.0f;
+            if (s == 1) {
+                lDDF = specConst(lc.z > 0.0f ? kInvPiF : 0.0f);
+                lRev = lDDF;
+                lExt1DirPdf = lc.z > 0.0f ? lc.z * kInvPiF : 0.0f;
+            } else {
+                Bsdf lB;
+                vertexBsdf(sc, st, lvi, __float_as_uint(lg.pg.w), lpd.flags, lambdas, lB);
+                RevQuery lq{V3{lg.nz.w, lg.tx.w, lg.ng.w}, lF.toLocal(lN), sel, true};
+                bsdfEvalRev(lB, lq, lc, lDDF, lRev);
+                lExt1DirPdf = bsdfPdfRev(lB, lq, lc, &eExt2DirPdf);
+            }
+            // eye end: importance of the lens or the BSDF
+            const V3 ec = eF.toLocal(cv);
+            Spec eDDF, eRev;
+            float eExt1DirPdf, lExt2DirPdf = 0.0f;
+            if (eLens) {
+                eDDF = specConst(idfInside(sc.camera, ec, eg.nz.w, eg.tx.w) ? 1.0f : 0.0f);
+                eRev = eDDF;
+                eExt1DirPdf = idfPdf(sc.camera, ec, eg.nz.w, eg.tx.w);
+            } else {
+                bsdfEvalRev(eB, eq, ec, eDDF, eRev);
+                eExt1DirPdf = bsdfPdfRev(eB, eq, ec, &lExt2DirPdf);
+            }
+            Spec ct;
+            bool nz = false;
+#pragma unroll
+            for (int q = 0; q < kNumLambda; ++q) {
+                ct.v[q] = lDDF.v[q] * G * eDDF.v[q];
+                nz |= ct.v[q] != 0.0f;
+            }
+            if (!nz) continue;
+            if ((lpd.flags & kVfWlSelected) || (ep.flags & kVfWlSelected)) {
+#pragma unroll
+                for (int q = 0; q < kNumLambda; ++q)
+                    if (q == sel) ct.v[q] *= kNumLambda;
+            }
+            // densities of the two subpaths' first and second extensions
+            const float lExt1Area = lExt1DirPdf * cosEyeEnd / dist2;
+            Spec tmp;
+#pragma unroll
+            for (int q = 0; q < kNumLambda; ++q) tmp.v[q] = lDDF.v[q] * cosLightEnd / lExt1DirPdf;
+            const float lExt1RR = s > 1 ? stdMin(importance(tmp, sel), 1.0f) : 1.0f;
+            float lExt2Area = 0.0f, lExt2RR = 0.0f;
+            if (t > 1) {
+                V3 d2 = eP - e2P;
+                const float dd2 = sqLength(d2);
+                d2 = d2 * (1.0f / sqrtf(dd2));
+                lExt2Area = lExt2DirPdf * absDot(d2, e2N) / dd2;
+#pragma unroll
+                for (int q = 0; q < kNumLambda; ++q) tmp.v[q] = eRev.v[q] * ep.cosIn / lExt2DirPdf;
+                lExt2RR = stdMin(importance(tmp, sel), 1.0f);
+            }
+            const float eExt1Area = eExt1DirPdf * cosLightEnd / dist2;
+#pragma unroll
+            for (int q = 0; q < kNumLambda; ++q) tmp.v[q] = eDDF.v[q] * cosEyeEnd / eExt1DirPdf;
+            const float eExt1RR = t > 1 ? stdMin(importance(tmp, sel), 1.0f) : 1.0f;
+            float eExt2Area = 0.0f, eExt2RR = 0.0f;
+            if (s > 1) {
+                const BptGeom l2 = st.geom[lvi - st.S];
+                V3 d2 = xyz(l2.pg) - lP;
+                const float dd2 = sqLength(d2);
+                d2 = d2 * (1.0f / sqrtf(dd2));
+                eExt2Area = eExt2DirPdf * absDot(d2, xyz(l2.ng)) / dd2;
+#pragma unroll
+                for (int q = 0; q < kNumLambda; ++q) tmp.v[q] = lRev.v[q] * lpd.cosIn / eExt2DirPdf;
+                eExt2RR = stdMin(importance(tmp, sel), 1.0f);
+            }
+            MisSide eyeSide{st.pdf, st.S, esp, t, 1, lExt1Area, lExt1RR, lExt2Area, lExt2RR};
+            MisSide lightSide{st.pdf, st.S, p, s, 0, eExt1Area, eExt1RR, eExt2Area, eExt2RR};
+            const float mis = misWeight(eyeSide, lightSide);
+            if (isinf(mis) || isnan(mis)) continue;
+            Spec lAlpha;
+            loadAlpha(st.alpha, lvi, lAlpha);
+            Spec c;
+            bool finite = true;
+#pragma unroll
+            for (int q = 0; q < kNumLambda; ++q) {
+                c.v[q] = ((mis * lAlpha.v[q]) * ct.v[q]) * eAlpha.v[q];
+                finite &= isfinite(c.v[q]);
+            }
+            if (!finite) {
+                atomicAdd(&st.stats[2], 1ull);
+                continue;
+            }
+            // Scene::testVisibility (Scene.cpp:96-112)
+            const float dist = length(lP - eP);
+            const V3 sd = (lP - eP) * (1.0f / dist);
+            ++shadowRays;
+            if (traceAny(sc, eP, sd, kRayEpsilon, dist * (1 - kRayEpsilon))) continue;
+            if (t > 1) {
+#pragma unroll
+                for (int q = 0; q < kNumLambda; ++q) own.v[q] += c.v[q];
+            } else {
+                float hx, hy;
+                idfPixel(sc.camera, ec, eg.nz.w, eg.tx.w, width, height, &hx, &hy);
+                const uint32_t ipx = min((uint32_t)fmaxf(hx, 0.0f), width - 1);
+                const uint32_t ipy = min((uint32_t)fmaxf(hy, 0.0f), height - 1);
+                const uint32_t pix = ipy * width + ipx;
+                // SpectrumStorage::add (spectrum_types.h:725-734): wavelength -> film bin
+#pragma unroll
+                for (int q = 0; q < kNumLambda; ++q) {
+                    const float f = __fmul_rn(__fdiv_rn(__fsub_rn(lambdas[q], kWavelengthLow),
+                                                        kWavelengthHigh - kWavelengthLow), (float)kNumLambda);
+                    const uint32_t bin = min((uint32_t)f, (uint32_t)(kNumLambda - 1));
+                    if (c.v[q] != 0.0f) atomicAdd(&st.splat[(size_t)bin * st.splatPixels + pix], c.v[q] * recBinWidth);
+                }
+            }
+        }
+        if (t > 1) {
+#pragma unroll
+            for (int q = 0; q < kNumLambda; ++q)
+                if (own.v[q] != 0.0f) atomicAdd(&st.L[(size_t)p * kNumLambda + q], own.v[q]);
+        }
+    }
+    if (shadowRays) atomicAdd(&st.stats[1], shadowRays);
+}
+
+// The wave's contributions into the compensated film: per pixel, the sums of
+// its paths in sample order (grid positions clamped into the last row /
+// column as ImageSensor::add does), then the splat film, which is cleared.
+__global__ void kBptAccumulate(BptState st, BptWave wv, float* filmSum, float* filmComp) {
+    const float recBinWidth = kNumLambda / (kWavelengthHigh - kWavelengthLow);
+    const uint32_t P = wv.width * wv.height;
+    for (uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x; pix < P; pix += gridDim.x * blockDim.x) {
+        float sum[kNumLambda], comp[kNumLambda];
+#pragma unroll
+        for (int b = 0; b < kNumLambda; ++b) {
+            sum[b] = filmSum[(size_t)b * P + pix];
+            comp[b] = filmComp[(size_t)b * P + pix];
+        }
+        const uint32_t x = pix % wv.width, y = pix / wv.width;
+        const uint32_t xEnd = x + 1 == wv.width ? wv.gridW : x + 1;
+        const uint32_t yEnd = y + 1 == wv.height ? wv.gridH : y + 1;
+        for (uint32_t s = 0; s < wv.samples; ++s)
+        for (uint32_t gy = y; gy < yEnd; ++gy)
+        for (uint32_t gx = x; gx < xEnd; ++gx) {
+            const uint32_t p = s * wv.gridPositions + gy * wv.gridW + gx;
+            const float wlOff = st.wlOffset[p];
+            float addend[kNumLambda];
+#pragma unroll
+            for (int b = 0; b < kNumLambda; ++b) addend[b] = 0.0f;
+#pragma unroll
+            for (int i = 0; i < kNumLambda; ++i) {
+                const float c = st.L[(size_t)p * kNumLambda + i];
+                const float lam = lambdaAt(i, wlOff);
+                const float f = __fmul_rn(__fdiv_rn(__fsub_rn(lam, kWavelengthLow), kWavelengthHigh - kWavelengthLow),
+                                          (float)kNumLambda);
+                const uint32_t bin = min((uint32_t)f, (uint32_t)(kNumLambda - 1));
+#pragma unroll
+                for (int b = 0; b < kNumLambda; ++b)
+                    if (b == (int)bin) addend[b] += c * recBinWidth;
+            }
+#pragma unroll
+            for (int b = 0; b < kNumLambda; ++b) kahanAdd(sum[b], comp[b], addend[b]);
+        }
+#pragma unroll
+        for (int b = 0; b < kNumLambda; ++b) {
+            float* sp = &st.splat[(size_t)b * st.splatPixels + pix];
+            kahanAdd(sum[b], comp[b], *sp);
+            *sp = 0.0f;
+            filmSum[(size_t)b * P + pix] = sum[b];
+            filmComp[(size_t)b * P + pix] = comp[b];
+        }
+    }
+}
+
+int gridFor(const void* kernel, int block) {
+    int dev = 0, sms = 0, perSM = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, kernel, block, 0);
+    return std::max(1, sms * std::max(1, perSM));
+}
+
+struct BptGrids {
+    int init, bounce, connect, accumulate;
+};
+const BptGrids &bptGrids() {
+    static BptGrids g;
+    static std::once_flag once;
+    std::call_once(once, [&]() {
+        g.init = gridFor((const void*)kBptInit, 256);
+        g.bounce = gridFor((const void*)kBptBounce, 256);
+        g.connect = gridFor((const void*)kBptConnect, 256);
+        g.accumulate = gridFor((const void*)kBptAccumulate, 256);
+    });
+    return g;
+}
+
+}  // namespace
+
+// Paths per wave of the bidirectional tracer when samples_per_wave is 0,
+// and the device memory its path state may take.
+#ifndef SLRGPU_BPT_WAVE_PATHS
+#define SLRGPU_BPT_WAVE_PATHS (1u << 20)
+#endif
+constexpr uint64_t kBptStateBudget = 8ull << 30;
+
+struct BptEngine {
+    BptState st{};
+    std::vector<void*> allocs;
+    uint32_t capN = 0, capD = 0, capPixels = 0;
+    ~BptEngine() { release(); }
+    void release() {
+        for (void* p : allocs) cudaFree(p);
+        allocs.clear();
+        st = BptState{};
+        capN = capD = capPixels = 0;
+    }
+    template <typename T>
+    T* alloc(size_t n, cudaError_t* e) {
+        void* p = nullptr;
+        *e = cudaMalloc(&p, std::max<size_t>(n, 1) * sizeof(T));
+        if (*e != cudaSuccess) return nullptr;
+        allocs.push_back(p);
+        return (T*)p;
+    }
+    int ensure(uint32_t N, uint32_t D, uint32_t pixels) {
+        if (N <= capN && D <= capD && pixels <= capPixels && !allocs.empty()) return SLRGPU_OK;
+        release();
+        cudaError_t e = cudaSuccess;
+        const size_t S = 2ull * N, V = (size_t)(D + 1) * S;
+        BptState s{};
+        s.N = N;
+        s.S = (uint32_t)S;
+        s.D = D;
+        bool ok = (s.geom = alloc<BptGeom>(V, &e)) && (s.pdf = alloc<BptPdf>(V, &e)) &&
+                  (s.alpha = alloc<float4>(V * 4, &e)) && (s.bsdfA = alloc<float4>(V * 4, &e)) &&
+                  (s.rayOrg = alloc<float4>(S, &e)) &&
+                  (s.rayDir = alloc<float4>(S, &e)) && (s.alphaPend = alloc<float4>(S * 4, &e)) &&
+                  (s.aux = alloc<float4>(S, &e)) && (s.rngCounter = alloc<uint32_t>(S, &e)) &&
+                  (s.numVerts = alloc<uint32_t>(S, &e)) && (s.rngKey = alloc<uint2>(N, &e)) &&
+                  (s.pix = alloc<float2>(N, &e)) && (s.wlOffset = alloc<float>(N, &e)) &&
+                  (s.sel = alloc<uint32_t>(N, &e)) && (s.L = alloc<float>((size_t)N * kNumLambda, &e)) &&
+                  (s.splat = alloc<float>((size_t)pixels * kNumLambda, &e)) &&
+                  (s.queue[0] = alloc<uint32_t>(S, &e)) && (s.queue[1] = alloc<uint32_t>(S, &e)) &&
+                  (s.connQueue = alloc<uint32_t>((size_t)N * (D + 1), &e)) &&
+                  (s.counters = alloc<uint32_t>(D + 2, &e)) && (s.stats = alloc<unsigned long long>(4, &e));
+        if (!ok) {
+            release();
+            setError(std::string("bidirectional path state allocation failed: ") + cudaGetErrorString(e));
+            return SLRGPU_ERR_OUT_OF_MEMORY;
+        }
+        s.splatPixels = pixels;
+        if (cudaMemset(s.splat, 0, (size_t)pixels * kNumLambda * sizeof(float)) != cudaSuccess) {
+            release();
+            setError("bidirectional path state initialisation failed");
+            return SLRGPU_ERR_CUDA;
+        }
+        st = s;
+        capN = N;
+        capD = D;
+        capPixels = pixels;
+        return SLRGPU_OK;
+    }
+};
+
+BptEngine* bptEngineCreate() { return new BptEngine(); }
+void bptEngineDestroy(BptEngine* e) { delete e; }
+
+uint64_t bptStateBytesPerPath(uint32_t maxDepth) {
+    const uint64_t V = 2ull * (maxDepth + 1);
+    return V * (sizeof(BptGeom) + sizeof(BptPdf) + 128) + 2 * (16 + 16 + 64 + 16 + 4 + 4) + 8 + 8 + 4 + 4 +
+           4 * kNumLambda + 8 + 4ull * (maxDepth + 1);
+}
+
+int renderBpt(BptEngine &eng, const DeviceScene &ds, const slrgpu_settings &s, float* filmSum, float* filmComp,
+              cudaStream_t stream, uint64_t* launches, std::vector<cudaEvent_t>* eventPool,
+              slrgpu_render_stats* stats) {
+    if (s.volumetric) {
+        setError("the volumetric bidirectional path tracer is not implemented");
+        return SLRGPU_ERR_UNSUPPORTED;
+    }
+    if (ds.sc.envPresent) {
+        setError("bidirectional path tracing with an environment light is not implemented");
+        return SLRGPU_ERR_UNSUPPORTED;
+    }
+    if (ds.sc.numLights == 0) {
+        setError("bidirectional path tracing needs at least one emitting surface");
+        return SLRGPU_ERR_INVALID_ARGUMENT;
+    }
+    if (s.max_depth < 1 || s.max_depth > 63) {
+        setError("bidirectional path tracing takes max_depth in [1, 63] (vertices per subpath after the first)");
+        return SLRGPU_ERR_INVALID_ARGUMENT;
+    }
+    const uint32_t D = s.max_depth;
+    const uint32_t gridW = (s.width + 7) / 8 * 8, gridH = (s.height + 7) / 8 * 8;
+    const uint32_t G = gridW * gridH;
+    const uint64_t perPath = bptStateBytesPerPath(D);
+    uint64_t want = s.samples_per_wave ? (uint64_t)s.samples_per_wave * G
+                                       : std::max<uint64_t>(G, (uint64_t)SLRGPU_BPT_WAVE_PATHS / G * G);
+    const uint64_t budgetPaths = std::max<uint64_t>(G, kBptStateBudget / perPath / G * G);
+    if (!s.samples_per_wave) want = std::min(want, budgetPaths);
+    uint32_t S = (uint32_t)std::min<uint64_t>(std::max<uint64_t>(1, want / G), s.spp);
+    const uint64_t N64 = (uint64_t)S * G;
+    if (N64 * (D + 1) * 2 >= (1ull << 32)) {
+        setError("bidirectional wave too large (paths x vertices exceed 2^32)");
+        return SLRGPU_ERR_INVALID_ARGUMENT;
+    }
+    const uint32_t N = (uint32_t)N64;
+    const uint32_t P = s.width * s.height;
+    int rc = eng.ensure(N, D, P);
+    if (rc != SLRGPU_OK) return rc;
+    BptState st = eng.st;
+    st.D = D;
+    st.splatPixels = P;
+    const BptGrids &g = bptGrids();
+    if (cudaMemsetAsync(st.stats, 0, 4 * sizeof(unsigned long long), stream) != cudaSuccess) {
+        setError("cudaMemsetAsync failed");
+        return SLRGPU_ERR_CUDA;
+    }
+    struct Mark { int cls; size_t ev; };
+    std::vector<Mark> marks;
+    size_t used = 0;
+    auto mark = [&](int cls) {
+        if (!eventPool) return;
+        if (used == eventPool->size()) {
+            cudaEvent_t e;
+            cudaEventCreate(&e);
+            eventPool->push_back(e);
+        }
+        marks.push_back(Mark{cls, used});
+        cudaEventRecord((*eventPool)[used++], stream);
+    };
+    auto markEnd = [&]() {
+        if (!eventPool) return;
+        if (used == eventPool->size()) {
+            cudaEvent_t e;
+            cudaEventCreate(&e);
+            eventPool->push_back(e);
+        }
+        cudaEventRecord((*eventPool)[used++], stream);
+    };
+    uint64_t nl = 0;
+    for (uint32_t base = 0; base < s.spp; base += S) {
+        BptWave wv;
+        wv.width = s.width;
+        wv.height = s.height;
+        wv.gridW = gridW;
+        wv.gridH = gridH;
+        wv.gridPositions = G;
+        wv.sampleBase = s.sample_base + base;
+        wv.samples = std::min(S, s.spp - base);
+        wv.seed = s.seed;
+        wv.numPaths = wv.samples * G;
+        cudaMemsetAsync(st.counters, 0, (D + 2) * sizeof(uint32_t), stream);
+        mark(SLRGPU_KERNEL_RAYGEN);
+        kBptInit<<<g.init, 256, 0, stream>>>(ds.sc, st, wv);
+        markEnd();
+        ++nl;
+        for (uint32_t b = 0; b < D; ++b) {
+            mark(SLRGPU_KERNEL_EXTEND);
+            kBptBounce<<<g.bounce, 256, 0, stream>>>(ds.sc, st, st.queue[b & 1], st.counters + b,
+                                                     st.queue[(b + 1) & 1], st.counters + b + 1);
+            markEnd();
+            ++nl;
+        }
+        mark(SLRGPU_KERNEL_SHADOW);
+        kBptConnect<<<g.connect, 256, 0, stream>>>(ds.sc, st, s.width, s.height, st.connQueue, st.counters + D + 1);
+        markEnd();
+        mark(SLRGPU_KERNEL_ACCUMULATE);
+        kBptAccumulate<<<g.accumulate, 256, 0, stream>>>(st, wv, filmSum, filmComp);
+        markEnd();
+        nl += 2;
+    }
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        setError(std::string("bidirectional kernels: ") + cudaGetErrorString(e));
+        return SLRGPU_ERR_CUDA;
+    }
+    if (launches) *launches += nl;
+    if (stats) {
+        unsigned long long h[4] = {0, 0, 0, 0};
+        if (cudaMemcpyAsync(h, st.stats, sizeof(h), cudaMemcpyDeviceToHost, stream) != cudaSuccess ||
+            cudaStreamSynchronize(stream) != cudaSuccess) {
+            setError("bidirectional statistics readback failed");
+            return SLRGPU_ERR_CUDA;
+        }
+        stats->extension_rays = h[0];
+        stats->shadow_rays = h[1];
+        stats->dropped_samples = h[2];
+        for (const Mark &m : marks) {
+            float kms = 0;
+            cudaEventElapsedTime(&kms, (*eventPool)[m.ev], (*eventPool)[m.ev + 1]);
+            stats->kernel_ms[m.cls] += kms;
+            stats->kernel_count[m.cls] += 1;
+        }
+    }
+    return SLRGPU_OK;
+}
+
+}  // namespace slrgpu

@@ -441,6 +441,8 @@ int slrgpu_render_noalloc(slrgpu_handle scene, const slrgpu_settings* settings, 
     if (!s->host.cameraPresent) return fail(SLRGPU_ERR_STATE, "scene has no camera");
     if (settings->volumetric && !s->host.medium.present)
         return fail(SLRGPU_ERR_INVALID_ARGUMENT, "volumetric render of a scene without medium");
+    if (settings->flags & SLRGPU_FLAG_BPT)
+        return fail(SLRGPU_ERR_UNSUPPORTED, "the allocation-free render has no bidirectional path tracer");
     cudaError_t e = cudaSetDevice(s->ctx->device);
     if (e != cudaSuccess) return fail(SLRGPU_ERR_CUDA, cudaGetErrorString(e));
     return renderNoAlloc(s->dev, *settings, film_device, (cudaStream_t)stream);
@@ -522,6 +524,8 @@ int slrgpu_server_submit(slrgpu_handle server, slrgpu_handle scene, const slrgpu
     if (!s->host.cameraPresent) return fail(SLRGPU_ERR_STATE, "scene has no camera");
     if (settings->volumetric && !s->host.medium.present)
         return fail(SLRGPU_ERR_INVALID_ARGUMENT, "volumetric render of a scene without medium");
+    if (settings->flags & SLRGPU_FLAG_BPT)
+        return fail(SLRGPU_ERR_UNSUPPORTED, "the server renders with the path tracers only");
     return rec->server->submit(&s->dev, &s->inFlight, *settings, request);
 }
 

@@ -415,14 +415,14 @@ __device__ __forceinline__ float bsdfPdfBody(const Bsdf &B, const BsdfQuery &q, 
 
 // Run-time dispatch, kept out of line so that kernels shading any material
 // carry one copy of every BSDF.
-__device__ __noinline__ void bsdfSampleInternal(const Bsdf &B, const BsdfQuery &q, float uc, float u0, float u1,
+static __device__ __noinline__ void bsdfSampleInternal(const Bsdf &B, const BsdfQuery &q, float uc, float u0, float u1,
                                                 BsdfSample* res, Spec &fs) {
     bsdfSampleBody<-1>(B, q, uc, u0, u1, res, fs);
 }
-__device__ __noinline__ void bsdfEvalInternal(const Bsdf &B, const BsdfQuery &q, V3 dir, Spec &fs) {
+static __device__ __noinline__ void bsdfEvalInternal(const Bsdf &B, const BsdfQuery &q, V3 dir, Spec &fs) {
     bsdfEvalBody<-1>(B, q, dir, fs);
 }
-__device__ __noinline__ float bsdfPdfInternal(const Bsdf &B, const BsdfQuery &q, V3 dir) {
+static __device__ __noinline__ float bsdfPdfInternal(const Bsdf &B, const BsdfQuery &q, V3 dir) {
     return bsdfPdfBody<-1>(B, q, dir);
 }
 

@@ -181,7 +181,7 @@ __device__ __forceinline__ void evalUpsampled(const float* __restrict__ basis, u
     }
 }
 
-__device__ __noinline__ void evalSpectrum(const DevScene &sc, int id, const float lambdas[kNumLambda], Spec &out) {
+static __device__ __noinline__ void evalSpectrum(const DevScene &sc, int id, const float lambdas[kNumLambda], Spec &out) {
     const DevSpectrum sp = sc.spectra[id];
     if (sp.kind == kSpecUpsampled) {
         evalUpsampled(sc.upsSpectra, sp.adj, sp.p0, sp.p1, sp.scale, lambdas, out);

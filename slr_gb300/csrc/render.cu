@@ -19,6 +19,7 @@
 #include "device_bsdf.cuh"
 #include "device_medium.cuh"
 #include "device_trace.cuh"
+#include "device_scene.cuh"
 
 namespace slrgpu {
 
@@ -34,22 +35,27 @@ namespace slrgpu {
 // ---------------------------------------------------------------------------
 // Path state (structure of arrays, N = paths per wave)
 // ---------------------------------------------------------------------------
+// The scalars of a path in one 32-byte record: one sector per thread,
+// wherever the compacted queues have scattered the path.
+struct __align__(16) PathScalars {
+    uint32_t info;       // bits 0-3 selected lambda, 4 wavelength selected, 5 previous delta, 8-15 depth
+    float wlOffset;
+    float prevPdf;       // density of the last BSDF sample (MIS of emission hits)
+    float initY;         // importance of the initial throughput (Russian roulette)
+    float camWeight;     // camera sample weight We0 We1 cos / (areaPDF dirPDF selectWLPDF)
+    uint32_t rngCounter;
+    uint32_t keyLo, keyHi;   // counter-RNG key of the path (seed, sample index, grid position)
+};
+static_assert(sizeof(PathScalars) == 32, "one sector per path");
+
 struct WaveState {
-    float4* rayOrg;      // xyz, tmin
-    float4* rayDir;      // xyz, tmax
+    float4* ray;         // [N][2]: origin xyz + tmin, direction xyz + tmax (one sector per path)
     float4* hit;         // t, b1, b2, prim bits
-    float* alpha;        // [16][N]
-    float* L;            // [16][N]
-    uint32_t* info;      // bits 0-3 selected lambda, 4 wavelength selected, 5 previous delta, 8-15 depth
-    float* wlOffset;
-    float* prevPdf;
-    float* initY;
-    float* camWeight;
-    uint32_t* rngCounter;
-    uint2* rngKey;       // counter-RNG key of the path (seed, sample index, grid position)
-    float4* shOrg;
-    float4* shDir;
-    float* shContrib;    // [16][N]
+    float* alpha;        // [N][16]: 16 contiguous values per path
+    float* L;            // [N][16]
+    PathScalars* ps;     // [N]
+    float4* shRay;       // [N][2]: shadow ray, as ray
+    float* shContrib;    // [N][16]
     uint32_t* queue[2];
     uint32_t* shadowQueue;
     uint32_t* classQueue;  // [kNumShadeClasses][N]: paths of one bounce sorted by shading class
@@ -107,171 +113,8 @@ constexpr uint32_t kInfoWlSelected = 1u << 4;
 constexpr uint32_t kInfoPrevDelta = 1u << 5;
 constexpr int kInfoDepthShift = 8;
 
-__device__ __forceinline__ void loadSpec(const float* base, uint32_t N, uint32_t p, Spec &s) {
-#pragma unroll
-    for (int i = 0; i < kNumLambda; ++i) s.v[i] = base[(size_t)i * N + p];
-}
-__device__ __forceinline__ void storeSpec(float* base, uint32_t N, uint32_t p, const Spec &s) {
-#pragma unroll
-    for (int i = 0; i < kNumLambda; ++i) base[(size_t)i * N + p] = s.v[i];
-}
-__device__ __forceinline__ void addSpec(float* base, uint32_t N, uint32_t p, const Spec &s) {
-#pragma unroll
-    for (int i = 0; i < kNumLambda; ++i) base[(size_t)i * N + p] += s.v[i];
-}
-
-// Warp-aggregated queue push.
-__device__ __forceinline__ void queuePush(uint32_t* queue, uint32_t* count, uint32_t value, bool pred) {
-    unsigned mask = __ballot_sync(__activemask(), pred);
-    if (!pred) return;
-    int leader = __ffs(mask) - 1;
-    int lane = threadIdx.x & 31;
-    uint32_t base = 0;
-    if (lane == leader) base = atomicAdd(count, (uint32_t)__popc(mask));
-    base = __shfl_sync(mask, base, leader);
-    queue[base + __popc(mask & ((1u << lane) - 1))] = value;
-}
-
 __device__ __forceinline__ uint64_t loadKey(const WaveState &ws, uint32_t p) {
-    uint2 k = ws.rngKey[p];
-    return ((uint64_t)k.y << 32) | k.x;
-}
-
-// ---------------------------------------------------------------------------
-// Camera
-// ---------------------------------------------------------------------------
-// Thin-lens perspective camera (PerspectiveCamera.cpp:31-83) and
-// equirectangular camera (EquirectangularCamera.cpp:25-69): ray and the
-// sample weight We0 We1 cos / (areaPDF dirPDF).
-__device__ __forceinline__ void cameraRay(const DevCamera &c, float lu0, float lu1, float px, float py,
-                                          V3* org, V3* dir, float* weight) {
-    V3 ex = V3{c.ex[0], c.ex[1], c.ex[2]}, ey = V3{c.ey[0], c.ey[1], c.ey[2]}, ez = V3{c.ez[0], c.ez[1], c.ez[2]};
-    Frame fr{ex, ey, ez};
-    if (c.kind == 0) {
-        float lx, ly;
-        concentricSampleDisk(lu0, lu1, &lx, &ly);
-        V3 orgLocal = V3{c.lensRadius * lx, c.lensRadius * ly, 0.0f};
-        *org = V3{c.org[0], c.org[1], c.org[2]} + orgLocal.x * ex + orgLocal.y * ey;
-        V3 pFocus = V3{c.opWidth * (0.5f - px), c.opHeight * (0.5f - py), c.objPlaneDist};
-        V3 dl = normalize(pFocus - orgLocal);
-        float dirPDF = c.imgPlaneDist * c.imgPlaneDist / ((dl.z * dl.z * dl.z) * c.imgPlaneArea);
-        float areaPDF = c.lensRadius > 0.0f ? 1.0f / (kPiF * c.lensRadius * c.lensRadius) : 1.0f;
-        *dir = fr.fromLocal(dl);
-        float cosT = absDot(*dir, ez);
-        *weight = cosT / (areaPDF * dirPDF);
-    } else {
-        *org = V3{c.org[0], c.org[1], c.org[2]};
-        float phi = c.phiAngle * (px - 0.5f);
-        float theta = 0.5f * kPiF + c.thetaAngle * (py - 0.5f);
-        float sp, cp, st, ct;
-        sincosf(phi, &sp, &cp);
-        sincosf(theta, &st, &ct);
-        V3 dl = V3{-sp * st, ct, cp * st};
-        float sinTheta = sqrtf(1.0f - dl.y * dl.y);
-        float dirPDF = 1.0f / (c.phiAngle * c.thetaAngle * sinTheta);
-        *dir = fr.fromLocal(dl);
-        // We0 We1 |cos| / (areaPDF dirPDF) with areaPDF = 1 (EquirectangularCamera.cpp:25-69).
-        *weight = absDot(*dir, ez) / dirPDF;
-    }
-}
-
-// ---------------------------------------------------------------------------
-// Environment
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ void toPolarYUp(V3 d, float* theta, float* phi) {
-    *theta = acosf(fminf(fmaxf(d.y, -1.0f), 1.0f));
-    const float twoPi = 6.28318530717958647692f;
-    *phi = fmodf(atan2f(-d.x, d.z) + twoPi, twoPi);
-}
-
-// Emitted radiance of the environment at texture coordinate (tu, tv):
-// (pi * texel * scale) * (1 / pi) (IBLEmitterSurfaceProperty.cpp:16-18, IBLEDF.cpp:18-21).
-__device__ __forceinline__ void envRadiance(const DevScene &sc, float tu, float tv, const float lambdas[kNumLambda],
-                                            Spec &Le) {
-    float u = fmodf(tu, 1.0f), v = fmodf(tv, 1.0f);
-    u += u < 0 ? 1.0f : 0.0f;
-    v += v < 0 ? 1.0f : 0.0f;
-    uint32_t px = min((uint32_t)(sc.envWidth * u), sc.envWidth - 1);
-    uint32_t py = min((uint32_t)(sc.envHeight * v), sc.envHeight - 1);
-    EnvTexel tx = sc.envTexels[(size_t)py * sc.envWidth + px];
-    evalUpsampled(sc.upsSpectra, tx.adj, tx.s, tx.t, tx.scale, lambdas, Le);
-#pragma unroll
-    for (int i = 0; i < kNumLambda; ++i) Le.v[i] = ((Le.v[i] * kPiF) * sc.envScale) * kInvPiF;
-}
-
-// RegularConstantContinuousDistribution1D::sample (distributions.cpp:205-214).
-__device__ __forceinline__ uint32_t prevPow2(uint32_t x) {
-    x |= x >> 1; x |= x >> 2; x |= x >> 4; x |= x >> 8; x |= x >> 16;
-    return x - (x >> 1);
-}
-// Alias-table sampling (Vose; O(1) instead of the CDF's binary search) of a
-// piecewise-constant distribution over [0, 1) with n bins: the bin is the
-// alias pick of u, the position inside it the leftover fraction of u
-// rescaled to [0, 1), the density that of the bin.  The tables hold the
-// PMF of the reference's CDFs, so the sampled distribution is the same.
-__device__ __forceinline__ uint32_t aliasPick(const AliasEntry* __restrict__ t, uint32_t n, float u, float* frac) {
-    const float x = u * (float)n;
-    const uint32_t i = min((uint32_t)x, n - 1);
-    const float f = fminf(x - (float)i, 0x1.fffffep-1f);
-    const AliasEntry e = t[i];
-    if (f < e.prob) {
-        *frac = f / e.prob;
-        return i;
-    }
-    *frac = (f - e.prob) / (1.0f - e.prob);
-    return e.alias;
-}
-
-__device__ __forceinline__ float sampleAlias(const AliasEntry* __restrict__ t, const float* __restrict__ pdf, uint32_t n,
-                                             float u, float* outPdf, uint32_t* bin) {
-    float frac;
-    const uint32_t k = aliasPick(t, n, u, &frac);
-    *outPdf = pdf[k];
-    *bin = k;
-    return fminf(((float)k + fminf(frac, 0x1.fffffep-1f)) / (float)n, 0x1.fffffep-1f);
-}
-
-
-__device__ __forceinline__ float envUVPdf(const DevScene &sc, float d0, float d1) {
-    uint32_t row = min((uint32_t)(sc.envMapH * d1), sc.envMapH - 1);
-    float top = sc.envTopPDF[min((int)(d1 * sc.envMapH), (int)sc.envMapH - 1)];
-    return top * sc.envRowPDF[(size_t)row * sc.envMapW + min((int)(d0 * sc.envMapW), (int)sc.envMapW - 1)];
-}
-
-// Area pdf of the environment at (phi, theta) (surface_object.cpp:281-286).
-__device__ __forceinline__ float envAreaPdf(const DevScene &sc, float phi, float theta) {
-    const float twoPi = 6.28318530717958647692f;
-    float uvPdf = envUVPdf(sc, phi / twoPi, theta / kPiF);
-    return uvPdf / (2.0f * kPiF * kPiF * sinf(theta));
-}
-
-// ---------------------------------------------------------------------------
-// Material -> BSDF (SurfaceMaterial::getBSDF)
-// ---------------------------------------------------------------------------
-__device__ __noinline__ void makeBsdf(const DevScene &sc, const DevMaterial &m, const float lambdas[kNumLambda],
-                                      bool wlSelected, Bsdf &B) {
-    B.kind = m.kind;
-    B.ax = m.alphaX;
-    B.ay = m.alphaY;
-    B.dispersive = !wlSelected;
-    switch (m.kind) {
-    case kMatMatte:
-        evalSpectrum(sc, m.spec[0], lambdas, B.a);
-        break;
-    case kMatSpecularReflection:
-    case kMatSpecularScattering:
-        evalSpectrum(sc, m.spec[0], lambdas, B.a);
-        evalSpectrum(sc, m.spec[1], lambdas, B.b);
-        evalSpectrum(sc, m.spec[2], lambdas, B.c);
-        break;
-    case kMatGGXReflection:
-    case kMatGGXScattering:
-        evalSpectrum(sc, m.spec[0], lambdas, B.a);
-        evalSpectrum(sc, m.spec[1], lambdas, B.b);
-        break;
-    default:
-        break;
-    }
+    return ((uint64_t)ws.ps[p].keyHi << 32) | ws.ps[p].keyLo;
 }
 
 // ---------------------------------------------------------------------------
@@ -292,7 +135,6 @@ __global__ void kRaygen(DevScene sc, WaveState ws, const __grid_constant__ WaveP
         uint32_t pixel = q - s * sg.gridPositions;
         uint32_t ix = pixel % sg.gridW, iy = pixel / sg.gridW;
         const uint64_t key = pathKey(sg.seed, (uint64_t)(sg.sampleBase + s) * sg.gridPositions + pixel);
-        ws.rngKey[p] = make_uint2((uint32_t)key, (uint32_t)(key >> 32));
         Rng rng{key, 0};
         // Draw order of Job::kernel: time, pixel (2), wavelength offset,
         // wavelength selection, lens (2) (PTRenderer.cpp:108-116).
@@ -307,20 +149,20 @@ __global__ void kRaygen(DevScene sc, WaveState ws, const __grid_constant__ WaveP
         V3 org, dir;
         float w;
         cameraRay(sc.camera, lu0, lu1, pxf / sg.width, pyf / sg.height, &org, &dir, &w);
-        ws.camWeight[p] = w / selectWLPDF;
-        ws.rayOrg[p] = make_float4(org.x, org.y, org.z, 0.0f);
-        ws.rayDir[p] = make_float4(dir.x, dir.y, dir.z, __int_as_float(0x7f800000));
-        ws.wlOffset[p] = wlOff;
-        ws.info[p] = sel;
-        ws.rngCounter[p] = rng.counter;
-        Spec one = specConst(1.0f);
-        ws.initY[p] = importance(one, (int)sel);
-        ws.prevPdf[p] = 0.0f;
-#pragma unroll
-        for (int i = 0; i < kNumLambda; ++i) {
-            ws.alpha[(size_t)i * ws.N + p] = 1.0f;
-            ws.L[(size_t)i * ws.N + p] = 0.0f;
-        }
+        ws.ray[2 * (size_t)p] = make_float4(org.x, org.y, org.z, 0.0f);
+        ws.ray[2 * (size_t)p + 1] = make_float4(dir.x, dir.y, dir.z, __int_as_float(0x7f800000));
+        PathScalars ps;
+        ps.info = sel;
+        ps.wlOffset = wlOff;
+        ps.prevPdf = 0.0f;
+        ps.initY = importance(specConst(1.0f), (int)sel);
+        ps.camWeight = w / selectWLPDF;
+        ps.rngCounter = rng.counter;
+        ps.keyLo = (uint32_t)key;
+        ps.keyHi = (uint32_t)(key >> 32);
+        ws.ps[p] = ps;
+        storeSpec(ws.alpha, p, specConst(1.0f));
+        storeSpec(ws.L, p, specConst(0.0f));
         ws.queue[0][p] = p;
     }
 }
@@ -329,7 +171,7 @@ __global__ void kExtend(DevScene sc, WaveState ws, const uint32_t* __restrict__ 
     const uint32_t n = *count;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         uint32_t p = queue[i];
-        float4 o = ws.rayOrg[p], d = ws.rayDir[p];
+        float4 o = ws.ray[2 * (size_t)p], d = ws.ray[2 * (size_t)p + 1];
         Hit h;
         traceClosest(sc, V3{o.x, o.y, o.z}, V3{d.x, d.y, d.z}, o.w, d.w, &h);
         ws.hit[p] = make_float4(h.t, h.b1, h.b2, __uint_as_float(h.prim));
@@ -348,62 +190,14 @@ __global__ void __launch_bounds__(256, SLRGPU_TRACE_MIN_BLOCKS) kShadow(DevScene
     const uint32_t n = *count;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         uint32_t p = queue[i];
-        float4 o = ws.shOrg[p], d = ws.shDir[p];
+        float4 o = ws.shRay[2 * (size_t)p], d = ws.shRay[2 * (size_t)p + 1];
         if (!traceAny(sc, V3{o.x, o.y, o.z}, V3{d.x, d.y, d.z}, o.w, d.w)) {
-#pragma unroll
-            for (int k = 0; k < kNumLambda; ++k)
-                ws.L[(size_t)k * ws.N + p] += ws.shContrib[(size_t)k * ws.N + p];
+            Spec c;
+            loadSpec(ws.shContrib, p, c);
+            addSpec(ws.L, p, c);
         }
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&ws.stats[1], (unsigned long long)n);
-}
-
-struct SurfPoint {
-    V3 p;
-    Frame frame;
-    V3 gn;
-};
-
-// Surface point of a hit (TriangleSurfaceShape.cpp:301-346): interpolated
-// shading normal, tangent made orthogonal to it, geometric normal.
-__device__ __forceinline__ void surfacePoint(const DevScene &sc, const DevPrim &pr, V3 org, V3 dir, float t, float mb1,
-                                             float mb2, SurfPoint &sp) {
-    sp.p = rn_ray_point(org, dir, t);   // TriangleSurfaceShape.cpp:250
-    float b0 = 1.0f - mb1 - mb2;
-    float b1 = mb1;
-    float b2 = 1.0f - b0 - b1;
-    float4 n0 = sc.vnrm[pr.v0], n1 = sc.vnrm[pr.v1], n2 = sc.vnrm[pr.v2];
-    float4 t0 = sc.vtan[pr.v0], t1 = sc.vtan[pr.v1], t2 = sc.vtan[pr.v2];
-    V3 z = normalize(b0 * V3{n0.x, n0.y, n0.z} + b1 * V3{n1.x, n1.y, n1.z} + b2 * V3{n2.x, n2.y, n2.z});
-    V3 x = b0 * V3{t0.x, t0.y, t0.z} + b1 * V3{t1.x, t1.y, t1.z} + b2 * V3{t2.x, t2.y, t2.z};
-    float dnt = dot(z, x);
-    x = normalize(x - dnt * z);
-    sp.frame = Frame{x, cross(z, x), z};
-    sp.gn = V3{pr.ngx, pr.ngy, pr.ngz};
-}
-
-// Light selection (Scene::selectSurfaceLight, Scene.cpp:137-155).  Returns
-// -1 for the environment, else the light index; *prob = selection probability.
-__device__ __forceinline__ int selectLight(const DevScene &sc, float u, float* prob) {
-    auto surf = [&](float uu, float* pr) -> int {
-        float frac;
-        const int idx = (int)aliasPick(sc.lightAlias, sc.numLights, uu, &frac);
-        *pr = sc.lightPMF[idx];
-        return idx;
-    };
-    if (sc.envPresent) {
-        float sumImps = sc.surfImportance + sc.envImportance;
-        float su = sumImps * u;
-        if (su < sc.surfImportance) {
-            float uu = u / (sc.surfImportance / sumImps);
-            int idx = surf(uu, prob);
-            *prob *= sc.surfImportance / sumImps;
-            return idx;
-        }
-        *prob = 1.0f * (sc.envImportance / sumImps);
-        return -1;
-    }
-    return surf(u, prob);
 }
 
 // ---------------------------------------------------------------------------
@@ -426,7 +220,7 @@ __global__ void __launch_bounds__(256, SLRGPU_TRACE_MIN_BLOCKS) kExtendSort(DevS
         uint32_t p = 0;
         if (active) {
             p = queue[i];
-            float4 o = ws.rayOrg[p], d = ws.rayDir[p];
+            float4 o = ws.ray[2 * (size_t)p], d = ws.ray[2 * (size_t)p + 1];
             Hit h;
             traceClosest(sc, V3{o.x, o.y, o.z}, V3{d.x, d.y, d.z}, o.w, d.w, &h);
             ws.hit[p] = make_float4(h.t, h.b1, h.b2, __uint_as_float(h.prim));
@@ -448,14 +242,14 @@ __global__ void kShadeMiss(DevScene sc, WaveState ws, const uint32_t* __restrict
     const float twoPi = 6.28318530717958647692f;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const uint32_t p = queue[i];
-        const uint32_t info = ws.info[p];
+        const uint32_t info = ws.ps[p].info;
         const uint32_t depth = info >> kInfoDepthShift;
         const bool prevDelta = (info & kInfoPrevDelta) != 0;
-        const float wlOff = ws.wlOffset[p];
+        const float wlOff = ws.ps[p].wlOffset;
         float lambdas[kNumLambda];
 #pragma unroll
         for (int k = 0; k < kNumLambda; ++k) lambdas[k] = lambdaAt(k, wlOff);
-        float4 rd = ws.rayDir[p];
+        float4 rd = ws.ray[2 * (size_t)p + 1];
         V3 dir = V3{rd.x, rd.y, rd.z};
         float theta, phi;
         toPolarYUp(dir, &theta, &phi);
@@ -465,25 +259,15 @@ __global__ void kShadeMiss(DevScene sc, WaveState ws, const uint32_t* __restrict
         if (depth > 0 && !prevDelta) {
             float lightProb = sc.envImportance / (sc.surfImportance + sc.envImportance);
             float lightPdf = lightProb * envAreaPdf(sc, phi, theta) * 1.0f / absDot(dir, -dir);
-            float bp = ws.prevPdf[p];
+            float bp = ws.ps[p].prevPdf;
             mis = (bp * bp) / (lightPdf * lightPdf + bp * bp);
         }
+        Spec a;
+        loadSpec(ws.alpha, p, a);
 #pragma unroll
-        for (int k = 0; k < kNumLambda; ++k)
-            ws.L[(size_t)k * ws.N + p] += ws.alpha[(size_t)k * ws.N + p] * Le.v[k] * mis;
+        for (int k = 0; k < kNumLambda; ++k) a.v[k] = a.v[k] * Le.v[k] * mis;
+        addSpec(ws.L, p, a);
     }
-}
-
-template <int K>
-__device__ __forceinline__ void makeBsdfK(const DevScene &sc, const DevMaterial &m, const float lambdas[kNumLambda],
-                                          bool wlSelected, Bsdf &B) {
-    B.kind = (uint32_t)K;
-    B.ax = m.alphaX;
-    B.ay = m.alphaY;
-    B.dispersive = !wlSelected;
-    evalSpectrum(sc, m.spec[0], lambdas, B.a);
-    if (K != kMatMatte) evalSpectrum(sc, m.spec[1], lambdas, B.b);
-    if (K == kMatSpecularReflection || K == kMatSpecularScattering) evalSpectrum(sc, m.spec[2], lambdas, B.c);
 }
 
 template <int K>
@@ -506,22 +290,22 @@ __global__ void __launch_bounds__(256, SLRGPU_SHADE_MIN_BLOCKS) kShadeSurf(DevSc
         bool extend = false, shadow = false;
         uint32_t p = active ? inQueue[i] : 0;
         if (active) {
-            uint32_t info = ws.info[p];
+            uint32_t info = ws.ps[p].info;
             const int sel = (int)(info & kInfoSelMask);
             bool wlSelected = (info & kInfoWlSelected) != 0;
             const bool prevDelta = (info & kInfoPrevDelta) != 0;
             uint32_t depth = info >> kInfoDepthShift;
-            const float wlOff = ws.wlOffset[p];
+            const float wlOff = ws.ps[p].wlOffset;
             float lambdas[kNumLambda];
 #pragma unroll
             for (int k = 0; k < kNumLambda; ++k) lambdas[k] = lambdaAt(k, wlOff);
-            Rng rng{loadKey(ws, p), ws.rngCounter[p]};
-            float4 ro = ws.rayOrg[p], rd = ws.rayDir[p];
+            Rng rng{loadKey(ws, p), ws.ps[p].rngCounter};
+            float4 ro = ws.ray[2 * (size_t)p], rd = ws.ray[2 * (size_t)p + 1];
             V3 org = V3{ro.x, ro.y, ro.z}, dir = V3{rd.x, rd.y, rd.z};
             float4 hv = ws.hit[p];
             const DevPrim pr = sc.prims[__float_as_uint(hv.w)];
             Spec alpha;
-            loadSpec(ws.alpha, N, p, alpha);
+            loadSpec(ws.alpha, p, alpha);
             bool alive = true;
             SurfPoint sp;
             surfacePoint(sc, pr, org, dir, hv.x, hv.y, hv.z, sp);
@@ -537,17 +321,17 @@ __global__ void __launch_bounds__(256, SLRGPU_SHADE_MIN_BLOCKS) kShadeSurf(DevSc
                     float lightProb = (sc.surfImportance / (sc.surfImportance + sc.envImportance)) * sc.lightPMF[0];
                     float dist2 = sqLength(sp.p - org);
                     float lightPdf = lightProb * pr.invArea * dist2 / absDot(dir, sp.gn);
-                    float bp = ws.prevPdf[p];
+                    float bp = ws.ps[p].prevPdf;
                     mis = (bp * bp) / (lightPdf * lightPdf + bp * bp);
                 }
                 Spec add;
 #pragma unroll
                 for (int k = 0; k < kNumLambda; ++k) add.v[k] = alpha.v[k] * (M.v[k] * edf) * mis;
-                addSpec(ws.L, N, p, add);
+                addSpec(ws.L, p, add);
             }
             // Russian roulette (PTRenderer.cpp:266-272).
             if (depth > 0) {
-                float cp = fminf(importance(alpha, sel) / ws.initY[p], 1.0f);
+                float cp = fminf(importance(alpha, sel) / ws.ps[p].initY, 1.0f);
                 if (rng.next() < cp) {
                     float r = 1.0f / cp;
 #pragma unroll
@@ -630,7 +414,7 @@ __global__ void __launch_bounds__(256, SLRGPU_SHADE_MIN_BLOCKS) kShadeSurf(DevSc
                             nz |= c.v[k] != 0.0f;
                         }
                         if (nz) {
-                            storeSpec(ws.shContrib, N, p, c);
+                            storeSpec(ws.shContrib, p, c);
                             float tmax;
                             V3 sdir;
                             if (atInf) {
@@ -642,8 +426,8 @@ __global__ void __launch_bounds__(256, SLRGPU_SHADE_MIN_BLOCKS) kShadeSurf(DevSc
                                 sdir = dd * (1.0f / dist);
                                 tmax = dist * (1 - kRayEpsilon);
                             }
-                            ws.shOrg[p] = make_float4(sp.p.x, sp.p.y, sp.p.z, kRayEpsilon);
-                            ws.shDir[p] = make_float4(sdir.x, sdir.y, sdir.z, tmax);
+                            ws.shRay[2 * (size_t)p] = make_float4(sp.p.x, sp.p.y, sp.p.z, kRayEpsilon);
+                            ws.shRay[2 * (size_t)p + 1] = make_float4(sdir.x, sdir.y, sdir.z, tmax);
                             shadow = true;
                         }
                     }
@@ -665,17 +449,17 @@ __global__ void __launch_bounds__(256, SLRGPU_SHADE_MIN_BLOCKS) kShadeSurf(DevSc
 #pragma unroll
                     for (int k = 0; k < kNumLambda; ++k) alpha.v[k] *= (fs.v[k] * cg) * r;
                     V3 nd = sp.frame.fromLocal(bs.dir);
-                    ws.rayOrg[p] = make_float4(sp.p.x, sp.p.y, sp.p.z, kRayEpsilon);
-                    ws.rayDir[p] = make_float4(nd.x, nd.y, nd.z, inf);
-                    ws.prevPdf[p] = bs.pdf;
+                    ws.ray[2 * (size_t)p] = make_float4(sp.p.x, sp.p.y, sp.p.z, kRayEpsilon);
+                    ws.ray[2 * (size_t)p + 1] = make_float4(nd.x, nd.y, nd.z, inf);
+                    ws.ps[p].prevPdf = bs.pdf;
                     info = (uint32_t)sel | (wlSelected ? kInfoWlSelected : 0u) |
                            (dirIsDelta(bs.type) ? kInfoPrevDelta : 0u) | (depth << kInfoDepthShift);
-                    ws.info[p] = info;
-                    storeSpec(ws.alpha, N, p, alpha);
+                    ws.ps[p].info = info;
+                    storeSpec(ws.alpha, p, alpha);
                     extend = true;
                 }
             }
-            ws.rngCounter[p] = rng.counter;
+            ws.ps[p].rngCounter = rng.counter;
         }
         queuePush(shQueue, shCount, p, active && shadow);
         queuePush(outQueue, outCount, p, active && extend);
@@ -745,22 +529,22 @@ __global__ void __launch_bounds__(256, SLRGPU_SHADEVOL_MIN_BLOCKS) kShadeVol(Dev
         bool extend = false, shadow = false;
         uint32_t p = active ? inQueue[i] : 0;
         if (active) {
-            uint32_t info = ws.info[p];
+            uint32_t info = ws.ps[p].info;
             const int sel = (int)(info & kInfoSelMask);
             bool wlSelected = (info & kInfoWlSelected) != 0;
             const bool prevDelta = (info & kInfoPrevDelta) != 0;
             uint32_t depth = info >> kInfoDepthShift;
-            const float wlOff = ws.wlOffset[p];
+            const float wlOff = ws.ps[p].wlOffset;
             float lambdas[kNumLambda];
 #pragma unroll
             for (int k = 0; k < kNumLambda; ++k) lambdas[k] = lambdaAt(k, wlOff);
-            Rng rng{loadKey(ws, p), ws.rngCounter[p]};
-            float4 ro = ws.rayOrg[p], rd = ws.rayDir[p];
+            Rng rng{loadKey(ws, p), ws.ps[p].rngCounter};
+            float4 ro = ws.ray[2 * (size_t)p], rd = ws.ray[2 * (size_t)p + 1];
             V3 org = V3{ro.x, ro.y, ro.z}, dir = V3{rd.x, rd.y, rd.z};
             float4 hv = ws.hit[p];
             uint32_t prim = __float_as_uint(hv.w);
             Spec alpha;
-            loadSpec(ws.alpha, N, p, alpha);
+            loadSpec(ws.alpha, p, alpha);
             bool alive = true;
 
             // Scene::interact (Scene.cpp:66-94): surface hit, then a medium
@@ -837,18 +621,18 @@ __global__ void __launch_bounds__(256, SLRGPU_SHADEVOL_MIN_BLOCKS) kShadeVol(Dev
                 if (emitting) {
                     float mis = 1.0f;
                     if (depth > 0 && !prevDelta) {
-                        float bp = ws.prevPdf[p];
+                        float bp = ws.ps[p].prevPdf;
                         mis = (bp * bp) / (lightPdf * lightPdf + bp * bp);
                     }
                     Spec add;
 #pragma unroll
                     for (int k = 0; k < kNumLambda; ++k) add.v[k] = alpha.v[k] * Le.v[k] * mis;
-                    addSpec(ws.L, N, p, add);
+                    addSpec(ws.L, p, add);
                 }
                 if (atInf) alive = false;
             }
             if (alive && depth > 0) {
-                float cp = fminf(importance(alpha, sel) / ws.initY[p], 1.0f);
+                float cp = fminf(importance(alpha, sel) / ws.ps[p].initY, 1.0f);
                 if (rng.next() < cp) {
                     float r = 1.0f / cp;
 #pragma unroll
@@ -951,7 +735,7 @@ __global__ void __launch_bounds__(256, SLRGPU_SHADEVOL_MIN_BLOCKS) kShadeVol(Dev
                         nz |= c.v[k] != 0.0f;
                     }
                     if (nz) {
-                        storeSpec(ws.shContrib, N, p, c);
+                        storeSpec(ws.shContrib, p, c);
                         float tmax;
                         V3 sdir;
                         if (lAtInf) {
@@ -963,8 +747,8 @@ __global__ void __launch_bounds__(256, SLRGPU_SHADEVOL_MIN_BLOCKS) kShadeVol(Dev
                             sdir = dd * (1.0f / dist);
                             tmax = dist * (1 - kRayEpsilon);
                         }
-                        ws.shOrg[p] = make_float4(P.x, P.y, P.z, kRayEpsilon);
-                        ws.shDir[p] = make_float4(sdir.x, sdir.y, sdir.z, tmax);
+                        ws.shRay[2 * (size_t)p] = make_float4(P.x, P.y, P.z, kRayEpsilon);
+                        ws.shRay[2 * (size_t)p + 1] = make_float4(sdir.x, sdir.y, sdir.z, tmax);
                         shadow = true;
                     }
                 }
@@ -995,21 +779,21 @@ __global__ void __launch_bounds__(256, SLRGPU_SHADEVOL_MIN_BLOCKS) kShadeVol(Dev
                     float r = 1.0f / bs.pdf;
 #pragma unroll
                     for (int k = 0; k < kNumLambda; ++k) alpha.v[k] *= (fs.v[k] * cg) * r;
-                    ws.rayOrg[p] = make_float4(P.x, P.y, P.z, kRayEpsilon);
-                    ws.rayDir[p] = make_float4(nd.x, nd.y, nd.z, inf);
-                    ws.prevPdf[p] = bs.pdf;
+                    ws.ray[2 * (size_t)p] = make_float4(P.x, P.y, P.z, kRayEpsilon);
+                    ws.ray[2 * (size_t)p + 1] = make_float4(nd.x, nd.y, nd.z, inf);
+                    ws.ps[p].prevPdf = bs.pdf;
                     info = (uint32_t)sel | (wlSelected ? kInfoWlSelected : 0u) |
                            (dirIsDelta(bs.type) ? kInfoPrevDelta : 0u) | (depth << kInfoDepthShift);
-                    ws.info[p] = info;
-                    storeSpec(ws.alpha, N, p, alpha);
+                    ws.ps[p].info = info;
+                    storeSpec(ws.alpha, p, alpha);
                     extend = true;
                 }
             }
             if (!extend) {
                 // keep the wavelength-selection flag for the shadow kernel
-                ws.info[p] = (uint32_t)sel | (wlSelected ? kInfoWlSelected : 0u) | (depth << kInfoDepthShift);
+                ws.ps[p].info = (uint32_t)sel | (wlSelected ? kInfoWlSelected : 0u) | (depth << kInfoDepthShift);
             }
-            ws.rngCounter[p] = rng.counter;
+            ws.ps[p].rngCounter = rng.counter;
         }
         queuePush(shQueue, shCount, p, active && shadow);
         queuePush(outQueue, outCount, p, active && extend);
@@ -1028,14 +812,14 @@ __global__ void kShadowVol(DevScene sc, WaveState ws, const uint32_t* __restrict
         uint32_t p = 0;
         if (i < n) {
             p = queue[i];
-            float4 o = ws.shOrg[p], d = ws.shDir[p];
+            float4 o = ws.shRay[2 * (size_t)p], d = ws.shRay[2 * (size_t)p + 1];
             if (!traceAny(sc, V3{o.x, o.y, o.z}, V3{d.x, d.y, d.z}, o.w, d.w)) {
                 if (sc.medium.present) {
                     pushMedium = true;
                 } else {
-#pragma unroll
-                    for (int k = 0; k < kNumLambda; ++k)
-                        ws.L[(size_t)k * ws.N + p] += ws.shContrib[(size_t)k * ws.N + p];
+                    Spec c;
+                    loadSpec(ws.shContrib, p, c);
+                    addSpec(ws.L, p, c);
                 }
             }
         }
@@ -1058,12 +842,12 @@ __global__ void __launch_bounds__(256, SLRGPU_MEDIUM_MIN_BLOCKS) kShadowVolMediu
     for (uint32_t item = blockIdx.x * blockDim.x + threadIdx.x; item < n; item += gridDim.x * blockDim.x) {
         const uint32_t p = queue[item / kNumLambda];
         const int wl = (int)(item % kNumLambda);
-        float4 o = ws.shOrg[p], d = ws.shDir[p];
-        const uint32_t info = ws.info[p];
+        float4 o = ws.shRay[2 * (size_t)p], d = ws.shRay[2 * (size_t)p + 1];
+        const uint32_t info = ws.ps[p].info;
         const int sel = (int)(info & kInfoSelMask);
         const bool wlSelected = (info & kInfoWlSelected) != 0;
         float lambdas[kNumLambda];
-        const float wlOff = ws.wlOffset[p];
+        const float wlOff = ws.ps[p].wlOffset;
 #pragma unroll
         for (int k = 0; k < kNumLambda; ++k) lambdas[k] = lambdaAt(k, wlOff);
         Spec sigmaE;
@@ -1072,7 +856,7 @@ __global__ void __launch_bounds__(256, SLRGPU_MEDIUM_MIN_BLOCKS) kShadowVolMediu
         Rng rng{mix64(loadKey(ws, p) ^ (0x9e3779b97f4a7c15ull * (bounce + 1))), (uint32_t)wl << 24};
         const float T = mediumTransmittanceWl(sc.medium, V3{o.x, o.y, o.z}, V3{d.x, d.y, d.z}, o.w, d.w, sig,
                                               !wlSelected || wl == sel, rng);
-        const size_t k = (size_t)wl * ws.N + p;
+        const size_t k = (size_t)p * kNumLambda + wl;
         if (T != 0.0f) ws.L[k] += T * ws.shContrib[k];
     }
 }
@@ -1106,16 +890,18 @@ __global__ void kAccumulate(WaveState ws, const __grid_constant__ WaveParams wpA
         for (uint32_t gy = y; gy < yEnd; ++gy)
         for (uint32_t gx = x; gx < xEnd; ++gx) {
             const uint32_t p = sg.pathBegin + s * sg.gridPositions + gy * sg.gridW + gx;
-            float w = ws.camWeight[p];
+            float w = ws.ps[p].camWeight;
+            Spec Lp;
+            loadSpec(ws.L, p, Lp);
             float c[kNumLambda];
             bool finite = true;
 #pragma unroll
             for (int i = 0; i < kNumLambda; ++i) {
-                c[i] = ws.L[(size_t)i * ws.N + p] * w;
+                c[i] = Lp.v[i] * w;
                 finite &= isfinite(c[i]);
             }
             if (!finite) { ++dropped; continue; }
-            float wlOff = ws.wlOffset[p];
+            float wlOff = ws.ps[p].wlOffset;
             float addend[kNumLambda];
 #pragma unroll
             for (int b = 0; b < kNumLambda; ++b) addend[b] = 0.0f;
@@ -1423,20 +1209,12 @@ int RenderEngine::ensure(uint32_t N, uint32_t maxDepth) {
     WaveState* w = new WaveState();
     std::memset(w, 0, sizeof(*w));
     w->N = N;
-    w->rayOrg = allocDev<float4>(allocs, N, &e); if (!w->rayOrg) goto fail;
-    w->rayDir = allocDev<float4>(allocs, N, &e); if (!w->rayDir) goto fail;
+    w->ray = allocDev<float4>(allocs, 2ull * N, &e); if (!w->ray) goto fail;
     w->hit = allocDev<float4>(allocs, N, &e); if (!w->hit) goto fail;
     w->alpha = allocDev<float>(allocs, (size_t)N * kNumLambda, &e); if (!w->alpha) goto fail;
     w->L = allocDev<float>(allocs, (size_t)N * kNumLambda, &e); if (!w->L) goto fail;
-    w->info = allocDev<uint32_t>(allocs, N, &e); if (!w->info) goto fail;
-    w->wlOffset = allocDev<float>(allocs, N, &e); if (!w->wlOffset) goto fail;
-    w->prevPdf = allocDev<float>(allocs, N, &e); if (!w->prevPdf) goto fail;
-    w->initY = allocDev<float>(allocs, N, &e); if (!w->initY) goto fail;
-    w->camWeight = allocDev<float>(allocs, N, &e); if (!w->camWeight) goto fail;
-    w->rngCounter = allocDev<uint32_t>(allocs, N, &e); if (!w->rngCounter) goto fail;
-    w->rngKey = allocDev<uint2>(allocs, N, &e); if (!w->rngKey) goto fail;
-    w->shOrg = allocDev<float4>(allocs, N, &e); if (!w->shOrg) goto fail;
-    w->shDir = allocDev<float4>(allocs, N, &e); if (!w->shDir) goto fail;
+    w->ps = allocDev<PathScalars>(allocs, N, &e); if (!w->ps) goto fail;
+    w->shRay = allocDev<float4>(allocs, 2ull * N, &e); if (!w->shRay) goto fail;
     w->shContrib = allocDev<float>(allocs, (size_t)N * kNumLambda, &e); if (!w->shContrib) goto fail;
     w->queue[0] = allocDev<uint32_t>(allocs, N, &e); if (!w->queue[0]) goto fail;
     w->queue[1] = allocDev<uint32_t>(allocs, N, &e); if (!w->queue[1]) goto fail;
@@ -1453,6 +1231,25 @@ fail:
     release();
     setError(std::string("path state allocation failed: ") + cudaGetErrorString(e));
     return SLRGPU_ERR_OUT_OF_MEMORY;
+}
+
+RenderEngine::~RenderEngine() {
+    release();
+    if (bpt) bptEngineDestroy(bpt);
+}
+
+int RenderEngine::ensureFilm(uint32_t P) {
+    if (filmPixels >= P) return SLRGPU_OK;
+    if (filmSum) cudaFree(filmSum);
+    if (filmComp) cudaFree(filmComp);
+    if (filmOut) cudaFree(filmOut);
+    filmSum = filmComp = filmOut = nullptr;
+    filmPixels = 0;
+    CUDA_TRY(cudaMalloc(&filmSum, (size_t)P * kNumLambda * sizeof(float)));
+    CUDA_TRY(cudaMalloc(&filmComp, (size_t)P * kNumLambda * sizeof(float)));
+    CUDA_TRY(cudaMalloc(&filmOut, (size_t)P * kNumLambda * sizeof(float)));
+    filmPixels = P;
+    return SLRGPU_OK;
 }
 
 void RenderEngine::release() {
@@ -1693,37 +1490,46 @@ int RenderEngine::render(const DeviceScene &ds, const slrgpu_settings &s, float*
         setError("image too large");
         return SLRGPU_ERR_INVALID_ARGUMENT;
     }
+    const bool bidir = (s.flags & SLRGPU_FLAG_BPT) != 0;
     const WavePlan pl = planWaves(s, SLRGPU_WAVE_PATHS);
     const uint32_t P = pl.filmPixels;
-    const uint64_t Nwant = (uint64_t)pl.S * pl.gridPositions;
-    if (Nwant > 0x7fffffffull) {
-        setError("paths per wave exceed 2^31");
-        return SLRGPU_ERR_INVALID_ARGUMENT;
+    if (!bidir) {
+        const uint64_t Nwant = (uint64_t)pl.S * pl.gridPositions;
+        if (Nwant > 0x7fffffffull) {
+            setError("paths per wave exceed 2^31");
+            return SLRGPU_ERR_INVALID_ARGUMENT;
+        }
+        int rc = ensure((uint32_t)Nwant, s.max_depth);
+        if (rc != SLRGPU_OK) return rc;
+    } else if (!bpt) {
+        bpt = bptEngineCreate();
     }
-    int rc = ensure((uint32_t)Nwant, s.max_depth);
+    int rc = ensureFilm(P);
     if (rc != SLRGPU_OK) return rc;
-    if (filmPixels < P) {
-        if (filmSum) cudaFree(filmSum);
-        if (filmComp) cudaFree(filmComp);
-        if (filmOut) cudaFree(filmOut);
-        filmSum = filmComp = filmOut = nullptr;
-        CUDA_TRY(cudaMalloc(&filmSum, (size_t)P * kNumLambda * sizeof(float)));
-        CUDA_TRY(cudaMalloc(&filmComp, (size_t)P * kNumLambda * sizeof(float)));
-        CUDA_TRY(cudaMalloc(&filmOut, (size_t)P * kNumLambda * sizeof(float)));
-        filmPixels = P;
-    }
-    WaveState w = *ws;
     CUDA_TRY(cudaMemsetAsync(filmSum, 0, (size_t)P * kNumLambda * sizeof(float), stream));
     CUDA_TRY(cudaMemsetAsync(filmComp, 0, (size_t)P * kNumLambda * sizeof(float), stream));
-    CUDA_TRY(cudaMemsetAsync(w.stats, 0, 4 * sizeof(unsigned long long), stream));
+    if (!bidir) CUDA_TRY(cudaMemsetAsync(ws->stats, 0, 4 * sizeof(unsigned long long), stream));
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     cudaEventRecord(e0, stream);
+    const bool profile = (s.flags & SLRGPU_FLAG_PROFILE_KERNELS) != 0;
     LaunchMarks lm;
     lm.stream = stream;
-    if (s.flags & SLRGPU_FLAG_PROFILE_KERNELS) lm.pool = &eventPool;
-    uint64_t launches = runWaves(ds, s, pl, w, filmSum, filmComp, stream, lm);
+    if (profile) lm.pool = &eventPool;
+    uint64_t launches = 0;
+    slrgpu_render_stats bst;
+    std::memset(&bst, 0, sizeof(bst));
+    if (bidir) {
+        rc = renderBpt(*bpt, ds, s, filmSum, filmComp, stream, &launches, profile ? &eventPool : nullptr, &bst);
+        if (rc != SLRGPU_OK) {
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            return rc;
+        }
+    } else {
+        launches = runWaves(ds, s, pl, *ws, filmSum, filmComp, stream, lm);
+    }
     CUDA_TRY(cudaGetLastError());
     float* dst = filmOnDevice ? film : filmOut;
     kFilmToPixelMajor<<<waveGrids(256).accumulate, 256, 0, stream>>>(filmSum, dst, P);
@@ -1732,7 +1538,7 @@ int RenderEngine::render(const DeviceScene &ds, const slrgpu_settings &s, float*
     if (!filmOnDevice)
         CUDA_TRY(cudaMemcpyAsync(film, filmOut, (size_t)P * kNumLambda * sizeof(float), cudaMemcpyDeviceToHost, stream));
     unsigned long long hstats[4] = {0, 0, 0, 0};
-    CUDA_TRY(cudaMemcpyAsync(hstats, w.stats, sizeof(hstats), cudaMemcpyDeviceToHost, stream));
+    if (!bidir) CUDA_TRY(cudaMemcpyAsync(hstats, ws->stats, sizeof(hstats), cudaMemcpyDeviceToHost, stream));
     CUDA_TRY(cudaStreamSynchronize(stream));
     float ms = 0;
     cudaEventElapsedTime(&ms, e0, e1);
@@ -1740,6 +1546,13 @@ int RenderEngine::render(const DeviceScene &ds, const slrgpu_settings &s, float*
     cudaEventDestroy(e1);
     if (stats) {
         std::memset(stats, 0, sizeof(*stats));
+        if (bidir) {
+            std::memcpy(stats->kernel_ms, bst.kernel_ms, sizeof(stats->kernel_ms));
+            std::memcpy(stats->kernel_count, bst.kernel_count, sizeof(stats->kernel_count));
+            hstats[0] = bst.extension_rays;
+            hstats[1] = bst.shadow_rays;
+            hstats[2] = bst.dropped_samples;
+        }
         for (const LaunchMarks::Mark &m : lm.marks) {
             float kms = 0;
             cudaEventElapsedTime(&kms, eventPool[m.ev], eventPool[m.ev + 1]);
@@ -1774,21 +1587,13 @@ constexpr uint32_t kNoAllocMaxPaths = 65536;
 constexpr uint32_t kNoAllocMaxDepth = 64;
 
 constexpr size_t naAlign(size_t x) { return (x + 255) & ~(size_t)255; }
-constexpr size_t kNaRayOrg = 0;
-constexpr size_t kNaRayDir = naAlign(kNaRayOrg + 16ull * kNoAllocMaxPaths);
-constexpr size_t kNaHit = naAlign(kNaRayDir + 16ull * kNoAllocMaxPaths);
+constexpr size_t kNaRay = 0;
+constexpr size_t kNaHit = naAlign(kNaRay + 32ull * kNoAllocMaxPaths);
 constexpr size_t kNaAlpha = naAlign(kNaHit + 16ull * kNoAllocMaxPaths);
 constexpr size_t kNaL = naAlign(kNaAlpha + 4ull * kNumLambda * kNoAllocMaxPaths);
-constexpr size_t kNaInfo = naAlign(kNaL + 4ull * kNumLambda * kNoAllocMaxPaths);
-constexpr size_t kNaWlOffset = naAlign(kNaInfo + 4ull * kNoAllocMaxPaths);
-constexpr size_t kNaPrevPdf = naAlign(kNaWlOffset + 4ull * kNoAllocMaxPaths);
-constexpr size_t kNaInitY = naAlign(kNaPrevPdf + 4ull * kNoAllocMaxPaths);
-constexpr size_t kNaCamWeight = naAlign(kNaInitY + 4ull * kNoAllocMaxPaths);
-constexpr size_t kNaRngCounter = naAlign(kNaCamWeight + 4ull * kNoAllocMaxPaths);
-constexpr size_t kNaRngKey = naAlign(kNaRngCounter + 4ull * kNoAllocMaxPaths);
-constexpr size_t kNaShOrg = naAlign(kNaRngKey + 8ull * kNoAllocMaxPaths);
-constexpr size_t kNaShDir = naAlign(kNaShOrg + 16ull * kNoAllocMaxPaths);
-constexpr size_t kNaShContrib = naAlign(kNaShDir + 16ull * kNoAllocMaxPaths);
+constexpr size_t kNaScalars = naAlign(kNaL + 4ull * kNumLambda * kNoAllocMaxPaths);
+constexpr size_t kNaShRay = naAlign(kNaScalars + sizeof(PathScalars) * kNoAllocMaxPaths);
+constexpr size_t kNaShContrib = naAlign(kNaShRay + 32ull * kNoAllocMaxPaths);
 constexpr size_t kNaQueue0 = naAlign(kNaShContrib + 4ull * kNumLambda * kNoAllocMaxPaths);
 constexpr size_t kNaQueue1 = naAlign(kNaQueue0 + 4ull * kNoAllocMaxPaths);
 constexpr size_t kNaShQueue = naAlign(kNaQueue1 + 4ull * kNoAllocMaxPaths);
@@ -1859,20 +1664,12 @@ int renderNoAlloc(const DeviceScene &ds, const slrgpu_settings &s, float* film, 
     WaveState w;
     std::memset(&w, 0, sizeof(w));
     w.N = pl.S * pl.gridPositions;
-    w.rayOrg = (float4*)(base + kNaRayOrg);
-    w.rayDir = (float4*)(base + kNaRayDir);
+    w.ray = (float4*)(base + kNaRay);
     w.hit = (float4*)(base + kNaHit);
     w.alpha = (float*)(base + kNaAlpha);
     w.L = (float*)(base + kNaL);
-    w.info = (uint32_t*)(base + kNaInfo);
-    w.wlOffset = (float*)(base + kNaWlOffset);
-    w.prevPdf = (float*)(base + kNaPrevPdf);
-    w.initY = (float*)(base + kNaInitY);
-    w.camWeight = (float*)(base + kNaCamWeight);
-    w.rngCounter = (uint32_t*)(base + kNaRngCounter);
-    w.rngKey = (uint2*)(base + kNaRngKey);
-    w.shOrg = (float4*)(base + kNaShOrg);
-    w.shDir = (float4*)(base + kNaShDir);
+    w.ps = (PathScalars*)(base + kNaScalars);
+    w.shRay = (float4*)(base + kNaShRay);
     w.shContrib = (float*)(base + kNaShContrib);
     w.queue[0] = (uint32_t*)(base + kNaQueue0);
     w.queue[1] = (uint32_t*)(base + kNaQueue1);

@@ -29,10 +29,12 @@ struct DeviceScene {
 };
 
 struct WaveState;
+struct BptEngine;   // bidirectional path state (bpt.cu)
 
 // Per-context path state and film buffers, grown on demand.
 struct RenderEngine {
     WaveState* ws = nullptr;
+    BptEngine* bpt = nullptr;
     std::vector<void*> allocs;
     uint32_t capacity = 0;
     uint32_t depthCapacity = 0;
@@ -43,11 +45,21 @@ struct RenderEngine {
     std::vector<cudaEvent_t> eventPool;
 
     int ensure(uint32_t paths, uint32_t maxDepth);
+    int ensureFilm(uint32_t pixels);
     void release();
     int render(const DeviceScene &ds, const slrgpu_settings &s, float* film, bool filmOnDevice,
                slrgpu_render_stats* stats, cudaStream_t stream);
-    ~RenderEngine() { release(); }
+    ~RenderEngine();
 };
+
+// Bidirectional path tracing (BPTRenderer) into a compensated 16-bin film
+// ([16][width * height] sum and compensation planes on the device, added
+// to).  eventPool non-null: per-kernel timing into stats->kernel_ms.
+BptEngine* bptEngineCreate();
+void bptEngineDestroy(BptEngine* e);
+int renderBpt(BptEngine &eng, const DeviceScene &ds, const slrgpu_settings &s, float* filmSum, float* filmComp,
+              cudaStream_t stream, uint64_t* launches, std::vector<cudaEvent_t>* eventPool,
+              slrgpu_render_stats* stats);
 
 // Wave slots (serving): path state for up to `paths` paths in flight.
 struct WaveSlot;

@@ -12,6 +12,7 @@ All scenes are synthetic and seeded; nothing is read from disk.
 """
 from __future__ import annotations
 
+import dataclasses
 import math
 
 import numpy as np
@@ -99,6 +100,34 @@ def box_scene(width: int = 256, height: int = 256) -> SceneDesc:
     d.camera = Camera("perspective", look_at((0.5, 0.5, 2.3), (0.5, 0.5, 0.0)), sensitivity=1.0,
                       aspect=width / height, fov_y=math.radians(38.0), lens_radius=0.0,
                       img_plane_dist=1.0, obj_plane_dist=2.3)
+    return d
+
+
+def glossy_box_scene(width: int = 256, height: int = 256) -> SceneDesc:
+    """The box scene with every BSDF kind under its ceiling light: the tall
+    block a rough GGX conductor (anisotropic), the short block smooth glass
+    (delta reflection / refraction), a small floating block rough GGX glass
+    and a mirror (delta conductor) on the back wall.  No environment, so both
+    the unidirectional and the bidirectional tracers take it."""
+    d = box_scene(width, height)
+    white = 0
+
+    def flat(v):
+        return d.spectrum_regular(np.array([v, v], np.float32), 360.0, 830.0)
+
+    metal = d.material("microfacet_reflection", (flat(1.5), flat(2.0)), 0.3, 0.15)
+    glass = d.material("specular_scattering", (d.spectrum_rgb(REFLECTANCE, 1.0, 1.0, 1.0), flat(1.0), flat(1.5)))
+    rough_glass = d.material("microfacet_scattering", (flat(1.0), flat(1.45)), 0.2, 0.2)
+    mirror = d.material("specular_reflection", (d.spectrum_rgb(REFLECTANCE, 0.95, 0.95, 0.95), flat(0.2), flat(3.0)))
+    # the two blocks of the box scene are its last two white meshes before the light
+    blocks = [i for i, m in enumerate(d.meshes) if m.material == white][-2:]
+    d.meshes[blocks[0]] = dataclasses.replace(d.meshes[blocks[0]], material=glass)
+    d.meshes[blocks[1]] = dataclasses.replace(d.meshes[blocks[1]], material=metal)
+    p, idx = _box((0.5, 0.62, 0.55), (0.12, 0.12, 0.12), 0.7)
+    d.mesh(p, idx, rough_glass)
+    q, qidx = _quad((0.55, 0.3, 0.001), (0.9, 0.3, 0.001), (0.9, 0.75, 0.001), (0.55, 0.75, 0.001))
+    nrm = np.tile(np.array((0, 0, 1), np.float32), (4, 1))
+    d.mesh(q, qidx, mirror, normals=nrm, tangents=_tangent_for(nrm), uvs=_quad_uv())
     return d
 
 
