@@ -68,11 +68,13 @@ BYTES_SHADE = 792
 BYTES_FILM = 256
 # Bidirectional tracer: per traced subpath vertex (ray 32 B + state 16 B +
 # throughput 64 B in; vertex record 160 B, throughput 64 B, ray and state
-# 48 B, previous vertex's reverse densities 8 B out; closest hit 48 B) and
-# per connection (light vertex 160 B, its predecessor 64 B, two density
-# records per MIS term ~64 B, shadow query 36 B, contribution 64 B).
+# 48 B, previous vertex's reverse densities 8 B out; closest hit 48 B), per
+# evaluated connection with a contribution (light vertex 160 B, its
+# predecessor 64 B, two density records per MIS term ~64 B, queued
+# connection 100 B out) and per shadow ray.
 BYTES_BPT_BOUNCE = 440
 BYTES_BPT_CONNECT = 390
+BYTES_BPT_SHADOW = 164   # queued connection 100 B in, any-hit query, 64 B atomic add out
 
 # DRAM bytes per unit of the dominant kernel class measured by ncu
 # (dram__bytes_read.sum + dram__bytes_write.sum over the class's launches of
@@ -553,8 +555,8 @@ def main():
     units = {1: (ext_rays, BYTES_EXTEND), 3: (sh_rays, BYTES_SHADOW), 2: (ext_rays, BYTES_SHADE),
              0: (samples_per_step * args.steps, 64), 4: (samples_per_step * args.steps, BYTES_FILM)}
     if BPT:
-        units.update({1: (ext_rays, BYTES_BPT_BOUNCE), 3: (sh_rays, BYTES_BPT_CONNECT),
-                      0: (samples_per_step * args.steps, 2 * 160 + 96)})
+        units.update({1: (ext_rays, BYTES_BPT_BOUNCE), 2: (sh_rays, BYTES_BPT_CONNECT),
+                      3: (sh_rays, BYTES_BPT_SHADOW), 0: (samples_per_step * args.steps, 2 * 160 + 96)})
     n_units, per_unit = units[dom]
     bytes_per_launch = n_units * per_unit / max(1, kern_n[dom])
     avg_launch_s = kern_ms[dom] * 1e-3 / max(1, kern_n[dom])
@@ -570,7 +572,8 @@ def main():
         roofline["traffic"] = measured * n_units / max(1, kern_n[dom])
         roofline["traffic_source"] = "ncu dram bytes per unit (profiles/dram_ggx_ibl_1m.md) x units per launch"
     if BPT:   # the bidirectional tracer's kernels behind the classes
-        roofline["kernel"] = {0: "kBptInit", 1: "kBptBounce", 3: "kBptConnect", 4: "kBptAccumulate"}.get(dom, names[dom])
+        roofline["kernel"] = {0: "kBptInit", 1: "kBptBounce", 2: "kBptConnect", 3: "kBptShadow",
+                              4: "kBptAccumulate"}.get(dom, names[dom])
     line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",

@@ -35,6 +35,12 @@
 
 namespace slrgpu {
 
+// Resident blocks per SM the traversal kernels are compiled for (the path
+// tracer's tuned value).
+#ifndef SLRGPU_TRACE_MIN_BLOCKS
+#define SLRGPU_TRACE_MIN_BLOCKS 4
+#endif
+
 namespace {
 
 // Vertex kinds.
@@ -90,11 +96,16 @@ struct BptState {
     float* wlOffset;      // [N]
     uint32_t* sel;        // [N]
     float* L;             // [N][16] contributions at the path's own pixel
-    float* splat;         // [16][pixels] contributions through the lens vertex
+    float* splat;         // [pixels][16] contributions through the lens vertex (film bins)
     uint32_t splatPixels;
     uint32_t* queue[2];   // [S]
     uint32_t* connQueue;  // [N * (D + 1)] eye vertex indices
-    uint32_t* counters;   // [D + 2] queue sizes per bounce, then the connection count
+    // connections that contribute, waiting for their shadow ray
+    uint32_t connCap;
+    float4* cRay;         // [connCap * 2] origin + tmin, direction + tmax
+    float4* cContrib;     // [connCap * 4] contribution (film bins when splatted)
+    uint32_t* cTarget;    // [connCap] path index, or pixel | kTargetSplat
+    uint32_t* counters;   // [D + 3] queue sizes per bounce, eye vertices to connect, queued connections
     unsigned long long* stats;   // 0 extension rays, 1 shadow rays, 2 dropped contributions
 };
 
@@ -532,176 +543,260 @@ __device__ __forceinline__ void vertexBsdf(const DevScene &sc, const BptState &s
     }
 }
 
-// Connections of one eye vertex with every light vertex of its path
-// (BPTRenderer.cpp:174-280).  Contributions to the path's own pixel (t > 1)
-// are summed in registers and added once per eye vertex.
+// One connection (BPTRenderer.cpp:174-280): eye vertex evi (t = its index
+// + 1) with light vertex s of the same path.  Returns false when the
+// connection adds nothing (zero connection term, invalid MIS weight) or is
+// dropped as non-finite (*dropped set); else the shadow ray and the
+// contribution, binned into film bins when it lands through the lens
+// (t = 1, *target = pixel | kTargetSplat) or per wavelength for the path's
+// own sum (*target = path).
+constexpr uint32_t kTargetSplat = 0x80000000u;
+__device__ bool connectOne(const DevScene &sc, const BptState &st, uint32_t evi, uint32_t s, uint32_t width,
+                           uint32_t height, float4* rayOrg, float4* rayDir, Spec &c, uint32_t* target,
+                           bool* dropped) {
+    *dropped = false;
+    const uint32_t k = evi / st.S;            // eye vertex index, t = k + 1
+    const uint32_t esp = evi - k * st.S;
+    const uint32_t p = esp - st.N;
+    const uint32_t t = k + 1;
+    const int sel = (int)st.sel[p];
+    const float wlOff = st.wlOffset[p];
+    float lambdas[kNumLambda];
+#pragma unroll
+    for (int q = 0; q < kNumLambda; ++q) lambdas[q] = lambdaAt(q, wlOff);
+    const BptGeom eg = st.geom[evi];
+    const BptPdf ep = st.pdf[evi];
+    const V3 eP = xyz(eg.pg), eN = xyz(eg.ng);
+    const Frame eF = vertexFrame(eg);
+    const bool eLens = (ep.flags >> kVfKindShift) == kVtxLens;
+    const size_t lvi = (size_t)(s - 1) * st.S + p;
+    const BptGeom lg = st.geom[lvi];
+    const BptPdf lpd = st.pdf[lvi];
+    const V3 lP = xyz(lg.pg), lN = xyz(lg.ng);
+    const Frame lF = vertexFrame(lg);
+    V3 cv = lP - eP;
+    const float dist2 = sqLength(cv);
+    cv = cv * (1.0f / sqrtf(dist2));
+    const float cosLightEnd = absDot(cv, lN);
+    const float cosEyeEnd = absDot(cv, eN);
+    const float G = cosEyeEnd * cosLightEnd / dist2;
+    // light end: EDF of the light vertex or the adjoint BSDF
+    const V3 lc = lF.toLocal(-cv);
+    Spec lDDF, lRev;
+    float lExt1DirPdf, eExt2DirPdf = 0.0f;
+    if (s == 1) {
+        lDDF = specConst(lc.z > 0.0f ? kInvPiF : 0.0f);
+        lRev = lDDF;
+        lExt1DirPdf = lc.z > 0.0f ? lc.z * kInvPiF : 0.0f;
+    } else {
+        Bsdf lB;
+        vertexBsdf(sc, st, lvi, __float_as_uint(lg.pg.w), lpd.flags, lambdas, lB);
+        RevQuery lq{V3{lg.nz.w, lg.tx.w, lg.ng.w}, lF.toLocal(lN), sel, true};
+        bsdfEvalRev(lB, lq, lc, lDDF, lRev);
+        lExt1DirPdf = bsdfPdfRev(lB, lq, lc, &eExt2DirPdf);
+    }
+    // eye end: importance of the lens or the BSDF
+    const V3 ec = eF.toLocal(cv);
+    Spec eDDF, eRev;
+    float eExt1DirPdf, lExt2DirPdf = 0.0f;
+    if (eLens) {
+        eDDF = specConst(idfInside(sc.camera, ec, eg.nz.w, eg.tx.w) ? 1.0f : 0.0f);
+        eRev = eDDF;
+        eExt1DirPdf = idfPdf(sc.camera, ec, eg.nz.w, eg.tx.w);
+    } else {
+        Bsdf eB;
+        vertexBsdf(sc, st, evi, __float_as_uint(eg.pg.w), ep.flags, lambdas, eB);
+        RevQuery eq{V3{eg.nz.w, eg.tx.w, eg.ng.w}, eF.toLocal(eN), sel, false};
+        bsdfEvalRev(eB, eq, ec, eDDF, eRev);
+        eExt1DirPdf = bsdfPdfRev(eB, eq, ec, &lExt2DirPdf);
+    }
+    Spec ct;
+    bool nz = false;
+#pragma unroll
+    for (int q = 0; q < kNumLambda; ++q) {
+        ct.v[q] = lDDF.v[q] * G * eDDF.v[q];
+        nz |= ct.v[q] != 0.0f;
+    }
+    if (!nz) return false;
+    if ((lpd.flags & kVfWlSelected) || (ep.flags & kVfWlSelected)) {
+#pragma unroll
+        for (int q = 0; q < kNumLambda; ++q)
+            if (q == sel) ct.v[q] *= kNumLambda;
+    }
+    // densities of the two subpaths' first and second extensions
+    const float lExt1Area = lExt1DirPdf * cosEyeEnd / dist2;
+    Spec tmp;
+#pragma unroll
+    for (int q = 0; q < kNumLambda; ++q) tmp.v[q] = lDDF.v[q] * cosLightEnd / lExt1DirPdf;
+    const float lExt1RR = s > 1 ? stdMin(importance(tmp, sel), 1.0f) : 1.0f;
+    float lExt2Area = 0.0f, lExt2RR = 0.0f;
+    if (t > 1) {
+        const BptGeom g2 = st.geom[evi - st.S];
+        V3 d2 = eP - xyz(g2.pg);
+        const float dd2 = sqLength(d2);
+        d2 = d2 * (1.0f / sqrtf(dd2));
+        lExt2Area = lExt2DirPdf * absDot(d2, xyz(g2.ng)) / dd2;
+#pragma unroll
+        for (int q = 0; q < kNumLambda; ++q) tmp.v[q] = eRev.v[q] * ep.cosIn / lExt2DirPdf;
+        lExt2RR = stdMin(importance(tmp, sel), 1.0f);
+    }
+    const float eExt1Area = eExt1DirPdf * cosLightEnd / dist2;
+#pragma unroll
+    for (int q = 0; q < kNumLambda; ++q) tmp.v[q] = eDDF.v[q] * cosEyeEnd / eExt1DirPdf;
+    const float eExt1RR = t > 1 ? stdMin(importance(tmp, sel), 1.0f) : 1.0f;
+    float eExt2Area = 0.0f, eExt2RR = 0.0f;
+    if (s > 1) {
+        const BptGeom l2 = st.geom[lvi - st.S];
+        V3 d2 = xyz(l2.pg) - lP;
+        const float dd2 = sqLength(d2);
+        d2 = d2 * (1.0f / sqrtf(dd2));
+        eExt2Area = eExt2DirPdf * absDot(d2, xyz(l2.ng)) / dd2;
+#pragma unroll
+        for (int q = 0; q < kNumLambda; ++q) tmp.v[q] = lRev.v[q] * lpd.cosIn / eExt2DirPdf;
+        eExt2RR = stdMin(importance(tmp, sel), 1.0f);
+    }
+    MisSide eyeSide{st.pdf, st.S, esp, t, 1, lExt1Area, lExt1RR, lExt2Area, lExt2RR};
+    MisSide lightSide{st.pdf, st.S, p, s, 0, eExt1Area, eExt1RR, eExt2Area, eExt2RR};
+    const float mis = misWeight(eyeSide, lightSide);
+    if (isinf(mis) || isnan(mis)) return false;
+    Spec lAlpha, eAlpha;
+    loadAlpha(st.alpha, lvi, lAlpha);
+    loadAlpha(st.alpha, evi, eAlpha);
+    bool finite = true;
+#pragma unroll
+    for (int q = 0; q < kNumLambda; ++q) {
+        c.v[q] = ((mis * lAlpha.v[q]) * ct.v[q]) * eAlpha.v[q];
+        finite &= isfinite(c.v[q]);
+    }
+    if (!finite) {
+        *dropped = true;
+        return false;
+    }
+    // Scene::testVisibility (Scene.cpp:96-112)
+    const float dist = length(lP - eP);
+    const V3 sd = (lP - eP) * (1.0f / dist);
+    *rayOrg = make_float4(eP.x, eP.y, eP.z, kRayEpsilon);
+    *rayDir = make_float4(sd.x, sd.y, sd.z, dist * (1 - kRayEpsilon));
+    if (t > 1) {
+        *target = p;
+        return true;
+    }
+    float hx, hy;
+    idfPixel(sc.camera, ec, eg.nz.w, eg.tx.w, width, height, &hx, &hy);
+    const uint32_t ipx = min((uint32_t)fmaxf(hx, 0.0f), width - 1);
+    const uint32_t ipy = min((uint32_t)fmaxf(hy, 0.0f), height - 1);
+    *target = (ipy * width + ipx) | kTargetSplat;
+    // SpectrumStorage::add (spectrum_types.h:725-734): wavelength -> film bin
+    const float recBinWidth = kNumLambda / (kWavelengthHigh - kWavelengthLow);
+    Spec binned = specConst(0.0f);
+#pragma unroll
+    for (int q = 0; q < kNumLambda; ++q) {
+        const float f = __fmul_rn(__fdiv_rn(__fsub_rn(lambdas[q], kWavelengthLow), kWavelengthHigh - kWavelengthLow),
+                                  (float)kNumLambda);
+        const uint32_t bin = min((uint32_t)f, (uint32_t)(kNumLambda - 1));
+#pragma unroll
+        for (int b = 0; b < kNumLambda; ++b)
+            if (b == (int)bin) binned.v[b] += c.v[q] * recBinWidth;
+    }
+    c = binned;
+    return true;
+}
+
+// Adds an unoccluded connection to the path's sum or, through the lens,
+// to the splat film (both [.][16], four 16-byte atomic additions).
+__device__ __forceinline__ void addConnection(const BptState &st, uint32_t target, const Spec &c) {
+    float4* dst = reinterpret_cast<float4*>((target & kTargetSplat) ? st.splat : st.L) +
+                  (size_t)(target & ~kTargetSplat) * (kNumLambda / 4);
+#pragma unroll
+    for (int k = 0; k < kNumLambda / 4; ++k) {
+        const float4 v = make_float4(c.v[4 * k], c.v[4 * k + 1], c.v[4 * k + 2], c.v[4 * k + 3]);
+        if (v.x != 0.0f || v.y != 0.0f || v.z != 0.0f || v.w != 0.0f) atomicAdd(dst + k, v);
+    }
+}
+
+// Connections of the queued eye vertices with every light vertex of their
+// paths, spread over the lanes of a warp: a warp takes 32 eye vertices,
+// prefix-sums their light-subpath lengths and gives each lane one
+// (eye vertex, light vertex) pair per round, so lanes stay busy whatever the
+// subpath lengths.  Connections that contribute go to the shadow queue (or,
+// when it is full, are traced here).
 __global__ void __launch_bounds__(256, 2) kBptConnect(DevScene sc, BptState st, uint32_t width, uint32_t height,
                                                       const uint32_t* __restrict__ queue,
-                                                      const uint32_t* __restrict__ count) {
+                                                      const uint32_t* __restrict__ count, uint32_t* shCount) {
     const uint32_t n = *count;
-    const float recBinWidth = kNumLambda / (kWavelengthHigh - kWavelengthLow);
-    unsigned long long shadowRays = 0;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const uint32_t evi = queue[i];
-        const uint32_t k = evi / st.S;            // eye vertex index, t = k + 1
-        const uint32_t esp = evi - k * st.S;
-        const uint32_t p = esp - st.N;
-        const uint32_t t = k + 1;
-        const uint32_t nL = st.numVerts[p];
-        const int sel = (int)st.sel[p];
-        const float wlOff = st.wlOffset[p];
-        float lambdas[kNumLambda];
-#pragma unroll
-        for (int q = 0; q < kNumLambda; ++q) lambdas[q] = lambdaAt(q, wlOff);
-        const BptGeom eg = st.geom[evi];
-        const BptPdf ep = st.pdf[evi];
-        const V3 eP = xyz(eg.pg), eN = xyz(eg.ng);
-        const Frame eF = vertexFrame(eg);
-        const bool eLens = (ep.flags >> kVfKindShift) == kVtxLens;
-        Bsdf eB;
-        RevQuery eq{V3{eg.nz.w, eg.tx.w, eg.ng.w}, eF.toLocal(eN), sel, false};
-        if (!eLens) vertexBsdf(sc, st, evi, __float_as_uint(eg.pg.w), ep.flags, lambdas, eB);
-        // the eye vertex before this one (t > 1)
-        V3 e2P{0, 0, 0}, e2N{0, 0, 0};
-        if (t > 1) {
-            const BptGeom g2 = st.geom[evi - st.S];
-            e2P = xyz(g2.pg);
-            e2N = xyz(g2.ng);
+    const uint32_t lane = threadIdx.x & 31;
+    const unsigned full = 0xffffffffu;
+    unsigned long long dropped = 0, traced = 0;
+    for (uint32_t base = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u; base < n; base += gridDim.x * blockDim.x) {
+        const uint32_t item = base + lane;
+        uint32_t evi = 0, nL = 0;
+        if (item < n) {
+            evi = queue[item];
+            const uint32_t p = evi % st.S - st.N;
+            nL = st.numVerts[p];
         }
-        Spec eAlpha;
-        loadAlpha(st.alpha, evi, eAlpha);
-        Spec own = specConst(0.0f);
-        for (uint32_t s = 1; s <= nL; ++s) {
-            const size_t lvi = (size_t)(s - 1) * st.S + p;
-            const BptGeom lg = st.geom[lvi];
-            const BptPdf lpd = st.pdf[lvi];
-            const V3 lP = xyz(lg.pg), lN = xyz(lg.ng);
-            const Frame lF = vertexFrame(lg);
-            V3 cv = lP - eP;
-            const float dist2 = sqLength(cv);
-            cv = cv * (1.0f / sqrtf(dist2));
-            const float cosLightEnd = absDot(cv, lN);
-            const float cosEyeEnd = absDot(cv, eN);
-            const float G = cosEyeEnd * cosLightEnd / dist2;
-            // light end: EDF of the light vertex or the adjoint BSDF
-            const V3 lc = lF.toLocal(-cv);
-            Spec lDDF, lRev;
-            float lExt1DirPdf, eExt2DirPdf = 0.0f;
-            if (s == 1) {
-                lDDF = specConst(lc.z > 0.0f ? kInvPiF : 0.0f);
-                lRev = lDDF;
-                lExt1DirPdf = lc.z > 0.0f ? lc.z * kInvPiF : 0.0f;
-            } else {
-                Bsdf lB;
-                vertexBsdf(sc, st, lvi, __float_as_uint(lg.pg.w), lpd.flags, lambdas, lB);
-                RevQuery lq{V3{lg.nz.w, lg.tx.w, lg.ng.w}, lF.toLocal(lN), sel, true};
-                bsdfEvalRev(lB, lq, lc, lDDF, lRev);
-                lExt1DirPdf = bsdfPdfRev(lB, lq, lc, &eExt2DirPdf);
-            }
-            // eye end: importance of the lens or the BSDF
-            const V3 ec = eF.toLocal(cv);
-            Spec eDDF, eRev;
-            float eExt1DirPdf, lExt2DirPdf = 0.0f;
-            if (eLens) {
-                eDDF = specConst(idfInside(sc.camera, ec, eg.nz.w, eg.tx.w) ? 1.0f : 0.0f);
-                eRev = eDDF;
-                eExt1DirPdf = idfPdf(sc.camera, ec, eg.nz.w, eg.tx.w);
-            } else {
-                bsdfEvalRev(eB, eq, ec, eDDF, eRev);
-                eExt1DirPdf = bsdfPdfRev(eB, eq, ec, &lExt2DirPdf);
-            }
-            Spec ct;
-            bool nz = false;
+        uint32_t incl = nL;
 #pragma unroll
-            for (int q = 0; q < kNumLambda; ++q) {
-                ct.v[q] = lDDF.v[q] * G * eDDF.v[q];
-                nz |= ct.v[q] != 0.0f;
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t v = __shfl_up_sync(full, incl, d);
+            if (lane >= (uint32_t)d) incl += v;
+        }
+        const uint32_t total = __shfl_sync(full, incl, 31);
+        for (uint32_t j0 = 0; j0 < total; j0 += 32) {
+            const uint32_t j = j0 + lane;
+            // owner lane: the number of lanes whose inclusive sum is <= j
+            uint32_t o = 0;
+#pragma unroll
+            for (uint32_t step = 16; step > 0; step >>= 1) {
+                const uint32_t v = __shfl_sync(full, incl, o + step - 1);
+                if (v <= j) o += step;
             }
-            if (!nz) continue;
-            if ((lpd.flags & kVfWlSelected) || (ep.flags & kVfWlSelected)) {
-#pragma unroll
-                for (int q = 0; q < kNumLambda; ++q)
-                    if (q == sel) ct.v[q] *= kNumLambda;
-            }
-            // densities of the two subpaths' first and second extensions
-            const float lExt1Area = lExt1DirPdf * cosEyeEnd / dist2;
-            Spec tmp;
-#pragma unroll
-            for (int q = 0; q < kNumLambda; ++q) tmp.v[q] = lDDF.v[q] * cosLightEnd / lExt1DirPdf;
-            const float lExt1RR = s > 1 ? stdMin(importance(tmp, sel), 1.0f) : 1.0f;
-            float lExt2Area = 0.0f, lExt2RR = 0.0f;
-            if (t > 1) {
-                V3 d2 = eP - e2P;
-                const float dd2 = sqLength(d2);
-                d2 = d2 * (1.0f / sqrtf(dd2));
-                lExt2Area = lExt2DirPdf * absDot(d2, e2N) / dd2;
-#pragma unroll
-                for (int q = 0; q < kNumLambda; ++q) tmp.v[q] = eRev.v[q] * ep.cosIn / lExt2DirPdf;
-                lExt2RR = stdMin(importance(tmp, sel), 1.0f);
-            }
-            const float eExt1Area = eExt1DirPdf * cosLightEnd / dist2;
-#pragma unroll
-            for (int q = 0; q < kNumLambda; ++q) tmp.v[q] = eDDF.v[q] * cosEyeEnd / eExt1DirPdf;
-            const float eExt1RR = t > 1 ? stdMin(importance(tmp, sel), 1.0f) : 1.0f;
-            float eExt2Area = 0.0f, eExt2RR = 0.0f;
-            if (s > 1) {
-                const BptGeom l2 = st.geom[lvi - st.S];
-                V3 d2 = xyz(l2.pg) - lP;
-                const float dd2 = sqLength(d2);
-                d2 = d2 * (1.0f / sqrtf(dd2));
-                eExt2Area = eExt2DirPdf * absDot(d2, xyz(l2.ng)) / dd2;
-#pragma unroll
-                for (int q = 0; q < kNumLambda; ++q) tmp.v[q] = lRev.v[q] * lpd.cosIn / eExt2DirPdf;
-                eExt2RR = stdMin(importance(tmp, sel), 1.0f);
-            }
-            MisSide eyeSide{st.pdf, st.S, esp, t, 1, lExt1Area, lExt1RR, lExt2Area, lExt2RR};
-            MisSide lightSide{st.pdf, st.S, p, s, 0, eExt1Area, eExt1RR, eExt2Area, eExt2RR};
-            const float mis = misWeight(eyeSide, lightSide);
-            if (isinf(mis) || isnan(mis)) continue;
-            Spec lAlpha;
-            loadAlpha(st.alpha, lvi, lAlpha);
+            o = min(o, 31u);
+            const uint32_t ev = __shfl_sync(full, evi, o);
+            const uint32_t first = __shfl_sync(full, incl, o) - __shfl_sync(full, nL, o);
+            bool push = false;
+            float4 ro, rd;
             Spec c;
-            bool finite = true;
-#pragma unroll
-            for (int q = 0; q < kNumLambda; ++q) {
-                c.v[q] = ((mis * lAlpha.v[q]) * ct.v[q]) * eAlpha.v[q];
-                finite &= isfinite(c.v[q]);
+            uint32_t target = 0;
+            if (j < total) {
+                bool drop;
+                push = connectOne(sc, st, ev, j - first + 1, width, height, &ro, &rd, c, &target, &drop);
+                dropped += drop ? 1 : 0;
             }
-            if (!finite) {
-                atomicAdd(&st.stats[2], 1ull);
-                continue;
-            }
-            // Scene::testVisibility (Scene.cpp:96-112)
-            const float dist = length(lP - eP);
-            const V3 sd = (lP - eP) * (1.0f / dist);
-            ++shadowRays;
-            if (traceAny(sc, eP, sd, kRayEpsilon, dist * (1 - kRayEpsilon))) continue;
-            if (t > 1) {
-#pragma unroll
-                for (int q = 0; q < kNumLambda; ++q) own.v[q] += c.v[q];
-            } else {
-                float hx, hy;
-                idfPixel(sc.camera, ec, eg.nz.w, eg.tx.w, width, height, &hx, &hy);
-                const uint32_t ipx = min((uint32_t)fmaxf(hx, 0.0f), width - 1);
-                const uint32_t ipy = min((uint32_t)fmaxf(hy, 0.0f), height - 1);
-                const uint32_t pix = ipy * width + ipx;
-                // SpectrumStorage::add (spectrum_types.h:725-734): wavelength -> film bin
-#pragma unroll
-                for (int q = 0; q < kNumLambda; ++q) {
-                    const float f = __fmul_rn(__fdiv_rn(__fsub_rn(lambdas[q], kWavelengthLow),
-                                                        kWavelengthHigh - kWavelengthLow), (float)kNumLambda);
-                    const uint32_t bin = min((uint32_t)f, (uint32_t)(kNumLambda - 1));
-                    if (c.v[q] != 0.0f) atomicAdd(&st.splat[(size_t)bin * st.splatPixels + pix], c.v[q] * recBinWidth);
+            const unsigned mask = __ballot_sync(full, push);
+            uint32_t slot = 0;
+            if (lane == 0 && mask) slot = atomicAdd(shCount, (uint32_t)__popc(mask));
+            slot = __shfl_sync(full, slot, 0) + __popc(mask & ((1u << lane) - 1));
+            if (push) {
+                if (slot < st.connCap) {
+                    st.cRay[2 * (size_t)slot] = ro;
+                    st.cRay[2 * (size_t)slot + 1] = rd;
+                    storeAlpha(st.cContrib, slot, c);
+                    st.cTarget[slot] = target;
+                } else {
+                    ++traced;
+                    if (!traceAny(sc, xyz(ro), xyz(rd), ro.w, rd.w)) addConnection(st, target, c);
                 }
             }
         }
-        if (t > 1) {
-#pragma unroll
-            for (int q = 0; q < kNumLambda; ++q)
-                if (own.v[q] != 0.0f) atomicAdd(&st.L[(size_t)p * kNumLambda + q], own.v[q]);
-        }
     }
-    if (shadowRays) atomicAdd(&st.stats[1], shadowRays);
+    if (dropped) atomicAdd(&st.stats[2], dropped);
+    if (traced) atomicAdd(&st.stats[1], traced);
+}
+
+// Shadow rays of the queued connections; unoccluded ones add their
+// contribution.
+__global__ void __launch_bounds__(256, SLRGPU_TRACE_MIN_BLOCKS) kBptShadow(DevScene sc, BptState st,
+                                                                         const uint32_t* __restrict__ shCount) {
+    const uint32_t n = min(*shCount, st.connCap);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float4 o = st.cRay[2 * (size_t)i], d = st.cRay[2 * (size_t)i + 1];
+        if (traceAny(sc, xyz(o), xyz(d), o.w, d.w)) continue;
+        Spec c;
+        loadAlpha(st.cContrib, i, c);
+        addConnection(st, st.cTarget[i], c);
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&st.stats[1], (unsigned long long)n);
 }
 
 // The wave's contributions into the compensated film: per pixel, the sums of
@@ -744,7 +839,7 @@ __global__ void kBptAccumulate(BptState st, BptWave wv, float* filmSum, float* f
         }
 #pragma unroll
         for (int b = 0; b < kNumLambda; ++b) {
-            float* sp = &st.splat[(size_t)b * st.splatPixels + pix];
+            float* sp = &st.splat[(size_t)pix * kNumLambda + b];
             kahanAdd(sum[b], comp[b], *sp);
             *sp = 0.0f;
             filmSum[(size_t)b * P + pix] = sum[b];
@@ -762,7 +857,7 @@ int gridFor(const void* kernel, int block) {
 }
 
 struct BptGrids {
-    int init, bounce, connect, accumulate;
+    int init, bounce, connect, shadow, accumulate;
 };
 const BptGrids &bptGrids() {
     static BptGrids g;
@@ -771,6 +866,7 @@ const BptGrids &bptGrids() {
         g.init = gridFor((const void*)kBptInit, 256);
         g.bounce = gridFor((const void*)kBptBounce, 256);
         g.connect = gridFor((const void*)kBptConnect, 256);
+        g.shadow = gridFor((const void*)kBptShadow, 256);
         g.accumulate = gridFor((const void*)kBptAccumulate, 256);
     });
     return g;
@@ -784,6 +880,8 @@ const BptGrids &bptGrids() {
 #define SLRGPU_BPT_WAVE_PATHS (1u << 20)
 #endif
 constexpr uint64_t kBptStateBudget = 8ull << 30;
+// Queued connections per path of a wave (more are traced in place).
+constexpr uint32_t kConnPerPath = 8;
 
 struct BptEngine {
     BptState st{};
@@ -824,13 +922,17 @@ struct BptEngine {
                   (s.splat = alloc<float>((size_t)pixels * kNumLambda, &e)) &&
                   (s.queue[0] = alloc<uint32_t>(S, &e)) && (s.queue[1] = alloc<uint32_t>(S, &e)) &&
                   (s.connQueue = alloc<uint32_t>((size_t)N * (D + 1), &e)) &&
-                  (s.counters = alloc<uint32_t>(D + 2, &e)) && (s.stats = alloc<unsigned long long>(4, &e));
+                  (s.cRay = alloc<float4>((size_t)kConnPerPath * N * 2, &e)) &&
+                  (s.cContrib = alloc<float4>((size_t)kConnPerPath * N * 4, &e)) &&
+                  (s.cTarget = alloc<uint32_t>((size_t)kConnPerPath * N, &e)) &&
+                  (s.counters = alloc<uint32_t>(D + 3, &e)) && (s.stats = alloc<unsigned long long>(4, &e));
         if (!ok) {
             release();
             setError(std::string("bidirectional path state allocation failed: ") + cudaGetErrorString(e));
             return SLRGPU_ERR_OUT_OF_MEMORY;
         }
         s.splatPixels = pixels;
+        s.connCap = kConnPerPath * N;
         if (cudaMemset(s.splat, 0, (size_t)pixels * kNumLambda * sizeof(float)) != cudaSuccess) {
             release();
             setError("bidirectional path state initialisation failed");
@@ -850,7 +952,7 @@ void bptEngineDestroy(BptEngine* e) { delete e; }
 uint64_t bptStateBytesPerPath(uint32_t maxDepth) {
     const uint64_t V = 2ull * (maxDepth + 1);
     return V * (sizeof(BptGeom) + sizeof(BptPdf) + 128) + 2 * (16 + 16 + 64 + 16 + 4 + 4) + 8 + 8 + 4 + 4 +
-           4 * kNumLambda + 8 + 4ull * (maxDepth + 1);
+           4 * kNumLambda + 8 + 4ull * (maxDepth + 1) + kConnPerPath * (32 + 64 + 4);
 }
 
 int renderBpt(BptEngine &eng, const DeviceScene &ds, const slrgpu_settings &s, float* filmSum, float* filmComp,
@@ -932,7 +1034,7 @@ int renderBpt(BptEngine &eng, const DeviceScene &ds, const slrgpu_settings &s, f
         wv.samples = std::min(S, s.spp - base);
         wv.seed = s.seed;
         wv.numPaths = wv.samples * G;
-        cudaMemsetAsync(st.counters, 0, (D + 2) * sizeof(uint32_t), stream);
+        cudaMemsetAsync(st.counters, 0, (D + 3) * sizeof(uint32_t), stream);
         mark(SLRGPU_KERNEL_RAYGEN);
         kBptInit<<<g.init, 256, 0, stream>>>(ds.sc, st, wv);
         markEnd();
@@ -944,13 +1046,17 @@ int renderBpt(BptEngine &eng, const DeviceScene &ds, const slrgpu_settings &s, f
             markEnd();
             ++nl;
         }
+        mark(SLRGPU_KERNEL_SHADE);
+        kBptConnect<<<g.connect, 256, 0, stream>>>(ds.sc, st, s.width, s.height, st.connQueue, st.counters + D + 1,
+                                                   st.counters + D + 2);
+        markEnd();
         mark(SLRGPU_KERNEL_SHADOW);
-        kBptConnect<<<g.connect, 256, 0, stream>>>(ds.sc, st, s.width, s.height, st.connQueue, st.counters + D + 1);
+        kBptShadow<<<g.shadow, 256, 0, stream>>>(ds.sc, st, st.counters + D + 2);
         markEnd();
         mark(SLRGPU_KERNEL_ACCUMULATE);
         kBptAccumulate<<<g.accumulate, 256, 0, stream>>>(st, wv, filmSum, filmComp);
         markEnd();
-        nl += 2;
+        nl += 3;
     }
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {
