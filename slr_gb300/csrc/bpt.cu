@@ -52,6 +52,7 @@ constexpr uint32_t kVfDelta = 1u;        // reached by a delta distribution (pos
 constexpr uint32_t kVfWlSelected = 2u;   // the subpath's wavelength was selected when the vertex was made
 constexpr int kVfKindShift = 4;         // vertex kind, 2 bits
 constexpr int kVfMatShift = 8;          // material kind of a surface vertex, 4 bits
+constexpr uint32_t kVfAtInf = 1u << 12;  // the light vertex on the environment (position = direction)
 
 // Geometry of a vertex (64 B).
 //   surface: pg.w = material index bits; ng.w, nz.w, tx.w = query direction
@@ -112,6 +113,18 @@ struct BptState {
 // aux.w info bits
 constexpr uint32_t kAuxDelta = 1u;        // the pending direction was sampled by a delta distribution
 constexpr uint32_t kAuxWlSelected = 2u;
+constexpr uint32_t kAuxPrevAtInf = 4u;    // the ray leaves the vertex at infinity (squared distance 1)
+
+// Orthonormal basis around a unit vector (Vector3D::makeCoordinateSystem,
+// BasicTypes/Vector3D.h:61-67: the branchless construction of Duff et al.
+// 2017, "Building an Orthonormal Basis, Revisited").
+__device__ __forceinline__ void orthonormalBasis(V3 z, V3* vx, V3* vy) {
+    const float sign = z.z >= 0.0f ? 1.0f : -1.0f;
+    const float a = -1.0f / (sign + z.z);
+    const float b = z.x * z.y * a;
+    *vx = V3{1.0f + sign * z.x * z.x * a, sign * b, -sign * z.x};
+    *vy = V3{b, sign + z.y * z.y * a, -z.y};
+}
 
 struct BptWave {
     uint32_t width, height, gridW, gridH, gridPositions;
@@ -213,8 +226,7 @@ __global__ void kBptInit(DevScene sc, BptState st, BptWave wv) {
             st.L[(size_t)p * kNumLambda + k] = 0.0f;
         }
 
-        // Light subpath: light vertex and its ray (BPTRenderer.cpp:122-149,
-        // surface_object.cpp:65-90, TriangleSurfaceShape.cpp:357-406).
+        // Light subpath: light vertex and its ray (BPTRenderer.cpp:122-149).
         {
             const uint32_t sp = p;
             Rng lr{key, kLightStream};
@@ -223,53 +235,105 @@ __global__ void kBptInit(DevScene sc, BptState st, BptWave wv) {
             const float u0 = lr.next(), u1 = lr.next();
             (void)lr.next();   // EDFSample::uComponent
             const float e0 = lr.next(), e1 = lr.next();
-            const DevPrim lpr = sc.prims[sc.lightPrims[li < 0 ? 0 : li]];
-            const float su = sqrtf(u0);
-            const float b0 = 1.0f - su, b1 = u1 * su, b2 = 1.0f - b0 - b1;
-            const float4 p0 = sc.vpos[lpr.v0], p1 = sc.vpos[lpr.v1], p2 = sc.vpos[lpr.v2];
-            const V3 lp = rn_bary(b0, xyz(p0), b1, xyz(p1), b2, xyz(p2));
-            const float4 n0 = sc.vnrm[lpr.v0], n1 = sc.vnrm[lpr.v1], n2 = sc.vnrm[lpr.v2];
-            const float4 t0 = sc.vtan[lpr.v0], t1 = sc.vtan[lpr.v1], t2 = sc.vtan[lpr.v2];
-            const V3 z = normalize(b0 * xyz(n0) + b1 * xyz(n1) + b2 * xyz(n2));
-            V3 x = normalize(b0 * xyz(t0) + b1 * xyz(t1) + b2 * xyz(t2));
-            const float dotNT = dot(z, x);
-            if (fabsf(dotNT) >= 0.01f) x = normalize(x - dotNT * z);
-            const Frame fr{x, cross(z, x), z};
-            const V3 gn = V3{lpr.ngx, lpr.ngy, lpr.ngz};
-            Spec Le0;
-            evalSpectrum(sc, sc.materials[lpr.material].emit, lambdas, Le0);
-            const float lightAreaPdf = lightProb * lpr.invArea;
-            Spec a0;
-#pragma unroll
-            for (int k = 0; k < kNumLambda; ++k) a0.v[k] = Le0.v[k] / lightAreaPdf;
             BptGeom g;
-            g.pg = make_float4(lp.x, lp.y, lp.z, 0.0f);
-            g.ng = make_float4(gn.x, gn.y, gn.z, 0.0f);
-            g.nz = make_float4(z.x, z.y, z.z, 0.0f);
-            g.tx = make_float4(x.x, x.y, x.z, 0.0f);
-            st.geom[sp] = g;
             BptPdf pd;
             pd.cosIn = 0.0f;
-            pd.areaPdf = lightAreaPdf;
             pd.rrProb = 1.0f;
             pd.revAreaPdf = 0.0f;
             pd.revRRProb = 0.0f;
-            pd.flags = kVtxLight << kVfKindShift;   // LowFreq position
             pd.pad0 = pd.pad1 = 0.0f;
+            Spec a0, a;
+            V3 org, dir;
+            float dirPdf, cosLast, tmin;
+            uint32_t info = 0;
+            if (li >= 0) {
+                // a point on an emitting triangle (surface_object.cpp:65-90,
+                // TriangleSurfaceShape.cpp:357-406), a cosine direction from
+                // its DiffuseEDF (basic_edfs.cpp:13-18)
+                const DevPrim lpr = sc.prims[sc.lightPrims[li]];
+                const float su = sqrtf(u0);
+                const float b0 = 1.0f - su, b1 = u1 * su, b2 = 1.0f - b0 - b1;
+                const float4 p0 = sc.vpos[lpr.v0], p1 = sc.vpos[lpr.v1], p2 = sc.vpos[lpr.v2];
+                const V3 lp = rn_bary(b0, xyz(p0), b1, xyz(p1), b2, xyz(p2));
+                const float4 n0 = sc.vnrm[lpr.v0], n1 = sc.vnrm[lpr.v1], n2 = sc.vnrm[lpr.v2];
+                const float4 t0 = sc.vtan[lpr.v0], t1 = sc.vtan[lpr.v1], t2 = sc.vtan[lpr.v2];
+                const V3 z = normalize(b0 * xyz(n0) + b1 * xyz(n1) + b2 * xyz(n2));
+                V3 x = normalize(b0 * xyz(t0) + b1 * xyz(t1) + b2 * xyz(t2));
+                const float dotNT = dot(z, x);
+                if (fabsf(dotNT) >= 0.01f) x = normalize(x - dotNT * z);
+                const Frame fr{x, cross(z, x), z};
+                const V3 gn = V3{lpr.ngx, lpr.ngy, lpr.ngz};
+                Spec Le0;
+                evalSpectrum(sc, sc.materials[lpr.material].emit, lambdas, Le0);
+                pd.areaPdf = lightProb * lpr.invArea;
+                pd.flags = kVtxLight << kVfKindShift;   // LowFreq position
+#pragma unroll
+                for (int k = 0; k < kNumLambda; ++k) a0.v[k] = Le0.v[k] / pd.areaPdf;
+                g.pg = make_float4(lp.x, lp.y, lp.z, 0.0f);
+                g.ng = make_float4(gn.x, gn.y, gn.z, 0.0f);
+                g.nz = make_float4(z.x, z.y, z.z, 0.0f);
+                g.tx = make_float4(x.x, x.y, x.z, 0.0f);
+                const V3 dl = cosineSampleHemisphere(e0, e1);
+                dirPdf = dl.z * kInvPiF;
+                dir = fr.fromLocal(dl);
+                const float cosG = absDot(dir, gn);
+#pragma unroll
+                for (int k = 0; k < kNumLambda; ++k) a.v[k] = a0.v[k] * kInvPiF * (cosG / dirPdf);
+                org = lp;
+                tmin = kRayEpsilon;
+                cosLast = dl.z;
+            } else {
+                // a point on the environment at infinity
+                // (InfiniteSphereSurfaceObject::sample/sampleRay,
+                // surface_object.cpp:201-272) and IBLEDF::sample (IBLEDF.cpp:11-16):
+                // the direction is the inward normal, the origin a point of
+                // the world disc facing it, outside the world sphere
+                const float twoPi = 6.28318530717958647692f;
+                float uvPdf, topPdf;
+                uint32_t row, col;
+                const float d1 = sampleAlias(sc.envTopAlias, sc.envTopPDF, sc.envMapH, u1, &topPdf, &row);
+                const float d0 = sampleAlias(sc.envRowAlias + (size_t)row * sc.envMapW,
+                                             sc.envRowPDF + (size_t)row * sc.envMapW, sc.envMapW, u0, &uvPdf, &col);
+                uvPdf *= topPdf;
+                const float phi = d0 * twoPi, theta = d1 * kPiF;
+                float sph, cph, sth, cth;
+                sincosf(phi, &sph, &cph);
+                sincosf(theta, &sth, &cth);
+                const V3 pos = V3{-sph * sth, cth, cph * sth};
+                const V3 x = normalize(V3{-cph, 0.0f, -sph});
+                const V3 gn = -pos;
+                pd.areaPdf = lightProb * (uvPdf / (2.0f * kPiF * kPiF * sth));
+                pd.flags = (kVtxLight << kVfKindShift) | kVfAtInf;
+                Spec Le;   // emittance x EDF value (1 / pi)
+                envRadiance(sc, phi / twoPi, theta / kPiF, lambdas, Le);
+#pragma unroll
+                for (int k = 0; k < kNumLambda; ++k) a0.v[k] = (Le.v[k] * kPiF) / pd.areaPdf;
+                g.pg = make_float4(pos.x, pos.y, pos.z, 0.0f);
+                g.ng = make_float4(gn.x, gn.y, gn.z, 0.0f);
+                g.nz = make_float4(gn.x, gn.y, gn.z, 0.0f);
+                g.tx = make_float4(x.x, x.y, x.z, 0.0f);
+                dirPdf = 1.0f / sc.worldDiscArea;
+                dir = gn;
+                float dx, dy;
+                concentricSampleDisk(e0, e1, &dx, &dy);
+                V3 vx, vy;
+                orthonormalBasis(dir, &vx, &vy);
+                const V3 wc = V3{sc.worldCenter[0], sc.worldCenter[1], sc.worldCenter[2]};
+                org = wc + (1.1f * sc.worldRadius) * pos + sc.worldRadius * (dx * vx + dy * vy);
+                const float cosG = absDot(dir, gn);
+#pragma unroll
+                for (int k = 0; k < kNumLambda; ++k) a.v[k] = a0.v[k] * kInvPiF * (cosG / dirPdf);
+                tmin = 0.0f;
+                cosLast = 1.0f;
+                info = kAuxPrevAtInf;
+            }
+            st.geom[sp] = g;
             st.pdf[sp] = pd;
             storeAlpha(st.alpha, sp, a0);
-            // DiffuseEDF::sample (basic_edfs.cpp:13-18)
-            const V3 dl = cosineSampleHemisphere(e0, e1);
-            const float dirPdf = dl.z * kInvPiF;
-            const V3 dir = fr.fromLocal(dl);
-            const float cosG = absDot(dir, gn);
-            Spec a;
-#pragma unroll
-            for (int k = 0; k < kNumLambda; ++k) a.v[k] = a0.v[k] * kInvPiF * (cosG / dirPdf);
             storeAlpha(st.alphaPend, sp, a);
-            st.rayOrg[sp] = make_float4(lp.x, lp.y, lp.z, kRayEpsilon);
+            st.rayOrg[sp] = make_float4(org.x, org.y, org.z, tmin);
             st.rayDir[sp] = make_float4(dir.x, dir.y, dir.z, 0.0f);
-            st.aux[sp] = make_float4(dirPdf, dl.z, 1.0f, __uint_as_float(0u));
+            st.aux[sp] = make_float4(dirPdf, cosLast, 1.0f, __uint_as_float(info));
             st.rngCounter[sp] = lr.counter;
             st.numVerts[sp] = 1;
             queuePush(st.queue[0], st.counters + 0, sp, dirPdf != 0.0f);
@@ -382,6 +446,21 @@ __device__ __forceinline__ float misWeight(const MisSide &eye, const MisSide &li
     return 1.0f / sum;
 }
 
+// Target of a contribution: the path's own sum, or a pixel of the splat film.
+constexpr uint32_t kTargetSplat = 0x80000000u;
+
+// Adds an unoccluded connection to the path's sum or, through the lens,
+// to the splat film (both [.][16], four 16-byte atomic additions).
+__device__ __forceinline__ void addConnection(const BptState &st, uint32_t target, const Spec &c) {
+    float4* dst = reinterpret_cast<float4*>((target & kTargetSplat) ? st.splat : st.L) +
+                  (size_t)(target & ~kTargetSplat) * (kNumLambda / 4);
+#pragma unroll
+    for (int k = 0; k < kNumLambda / 4; ++k) {
+        const float4 v = make_float4(c.v[4 * k], c.v[4 * k + 1], c.v[4 * k + 2], c.v[4 * k + 3]);
+        if (v.x != 0.0f || v.y != 0.0f || v.z != 0.0f || v.w != 0.0f) atomicAdd(dst + k, v);
+    }
+}
+
 __device__ __forceinline__ Frame vertexFrame(const BptGeom &g) {
     V3 z = xyz(g.nz), x = xyz(g.tx);
     return Frame{x, cross(z, x), z};
@@ -406,6 +485,51 @@ __global__ void __launch_bounds__(256, 2) kBptBounce(DevScene sc, BptState st, c
             const V3 org = xyz(ro), dir = xyz(rd);
             Hit h;
             traceClosest(sc, org, dir, ro.w, inf, &h);
+            if (h.prim == kNoHit && !adjoint && sc.envPresent) {
+                // The eye subpath reaches the environment: a vertex at
+                // infinity (InfiniteSphereSurfaceShape.cpp:50-80) whose
+                // implicit path is weighted against the light subpaths that
+                // start there (BPTRenderer.cpp:318-345); the vertex is then
+                // dropped and the subpath ends.
+                const float twoPi = 6.28318530717958647692f;
+                const float4 ax = st.aux[sp];
+                const float dirPdf = ax.x, cosLast = ax.y, rrPend = ax.z;
+                const uint32_t info = __float_as_uint(ax.w);
+                const uint32_t k = st.numVerts[sp];
+                const float cosOut = absDot(-dir, -dir);
+                const BptPdf pd{cosOut, dirPdf * cosOut, rrPend, 0.0f, 0.0f,
+                                (kVtxSurface << kVfKindShift) | ((info & kAuxDelta) ? kVfDelta : 0u), 0.0f, 0.0f};
+                st.pdf[(size_t)k * st.S + sp] = pd;   // read by the MIS weight only
+                float theta, phi;
+                toPolarYUp(dir, &theta, &phi);
+                const float wlOff = st.wlOffset[p];
+                const int sel = (int)st.sel[p];
+                float lambdas[kNumLambda];
+#pragma unroll
+                for (int q = 0; q < kNumLambda; ++q) lambdas[q] = lambdaAt(q, wlOff);
+                Spec Le;   // emittance x IBLEDF value
+                envRadiance(sc, phi / twoPi, theta / kPiF, lambdas, Le);
+                const float envProb = sc.envImportance / (sc.surfImportance + sc.envImportance);
+                const float e1 = envProb * envAreaPdf(sc, phi, theta);
+                const float e2 = (1.0f / sc.worldDiscArea) * cosLast;
+                MisSide eye{st.pdf, st.S, sp, k + 1, 1, e1, 1.0f, e2, 1.0f};
+                MisSide light{st.pdf, st.S, p, 0, 0, 0.0f, 0.0f, 0.0f, 0.0f};
+                const float mis = misWeight(eye, light);
+                if (!isinf(mis) && !isnan(mis)) {
+                    Spec alpha;
+                    loadAlpha(st.alphaPend, sp, alpha);
+                    Spec c;
+                    bool finite = true;
+#pragma unroll
+                    for (int q = 0; q < kNumLambda; ++q) {
+                        c.v[q] = (mis * alpha.v[q]) * Le.v[q];
+                        if ((info & kAuxWlSelected) && q == sel) c.v[q] *= kNumLambda;
+                        finite &= isfinite(c.v[q]);
+                    }
+                    if (finite) addConnection(st, p, c);
+                    else atomicAdd(&st.stats[2], 1ull);
+                }
+            }
             if (h.prim != kNoHit) {
                 const DevPrim pr = sc.prims[h.prim];
                 SurfPoint spt;
@@ -415,7 +539,7 @@ __global__ void __launch_bounds__(256, 2) kBptBounce(DevScene sc, BptState st, c
                 uint32_t info = __float_as_uint(ax.w);
                 bool wlSelected = (info & kAuxWlSelected) != 0;
                 const uint32_t k = st.numVerts[sp];   // index of the new vertex
-                const float dist2 = sqLength(spt.p - org);
+                const float dist2 = (info & kAuxPrevAtInf) ? 1.0f : sqLength(spt.p - org);
                 const V3 dirOut = spt.frame.toLocal(-dir);
                 const V3 gnl = spt.frame.toLocal(spt.gn);
                 const float cosOut = absDot(-dir, spt.gn);
@@ -475,13 +599,8 @@ __global__ void __launch_bounds__(256, 2) kBptBounce(DevScene sc, BptState st, c
                             if (wlSelected && q == sel) c.v[q] *= kNumLambda;
                             finite &= isfinite(c.v[q]);
                         }
-                        if (finite) {
-#pragma unroll
-                            for (int q = 0; q < kNumLambda; ++q)
-                                if (c.v[q] != 0.0f) atomicAdd(&st.L[(size_t)p * kNumLambda + q], c.v[q]);
-                        } else {
-                            atomicAdd(&st.stats[2], 1ull);
-                        }
+                        if (finite) addConnection(st, p, c);
+                        else atomicAdd(&st.stats[2], 1ull);
                     }
                 }
                 if (k < st.D) {
@@ -550,7 +669,6 @@ __device__ __forceinline__ void vertexBsdf(const DevScene &sc, const BptState &s
 // contribution, binned into film bins when it lands through the lens
 // (t = 1, *target = pixel | kTargetSplat) or per wavelength for the path's
 // own sum (*target = path).
-constexpr uint32_t kTargetSplat = 0x80000000u;
 __device__ bool connectOne(const DevScene &sc, const BptState &st, uint32_t evi, uint32_t s, uint32_t width,
                            uint32_t height, float4* rayOrg, float4* rayDir, Spec &c, uint32_t* target,
                            bool* dropped) {
@@ -574,9 +692,12 @@ __device__ bool connectOne(const DevScene &sc, const BptState &st, uint32_t evi,
     const BptPdf lpd = st.pdf[lvi];
     const V3 lP = xyz(lg.pg), lN = xyz(lg.ng);
     const Frame lF = vertexFrame(lg);
-    V3 cv = lP - eP;
-    const float dist2 = sqLength(cv);
-    cv = cv * (1.0f / sqrtf(dist2));
+    // InteractionPoint::getDirectionFrom (geometry.h:147-157): a vertex at
+    // infinity is a direction at squared distance 1
+    const bool lInf = (lpd.flags & kVfAtInf) != 0;
+    V3 cv = lInf ? lP : lP - eP;
+    const float dist2 = lInf ? 1.0f : sqLength(cv);
+    cv = lInf ? normalize(cv) : cv * (1.0f / sqrtf(dist2));
     const float cosLightEnd = absDot(cv, lN);
     const float cosEyeEnd = absDot(cv, eN);
     const float G = cosEyeEnd * cosLightEnd / dist2;
@@ -584,7 +705,11 @@ __device__ bool connectOne(const DevScene &sc, const BptState &st, uint32_t evi,
     const V3 lc = lF.toLocal(-cv);
     Spec lDDF, lRev;
     float lExt1DirPdf, eExt2DirPdf = 0.0f;
-    if (s == 1) {
+    if (lInf) {   // IBLEDF (IBLEDF.cpp:18-30)
+        lDDF = specConst(kInvPiF);
+        lRev = lDDF;
+        lExt1DirPdf = 1.0f / sc.worldDiscArea;
+    } else if (s == 1) {   // DiffuseEDF (basic_edfs.cpp:20-30)
         lDDF = specConst(lc.z > 0.0f ? kInvPiF : 0.0f);
         lRev = lDDF;
         lExt1DirPdf = lc.z > 0.0f ? lc.z * kInvPiF : 0.0f;
@@ -647,9 +772,10 @@ __device__ bool connectOne(const DevScene &sc, const BptState &st, uint32_t evi,
     float eExt2Area = 0.0f, eExt2RR = 0.0f;
     if (s > 1) {
         const BptGeom l2 = st.geom[lvi - st.S];
-        V3 d2 = xyz(l2.pg) - lP;
-        const float dd2 = sqLength(d2);
-        d2 = d2 * (1.0f / sqrtf(dd2));
+        const bool l2Inf = (st.pdf[lvi - st.S].flags & kVfAtInf) != 0;
+        V3 d2 = l2Inf ? xyz(l2.pg) : xyz(l2.pg) - lP;
+        const float dd2 = l2Inf ? 1.0f : sqLength(d2);
+        d2 = l2Inf ? normalize(d2) : d2 * (1.0f / sqrtf(dd2));
         eExt2Area = eExt2DirPdf * absDot(d2, xyz(l2.ng)) / dd2;
 #pragma unroll
         for (int q = 0; q < kNumLambda; ++q) tmp.v[q] = lRev.v[q] * lpd.cosIn / eExt2DirPdf;
@@ -673,10 +799,14 @@ __device__ bool connectOne(const DevScene &sc, const BptState &st, uint32_t evi,
         return false;
     }
     // Scene::testVisibility (Scene.cpp:96-112)
-    const float dist = length(lP - eP);
-    const V3 sd = (lP - eP) * (1.0f / dist);
     *rayOrg = make_float4(eP.x, eP.y, eP.z, kRayEpsilon);
-    *rayDir = make_float4(sd.x, sd.y, sd.z, dist * (1 - kRayEpsilon));
+    if (lInf) {
+        *rayDir = make_float4(cv.x, cv.y, cv.z, 3.402823466e+38f);
+    } else {
+        const float dist = length(lP - eP);
+        const V3 sd = (lP - eP) * (1.0f / dist);
+        *rayDir = make_float4(sd.x, sd.y, sd.z, dist * (1 - kRayEpsilon));
+    }
     if (t > 1) {
         *target = p;
         return true;
@@ -700,18 +830,6 @@ __device__ bool connectOne(const DevScene &sc, const BptState &st, uint32_t evi,
     }
     c = binned;
     return true;
-}
-
-// Adds an unoccluded connection to the path's sum or, through the lens,
-// to the splat film (both [.][16], four 16-byte atomic additions).
-__device__ __forceinline__ void addConnection(const BptState &st, uint32_t target, const Spec &c) {
-    float4* dst = reinterpret_cast<float4*>((target & kTargetSplat) ? st.splat : st.L) +
-                  (size_t)(target & ~kTargetSplat) * (kNumLambda / 4);
-#pragma unroll
-    for (int k = 0; k < kNumLambda / 4; ++k) {
-        const float4 v = make_float4(c.v[4 * k], c.v[4 * k + 1], c.v[4 * k + 2], c.v[4 * k + 3]);
-        if (v.x != 0.0f || v.y != 0.0f || v.z != 0.0f || v.w != 0.0f) atomicAdd(dst + k, v);
-    }
 }
 
 // Connections of the queued eye vertices with every light vertex of their
@@ -962,12 +1080,8 @@ int renderBpt(BptEngine &eng, const DeviceScene &ds, const slrgpu_settings &s, f
         setError("the volumetric bidirectional path tracer is not implemented");
         return SLRGPU_ERR_UNSUPPORTED;
     }
-    if (ds.sc.envPresent) {
-        setError("bidirectional path tracing with an environment light is not implemented");
-        return SLRGPU_ERR_UNSUPPORTED;
-    }
-    if (ds.sc.numLights == 0) {
-        setError("bidirectional path tracing needs at least one emitting surface");
+    if (ds.sc.numLights == 0 && !ds.sc.envPresent) {
+        setError("bidirectional path tracing needs a light (an emitting surface or an environment)");
         return SLRGPU_ERR_INVALID_ARGUMENT;
     }
     if (s.max_depth < 1 || s.max_depth > 63) {

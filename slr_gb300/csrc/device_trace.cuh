@@ -194,25 +194,30 @@ __device__ __forceinline__ bool traceClosest(const DevScene &sc, V3 org, V3 dir,
             float tn[4];
             uint32_t ch[4];
             uint32_t mask = testChildren(sc.nodes, cur, org, inv, tmin, tmax, tn, ch, sc.watertight != 0);
-            // Order hit children near to far; visit the nearest next and push the rest.
-            uint32_t order[4];
-            int n = 0;
-#pragma unroll
-            for (int k = 0; k < 4; ++k)
-                if (mask & (1u << k)) order[n++] = k;
-            // insertion sort by tn (n <= 4)
-            for (int a = 1; a < n; ++a) {
-                uint32_t x = order[a];
-                int b = a - 1;
-                while (b >= 0 && tn[order[b]] > tn[x]) { order[b + 1] = order[b]; --b; }
-                order[b + 1] = x;
+            if (mask == 0) goto pop;
+            // Order the hit children near to far (ties in child order) with a
+            // five-comparator sorting network on registers; missed children
+            // sort last at +inf.  Visit the nearest next, push the rest far
+            // to near.
+            float t0 = (mask & 1u) ? tn[0] : __int_as_float(0x7f800000);
+            float t1 = (mask & 2u) ? tn[1] : __int_as_float(0x7f800000);
+            float t2 = (mask & 4u) ? tn[2] : __int_as_float(0x7f800000);
+            float t3 = (mask & 8u) ? tn[3] : __int_as_float(0x7f800000);
+            uint32_t c0 = ch[0], c1 = ch[1], c2 = ch[2], c3 = ch[3];
+            uint32_t k0 = 0, k1 = 1, k2 = 2, k3 = 3;
+#define SLRGPU_CSWAP(a, b)                                                           \
+            if (t##b < t##a || (t##b == t##a && k##b < k##a)) {                      \
+                float tt = t##a; t##a = t##b; t##b = tt;                             \
+                uint32_t cc = c##a; c##a = c##b; c##b = cc;                          \
+                uint32_t kk = k##a; k##a = k##b; k##b = kk;                          \
             }
-            if (n == 0) goto pop;
-            for (int k = n - 1; k >= 1; --k) {
-                if (sp < kTraceStack) stack[sp++] = StackEntry{ch[order[k]], tn[order[k]]};
-                else ok = false;
-            }
-            cur = ch[order[0]];
+            SLRGPU_CSWAP(0, 1) SLRGPU_CSWAP(2, 3) SLRGPU_CSWAP(0, 2) SLRGPU_CSWAP(1, 3) SLRGPU_CSWAP(1, 2)
+#undef SLRGPU_CSWAP
+            const int n = __popc(mask);
+            if (n > 3) { if (sp < kTraceStack) stack[sp++] = StackEntry{c3, t3}; else ok = false; }
+            if (n > 2) { if (sp < kTraceStack) stack[sp++] = StackEntry{c2, t2}; else ok = false; }
+            if (n > 1) { if (sp < kTraceStack) stack[sp++] = StackEntry{c1, t1}; else ok = false; }
+            cur = c0;
             continue;
         } else {
             uint32_t first = cur & kLeafFirstMask;

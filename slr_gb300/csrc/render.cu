@@ -270,13 +270,18 @@ __global__ void kShadeMiss(DevScene sc, WaveState ws, const uint32_t* __restrict
     }
 }
 
-template <int K>
 // Resident blocks per SM the shading kernels are compiled for (register cap
-// 65536 / (256 x this)); a compile-time tuning constant.
+// 65536 / (256 x this)); compile-time tuning constants, the GGX dielectric's
+// (the largest body: per-wavelength refraction) on its own.
 #ifndef SLRGPU_SHADE_MIN_BLOCKS
 #define SLRGPU_SHADE_MIN_BLOCKS 3   // 85 registers: +9 % on the 1M-triangle benchmark over 2 (128)
 #endif
-__global__ void __launch_bounds__(256, SLRGPU_SHADE_MIN_BLOCKS) kShadeSurf(DevScene sc, WaveState ws, uint32_t maxDepth,
+#ifndef SLRGPU_SHADE_DIELECTRIC_MIN_BLOCKS
+#define SLRGPU_SHADE_DIELECTRIC_MIN_BLOCKS SLRGPU_SHADE_MIN_BLOCKS
+#endif
+template <int K>
+__global__ void __launch_bounds__(256, K == kMatGGXScattering ? SLRGPU_SHADE_DIELECTRIC_MIN_BLOCKS
+                                                               : SLRGPU_SHADE_MIN_BLOCKS) kShadeSurf(DevScene sc, WaveState ws, uint32_t maxDepth,
                                                   const uint32_t* __restrict__ inQueue,
                                                   const uint32_t* __restrict__ inCount, uint32_t* outQueue,
                                                   uint32_t* outCount, uint32_t* shQueue, uint32_t* shCount) {

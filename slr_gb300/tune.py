@@ -14,7 +14,8 @@ other knobs as they were.
 
 Knobs (resident blocks of 256 threads per SM the kernels are compiled for):
 SLRGPU_TRACE_MIN_BLOCKS (closest/any-hit traversal), SLRGPU_SHADE_MIN_BLOCKS
-(surface shading), SLRGPU_SHADEVOL_MIN_BLOCKS (volumetric shading),
+(surface shading), SLRGPU_SHADE_DIELECTRIC_MIN_BLOCKS (GGX dielectric
+shading), SLRGPU_SHADEVOL_MIN_BLOCKS (volumetric shading),
 SLRGPU_MEDIUM_MIN_BLOCKS (medium transmittance); and the paths per wave.
 """
 from __future__ import annotations
@@ -33,17 +34,21 @@ TUNING = PKG / "tuning.json"
 KNOBS = {
     "SLRGPU_TRACE_MIN_BLOCKS": [3, 4, 5],
     "SLRGPU_SHADE_MIN_BLOCKS": [2, 3, 4],
+    "SLRGPU_SHADE_DIELECTRIC_MIN_BLOCKS": [2, 3, 4],
     "SLRGPU_SHADEVOL_MIN_BLOCKS": [2, 3],
     "SLRGPU_MEDIUM_MIN_BLOCKS": [2, 3, 4],
 }
-DEFAULTS = {"SLRGPU_TRACE_MIN_BLOCKS": 4, "SLRGPU_SHADE_MIN_BLOCKS": 3, "SLRGPU_SHADEVOL_MIN_BLOCKS": 3,
-            "SLRGPU_MEDIUM_MIN_BLOCKS": 4, "wave_paths": 1 << 22}   # the sources' defaults
+DEFAULTS = {"SLRGPU_TRACE_MIN_BLOCKS": 4, "SLRGPU_SHADE_MIN_BLOCKS": 3, "SLRGPU_SHADE_DIELECTRIC_MIN_BLOCKS": 3,
+            "SLRGPU_SHADEVOL_MIN_BLOCKS": 3, "SLRGPU_MEDIUM_MIN_BLOCKS": 4,
+            "wave_paths": 1 << 22}   # the sources' defaults
 WAVE_PATHS = [1 << 22, 1 << 23, 1 << 24, 1 << 25, 1 << 26]
 # The knobs a workload exercises (a knob of kernels the workload never
 # launches would only be tuned to noise).
 WORKLOAD_KNOBS = {
-    "small": ["SLRGPU_TRACE_MIN_BLOCKS", "SLRGPU_SHADE_MIN_BLOCKS", "wave_paths"],
-    "ggx_ibl_1m": ["SLRGPU_TRACE_MIN_BLOCKS", "SLRGPU_SHADE_MIN_BLOCKS", "wave_paths"],
+    "small": ["SLRGPU_TRACE_MIN_BLOCKS", "SLRGPU_SHADE_MIN_BLOCKS", "SLRGPU_SHADE_DIELECTRIC_MIN_BLOCKS",
+              "wave_paths"],
+    "ggx_ibl_1m": ["SLRGPU_TRACE_MIN_BLOCKS", "SLRGPU_SHADE_MIN_BLOCKS", "SLRGPU_SHADE_DIELECTRIC_MIN_BLOCKS",
+                   "wave_paths"],
     "volumetric_small": ["SLRGPU_SHADEVOL_MIN_BLOCKS", "SLRGPU_MEDIUM_MIN_BLOCKS"],
 }
 

@@ -120,11 +120,20 @@ def test_bpt_waves_sum_like_one(gpu_lib):
     np.testing.assert_allclose(a, c0 + c1, rtol=1e-4, atol=1e-5)
 
 
+def test_bpt_environment_matches_reference(gpu_lib, oracle_lib):
+    """GGX conductors and dielectrics under the image-based environment (a
+    small version of the 1M-triangle scene): light subpaths that start on
+    the environment at infinity (IBLEDF, world-disc origins), eye subpaths
+    that escape to it, and connections toward a vertex at infinity."""
+    desc = scenes.heightfield_scene(grid=24, spheres=5, sphere_freq=3, env_size=(64, 32), width=20, height=20)
+    w = h = 20
+    spp, depth = 8, 8
+    rm, _ = oracle_bpt_batches(oracle_lib, desc, w, h, spp, depth, 40, 1700)
+    gm, _ = gpu_bpt_batches(gpu_lib, desc, w, h, spp, depth, 160)
+    compare(gm, rm, frac_limit=0.02)
+
+
 def test_bpt_rejects_what_it_does_not_implement(gpu_lib):
-    env_scene = gpu_lib.Scene(scenes.heightfield_scene(grid=8, spheres=1, sphere_freq=1, env_size=(16, 8),
-                                                       width=8, height=8))
-    with pytest.raises(gpu_lib.SlrGpuError):
-        env_scene.render(8, 8, 1, 4, bpt=True)            # environment light
     vol = gpu_lib.Scene(scenes.medium_box_scene(8, 8, grid=8))
     with pytest.raises(gpu_lib.SlrGpuError):
         vol.render(8, 8, 1, 4, bpt=True, volumetric=True)  # VolumetricBPTRenderer
