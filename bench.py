@@ -24,7 +24,8 @@ not a benchmark line.
 
 ``--workload bpt_box`` renders the box scene with the bidirectional path
 tracer (BPTRenderer semantics, 16 vertices per subpath) at 512 x 512 and
-16 spp; its CPU baseline is the reference's BPTRenderer.
+16 spp; its CPU baseline is the reference's BPTRenderer.  ``bpt_volumetric``
+does the same for VolumetricBPTRenderer on the volumetric box.
 
 ``--workload serving`` runs the serving stream (512 requests, Poisson
 arrivals at 20/s, 8 scenes of 1k-2M triangles, half with a medium) through
@@ -161,7 +162,7 @@ def cpu_baseline(desc, threads: int, seconds_target: float = 12.0):
     while total_s < seconds_target and frames < 16:
         if BPT:   # one BPT render per reference sensor
             ref = O.RefScene(desc) if frames else ref
-            _, s = ref.render_bpt(WIDTH, HEIGHT, 1, MAX_DEPTH, seed=frames, threads=threads)
+            _, s = ref.render_bpt(WIDTH, HEIGHT, 1, MAX_DEPTH, seed=frames, threads=threads, volumetric=VOLUMETRIC)
         else:
             _, s = ref.render(WIDTH, HEIGHT, 1, MAX_DEPTH, seed=frames, threads=threads, volumetric=VOLUMETRIC)
         total_samples += WIDTH * HEIGHT
@@ -185,7 +186,7 @@ def run_reference(args):
     for i in range(args.warmup + args.steps):
         if BPT:   # one BPT render per reference sensor
             ref = O.RefScene(desc) if i else ref
-            _, s = ref.render_bpt(WIDTH, HEIGHT, 1, MAX_DEPTH, seed=i, threads=threads)
+            _, s = ref.render_bpt(WIDTH, HEIGHT, 1, MAX_DEPTH, seed=i, threads=threads, volumetric=VOLUMETRIC)
         else:
             _, s = ref.render(WIDTH, HEIGHT, 1, MAX_DEPTH, seed=i, threads=threads, volumetric=VOLUMETRIC)
         if i >= args.warmup:
@@ -409,6 +410,11 @@ def _workloads():
                         text="bpt_box: the box scene (Lambert walls and blocks, 0.25x0.25 ceiling light), "
                              "BPTRenderer, 16 vertices per subpath, 512x512, 16 spp, seed 0",
                         scene=lambda: scenes.box_scene(512, 512)),
+        "bpt_volumetric": dict(width=256, height=256, spp=16, depth=16, volumetric=True, bpt=True,
+                               text="bpt_volumetric: the volumetric box (256^3 fBm density grid, sigma_t max 20, "
+                                    "albedo 0.9, HG g 0.7), VolumetricBPTRenderer, 16 vertices per subpath, "
+                                    "256x256, 16 spp",
+                               scene=lambda: scenes.medium_box_scene(256, 256, grid=256)),
         "bpt_box_small": dict(width=256, height=256, spp=4, depth=16, volumetric=False, bpt=True,
                               text="bpt_box_small: the bidirectional box workload at 256x256, 4 spp (profiler "
                                    "captures)",
@@ -439,8 +445,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--spp", type=int, default=None)
     ap.add_argument("--workload", default="ggx_ibl_1m",
-                    choices=["ggx_ibl_1m", "small", "box", "bpt_box", "bpt_box_small", "volumetric", "volumetric_small",
-                             "serving", "traversal"])
+                    choices=["ggx_ibl_1m", "small", "box", "bpt_box", "bpt_volumetric", "bpt_box_small", "volumetric",
+                             "volumetric_small", "serving", "traversal"])
     ap.add_argument("--requests", type=int, default=512)
     args = ap.parse_args()
     if args.workload == "serving":

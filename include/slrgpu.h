@@ -88,13 +88,14 @@ typedef struct slrgpu_settings {
  * reference only for rays within rounding of an edge or vertex. */
 #define SLRGPU_FLAG_WATERTIGHT 2u
 /* settings.flags: bidirectional path tracing, BPTRenderer(spp)
- * (libSLR/Renderer/BPTRenderer.h:117-123, BPTRenderer.cpp:25-431), instead
- * of PTRenderer.  max_depth (1..63) then caps each subpath at max_depth
- * vertices after its first (the reference ends subpaths by Russian roulette
- * only).  Surface lights only: scenes with an environment, and volumetric = 1
- * (VolumetricBPTRenderer), return SLRGPU_ERR_UNSUPPORTED.  Contributions
+ * (libSLR/Renderer/BPTRenderer.h:117-123, BPTRenderer.cpp:25-431), or with
+ * volumetric = 1 VolumetricBPTRenderer(spp) (VolumetricBPTRenderer.cpp),
+ * instead of the path tracers.  max_depth (1..63) then caps each subpath at
+ * max_depth vertices after its first (the reference ends subpaths by Russian
+ * roulette only).  Surface lights and the environment.  Contributions
  * through the lens vertex land on the pixel they project to;
- * slrgpu_render_stats.dropped_samples counts non-finite contributions. */
+ * slrgpu_render_stats.dropped_samples counts non-finite contributions.  The
+ * allocation-free render and the server return SLRGPU_ERR_UNSUPPORTED. */
 #define SLRGPU_FLAG_BPT 4u
 
 /* Kernel classes of the wavefront (index into kernel_ms / kernel_count). */

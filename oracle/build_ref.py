@@ -56,6 +56,9 @@ Build-only patches (all applied to the copy):
 * P10 ``Renderer/BPTRenderer.cpp:338``: a non-finite implicit-path
   contribution is dropped and counted instead of being added to the film
   (where one NaN would spoil the pixel for good).
+* P11 ``Renderer/VolumetricBPTRenderer.cpp``: P9 and P10 for the volumetric
+  bidirectional renderer (cap before the sample at ``:358``, ``:84``,
+  ``:269``, ``:349``).
 """
 from __future__ import annotations
 
@@ -74,7 +77,7 @@ SRC_COPY = REF_OUT / "src" / "libSLR"
 OBJ_DIR = REF_OUT / "obj"
 LIB = REF_OUT / "libslr_ref.so"
 DEFAULT_REFERENCE = "/root/reference"
-PATCH_SET = "P1 P2 P3 P4 P5 P6 P7 P8 P9 P10\n"
+PATCH_SET = "P1 P2 P3 P4 P5 P6 P7 P8 P9 P10 P11\n"
 
 # Files excluded from the reference's own build (libSLR/CMakeLists.txt:45-51).
 EXCLUDED = {
@@ -172,6 +175,19 @@ def copy_and_patch(ref_root: Path) -> None:
                           "                    else slr_oracle_dropped_samples.fetch_add(1);", "P10 BPT implicit")
         return t.replace("namespace SLR {", decl + "namespace SLR {", 1)
     patch("Renderer/BPTRenderer.cpp", p9_bpt)
+    def p11_vbpt(t: str) -> str:
+        t = _replace_once(t, "            ABDFQueryResult* abdfResult;\n            SampledSpectrum abdfValue = abdf->sample(",
+                          "            if (vertices.size() > slr_oracle_max_depth)\n                break;\n"
+                          "            ABDFQueryResult* abdfResult;\n            SampledSpectrum abdfValue = abdf->sample(",
+                          "P11 VBPT cap")
+        t = _replace_once(t, "sensor->saveImage(filename,", "if (0) sensor->saveImage(filename,", "P11 VBPT save")
+        t = _replace_once(t, 'slrDevPrintf("Unexpected value detected: %s at (%f, %f)\\n", contribution.toString().c_str(), p.x, p.y);',
+                          "slr_oracle_dropped_samples.fetch_add(1);", "P11 VBPT drop")
+        t = _replace_once(t, "                    sensor->add(curPx, curPy, wls, contribution);",
+                          "                    if (contribution.allFinite()) sensor->add(curPx, curPy, wls, contribution);\n"
+                          "                    else slr_oracle_dropped_samples.fetch_add(1);", "P11 VBPT implicit")
+        return t.replace("namespace SLR {", decl + "namespace SLR {", 1)
+    patch("Renderer/VolumetricBPTRenderer.cpp", p11_vbpt)
     # P7: the stock reporter is replaced by oracle/progress_reporter_noop.cpp
     (SRC_COPY / "Core" / "ProgressReporter.cpp").unlink()
     (REF_OUT / "src" / "PATCHED").write_text(PATCH_SET)

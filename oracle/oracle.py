@@ -49,7 +49,7 @@ def lib():
             "ora_camera_equirect": (I, [P, fp, F, F, F]),
             "ora_build": (I, [P]),
             "ora_render": (I, [P, I, I, I, I, I, I, I, fp, dp]),
-            "ora_render_bpt": (I, [P, I, I, I, I, I, I, fp, dp]),
+            "ora_render_bpt": (I, [P, I, I, I, I, I, I, I, fp, dp]),
             "ora_sbvh_build": (I, [P, up, up, fp, up]),
             "ora_sbvh_dump": (I, [P, fp, up, up]),
             "ora_trace": (I, [P, fp, I, I, I, up, fp, fp, fp]),
@@ -173,14 +173,14 @@ class RefScene:
         self.last_dropped = int(lib().ora_dropped_samples())
         return film, sec.value
 
-    def render_bpt(self, width, height, spp, max_depth, seed=0, threads=None):
-        """BPTRenderer: returns (film sum (h, w, 16) float32, render seconds).
-        One BPT render per RefScene (the reference's sensor cannot take a
-        second one)."""
+    def render_bpt(self, width, height, spp, max_depth, seed=0, threads=None, volumetric=False):
+        """BPTRenderer (VolumetricBPTRenderer with volumetric=True): returns
+        (film sum (h, w, 16) float32, render seconds).  One BPT render per
+        RefScene (the reference's sensor cannot take a second one)."""
         threads = threads or os.cpu_count() or 1
         film = np.zeros((height, width, 16), np.float32)
         sec = C.c_double(0)
-        rc = lib().ora_render_bpt(self.h, spp, max_depth, width, height, threads, seed,
+        rc = lib().ora_render_bpt(self.h, int(volumetric), spp, max_depth, width, height, threads, seed,
                                   film.ctypes.data_as(C.POINTER(C.c_float)), C.byref(sec))
         if rc == -2:
             raise RuntimeError("one BPT render per oracle scene")

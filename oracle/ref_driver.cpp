@@ -61,6 +61,7 @@
 #include "Renderer/PTRenderer.h"
 #include "Renderer/VolumetricPTRenderer.h"
 #include "Renderer/BPTRenderer.h"
+#include "Renderer/VolumetricBPTRenderer.h"
 #include "MediumMaterial/basic_medium_materials.h"
 #include "Core/medium_material.h"
 #include "Core/medium_object.h"
@@ -362,14 +363,15 @@ int ora_render(void* p, int volumetric, int spp, int maxDepth, int w, int h, int
     return 0;
 }
 
-// Renders with BPTRenderer and copies the 16-bin film, main buffer plus the
+// Renders with BPTRenderer (volumetric == 0) or VolumetricBPTRenderer
+// (VolumetricBPTRenderer.cpp:25-101) and copies the 16-bin film, main buffer plus the
 // per-thread buffers that collect the light-tracing connections
 // (BPTRenderer.cpp:268-276; ImageSensor::saveImage adds them the same way,
 // ImageSensor.cpp:154-156).  ImageSensor::addSeparatedBuffers
 // (ImageSensor.cpp:54-63) allocates buffers only beyond those it already
 // has, into a new pointer array, so a second BPT render through the same
 // sensor would clear unallocated buffers: one BPT render per scene (-2).
-int ora_render_bpt(void* p, int spp, int maxDepth, int w, int h, int threads, int seed, float* film,
+int ora_render_bpt(void* p, int volumetric, int spp, int maxDepth, int w, int h, int threads, int seed, float* film,
                    double* seconds) {
     OraScene* s = (OraScene*)p;
     if (!s->built || !s->scene->getCamera()) return -1;
@@ -385,9 +387,11 @@ int ora_render_bpt(void* p, int spp, int maxDepth, int w, int h, int threads, in
     settings.addItem(RenderSettingItem::Brightness, 1.0f);
     settings.addItem(RenderSettingItem::RNGSeed, (int32_t)seed);
     slr_oracle_dropped_samples.store(0);
-    BPTRenderer r(spp);
+    std::unique_ptr<Renderer> r;
+    if (volumetric) r.reset(new VolumetricBPTRenderer(spp));
+    else r.reset(new BPTRenderer(spp));
     auto t0 = std::chrono::steady_clock::now();
-    r.render(*s->scene, settings);
+    r->render(*s->scene, settings);
     auto t1 = std::chrono::steady_clock::now();
     if (seconds) *seconds = std::chrono::duration<double>(t1 - t0).count();
     const ImageSensor* sensor = s->scene->getCamera()->getSensor();

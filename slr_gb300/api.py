@@ -553,6 +553,8 @@ class BidirectionalPathTracingRenderer:
     max_depth caps each subpath at that many vertices beyond its first (the
     reference ends subpaths by Russian roulette only)."""
 
+    volumetric = False
+
     def __init__(self, spp: int, max_depth: int = 32):
         self.spp = int(spp)
         self.max_depth = int(max_depth)
@@ -561,9 +563,16 @@ class BidirectionalPathTracingRenderer:
         w = int(settings.get(RenderSettingItem.ImageWidth))
         h = int(settings.get(RenderSettingItem.ImageHeight))
         seed = int(settings.get(RenderSettingItem.RNGSeed, 0)) & 0xffffffff
-        film, stats = scene.render(w, h, self.spp, self.max_depth, seed=seed, bpt=True)
+        film, stats = scene.render(w, h, self.spp, self.max_depth, seed=seed, bpt=True, volumetric=self.volumetric)
         self.last_stats = stats
         return film
+
+
+class VolumetricBidirectionalPathTracingRenderer(BidirectionalPathTracingRenderer):
+    """Drop-in for SLR::VolumetricBPTRenderer(spp)
+    (libSLR/Renderer/VolumetricBPTRenderer.h:121)."""
+
+    volumetric = True
 
 
 class VolumetricPathTracingRenderer(PathTracingRenderer):

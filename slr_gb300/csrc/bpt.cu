@@ -31,6 +31,7 @@
 #include <mutex>
 
 #include "device_bsdf_rev.cuh"
+#include "device_medium.cuh"
 #include "device_scene.cuh"
 
 namespace slrgpu {
@@ -40,6 +41,9 @@ namespace slrgpu {
 #ifndef SLRGPU_TRACE_MIN_BLOCKS
 #define SLRGPU_TRACE_MIN_BLOCKS 4
 #endif
+#ifndef SLRGPU_MEDIUM_MIN_BLOCKS
+#define SLRGPU_MEDIUM_MIN_BLOCKS 4
+#endif
 
 namespace {
 
@@ -47,6 +51,7 @@ namespace {
 constexpr uint32_t kVtxLens = 0;
 constexpr uint32_t kVtxLight = 1;
 constexpr uint32_t kVtxSurface = 2;
+constexpr uint32_t kVtxMedium = 3;       // a scattering point in the medium (volumetric BPT)
 // BptPdf::flags
 constexpr uint32_t kVfDelta = 1u;        // reached by a delta distribution (position or direction)
 constexpr uint32_t kVfWlSelected = 2u;   // the subpath's wavelength was selected when the vertex was made
@@ -106,7 +111,11 @@ struct BptState {
     float4* cRay;         // [connCap * 2] origin + tmin, direction + tmax
     float4* cContrib;     // [connCap * 4] contribution (film bins when splatted)
     uint32_t* cTarget;    // [connCap] path index, or pixel | kTargetSplat
-    uint32_t* counters;   // [D + 3] queue sizes per bounce, eye vertices to connect, queued connections
+    uint32_t* cPath;      // [connCap] path of the connection (volumetric: wavelengths, RNG key)
+    uint32_t* cMeta;      // [connCap] eye vertex index << 8 | light vertex number (volumetric RNG stream)
+    uint32_t* mQueue;     // [connCap] unoccluded connections whose transmittance is due (volumetric)
+    uint32_t* counters;   // [D + 4] queue sizes per bounce, eye vertices to connect, queued
+                          // connections, connections waiting for their transmittance
     unsigned long long* stats;   // 0 extension rays, 1 shadow rays, 2 dropped contributions
 };
 
@@ -115,16 +124,6 @@ constexpr uint32_t kAuxDelta = 1u;        // the pending direction was sampled b
 constexpr uint32_t kAuxWlSelected = 2u;
 constexpr uint32_t kAuxPrevAtInf = 4u;    // the ray leaves the vertex at infinity (squared distance 1)
 
-// Orthonormal basis around a unit vector (Vector3D::makeCoordinateSystem,
-// BasicTypes/Vector3D.h:61-67: the branchless construction of Duff et al.
-// 2017, "Building an Orthonormal Basis, Revisited").
-__device__ __forceinline__ void orthonormalBasis(V3 z, V3* vx, V3* vy) {
-    const float sign = z.z >= 0.0f ? 1.0f : -1.0f;
-    const float a = -1.0f / (sign + z.z);
-    const float b = z.x * z.y * a;
-    *vx = V3{1.0f + sign * z.x * z.x * a, sign * b, -sign * z.x};
-    *vy = V3{b, sign + z.y * z.y * a, -z.y};
-}
 
 struct BptWave {
     uint32_t width, height, gridW, gridH, gridPositions;
@@ -201,7 +200,9 @@ __device__ __forceinline__ void idfPixel(const DevCamera &c, V3 d, float lu, flo
 // ---------------------------------------------------------------------------
 // Kernels
 // ---------------------------------------------------------------------------
-// Job::kernel up to the two subpath generations (BPTRenderer.cpp:107-172).
+// Job::kernel up to the two subpath generations (BPTRenderer.cpp:107-172,
+// VolumetricBPTRenderer.cpp:107-174).
+template <bool VOL>
 __global__ void kBptInit(DevScene sc, BptState st, BptWave wv) {
     const float selectWLPDF = kNumLambda / (kWavelengthHigh - kWavelengthLow);
     for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < wv.numPaths; p += gridDim.x * blockDim.x) {
@@ -231,7 +232,13 @@ __global__ void kBptInit(DevScene sc, BptState st, BptWave wv) {
             const uint32_t sp = p;
             Rng lr{key, kLightStream};
             float lightProb;
-            const int li = selectLight(sc, lr.next(), &lightProb);
+            int li;
+            if (VOL) {   // Scene::selectLight over surfaces, media and the environment
+                const int kind = selectLight3(sc, lr.next(), &li, &lightProb);
+                if (kind != 0) li = -1;
+            } else {     // Scene::selectSurfaceLight
+                li = selectLight(sc, lr.next(), &lightProb);
+            }
             const float u0 = lr.next(), u1 = lr.next();
             (void)lr.next();   // EDFSample::uComponent
             const float e0 = lr.next(), e1 = lr.next();
@@ -316,8 +323,9 @@ __global__ void kBptInit(DevScene sc, BptState st, BptWave wv) {
                 dir = gn;
                 float dx, dy;
                 concentricSampleDisk(e0, e1, &dx, &dy);
-                V3 vx, vy;
-                orthonormalBasis(dir, &vx, &vy);
+                // Vector3D::makeCoordinateSystem (Vector3D.h:61-67)
+                const Frame db = frameFromZ(dir);
+                const V3 vx = db.x, vy = db.y;
                 const V3 wc = V3{sc.worldCenter[0], sc.worldCenter[1], sc.worldCenter[2]};
                 org = wc + (1.1f * sc.worldRadius) * pos + sc.worldRadius * (dx * vx + dy * vy);
                 const float cosG = absDot(dir, gn);
@@ -466,13 +474,31 @@ __device__ __forceinline__ Frame vertexFrame(const BptGeom &g) {
     return Frame{x, cross(z, x), z};
 }
 
+// Film bin of a wavelength (SpectrumStorage::add, spectrum_types.h:729).
+__device__ __forceinline__ uint32_t filmBin(float lambda) {
+    const float f = __fmul_rn(__fdiv_rn(__fsub_rn(lambda, kWavelengthLow), kWavelengthHigh - kWavelengthLow),
+                              (float)kNumLambda);
+    return min((uint32_t)f, (uint32_t)(kNumLambda - 1));
+}
+
+// Cosine factor of a vertex toward a direction: |cos| against the
+// geometric normal, 1 for a point in the medium (MediumPoint::calcCosTerm,
+// geometry.h:281-283).
+__device__ __forceinline__ float vertexCos(const BptGeom &g, uint32_t flags, V3 d) {
+    return ((flags >> kVfKindShift) & 3u) == kVtxMedium ? 1.0f : absDot(d, xyz(g.ng));
+}
+
 // One bounce of every live subpath: generateSubPath's loop body
-// (BPTRenderer.cpp:304-379).  A subpath holds at most D + 1 vertices.
+// (BPTRenderer.cpp:304-379; VOL: VolumetricBPTRenderer.cpp:311-391, where
+// Scene::interact may stop the ray at a scattering point in the medium).  A
+// subpath holds at most D + 1 vertices.
+template <bool VOL>
 __global__ void __launch_bounds__(256, 2) kBptBounce(DevScene sc, BptState st, const uint32_t* __restrict__ inQueue,
                                                      const uint32_t* __restrict__ inCount, uint32_t* outQueue,
                                                      uint32_t* outCount) {
     const uint32_t n = *inCount;
     const float inf = __int_as_float(0x7f800000);
+    const float twoPi = 6.28318530717958647692f;
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
         const uint32_t i = base + threadIdx.x;
         const bool active = i < n;
@@ -483,75 +509,108 @@ __global__ void __launch_bounds__(256, 2) kBptBounce(DevScene sc, BptState st, c
             const uint32_t p = adjoint ? sp : sp - st.N;
             const float4 ro = st.rayOrg[sp], rd = st.rayDir[sp];
             const V3 org = xyz(ro), dir = xyz(rd);
+            const float4 ax = st.aux[sp];
+            const float dirPdf = ax.x, cosLast = ax.y, rrPend = ax.z;
+            uint32_t info = __float_as_uint(ax.w);
+            bool wlSelected = (info & kAuxWlSelected) != 0;
+            const uint32_t k = st.numVerts[sp];   // index of the new vertex
+            const float wlOff = st.wlOffset[p];
+            const int sel = (int)st.sel[p];
+            float lambdas[kNumLambda];
+#pragma unroll
+            for (int q = 0; q < kNumLambda; ++q) lambdas[q] = lambdaAt(q, wlOff);
+            Rng rng{keyOf(st, p), st.rngCounter[sp]};
+            Spec alpha;
+            loadAlpha(st.alphaPend, sp, alpha);
             Hit h;
             traceClosest(sc, org, dir, ro.w, inf, &h);
-            if (h.prim == kNoHit && !adjoint && sc.envPresent) {
-                // The eye subpath reaches the environment: a vertex at
-                // infinity (InfiniteSphereSurfaceShape.cpp:50-80) whose
-                // implicit path is weighted against the light subpaths that
-                // start there (BPTRenderer.cpp:318-345); the vertex is then
-                // dropped and the subpath ends.
-                const float twoPi = 6.28318530717958647692f;
-                const float4 ax = st.aux[sp];
-                const float dirPdf = ax.x, cosLast = ax.y, rrPend = ax.z;
-                const uint32_t info = __float_as_uint(ax.w);
-                const uint32_t k = st.numVerts[sp];
-                const float cosOut = absDot(-dir, -dir);
-                const BptPdf pd{cosOut, dirPdf * cosOut, rrPend, 0.0f, 0.0f,
-                                (kVtxSurface << kVfKindShift) | ((info & kAuxDelta) ? kVfDelta : 0u), 0.0f, 0.0f};
-                st.pdf[(size_t)k * st.S + sp] = pd;   // read by the MIS weight only
-                float theta, phi;
-                toPolarYUp(dir, &theta, &phi);
-                const float wlOff = st.wlOffset[p];
-                const int sel = (int)st.sel[p];
-                float lambdas[kNumLambda];
+            // Scene::interact (Scene.cpp:66-94): a collision in the medium
+            // before the surface, with the medium throughput on the way.
+            bool medHit = false;
+            float tMed = 0.0f;
+            V3 mparam = V3{0, 0, 0};
+            Spec sigmaE;
+            if (VOL && sc.medium.present) {
+                evalSpectrum(sc, sc.medium.sigmaE, lambdas, sigmaE);
+                Spec thr;
+                medHit = mediumInteract(sc.medium, org, dir, ro.w, h.prim == kNoHit ? inf : h.t, sigmaE, sel,
+                                        wlSelected, rng, &tMed, &mparam, thr);
 #pragma unroll
-                for (int q = 0; q < kNumLambda; ++q) lambdas[q] = lambdaAt(q, wlOff);
-                Spec Le;   // emittance x IBLEDF value
-                envRadiance(sc, phi / twoPi, theta / kPiF, lambdas, Le);
-                const float envProb = sc.envImportance / (sc.surfImportance + sc.envImportance);
-                const float e1 = envProb * envAreaPdf(sc, phi, theta);
-                const float e2 = (1.0f / sc.worldDiscArea) * cosLast;
-                MisSide eye{st.pdf, st.S, sp, k + 1, 1, e1, 1.0f, e2, 1.0f};
-                MisSide light{st.pdf, st.S, p, 0, 0, 0.0f, 0.0f, 0.0f, 0.0f};
-                const float mis = misWeight(eye, light);
-                if (!isinf(mis) && !isnan(mis)) {
-                    Spec alpha;
-                    loadAlpha(st.alphaPend, sp, alpha);
-                    Spec c;
-                    bool finite = true;
-#pragma unroll
-                    for (int q = 0; q < kNumLambda; ++q) {
-                        c.v[q] = (mis * alpha.v[q]) * Le.v[q];
-                        if ((info & kAuxWlSelected) && q == sel) c.v[q] *= kNumLambda;
-                        finite &= isfinite(c.v[q]);
-                    }
-                    if (finite) addConnection(st, p, c);
-                    else atomicAdd(&st.stats[2], 1ull);
-                }
+                for (int q = 0; q < kNumLambda; ++q) alpha.v[q] *= thr.v[q];
             }
-            if (h.prim != kNoHit) {
-                const DevPrim pr = sc.prims[h.prim];
-                SurfPoint spt;
-                surfacePoint(sc, pr, org, dir, h.t, h.b1, h.b2, spt);
-                const float4 ax = st.aux[sp];
-                float dirPdf = ax.x, cosLast = ax.y, rrPend = ax.z;
-                uint32_t info = __float_as_uint(ax.w);
-                bool wlSelected = (info & kAuxWlSelected) != 0;
-                const uint32_t k = st.numVerts[sp];   // index of the new vertex
-                const float dist2 = (info & kAuxPrevAtInf) ? 1.0f : sqLength(spt.p - org);
-                const V3 dirOut = spt.frame.toLocal(-dir);
-                const V3 gnl = spt.frame.toLocal(spt.gn);
-                const float cosOut = absDot(-dir, spt.gn);
+            if (!medHit && h.prim == kNoHit) {
+                if (!adjoint && sc.envPresent) {
+                    // The eye subpath reaches the environment: a vertex at
+                    // infinity (InfiniteSphereSurfaceShape.cpp:50-80) whose
+                    // implicit path is weighted against the light subpaths
+                    // that start there (BPTRenderer.cpp:318-345); the vertex
+                    // is then dropped and the subpath ends.
+                    const float cosOut = absDot(-dir, -dir);
+                    const BptPdf pd{cosOut, dirPdf * cosOut, rrPend, 0.0f, 0.0f,
+                                    (kVtxSurface << kVfKindShift) | ((info & kAuxDelta) ? kVfDelta : 0u), 0.0f, 0.0f};
+                    st.pdf[(size_t)k * st.S + sp] = pd;   // read by the MIS weight only
+                    float theta, phi;
+                    toPolarYUp(dir, &theta, &phi);
+                    Spec Le;   // emittance x IBLEDF value
+                    envRadiance(sc, phi / twoPi, theta / kPiF, lambdas, Le);
+                    // the light probability Scene::intersect gives the
+                    // environment; Scene::interact leaves the sphere's own 1
+                    const float envProb = VOL ? 1.0f : sc.envImportance / (sc.surfImportance + sc.envImportance);
+                    const float e1 = envProb * envAreaPdf(sc, phi, theta);
+                    const float e2 = (1.0f / sc.worldDiscArea) * cosLast;
+                    MisSide eye{st.pdf, st.S, sp, k + 1, 1, e1, 1.0f, e2, 1.0f};
+                    MisSide light{st.pdf, st.S, p, 0, 0, 0.0f, 0.0f, 0.0f, 0.0f};
+                    const float mis = misWeight(eye, light);
+                    if (!isinf(mis) && !isnan(mis)) {
+                        Spec c;
+                        bool finite = true;
+#pragma unroll
+                        for (int q = 0; q < kNumLambda; ++q) {
+                            c.v[q] = (mis * alpha.v[q]) * Le.v[q];
+                            if (wlSelected && q == sel) c.v[q] *= kNumLambda;
+                            finite &= isfinite(c.v[q]);
+                        }
+                        if (finite) addConnection(st, p, c);
+                        else atomicAdd(&st.stats[2], 1ull);
+                    }
+                }
+            } else {
+                // the new vertex: a surface point or a scattering point in the medium
+                V3 P, gn;
+                Frame fr;
+                DevMaterial mat;
+                float invArea = 0.0f;
+                if (medHit) {
+                    P = rn_ray_point(org, dir, tMed);
+                    fr = frameFromZ(normalize(dir));
+                    gn = V3{0.0f, 0.0f, 0.0f};
+                    const float dens = mediumDensity(sc.medium, mparam);
+                    // alpha *= the extinction coefficient at the point
+#pragma unroll
+                    for (int q = 0; q < kNumLambda; ++q) alpha.v[q] *= dens * sigmaE.v[q];
+                    mat.kind = kMatNull;
+                    mat.emit = -1;
+                } else {
+                    const DevPrim pr = sc.prims[h.prim];
+                    SurfPoint spt;
+                    surfacePoint(sc, pr, org, dir, h.t, h.b1, h.b2, spt);
+                    P = spt.p;
+                    fr = spt.frame;
+                    gn = spt.gn;
+                    mat = sc.materials[pr.material];
+                    invArea = pr.invArea;
+                }
+                const float dist2 = (info & kAuxPrevAtInf) ? 1.0f : sqLength(P - org);
+                const V3 dirOut = fr.toLocal(-dir);
+                const V3 gnl = fr.toLocal(gn);
+                const float cosOut = medHit ? 1.0f : absDot(-dir, gn);
                 const float areaPdf = dirPdf * cosOut / dist2;
-                Spec alpha;
-                loadAlpha(st.alphaPend, sp, alpha);
                 const size_t vi = (size_t)k * st.S + sp;
                 BptGeom g;
-                g.pg = make_float4(spt.p.x, spt.p.y, spt.p.z, __uint_as_float(pr.material));
-                g.ng = make_float4(spt.gn.x, spt.gn.y, spt.gn.z, dirOut.z);
-                g.nz = make_float4(spt.frame.z.x, spt.frame.z.y, spt.frame.z.z, dirOut.x);
-                g.tx = make_float4(spt.frame.x.x, spt.frame.x.y, spt.frame.x.z, dirOut.y);
+                g.pg = make_float4(P.x, P.y, P.z, __uint_as_float(medHit ? 0u : sc.prims[h.prim].material));
+                g.ng = make_float4(gn.x, gn.y, gn.z, dirOut.z);
+                g.nz = make_float4(fr.z.x, fr.z.y, fr.z.z, dirOut.x);
+                g.tx = make_float4(fr.x.x, fr.x.y, fr.x.z, dirOut.y);
                 st.geom[vi] = g;
                 BptPdf pd;
                 pd.cosIn = cosOut;
@@ -559,8 +618,7 @@ __global__ void __launch_bounds__(256, 2) kBptBounce(DevScene sc, BptState st, c
                 pd.rrProb = rrPend;
                 pd.revAreaPdf = 0.0f;
                 pd.revRRProb = 0.0f;
-                const DevMaterial mat = sc.materials[pr.material];
-                pd.flags = (kVtxSurface << kVfKindShift) | (mat.kind << kVfMatShift) |
+                pd.flags = ((medHit ? kVtxMedium : kVtxSurface) << kVfKindShift) | (mat.kind << kVfMatShift) |
                            ((info & kAuxDelta) ? kVfDelta : 0u) | (wlSelected ? kVfWlSelected : 0u);
                 pd.pad0 = pd.pad1 = 0.0f;
                 st.pdf[vi] = pd;
@@ -568,24 +626,37 @@ __global__ void __launch_bounds__(256, 2) kBptBounce(DevScene sc, BptState st, c
                 st.numVerts[sp] = k + 1;
                 conn = !adjoint;
 
-                const float wlOff = st.wlOffset[p];
-                const int sel = (int)st.sel[p];
-                float lambdas[kNumLambda];
-#pragma unroll
-                for (int q = 0; q < kNumLambda; ++q) lambdas[q] = lambdaAt(q, wlOff);
+                // the vertex's BSDF: the material's, or the medium's
+                // VolumetricBSDF (albedo x Henyey-Greenstein,
+                // directional_distribution_functions.cpp:78-104,
+                // medium_object.cpp:106-112)
                 Bsdf B;
-                makeBsdf(sc, mat, lambdas, wlSelected, B);
-                storeAlpha(st.bsdfA, vi, B.a);   // the connections reuse it (Lambert reflectance)
+                if (medHit) {
+                    B.kind = kMatNull;
+                    B.ax = B.ay = 0.0f;
+                    B.dispersive = false;
+                    Spec sigmaS;
+                    evalSpectrum(sc, sc.medium.sigmaS, lambdas, sigmaS);
+                    const bool in = !outsideUnit(mparam);
+#pragma unroll
+                    for (int q = 0; q < kNumLambda; ++q)
+                        B.a.v[q] = (in && sigmaE.v[q] > 0) ? sigmaS.v[q] / sigmaE.v[q] : 0.0f;
+                } else {
+                    makeBsdf(sc, mat, lambdas, wlSelected, B);
+                }
+                storeAlpha(st.bsdfA, vi, B.a);   // the connections reuse it (Lambert reflectance, albedo)
                 // Implicit path, no light subpath vertex (BPTRenderer.cpp:318-340).
-                if (!adjoint && mat.emit >= 0) {
+                if (!adjoint && !medHit && mat.emit >= 0) {
                     Spec Le0;
                     evalSpectrum(sc, mat.emit, lambdas, Le0);
                     const float Le1 = dirOut.z > 0.0f ? kInvPiF : 0.0f;
-                    // Scene::intersect's light probability: the emitter's share
-                    // of the surface aggregate (all emitting triangles weigh 1).
-                    const float hitLightProb = (sc.surfImportance / (sc.surfImportance + sc.envImportance)) *
-                                               sc.lightPMF[0];
-                    const float e1 = hitLightProb * pr.invArea;
+                    // The light probability of the hit: Scene::intersect gives
+                    // the emitter's share of the surface aggregate times the
+                    // surfaces' share of all lights (all emitting triangles
+                    // weigh 1); Scene::interact (volumetric) leaves the
+                    // surfaces' share out (Scene.cpp:80-84).
+                    const float surfShare = VOL ? 1.0f : sc.surfImportance / (sc.surfImportance + sc.envImportance);
+                    const float e1 = surfShare * sc.lightPMF[0] * invArea;
                     const float e2 = (dirOut.z > 0.0f ? dirOut.z * kInvPiF : 0.0f) * cosLast / dist2;
                     MisSide eye{st.pdf, st.S, sp, k + 1, 1, e1, 1.0f, e2, 1.0f};
                     MisSide light{st.pdf, st.S, p, 0, 0, 0.0f, 0.0f, 0.0f, 0.0f};
@@ -604,17 +675,27 @@ __global__ void __launch_bounds__(256, 2) kBptBounce(DevScene sc, BptState st, c
                     }
                 }
                 if (k < st.D) {
-                    Rng rng{keyOf(st, p), st.rngCounter[sp]};
-                    RevQuery q{dirOut, gnl, sel, adjoint};
-                    const float uc = rng.next(), u0 = rng.next(), u1 = rng.next();
                     BsdfSample bs;
                     Spec fs, revFs;
                     float revPdf;
-                    bsdfSampleRev(B, q, uc, u0, u1, &bs, fs, &revPdf, revFs);
+                    if (medHit) {
+                        // PhaseFunction sample (basic_phase_functions.cpp:38-52)
+                        const float u0 = rng.next(), u1 = rng.next();
+                        bs.dir = hgSample(sc.medium.g, u0, u1, &bs.pdf);
+                        bs.type = kDirLowFreq;
+                        revPdf = bs.pdf;
+#pragma unroll
+                        for (int q = 0; q < kNumLambda; ++q) fs.v[q] = B.a.v[q] * bs.pdf;
+                        revFs = fs;
+                    } else {
+                        RevQuery q{dirOut, gnl, sel, adjoint};
+                        const float uc = rng.next(), u0 = rng.next(), u1 = rng.next();
+                        bsdfSampleRev(B, q, uc, u0, u1, &bs, fs, &revPdf, revFs);
+                    }
                     if (bs.pdf != 0.0f && !specIsZero(fs)) {
                         if ((bs.type & kDirDispersive) && !wlSelected) wlSelected = true;
-                        const V3 vecIn = spt.frame.fromLocal(bs.dir);
-                        const float cosIn = absDot(vecIn, spt.gn);
+                        const V3 vecIn = fr.fromLocal(bs.dir);
+                        const float cosIn = medHit ? 1.0f : absDot(vecIn, gn);
                         Spec weight;
 #pragma unroll
                         for (int c = 0; c < kNumLambda; ++c) weight.v[c] = fs.v[c] * (cosIn / bs.pdf);
@@ -630,16 +711,16 @@ __global__ void __launch_bounds__(256, 2) kBptBounce(DevScene sc, BptState st, c
                             for (int c = 0; c < kNumLambda; ++c) rv.v[c] = revFs.v[c] * cosOut / revPdf;
                             prev->revRRProb = stdMin(importance(rv, sel), 1.0f);
                             storeAlpha(st.alphaPend, sp, alpha);
-                            st.rayOrg[sp] = make_float4(spt.p.x, spt.p.y, spt.p.z, kRayEpsilon);
+                            st.rayOrg[sp] = make_float4(P.x, P.y, P.z, kRayEpsilon);
                             st.rayDir[sp] = make_float4(vecIn.x, vecIn.y, vecIn.z, 0.0f);
                             info = (dirIsDelta(bs.type) ? kAuxDelta : 0u) | (wlSelected ? kAuxWlSelected : 0u);
                             st.aux[sp] = make_float4(bs.pdf, cosIn, rr, __uint_as_float(info));
                             extend = true;
                         }
                     }
-                    st.rngCounter[sp] = rng.counter;
                 }
             }
+            st.rngCounter[sp] = rng.counter;
         }
         queuePush(outQueue, outCount, sp, active && extend);
         queuePush(st.connQueue, st.counters + st.D + 1, sp + (uint32_t)(st.numVerts[sp] - 1) * st.S,
@@ -662,13 +743,15 @@ __device__ __forceinline__ void vertexBsdf(const DevScene &sc, const BptState &s
     }
 }
 
-// One connection (BPTRenderer.cpp:174-280): eye vertex evi (t = its index
-// + 1) with light vertex s of the same path.  Returns false when the
-// connection adds nothing (zero connection term, invalid MIS weight) or is
-// dropped as non-finite (*dropped set); else the shadow ray and the
-// contribution, binned into film bins when it lands through the lens
-// (t = 1, *target = pixel | kTargetSplat) or per wavelength for the path's
-// own sum (*target = path).
+// One connection (BPTRenderer.cpp:174-280; VOL: VolumetricBPTRenderer.cpp:
+// 174-286): eye vertex evi (t = its index + 1) with light vertex s of the
+// same path.  Returns false when the connection adds nothing (zero
+// connection term, invalid MIS weight) or is dropped as non-finite
+// (*dropped set); else the shadow ray and the contribution, *target = path,
+// or pixel | kTargetSplat when it lands through the lens (t = 1).  Without
+// a medium the splat contribution comes binned into film bins; VOL leaves it
+// per wavelength for the transmittance.
+template <bool VOL>
 __device__ bool connectOne(const DevScene &sc, const BptState &st, uint32_t evi, uint32_t s, uint32_t width,
                            uint32_t height, float4* rayOrg, float4* rayDir, Spec &c, uint32_t* target,
                            bool* dropped) {
@@ -684,13 +767,14 @@ __device__ bool connectOne(const DevScene &sc, const BptState &st, uint32_t evi,
     for (int q = 0; q < kNumLambda; ++q) lambdas[q] = lambdaAt(q, wlOff);
     const BptGeom eg = st.geom[evi];
     const BptPdf ep = st.pdf[evi];
-    const V3 eP = xyz(eg.pg), eN = xyz(eg.ng);
+    const V3 eP = xyz(eg.pg);
     const Frame eF = vertexFrame(eg);
-    const bool eLens = (ep.flags >> kVfKindShift) == kVtxLens;
+    const uint32_t eKind = ep.flags >> kVfKindShift & 3u;
     const size_t lvi = (size_t)(s - 1) * st.S + p;
     const BptGeom lg = st.geom[lvi];
     const BptPdf lpd = st.pdf[lvi];
-    const V3 lP = xyz(lg.pg), lN = xyz(lg.ng);
+    const uint32_t lKind = lpd.flags >> kVfKindShift & 3u;
+    const V3 lP = xyz(lg.pg);
     const Frame lF = vertexFrame(lg);
     // InteractionPoint::getDirectionFrom (geometry.h:147-157): a vertex at
     // infinity is a direction at squared distance 1
@@ -698,10 +782,10 @@ __device__ bool connectOne(const DevScene &sc, const BptState &st, uint32_t evi,
     V3 cv = lInf ? lP : lP - eP;
     const float dist2 = lInf ? 1.0f : sqLength(cv);
     cv = lInf ? normalize(cv) : cv * (1.0f / sqrtf(dist2));
-    const float cosLightEnd = absDot(cv, lN);
-    const float cosEyeEnd = absDot(cv, eN);
+    const float cosLightEnd = vertexCos(lg, lpd.flags, cv);
+    const float cosEyeEnd = vertexCos(eg, ep.flags, cv);
     const float G = cosEyeEnd * cosLightEnd / dist2;
-    // light end: EDF of the light vertex or the adjoint BSDF
+    // light end: EDF of the light vertex, the adjoint BSDF or the medium's
     const V3 lc = lF.toLocal(-cv);
     Spec lDDF, lRev;
     float lExt1DirPdf, eExt2DirPdf = 0.0f;
@@ -713,25 +797,41 @@ __device__ bool connectOne(const DevScene &sc, const BptState &st, uint32_t evi,
         lDDF = specConst(lc.z > 0.0f ? kInvPiF : 0.0f);
         lRev = lDDF;
         lExt1DirPdf = lc.z > 0.0f ? lc.z * kInvPiF : 0.0f;
+    } else if (VOL && lKind == kVtxMedium) {   // albedo x Henyey-Greenstein, symmetric
+        Spec albedo;
+        loadAlpha(st.bsdfA, lvi, albedo);
+        lExt1DirPdf = hgValue(sc.medium.g, lc.z);
+        eExt2DirPdf = lExt1DirPdf;
+#pragma unroll
+        for (int q = 0; q < kNumLambda; ++q) lDDF.v[q] = albedo.v[q] * lExt1DirPdf;
+        lRev = lDDF;
     } else {
         Bsdf lB;
         vertexBsdf(sc, st, lvi, __float_as_uint(lg.pg.w), lpd.flags, lambdas, lB);
-        RevQuery lq{V3{lg.nz.w, lg.tx.w, lg.ng.w}, lF.toLocal(lN), sel, true};
+        RevQuery lq{V3{lg.nz.w, lg.tx.w, lg.ng.w}, lF.toLocal(xyz(lg.ng)), sel, true};
         bsdfEvalRev(lB, lq, lc, lDDF, lRev);
         lExt1DirPdf = bsdfPdfRev(lB, lq, lc, &eExt2DirPdf);
     }
-    // eye end: importance of the lens or the BSDF
+    // eye end: importance of the lens, the BSDF or the medium's
     const V3 ec = eF.toLocal(cv);
     Spec eDDF, eRev;
     float eExt1DirPdf, lExt2DirPdf = 0.0f;
-    if (eLens) {
+    if (eKind == kVtxLens) {
         eDDF = specConst(idfInside(sc.camera, ec, eg.nz.w, eg.tx.w) ? 1.0f : 0.0f);
         eRev = eDDF;
         eExt1DirPdf = idfPdf(sc.camera, ec, eg.nz.w, eg.tx.w);
+    } else if (VOL && eKind == kVtxMedium) {
+        Spec albedo;
+        loadAlpha(st.bsdfA, evi, albedo);
+        eExt1DirPdf = hgValue(sc.medium.g, ec.z);
+        lExt2DirPdf = eExt1DirPdf;
+#pragma unroll
+        for (int q = 0; q < kNumLambda; ++q) eDDF.v[q] = albedo.v[q] * eExt1DirPdf;
+        eRev = eDDF;
     } else {
         Bsdf eB;
         vertexBsdf(sc, st, evi, __float_as_uint(eg.pg.w), ep.flags, lambdas, eB);
-        RevQuery eq{V3{eg.nz.w, eg.tx.w, eg.ng.w}, eF.toLocal(eN), sel, false};
+        RevQuery eq{V3{eg.nz.w, eg.tx.w, eg.ng.w}, eF.toLocal(xyz(eg.ng)), sel, false};
         bsdfEvalRev(eB, eq, ec, eDDF, eRev);
         eExt1DirPdf = bsdfPdfRev(eB, eq, ec, &lExt2DirPdf);
     }
@@ -757,10 +857,11 @@ __device__ bool connectOne(const DevScene &sc, const BptState &st, uint32_t evi,
     float lExt2Area = 0.0f, lExt2RR = 0.0f;
     if (t > 1) {
         const BptGeom g2 = st.geom[evi - st.S];
+        const uint32_t f2 = st.pdf[evi - st.S].flags;
         V3 d2 = eP - xyz(g2.pg);
         const float dd2 = sqLength(d2);
         d2 = d2 * (1.0f / sqrtf(dd2));
-        lExt2Area = lExt2DirPdf * absDot(d2, xyz(g2.ng)) / dd2;
+        lExt2Area = lExt2DirPdf * vertexCos(g2, f2, d2) / dd2;
 #pragma unroll
         for (int q = 0; q < kNumLambda; ++q) tmp.v[q] = eRev.v[q] * ep.cosIn / lExt2DirPdf;
         lExt2RR = stdMin(importance(tmp, sel), 1.0f);
@@ -772,11 +873,12 @@ __device__ bool connectOne(const DevScene &sc, const BptState &st, uint32_t evi,
     float eExt2Area = 0.0f, eExt2RR = 0.0f;
     if (s > 1) {
         const BptGeom l2 = st.geom[lvi - st.S];
-        const bool l2Inf = (st.pdf[lvi - st.S].flags & kVfAtInf) != 0;
+        const uint32_t f2 = st.pdf[lvi - st.S].flags;
+        const bool l2Inf = (f2 & kVfAtInf) != 0;
         V3 d2 = l2Inf ? xyz(l2.pg) : xyz(l2.pg) - lP;
         const float dd2 = l2Inf ? 1.0f : sqLength(d2);
         d2 = l2Inf ? normalize(d2) : d2 * (1.0f / sqrtf(dd2));
-        eExt2Area = eExt2DirPdf * absDot(d2, xyz(l2.ng)) / dd2;
+        eExt2Area = eExt2DirPdf * vertexCos(l2, f2, d2) / dd2;
 #pragma unroll
         for (int q = 0; q < kNumLambda; ++q) tmp.v[q] = lRev.v[q] * lpd.cosIn / eExt2DirPdf;
         eExt2RR = stdMin(importance(tmp, sel), 1.0f);
@@ -798,7 +900,7 @@ __device__ bool connectOne(const DevScene &sc, const BptState &st, uint32_t evi,
         *dropped = true;
         return false;
     }
-    // Scene::testVisibility (Scene.cpp:96-112)
+    // Scene::testVisibility (Scene.cpp:96-135)
     *rayOrg = make_float4(eP.x, eP.y, eP.z, kRayEpsilon);
     if (lInf) {
         *rayDir = make_float4(cv.x, cv.y, cv.z, 3.402823466e+38f);
@@ -816,14 +918,13 @@ __device__ bool connectOne(const DevScene &sc, const BptState &st, uint32_t evi,
     const uint32_t ipx = min((uint32_t)fmaxf(hx, 0.0f), width - 1);
     const uint32_t ipy = min((uint32_t)fmaxf(hy, 0.0f), height - 1);
     *target = (ipy * width + ipx) | kTargetSplat;
+    if (VOL) return true;
     // SpectrumStorage::add (spectrum_types.h:725-734): wavelength -> film bin
     const float recBinWidth = kNumLambda / (kWavelengthHigh - kWavelengthLow);
     Spec binned = specConst(0.0f);
 #pragma unroll
     for (int q = 0; q < kNumLambda; ++q) {
-        const float f = __fmul_rn(__fdiv_rn(__fsub_rn(lambdas[q], kWavelengthLow), kWavelengthHigh - kWavelengthLow),
-                                  (float)kNumLambda);
-        const uint32_t bin = min((uint32_t)f, (uint32_t)(kNumLambda - 1));
+        const uint32_t bin = filmBin(lambdas[q]);
 #pragma unroll
         for (int b = 0; b < kNumLambda; ++b)
             if (b == (int)bin) binned.v[b] += c.v[q] * recBinWidth;
@@ -832,12 +933,35 @@ __device__ bool connectOne(const DevScene &sc, const BptState &st, uint32_t evi,
     return true;
 }
 
+// Medium transmittance of one wavelength of a connection (Scene::testVisibility,
+// Scene.cpp:114-135, with MediumObjectAggregate::evaluateTransmittance): the
+// kernel's wavelengths are never selected there, so every wavelength is
+// tracked; the random numbers come from a stream of the connection.
+__device__ __forceinline__ float connectionTransmittance(const DevScene &sc, const BptState &st, float4 o, float4 d,
+                                                         uint32_t p, uint32_t meta, int wl, const Spec &sigmaE) {
+    Rng rng{mix64(keyOf(st, p) ^ (0x9e3779b97f4a7c15ull * (meta + 1))), (uint32_t)wl << 24};
+    return mediumTransmittanceWl(sc.medium, xyz(o), xyz(d), o.w, d.w, specAt(sigmaE, wl), true, rng);
+}
+
+// Adds one wavelength of a volumetric connection (film bin for a splat).
+__device__ __forceinline__ void addConnectionWl(const BptState &st, uint32_t target, uint32_t p, int wl, float v) {
+    if (v == 0.0f) return;
+    if (target & kTargetSplat) {
+        const float recBinWidth = kNumLambda / (kWavelengthHigh - kWavelengthLow);
+        const uint32_t bin = filmBin(lambdaAt(wl, st.wlOffset[p]));
+        atomicAdd(&st.splat[(size_t)(target & ~kTargetSplat) * kNumLambda + bin], v * recBinWidth);
+    } else {
+        atomicAdd(&st.L[(size_t)target * kNumLambda + wl], v);
+    }
+}
+
 // Connections of the queued eye vertices with every light vertex of their
 // paths, spread over the lanes of a warp: a warp takes 32 eye vertices,
 // prefix-sums their light-subpath lengths and gives each lane one
 // (eye vertex, light vertex) pair per round, so lanes stay busy whatever the
 // subpath lengths.  Connections that contribute go to the shadow queue (or,
 // when it is full, are traced here).
+template <bool VOL>
 __global__ void __launch_bounds__(256, 2) kBptConnect(DevScene sc, BptState st, uint32_t width, uint32_t height,
                                                       const uint32_t* __restrict__ queue,
                                                       const uint32_t* __restrict__ count, uint32_t* shCount) {
@@ -872,13 +996,14 @@ __global__ void __launch_bounds__(256, 2) kBptConnect(DevScene sc, BptState st, 
             o = min(o, 31u);
             const uint32_t ev = __shfl_sync(full, evi, o);
             const uint32_t first = __shfl_sync(full, incl, o) - __shfl_sync(full, nL, o);
+            const uint32_t sIdx = j - first + 1;
             bool push = false;
             float4 ro, rd;
             Spec c;
             uint32_t target = 0;
             if (j < total) {
                 bool drop;
-                push = connectOne(sc, st, ev, j - first + 1, width, height, &ro, &rd, c, &target, &drop);
+                push = connectOne<VOL>(sc, st, ev, sIdx, width, height, &ro, &rd, c, &target, &drop);
                 dropped += drop ? 1 : 0;
             }
             const unsigned mask = __ballot_sync(full, push);
@@ -886,14 +1011,39 @@ __global__ void __launch_bounds__(256, 2) kBptConnect(DevScene sc, BptState st, 
             if (lane == 0 && mask) slot = atomicAdd(shCount, (uint32_t)__popc(mask));
             slot = __shfl_sync(full, slot, 0) + __popc(mask & ((1u << lane) - 1));
             if (push) {
+                const uint32_t p = ev % st.S - st.N;
+                const uint32_t meta = (ev / st.S) << 8 | sIdx;
                 if (slot < st.connCap) {
                     st.cRay[2 * (size_t)slot] = ro;
                     st.cRay[2 * (size_t)slot + 1] = rd;
                     storeAlpha(st.cContrib, slot, c);
                     st.cTarget[slot] = target;
+                    if (VOL) {
+                        st.cPath[slot] = p;
+                        st.cMeta[slot] = meta;
+                    }
                 } else {
                     ++traced;
-                    if (!traceAny(sc, xyz(ro), xyz(rd), ro.w, rd.w)) addConnection(st, target, c);
+                    if (!traceAny(sc, xyz(ro), xyz(rd), ro.w, rd.w)) {
+                        if (VOL && sc.medium.present) {
+                            float lambdas[kNumLambda];
+                            const float wlOff = st.wlOffset[p];
+#pragma unroll
+                            for (int q = 0; q < kNumLambda; ++q) lambdas[q] = lambdaAt(q, wlOff);
+                            Spec sigmaE;
+                            evalSpectrum(sc, sc.medium.sigmaE, lambdas, sigmaE);
+                            for (int wl = 0; wl < kNumLambda; ++wl) {
+                                const float cw = specAt(c, wl);
+                                if (cw == 0.0f) continue;
+                                addConnectionWl(st, target, p, wl,
+                                                cw * connectionTransmittance(sc, st, ro, rd, p, meta, wl, sigmaE));
+                            }
+                        } else if (VOL) {
+                            for (int wl = 0; wl < kNumLambda; ++wl) addConnectionWl(st, target, p, wl, specAt(c, wl));
+                        } else {
+                            addConnection(st, target, c);
+                        }
+                    }
                 }
             }
         }
@@ -903,18 +1053,56 @@ __global__ void __launch_bounds__(256, 2) kBptConnect(DevScene sc, BptState st, 
 }
 
 // Shadow rays of the queued connections; unoccluded ones add their
-// contribution.
+// contribution, or (VOL) wait for their medium transmittance.
+template <bool VOL>
 __global__ void __launch_bounds__(256, SLRGPU_TRACE_MIN_BLOCKS) kBptShadow(DevScene sc, BptState st,
-                                                                         const uint32_t* __restrict__ shCount) {
+                                                                         const uint32_t* __restrict__ shCount,
+                                                                         uint32_t* medCount) {
     const uint32_t n = min(*shCount, st.connCap);
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const float4 o = st.cRay[2 * (size_t)i], d = st.cRay[2 * (size_t)i + 1];
-        if (traceAny(sc, xyz(o), xyz(d), o.w, d.w)) continue;
-        Spec c;
-        loadAlpha(st.cContrib, i, c);
-        addConnection(st, st.cTarget[i], c);
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+        const uint32_t i = base + threadIdx.x;
+        bool pushMedium = false;
+        if (i < n) {
+            const float4 o = st.cRay[2 * (size_t)i], d = st.cRay[2 * (size_t)i + 1];
+            if (!traceAny(sc, xyz(o), xyz(d), o.w, d.w)) {
+                if (VOL) {
+                    pushMedium = true;
+                } else {
+                    Spec c;
+                    loadAlpha(st.cContrib, i, c);
+                    addConnection(st, st.cTarget[i], c);
+                }
+            }
+        }
+        if (VOL) queuePush(st.mQueue, medCount, i, pushMedium);
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&st.stats[1], (unsigned long long)n);
+}
+
+// Medium transmittance of the unoccluded volumetric connections, one thread
+// per (connection, wavelength) as the path tracer's shadow rays do.
+__global__ void __launch_bounds__(256, SLRGPU_MEDIUM_MIN_BLOCKS) kVbptMedium(DevScene sc, BptState st,
+                                                                           const uint32_t* __restrict__ medCount) {
+    const uint32_t n = *medCount * kNumLambda;
+    for (uint32_t item = blockIdx.x * blockDim.x + threadIdx.x; item < n; item += gridDim.x * blockDim.x) {
+        const uint32_t slot = st.mQueue[item / kNumLambda];
+        const int wl = (int)(item % kNumLambda);
+        const float cw = reinterpret_cast<const float*>(st.cContrib)[(size_t)slot * kNumLambda + wl];
+        if (cw == 0.0f) continue;
+        const uint32_t p = st.cPath[slot];
+        float T = 1.0f;
+        if (sc.medium.present) {
+            float lambdas[kNumLambda];
+            const float wlOff = st.wlOffset[p];
+#pragma unroll
+            for (int q = 0; q < kNumLambda; ++q) lambdas[q] = lambdaAt(q, wlOff);
+            Spec sigmaE;
+            evalSpectrum(sc, sc.medium.sigmaE, lambdas, sigmaE);
+            T = connectionTransmittance(sc, st, st.cRay[2 * (size_t)slot], st.cRay[2 * (size_t)slot + 1], p,
+                                        st.cMeta[slot], wl, sigmaE);
+        }
+        addConnectionWl(st, st.cTarget[slot], p, wl, cw * T);
+    }
 }
 
 // The wave's contributions into the compensated film: per pixel, the sums of
@@ -975,16 +1163,21 @@ int gridFor(const void* kernel, int block) {
 }
 
 struct BptGrids {
-    int init, bounce, connect, shadow, accumulate;
+    int init[2], bounce[2], connect[2], shadow[2], medium, accumulate;
 };
 const BptGrids &bptGrids() {
     static BptGrids g;
     static std::once_flag once;
     std::call_once(once, [&]() {
-        g.init = gridFor((const void*)kBptInit, 256);
-        g.bounce = gridFor((const void*)kBptBounce, 256);
-        g.connect = gridFor((const void*)kBptConnect, 256);
-        g.shadow = gridFor((const void*)kBptShadow, 256);
+        g.init[0] = gridFor((const void*)kBptInit<false>, 256);
+        g.init[1] = gridFor((const void*)kBptInit<true>, 256);
+        g.bounce[0] = gridFor((const void*)kBptBounce<false>, 256);
+        g.bounce[1] = gridFor((const void*)kBptBounce<true>, 256);
+        g.connect[0] = gridFor((const void*)kBptConnect<false>, 256);
+        g.connect[1] = gridFor((const void*)kBptConnect<true>, 256);
+        g.shadow[0] = gridFor((const void*)kBptShadow<false>, 256);
+        g.shadow[1] = gridFor((const void*)kBptShadow<true>, 256);
+        g.medium = gridFor((const void*)kVbptMedium, 256);
         g.accumulate = gridFor((const void*)kBptAccumulate, 256);
     });
     return g;
@@ -1043,7 +1236,10 @@ struct BptEngine {
                   (s.cRay = alloc<float4>((size_t)kConnPerPath * N * 2, &e)) &&
                   (s.cContrib = alloc<float4>((size_t)kConnPerPath * N * 4, &e)) &&
                   (s.cTarget = alloc<uint32_t>((size_t)kConnPerPath * N, &e)) &&
-                  (s.counters = alloc<uint32_t>(D + 3, &e)) && (s.stats = alloc<unsigned long long>(4, &e));
+                  (s.cPath = alloc<uint32_t>((size_t)kConnPerPath * N, &e)) &&
+                  (s.cMeta = alloc<uint32_t>((size_t)kConnPerPath * N, &e)) &&
+                  (s.mQueue = alloc<uint32_t>((size_t)kConnPerPath * N, &e)) &&
+                  (s.counters = alloc<uint32_t>(D + 4, &e)) && (s.stats = alloc<unsigned long long>(4, &e));
         if (!ok) {
             release();
             setError(std::string("bidirectional path state allocation failed: ") + cudaGetErrorString(e));
@@ -1070,16 +1266,13 @@ void bptEngineDestroy(BptEngine* e) { delete e; }
 uint64_t bptStateBytesPerPath(uint32_t maxDepth) {
     const uint64_t V = 2ull * (maxDepth + 1);
     return V * (sizeof(BptGeom) + sizeof(BptPdf) + 128) + 2 * (16 + 16 + 64 + 16 + 4 + 4) + 8 + 8 + 4 + 4 +
-           4 * kNumLambda + 8 + 4ull * (maxDepth + 1) + kConnPerPath * (32 + 64 + 4);
+           4 * kNumLambda + 8 + 4ull * (maxDepth + 1) + kConnPerPath * (32 + 64 + 16);
 }
 
 int renderBpt(BptEngine &eng, const DeviceScene &ds, const slrgpu_settings &s, float* filmSum, float* filmComp,
               cudaStream_t stream, uint64_t* launches, std::vector<cudaEvent_t>* eventPool,
               slrgpu_render_stats* stats) {
-    if (s.volumetric) {
-        setError("the volumetric bidirectional path tracer is not implemented");
-        return SLRGPU_ERR_UNSUPPORTED;
-    }
+    const bool vol = s.volumetric != 0;
     if (ds.sc.numLights == 0 && !ds.sc.envPresent) {
         setError("bidirectional path tracing needs a light (an emitting surface or an environment)");
         return SLRGPU_ERR_INVALID_ARGUMENT;
@@ -1148,25 +1341,43 @@ int renderBpt(BptEngine &eng, const DeviceScene &ds, const slrgpu_settings &s, f
         wv.samples = std::min(S, s.spp - base);
         wv.seed = s.seed;
         wv.numPaths = wv.samples * G;
-        cudaMemsetAsync(st.counters, 0, (D + 3) * sizeof(uint32_t), stream);
+        cudaMemsetAsync(st.counters, 0, (D + 4) * sizeof(uint32_t), stream);
         mark(SLRGPU_KERNEL_RAYGEN);
-        kBptInit<<<g.init, 256, 0, stream>>>(ds.sc, st, wv);
+        if (vol) kBptInit<true><<<g.init[1], 256, 0, stream>>>(ds.sc, st, wv);
+        else kBptInit<false><<<g.init[0], 256, 0, stream>>>(ds.sc, st, wv);
         markEnd();
         ++nl;
         for (uint32_t b = 0; b < D; ++b) {
             mark(SLRGPU_KERNEL_EXTEND);
-            kBptBounce<<<g.bounce, 256, 0, stream>>>(ds.sc, st, st.queue[b & 1], st.counters + b,
-                                                     st.queue[(b + 1) & 1], st.counters + b + 1);
+            if (vol)
+                kBptBounce<true><<<g.bounce[1], 256, 0, stream>>>(ds.sc, st, st.queue[b & 1], st.counters + b,
+                                                                   st.queue[(b + 1) & 1], st.counters + b + 1);
+            else
+                kBptBounce<false><<<g.bounce[0], 256, 0, stream>>>(ds.sc, st, st.queue[b & 1], st.counters + b,
+                                                                    st.queue[(b + 1) & 1], st.counters + b + 1);
             markEnd();
             ++nl;
         }
         mark(SLRGPU_KERNEL_SHADE);
-        kBptConnect<<<g.connect, 256, 0, stream>>>(ds.sc, st, s.width, s.height, st.connQueue, st.counters + D + 1,
-                                                   st.counters + D + 2);
+        if (vol)
+            kBptConnect<true><<<g.connect[1], 256, 0, stream>>>(ds.sc, st, s.width, s.height, st.connQueue,
+                                                                 st.counters + D + 1, st.counters + D + 2);
+        else
+            kBptConnect<false><<<g.connect[0], 256, 0, stream>>>(ds.sc, st, s.width, s.height, st.connQueue,
+                                                                  st.counters + D + 1, st.counters + D + 2);
         markEnd();
         mark(SLRGPU_KERNEL_SHADOW);
-        kBptShadow<<<g.shadow, 256, 0, stream>>>(ds.sc, st, st.counters + D + 2);
+        if (vol)
+            kBptShadow<true><<<g.shadow[1], 256, 0, stream>>>(ds.sc, st, st.counters + D + 2, st.counters + D + 3);
+        else
+            kBptShadow<false><<<g.shadow[0], 256, 0, stream>>>(ds.sc, st, st.counters + D + 2, st.counters + D + 3);
         markEnd();
+        if (vol) {
+            mark(SLRGPU_KERNEL_SHADOW);
+            kVbptMedium<<<g.medium, 256, 0, stream>>>(ds.sc, st, st.counters + D + 3);
+            markEnd();
+            ++nl;
+        }
         mark(SLRGPU_KERNEL_ACCUMULATE);
         kBptAccumulate<<<g.accumulate, 256, 0, stream>>>(st, wv, filmSum, filmComp);
         markEnd();

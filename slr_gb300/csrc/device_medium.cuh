@@ -150,7 +150,7 @@ __device__ __forceinline__ void svPolyCoeffs(const DevMedium &m, V3 entry, V3 ex
 // false (and *dist = dmax) when the walk leaves the segment.
 constexpr int kMaxSvSteps = 4096;
 
-__device__ __noinline__ bool svTraverse(const DevMedium &m, V3 org, V3 dir, float dmin, float dmax, float u,
+static __device__ __noinline__ bool svTraverse(const DevMedium &m, V3 org, V3 dir, float dmin, float dmax, float u,
                                         float sigma, const SvSetup &s, SvWalk &w, float* dist, float* majorant) {
     float sampledOD = -logf(1 - u);
     if (sampledOD == 0.0f) {

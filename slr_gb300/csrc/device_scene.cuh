@@ -234,6 +234,47 @@ __device__ __forceinline__ int selectLight(const DevScene &sc, float u, float* p
 }
 
 
+// Scene::selectLight (Scene.cpp:157-188) with sampleDiscrete
+// (distributions.cpp:16-36) over {surfaces, media, environment}.  Returns 0
+// surface (light index in *li), 2 environment; *prob = selection probability.
+__device__ __forceinline__ int selectLight3(const DevScene &sc, float u, int* li, float* prob) {
+    float imps[3] = {sc.surfImportance, sc.medium.importance, sc.envImportance};
+    // compensated sums as in the reference
+    float sum = 0.0f, c = 0.0f;
+    for (int i = 0; i < 3; ++i) {
+        float y = imps[i] - c, t = sum + y;
+        c = (t - sum) - y;
+        sum = t;
+    }
+    float su = u * sum;
+    float cum = 0.0f, cc = 0.0f, base = 0.0f;
+    int idx = 0;
+    float prob1st = imps[0] / sum, remapped = u;
+    bool found = false;
+    for (int i = 0; i < 3; ++i) {
+        base = cum;
+        float y = imps[i] - cc, t = cum + y;
+        cc = (t - cum) - y;
+        cum = t;
+        if (!found && su < cum) {
+            idx = i;
+            prob1st = imps[i] / sum;
+            remapped = (su - base) / imps[i];
+            found = true;
+        }
+    }
+    if (idx == 0) {
+        float frac;
+        const int j = (int)aliasPick(sc.lightAlias, sc.numLights, remapped, &frac);
+        *li = j;
+        *prob = sc.lightPMF[j] * prob1st;
+    } else {
+        *li = -1;
+        *prob = 1.0f * prob1st;
+    }
+    return idx;
+}
+
 template <int K>
 __device__ __forceinline__ void makeBsdfK(const DevScene &sc, const DevMaterial &m, const float lambdas[kNumLambda],
                                           bool wlSelected, Bsdf &B) {

@@ -19,11 +19,11 @@ from test_gpu_render import check_statistical_parity
 pytestmark = pytest.mark.gpu
 
 
-def oracle_bpt_batches(oracle_lib, desc, w, h, spp, depth, batches, seed0):
+def oracle_bpt_batches(oracle_lib, desc, w, h, spp, depth, batches, seed0, volumetric=False):
     means, dropped = [], 0
     for k in range(batches):
         ref = oracle_lib.RefScene(desc)      # one BPT render per reference sensor
-        film, _ = ref.render_bpt(w, h, spp, depth, seed=seed0 + k, threads=os.cpu_count())
+        film, _ = ref.render_bpt(w, h, spp, depth, seed=seed0 + k, threads=os.cpu_count(), volumetric=volumetric)
         dropped += ref.last_dropped
         means.append(film.astype(np.float64) / spp)
     return np.stack(means), dropped
@@ -133,11 +133,24 @@ def test_bpt_environment_matches_reference(gpu_lib, oracle_lib):
     compare(gm, rm, frac_limit=0.02)
 
 
-def test_bpt_rejects_what_it_does_not_implement(gpu_lib):
-    vol = gpu_lib.Scene(scenes.medium_box_scene(8, 8, grid=8))
-    with pytest.raises(gpu_lib.SlrGpuError):
-        vol.render(8, 8, 1, 4, bpt=True, volumetric=True)  # VolumetricBPTRenderer
+def test_volumetric_bpt_matches_reference(gpu_lib, oracle_lib):
+    """VolumetricBPTRenderer: the fBm medium (sigma_t max 20, albedo 0.9,
+    Henyey-Greenstein g = 0.7) in the box.  Subpaths stop at scattering
+    points in the medium (delta tracking with spectral ratio-tracking
+    throughput), medium vertices connect through albedo x phase function,
+    and every connection carries its spectral transmittance."""
+    desc = scenes.medium_box_scene(16, 16, grid=16)
+    w = h = 16
+    spp, depth = 8, 16
+    rm, _ = oracle_bpt_batches(oracle_lib, desc, w, h, spp, depth, 48, 2100, volumetric=True)
+    gm, _ = gpu_bpt_batches(gpu_lib, desc, w, h, spp, depth, 192, volumetric=True)
+    compare(gm, rm, frac_limit=0.02)
+
+
+def test_bpt_rejects_invalid_settings(gpu_lib):
     box = gpu_lib.Scene(scenes.box_scene(8, 8))
+    with pytest.raises(gpu_lib.SlrGpuError):
+        box.render(8, 8, 1, 4, bpt=True, volumetric=True)  # volumetric render of a scene without medium
     with pytest.raises(gpu_lib.SlrGpuError):
         box.render(8, 8, 1, 0, bpt=True)                   # no vertex beyond the first
     with pytest.raises(gpu_lib.SlrGpuError):
