@@ -147,3 +147,21 @@ def test_alias_tables_carry_the_reference_pmfs(gpu_lib):
     lp, la = box.alias_tables()["lights"]
     assert len(lp) == 2
     np.testing.assert_allclose(_alias_pmf(lp, la), [0.5, 0.5])
+
+
+def test_reference_bpt_agrees_with_pt(oracle_lib):
+    """The oracle's bidirectional renderer (BPTRenderer with the subpath cap,
+    its light-tracing buffers summed into the film) and its path tracer
+    estimate the same image of the box: per-batch image sums within 4
+    combined standard errors.  A film that missed the separated buffers
+    (the t = 1 connections) would fall short by their share."""
+    desc = scenes.box_scene(16, 16)
+    k, spp = 12, 32
+    tb, tp = [], []
+    for i in range(k):
+        ref = oracle_lib.RefScene(desc)
+        tb.append(ref.render_bpt(16, 16, spp, 40, seed=10 + i, threads=os.cpu_count())[0].sum(dtype=np.float64) / spp)
+        tp.append(ref.render(16, 16, spp, 40, seed=100 + i, threads=os.cpu_count())[0].sum(dtype=np.float64) / spp)
+    tb, tp = np.array(tb), np.array(tp)
+    z = (tb.mean() - tp.mean()) / np.sqrt(tb.var(ddof=1) / k + tp.var(ddof=1) / k)
+    assert abs(z) < 4.0, (tb.mean(), tp.mean(), z)
