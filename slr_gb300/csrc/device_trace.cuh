@@ -117,23 +117,23 @@ __device__ __forceinline__ bool wtIntersect(const float4* __restrict__ wv, uint3
 // BVH Ray Traversal", JCGT 2013) so that rounding cannot reject a box the
 // ray only grazes at a face, edge or corner; the watertight triangle test
 // needs it, the reference's arithmetic does not have it.
+template <bool ROBUST>
 __device__ __forceinline__ float slabTest(float lox, float hix, float loy, float hiy, float loz, float hiz,
-                                          V3 org, V3 inv, float tmin, float tmax, bool robust = false) {
-    const float widen = robust ? 1.0000008f : 1.0f;
+                                          V3 org, V3 inv, float tmin, float tmax) {
     float d0 = tmin, d1 = tmax;
     float tn = __fmul_rn(__fsub_rn(lox, org.x), inv.x), tf = __fmul_rn(__fsub_rn(hix, org.x), inv.x);
     if (tn > tf) { float s = tn; tn = tf; tf = s; }
-    tf = __fmul_rn(tf, widen);
+    if (ROBUST) tf = __fmul_rn(tf, 1.0000008f);
     d0 = tn > d0 ? tn : d0;
     d1 = tf < d1 ? tf : d1;
     tn = __fmul_rn(__fsub_rn(loy, org.y), inv.y); tf = __fmul_rn(__fsub_rn(hiy, org.y), inv.y);
     if (tn > tf) { float s = tn; tn = tf; tf = s; }
-    tf = __fmul_rn(tf, widen);
+    if (ROBUST) tf = __fmul_rn(tf, 1.0000008f);
     d0 = tn > d0 ? tn : d0;
     d1 = tf < d1 ? tf : d1;
     tn = __fmul_rn(__fsub_rn(loz, org.z), inv.z); tf = __fmul_rn(__fsub_rn(hiz, org.z), inv.z);
     if (tn > tf) { float s = tn; tn = tf; tf = s; }
-    tf = __fmul_rn(tf, widen);
+    if (ROBUST) tf = __fmul_rn(tf, 1.0000008f);
     d0 = tn > d0 ? tn : d0;
     d1 = tf < d1 ? tf : d1;
     return (d0 > d1) ? __int_as_float(0x7f800000) : d0;
@@ -145,9 +145,9 @@ struct StackEntry {
 };
 
 // Box test of the 4 children of a node; returns the hit mask and entry distances.
+template <bool ROBUST>
 __device__ __forceinline__ uint32_t testChildren(const BvhNode4* __restrict__ nodes, uint32_t ni, V3 org, V3 inv,
-                                                 float tmin, float tmax, float tn[4], uint32_t ch[4],
-                                                 bool robust = false) {
+                                                 float tmin, float tmax, float tn[4], uint32_t ch[4]) {
     const float4* np = reinterpret_cast<const float4*>(nodes + ni);
     float4 lx = __ldg(np + 0), hx = __ldg(np + 1), ly = __ldg(np + 2), hy = __ldg(np + 3);
     float4 lz = __ldg(np + 4), hz = __ldg(np + 5);
@@ -159,7 +159,7 @@ __device__ __forceinline__ uint32_t testChildren(const BvhNode4* __restrict__ no
     float lza[4] = {lz.x, lz.y, lz.z, lz.w}, hza[4] = {hz.x, hz.y, hz.z, hz.w};
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
-        tn[k] = slabTest(lxa[k], hxa[k], lya[k], hya[k], lza[k], hza[k], org, inv, tmin, tmax, robust);
+        tn[k] = slabTest<ROBUST>(lxa[k], hxa[k], lya[k], hya[k], lza[k], hza[k], org, inv, tmin, tmax);
         if (ch[k] != kChildEmpty && tn[k] != __int_as_float(0x7f800000)) mask |= 1u << k;
     }
     return mask;
@@ -176,14 +176,17 @@ __device__ __forceinline__ TriFrag loadFrag(const TriFrag* __restrict__ frags, u
 }
 
 // Closest hit over [tmin, tmax].  Returns false on stack overflow (the hit
-// found so far is still reported).
-__device__ __forceinline__ bool traceClosest(const DevScene &sc, V3 org, V3 dir, float tmin, float tmax, Hit* hit) {
+// found so far is still reported).  WT: the watertight triangle test with
+// conservative box tests, compiled separately so that the default walk
+// carries none of it.
+template <bool WT>
+__device__ __forceinline__ bool traceClosestT(const DevScene &sc, V3 org, V3 dir, float tmin, float tmax, Hit* hit) {
     hit->prim = kNoHit;
     hit->t = __int_as_float(0x7f800000);
     hit->b1 = hit->b2 = 0.0f;
     V3 inv = V3{__fdiv_rn(1.0f, dir.x), __fdiv_rn(1.0f, dir.y), __fdiv_rn(1.0f, dir.z)};
     WtRay wr;
-    if (sc.watertight) wr = wtSetup(org, dir);
+    if (WT) wr = wtSetup(org, dir);
     StackEntry stack[kTraceStack];
     int sp = 0;
     uint32_t cur = 0;
@@ -193,7 +196,7 @@ __device__ __forceinline__ bool traceClosest(const DevScene &sc, V3 org, V3 dir,
         if (!(cur & kLeafBit)) {
             float tn[4];
             uint32_t ch[4];
-            uint32_t mask = testChildren(sc.nodes, cur, org, inv, tmin, tmax, tn, ch, sc.watertight != 0);
+            uint32_t mask = testChildren<WT>(sc.nodes, cur, org, inv, tmin, tmax, tn, ch);
             if (mask == 0) goto pop;
             // Order the hit children near to far (ties in child order) with a
             // five-comparator sorting network on registers; missed children
@@ -226,7 +229,7 @@ __device__ __forceinline__ bool traceClosest(const DevScene &sc, V3 org, V3 dir,
                 float t, b1, b2;
                 uint32_t prim;
                 bool h;
-                if (sc.watertight) {
+                if (WT) {
                     h = wtIntersect(sc.wtVerts, first + i, wr, tmin, tmax, &t, &b1, &b2, &prim);
                 } else {
                     TriFrag f = loadFrag(sc.frags, first + i);
@@ -251,12 +254,18 @@ __device__ __forceinline__ bool traceClosest(const DevScene &sc, V3 org, V3 dir,
     }
 }
 
+__device__ __forceinline__ bool traceClosest(const DevScene &sc, V3 org, V3 dir, float tmin, float tmax, Hit* hit) {
+    return sc.watertight ? traceClosestT<true>(sc, org, dir, tmin, tmax, hit)
+                         : traceClosestT<false>(sc, org, dir, tmin, tmax, hit);
+}
+
 // Any hit over [tmin, tmax]: true when the segment is occluded.
-__device__ __forceinline__ bool traceAny(const DevScene &sc, V3 org, V3 dir, float tmin, float tmax) {
+template <bool WT>
+__device__ __forceinline__ bool traceAnyT(const DevScene &sc, V3 org, V3 dir, float tmin, float tmax) {
     if (sc.numPrims == 0) return false;
     V3 inv = V3{__fdiv_rn(1.0f, dir.x), __fdiv_rn(1.0f, dir.y), __fdiv_rn(1.0f, dir.z)};
     WtRay wr;
-    if (sc.watertight) wr = wtSetup(org, dir);
+    if (WT) wr = wtSetup(org, dir);
     uint32_t stack[kTraceStack];
     int sp = 0;
     uint32_t cur = 0;
@@ -264,7 +273,7 @@ __device__ __forceinline__ bool traceAny(const DevScene &sc, V3 org, V3 dir, flo
         if (!(cur & kLeafBit)) {
             float tn[4];
             uint32_t ch[4];
-            uint32_t mask = testChildren(sc.nodes, cur, org, inv, tmin, tmax, tn, ch, sc.watertight != 0);
+            uint32_t mask = testChildren<WT>(sc.nodes, cur, org, inv, tmin, tmax, tn, ch);
             bool have = false;
             uint32_t next = 0;
 #pragma unroll
@@ -280,7 +289,7 @@ __device__ __forceinline__ bool traceAny(const DevScene &sc, V3 org, V3 dir, flo
             uint32_t count = ((cur >> kLeafCountShift) & 0x1f) + 1;
             for (uint32_t i = 0; i < count; ++i) {
                 float t, b1, b2;
-                if (sc.watertight) {
+                if (WT) {
                     uint32_t prim;
                     if (wtIntersect(sc.wtVerts, first + i, wr, tmin, tmax, &t, &b1, &b2, &prim)) return true;
                 } else {
@@ -292,6 +301,10 @@ __device__ __forceinline__ bool traceAny(const DevScene &sc, V3 org, V3 dir, flo
         if (sp == 0) return false;
         cur = stack[--sp];
     }
+}
+
+__device__ __forceinline__ bool traceAny(const DevScene &sc, V3 org, V3 dir, float tmin, float tmax) {
+    return sc.watertight ? traceAnyT<true>(sc, org, dir, tmin, tmax) : traceAnyT<false>(sc, org, dir, tmin, tmax);
 }
 
 }  // namespace slrgpu
