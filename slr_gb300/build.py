@@ -52,6 +52,8 @@ def tuning_flags() -> list[str]:
         return []
     t = json.loads(tuning.read_text())
     flags = [f"-D{k}={int(v)}" for k, v in sorted(t.get("knobs", {}).items())]
+    if "bvh_width" in t:
+        flags.append(f"-DSLRGPU_BVH_WIDTH={int(t['bvh_width'])}")
     if "wave_paths" in t:
         flags.append(f"-DSLRGPU_WAVE_PATHS={int(t['wave_paths'])}u")
     return flags
@@ -69,6 +71,8 @@ def build(verbose: bool = False, force: bool = False, extra_nvcc: list[str] | No
     BUILD.mkdir(exist_ok=True)
     LIB_DIR.mkdir(exist_ok=True)
     inc = [f"-I{cuda / 'include'}", f"-I{CSRC}"]
+    # layout constants the host build shares with the kernels (BVH width)
+    host_defs = [f for f in extra_nvcc if f.startswith("-DSLRGPU_BVH_WIDTH=")]
     deps = sorted(CSRC.glob("*.h")) + sorted(CSRC.glob("*.cuh")) + sorted(CSRC.glob("*.inc")) + \
         [PKG.parent / "include" / "slrgpu.h"]
     newest_dep = max(p.stat().st_mtime for p in deps)
@@ -80,7 +84,7 @@ def build(verbose: bool = False, force: bool = False, extra_nvcc: list[str] | No
         s = CSRC / src
         if force or not o.exists() or o.stat().st_mtime < max(s.stat().st_mtime, newest_dep):
             jobs.append(["g++", "-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-unused-function",
-                         *inc, "-c", str(s), "-o", str(o)])
+                         *host_defs, *inc, "-c", str(s), "-o", str(o)])
     for src in CUDA_SOURCES:
         o = BUILD / (src + ".o")
         objs.append(o)

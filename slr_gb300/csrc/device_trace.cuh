@@ -146,23 +146,74 @@ struct StackEntry {
 
 // Box test of the 4 children of a node; returns the hit mask and entry distances.
 template <bool ROBUST>
-__device__ __forceinline__ uint32_t testChildren(const BvhNode4* __restrict__ nodes, uint32_t ni, V3 org, V3 inv,
-                                                 float tmin, float tmax, float tn[4], uint32_t ch[4]) {
+__device__ __forceinline__ uint32_t testChildren(const BvhNode* __restrict__ nodes, uint32_t ni, V3 org, V3 inv,
+                                                 float tmin, float tmax, float tn[kBvhWidth],
+                                                 uint32_t ch[kBvhWidth]) {
+    // 128-bit loads: Q float4 per coordinate array, then the child words
+    constexpr int Q = kBvhWidth / 4;
     const float4* np = reinterpret_cast<const float4*>(nodes + ni);
-    float4 lx = __ldg(np + 0), hx = __ldg(np + 1), ly = __ldg(np + 2), hy = __ldg(np + 3);
-    float4 lz = __ldg(np + 4), hz = __ldg(np + 5);
-    uint4 c = __ldg(reinterpret_cast<const uint4*>(np + 6));
-    ch[0] = c.x; ch[1] = c.y; ch[2] = c.z; ch[3] = c.w;
     uint32_t mask = 0;
-    float lxa[4] = {lx.x, lx.y, lx.z, lx.w}, hxa[4] = {hx.x, hx.y, hx.z, hx.w};
-    float lya[4] = {ly.x, ly.y, ly.z, ly.w}, hya[4] = {hy.x, hy.y, hy.z, hy.w};
-    float lza[4] = {lz.x, lz.y, lz.z, lz.w}, hza[4] = {hz.x, hz.y, hz.z, hz.w};
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        tn[k] = slabTest<ROBUST>(lxa[k], hxa[k], lya[k], hya[k], lza[k], hza[k], org, inv, tmin, tmax);
-        if (ch[k] != kChildEmpty && tn[k] != __int_as_float(0x7f800000)) mask |= 1u << k;
+    for (int q = 0; q < Q; ++q) {
+        const float4 lx = __ldg(np + 0 * Q + q), hx = __ldg(np + 1 * Q + q), ly = __ldg(np + 2 * Q + q);
+        const float4 hy = __ldg(np + 3 * Q + q), lz = __ldg(np + 4 * Q + q), hz = __ldg(np + 5 * Q + q);
+        const uint4 c = __ldg(reinterpret_cast<const uint4*>(np + 6 * Q) + q);
+        const float lxa[4] = {lx.x, lx.y, lx.z, lx.w}, hxa[4] = {hx.x, hx.y, hx.z, hx.w};
+        const float lya[4] = {ly.x, ly.y, ly.z, ly.w}, hya[4] = {hy.x, hy.y, hy.z, hy.w};
+        const float lza[4] = {lz.x, lz.y, lz.z, lz.w}, hza[4] = {hz.x, hz.y, hz.z, hz.w};
+        const uint32_t ca[4] = {c.x, c.y, c.z, c.w};
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const int i = 4 * q + k;
+            ch[i] = ca[k];
+            tn[i] = slabTest<ROBUST>(lxa[k], hxa[k], lya[k], hya[k], lza[k], hza[k], org, inv, tmin, tmax);
+            if (ch[i] != kChildEmpty && tn[i] != __int_as_float(0x7f800000)) mask |= 1u << i;
+        }
     }
     return mask;
+}
+
+// Orders the hit children of a node near to far (ties in child order) with a
+// sorting network on registers (5 comparators for 4 children, Batcher's 19
+// for 8); missed children sort last at +inf.  Pushes all but the nearest,
+// far to near, and returns the nearest.
+__device__ __forceinline__ uint32_t orderChildren(uint32_t mask, const float tn[kBvhWidth],
+                                                  const uint32_t ch[kBvhWidth], StackEntry* stack, int &sp,
+                                                  bool &ok) {
+    float t[kBvhWidth];
+    uint32_t c[kBvhWidth], k[kBvhWidth];
+#pragma unroll
+    for (int i = 0; i < kBvhWidth; ++i) {
+        t[i] = ((mask >> i) & 1u) ? tn[i] : __int_as_float(0x7f800000);
+        c[i] = ch[i];
+        k[i] = (uint32_t)i;
+    }
+#define SLRGPU_CSWAP(a, b)                                                           \
+    if (t[b] < t[a] || (t[b] == t[a] && k[b] < k[a])) {                              \
+        float tt = t[a]; t[a] = t[b]; t[b] = tt;                                     \
+        uint32_t cc = c[a]; c[a] = c[b]; c[b] = cc;                                  \
+        uint32_t kk = k[a]; k[a] = k[b]; k[b] = kk;                                  \
+    }
+    if constexpr (kBvhWidth == 4) {
+        SLRGPU_CSWAP(0, 1) SLRGPU_CSWAP(2, 3) SLRGPU_CSWAP(0, 2) SLRGPU_CSWAP(1, 3) SLRGPU_CSWAP(1, 2)
+    } else {
+        SLRGPU_CSWAP(0, 1) SLRGPU_CSWAP(2, 3) SLRGPU_CSWAP(4, 5) SLRGPU_CSWAP(6, 7)
+        SLRGPU_CSWAP(0, 2) SLRGPU_CSWAP(1, 3) SLRGPU_CSWAP(4, 6) SLRGPU_CSWAP(5, 7)
+        SLRGPU_CSWAP(1, 2) SLRGPU_CSWAP(5, 6)
+        SLRGPU_CSWAP(0, 4) SLRGPU_CSWAP(1, 5) SLRGPU_CSWAP(2, 6) SLRGPU_CSWAP(3, 7)
+        SLRGPU_CSWAP(2, 4) SLRGPU_CSWAP(3, 5)
+        SLRGPU_CSWAP(1, 2) SLRGPU_CSWAP(3, 4) SLRGPU_CSWAP(5, 6)
+    }
+#undef SLRGPU_CSWAP
+    const int n = __popc(mask);
+#pragma unroll
+    for (int i = kBvhWidth - 1; i >= 1; --i) {
+        if (i < n) {
+            if (sp < kTraceStack) stack[sp++] = StackEntry{c[i], t[i]};
+            else ok = false;
+        }
+    }
+    return c[0];
 }
 
 __device__ __forceinline__ TriFrag loadFrag(const TriFrag* __restrict__ frags, uint32_t i) {
@@ -194,33 +245,11 @@ __device__ __forceinline__ bool traceClosestT(const DevScene &sc, V3 org, V3 dir
     if (sc.numPrims == 0) return true;
     for (;;) {
         if (!(cur & kLeafBit)) {
-            float tn[4];
-            uint32_t ch[4];
+            float tn[kBvhWidth];
+            uint32_t ch[kBvhWidth];
             uint32_t mask = testChildren<WT>(sc.nodes, cur, org, inv, tmin, tmax, tn, ch);
             if (mask == 0) goto pop;
-            // Order the hit children near to far (ties in child order) with a
-            // five-comparator sorting network on registers; missed children
-            // sort last at +inf.  Visit the nearest next, push the rest far
-            // to near.
-            float t0 = (mask & 1u) ? tn[0] : __int_as_float(0x7f800000);
-            float t1 = (mask & 2u) ? tn[1] : __int_as_float(0x7f800000);
-            float t2 = (mask & 4u) ? tn[2] : __int_as_float(0x7f800000);
-            float t3 = (mask & 8u) ? tn[3] : __int_as_float(0x7f800000);
-            uint32_t c0 = ch[0], c1 = ch[1], c2 = ch[2], c3 = ch[3];
-            uint32_t k0 = 0, k1 = 1, k2 = 2, k3 = 3;
-#define SLRGPU_CSWAP(a, b)                                                           \
-            if (t##b < t##a || (t##b == t##a && k##b < k##a)) {                      \
-                float tt = t##a; t##a = t##b; t##b = tt;                             \
-                uint32_t cc = c##a; c##a = c##b; c##b = cc;                          \
-                uint32_t kk = k##a; k##a = k##b; k##b = kk;                          \
-            }
-            SLRGPU_CSWAP(0, 1) SLRGPU_CSWAP(2, 3) SLRGPU_CSWAP(0, 2) SLRGPU_CSWAP(1, 3) SLRGPU_CSWAP(1, 2)
-#undef SLRGPU_CSWAP
-            const int n = __popc(mask);
-            if (n > 3) { if (sp < kTraceStack) stack[sp++] = StackEntry{c3, t3}; else ok = false; }
-            if (n > 2) { if (sp < kTraceStack) stack[sp++] = StackEntry{c2, t2}; else ok = false; }
-            if (n > 1) { if (sp < kTraceStack) stack[sp++] = StackEntry{c1, t1}; else ok = false; }
-            cur = c0;
+            cur = orderChildren(mask, tn, ch, stack, sp, ok);
             continue;
         } else {
             uint32_t first = cur & kLeafFirstMask;
@@ -271,13 +300,13 @@ __device__ __forceinline__ bool traceAnyT(const DevScene &sc, V3 org, V3 dir, fl
     uint32_t cur = 0;
     for (;;) {
         if (!(cur & kLeafBit)) {
-            float tn[4];
-            uint32_t ch[4];
+            float tn[kBvhWidth];
+            uint32_t ch[kBvhWidth];
             uint32_t mask = testChildren<WT>(sc.nodes, cur, org, inv, tmin, tmax, tn, ch);
             bool have = false;
             uint32_t next = 0;
 #pragma unroll
-            for (int k = 0; k < 4; ++k) {
+            for (int k = 0; k < kBvhWidth; ++k) {
                 if (mask & (1u << k)) {
                     if (!have) { next = ch[k]; have = true; }
                     else if (sp < kTraceStack) stack[sp++] = ch[k];

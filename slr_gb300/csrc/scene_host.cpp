@@ -1020,7 +1020,7 @@ struct WideBuilder {
         return kLeafBit | ((count - 1) << kLeafCountShift) | first;
     }
 
-    void setBox(BvhNode4 &n, int slot, const SbvhNode &s) {
+    void setBox(BvhNode &n, int slot, const SbvhNode &s) {
         n.lox[slot] = s.bmin[0]; n.hix[slot] = s.bmax[0];
         n.loy[slot] = s.bmin[1]; n.hiy[slot] = s.bmax[1];
         n.loz[slot] = s.bmin[2]; n.hiz[slot] = s.bmax[2];
@@ -1039,7 +1039,7 @@ struct WideBuilder {
             uint32_t idx = (uint32_t)out->nodes.size();
             out->nodes.emplace_back();
             uint32_t remaining = s.count, off = s.offset;
-            BvhNode4 tmp;
+            BvhNode tmp;
             initNode(tmp);
             int slot = 0;
             while (remaining > 0 && slot < kBvhWidth) {
@@ -1070,7 +1070,7 @@ struct WideBuilder {
         return child((uint32_t)nodes.size() - 1);
     }
 
-    static void initNode(BvhNode4 &n) {
+    static void initNode(BvhNode &n) {
         for (int k = 0; k < kBvhWidth; ++k) {
             n.lox[k] = n.loy[k] = n.loz[k] = INFINITY;
             n.hix[k] = n.hiy[k] = n.hiz[k] = -INFINITY;
@@ -1095,7 +1095,7 @@ struct WideBuilder {
             kids[best] = b.nodes[open].c0;
             kids.insert(kids.begin() + best + 1, b.nodes[open].c1);
         }
-        BvhNode4 node;
+        BvhNode node;
         initNode(node);
         int slot = 0;
         for (size_t k = 0; k < kids.size(); ++k) {
@@ -1119,7 +1119,7 @@ void collapseToWide(const SbvhResult &b, const float* triPositions, WideBvh* out
     if (root.leaf) {
         // Root is a leaf (or the scene is empty): one wide node with it.
         out->nodes.emplace_back();
-        BvhNode4 node;
+        BvhNode node;
         WideBuilder::initNode(node);
         if (root.count > 0) {
             wb.setBox(node, 0, root);

@@ -53,7 +53,7 @@ bool buildSbvh(const float* triPositions, uint32_t numTris, SbvhResult* out, std
 
 // ---- wide BVH -----------------------------------------------------------------
 struct WideBvh {
-    std::vector<BvhNode4> nodes;
+    std::vector<BvhNode> nodes;
     std::vector<TriFrag> frags;
 };
 void collapseToWide(const SbvhResult &b, const float* triPositions, WideBvh* out);

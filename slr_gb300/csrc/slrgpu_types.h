@@ -67,21 +67,28 @@ struct DevPrim {
     float ngx, ngy, ngz, invArea;
 };
 
-// Wide BVH node: BVH_WIDTH children, SoA boxes, one 128-byte line for 4-wide.
+// Wide BVH node: kBvhWidth children (4 or 8, a compile-time tuning constant
+// shared by the host build and the kernels), SoA boxes: one 128-byte line
+// for 4-wide, two for 8-wide, read as 128-bit loads.
 // child[k]: 0xffffffff = empty; bit 31 set = leaf with first fragment in
 // bits [0, 26) and (count - 1) in bits [26, 31); else internal node index.
-constexpr int kBvhWidth = 4;
+#ifndef SLRGPU_BVH_WIDTH
+#define SLRGPU_BVH_WIDTH 4
+#endif
+constexpr int kBvhWidth = SLRGPU_BVH_WIDTH;
+static_assert(kBvhWidth == 4 || kBvhWidth == 8, "BVH width 4 or 8");
 constexpr uint32_t kChildEmpty = 0xffffffffu;
 constexpr uint32_t kLeafBit = 0x80000000u;
 constexpr int kLeafCountShift = 26;
 constexpr uint32_t kLeafFirstMask = (1u << kLeafCountShift) - 1;
 constexpr int kMaxLeafCount = 32;
 
-struct alignas(128) BvhNode4 {
-    float lox[4], hix[4], loy[4], hiy[4], loz[4], hiz[4];
-    uint32_t child[4];
-    uint32_t pad[4];
+struct alignas(128) BvhNode {
+    float lox[kBvhWidth], hix[kBvhWidth], loy[kBvhWidth], hiy[kBvhWidth], loz[kBvhWidth], hiz[kBvhWidth];
+    uint32_t child[kBvhWidth];
+    uint32_t pad[kBvhWidth];
 };
+static_assert(sizeof(BvhNode) == 32 * kBvhWidth, "whole cache lines");
 
 // Traversal fragment (48 B, leaf order): v0.xyz + prim id bits, e01 = p1 - p0,
 // e02 = p2 - p0 (precomputed with the same float subtraction as the test).
@@ -132,7 +139,7 @@ struct AliasEntry {
 
 struct DevScene {
     // geometry / traversal
-    const BvhNode4* nodes;
+    const BvhNode* nodes;
     const TriFrag* frags;
     const float4* wtVerts;  // per fragment: v0 (w = prim id bits), v1, v2 as given (watertight test)
     uint32_t watertight;    // 1: watertight triangle test instead of the reference's

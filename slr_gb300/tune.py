@@ -16,7 +16,8 @@ Knobs (resident blocks of 256 threads per SM the kernels are compiled for):
 SLRGPU_TRACE_MIN_BLOCKS (closest/any-hit traversal), SLRGPU_SHADE_MIN_BLOCKS
 (surface shading), SLRGPU_SHADE_DIELECTRIC_MIN_BLOCKS (GGX dielectric
 shading), SLRGPU_SHADEVOL_MIN_BLOCKS (volumetric shading),
-SLRGPU_MEDIUM_MIN_BLOCKS (medium transmittance); and the paths per wave.
+SLRGPU_MEDIUM_MIN_BLOCKS (medium transmittance); the paths per wave; and
+the BVH width (4 or 8 children per node, host build and kernels alike).
 """
 from __future__ import annotations
 
@@ -40,15 +41,16 @@ KNOBS = {
 }
 DEFAULTS = {"SLRGPU_TRACE_MIN_BLOCKS": 4, "SLRGPU_SHADE_MIN_BLOCKS": 3, "SLRGPU_SHADE_DIELECTRIC_MIN_BLOCKS": 3,
             "SLRGPU_SHADEVOL_MIN_BLOCKS": 3, "SLRGPU_MEDIUM_MIN_BLOCKS": 4,
-            "wave_paths": 1 << 22}   # the sources' defaults
+            "wave_paths": 1 << 22, "bvh_width": 4}   # the sources' defaults
 WAVE_PATHS = [1 << 22, 1 << 23, 1 << 24, 1 << 25, 1 << 26]
+BVH_WIDTHS = [4, 8]
 # The knobs a workload exercises (a knob of kernels the workload never
 # launches would only be tuned to noise).
 WORKLOAD_KNOBS = {
-    "small": ["SLRGPU_TRACE_MIN_BLOCKS", "SLRGPU_SHADE_MIN_BLOCKS", "SLRGPU_SHADE_DIELECTRIC_MIN_BLOCKS",
-              "wave_paths"],
-    "ggx_ibl_1m": ["SLRGPU_TRACE_MIN_BLOCKS", "SLRGPU_SHADE_MIN_BLOCKS", "SLRGPU_SHADE_DIELECTRIC_MIN_BLOCKS",
-                   "wave_paths"],
+    "small": ["bvh_width", "SLRGPU_TRACE_MIN_BLOCKS", "SLRGPU_SHADE_MIN_BLOCKS",
+              "SLRGPU_SHADE_DIELECTRIC_MIN_BLOCKS", "wave_paths"],
+    "ggx_ibl_1m": ["bvh_width", "SLRGPU_TRACE_MIN_BLOCKS", "SLRGPU_SHADE_MIN_BLOCKS",
+                   "SLRGPU_SHADE_DIELECTRIC_MIN_BLOCKS", "wave_paths"],
     "volumetric_small": ["SLRGPU_SHADEVOL_MIN_BLOCKS", "SLRGPU_MEDIUM_MIN_BLOCKS"],
 }
 
@@ -77,7 +79,10 @@ print(best)
 
 
 def _flags(cfg: dict) -> list[str]:
-    return [f"-D{k}={v}" for k, v in sorted(cfg.items()) if k in KNOBS]
+    flags = [f"-D{k}={v}" for k, v in sorted(cfg.items()) if k in KNOBS]
+    if "bvh_width" in cfg:
+        flags.append(f"-DSLRGPU_BVH_WIDTH={int(cfg['bvh_width'])}")
+    return flags
 
 
 def measure(cfg: dict, workload: str) -> float:
@@ -104,10 +109,11 @@ def main() -> int:
     best = dict(DEFAULTS)
     best.update({k: v for k, v in prev.get("knobs", {}).items() if k in KNOBS})
     best["wave_paths"] = prev.get("wave_paths", DEFAULTS["wave_paths"])
+    best["bvh_width"] = prev.get("bvh_width", DEFAULTS["bvh_width"])
     log = []
     best_val = measure(best, args.workload)
     log.append({"config": dict(best), "samples_per_s": best_val})
-    space = dict(KNOBS, wave_paths=WAVE_PATHS)
+    space = dict(KNOBS, wave_paths=WAVE_PATHS, bvh_width=BVH_WIDTHS)
     for _ in range(args.rounds):
         for knob in WORKLOAD_KNOBS[args.workload]:
             values = space[knob]
@@ -122,11 +128,13 @@ def main() -> int:
                     best, best_val = cand, val
     runs = dict(prev.get("runs", {}))
     runs[args.workload] = {"samples_per_s": best_val, "trials": log}
-    result = {"knobs": {k: best[k] for k in KNOBS}, "wave_paths": best["wave_paths"], "runs": runs}
+    result = {"knobs": {k: best[k] for k in KNOBS}, "wave_paths": best["wave_paths"], "bvh_width": best["bvh_width"],
+              "runs": runs}
     TUNING.write_text(json.dumps(result, indent=1) + "\n")
     # rebuild with the chosen flags
     subprocess.run([sys.executable, str(PKG / "build.py"), "--force"], check=True, stdout=subprocess.DEVNULL)
-    print(json.dumps({"knobs": result["knobs"], "wave_paths": result["wave_paths"], "samples_per_s": best_val}))
+    print(json.dumps({"knobs": result["knobs"], "wave_paths": result["wave_paths"], "bvh_width": result["bvh_width"],
+                      "samples_per_s": best_val}))
     return 0
 
 
