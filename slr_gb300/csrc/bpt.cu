@@ -955,20 +955,24 @@ __device__ __forceinline__ void addConnectionWl(const BptState &st, uint32_t tar
     }
 }
 
-// Connections of the queued eye vertices with every light vertex of their
-// paths, spread over the lanes of a warp: a warp takes 32 eye vertices,
-// prefix-sums their light-subpath lengths and gives each lane one
-// (eye vertex, light vertex) pair per round, so lanes stay busy whatever the
-// subpath lengths.  Connections that contribute go to the shadow queue (or,
-// when it is full, are traced here).
+// Connections of the queued eye vertices [first, first + count) with every
+// light vertex of their paths, spread over the lanes of a warp: a warp takes
+// 32 eye vertices, prefix-sums their light-subpath lengths and gives each
+// lane one (eye vertex, light vertex) pair per round, so lanes stay busy
+// whatever the subpath lengths.  Connections that contribute go to the
+// shadow queue.
 template <bool VOL>
 __global__ void __launch_bounds__(256, 2) kBptConnect(DevScene sc, BptState st, uint32_t width, uint32_t height,
                                                       const uint32_t* __restrict__ queue,
-                                                      const uint32_t* __restrict__ count, uint32_t* shCount) {
-    const uint32_t n = *count;
+                                                      const uint32_t* __restrict__ count, uint32_t first,
+                                                      uint32_t maxItems, uint32_t* shCount) {
+    const uint32_t total0 = *count;
+    const uint32_t end = total0 > first ? min(total0, first + maxItems) : first;
+    const uint32_t n = end - first;
+    queue += first;
     const uint32_t lane = threadIdx.x & 31;
     const unsigned full = 0xffffffffu;
-    unsigned long long dropped = 0, traced = 0;
+    unsigned long long dropped = 0;
     for (uint32_t base = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u; base < n; base += gridDim.x * blockDim.x) {
         const uint32_t item = base + lane;
         uint32_t evi = 0, nL = 0;
@@ -1013,43 +1017,19 @@ __global__ void __launch_bounds__(256, 2) kBptConnect(DevScene sc, BptState st, 
             if (push) {
                 const uint32_t p = ev % st.S - st.N;
                 const uint32_t meta = (ev / st.S) << 8 | sIdx;
-                if (slot < st.connCap) {
-                    st.cRay[2 * (size_t)slot] = ro;
-                    st.cRay[2 * (size_t)slot + 1] = rd;
-                    storeAlpha(st.cContrib, slot, c);
-                    st.cTarget[slot] = target;
-                    if (VOL) {
-                        st.cPath[slot] = p;
-                        st.cMeta[slot] = meta;
-                    }
-                } else {
-                    ++traced;
-                    if (!traceAny(sc, xyz(ro), xyz(rd), ro.w, rd.w)) {
-                        if (VOL && sc.medium.present) {
-                            float lambdas[kNumLambda];
-                            const float wlOff = st.wlOffset[p];
-#pragma unroll
-                            for (int q = 0; q < kNumLambda; ++q) lambdas[q] = lambdaAt(q, wlOff);
-                            Spec sigmaE;
-                            evalSpectrum(sc, sc.medium.sigmaE, lambdas, sigmaE);
-                            for (int wl = 0; wl < kNumLambda; ++wl) {
-                                const float cw = specAt(c, wl);
-                                if (cw == 0.0f) continue;
-                                addConnectionWl(st, target, p, wl,
-                                                cw * connectionTransmittance(sc, st, ro, rd, p, meta, wl, sigmaE));
-                            }
-                        } else if (VOL) {
-                            for (int wl = 0; wl < kNumLambda; ++wl) addConnectionWl(st, target, p, wl, specAt(c, wl));
-                        } else {
-                            addConnection(st, target, c);
-                        }
-                    }
+                // a pass never holds more connections than the queue (see renderBpt)
+                st.cRay[2 * (size_t)slot] = ro;
+                st.cRay[2 * (size_t)slot + 1] = rd;
+                storeAlpha(st.cContrib, slot, c);
+                st.cTarget[slot] = target;
+                if (VOL) {
+                    st.cPath[slot] = p;
+                    st.cMeta[slot] = meta;
                 }
             }
         }
     }
     if (dropped) atomicAdd(&st.stats[2], dropped);
-    if (traced) atomicAdd(&st.stats[1], traced);
 }
 
 // Shadow rays of the queued connections; unoccluded ones add their
@@ -1191,8 +1171,9 @@ const BptGrids &bptGrids() {
 #define SLRGPU_BPT_WAVE_PATHS (1u << 20)
 #endif
 constexpr uint64_t kBptStateBudget = 8ull << 30;
-// Queued connections per path of a wave (more are traced in place).
-constexpr uint32_t kConnPerPath = 8;
+// Connections the shadow queue holds per path of a wave; the connection
+// passes take kConnPerPath / (max_depth + 1) paths' worth of eye vertices.
+constexpr uint32_t kConnPerPath = 16;
 
 struct BptEngine {
     BptState st{};
@@ -1358,30 +1339,50 @@ int renderBpt(BptEngine &eng, const DeviceScene &ds, const slrgpu_settings &s, f
             markEnd();
             ++nl;
         }
-        mark(SLRGPU_KERNEL_SHADE);
-        if (vol)
-            kBptConnect<true><<<g.connect[1], 256, 0, stream>>>(ds.sc, st, s.width, s.height, st.connQueue,
-                                                                 st.counters + D + 1, st.counters + D + 2);
-        else
-            kBptConnect<false><<<g.connect[0], 256, 0, stream>>>(ds.sc, st, s.width, s.height, st.connQueue,
-                                                                  st.counters + D + 1, st.counters + D + 2);
-        markEnd();
-        mark(SLRGPU_KERNEL_SHADOW);
-        if (vol)
-            kBptShadow<true><<<g.shadow[1], 256, 0, stream>>>(ds.sc, st, st.counters + D + 2, st.counters + D + 3);
-        else
-            kBptShadow<false><<<g.shadow[0], 256, 0, stream>>>(ds.sc, st, st.counters + D + 2, st.counters + D + 3);
-        markEnd();
-        if (vol) {
-            mark(SLRGPU_KERNEL_SHADOW);
-            kVbptMedium<<<g.medium, 256, 0, stream>>>(ds.sc, st, st.counters + D + 3);
+        // Connections in passes of at most connCap / (D + 1) eye vertices:
+        // each has at most D + 1 light vertices to connect to, so a pass
+        // never overfills the shadow queue.  The number of eye vertices is
+        // read back once per wave.
+        uint32_t items = 0;
+        if (cudaMemcpyAsync(&items, st.counters + D + 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream) !=
+                cudaSuccess ||
+            cudaStreamSynchronize(stream) != cudaSuccess) {
+            setError("bidirectional connection count readback failed");
+            return SLRGPU_ERR_CUDA;
+        }
+        const uint32_t perPass = std::max(1u, st.connCap / (D + 1));
+        for (uint32_t first = 0; first < items; first += perPass) {
+            cudaMemsetAsync(st.counters + D + 2, 0, 2 * sizeof(uint32_t), stream);
+            mark(SLRGPU_KERNEL_SHADE);
+            if (vol)
+                kBptConnect<true><<<g.connect[1], 256, 0, stream>>>(ds.sc, st, s.width, s.height, st.connQueue,
+                                                                     st.counters + D + 1, first, perPass,
+                                                                     st.counters + D + 2);
+            else
+                kBptConnect<false><<<g.connect[0], 256, 0, stream>>>(ds.sc, st, s.width, s.height, st.connQueue,
+                                                                      st.counters + D + 1, first, perPass,
+                                                                      st.counters + D + 2);
             markEnd();
-            ++nl;
+            mark(SLRGPU_KERNEL_SHADOW);
+            if (vol)
+                kBptShadow<true><<<g.shadow[1], 256, 0, stream>>>(ds.sc, st, st.counters + D + 2,
+                                                                   st.counters + D + 3);
+            else
+                kBptShadow<false><<<g.shadow[0], 256, 0, stream>>>(ds.sc, st, st.counters + D + 2,
+                                                                    st.counters + D + 3);
+            markEnd();
+            nl += 2;
+            if (vol) {
+                mark(SLRGPU_KERNEL_SHADOW);
+                kVbptMedium<<<g.medium, 256, 0, stream>>>(ds.sc, st, st.counters + D + 3);
+                markEnd();
+                ++nl;
+            }
         }
         mark(SLRGPU_KERNEL_ACCUMULATE);
         kBptAccumulate<<<g.accumulate, 256, 0, stream>>>(st, wv, filmSum, filmComp);
         markEnd();
-        nl += 3;
+        ++nl;
     }
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {

@@ -101,10 +101,13 @@ __device__ __forceinline__ Spec specConst(float c) {
     return s;
 }
 
-// lambda_i = 360 + 470 (i + offset) / 16 (spectrum_types.h:59-68).
+// lambda_i = 360 + 470 (i + offset) / 16 (spectrum_types.h:59-68).  The
+// division by 16 is a multiplication by 2^-4, exact for the (non-negative,
+// normal or zero) dividends that occur, so the IEEE quotient is kept.
+static_assert(kNumLambda == 16, "the scale 2^-4 below is 1 / kNumLambda");
 __device__ __forceinline__ float lambdaAt(int i, float offset) {
-    return __fadd_rn(kWavelengthLow, __fdiv_rn(__fmul_rn(kWavelengthHigh - kWavelengthLow, __fadd_rn((float)i, offset)),
-                                               (float)kNumLambda));
+    return __fadd_rn(kWavelengthLow, __fmul_rn(__fmul_rn(kWavelengthHigh - kWavelengthLow, __fadd_rn((float)i, offset)),
+                                               0.0625f));
 }
 
 // SampledSpectrum::importance (spectrum_types.h:473-486).

@@ -128,8 +128,11 @@ def test_bpt_environment_matches_reference(gpu_lib, oracle_lib):
     desc = scenes.heightfield_scene(grid=24, spheres=5, sphere_freq=3, env_size=(64, 32), width=20, height=20)
     w = h = 20
     spp, depth = 8, 8
-    rm, _ = oracle_bpt_batches(oracle_lib, desc, w, h, spp, depth, 40, 1700)
-    gm, _ = gpu_bpt_batches(gpu_lib, desc, w, h, spp, depth, 160)
+    # The 2-degree sun of radiance 5e4 makes the per-bin estimates heavy
+    # tailed; enough batches keep the estimated standard errors honest
+    # (with 40 reference batches the exceedance fraction ranged up to 2 %).
+    rm, _ = oracle_bpt_batches(oracle_lib, desc, w, h, spp, depth, 96, 1700)
+    gm, _ = gpu_bpt_batches(gpu_lib, desc, w, h, spp, depth, 384)
     compare(gm, rm, frac_limit=0.02)
 
 
