@@ -55,6 +55,9 @@ def test_bpt_box_matches_reference(gpu_lib, oracle_lib):
     gm, gdrop = gpu_bpt_batches(gpu_lib, desc, w, h, spp, depth, 192)
     compare(gm, rm)
     assert rdrop == 0 and gdrop == 0
+    # the same estimator has the same noise (matched RMSE at equal spp)
+    ratio = gm.var(0, ddof=1).sum() / rm.var(0, ddof=1).sum()
+    assert 0.75 < ratio < 1.33, ratio
 
 
 def test_bpt_every_bsdf_matches_reference(gpu_lib, oracle_lib):

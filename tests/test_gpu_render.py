@@ -29,8 +29,16 @@ def gpu_batches(gpu_lib, desc, w, h, spp, depth, batches, seed0=50000):
 def check_statistical_parity(mg, vg, kg, mr, vr, kr, frac_limit=0.015, tg=None, tr=None):
     """tg, tr: per-batch image sums, when known; the image-wide test then
     uses their spread, which includes the correlation between the bins of one
-    pixel (one path adds to all 16 wavelength bins)."""
-    se = np.sqrt(vg / kg + vr / kr)
+    pixel (one path adds to all 16 wavelength bins).
+
+    Per bin, the standard error uses the pooled variance of both sides: the
+    hypothesis under test is that the two renderers run the same estimator,
+    whose batch variance is then common to both, and pooling keeps a
+    heavy-tailed bin's variance estimate from resting on the smaller batch
+    count alone (with 48 reference batches the unpooled exceedance fraction
+    of an unbiased pair fluctuated up to ~2 %)."""
+    pooled = ((kg - 1) * vg + (kr - 1) * vr) / (kg + kr - 2)
+    se = np.sqrt(pooled / kg + pooled / kr)
     diff = mg - mr
     zero = se == 0
     assert np.all(np.abs(diff[zero]) < 1e-6), "deterministic-zero bins differ"
@@ -51,6 +59,11 @@ def test_box_scene_matches_reference(gpu_lib):
     mg, vg, dropped, _ = gpu_batches(gpu_lib, desc, 32, 32, int(g["spp"]), int(g["max_depth"]), 192)
     frac, gz = check_statistical_parity(mg, vg, 192, g["mean"], g["var"], int(g["batches"]))
     assert dropped == 0
+    # Same estimator, same noise: the summed per-bin variance of a batch
+    # mean matches the reference's, so equal sample counts give equal RMSE
+    # (the throughput ratios compare at matched RMSE).
+    ratio = vg.sum() / g["var"].sum()
+    assert 0.75 < ratio < 1.33, ratio
 
 
 def test_ragged_image_matches_reference(gpu_lib, oracle_lib):
@@ -163,7 +176,7 @@ def test_cameras_match_reference(gpu_lib, oracle_lib, kind):
     else:
         desc.camera = Camera("equirect", scenes.look_at((0.5, 0.45, 0.6), (0.5, 0.45, 0.0)), sensitivity=1.0,
                              phi_angle=2 * np.pi, theta_angle=np.pi)
-    spp, depth, kr, kg = 8, 4, 48, 192
+    spp, depth, kr, kg = 8, 4, 96, 192
     ref = oracle_lib.RefScene(desc)
     rm = np.stack([ref.render(w, h, spp, depth, seed=900 + k, threads=os.cpu_count())[0].astype(np.float64) / spp
                    for k in range(kr)])
