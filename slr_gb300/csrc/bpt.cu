@@ -938,9 +938,10 @@ __device__ bool connectOne(const DevScene &sc, const BptState &st, uint32_t evi,
 // kernel's wavelengths are never selected there, so every wavelength is
 // tracked; the random numbers come from a stream of the connection.
 __device__ __forceinline__ float connectionTransmittance(const DevScene &sc, const BptState &st, float4 o, float4 d,
-                                                         uint32_t p, uint32_t meta, int wl, const Spec &sigmaE) {
+                                                         uint32_t p, uint32_t meta, int wl) {
     Rng rng{mix64(keyOf(st, p) ^ (0x9e3779b97f4a7c15ull * (meta + 1))), (uint32_t)wl << 24};
-    return mediumTransmittanceWl(sc.medium, xyz(o), xyz(d), o.w, d.w, specAt(sigmaE, wl), true, rng);
+    const float sig = evalSpectrumAt(sc, sc.medium.sigmaE, lambdaAt(wl, st.wlOffset[p]));
+    return mediumTransmittanceWl(sc.medium, xyz(o), xyz(d), o.w, d.w, sig, true, rng);
 }
 
 // Adds one wavelength of a volumetric connection (film bin for a splat).
@@ -1071,16 +1072,9 @@ __global__ void __launch_bounds__(256, SLRGPU_MEDIUM_MIN_BLOCKS) kVbptMedium(Dev
         if (cw == 0.0f) continue;
         const uint32_t p = st.cPath[slot];
         float T = 1.0f;
-        if (sc.medium.present) {
-            float lambdas[kNumLambda];
-            const float wlOff = st.wlOffset[p];
-#pragma unroll
-            for (int q = 0; q < kNumLambda; ++q) lambdas[q] = lambdaAt(q, wlOff);
-            Spec sigmaE;
-            evalSpectrum(sc, sc.medium.sigmaE, lambdas, sigmaE);
+        if (sc.medium.present)
             T = connectionTransmittance(sc, st, st.cRay[2 * (size_t)slot], st.cRay[2 * (size_t)slot + 1], p,
-                                        st.cMeta[slot], wl, sigmaE);
-        }
+                                        st.cMeta[slot], wl);
         addConnectionWl(st, st.cTarget[slot], p, wl, cw * T);
     }
 }

@@ -229,4 +229,52 @@ static __device__ __noinline__ void evalSpectrum(const DevScene &sc, int id, con
     }
 }
 
+// One wavelength of evalSpectrum: the same arithmetic for that wavelength
+// (every wavelength of evalSpectrum is computed on its own; the irregular
+// search from the previous wavelength's bracket finds the same bracket as a
+// search from the start), for threads that need a single wavelength.
+static __device__ __noinline__ float evalSpectrumAt(const DevScene &sc, int id, float lambda) {
+    const DevSpectrum sp = sc.spectra[id];
+    if (sp.kind == kSpecUpsampled) {
+        int idx[4]; float w[4]; int n;
+        upsWeights(sp.adj, sp.p0, sp.p1, idx, w, &n);
+        float p = __fdiv_rn(__fsub_rn(lambda, 360.0f), 470.0f);
+        p = fminf(fmaxf(p, 0.0f), 1.0f);
+        const float sBinF = __fmul_rn(p, (float)(kUpsNumSamples - 1));
+        const uint32_t sBin = min((uint32_t)sBinF, (uint32_t)(kUpsNumSamples - 1));
+        const uint32_t sBinNext = min(sBin + 1, (uint32_t)(kUpsNumSamples - 1));
+        const float tt = __fsub_rn(sBinF, (float)sBin);
+        const float omt = __fsub_rn(1.0f, tt);
+        float acc = 0.0f;
+        for (int j = 0; j < n; ++j) {
+            const float* b = sc.upsSpectra + idx[j] * kUpsNumSamples;
+            const float lerp = __fadd_rn(__fmul_rn(__ldg(b + sBin), omt), __fmul_rn(__ldg(b + sBinNext), tt));
+            acc = __fadd_rn(acc, __fmul_rn(w[j], lerp));
+        }
+        return __fmul_rn(acc, sp.scale);
+    }
+    if (sp.kind == kSpecRegular) {
+        const float* v = sc.specValues + sp.offset;
+        const float nm1 = (float)(sp.count - 1);
+        const float binF = __fmul_rn(__fdiv_rn(__fsub_rn(lambda, sp.p0), __fsub_rn(sp.p1, sp.p0)), nm1);
+        if (binF <= 0.0f) return v[0];
+        if (binF >= nm1) return v[sp.count - 1];
+        const int bin = (int)binF;
+        const float t = __fsub_rn(binF, (float)bin);
+        return __fadd_rn(__fmul_rn(__fsub_rn(1.0f, t), v[bin]), __fmul_rn(t, v[bin + 1]));
+    }
+    const float* wl = sc.specValues + sp.offset;
+    const float* v = wl + sp.count;
+    uint32_t lo = 0, hi = sp.count;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (wl[mid] < lambda) lo = mid + 1; else hi = mid;
+    }
+    const int low = max((int)lo - 1, 0);
+    if (low >= (int)sp.count - 1) return v[sp.count - 1];
+    const float t = __fdiv_rn(__fsub_rn(lambda, wl[low]), __fsub_rn(wl[low + 1], wl[low]));
+    if (t <= 0.0f) return v[0];
+    return __fadd_rn(__fmul_rn(__fsub_rn(1.0f, t), v[low]), __fmul_rn(t, v[low + 1]));
+}
+
 }  // namespace slrgpu

@@ -58,7 +58,7 @@ struct WaveState {
     float* shContrib;    // [N][16]
     uint32_t* queue[2];
     uint32_t* shadowQueue;
-    uint32_t* classQueue;  // [kNumShadeClasses][N]: paths of one bounce sorted by shading class
+    uint32_t* classQueue;  // [kNumClassQueues][N]: paths of one bounce sorted by shading class
     uint32_t* counters;    // [kCtrStride * (maxDepth + 2)], see kCtr*
     unsigned long long* stats;  // 0 extension rays, 1 shadow rays, 2 dropped samples
     uint32_t N;
@@ -100,13 +100,21 @@ struct WaveParams {
     WaveSegment seg[kMaxWaveSegments];
 };
 
-// Per-bounce counter block: [0, kNumShadeClasses) paths per shading class,
-// kCtrExt paths in the extension queue of the bounce, kCtrShadow shadow rays.
+// Per-bounce counter block: [0, kNumClassQueues - 1) paths per shading
+// class, kCtrExt paths in the extension queue of the bounce, kCtrShadow
+// shadow rays, kCtrMedShadow shadow rays waiting for their transmittance.
 constexpr int kNumShadeClasses = 6;   // the five material kinds + environment / miss
 constexpr int kClassMiss = 5;
-constexpr int kCtrStride = 8;
-constexpr int kCtrExt = 6;
-constexpr int kCtrShadow = 7;
+constexpr int kClassMedium = 6;       // volumetric: a scattering point in the medium
+constexpr int kQueueMedShadow = 7;    // volumetric: unoccluded shadow rays waiting for their transmittance
+constexpr int kNumClassQueues = 8;
+constexpr int kCtrStride = 10;
+constexpr int kCtrExt = 7;
+constexpr int kCtrShadow = 8;
+constexpr int kCtrMedShadow = 9;
+// hit.w of a path whose ray stopped at a collision in the medium (hit.x = its
+// distance, hit.y = 1 inside the density grid's unit cube)
+constexpr uint32_t kMediumHit = 0xfffffffeu;
 
 constexpr uint32_t kInfoSelMask = 0xfu;
 constexpr uint32_t kInfoWlSelected = 1u << 4;
@@ -478,6 +486,70 @@ __global__ void __launch_bounds__(256, K == kMatGGXScattering ? SLRGPU_SHADE_DIE
 #ifndef SLRGPU_SHADEVOL_MIN_BLOCKS
 #define SLRGPU_SHADEVOL_MIN_BLOCKS 3   // measured best on the volumetric benchmark (2, 3 tried)
 #endif
+// Scene::interact for the volumetric integrator (Scene.cpp:66-94): the
+// closest surface hit is known; a collision in the medium before it may stop
+// the ray (delta tracking at the selected wavelength, ratio-tracking
+// throughput for the others).  The throughput (and a collision's extinction
+// coefficient) goes into alpha, the path into the queue of its class: the
+// medium, a surface material kind, or the environment.  Splitting the
+// interaction from the shading keeps each shading kernel's code to one
+// vertex kind.
+__global__ void __launch_bounds__(256, SLRGPU_SHADEVOL_MIN_BLOCKS) kVolInteract(DevScene sc, WaveState ws,
+                                                                              const uint32_t* __restrict__ queue,
+                                                                              const uint32_t* __restrict__ count,
+                                                                              uint32_t* classCounts) {
+    const uint32_t n = *count;
+    const float inf = __int_as_float(0x7f800000);
+    const DevMedium &med = sc.medium;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+        const uint32_t i = base + threadIdx.x;
+        int cls = -1;
+        uint32_t p = 0;
+        if (i < n) {
+            p = queue[i];
+            float4 hv = ws.hit[p];
+            const uint32_t prim = __float_as_uint(hv.w);
+            bool medHit = false;
+            if (med.present) {
+                const uint32_t info = ws.ps[p].info;
+                const int sel = (int)(info & kInfoSelMask);
+                const bool wlSelected = (info & kInfoWlSelected) != 0;
+                const float wlOff = ws.ps[p].wlOffset;
+                float lambdas[kNumLambda];
+#pragma unroll
+                for (int k = 0; k < kNumLambda; ++k) lambdas[k] = lambdaAt(k, wlOff);
+                Rng rng{loadKey(ws, p), ws.ps[p].rngCounter};
+                const float4 ro = ws.ray[2 * (size_t)p], rd = ws.ray[2 * (size_t)p + 1];
+                const V3 org = V3{ro.x, ro.y, ro.z}, dir = V3{rd.x, rd.y, rd.z};
+                Spec sigmaE, thr, alpha;
+                evalSpectrum(sc, med.sigmaE, lambdas, sigmaE);
+                float tMed = 0.0f;
+                V3 mparam = V3{0, 0, 0};
+                medHit = mediumInteract(med, org, dir, ro.w, prim == kNoHit ? inf : hv.x, sigmaE, sel, wlSelected,
+                                        rng, &tMed, &mparam, thr);
+                loadSpec(ws.alpha, p, alpha);
+#pragma unroll
+                for (int k = 0; k < kNumLambda; ++k) alpha.v[k] *= thr.v[k];
+                if (medHit) {
+                    const float dens = mediumDensity(med, mparam);
+#pragma unroll
+                    for (int k = 0; k < kNumLambda; ++k) alpha.v[k] *= dens * sigmaE.v[k];
+                    ws.hit[p] = make_float4(tMed, outsideUnit(mparam) ? 0.0f : 1.0f, 0.0f, __uint_as_float(kMediumHit));
+                }
+                storeSpec(ws.alpha, p, alpha);
+                ws.ps[p].rngCounter = rng.counter;
+            }
+            if (medHit) cls = kClassMedium;
+            else if (prim != kNoHit) cls = (int)sc.materials[sc.prims[prim].material].kind;
+            else if (sc.envPresent) cls = kClassMiss;
+        }
+#pragma unroll
+        for (int c = 0; c < kNumClassQueues - 1; ++c)
+            queuePush(ws.classQueue + (size_t)c * ws.N, classCounts + c, p, cls == c);
+    }
+}
+
+template <int K>
 __global__ void __launch_bounds__(256, SLRGPU_SHADEVOL_MIN_BLOCKS) kShadeVol(DevScene sc, WaveState ws, uint32_t maxDepth,
                                                  const uint32_t* __restrict__ inQueue,
                                                  const uint32_t* __restrict__ inCount, uint32_t* outQueue,
@@ -511,37 +583,26 @@ __global__ void __launch_bounds__(256, SLRGPU_SHADEVOL_MIN_BLOCKS) kShadeVol(Dev
             loadSpec(ws.alpha, p, alpha);
             bool alive = true;
 
-            // Scene::interact (Scene.cpp:66-94): surface hit, then a medium
-            // collision before it.
-            float tSurf = prim == kNoHit ? inf : hv.x;
-            bool medHit = false;
-            float tMed = 0.0f;
-            V3 mparam = V3{0, 0, 0};
-            Spec sigmaE;
-            if (med.present) {
-                evalSpectrum(sc, med.sigmaE, lambdas, sigmaE);
-                Spec thr;
-                medHit = mediumInteract(med, org, dir, ro.w, tSurf, sigmaE, sel, wlSelected, rng, &tMed, &mparam, thr);
-#pragma unroll
-                for (int k = 0; k < kNumLambda; ++k) alpha.v[k] *= thr.v[k];
-            }
-            // Interaction point.
-            V3 P;
-            Frame frame;
+            // The interaction (kVolInteract): K is its class; the medium
+            // throughput and a collision's extinction are in alpha already.
+            constexpr bool isMedium = K == kClassMedium;
+            constexpr bool atInf = K == kClassMiss;
+            constexpr int KB = K < kClassMiss ? K : (int)kMatMatte;   // the material kind of surface classes
+            V3 P = V3{0, 0, 0};
+            Frame frame = Frame{V3{1, 0, 0}, V3{0, 1, 0}, V3{0, 0, 1}};
             V3 gn = V3{0, 0, 1};
             DevMaterial mat;
             mat.kind = kMatNull;
             mat.emit = -1;
-            bool isMedium = false, atInf = false;
             float hitInvArea = 0.0f;
-            if (medHit) {
-                isMedium = true;
-                P = rn_ray_point(org, dir, tMed);
+            Spec sigmaE;
+            bool inMedium = false;
+            if (isMedium) {
+                P = rn_ray_point(org, dir, hv.x);
                 frame = frameFromZ(normalize(dir));
-                float dens = mediumDensity(med, mparam);
-#pragma unroll
-                for (int k = 0; k < kNumLambda; ++k) alpha.v[k] *= dens * sigmaE.v[k];
-            } else if (prim != kNoHit) {
+                evalSpectrum(sc, med.sigmaE, lambdas, sigmaE);
+                inMedium = hv.y != 0.0f;
+            } else if (!atInf) {
                 const DevPrim pr = sc.prims[prim];
                 SurfPoint sp;
                 surfacePoint(sc, pr, org, dir, hv.x, hv.y, hv.z, sp);
@@ -550,10 +611,6 @@ __global__ void __launch_bounds__(256, SLRGPU_SHADEVOL_MIN_BLOCKS) kShadeVol(Dev
                 gn = sp.gn;
                 mat = sc.materials[pr.material];
                 hitInvArea = pr.invArea;
-            } else if (sc.envPresent) {
-                atInf = true;
-            } else {
-                alive = false;
             }
             if (alive) {
                 // Emission (VolumetricPTRenderer.cpp:175-180, :262-278).  The
@@ -615,17 +672,17 @@ __global__ void __launch_bounds__(256, SLRGPU_SHADEVOL_MIN_BLOCKS) kShadeVol(Dev
                 Spec albedo;
                 if (isMedium) {
                     B.kind = kMatNull;
-                    bool in = !outsideUnit(mparam);
+                    const bool in = inMedium;
                     Spec sigmaS;
                     evalSpectrum(sc, med.sigmaS, lambdas, sigmaS);
 #pragma unroll
                     for (int k = 0; k < kNumLambda; ++k)
                         albedo.v[k] = (in && sigmaE.v[k] > 0) ? sigmaS.v[k] / sigmaE.v[k] : 0.0f;
                 } else {
-                    makeBsdf(sc, mat, lambdas, wlSelected, B);
+                    makeBsdfK<KB>(sc, mat, lambdas, wlSelected, B);
                 }
                 BsdfQuery q{dirOut, frame.toLocal(gn), sel};
-                const bool nonDelta = isMedium || bsdfHasNonDelta(B.kind);
+                const bool nonDelta = isMedium || bsdfHasNonDelta(KB);
                 if (nonDelta && (sc.numLights > 0 || sc.envPresent)) {
                     int li;
                     float lightProb;
@@ -683,8 +740,8 @@ __global__ void __launch_bounds__(256, SLRGPU_SHADEVOL_MIN_BLOCKS) kShadeVol(Dev
                         for (int k = 0; k < kNumLambda; ++k) fv.v[k] = albedo.v[k] * ph;
                         apdf = ph;
                     } else {
-                        bsdfEval(B, q, sdl, fv);
-                        apdf = bsdfPdf(B, q, sdl);
+                        bsdfEval<KB>(B, q, sdl, fv);
+                        apdf = bsdfPdf<KB>(B, q, sdl);
                     }
                     float abdfPdf = apdf * cosLight / dist2;
                     float mis = 1.0f;
@@ -729,7 +786,7 @@ __global__ void __launch_bounds__(256, SLRGPU_SHADEVOL_MIN_BLOCKS) kShadeVol(Dev
                     for (int k = 0; k < kNumLambda; ++k) fs.v[k] = albedo.v[k] * pdf;
                 } else {
                     float uc = rng.next(), u0 = rng.next(), u1 = rng.next();
-                    bsdfSample(B, q, uc, u0, u1, &bs, fs);
+                    bsdfSample<KB>(B, q, uc, u0, u1, &bs, fs);
                 }
                 if (bs.pdf == 0.0f || specIsZero(fs)) {
                     alive = false;
@@ -810,13 +867,8 @@ __global__ void __launch_bounds__(256, SLRGPU_MEDIUM_MIN_BLOCKS) kShadowVolMediu
         const uint32_t info = ws.ps[p].info;
         const int sel = (int)(info & kInfoSelMask);
         const bool wlSelected = (info & kInfoWlSelected) != 0;
-        float lambdas[kNumLambda];
-        const float wlOff = ws.ps[p].wlOffset;
-#pragma unroll
-        for (int k = 0; k < kNumLambda; ++k) lambdas[k] = lambdaAt(k, wlOff);
-        Spec sigmaE;
-        evalSpectrum(sc, sc.medium.sigmaE, lambdas, sigmaE);   // same values as the shading kernel's
-        const float sig = specAt(sigmaE, wl);
+        // this thread's wavelength only, with the shading kernel's arithmetic
+        const float sig = evalSpectrumAt(sc, sc.medium.sigmaE, lambdaAt(wl, ws.ps[p].wlOffset));
         Rng rng{mix64(loadKey(ws, p) ^ (0x9e3779b97f4a7c15ull * (bounce + 1))), (uint32_t)wl << 24};
         const float T = mediumTransmittanceWl(sc.medium, V3{o.x, o.y, o.z}, V3{d.x, d.y, d.z}, o.w, d.w, sig,
                                               !wlSelected || wl == sel, rng);
@@ -1183,7 +1235,7 @@ int RenderEngine::ensure(uint32_t N, uint32_t maxDepth) {
     w->queue[0] = allocDev<uint32_t>(allocs, N, &e); if (!w->queue[0]) goto fail;
     w->queue[1] = allocDev<uint32_t>(allocs, N, &e); if (!w->queue[1]) goto fail;
     w->shadowQueue = allocDev<uint32_t>(allocs, N, &e); if (!w->shadowQueue) goto fail;
-    w->classQueue = allocDev<uint32_t>(allocs, (size_t)N * kNumShadeClasses, &e); if (!w->classQueue) goto fail;
+    w->classQueue = allocDev<uint32_t>(allocs, (size_t)N * kNumClassQueues, &e); if (!w->classQueue) goto fail;
     w->counters = allocDev<uint32_t>(allocs, (size_t)kCtrStride * (maxDepth + 2), &e); if (!w->counters) goto fail;
     w->stats = allocDev<unsigned long long>(allocs, 4, &e); if (!w->stats) goto fail;
     ws = w;
@@ -1240,8 +1292,9 @@ static int gridFor(const void* kernel, int block) {
 // Persistent grid sizes (resident blocks per SM x SMs) of the wave kernels,
 // computed once per process.
 struct WaveGrids {
-    int raygen, extend, shadow, accumulate, shadeVol, shadowVol, shadowVolMedium, extendSort, shadeMiss;
+    int raygen, extend, shadow, accumulate, volInteract, shadowVol, shadowVolMedium, extendSort, shadeMiss;
     int shadeSurf[kNumShadeClasses - 1];
+    int shadeVol[kNumClassQueues - 1];
 };
 static const WaveGrids &waveGrids(int block) {
     static WaveGrids g;
@@ -1251,7 +1304,14 @@ static const WaveGrids &waveGrids(int block) {
         g.extend = gridFor((const void*)kExtend, block);
         g.shadow = gridFor((const void*)kShadow, block);
         g.accumulate = gridFor((const void*)kAccumulate, block);
-        g.shadeVol = gridFor((const void*)kShadeVol, block);
+        g.volInteract = gridFor((const void*)kVolInteract, block);
+        g.shadeVol[0] = gridFor((const void*)kShadeVol<0>, block);
+        g.shadeVol[1] = gridFor((const void*)kShadeVol<1>, block);
+        g.shadeVol[2] = gridFor((const void*)kShadeVol<2>, block);
+        g.shadeVol[3] = gridFor((const void*)kShadeVol<3>, block);
+        g.shadeVol[4] = gridFor((const void*)kShadeVol<4>, block);
+        g.shadeVol[5] = gridFor((const void*)kShadeVol<5>, block);
+        g.shadeVol[6] = gridFor((const void*)kShadeVol<6>, block);
         g.shadowVol = gridFor((const void*)kShadowVol, block);
         g.shadowVolMedium = gridFor((const void*)kShadowVolMedium, block);
         g.extendSort = gridFor((const void*)kExtendSort, block);
@@ -1338,20 +1398,44 @@ static uint64_t runWave(const DeviceScene &ds0, const WaveState &w, const WavePa
             lm.begin(SLRGPU_KERNEL_EXTEND);
             kExtend<<<g.extend, block, 0, stream>>>(ds.sc, w, inQueue, ctr + kCtrExt);
             lm.end();
+            // the medium collision (or not), then one shading kernel per
+            // vertex class present
             lm.begin(SLRGPU_KERNEL_SHADE);
-            kShadeVol<<<g.shadeVol, block, 0, stream>>>(ds.sc, w, D, inQueue, ctr + kCtrExt, outQueue,
-                                                        next + kCtrExt, w.shadowQueue, ctr + kCtrShadow);
+            kVolInteract<<<g.volInteract, block, 0, stream>>>(ds.sc, w, inQueue, ctr + kCtrExt, ctr);
             lm.end();
-            // unoccluded shadow rays that cross the medium: class queue 0 and
-            // its counter (unused by the volumetric integrator otherwise)
+            launches += 2;
+            for (int k = 0; k < kNumClassQueues - 1; ++k) {
+                const bool present = k < kClassMiss ? (ds.kindMask & (1u << k)) != 0
+                                                    : (k == kClassMiss ? ds.sc.envPresent != 0 : ds.sc.medium.present != 0);
+                if (!present) continue;
+                const uint32_t* cq = w.classQueue + (size_t)k * w.N;
+                lm.begin(SLRGPU_KERNEL_SHADE);
+#define SLRGPU_SHADEVOL(KK)                                                                              \
+    kShadeVol<KK><<<g.shadeVol[KK], block, 0, stream>>>(ds.sc, w, D, cq, ctr + k, outQueue, next + kCtrExt, \
+                                                        w.shadowQueue, ctr + kCtrShadow)
+                switch (k) {
+                case 0: SLRGPU_SHADEVOL(0); break;
+                case 1: SLRGPU_SHADEVOL(1); break;
+                case 2: SLRGPU_SHADEVOL(2); break;
+                case 3: SLRGPU_SHADEVOL(3); break;
+                case 4: SLRGPU_SHADEVOL(4); break;
+                case 5: SLRGPU_SHADEVOL(5); break;
+                default: SLRGPU_SHADEVOL(6); break;
+                }
+#undef SLRGPU_SHADEVOL
+                lm.end();
+                ++launches;
+            }
+            // unoccluded shadow rays that cross the medium wait in their own queue
+            uint32_t* medQueue = w.classQueue + (size_t)kQueueMedShadow * w.N;
             lm.begin(SLRGPU_KERNEL_SHADOW);
-            kShadowVol<<<g.shadowVol, block, 0, stream>>>(ds.sc, w, w.shadowQueue, ctr + kCtrShadow, w.classQueue,
-                                                          ctr + 0);
+            kShadowVol<<<g.shadowVol, block, 0, stream>>>(ds.sc, w, w.shadowQueue, ctr + kCtrShadow, medQueue,
+                                                          ctr + kCtrMedShadow);
             lm.end();
             lm.begin(SLRGPU_KERNEL_SHADOW);
-            kShadowVolMedium<<<g.shadowVolMedium, block, 0, stream>>>(ds.sc, w, w.classQueue, ctr + 0, b);
+            kShadowVolMedium<<<g.shadowVolMedium, block, 0, stream>>>(ds.sc, w, medQueue, ctr + kCtrMedShadow, b);
             lm.end();
-            launches += 4;
+            launches += 2;
             continue;
         }
         // Closest hits, sorted into one queue per shading class.
@@ -1562,7 +1646,7 @@ constexpr size_t kNaQueue0 = naAlign(kNaShContrib + 4ull * kNumLambda * kNoAlloc
 constexpr size_t kNaQueue1 = naAlign(kNaQueue0 + 4ull * kNoAllocMaxPaths);
 constexpr size_t kNaShQueue = naAlign(kNaQueue1 + 4ull * kNoAllocMaxPaths);
 constexpr size_t kNaClassQueue = naAlign(kNaShQueue + 4ull * kNoAllocMaxPaths);
-constexpr size_t kNaCounters = naAlign(kNaClassQueue + 4ull * kNumShadeClasses * kNoAllocMaxPaths);
+constexpr size_t kNaCounters = naAlign(kNaClassQueue + 4ull * kNumClassQueues * kNoAllocMaxPaths);
 constexpr size_t kNaStats = naAlign(kNaCounters + 4ull * kCtrStride * (kNoAllocMaxDepth + 2));
 constexpr size_t kNaFilmSum = naAlign(kNaStats + 8ull * 4);
 constexpr size_t kNaFilmComp = naAlign(kNaFilmSum + 4ull * kNumLambda * kNoAllocMaxPaths);
