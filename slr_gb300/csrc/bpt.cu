@@ -114,8 +114,9 @@ struct BptState {
     uint32_t* cPath;      // [connCap] path of the connection (volumetric: wavelengths, RNG key)
     uint32_t* cMeta;      // [connCap] eye vertex index << 8 | light vertex number (volumetric RNG stream)
     uint32_t* mQueue;     // [connCap] unoccluded connections whose transmittance is due (volumetric)
-    uint32_t* counters;   // [D + 4] queue sizes per bounce, eye vertices to connect, queued
-                          // connections, connections waiting for their transmittance
+    uint32_t* counters;   // [D + 5] queue sizes per bounce, eye vertices to connect, queued
+                          // connections, connections waiting for their transmittance, the
+                          // transmittance kernel's work counter
     unsigned long long* stats;   // 0 extension rays, 1 shadow rays, 2 dropped contributions
 };
 
@@ -933,17 +934,6 @@ __device__ bool connectOne(const DevScene &sc, const BptState &st, uint32_t evi,
     return true;
 }
 
-// Medium transmittance of one wavelength of a connection (Scene::testVisibility,
-// Scene.cpp:114-135, with MediumObjectAggregate::evaluateTransmittance): the
-// kernel's wavelengths are never selected there, so every wavelength is
-// tracked; the random numbers come from a stream of the connection.
-__device__ __forceinline__ float connectionTransmittance(const DevScene &sc, const BptState &st, float4 o, float4 d,
-                                                         uint32_t p, uint32_t meta, int wl) {
-    Rng rng{mix64(keyOf(st, p) ^ (0x9e3779b97f4a7c15ull * (meta + 1))), (uint32_t)wl << 24};
-    const float sig = evalSpectrumAt(sc, sc.medium.sigmaE, lambdaAt(wl, st.wlOffset[p]));
-    return mediumTransmittanceWl(sc.medium, xyz(o), xyz(d), o.w, d.w, sig, true, rng);
-}
-
 // Adds one wavelength of a volumetric connection (film bin for a splat).
 __device__ __forceinline__ void addConnectionWl(const BptState &st, uint32_t target, uint32_t p, int wl, float v) {
     if (v == 0.0f) return;
@@ -1060,22 +1050,53 @@ __global__ void __launch_bounds__(256, SLRGPU_TRACE_MIN_BLOCKS) kBptShadow(DevSc
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&st.stats[1], (unsigned long long)n);
 }
 
-// Medium transmittance of the unoccluded volumetric connections, one thread
-// per (connection, wavelength) as the path tracer's shadow rays do.
+// Medium transmittance of the unoccluded volumetric connections
+// (Scene::testVisibility, Scene.cpp:114-135, with
+// MediumObjectAggregate::evaluateTransmittance), one walk per (connection,
+// wavelength) as the path tracer's shadow rays do: the kernel's wavelengths
+// are never selected there, so every wavelength is tracked, each from its own
+// counter range of a stream of the connection; lanes take the next walk as
+// soon as theirs ends (TrWalk).
 __global__ void __launch_bounds__(256, SLRGPU_MEDIUM_MIN_BLOCKS) kVbptMedium(DevScene sc, BptState st,
-                                                                           const uint32_t* __restrict__ medCount) {
+                                                                           const uint32_t* __restrict__ medCount,
+                                                                           uint32_t* take) {
     const uint32_t n = *medCount * kNumLambda;
-    for (uint32_t item = blockIdx.x * blockDim.x + threadIdx.x; item < n; item += gridDim.x * blockDim.x) {
-        const uint32_t slot = st.mQueue[item / kNumLambda];
-        const int wl = (int)(item % kNumLambda);
-        const float cw = reinterpret_cast<const float*>(st.cContrib)[(size_t)slot * kNumLambda + wl];
-        if (cw == 0.0f) continue;
-        const uint32_t p = st.cPath[slot];
-        float T = 1.0f;
-        if (sc.medium.present)
-            T = connectionTransmittance(sc, st, st.cRay[2 * (size_t)slot], st.cRay[2 * (size_t)slot + 1], p,
-                                        st.cMeta[slot], wl);
-        addConnectionWl(st, st.cTarget[slot], p, wl, cw * T);
+    uint32_t poolNext = 0, poolEnd = 0;
+    TrWalk q;
+    uint32_t slot = 0;
+    int wl = 0;
+    float cw = 0.0f;
+    bool walking = false, exhausted = false;
+    for (;;) {
+        for (;;) {
+            const bool need = !walking && !exhausted;
+            if (!__any_sync(0xffffffffu, need)) break;
+            const uint32_t item = trTake(need, take, poolNext, poolEnd);
+            if (!need) continue;
+            if (item >= n) {
+                exhausted = true;
+                continue;
+            }
+            slot = st.mQueue[item / kNumLambda];
+            wl = (int)(item % kNumLambda);
+            cw = reinterpret_cast<const float*>(st.cContrib)[(size_t)slot * kNumLambda + wl];
+            if (cw == 0.0f) continue;
+            const uint32_t p = st.cPath[slot];
+            if (!sc.medium.present) {
+                addConnectionWl(st, st.cTarget[slot], p, wl, cw);
+                continue;
+            }
+            const float4 o = st.cRay[2 * (size_t)slot], d = st.cRay[2 * (size_t)slot + 1];
+            const Rng rng{mix64(keyOf(st, p) ^ (0x9e3779b97f4a7c15ull * (st.cMeta[slot] + 1))), (uint32_t)wl << 24};
+            const float sig = evalSpectrumAt(sc, sc.medium.sigmaE, lambdaAt(wl, st.wlOffset[p]));
+            walking = trBegin(sc.medium, q, xyz(o), xyz(d), o.w, d.w, sig, true, rng);
+            if (!walking) addConnectionWl(st, st.cTarget[slot], p, wl, cw * q.T);
+        }
+        if (!__any_sync(0xffffffffu, walking)) break;
+        if (walking) {
+            walking = trStep(sc.medium, q);
+            if (!walking) addConnectionWl(st, st.cTarget[slot], st.cPath[slot], wl, cw * q.T);
+        }
     }
 }
 
@@ -1214,7 +1235,7 @@ struct BptEngine {
                   (s.cPath = alloc<uint32_t>((size_t)kConnPerPath * N, &e)) &&
                   (s.cMeta = alloc<uint32_t>((size_t)kConnPerPath * N, &e)) &&
                   (s.mQueue = alloc<uint32_t>((size_t)kConnPerPath * N, &e)) &&
-                  (s.counters = alloc<uint32_t>(D + 4, &e)) && (s.stats = alloc<unsigned long long>(4, &e));
+                  (s.counters = alloc<uint32_t>(D + 5, &e)) && (s.stats = alloc<unsigned long long>(4, &e));
         if (!ok) {
             release();
             setError(std::string("bidirectional path state allocation failed: ") + cudaGetErrorString(e));
@@ -1316,7 +1337,7 @@ int renderBpt(BptEngine &eng, const DeviceScene &ds, const slrgpu_settings &s, f
         wv.samples = std::min(S, s.spp - base);
         wv.seed = s.seed;
         wv.numPaths = wv.samples * G;
-        cudaMemsetAsync(st.counters, 0, (D + 4) * sizeof(uint32_t), stream);
+        cudaMemsetAsync(st.counters, 0, (D + 5) * sizeof(uint32_t), stream);
         mark(SLRGPU_KERNEL_RAYGEN);
         if (vol) kBptInit<true><<<g.init[1], 256, 0, stream>>>(ds.sc, st, wv);
         else kBptInit<false><<<g.init[0], 256, 0, stream>>>(ds.sc, st, wv);
@@ -1346,7 +1367,7 @@ int renderBpt(BptEngine &eng, const DeviceScene &ds, const slrgpu_settings &s, f
         }
         const uint32_t perPass = std::max(1u, st.connCap / (D + 1));
         for (uint32_t first = 0; first < items; first += perPass) {
-            cudaMemsetAsync(st.counters + D + 2, 0, 2 * sizeof(uint32_t), stream);
+            cudaMemsetAsync(st.counters + D + 2, 0, 3 * sizeof(uint32_t), stream);
             mark(SLRGPU_KERNEL_SHADE);
             if (vol)
                 kBptConnect<true><<<g.connect[1], 256, 0, stream>>>(ds.sc, st, s.width, s.height, st.connQueue,
@@ -1368,7 +1389,7 @@ int renderBpt(BptEngine &eng, const DeviceScene &ds, const slrgpu_settings &s, f
             nl += 2;
             if (vol) {
                 mark(SLRGPU_KERNEL_SHADOW);
-                kVbptMedium<<<g.medium, 256, 0, stream>>>(ds.sc, st, st.counters + D + 3);
+                kVbptMedium<<<g.medium, 256, 0, stream>>>(ds.sc, st, st.counters + D + 3, st.counters + D + 4);
                 markEnd();
                 ++nl;
             }

@@ -388,40 +388,127 @@ __device__ __forceinline__ void mediumTransmittance(const DevMedium &m, V3 org, 
     }
 }
 
-// One wavelength of mediumTransmittance, for a thread per (ray, wavelength):
-// the same boundary walk and per-segment estimate; `evaluate` false (a
-// wavelength other than the selected one) gives 0 once the ray crosses the
-// medium and 1 otherwise, as the spectral version does.
-template <class R>
-__device__ __noinline__ float mediumTransmittanceWl(const DevMedium &m, V3 org, V3 dir, float dmin, float dmax,
-                                                    float sig, bool evaluate, R &rng) {
-    float T = 1.0f;
-    float rmin = dmin;
-    bool inside = mediumContains(m, org + rmin * dir);
-    for (int guard = 0; guard < 8; ++guard) {
+// One wavelength of mediumTransmittance as a resumable walk, for one lane per
+// (ray, wavelength): the same boundary crossings and per-segment ratio
+// tracking, with the state kept between two tentative collisions so that a
+// lane whose walk has ended can start the next (ray, wavelength) while the
+// other lanes of its warp go on.  `evaluate` false (a wavelength other than
+// the selected one) gives 0 once the ray crosses the medium and 1 otherwise,
+// as the spectral version does.
+struct TrWalk {
+    V3 org, dir;
+    float dmax, sig;
+    Rng rng;
+    float T;            // product of the finished segments
+    float t;            // the current segment's ratio-tracking estimate
+    float rmin, segEnd, sd;
+    int guard;
+    bool inside, nextInside, evaluate;
+    SvSetup s;
+    SvWalk w;
+};
+
+// Runs the boundary loop until a segment inside the medium is ready to walk
+// (true) or the estimate q.T is final (false).
+__device__ __forceinline__ bool trAdvance(const DevMedium &m, TrWalk &q) {
+    for (; q.guard < 8; ++q.guard) {
         float dist;
         bool enter;
-        bool nextInside = false;
+        q.nextInside = false;
         float distNext = __int_as_float(0x7f800000);
-        if (mediumIntersectBoundary(m, org, dir, rmin, dmax, &dist, &enter) && dist < distNext) {
+        if (mediumIntersectBoundary(m, q.org, q.dir, q.rmin, q.dmax, &dist, &enter) && dist < distNext) {
             distNext = dist;
-            nextInside = enter;
+            q.nextInside = enter;
         }
-        if (inside && nextInside) inside = false;
-        distNext = fminf(distNext, dmax);
-        if (isinf(distNext)) return T;
-        if (inside) {
-            if (!evaluate) return 0.0f;
-            SvSetup s;
-            svSetup(m, org, dir, rmin, s);
-            T *= ratioTrackSegment(m, org, dir, rmin, distNext, s, sig, rng);
-            if (T == 0.0f) return 0.0f;
+        if (q.inside && q.nextInside) q.inside = false;
+        distNext = fminf(distNext, q.dmax);
+        if (isinf(distNext)) return false;
+        q.segEnd = distNext;
+        if (q.inside) {
+            if (!q.evaluate) {
+                q.T = 0.0f;
+                return false;
+            }
+            svSetup(m, q.org, q.dir, q.rmin, q.s);
+            q.w = q.s.init;
+            q.t = 1.0f;
+            q.sd = q.rmin;
+            if (q.sd < q.segEnd) return true;
+            q.T *= q.t;      // an empty segment estimates 1
         }
-        if (distNext == dmax) return T;
-        rmin = distNext * (1.0f + kRayEpsilon);
-        inside = nextInside;
+        if (q.segEnd == q.dmax) return false;
+        q.rmin = q.segEnd * (1.0f + kRayEpsilon);
+        q.inside = q.nextInside;
     }
-    return T;
+    return false;
+}
+
+__device__ __forceinline__ bool trBegin(const DevMedium &m, TrWalk &q, V3 org, V3 dir, float dmin, float dmax,
+                                        float sig, bool evaluate, Rng rng) {
+    q.org = org;
+    q.dir = dir;
+    q.dmax = dmax;
+    q.sig = sig;
+    q.evaluate = evaluate;
+    q.rng = rng;
+    q.T = 1.0f;
+    q.rmin = dmin;
+    q.guard = 0;
+    q.inside = mediumContains(m, org + dmin * dir);
+    return trAdvance(m, q);
+}
+
+// One tentative collision of the current segment (ratioTrackSegment's loop
+// body).  Returns true while the walk goes on; q.T is final otherwise.
+__device__ __forceinline__ bool trStep(const DevMedium &m, TrWalk &q) {
+    float maj;
+    const bool tent = svTraverse(m, q.org, q.dir, q.sd, q.segEnd, q.rng.next(), q.sig, q.s, q.w, &q.sd, &maj);
+    bool segDone = !(q.sd < q.segEnd);
+    if (tent) {
+        float ext = q.sig * mediumDensity(m, mediumLocal(m, q.org + q.sd * q.dir));
+        float prob = ext / maj;
+        if (maj != 0.0f) q.t *= (1.0f - prob);
+        if (q.t < 0.1f) {
+            if (q.rng.next() < q.t) {
+                q.t = 1.0f;
+            } else {
+                q.t = 0.0f;
+                segDone = true;
+            }
+        }
+    }
+    if (!segDone) return true;
+    q.T *= q.t;
+    if (q.T == 0.0f) return false;
+    if (q.segEnd == q.dmax) return false;
+    q.rmin = q.segEnd * (1.0f + kRayEpsilon);
+    q.inside = q.nextInside;
+    ++q.guard;
+    return trAdvance(m, q);
+}
+
+// Hands out work items [0, n) to the lanes of a warp that ask for one, in
+// chunks of kTrChunk taken from a global counter (one atomic per chunk).
+// All 32 lanes call it together; the chunk range is the same in every lane.
+constexpr uint32_t kTrChunk = 64;
+
+__device__ __forceinline__ uint32_t trTake(bool need, uint32_t* take, uint32_t &poolNext, uint32_t &poolEnd) {
+    const unsigned mask = __ballot_sync(0xffffffffu, need);
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t k = __popc(mask), rank = __popc(mask & ((1u << lane) - 1));
+    uint32_t item = poolNext + rank;
+    const uint32_t avail = poolEnd - poolNext;
+    if (k > avail) {
+        uint32_t c = 0;
+        if (lane == 0) c = atomicAdd(take, kTrChunk);
+        c = __shfl_sync(0xffffffffu, c, 0);
+        if (rank >= avail) item = c + (rank - avail);
+        poolNext = c + (k - avail);
+        poolEnd = c + kTrChunk;
+    } else {
+        poolNext += k;
+    }
+    return item;
 }
 
 // Henyey-Greenstein phase function (PhaseFunction/basic_phase_functions.cpp:36-65).

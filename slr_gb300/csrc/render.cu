@@ -102,16 +102,18 @@ struct WaveParams {
 
 // Per-bounce counter block: [0, kNumClassQueues - 1) paths per shading
 // class, kCtrExt paths in the extension queue of the bounce, kCtrShadow
-// shadow rays, kCtrMedShadow shadow rays waiting for their transmittance.
+// shadow rays, kCtrMedShadow shadow rays waiting for their transmittance,
+// kCtrMedTake the transmittance kernel's work counter.
 constexpr int kNumShadeClasses = 6;   // the five material kinds + environment / miss
 constexpr int kClassMiss = 5;
 constexpr int kClassMedium = 6;       // volumetric: a scattering point in the medium
 constexpr int kQueueMedShadow = 7;    // volumetric: unoccluded shadow rays waiting for their transmittance
 constexpr int kNumClassQueues = 8;
-constexpr int kCtrStride = 10;
+constexpr int kCtrStride = 11;
 constexpr int kCtrExt = 7;
 constexpr int kCtrShadow = 8;
 constexpr int kCtrMedShadow = 9;
+constexpr int kCtrMedTake = 10;
 // hit.w of a path whose ray stopped at a collision in the medium (hit.x = its
 // distance, hit.y = 1 inside the density grid's unit cube)
 constexpr uint32_t kMediumHit = 0xfffffffeu;
@@ -849,31 +851,59 @@ __global__ void kShadowVol(DevScene sc, WaveState ws, const uint32_t* __restrict
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&ws.stats[1], (unsigned long long)n);
 }
 
-// Medium transmittance of the unoccluded shadow rays, one thread per (ray,
-// wavelength): the 16 ratio-tracking walks of a ray run side by side in
-// consecutive lanes instead of one after another.  Each wavelength draws
-// from its own counter range of the ray's per-bounce random stream.
+// Medium transmittance of the unoccluded shadow rays: one ratio-tracking walk
+// per (ray, wavelength).  The walks of a warp take different numbers of
+// steps, so each lane runs its walk one tentative collision at a time and
+// takes the next (ray, wavelength) as soon as its own walk ends; the warp
+// stays full until the queue runs dry.  Each wavelength draws from its own
+// counter range of the ray's per-bounce random stream.
 #ifndef SLRGPU_MEDIUM_MIN_BLOCKS
 #define SLRGPU_MEDIUM_MIN_BLOCKS 4     // 64 registers; measured best of 2, 3, 4
 #endif
 __global__ void __launch_bounds__(256, SLRGPU_MEDIUM_MIN_BLOCKS) kShadowVolMedium(DevScene sc, WaveState ws,
                                                                                   const uint32_t* __restrict__ queue,
-                                 const uint32_t* __restrict__ count, uint32_t bounce) {
+                                 const uint32_t* __restrict__ count, uint32_t* take, uint32_t bounce) {
     const uint32_t n = *count * kNumLambda;
-    for (uint32_t item = blockIdx.x * blockDim.x + threadIdx.x; item < n; item += gridDim.x * blockDim.x) {
-        const uint32_t p = queue[item / kNumLambda];
-        const int wl = (int)(item % kNumLambda);
-        float4 o = ws.shRay[2 * (size_t)p], d = ws.shRay[2 * (size_t)p + 1];
-        const uint32_t info = ws.ps[p].info;
-        const int sel = (int)(info & kInfoSelMask);
-        const bool wlSelected = (info & kInfoWlSelected) != 0;
-        // this thread's wavelength only, with the shading kernel's arithmetic
-        const float sig = evalSpectrumAt(sc, sc.medium.sigmaE, lambdaAt(wl, ws.ps[p].wlOffset));
-        Rng rng{mix64(loadKey(ws, p) ^ (0x9e3779b97f4a7c15ull * (bounce + 1))), (uint32_t)wl << 24};
-        const float T = mediumTransmittanceWl(sc.medium, V3{o.x, o.y, o.z}, V3{d.x, d.y, d.z}, o.w, d.w, sig,
-                                              !wlSelected || wl == sel, rng);
-        const size_t k = (size_t)p * kNumLambda + wl;
-        if (T != 0.0f) ws.L[k] += T * ws.shContrib[k];
+    uint32_t poolNext = 0, poolEnd = 0;
+    TrWalk q;
+    uint32_t item = 0;
+    bool walking = false, exhausted = false;
+    for (;;) {
+        // lanes without a walk take items until theirs needs steps
+        for (;;) {
+            const bool need = !walking && !exhausted;
+            if (!__any_sync(0xffffffffu, need)) break;
+            const uint32_t it = trTake(need, take, poolNext, poolEnd);
+            if (!need) continue;
+            if (it >= n) {
+                exhausted = true;
+                continue;
+            }
+            item = it;
+            const uint32_t p = queue[item / kNumLambda];
+            const int wl = (int)(item % kNumLambda);
+            const float4 o = ws.shRay[2 * (size_t)p], d = ws.shRay[2 * (size_t)p + 1];
+            const uint32_t info = ws.ps[p].info;
+            const int sel = (int)(info & kInfoSelMask);
+            const bool wlSelected = (info & kInfoWlSelected) != 0;
+            // this thread's wavelength only, with the shading kernel's arithmetic
+            const float sig = evalSpectrumAt(sc, sc.medium.sigmaE, lambdaAt(wl, ws.ps[p].wlOffset));
+            const Rng rng{mix64(loadKey(ws, p) ^ (0x9e3779b97f4a7c15ull * (bounce + 1))), (uint32_t)wl << 24};
+            walking = trBegin(sc.medium, q, V3{o.x, o.y, o.z}, V3{d.x, d.y, d.z}, o.w, d.w, sig,
+                              !wlSelected || wl == sel, rng);
+            if (!walking && q.T != 0.0f) {
+                const size_t k = (size_t)p * kNumLambda + wl;
+                ws.L[k] += q.T * ws.shContrib[k];
+            }
+        }
+        if (!__any_sync(0xffffffffu, walking)) break;
+        if (walking) {
+            walking = trStep(sc.medium, q);
+            if (!walking && q.T != 0.0f) {
+                const size_t k = (size_t)queue[item / kNumLambda] * kNumLambda + item % kNumLambda;
+                ws.L[k] += q.T * ws.shContrib[k];
+            }
+        }
     }
 }
 
@@ -1433,7 +1463,8 @@ static uint64_t runWave(const DeviceScene &ds0, const WaveState &w, const WavePa
                                                           ctr + kCtrMedShadow);
             lm.end();
             lm.begin(SLRGPU_KERNEL_SHADOW);
-            kShadowVolMedium<<<g.shadowVolMedium, block, 0, stream>>>(ds.sc, w, medQueue, ctr + kCtrMedShadow, b);
+            kShadowVolMedium<<<g.shadowVolMedium, block, 0, stream>>>(ds.sc, w, medQueue, ctr + kCtrMedShadow,
+                                                                      ctr + kCtrMedTake, b);
             lm.end();
             launches += 2;
             continue;
