@@ -47,10 +47,16 @@ __device__ __forceinline__ float mediumCoarseDensity(const DevMedium &m, V3 para
     return d + m.maxDiff[cell];
 }
 
+// Position in the medium's unit cube.  The divisions of the reference become
+// multiplications by reciprocals computed once on the host (results differ
+// in the last bit; the walks are issue-bound and an IEEE division is a
+// sequence of instructions).
 __device__ __forceinline__ V3 mediumLocal(const DevMedium &m, V3 p) {
-    return V3{(p.x - m.bmin[0]) / (m.bmax[0] - m.bmin[0]), (p.y - m.bmin[1]) / (m.bmax[1] - m.bmin[1]),
-              (p.z - m.bmin[2]) / (m.bmax[2] - m.bmin[2])};
+    return V3{(p.x - m.bmin[0]) * m.invExtent[0], (p.y - m.bmin[1]) * m.invExtent[1],
+              (p.z - m.bmin[2]) * m.invExtent[2]};
 }
+
+constexpr float kThird = 1.0f / 3.0f;
 
 __device__ __forceinline__ bool mediumContains(const DevMedium &m, V3 p) {
     return p.x >= m.bmin[0] && p.x < m.bmax[0] && p.y >= m.bmin[1] && p.y < m.bmax[1] && p.z >= m.bmin[2] &&
@@ -126,8 +132,10 @@ __device__ __forceinline__ void svPolyCoeffs(const DevMedium &m, V3 entry, V3 ex
           d111 = __ldg(s + i0 + sxy + sx + 1);
     V3 base = V3{m.bmin[0] + cell[0] * m.svWidth[0], m.bmin[1] + cell[1] * m.svWidth[1],
                  m.bmin[2] + cell[2] * m.svWidth[2]};
-    V3 ep = V3{(entry.x - base.x) / m.svWidth[0], (entry.y - base.y) / m.svWidth[1], (entry.z - base.z) / m.svWidth[2]};
-    V3 op = V3{(exit.x - base.x) / m.svWidth[0], (exit.y - base.y) / m.svWidth[1], (exit.z - base.z) / m.svWidth[2]};
+    V3 ep = V3{(entry.x - base.x) * m.invSvWidth[0], (entry.y - base.y) * m.invSvWidth[1],
+               (entry.z - base.z) * m.invSvWidth[2]};
+    V3 op = V3{(exit.x - base.x) * m.invSvWidth[0], (exit.y - base.y) * m.invSvWidth[1],
+               (exit.z - base.z) * m.invSvWidth[2]};
     V3 dl = op - ep;
     float dxyz = d111 - d011 - d101 - d110 + d001 + d010 + d100 - d000;
     float dxy = d000 - d100 - d010 + d110;
@@ -175,7 +183,7 @@ static __device__ __noinline__ bool svTraverse(const DevMedium &m, V3 org, V3 di
         exitDist = w.maxt[axis];
         exitP = org + exitDist * dir;
         svPolyCoeffs(m, entryP, exitP, w.sv, c);
-        exitOD += (exitDist - entryDist) * sigma * (c[0] + c[1] / 2 + c[2] / 3 + c[3] / 4);
+        exitOD += (exitDist - entryDist) * sigma * (c[0] + c[1] * 0.5f + c[2] * kThird + c[3] * 0.25f);
         if (exitOD >= sampledOD) break;
         w.sv[axis] += s.step[axis];
         if (w.sv[axis] == s.outside[axis] || exitDist >= dmax || ++steps > kMaxSvSteps) {
@@ -193,8 +201,8 @@ static __device__ __noinline__ bool svTraverse(const DevMedium &m, V3 org, V3 di
     while (fabsf(cur - prev) >= 1e-3f * fabsf(cur) && iters < 100) {
         prev = cur;
         cur = pLow + (pHigh - pLow) * (sampledOD - odLow) / (odHigh - odLow);
-        float temp = sigma * (c[0] * cur + c[1] * cur * cur / 2 + c[2] * cur * cur * cur / 3 +
-                              c[3] * cur * cur * cur * cur / 4);
+        float temp = sigma * (c[0] * cur + c[1] * cur * cur * 0.5f + c[2] * cur * cur * cur * kThird +
+                              c[3] * cur * cur * cur * cur * 0.25f);
         float od = entryOD + (exitDist - entryDist) * temp;
         ++iters;
         if (od < sampledOD) { pLow = cur; odLow = od; }

@@ -1223,6 +1223,8 @@ int uploadScene(const HostScene &hs, const BuiltScene &bs, DeviceScene* ds) {
             m.bmin[k] = hs.medium.bmin[k];
             m.bmax[k] = hs.medium.bmax[k];
             m.svWidth[k] = bs.superVoxels.width[k];
+            m.invSvWidth[k] = 1.0f / m.svWidth[k];
+            m.invExtent[k] = 1.0f / (m.bmax[k] - m.bmin[k]);
         }
         m.sigmaS = hs.medium.sigmaS;
         m.sigmaE = hs.medium.sigmaE;

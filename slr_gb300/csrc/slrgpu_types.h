@@ -122,6 +122,8 @@ struct DevMedium {
     uint32_t svx, svy, svz;       // super-voxel corners per axis
     float bmin[3], bmax[3];
     float svWidth[3];             // (bmax - bmin) / (sv - 1)
+    float invSvWidth[3];          // 1 / svWidth
+    float invExtent[3];           // 1 / (bmax - bmin)
     const float* density;         // [nz][ny][nx]
     const float* superVoxels;     // [svz][svy][svx]
     const float* maxDiff;         // [svz-1][svy-1][svx-1]
