@@ -96,6 +96,7 @@ struct SvWalk {
 struct SvSetup {
     int step[3];
     int outside[3];
+    float invD[3];      // 1 / direction: the plane distances are multiplications
     SvWalk init;
 };
 
@@ -107,16 +108,17 @@ __device__ __forceinline__ void svSetup(const DevMedium &m, V3 org, V3 dir, floa
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
         s.init.sv[i] = min((int)(lp[i] * (n[i] - 1)), (int)n[i] - 2);
+        s.invD[i] = 1.0f / d[i];
         if (d[i] > 0) {
             s.step[i] = 1;
             s.outside[i] = (int)n[i] - 1;
             float plane = m.bmin[i] + m.svWidth[i] * (s.init.sv[i] + 1);
-            s.init.maxt[i] = (plane - o[i]) / d[i];
+            s.init.maxt[i] = (plane - o[i]) * s.invD[i];
         } else {
             s.step[i] = -1;
             s.outside[i] = -1;
             float plane = m.bmin[i] + m.svWidth[i] * (s.init.sv[i] + 0);
-            s.init.maxt[i] = (plane - o[i]) / d[i];
+            s.init.maxt[i] = (plane - o[i]) * s.invD[i];
         }
     }
 }
@@ -170,7 +172,6 @@ static __device__ __noinline__ bool svTraverse(const DevMedium &m, V3 org, V3 di
     V3 entryP, exitP = org + exitDist * dir;
     float entryOD = 0.0f, exitOD = 0.0f;
     float c[4];
-    const float o[3] = {org.x, org.y, org.z}, d[3] = {dir.x, dir.y, dir.z};
     int steps = 0;
     for (;;) {
         entryP = exitP;
@@ -192,7 +193,8 @@ static __device__ __noinline__ bool svTraverse(const DevMedium &m, V3 org, V3 di
             return false;
         }
         float plane = m.bmin[axis] + m.svWidth[axis] * (w.sv[axis] + (s.step[axis] == 1 ? 1 : 0));
-        w.maxt[axis] = (plane - o[axis]) / d[axis];
+        const float oa = axis == 0 ? org.x : (axis == 1 ? org.y : org.z);
+        w.maxt[axis] = (plane - oa) * s.invD[axis];
     }
     // Regula falsi on the integrated majorant.
     float pLow = 0.0f, pHigh = 1.0f, odLow = entryOD, odHigh = exitOD;
@@ -200,7 +202,7 @@ static __device__ __noinline__ bool svTraverse(const DevMedium &m, V3 org, V3 di
     int iters = 0;
     while (fabsf(cur - prev) >= 1e-3f * fabsf(cur) && iters < 100) {
         prev = cur;
-        cur = pLow + (pHigh - pLow) * (sampledOD - odLow) / (odHigh - odLow);
+        cur = pLow + (pHigh - pLow) * __fdividef(sampledOD - odLow, odHigh - odLow);
         float temp = sigma * (c[0] * cur + c[1] * cur * cur * 0.5f + c[2] * cur * cur * cur * kThird +
                               c[3] * cur * cur * cur * cur * 0.25f);
         float od = entryOD + (exitDist - entryDist) * temp;
