@@ -477,7 +477,7 @@ __device__ __forceinline__ Frame vertexFrame(const BptGeom &g) {
 
 // Film bin of a wavelength (SpectrumStorage::add, spectrum_types.h:729).
 __device__ __forceinline__ uint32_t filmBin(float lambda) {
-    const float f = __fmul_rn(__fdiv_rn(__fsub_rn(lambda, kWavelengthLow), kWavelengthHigh - kWavelengthLow),
+    const float f = __fmul_rn(divRange(__fsub_rn(lambda, kWavelengthLow)),
                               (float)kNumLambda);
     return min((uint32_t)f, (uint32_t)(kNumLambda - 1));
 }
@@ -1128,7 +1128,7 @@ __global__ void kBptAccumulate(BptState st, BptWave wv, float* filmSum, float* f
             for (int i = 0; i < kNumLambda; ++i) {
                 const float c = st.L[(size_t)p * kNumLambda + i];
                 const float lam = lambdaAt(i, wlOff);
-                const float f = __fmul_rn(__fdiv_rn(__fsub_rn(lam, kWavelengthLow), kWavelengthHigh - kWavelengthLow),
+                const float f = __fmul_rn(divRange(__fsub_rn(lam, kWavelengthLow)),
                                           (float)kNumLambda);
                 const uint32_t bin = min((uint32_t)f, (uint32_t)(kNumLambda - 1));
 #pragma unroll

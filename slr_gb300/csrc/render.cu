@@ -954,7 +954,7 @@ __global__ void kAccumulate(WaveState ws, const __grid_constant__ WaveParams wpA
 #pragma unroll
             for (int i = 0; i < kNumLambda; ++i) {
                 float lam = lambdaAt(i, wlOff);
-                float f = __fmul_rn(__fdiv_rn(__fsub_rn(lam, kWavelengthLow), kWavelengthHigh - kWavelengthLow), (float)kNumLambda);
+                float f = __fmul_rn(divRange(__fsub_rn(lam, kWavelengthLow)), (float)kNumLambda);
                 uint32_t bin = min((uint32_t)f, (uint32_t)(kNumLambda - 1));
 #pragma unroll
                 for (int b = 0; b < kNumLambda; ++b)
