@@ -486,7 +486,10 @@ __global__ void __launch_bounds__(256, K == kMatGGXScattering ? SLRGPU_SHADE_DIE
 // libSLR/Renderer/VolumetricPTRenderer.cpp:146-296)
 // ---------------------------------------------------------------------------
 #ifndef SLRGPU_SHADEVOL_MIN_BLOCKS
-#define SLRGPU_SHADEVOL_MIN_BLOCKS 3   // measured best on the volumetric benchmark (2, 3 tried)
+#define SLRGPU_SHADEVOL_MIN_BLOCKS 3   // resident blocks per SM of the volumetric shading kernels
+#endif
+#ifndef SLRGPU_VOLINTERACT_MIN_BLOCKS
+#define SLRGPU_VOLINTERACT_MIN_BLOCKS SLRGPU_SHADEVOL_MIN_BLOCKS   // of the free-flight kernel
 #endif
 // Scene::interact for the volumetric integrator (Scene.cpp:66-94): the
 // closest surface hit is known; a collision in the medium before it may stop
@@ -496,7 +499,7 @@ __global__ void __launch_bounds__(256, K == kMatGGXScattering ? SLRGPU_SHADE_DIE
 // medium, a surface material kind, or the environment.  Splitting the
 // interaction from the shading keeps each shading kernel's code to one
 // vertex kind.
-__global__ void __launch_bounds__(256, SLRGPU_SHADEVOL_MIN_BLOCKS) kVolInteract(DevScene sc, WaveState ws,
+__global__ void __launch_bounds__(256, SLRGPU_VOLINTERACT_MIN_BLOCKS) kVolInteract(DevScene sc, WaveState ws,
                                                                               const uint32_t* __restrict__ queue,
                                                                               const uint32_t* __restrict__ count,
                                                                               uint32_t* classCounts) {

@@ -38,9 +38,10 @@ KNOBS = {
     "SLRGPU_SHADE_DIELECTRIC_MIN_BLOCKS": [2, 3, 4],
     "SLRGPU_SHADEVOL_MIN_BLOCKS": [2, 3],
     "SLRGPU_MEDIUM_MIN_BLOCKS": [2, 3, 4],
+    "SLRGPU_VOLINTERACT_MIN_BLOCKS": [2, 3, 4],
 }
 DEFAULTS = {"SLRGPU_TRACE_MIN_BLOCKS": 4, "SLRGPU_SHADE_MIN_BLOCKS": 3, "SLRGPU_SHADE_DIELECTRIC_MIN_BLOCKS": 3,
-            "SLRGPU_SHADEVOL_MIN_BLOCKS": 3, "SLRGPU_MEDIUM_MIN_BLOCKS": 4,
+            "SLRGPU_SHADEVOL_MIN_BLOCKS": 3, "SLRGPU_MEDIUM_MIN_BLOCKS": 4, "SLRGPU_VOLINTERACT_MIN_BLOCKS": 3,
             "wave_paths": 1 << 22, "bvh_width": 4}   # the sources' defaults
 WAVE_PATHS = [1 << 22, 1 << 23, 1 << 24, 1 << 25, 1 << 26]
 BVH_WIDTHS = [4, 8]
@@ -51,7 +52,7 @@ WORKLOAD_KNOBS = {
               "SLRGPU_SHADE_DIELECTRIC_MIN_BLOCKS", "wave_paths"],
     "ggx_ibl_1m": ["bvh_width", "SLRGPU_TRACE_MIN_BLOCKS", "SLRGPU_SHADE_MIN_BLOCKS",
                    "SLRGPU_SHADE_DIELECTRIC_MIN_BLOCKS", "wave_paths"],
-    "volumetric_small": ["SLRGPU_SHADEVOL_MIN_BLOCKS", "SLRGPU_MEDIUM_MIN_BLOCKS"],
+    "volumetric_small": ["SLRGPU_VOLINTERACT_MIN_BLOCKS", "SLRGPU_SHADEVOL_MIN_BLOCKS", "SLRGPU_MEDIUM_MIN_BLOCKS"],
 }
 
 # The timed workload of each candidate: scene recipe, size, spp, depth, integrator.
