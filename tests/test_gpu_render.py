@@ -149,6 +149,22 @@ def test_renderer_interface(gpu_lib):
     assert renderer.last_stats.path_samples == 16 * 16 * 4
 
 
+def test_volumetric_film_is_reproducible(gpu_lib):
+    """The transmittance walks are handed to lanes in whatever order the
+    warps draw them from a shared counter, but each (shadow ray, wavelength)
+    draws its own random stream and adds to its own path, and paths reach the
+    film in sample order: the same seed gives the same film bit for bit, in
+    one wave or in several."""
+    desc = scenes.medium_box_scene(24, 24, grid=32)
+    s = gpu_lib.Scene(desc)
+    a, _ = s.render(24, 24, 8, 16, seed=11, volumetric=True)
+    b, _ = s.render(24, 24, 8, 16, seed=11, volumetric=True)
+    c, _ = s.render(24, 24, 8, 16, seed=11, volumetric=True, samples_per_wave=3)
+    assert np.array_equal(a, b)
+    assert np.array_equal(a, c)
+    assert a.sum() > 0
+
+
 def test_sharded_render_sums_to_whole(gpu_lib):
     """Three ranks' sample ranges (slr_gb300/replicas.py) rendered with
     sample_base sum to the unsharded film: the same samples, summed in a
