@@ -5,8 +5,10 @@ checker / the timed CPU baseline, never by the product path.
 """
 from __future__ import annotations
 
+import contextlib
 import ctypes as C
 import os
+import sys
 from pathlib import Path
 
 import numpy as np
@@ -15,6 +17,32 @@ HERE = Path(__file__).resolve().parent
 LIB_PATH = HERE / "_ref" / "libslr_ref.so"
 
 _lib = None
+_libc = None
+
+
+@contextlib.contextmanager
+def _quiet():
+    """Sends the reference's progress lines (``slrprintf`` of the renderers
+    and of the SBVH build, which go to the C stdout) to /dev/null for the
+    duration of a call, unless SLR_ORACLE_VERBOSE is set."""
+    global _libc
+    if os.environ.get("SLR_ORACLE_VERBOSE"):
+        yield
+        return
+    if _libc is None:
+        _libc = C.CDLL(None)
+    sys.stdout.flush()
+    _libc.fflush(None)
+    saved = os.dup(1)
+    devnull = os.open(os.devnull, os.O_WRONLY)
+    try:
+        os.dup2(devnull, 1)
+        yield
+    finally:
+        _libc.fflush(None)
+        os.dup2(saved, 1)
+        os.close(saved)
+        os.close(devnull)
 
 
 def available() -> bool:
@@ -154,7 +182,8 @@ class RefScene:
                 L.ora_camera_equirect(self.h, mp, cam.sensitivity, cam.phi_angle, cam.theta_angle)
         self._keep = keep
         if build:
-            L.ora_build(self.h)
+            with _quiet():
+                L.ora_build(self.h)
 
     def __del__(self):
         if getattr(self, "h", None) and _lib is not None:
@@ -166,8 +195,9 @@ class RefScene:
         threads = threads or os.cpu_count() or 1
         film = np.zeros((height, width, 16), np.float32)
         sec = C.c_double(0)
-        rc = lib().ora_render(self.h, int(volumetric), spp, max_depth, width, height, threads, seed,
-                              film.ctypes.data_as(C.POINTER(C.c_float)), C.byref(sec))
+        with _quiet():
+            rc = lib().ora_render(self.h, int(volumetric), spp, max_depth, width, height, threads, seed,
+                                  film.ctypes.data_as(C.POINTER(C.c_float)), C.byref(sec))
         if rc != 0:
             raise RuntimeError("oracle render failed")
         self.last_dropped = int(lib().ora_dropped_samples())
@@ -180,8 +210,9 @@ class RefScene:
         threads = threads or os.cpu_count() or 1
         film = np.zeros((height, width, 16), np.float32)
         sec = C.c_double(0)
-        rc = lib().ora_render_bpt(self.h, int(volumetric), spp, max_depth, width, height, threads, seed,
-                                  film.ctypes.data_as(C.POINTER(C.c_float)), C.byref(sec))
+        with _quiet():
+            rc = lib().ora_render_bpt(self.h, int(volumetric), spp, max_depth, width, height, threads, seed,
+                                      film.ctypes.data_as(C.POINTER(C.c_float)), C.byref(sec))
         if rc == -2:
             raise RuntimeError("one BPT render per oracle scene")
         if rc != 0:
@@ -192,7 +223,8 @@ class RefScene:
     def sbvh_stats(self):
         nf, dep, nn = C.c_uint32(), C.c_uint32(), C.c_uint32()
         cost = C.c_float()
-        lib().ora_sbvh_build(self.h, C.byref(nf), C.byref(dep), C.byref(cost), C.byref(nn))
+        with _quiet():
+            lib().ora_sbvh_build(self.h, C.byref(nf), C.byref(dep), C.byref(cost), C.byref(nn))
         return {"fragments": nf.value, "depth": dep.value, "cost": cost.value, "nodes": nn.value}
 
     def sbvh_dump(self):
@@ -214,9 +246,10 @@ class RefScene:
         t = np.zeros(n, np.float32)
         b1 = np.zeros(n, np.float32)
         b2 = np.zeros(n, np.float32)
-        lib().ora_trace(self.h, rp, n, int(anyhit), threads, prim.ctypes.data_as(C.POINTER(C.c_uint32)),
-                        t.ctypes.data_as(C.POINTER(C.c_float)), b1.ctypes.data_as(C.POINTER(C.c_float)),
-                        b2.ctypes.data_as(C.POINTER(C.c_float)))
+        with _quiet():
+            lib().ora_trace(self.h, rp, n, int(anyhit), threads, prim.ctypes.data_as(C.POINTER(C.c_uint32)),
+                            t.ctypes.data_as(C.POINTER(C.c_float)), b1.ctypes.data_as(C.POINTER(C.c_float)),
+                            b2.ctypes.data_as(C.POINTER(C.c_float)))
         return (prim.astype(bool) if anyhit else prim), t, b1, b2
 
     def spectrum_eval(self, spectrum_index: int, lambdas: np.ndarray) -> np.ndarray:

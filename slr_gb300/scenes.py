@@ -1,6 +1,7 @@
 """Procedural scenes for the benchmark and parity configurations.
 
-All scenes are synthetic and seeded; nothing is read from disk.
+All scenes are synthetic and seeded; the only file they touch is the cache of
+large noise grids (:func:`fbm_density_grid`).
 
 * :func:`box_scene`   - the closed-box scene: a [0,1]^3 box of 10 triangles
   (open front face), two rotated boxes of 12 triangles each and a 0.25 x 0.25
@@ -14,6 +15,7 @@ from __future__ import annotations
 
 import dataclasses
 import math
+import os
 
 import numpy as np
 
@@ -313,15 +315,43 @@ def heightfield_scene(grid: int = 512, spheres: int = 64, sphere_freq: int = 20,
 
 def fbm_density_grid(n: int, seed: int = 0, octaves: int = 5) -> np.ndarray:
     """n^3 density grid [z][y][x]: max(0, 5-octave fBm improved Perlin),
-    normalised to a maximum of 1."""
+    normalised to a maximum of 1.  Evaluated in slabs of z (the same numbers
+    as one whole-grid evaluation, with far smaller temporaries); grids of
+    128^3 and larger are kept in slr_gb300/_cache (or $SLR_GB300_CACHE) after
+    the first evaluation, which takes about half a minute at 256^3."""
+    cache_dir = os.environ.get("SLR_GB300_CACHE", os.path.join(os.path.dirname(os.path.abspath(__file__)), "_cache"))
+    path = os.path.join(cache_dir, f"fbm_{n}_{seed}_{octaves}.npy")
+    if n >= 128 and os.path.isfile(path):
+        try:
+            d = np.load(path)
+            if d.shape == (n, n, n) and d.dtype == np.float32:
+                return d
+        except (OSError, ValueError):
+            pass
     noise = ImprovedPerlin(seed + 7)
     c = (np.arange(n) + 0.5) / n
-    Z, Y, X = np.meshgrid(c, c, c, indexing="ij")
-    d = np.maximum(noise.fbm(X * 3.0 + 0.13, Y * 3.0 + 0.71, Z * 3.0 + 0.37, octaves=octaves), 0.0)
+    Y, X = np.meshgrid(c, c, indexing="ij")
+    d = np.empty((n, n, n), np.float64)
+    slab = max(1, (1 << 20) // (n * n))
+    for z0 in range(0, n, slab):
+        zs = c[z0:z0 + slab]
+        Z = np.broadcast_to(zs[:, None, None], (len(zs), n, n))
+        d[z0:z0 + slab] = np.maximum(noise.fbm(np.broadcast_to(X * 3.0 + 0.13, Z.shape),
+                                               np.broadcast_to(Y * 3.0 + 0.71, Z.shape), Z * 3.0 + 0.37,
+                                               octaves=octaves), 0.0)
     m = d.max()
     if m > 0:
         d /= m
-    return d.astype(np.float32)
+    d = d.astype(np.float32)
+    if n >= 128:
+        try:
+            os.makedirs(cache_dir, exist_ok=True)
+            tmp = f"{path}.{os.getpid()}.tmp.npy"
+            np.save(tmp, d)
+            os.replace(tmp, path)
+        except OSError:
+            pass
+    return d
 
 
 def medium_box_scene(width: int = 512, height: int = 512, grid: int = 256, seed: int = 0, sigma_t_max: float = 20.0,

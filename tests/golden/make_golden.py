@@ -3,15 +3,18 @@
 reference renderer built by oracle/build_ref.py).  Run from the repository
 root:  python tests/golden/make_golden.py
 
-* box_render_32.npz - reference PTRenderer on the box scene at 32x32, max
-  depth 8: per pixel and film bin the mean and variance of K independent
-  batch estimates (film sum / spp of each batch), for the statistical image
-  parity test.
+* images/<case>.npz - for every image case of tests/image_cases.py that
+  keeps a fixture: per pixel and film bin the mean and variance of the
+  reference renderer's independent batch estimates (film sum / spp of each
+  batch, one seed and ONE render thread per batch, so the numbers do not
+  depend on scheduling), the per-batch image sums and edge sums, and the
+  dropped-sample count.
 * trace_box.npz, trace_soup.npz - ray sets with the reference SBVH's closest
   hit (prim, t) and any-hit result.
 * bsdf_kat.npz - reference BSDF sample / evaluate / pdf results at fixed
   (query, sample) tuples.
 """
+import argparse
 import os
 import sys
 
@@ -24,26 +27,20 @@ from oracle import oracle as O  # noqa: E402
 from slr_gb300 import scenes  # noqa: E402
 from tests import helpers  # noqa: E402
 from tests.bsdf_cases import bsdf_cases  # noqa: E402
+from tests import image_cases  # noqa: E402
 
 OUT = os.path.join(ROOT, "tests", "golden")
 
 
-def render_batches(desc, w, h, spp, depth, batches, seed0=1000):
-    ref = O.RefScene(desc)
-    means = []
-    for k in range(batches):
-        film, _ = ref.render(w, h, spp, depth, seed=seed0 + k, threads=os.cpu_count())
-        means.append(film / spp)
-    m = np.stack(means).astype(np.float64)
-    return m.mean(0), m.var(0, ddof=1)
+def make_images(names):
+    for name in names:
+        case = image_cases.CASES[name]
+        st = image_cases.reference_stats(case)
+        image_cases.save_golden(case, st)
+        print(f"{name}: {st['batches']} batches, image sum {st['sums'].mean():.6g}, dropped {st['dropped']}")
 
 
-def main():
-    desc = scenes.box_scene(32, 32)
-    K, spp = 48, 8
-    mean, var = render_batches(desc, 32, 32, spp, 8, K)
-    np.savez_compressed(os.path.join(OUT, "box_render_32.npz"), mean=mean.astype(np.float32),
-                        var=var.astype(np.float32), batches=K, spp=spp, max_depth=8)
+def make_rays_and_bsdfs():
     for name, d, n in (("trace_box", scenes.box_scene(32, 32), 20000), ("trace_soup", helpers.triangle_soup(3000, 7), 20000)):
         rays = helpers.random_rays(d, n, seed=11)
         ref = O.RefScene(d)
@@ -56,6 +53,17 @@ def main():
                            case.get("ay", 0.0), case["queries"])
         kat[case["name"]] = out
     np.savez_compressed(os.path.join(OUT, "bsdf_kat.npz"), **kat)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("images", nargs="*", help="image cases to regenerate (default: every case with a fixture)")
+    ap.add_argument("--rays-and-bsdfs", action="store_true", help="also regenerate the ray and BSDF fixtures")
+    a = ap.parse_args()
+    names = a.images or [n for n, c in image_cases.CASES.items() if c.golden]
+    make_images(names)
+    if a.rays_and_bsdfs:
+        make_rays_and_bsdfs()
     print("golden fixtures written to", OUT)
 
 

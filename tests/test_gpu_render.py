@@ -1,133 +1,57 @@
-"""Image parity on the GPU: per pixel and film bin, the GPU estimate agrees
-with the reference renderer's within 3 standard errors of the Monte Carlo
-estimate (expected exceedance 0.27% per bin; the test allows 1.5% because the
-standard errors are themselves estimated from a finite number of batches),
-and the image-wide sums agree within 4 combined standard errors."""
-import os
+"""Image parity on the GPU against the reference renderer.
 
+Per pixel and film bin, the GPU's Monte Carlo mean agrees with the
+reference's within 3 standard errors (expected exceedance 0.27 % per bin; the
+limit allows for standard errors that are themselves estimated from a finite
+number of batches), and the per-batch image sums agree within 4 standard
+errors.  The reference statistics come from one-thread reference renders
+(tests/image_cases.py), so every verdict is a fixed function of fixed seeds.
+"""
 import numpy as np
 import pytest
 
 from slr_gb300 import scenes
+from tests import image_cases as IC
 
 pytestmark = pytest.mark.gpu
-GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+
+PT_CASES = ["box_32", "ragged_box", "ragged_ggx_ibl", "ggx_ibl_24", "volumetric_20", "thin_lens", "equirect"]
 
 
-def gpu_batches(gpu_lib, desc, w, h, spp, depth, batches, seed0=50000):
-    s = gpu_lib.Scene(desc)
-    means = []
-    dropped = 0
-    for k in range(batches):
-        film, st = s.render(w, h, spp, depth, seed=seed0 + k)
-        dropped += st.dropped_samples
-        means.append(film.astype(np.float64) / spp)
-    m = np.stack(means)
-    return m.mean(0), m.var(0, ddof=1), dropped, m.reshape(batches, -1).sum(1)
-
-
-def check_statistical_parity(mg, vg, kg, mr, vr, kr, frac_limit=0.015, tg=None, tr=None):
-    """tg, tr: per-batch image sums, when known; the image-wide test then
-    uses their spread, which includes the correlation between the bins of one
-    pixel (one path adds to all 16 wavelength bins).
-
-    Per bin, the standard error uses the pooled variance of both sides: the
-    hypothesis under test is that the two renderers run the same estimator,
-    whose batch variance is then common to both, and pooling keeps a
-    heavy-tailed bin's variance estimate from resting on the smaller batch
-    count alone (with 48 reference batches the unpooled exceedance fraction
-    of an unbiased pair fluctuated up to ~2 %)."""
-    pooled = ((kg - 1) * vg + (kr - 1) * vr) / (kg + kr - 2)
-    se = np.sqrt(pooled / kg + pooled / kr)
-    diff = mg - mr
-    zero = se == 0
-    assert np.all(np.abs(diff[zero]) < 1e-6), "deterministic-zero bins differ"
-    z = np.abs(diff[~zero]) / se[~zero]
-    frac = float((z > 3).mean())
-    if tg is not None and tr is not None:
-        gz = (tg.mean() - tr.mean()) / np.sqrt(tg.var(ddof=1) / len(tg) + tr.var(ddof=1) / len(tr))
-    else:
-        gz = diff.sum() / np.sqrt((vg / kg).sum() + (vr / kr).sum())
-    assert frac < frac_limit, f"{frac:.4f} of bins beyond 3 sigma"
-    assert abs(gz) < 4.0, f"image-wide sum differs by {gz:.2f} sigma"
-    return frac, gz
-
-
-def test_box_scene_matches_reference(gpu_lib):
-    g = np.load(os.path.join(GOLDEN, "box_render_32.npz"))
-    desc = scenes.box_scene(32, 32)
-    mg, vg, dropped, _ = gpu_batches(gpu_lib, desc, 32, 32, int(g["spp"]), int(g["max_depth"]), 192)
-    frac, gz = check_statistical_parity(mg, vg, 192, g["mean"], g["var"], int(g["batches"]))
-    assert dropped == 0
-    # Same estimator, same noise: the summed per-bin variance of a batch
-    # mean matches the reference's, so equal sample counts give equal RMSE
-    # (the throughput ratios compare at matched RMSE).
-    ratio = vg.sum() / g["var"].sum()
-    assert 0.75 < ratio < 1.33, ratio
-
-
-def test_ragged_image_matches_reference(gpu_lib, oracle_lib):
-    """21 x 13 pixels: neither side a multiple of the reference's 8 x 8 sensor
-    tiles, so the last column and row also collect the samples of the
-    overhanging tile positions, as ImageSensor::add clamps them there."""
-    w, h = 21, 13
-    desc = scenes.heightfield_scene(grid=24, spheres=5, sphere_freq=3, env_size=(64, 32), width=w, height=h)
-    spp, depth, kr, kg = 8, 3, 64, 192
-    ref = oracle_lib.RefScene(desc)
-    rm = np.stack([ref.render(w, h, spp, depth, seed=700 + k, threads=os.cpu_count())[0].astype(np.float64) / spp
-                   for k in range(kr)])
-    mg, vg, _, tg = gpu_batches(gpu_lib, desc, w, h, spp, depth, kg)
-    check_statistical_parity(mg, vg, kg, rm.mean(0), rm.var(0, ddof=1), kr, tg=tg, tr=rm.reshape(kr, -1).sum(1))
-
-
-def test_ggx_ibl_scene_matches_reference(gpu_lib, oracle_lib):
-    """GGX conductors/dielectrics under the image-based environment (small
-    version of the 1M-triangle scene), against the live reference."""
-    desc = scenes.heightfield_scene(grid=24, spheres=5, sphere_freq=3, env_size=(64, 32), width=24, height=24)
-    w = h = 24
-    spp, depth, kr, kg = 8, 10, 40, 160
-    ref = oracle_lib.RefScene(desc)
-    means = []
-    for k in range(kr):
-        film, _ = ref.render(w, h, spp, depth, seed=100 + k, threads=os.cpu_count())
-        means.append(film.astype(np.float64) / spp)
-    rm = np.stack(means)
-    mg, vg, _, tg = gpu_batches(gpu_lib, desc, w, h, spp, depth, kg)
-    check_statistical_parity(mg, vg, kg, rm.mean(0), rm.var(0, ddof=1), kr, frac_limit=0.02, tg=tg,
-                             tr=rm.reshape(kr, -1).sum(1))
-
-
-def test_volumetric_box_matches_reference(gpu_lib, oracle_lib):
-    """Heterogeneous fBm medium (sigma_t max 20, albedo 0.9, HG g = 0.7) in
-    the box, VolumetricPTRenderer semantics, against the live reference.
-    Both renderers drop the same kind of non-finite samples (next-event
-    estimation from a vertex on the light toward a coplanar light point), so
-    the dropped fractions must agree too."""
-    desc = scenes.medium_box_scene(20, 20, grid=32)
-    w = h = 20
-    spp, depth, kr, kg = 8, 32, 48, 192
-    ref = oracle_lib.RefScene(desc)
-    means, rdrop = [], 0
-    for k in range(kr):
-        film, _ = ref.render(w, h, spp, depth, seed=300 + k, threads=os.cpu_count(), volumetric=True)
-        rdrop += ref.last_dropped
-        means.append(film.astype(np.float64) / spp)
-    rm = np.stack(means)
-    s = gpu_lib.Scene(desc)
-    gmeans, gdrop = [], 0
-    for k in range(kg):
-        film, st = s.render(w, h, spp, depth, seed=90000 + k, volumetric=True)
-        gdrop += st.dropped_samples
-        gmeans.append(film.astype(np.float64) / spp)
-    gm = np.stack(gmeans)
-    check_statistical_parity(gm.mean(0), gm.var(0, ddof=1), kg, rm.mean(0), rm.var(0, ddof=1), kr, frac_limit=0.02,
-                             tg=gm.reshape(kg, -1).sum(1), tr=rm.reshape(kr, -1).sum(1))
-    grid = ((w + 7) // 8 * 8) * ((h + 7) // 8 * 8)     # sample positions, whole 8 x 8 tiles
-    nr, ng = kr * grid * spp, kg * grid * spp
-    pr, pg = rdrop / nr, gdrop / ng
-    pooled = (rdrop + gdrop) / (nr + ng)
+def dropped_rates_agree(g, r, case):
+    """Both renderers drop the same kind of non-finite samples (next-event
+    estimation from a vertex on the light toward a coplanar light point in
+    the volumetric tracer): the dropped fractions agree within 4 standard
+    errors of a two-sample binomial comparison."""
+    grid = ((case.w + 7) // 8 * 8) * ((case.h + 7) // 8 * 8)     # sample positions, whole 8 x 8 tiles
+    nr, ng = r["batches"] * grid * case.spp, g["batches"] * grid * case.spp
+    pr, pg = r["dropped"] / nr, g["dropped"] / ng
+    pooled = (r["dropped"] + g["dropped"]) / (nr + ng)
     se = np.sqrt(pooled * (1 - pooled) * (1 / nr + 1 / ng)) + 1e-12
-    assert abs(pr - pg) < 4 * se, (pr, pg)
+    assert abs(pr - pg) < 4 * se, (pr, pg, se)
+
+
+@pytest.mark.parametrize("name", PT_CASES)
+def test_image_matches_reference(gpu_lib, name):
+    """The box (32^2); ragged images whose sides are not multiples of the
+    8 x 8 sensor tiles, where the last column and row also collect the
+    overhanging tile positions (ImageSensor.cpp:125-130, PTRenderer.cpp:104-110),
+    with and without the image-based environment and its 5e4 sun; GGX
+    conductors and dielectrics under the environment; the fBm medium
+    (VolumetricPTRenderer); the thin-lens and equirectangular cameras
+    (PerspectiveCamera.cpp:31-83, EquirectangularCamera.cpp:25-69)."""
+    case = IC.CASES[name]
+    r = IC.load_reference(case)
+    g = IC.gpu_stats(gpu_lib, case)
+    rep = IC.parity_report(g, r, ragged=name.startswith("ragged"))
+    IC.assert_parity(rep, case.frac_limit, name)
+    assert g["mean"].sum() > 0
+    dropped_rates_agree(g, r, case)
+    if name in ("box_32", "ragged_box"):
+        # Same estimator, same noise: the summed per-bin variance of a batch
+        # mean matches the reference's, so equal sample counts give equal
+        # RMSE (the throughput ratios compare at matched RMSE).
+        assert 0.75 < rep["var_ratio"] < 1.33, rep
 
 
 def test_render_settings_validation(gpu_lib):
@@ -175,30 +99,6 @@ def test_sharded_render_sums_to_whole(gpu_lib):
     parts = [render_shard(s, 32, 32, 16, 8, seed=5, world=3, rank=r)[0] for r in range(3)]
     np.testing.assert_allclose(sum(parts), whole, rtol=2e-5, atol=1e-6)
     assert not np.array_equal(parts[0], parts[1])
-
-
-@pytest.mark.parametrize("kind", ["thin_lens", "equirect"])
-def test_cameras_match_reference(gpu_lib, oracle_lib, kind):
-    """The thin-lens camera (lens radius 0.04, focused at the back wall) and
-    the equirectangular camera (inside the box, full sphere) against the live
-    reference (PerspectiveCamera.cpp:31-83, EquirectangularCamera.cpp:25-69)."""
-    from slr_gb300.scene_desc import Camera
-    w, h = (24, 16) if kind == "thin_lens" else (32, 16)
-    desc = scenes.box_scene(w, h)
-    if kind == "thin_lens":
-        desc.camera = Camera("perspective", scenes.look_at((0.5, 0.5, 2.3), (0.5, 0.5, 0.0)), sensitivity=1.0,
-                             aspect=w / h, fov_y=np.radians(38.0), lens_radius=0.04, img_plane_dist=1.0,
-                             obj_plane_dist=2.3)
-    else:
-        desc.camera = Camera("equirect", scenes.look_at((0.5, 0.45, 0.6), (0.5, 0.45, 0.0)), sensitivity=1.0,
-                             phi_angle=2 * np.pi, theta_angle=np.pi)
-    spp, depth, kr, kg = 8, 4, 96, 192
-    ref = oracle_lib.RefScene(desc)
-    rm = np.stack([ref.render(w, h, spp, depth, seed=900 + k, threads=os.cpu_count())[0].astype(np.float64) / spp
-                   for k in range(kr)])
-    mg, vg, _, tg = gpu_batches(gpu_lib, desc, w, h, spp, depth, kg)
-    check_statistical_parity(mg, vg, kg, rm.mean(0), rm.var(0, ddof=1), kr, tg=tg, tr=rm.reshape(kr, -1).sum(1))
-    assert mg.sum() > 0
 
 
 def test_degenerate_scenes(gpu_lib):
