@@ -301,47 +301,11 @@ def run_traversal(args):
     from oracle import oracle as O
     desc = scenes.heightfield_scene(seed=0)
     scene = api.Scene(desc)
+    from slr_gb300 import raysets
     n_side = 4096
     n = n_side * n_side
-    dev = torch.device("cuda")
-    g = torch.Generator(device=dev)
-    g.manual_seed(0)
-    # coherent: pinhole through pixel centres, the scene camera's frame
-    cam = desc.camera
-    m = torch.tensor(cam.cam_to_world, dtype=torch.float64, device=dev)
-    th = np.tan(cam.fov_y / 2)
-    ij = torch.arange(n_side, dtype=torch.float64, device=dev) + 0.5
-    y, x = torch.meshgrid(ij, ij, indexing="ij")
-    lx = (0.5 - x / n_side) * 2 * th * cam.aspect      # mirrored image x (PerspectiveCamera)
-    ly = (0.5 - y / n_side) * 2 * th
-    dl = torch.stack([lx, ly, torch.ones_like(lx)], -1).reshape(-1, 3)
-    dw = dl @ m[:3, :3].T
-    dw = dw / dw.norm(dim=1, keepdim=True)
-    coherent = torch.zeros((n, 8), dtype=torch.float32, device=dev)
-    coherent[:, 0:3] = m[:3, 3].float()
-    coherent[:, 4:7] = dw.float()
-    coherent[:, 7] = float("inf")
-    # incoherent: area-weighted surface points, uniform directions
-    tris = torch.tensor(desc.triangle_arrays(), dtype=torch.float32, device=dev)
-    area = 0.5 * torch.linalg.cross(tris[:, 1] - tris[:, 0], tris[:, 2] - tris[:, 0]).norm(dim=1)
-    pick = torch.multinomial(area, n, replacement=True, generator=g)
-    u0 = torch.rand(n, device=dev, generator=g)
-    u1 = torch.rand(n, device=dev, generator=g)
-    su = u0.sqrt()
-    b0, b1 = 1 - su, u1 * su
-    t = tris[pick]
-    org = b0[:, None] * t[:, 0] + b1[:, None] * t[:, 1] + (1 - b0 - b1)[:, None] * t[:, 2]
-    z = torch.rand(n, device=dev, generator=g) * 2 - 1
-    phi = torch.rand(n, device=dev, generator=g) * 2 * np.pi
-    sz = (1 - z * z).clamp_min(0).sqrt()
-    incoherent = torch.zeros((n, 8), dtype=torch.float32, device=dev)
-    incoherent[:, 0:3] = org
-    incoherent[:, 3] = 1e-4
-    incoherent[:, 4] = sz * torch.cos(phi)
-    incoherent[:, 5] = sz * torch.sin(phi)
-    incoherent[:, 6] = z
-    incoherent[:, 7] = 0.1 + 9.9 * torch.rand(n, device=dev, generator=g)
-    del tris, pick, t, org
+    coherent = raysets.coherent_rays(desc, n_side)
+    incoherent = raysets.incoherent_rays(desc, n, seed=0)
     torch.cuda.synchronize()
     results = {}
     ref = O.RefScene(desc, build=False)

@@ -19,6 +19,7 @@ from __future__ import annotations
 
 import ctypes as C
 import enum
+import os
 import re
 from pathlib import Path
 
@@ -27,7 +28,10 @@ import numpy as np
 from .scene_desc import SceneDesc
 
 PKG = Path(__file__).resolve().parent
-LIB_PATH = PKG / "lib" / "libslrgpu.so"
+# SLRGPU_LIB_VARIANT=w8 loads the build with 8-wide BVH nodes
+# (slr_gb300/build.py); the default is the tuned build.
+_VARIANT = os.environ.get("SLRGPU_LIB_VARIANT", "")
+LIB_PATH = PKG / "lib" / (f"libslrgpu_{_VARIANT}.so" if _VARIANT else "libslrgpu.so")
 HEADER = PKG.parent / "include" / "slrgpu.h"
 
 _lib = None

@@ -59,53 +59,79 @@ def tuning_flags() -> list[str]:
     return flags
 
 
-def build(verbose: bool = False, force: bool = False, extra_nvcc: list[str] | None = None) -> Path:
-    extra_nvcc = list(extra_nvcc or []) + tuning_flags()
-    # rebuild the CUDA objects when the tuned flags change
-    stamp = BUILD / "nvcc_flags"
-    BUILD.mkdir(exist_ok=True)
-    if not stamp.is_file() or stamp.read_text() != " ".join(extra_nvcc):
-        force = True
+# Library variants: the tuned build, and the same sources with 8-wide BVH
+# nodes (the BVH width is a compile-time layout constant shared by the host
+# collapse and the kernels; the 8-wide variant exists so that both widths are
+# tested).  SLRGPU_LIB_VARIANT selects the one slr_gb300.api loads.
+VARIANTS = {"": [], "w8": ["-DSLRGPU_BVH_WIDTH=8"]}
+
+
+def lib_path(variant: str = "") -> Path:
+    return LIB_DIR / (f"libslrgpu_{variant}.so" if variant else "libslrgpu.so")
+
+
+def _variant_flags(variant: str, extra: list[str]) -> list[str]:
+    flags = list(extra)
+    if VARIANTS[variant]:
+        flags = [f for f in flags if not f.startswith("-DSLRGPU_BVH_WIDTH=")] + VARIANTS[variant]
+    return flags
+
+
+def build(verbose: bool = False, force: bool = False, extra_nvcc: list[str] | None = None,
+          variants: tuple[str, ...] = ("", "w8")) -> Path:
+    """Compiles every translation unit of every variant in one parallel pass
+    and links each variant's shared library; returns the default library."""
+    base_flags = list(extra_nvcc or []) + tuning_flags()
     cuda = _cuda_home()
     nvcc = str(cuda / "bin" / "nvcc")
-    BUILD.mkdir(exist_ok=True)
     LIB_DIR.mkdir(exist_ok=True)
     inc = [f"-I{cuda / 'include'}", f"-I{CSRC}"]
-    # layout constants the host build shares with the kernels (BVH width)
-    host_defs = [f for f in extra_nvcc if f.startswith("-DSLRGPU_BVH_WIDTH=")]
     deps = sorted(CSRC.glob("*.h")) + sorted(CSRC.glob("*.cuh")) + sorted(CSRC.glob("*.inc")) + \
         [PKG.parent / "include" / "slrgpu.h"]
     newest_dep = max(p.stat().st_mtime for p in deps)
-    jobs = []
-    objs = []
-    for src in HOST_SOURCES:
-        o = BUILD / (src + ".o")
-        objs.append(o)
-        s = CSRC / src
-        if force or not o.exists() or o.stat().st_mtime < max(s.stat().st_mtime, newest_dep):
-            jobs.append(["g++", "-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-unused-function",
-                         *host_defs, *inc, "-c", str(s), "-o", str(o)])
-    for src in CUDA_SOURCES:
-        o = BUILD / (src + ".o")
-        objs.append(o)
-        s = CSRC / src
-        if force or not o.exists() or o.stat().st_mtime < max(s.stat().st_mtime, newest_dep):
-            jobs.append([nvcc, "-std=c++17", "-O3", "-lineinfo", *ARCH, "-Xcompiler", "-fPIC",
-                         "-Xcompiler", "-ffp-contract=off", "-Xptxas", "-v", *(extra_nvcc or []),
-                         *inc, "-c", str(s), "-o", str(o)])
+    jobs, links = [], []
+    for variant in variants:
+        flags = _variant_flags(variant, base_flags)
+        bdir = BUILD if not variant else PKG / f"_build_{variant}"
+        bdir.mkdir(exist_ok=True)
+        # rebuild the objects when the flags change
+        stamp = bdir / "nvcc_flags"
+        vforce = force or not stamp.is_file() or stamp.read_text() != " ".join(flags)
+        # layout constants the host build shares with the kernels (BVH width)
+        host_defs = [f for f in flags if f.startswith("-DSLRGPU_BVH_WIDTH=")]
+        objs, vjobs = [], []
+        for src in HOST_SOURCES:
+            o = bdir / (src + ".o")
+            objs.append(o)
+            sp = CSRC / src
+            if vforce or not o.exists() or o.stat().st_mtime < max(sp.stat().st_mtime, newest_dep):
+                vjobs.append(["g++", "-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-unused-function",
+                              *host_defs, *inc, "-c", str(sp), "-o", str(o)])
+        for src in CUDA_SOURCES:
+            o = bdir / (src + ".o")
+            objs.append(o)
+            sp = CSRC / src
+            if vforce or not o.exists() or o.stat().st_mtime < max(sp.stat().st_mtime, newest_dep):
+                vjobs.append([nvcc, "-std=c++17", "-O3", "-lineinfo", *ARCH, "-Xcompiler", "-fPIC",
+                              "-Xcompiler", "-ffp-contract=off", "-Xptxas", "-v", *flags,
+                              *inc, "-c", str(sp), "-o", str(o)])
+        jobs += vjobs
+        links.append((variant, objs, stamp, flags, bool(vjobs)))
     with cf.ThreadPoolExecutor(max_workers=max(1, len(jobs))) as ex:
         for cmd, rc, out in ex.map(_run, jobs):
             if rc != 0:
                 raise RuntimeError(f"compile failed: {' '.join(cmd)}\n{out[-6000:]}")
             if verbose:
                 print(out)
-    stamp.write_text(" ".join(extra_nvcc))
-    if jobs or not LIB.exists():
-        cmd = [nvcc, "-shared", *ARCH, "-o", str(LIB), *[str(o) for o in objs], "-lcudart_static", "-lrt",
-               "-lpthread", "-ldl"]
-        _, rc, out = _run(cmd)
-        if rc != 0:
-            raise RuntimeError(f"link failed: {' '.join(cmd)}\n{out[-6000:]}")
+    for variant, objs, stamp, flags, rebuilt in links:
+        stamp.write_text(" ".join(flags))
+        lib = lib_path(variant)
+        if rebuilt or not lib.exists():
+            cmd = [nvcc, "-shared", *ARCH, "-o", str(lib), *[str(o) for o in objs], "-lcudart_static", "-lrt",
+                   "-lpthread", "-ldl"]
+            _, rc, out = _run(cmd)
+            if rc != 0:
+                raise RuntimeError(f"link failed: {' '.join(cmd)}\n{out[-6000:]}")
     return LIB
 
 

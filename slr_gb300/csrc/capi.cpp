@@ -423,6 +423,7 @@ int slrgpu_render(slrgpu_handle scene, const slrgpu_settings* settings, float* f
     const bool mutating = false;
     GET_SCENE(s, scene);
     if (!settings || !film) return fail(SLRGPU_ERR_INVALID_ARGUMENT, "settings and film must not be NULL");
+    if (int rc = checkImageSize(settings->width, settings->height)) return rc;
     if (!s->committed) return fail(SLRGPU_ERR_NOT_COMMITTED, "scene not committed");
     if (!s->host.cameraPresent) return fail(SLRGPU_ERR_STATE, "scene has no camera");
     if (settings->volumetric && !s->host.medium.present)
@@ -437,6 +438,7 @@ int slrgpu_render_noalloc(slrgpu_handle scene, const slrgpu_settings* settings, 
     const bool mutating = false;
     GET_SCENE(s, scene);
     if (!settings || !film_device) return fail(SLRGPU_ERR_INVALID_ARGUMENT, "settings and film must not be NULL");
+    if (int rc = checkImageSize(settings->width, settings->height)) return rc;
     if (!s->committed) return fail(SLRGPU_ERR_NOT_COMMITTED, "scene not committed");
     if (!s->host.cameraPresent) return fail(SLRGPU_ERR_STATE, "scene has no camera");
     if (settings->volumetric && !s->host.medium.present)

@@ -74,6 +74,26 @@ __host__ __device__ __forceinline__ uint32_t padToTile(uint32_t n) {
     return (n + kSensorTile - 1) / kSensorTile * kSensorTile;
 }
 
+// Image sizes every entry point accepts: both sides positive and at most
+// 2^20 (so the tile padding cannot wrap a 32-bit side), and at most 2^31 - 1
+// positions in the tile-padded grid (path and film indices are 32-bit).
+// The product is formed in 64 bits.
+int checkImageSize(uint32_t width, uint32_t height) {
+    if (width == 0 || height == 0) {
+        setError("width and height must be positive");
+        return SLRGPU_ERR_INVALID_ARGUMENT;
+    }
+    if (width > kMaxImageSide || height > kMaxImageSide) {
+        setError("width and height must be at most 2^20");
+        return SLRGPU_ERR_INVALID_ARGUMENT;
+    }
+    if ((uint64_t)padToTile(width) * padToTile(height) > 0x7fffffffull) {
+        setError("image too large: the tile-padded sample grid exceeds 2^31 - 1 positions");
+        return SLRGPU_ERR_INVALID_ARGUMENT;
+    }
+    return SLRGPU_OK;
+}
+
 // One request's share of a wave: `samples` consecutive sample indices from
 // `sampleBase`, each over every position of the request's tile-padded grid,
 // as the paths [pathBegin, pathBegin + samples * gridPositions).  A path's
@@ -1360,28 +1380,42 @@ static const WaveGrids &waveGrids(int block) {
     return g;
 }
 
-// Optional per-launch timing of the wave kernels by kernel class.
+// Optional per-launch timing of the wave kernels by kernel class.  Timing
+// stops (and the incomplete mark is dropped) if an event cannot be created or
+// recorded; the render itself goes on.
 struct LaunchMarks {
     std::vector<cudaEvent_t>* pool = nullptr;   // null: no timing
     cudaStream_t stream = 0;
     struct Mark { int cls; size_t ev; };
     std::vector<Mark> marks;
     size_t used = 0;
-    cudaEvent_t next() {
+    bool pending = false;                       // the last mark still needs its end event
+    bool record() {
         if (used == pool->size()) {
             cudaEvent_t e;
-            cudaEventCreate(&e);
+            if (cudaEventCreate(&e) != cudaSuccess) return false;
             pool->push_back(e);
         }
-        return (*pool)[used++];
+        return cudaEventRecord((*pool)[used++], stream) == cudaSuccess;
+    }
+    void stop() {
+        if (pending) marks.pop_back();
+        pending = false;
+        pool = nullptr;
     }
     void begin(int cls) {
         if (!pool) return;
         marks.push_back(Mark{cls, used});
-        cudaEventRecord(next(), stream);
+        pending = true;
+        if (!record()) stop();
     }
     void end() {
-        if (pool) cudaEventRecord(next(), stream);
+        if (!pool) return;
+        if (!record()) {
+            stop();
+            return;
+        }
+        pending = false;
     }
 };
 
@@ -1410,16 +1444,19 @@ static WavePlan planWaves(const slrgpu_settings &s, uint32_t autoPaths) {
 // One wave: camera rays for every path of the wave's segments, then per
 // bounce the extension, shading and shadow kernels over the device-side
 // queues, then the film update of every segment.  Stream-ordered; counters,
-// queues and path state live in w.  Returns the number of kernel launches.
-static uint64_t runWave(const DeviceScene &ds0, const WaveState &w, const WaveParams &wp, uint32_t D, bool volumetric,
-                        bool watertight, cudaStream_t stream, LaunchMarks &lm, const WaveParams* wpDev = nullptr) {
+// queues and path state live in w.  Adds the number of kernel launches to
+// *launchCount; returns SLRGPU_OK, or SLRGPU_ERR_CUDA (error text set) when
+// the counter reset or a launch was rejected.
+static int runWave(const DeviceScene &ds0, const WaveState &w, const WaveParams &wp, uint32_t D, bool volumetric,
+                   bool watertight, cudaStream_t stream, LaunchMarks &lm, uint64_t* launchCount,
+                   const WaveParams* wpDev = nullptr) {
     // the scene as the kernels see it, with the triangle test chosen
     struct { DevScene sc; uint32_t kindMask; } ds{ds0.sc, ds0.kindMask};
     ds.sc.watertight = watertight ? 1u : 0u;
     const int block = 256;
     const WaveGrids &g = waveGrids(block);
     uint64_t launches = 0;
-    cudaMemsetAsync(w.counters, 0, (size_t)kCtrStride * (D + 2) * sizeof(uint32_t), stream);
+    CUDA_TRY(cudaMemsetAsync(w.counters, 0, (size_t)kCtrStride * (D + 2) * sizeof(uint32_t), stream));
     lm.begin(SLRGPU_KERNEL_RAYGEN);
     kRaygen<<<g.raygen, block, 0, stream>>>(ds.sc, w, wp, wpDev);
     lm.end();
@@ -1525,14 +1562,15 @@ static uint64_t runWave(const DeviceScene &ds0, const WaveState &w, const WavePa
     kAccumulate<<<g.accumulate, block, 0, stream>>>(w, wp, wpDev);
     lm.end();
     ++launches;
-    return launches;
+    *launchCount += launches;
+    CUDA_TRY(cudaGetLastError());
+    return SLRGPU_OK;
 }
 
 // The wave loop of one render (slrgpu_render, slrgpu_render_noalloc): waves
 // of pl.S sample indices over the whole sample grid, one segment each.
-static uint64_t runWaves(const DeviceScene &ds, const slrgpu_settings &s, const WavePlan &pl, const WaveState &w,
-                         float* filmSum, float* filmComp, cudaStream_t stream, LaunchMarks &lm) {
-    uint64_t launches = 0;
+static int runWaves(const DeviceScene &ds, const slrgpu_settings &s, const WavePlan &pl, const WaveState &w,
+                    float* filmSum, float* filmComp, cudaStream_t stream, LaunchMarks &lm, uint64_t* launches) {
     for (uint32_t base = 0; base < s.spp; base += pl.S) {
         WaveParams wp;
         std::memset(&wp, 0, sizeof(wp));
@@ -1553,25 +1591,23 @@ static uint64_t runWaves(const DeviceScene &ds, const slrgpu_settings &s, const 
         wp.numSegments = 1;
         wp.numPaths = sg.samples * pl.gridPositions;
         wp.filmPixels = s.width * s.height;
-        launches += runWave(ds, w, wp, s.max_depth, s.volumetric != 0, (s.flags & SLRGPU_FLAG_WATERTIGHT) != 0,
-                            stream, lm);
+        int rc = runWave(ds, w, wp, s.max_depth, s.volumetric != 0, (s.flags & SLRGPU_FLAG_WATERTIGHT) != 0,
+                         stream, lm, launches);
+        if (rc != SLRGPU_OK) return rc;
     }
-    return launches;
+    return SLRGPU_OK;
 }
 
 int RenderEngine::render(const DeviceScene &ds, const slrgpu_settings &s, float* film, bool filmOnDevice,
                          slrgpu_render_stats* stats, cudaStream_t stream) {
     auto t0 = std::chrono::steady_clock::now();
-    if (s.width == 0 || s.height == 0 || s.spp == 0) {
+    if (s.spp == 0) {
         setError("width, height and spp must be positive");
         return SLRGPU_ERR_INVALID_ARGUMENT;
     }
+    if (int rc = checkImageSize(s.width, s.height)) return rc;
     if (s.max_depth > 1000) {
         setError("max_depth must be <= 1000");
-        return SLRGPU_ERR_INVALID_ARGUMENT;
-    }
-    if ((uint64_t)padToTile(s.width) * padToTile(s.height) > 0x7fffffffull) {
-        setError("image too large");
         return SLRGPU_ERR_INVALID_ARGUMENT;
     }
     const bool bidir = (s.flags & SLRGPU_FLAG_BPT) != 0;
@@ -1593,10 +1629,18 @@ int RenderEngine::render(const DeviceScene &ds, const slrgpu_settings &s, float*
     CUDA_TRY(cudaMemsetAsync(filmSum, 0, (size_t)P * kNumLambda * sizeof(float), stream));
     CUDA_TRY(cudaMemsetAsync(filmComp, 0, (size_t)P * kNumLambda * sizeof(float), stream));
     if (!bidir) CUDA_TRY(cudaMemsetAsync(ws->stats, 0, 4 * sizeof(unsigned long long), stream));
-    cudaEvent_t e0, e1;
-    cudaEventCreate(&e0);
-    cudaEventCreate(&e1);
-    cudaEventRecord(e0, stream);
+    // the render's start and end events, destroyed on every return path
+    struct EventPair {
+        cudaEvent_t e[2] = {nullptr, nullptr};
+        ~EventPair() {
+            for (cudaEvent_t x : e)
+                if (x) cudaEventDestroy(x);
+        }
+    } events;
+    CUDA_TRY(cudaEventCreate(&events.e[0]));
+    CUDA_TRY(cudaEventCreate(&events.e[1]));
+    cudaEvent_t e0 = events.e[0], e1 = events.e[1];
+    CUDA_TRY(cudaEventRecord(e0, stream));
     const bool profile = (s.flags & SLRGPU_FLAG_PROFILE_KERNELS) != 0;
     LaunchMarks lm;
     lm.stream = stream;
@@ -1606,28 +1650,23 @@ int RenderEngine::render(const DeviceScene &ds, const slrgpu_settings &s, float*
     std::memset(&bst, 0, sizeof(bst));
     if (bidir) {
         rc = renderBpt(*bpt, ds, s, filmSum, filmComp, stream, &launches, profile ? &eventPool : nullptr, &bst);
-        if (rc != SLRGPU_OK) {
-            cudaEventDestroy(e0);
-            cudaEventDestroy(e1);
-            return rc;
-        }
+        if (rc != SLRGPU_OK) return rc;
     } else {
-        launches = runWaves(ds, s, pl, *ws, filmSum, filmComp, stream, lm);
+        rc = runWaves(ds, s, pl, *ws, filmSum, filmComp, stream, lm, &launches);
+        if (rc != SLRGPU_OK) return rc;
     }
     CUDA_TRY(cudaGetLastError());
     float* dst = filmOnDevice ? film : filmOut;
     kFilmToPixelMajor<<<waveGrids(256).accumulate, 256, 0, stream>>>(filmSum, dst, P);
     ++launches;
-    cudaEventRecord(e1, stream);
+    CUDA_TRY(cudaEventRecord(e1, stream));
     if (!filmOnDevice)
         CUDA_TRY(cudaMemcpyAsync(film, filmOut, (size_t)P * kNumLambda * sizeof(float), cudaMemcpyDeviceToHost, stream));
     unsigned long long hstats[4] = {0, 0, 0, 0};
     if (!bidir) CUDA_TRY(cudaMemcpyAsync(hstats, ws->stats, sizeof(hstats), cudaMemcpyDeviceToHost, stream));
     CUDA_TRY(cudaStreamSynchronize(stream));
     float ms = 0;
-    cudaEventElapsedTime(&ms, e0, e1);
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
+    CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
     if (stats) {
         std::memset(stats, 0, sizeof(*stats));
         if (bidir) {
@@ -1702,23 +1741,25 @@ int renderNoAlloc(const DeviceScene &ds, const slrgpu_settings &s, float* film, 
         setError("film must be a device pointer");
         return SLRGPU_ERR_INVALID_ARGUMENT;
     }
-    if (s.width == 0 || s.height == 0 || s.spp == 0) {
+    if (s.spp == 0) {
         setError("width, height and spp must be positive");
         return SLRGPU_ERR_INVALID_ARGUMENT;
     }
+    if (int rc = checkImageSize(s.width, s.height)) return rc;
     if ((uint64_t)padToTile(s.width) * padToTile(s.height) > kNoAllocMaxPaths) {
         setError("slrgpu_render_noalloc: the sample grid (width and height rounded up to multiples of 8) exceeds "
-                 "the fixed scratch limit of 65536 pixels");
+                 "the fixed scratch limit of " + std::to_string(kNoAllocMaxPaths) + " positions");
         return SLRGPU_ERR_INVALID_ARGUMENT;
     }
     if (s.max_depth > kNoAllocMaxDepth) {
-        setError("slrgpu_render_noalloc: max_depth exceeds the fixed scratch limit of 64");
+        setError("slrgpu_render_noalloc: max_depth exceeds the fixed scratch limit of " +
+                 std::to_string(kNoAllocMaxDepth));
         return SLRGPU_ERR_INVALID_ARGUMENT;
     }
     const WavePlan pl = planWaves(s, kNoAllocMaxPaths);
     if ((uint64_t)pl.S * pl.gridPositions > kNoAllocMaxPaths) {
-        setError("slrgpu_render_noalloc: sample grid * samples_per_wave exceeds the fixed scratch limit of 65536 "
-                 "paths");
+        setError("slrgpu_render_noalloc: sample grid * samples_per_wave exceeds the fixed scratch limit of " +
+                 std::to_string(kNoAllocMaxPaths) + " paths");
         return SLRGPU_ERR_INVALID_ARGUMENT;
     }
     const uint32_t P = pl.filmPixels;
@@ -1769,7 +1810,8 @@ int renderNoAlloc(const DeviceScene &ds, const slrgpu_settings &s, float* film, 
     CUDA_TRY(cudaMemsetAsync(filmComp, 0, (size_t)P * kNumLambda * sizeof(float), stream));
     CUDA_TRY(cudaMemsetAsync(w.stats, 0, 4 * sizeof(unsigned long long), stream));
     LaunchMarks lm;
-    runWaves(ds, s, pl, w, filmSum, filmComp, stream, lm);
+    uint64_t launches = 0;
+    if (int rc = runWaves(ds, s, pl, w, filmSum, filmComp, stream, lm, &launches)) return rc;
     kFilmToPixelMajor<<<waveGrids(256).accumulate, 256, 0, stream>>>(filmSum, film, P);
     CUDA_TRY(cudaGetLastError());
     return SLRGPU_OK;
@@ -1955,10 +1997,10 @@ int launchWave(const DeviceScene &ds, WaveSlot* slot, const SegmentDesc* segs, i
     wp.filmPixels = (uint32_t)pixels;
     if (!useGraph) {
         LaunchMarks lm;
-        uint64_t n = runWave(ds, *slot->engine.ws, wp, maxDepth, volumetric, watertight, stream, lm);
+        uint64_t n = 0;
+        int rc = runWave(ds, *slot->engine.ws, wp, maxDepth, volumetric, watertight, stream, lm, &n);
         if (launches) *launches += n;
-        CUDA_TRY(cudaGetLastError());
-        return SLRGPU_OK;
+        return rc;
     }
     WaveSlot::Graph* graph = nullptr;
     for (WaveSlot::Graph &g : slot->graphs)
@@ -1973,9 +2015,14 @@ int launchWave(const DeviceScene &ds, WaveSlot* slot, const SegmentDesc* segs, i
         LaunchMarks lm;
         cudaGraph_t g = nullptr;
         CUDA_TRY(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
-        uint64_t n = runWave(ds, *slot->engine.ws, empty, maxDepth, volumetric, watertight, stream, lm,
-                             slot->dParams);
+        uint64_t n = 0;
+        int rc = runWave(ds, *slot->engine.ws, empty, maxDepth, volumetric, watertight, stream, lm, &n,
+                         slot->dParams);
         cudaError_t e = cudaStreamEndCapture(stream, &g);
+        if (rc != SLRGPU_OK) {
+            if (g) cudaGraphDestroy(g);
+            return rc;
+        }
         if (e != cudaSuccess) {
             setError(std::string("wave capture failed: ") + cudaGetErrorString(e));
             return SLRGPU_ERR_CUDA;

@@ -76,6 +76,10 @@ WaveSlot* waveSlotCreate(uint32_t paths, uint32_t maxDepth, std::string* err);
 void waveSlotDestroy(WaveSlot* slot);
 uint32_t waveSlotCapacity(const WaveSlot* slot);
 uint32_t sampleGridPositions(uint32_t width, uint32_t height);
+// Largest image side any entry point accepts; checkImageSize() also bounds
+// the tile-padded grid to 2^31 - 1 positions (sets the error text).
+constexpr uint32_t kMaxImageSide = 1u << 20;
+int checkImageSize(uint32_t width, uint32_t height);
 // useGraph: replay the slot's captured graph for this (scene, depth,
 // integrator), capturing it on first use.
 int launchWave(const DeviceScene &ds, WaveSlot* slot, const SegmentDesc* segs, int numSegs, uint32_t maxDepth,

@@ -85,10 +85,11 @@ double Server::now() const {
 }
 
 int Server::submit(const DeviceScene* ds, std::atomic<int>* pin, const slrgpu_settings &s, uint64_t* id) {
-    if (s.width == 0 || s.height == 0 || s.spp == 0) {
+    if (s.spp == 0) {
         setError("width, height and spp must be positive");
         return SLRGPU_ERR_INVALID_ARGUMENT;
     }
+    if (int rc = checkImageSize(s.width, s.height)) return rc;
     if (s.max_depth > cfg_.max_depth) {
         setError("max_depth exceeds the server's max_depth");
         return SLRGPU_ERR_INVALID_ARGUMENT;

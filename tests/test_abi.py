@@ -37,6 +37,26 @@ def test_invalid_handles_and_arguments(gpu_lib):
     assert L.slrgpu_scene_destroy(h.value) == 0
 
 
+@pytest.mark.parametrize("entry", ["slrgpu_render", "slrgpu_render_noalloc"])
+def test_image_size_limits_checked_before_any_device_work(gpu_lib, entry):
+    """Sides above 2^20 (where rounding a 32-bit side up to the 8 x 8 sensor
+    tiles would wrap to 0) and tile-padded grids above 2^31 - 1 positions are
+    rejected as invalid arguments before the scene's state is looked at."""
+    L = gpu_lib.lib()
+    h = C.c_uint64()
+    assert L.slrgpu_scene_create(0, C.byref(h)) == 0
+    film = np.zeros(16, np.float32)
+    fn = getattr(L, entry)
+    tail = (0, None) if entry == "slrgpu_render" else (None,)
+    for w, hh in ((0xFFFFFFF9, 8), (8, 0xFFFFFFFF), ((1 << 20) + 1, 1), (1 << 20, 1 << 12), (0, 8)):
+        st = gpu_lib.Settings(w, hh, 1, 1, 0, 0, 0, 0)
+        assert fn(h.value, C.byref(st), C.c_void_p(film.ctypes.data), *tail) == -1, (w, hh)
+        assert b"width" in L.slrgpu_last_error() or b"too large" in L.slrgpu_last_error()
+    st = gpu_lib.Settings(8, 8, 1, 1, 0, 0, 0, 0)
+    assert fn(h.value, C.byref(st), C.c_void_p(film.ctypes.data), *tail) == -5   # valid size: the scene state is next
+    assert L.slrgpu_scene_destroy(h.value) == 0
+
+
 def test_host_build_of_empty_scene(gpu_lib):
     from slr_gb300.scene_desc import SceneDesc
     s = gpu_lib.Scene(SceneDesc(), host_only=True)
