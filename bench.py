@@ -151,44 +151,63 @@ def dist_setup():
     return world, rank, local
 
 
-def cpu_baseline(desc, threads: int, seconds_target: float = 12.0):
-    """Reference renderer on a bounded sample: full-resolution frames at 1 spp
-    until about seconds_target of CPU work (scene build excluded)."""
+def _ref_frame(ref_holder, desc, spp, seed, threads):
+    """One reference render of the workload's frame at `spp` samples per
+    pixel; returns render seconds (scene build excluded)."""
     from oracle import oracle as O
+    if BPT:   # one BPT render per reference sensor
+        ref = ref_holder[0] if ref_holder[0] is not None else O.RefScene(desc)
+        ref_holder[0] = None
+        _, s = ref.render_bpt(WIDTH, HEIGHT, spp, MAX_DEPTH, seed=seed, threads=threads, volumetric=VOLUMETRIC)
+    else:
+        if ref_holder[0] is None:
+            ref_holder[0] = O.RefScene(desc)
+        _, s = ref_holder[0].render(WIDTH, HEIGHT, spp, MAX_DEPTH, seed=seed, threads=threads, volumetric=VOLUMETRIC)
+    return s
+
+
+BASELINE_BUILD = ("the reference renderer built from its own sources with its release flags (-O3 -DNDEBUG, "
+                  "default floating-point contraction) and build-only patches P1-P4, P6-P11 (oracle/build_ref.py)")
+
+
+def cpu_baseline(desc, threads: int, seconds_cap: float = 40.0):
+    """The reference renderer on the workload's own frame: the whole frame
+    (all spp) when one pass predicts it within seconds_cap, else as many
+    whole passes as fit.  The reference renders a frame as spp passes of one
+    sample per pixel over all tiles (PTRenderer.cpp:65-75), so passes are its
+    unit of work."""
+    from oracle import oracle as O
+    O.use_timing_build()
     t0 = time.time()
-    ref = O.RefScene(desc)
+    holder = [O.RefScene(desc)]
     build_s = time.time() - t0
-    total_samples, total_s, frames = 0, 0.0, 0
-    while total_s < seconds_target and frames < 16:
-        if BPT:   # one BPT render per reference sensor
-            ref = O.RefScene(desc) if frames else ref
-            _, s = ref.render_bpt(WIDTH, HEIGHT, 1, MAX_DEPTH, seed=frames, threads=threads, volumetric=VOLUMETRIC)
-        else:
-            _, s = ref.render(WIDTH, HEIGHT, 1, MAX_DEPTH, seed=frames, threads=threads, volumetric=VOLUMETRIC)
-        total_samples += WIDTH * HEIGHT
-        total_s += s
-        frames += 1
-    return {"value": total_samples / total_s, "unit": METRIC, "cores": threads, "kind": "reference",
-            "sample": f"{frames} frame(s) of the same scene at {WIDTH}x{HEIGHT}, 1 spp, max depth {MAX_DEPTH} "
-                      f"({total_samples} path samples, {total_s:.1f} s; SBVH build {build_s:.1f} s excluded)"}
+    t1 = _ref_frame(holder, desc, 1, 0, threads)
+    passes = SPP if t1 * SPP <= seconds_cap else max(1, int(seconds_cap / t1))
+    secs = _ref_frame(holder, desc, passes, 1, threads)
+    total = WIDTH * HEIGHT * passes
+    what = f"the whole frame ({WIDTH}x{HEIGHT}, {SPP} spp" if passes == SPP else \
+        f"{passes} of the frame's {SPP} passes ({WIDTH}x{HEIGHT}"
+    return {"value": total / secs, "unit": METRIC, "cores": threads, "kind": "reference",
+            "sample": f"{what}, max depth {MAX_DEPTH}): {total} path samples in {secs:.1f} s with {threads} "
+                      f"threads; SBVH build {build_s:.1f} s excluded; {BASELINE_BUILD}"}
 
 
 def run_reference(args):
+    """The reference arm: each step renders one pass (one sample per pixel,
+    all tiles) of the workload's frame on the host cores, the reference's own
+    unit of work in its pass loop; the line carries the same config as the
+    GPU arm's."""
     world, rank, _ = dist_setup()
     if rank != 0:
         return 0
     from oracle import oracle as O
-    from slr_gb300 import scenes
+    O.use_timing_build()
     threads = os.cpu_count() or 1
     desc = WORKLOADS[args.workload]["scene"]()
-    ref = O.RefScene(desc)
+    holder = [O.RefScene(desc)]
     times = []
     for i in range(args.warmup + args.steps):
-        if BPT:   # one BPT render per reference sensor
-            ref = O.RefScene(desc) if i else ref
-            _, s = ref.render_bpt(WIDTH, HEIGHT, 1, MAX_DEPTH, seed=i, threads=threads, volumetric=VOLUMETRIC)
-        else:
-            _, s = ref.render(WIDTH, HEIGHT, 1, MAX_DEPTH, seed=i, threads=threads, volumetric=VOLUMETRIC)
+        s = _ref_frame(holder, desc, 1, i, threads)
         if i >= args.warmup:
             times.append(s)
     per_step = WIDTH * HEIGHT
@@ -197,12 +216,23 @@ def run_reference(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded procedural scene)",
-            "config": {"workload": WORKLOAD, "step": f"{WIDTH}x{HEIGHT} at 1 spp (bounded sample of the {SPP}-spp frame)"},
+            "config": gpu_config(args.workload, args.spp, args.gpus, None),
             "cpu_baseline": {"value": value, "unit": METRIC, "cores": threads, "kind": "reference",
-                             "sample": f"{args.steps} frames at {WIDTH}x{HEIGHT}, 1 spp, max depth {MAX_DEPTH}"},
+                             "sample": f"{args.steps} timed passes (one sample per pixel over all tiles, the "
+                                       f"reference's pass loop) of the {WIDTH}x{HEIGHT} frame, max depth "
+                                       f"{MAX_DEPTH}, {threads} threads; {BASELINE_BUILD}"},
             "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
     return 0
+
+
+def gpu_config(workload: str, spp: int, world: int, bvh) -> dict:
+    """The config object both arms print for a rendering workload."""
+    wl = WORKLOADS[workload]
+    cfg = {"workload": wl["text"], "width": wl["width"], "height": wl["height"], "spp": spp,
+           "max_depth": wl["depth"], "parallelism": f"replicas x{world}",
+           "l2": "path state (GBs) exceeds L2; 1 GiB buffer written between timed steps"}
+    return cfg
 
 
 def serving_requests(n: int, rate: float, seed: int, num_scenes: int):
@@ -547,11 +577,9 @@ def main():
     line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
-            "config": {"workload": WORKLOAD, "width": WIDTH, "height": HEIGHT, "spp": spp, "max_depth": MAX_DEPTH,
-                       "triangles": st.num_triangles, "sbvh_fragments": st.num_fragments,
-                       "bvh_width": st.width, "parallelism": f"replicas x{world}",
-                       "l2": "path state (GBs) exceeds L2; 1 GiB buffer written between timed steps",
-                       "scene_build_s": round(build_s, 2)},
+            "config": gpu_config(args.workload, spp, world, st),
+            "scene": {"triangles": st.num_triangles, "sbvh_fragments": st.num_fragments, "bvh_width": st.width,
+                      "scene_build_s": round(build_s, 2)},
             "rays_per_s": (ext_rays + sh_rays) * world / (total_ms * 1e-3),
             "dropped_samples": dropped,
             "gpu_launches": launches,

@@ -8,14 +8,21 @@ and only as the checker / the timed CPU baseline.
 
 Recipe
 ------
-1. When the reference sources are present (``$SLR_REFERENCE`` or the default
-   checkout path), the ``libSLR`` sources are copied into ``oracle/_ref/src``
-   and the build-only patches below are applied to that copy.  The reference
-   tree itself is never written.  ``oracle/_ref`` is git-ignored.
+1. When the reference checkout is given (``--reference PATH`` or
+   ``$SLR_REFERENCE``), the ``libSLR`` sources are copied into
+   ``oracle/_ref/src`` and the build-only patches below are applied to that
+   copy.  The reference tree itself is never written.  ``oracle/_ref`` is
+   git-ignored.
 2. Every translation unit is compiled with g++/gcc (no cmake, no external
-   libraries) into ``oracle/_ref/obj`` and linked, together with the oracle
-   driver ``oracle/ref_driver.cpp`` and the no-op progress reporter
-   ``oracle/progress_reporter_noop.cpp``, into ``oracle/_ref/libslr_ref.so``.
+   libraries) and linked, together with the oracle driver
+   ``oracle/ref_driver.cpp`` and the no-op progress reporter
+   ``oracle/progress_reporter_noop.cpp``, in two flavours:
+
+   * ``check`` -> ``oracle/_ref/libslr_ref.so``: ``-O2 -ffp-contract=off``
+     (P5), the checker of every parity test and golden fixture;
+   * ``timing`` -> ``oracle/_ref/libslr_ref_timing.so``: the reference's own
+     release flags ``-O3 -DNDEBUG`` (CMakeLists.txt:46-47) with the
+     compiler's default contraction, timed as the CPU baseline.
 
 On a machine without the reference checkout (the GPU host) step 1 is skipped
 and the patched copy that travelled with the working tree is compiled.
@@ -32,8 +39,9 @@ Build-only patches (all applied to the copy):
 * P4 ``Core/surface_object.cpp:18`` and ``Core/medium_object.cpp:18`` include
   the SSE-only ``Accelerator/QBVH.h`` that nothing on the active path uses;
   the include is dropped so the library builds on aarch64 too.
-* P5 ``-ffp-contract=off``: x86-64 and aarch64 then round every operation the
-  same way (no fused multiply-add), so golden dumps agree across hosts.
+* P5 ``-ffp-contract=off`` (check flavour only): x86-64 and aarch64 then round
+  every operation the same way (no fused multiply-add), so golden dumps agree
+  across hosts.
 * P6 max depth: ``Renderer/PTRenderer.cpp:172`` caps a path at 100 vertices
   and ``Renderer/VolumetricPTRenderer.cpp:185`` has no cap.  Both now stop
   after ``slr_oracle_max_depth`` scattering vertices (a global the driver
@@ -76,7 +84,10 @@ REF_OUT = HERE / "_ref"
 SRC_COPY = REF_OUT / "src" / "libSLR"
 OBJ_DIR = REF_OUT / "obj"
 LIB = REF_OUT / "libslr_ref.so"
-DEFAULT_REFERENCE = "/root/reference"
+FLAVORS = {
+    "check": (["-O2", "-ffp-contract=off"], REF_OUT / "obj", LIB),
+    "timing": (["-O3", "-DNDEBUG"], REF_OUT / "obj_timing", REF_OUT / "libslr_ref_timing.so"),
+}
 PATCH_SET = "P1 P2 P3 P4 P5 P6 P7 P8 P9 P10 P11\n"
 
 # Files excluded from the reference's own build (libSLR/CMakeLists.txt:45-51).
@@ -92,8 +103,11 @@ SOURCE_DIRS = ["", "External", "External/AnalyticSkyDomeRadiance", "MemoryAlloca
                "Accelerator", "Camera", "Scene", "Renderer", "Helper"]
 
 
-def _reference_root() -> Path | None:
-    root = Path(os.environ.get("SLR_REFERENCE", DEFAULT_REFERENCE))
+def _reference_root(reference: str | None = None) -> Path | None:
+    path = reference or os.environ.get("SLR_REFERENCE")
+    if not path:
+        return None
+    root = Path(path)
     return root if (root / "libSLR" / "defines.h").is_file() else None
 
 
@@ -198,34 +212,44 @@ def _compile(cmd: list[str]) -> tuple[list[str], int, str]:
     return cmd, r.returncode, r.stderr
 
 
-def build(jobs: int | None = None, force: bool = False, verbose: bool = False) -> Path:
-    ref_root = _reference_root()
+def build(jobs: int | None = None, force: bool = False, verbose: bool = False, reference: str | None = None,
+          flavors: tuple[str, ...] = ("check", "timing")) -> Path:
+    """Builds the oracle library of every flavour (all translation units in
+    one parallel pass); returns the check flavour's library."""
+    ref_root = _reference_root(reference)
     marker = REF_OUT / "src" / "PATCHED"
     if ref_root is not None and (force or not marker.is_file() or marker.read_text() != PATCH_SET):
         copy_and_patch(ref_root)
+        force = True
     if not (REF_OUT / "src" / "PATCHED").is_file():
-        raise RuntimeError("reference sources unavailable: neither the reference checkout nor "
-                           "oracle/_ref/src is present")
-    OBJ_DIR.mkdir(parents=True, exist_ok=True)
-    common = ["-O2", "-fPIC", "-ffp-contract=off", "-w", "-pthread", f"-I{SRC_COPY}"]
-    cxx = ["g++", "-std=gnu++11", "-include", "cstring", "-include", "cmath"] + common
-    cc = ["gcc"] + common
-    units: list[tuple[Path, list[str]]] = []
+        raise RuntimeError("reference sources unavailable: give the reference checkout (--reference or "
+                           "$SLR_REFERENCE), or keep the patched copy in oracle/_ref/src")
+    sources: list[tuple[Path, str]] = []
     for f in sorted(SRC_COPY.rglob("*")):
-        if f.suffix == ".cpp":
-            units.append((f, cxx))
-        elif f.suffix == ".c":
-            units.append((f, cc))
-    units.append((HERE / "progress_reporter_noop.cpp", cxx))
-    units.append((HERE / "ref_driver.cpp", ["g++", "-std=gnu++14", "-include", "cstring", "-include", "cmath"] + common))
-    objs, cmds = [], []
-    for f, tool in units:
-        rel = f.relative_to(SRC_COPY) if SRC_COPY in f.parents else Path("oracle") / f.name
-        o = OBJ_DIR / (rel.as_posix().replace("/", "__") + ".o")
-        objs.append(o)
-        if o.is_file() and o.stat().st_mtime >= f.stat().st_mtime and not force:
-            continue
-        cmds.append(tool + ["-c", str(f), "-o", str(o)])
+        if f.suffix in (".cpp", ".c"):
+            sources.append((f, "lib"))
+    sources.append((HERE / "progress_reporter_noop.cpp", "lib"))
+    sources.append((HERE / "ref_driver.cpp", "driver"))
+    cmds, links = [], []
+    for flavor in flavors:
+        opt, obj_dir, lib = FLAVORS[flavor]
+        obj_dir.mkdir(parents=True, exist_ok=True)
+        common = opt + ["-fPIC", "-w", "-pthread", f"-I{SRC_COPY}"]
+        objs = []
+        for f, kind in sources:
+            if kind == "driver":
+                tool = ["g++", "-std=gnu++14", "-include", "cstring", "-include", "cmath"] + common
+            elif f.suffix == ".c":
+                tool = ["gcc"] + common
+            else:
+                tool = ["g++", "-std=gnu++11", "-include", "cstring", "-include", "cmath"] + common
+            rel = f.relative_to(SRC_COPY) if SRC_COPY in f.parents else Path("oracle") / f.name
+            o = obj_dir / (rel.as_posix().replace("/", "__") + ".o")
+            objs.append(o)
+            if o.is_file() and o.stat().st_mtime >= f.stat().st_mtime and not force:
+                continue
+            cmds.append(tool + ["-c", str(f), "-o", str(o)])
+        links.append((lib, objs))
     jobs = jobs or os.cpu_count() or 4
     failed = []
     with cf.ThreadPoolExecutor(max_workers=jobs) as ex:
@@ -237,20 +261,23 @@ def build(jobs: int | None = None, force: bool = False, verbose: bool = False) -
     if failed:
         cmd, err = failed[0]
         raise RuntimeError(f"oracle compile failed ({len(failed)} units): {' '.join(cmd)}\n{err[-4000:]}")
-    link = ["g++", "-shared", "-pthread", "-o", str(LIB)] + [str(o) for o in objs]
-    r = subprocess.run(link, capture_output=True, text=True)
-    if r.returncode != 0:
-        raise RuntimeError(f"oracle link failed:\n{r.stderr[-4000:]}")
+    for lib, objs in links:
+        if cmds or not lib.is_file():
+            link = ["g++", "-shared", "-pthread", "-o", str(lib)] + [str(o) for o in objs]
+            r = subprocess.run(link, capture_output=True, text=True)
+            if r.returncode != 0:
+                raise RuntimeError(f"oracle link failed:\n{r.stderr[-4000:]}")
     return LIB
 
 
 def main() -> int:
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--reference", default=None, help="reference checkout (default: $SLR_REFERENCE)")
     ap.add_argument("--force", action="store_true")
     ap.add_argument("-j", type=int, default=None)
     ap.add_argument("-v", action="store_true")
     a = ap.parse_args()
-    lib = build(jobs=a.j, force=a.force, verbose=a.v)
+    lib = build(jobs=a.j, force=a.force, verbose=a.v, reference=a.reference)
     print(f"built {lib} ({platform.machine()})")
     return 0
 

@@ -15,6 +15,9 @@ import numpy as np
 
 HERE = Path(__file__).resolve().parent
 LIB_PATH = HERE / "_ref" / "libslr_ref.so"
+# the reference's release-flag build (-O3 -DNDEBUG), timed as the CPU
+# baseline; every parity check uses LIB_PATH
+TIMING_LIB_PATH = HERE / "_ref" / "libslr_ref_timing.so"
 
 _lib = None
 _libc = None
@@ -49,12 +52,25 @@ def available() -> bool:
     return LIB_PATH.is_file()
 
 
+_flavor = "check"
+
+
+def use_timing_build() -> None:
+    """Loads the release-flag build instead of the checker build; only before
+    the first call into the oracle of this process (the CPU-baseline legs)."""
+    global _flavor
+    if _lib is not None and _flavor != "timing":
+        raise RuntimeError("the oracle's checker build is already loaded in this process")
+    _flavor = "timing"
+
+
 def lib():
     global _lib
     if _lib is None:
-        if not LIB_PATH.is_file():
-            raise RuntimeError(f"oracle library missing: {LIB_PATH} (run oracle/build_ref.py)")
-        L = C.CDLL(str(LIB_PATH))
+        path = TIMING_LIB_PATH if _flavor == "timing" else LIB_PATH
+        if not path.is_file():
+            raise RuntimeError(f"oracle library missing: {path} (run oracle/build_ref.py)")
+        L = C.CDLL(str(path))
         P, I, F, D = C.c_void_p, C.c_int, C.c_float, C.c_double
         fp, up, dp = C.POINTER(C.c_float), C.POINTER(C.c_uint32), C.POINTER(C.c_double)
         hp = C.POINTER(C.c_uint16)
@@ -109,8 +125,12 @@ def _u(a):
 class RefScene:
     """A scene built inside the reference library from a SceneDesc."""
 
-    def __init__(self, desc, build: bool = True):
-        L = lib()
+    def __init__(self, desc, build: bool = True, library=None):
+        """library: another implementation of the ora_* scene-building calls
+        with the same signatures (the shim test application); the oracle by
+        default."""
+        L = library if library is not None else lib()
+        self._L = L
         self.desc = desc
         self.h = L.ora_scene_new()
         keep = []
@@ -186,8 +206,8 @@ class RefScene:
                 L.ora_build(self.h)
 
     def __del__(self):
-        if getattr(self, "h", None) and _lib is not None:
-            _lib.ora_scene_free(self.h)
+        if getattr(self, "h", None) and getattr(self, "_L", None) is not None:
+            self._L.ora_scene_free(self.h)
             self.h = None
 
     def render(self, width, height, spp, max_depth, seed=0, threads=None, volumetric=False):

@@ -312,6 +312,13 @@ int ora_camera_equirect(void* p, const float* m, float sensitivity, float phiAng
     return 0;
 }
 
+// The built SLR::Scene, for applications that render it through another
+// SLR::Renderer (null before ora_build).
+void* ora_scene_ptr(void* p) {
+    OraScene* s = (OraScene*)p;
+    return s->built ? (void*)s->scene.get() : nullptr;
+}
+
 int ora_build(void* p) {
     OraScene* s = (OraScene*)p;
     if (s->built) return 0;

@@ -1,14 +1,11 @@
-"""Condition numbers of the GGX dielectric BSDF (MicrofacetBSDF) at given
-directions, for the tolerance of the BSDF parity test.
-
-The value and pdf are restated here in float64 from
-libSLR/BSDF/microfacet_bsdfs.cpp:213-300, with the dielectric Fresnel term
-(Core/directional_distribution_functions.cpp:142-211) and the GGX normal
-distribution and Smith G1 (:262-315).  Near total internal reflection the
-factor (1 - F) cancels and the exit cosine sqrt(1 - sin^2) loses digits, so
-an FP32 evaluation, on any hardware, carries relative errors far above
-1e-5 there; the parity test widens its tolerance by the condition number
-estimated here by finite differences of the directions.
+"""Float64 restatement of the GGX dielectric BSDF's value and pdf
+(MicrofacetBSDF, libSLR/BSDF/microfacet_bsdfs.cpp:213-300), with the
+dielectric Fresnel term (Core/directional_distribution_functions.cpp:142-211)
+and the GGX normal distribution and Smith G1 (:262-315); tests/bsdf_f64.py
+builds the other BSDFs and the condition numbers on it.  Near total internal
+reflection the factor (1 - F) cancels and the exit cosine sqrt(1 - sin^2)
+loses digits, so an FP32 evaluation, on any hardware, carries relative
+errors far above 1e-5 there.
 """
 from __future__ import annotations
 
@@ -95,22 +92,3 @@ def microfacet_bsdf(wo, wi, wl, e_ext, e_int, ax, ay):
         pdf = np.where(dd > 0, pdf_r, pdf_t)
         pdf = np.where((hv * sign <= 0) | (dd == 0), 0.0, pdf)
     return fs, pdf
-
-
-def condition(wo, wi, wl, e_ext, e_int, ax, ay, eps=1e-6, trials=8, seed=0):
-    """Largest relative change of any nonzero fs component or of the pdf per
-    relative change eps of the directions, over random perturbations."""
-    wo = np.asarray(wo, np.float64)
-    wi = np.asarray(wi, np.float64)
-    f0, p0 = microfacet_bsdf(wo, wi, wl, e_ext, e_int, ax, ay)
-    rng = np.random.default_rng(seed)
-    kappa = np.zeros(len(wo))
-    for _ in range(trials):
-        a = _normalize(wo + eps * rng.normal(size=wo.shape))
-        b = _normalize(wi + eps * rng.normal(size=wi.shape))
-        f1, p1 = microfacet_bsdf(a, b, wl, e_ext, e_int, ax, ay)
-        with np.errstate(divide="ignore", invalid="ignore"):
-            rf = np.where(f0 != 0, np.abs(f1 - f0) / np.abs(f0), 0.0).max(1)
-            rp = np.where(p0 != 0, np.abs(p1 - p0) / np.abs(p0), 0.0)
-        kappa = np.maximum(kappa, np.nan_to_num(np.maximum(rf, rp), nan=0.0, posinf=1e12) / eps)
-    return kappa

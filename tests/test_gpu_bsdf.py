@@ -1,37 +1,37 @@
 """BSDF parity on the GPU: sampled value, sampled direction, pdf, evaluated
 value and evaluated pdf agree with the reference's BSDFs at the same
-(query, sample) inputs within 1e-5 relative (FP32).
+(query, sample) inputs within 1e-5 (FP32; directions absolute, values and
+pdfs relative), on every query.
 
-Tolerances: directions are unit vectors, so they are compared component-wise
-with an absolute 1e-5.  Values and pdfs are compared relative to the
-reference value with a floor of 1e-6 of the case's largest magnitude; for
-queries whose result is ill-conditioned (the shading-normal correction
-|d.z / dot(d, n_g)| with |dot(d, n_g)| < 1e-2, or |d.z| < 1e-3, where a
-1-ulp change of the direction moves the value by more than 1e-5) the
-relative tolerance is 1e-5 times the condition factor."""
+Where FP32 itself cannot resolve an output to 1e-5 (grazing shading-normal
+corrections, near-grazing visible-normal sampling, dielectric microfacet
+values near total internal reflection), two FP32 implementations of the same
+formula differ by up to the output's condition number times their rounding.
+The tolerance then grows to 1e-5 + kappa * 16 * 2^-24, with kappa computed in
+float64 from the query alone (tests/bsdf_f64.py: finite differences of a
+float64 restatement of the reference's BSDFs, itself pinned against the
+reference's outputs in test_cpu_parity.py), never from the GPU's result.
+Sampling succeeds on exactly the same queries, with the same sampled
+direction types.  The delta BSDFs (specular reflection and refraction) need
+no widening.  Each case prints the share of queries strictly within 1e-5."""
 import os
 
 import numpy as np
 import pytest
 
+from tests import bsdf_f64
 from tests.bsdf_cases import bsdf_cases
-from tests.bsdf_conditioning import condition
 
 pytestmark = pytest.mark.gpu
 GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
-RTOL = 1e-5
+TOL = 1e-5
+ROUNDING = 16 * 2.0 ** -24
 
 
-def _cond(dirs, gn):
-    """Condition factor of the shading-normal correction for each direction."""
-    dg = np.abs((dirs * gn).sum(1))
-    dz = np.abs(dirs[:, 2])
-    return np.maximum(1.0, np.maximum(1e-2 / np.maximum(dg, 1e-12), 1e-3 / np.maximum(dz, 1e-12)))
-
-
-def _rel_ok(a, b, scale, cond):
-    tol = RTOL * cond[:, None] if a.ndim == 2 else RTOL * cond
-    return np.abs(a - b) <= tol * np.maximum(np.abs(b), 1e-6 * scale)
+def _rel(a, b):
+    with np.errstate(divide="ignore", invalid="ignore"):
+        r = np.abs(a - b) / np.abs(b)
+    return np.where((a == 0) & (b == 0), 0.0, np.nan_to_num(r, nan=np.inf))
 
 
 @pytest.mark.parametrize("case", bsdf_cases(), ids=lambda c: c["name"])
@@ -43,39 +43,22 @@ def test_bsdf_matches_reference(gpu_lib, case):
                      case.get("ay", 0.0), q)
     ok_ref = ref[:, 19] > 0
     ok_gpu = out[:, 19] > 0
-    # sampling succeeds on the same queries
-    assert (ok_ref != ok_gpu).sum() <= max(1, len(ref) // 500), (ok_ref != ok_gpu).sum()
-    both = ok_ref & ok_gpu
-    assert both.sum() > 0.5 * len(ref)
-    r, g, qb = ref[both], out[both], q[both]
-    assert np.array_equal(r[:, 20], g[:, 20]), "sampled direction types differ"
-    dir_err = np.abs(g[:, 16:19] - r[:, 16:19]).max(1)
-    cond_s = _cond(r[:, 16:19].astype(np.float64), qb[:, 3:6].astype(np.float64))
-    assert (dir_err <= 1e-5 * cond_s).mean() > 0.999, np.sort(dir_err)[-5:]
-    # A sampled value or pdf is evaluated at the sampled direction, so a
-    # direction that differs by |dd| moves it, to first order, by
-    # |dd| (1/|d.z| + 1/|dot(d, n_g)| + 1) relative (shading-normal correction,
-    # cosine and microfacet terms); the tolerance adds that amount.
-    rd = r[:, 16:19].astype(np.float64)
-    sens = 1.0 / np.maximum(np.abs(rd[:, 2]), 1e-12) + 1.0 / np.maximum(np.abs((rd * qb[:, 3:6]).sum(1)), 1e-12) + 1.0
-    cond_v = np.maximum(cond_s, 1.0 + 10.0 * dir_err * sens / RTOL)
-    cond_e = _cond(q[:, 11:14].astype(np.float64), q[:, 3:6].astype(np.float64))
-    if case["kind"] == "ggx_bsdf":
-        # Near total internal reflection the dielectric microfacet value and
-        # pdf are ill-conditioned in FP32 (1 - F cancels): widen by the
-        # condition number per unit relative change of the directions, times
-        # FP32 input rounding (6e-8) and a factor 100 for the rounding of the
-        # ~50 operations in between.
-        args = (case["spec0"], case["spec1"], case["ax"], case["ay"])
-        k_s = condition(qb[:, 0:3], rd, qb[:, 6].astype(int), *args)
-        k_e = condition(q[:, 0:3], q[:, 11:14], q[:, 6].astype(int), *args)
-        cond_v = np.maximum(cond_v, 6e-6 * k_s / RTOL)
-        cond_e = np.maximum(cond_e, 6e-6 * k_e / RTOL)
-    fs_ok = _rel_ok(g[:, 0:16], r[:, 0:16], np.abs(r[:, 0:16]).max() + 1e-30, cond_v).all(1)
-    pdf_ok = _rel_ok(g[:, 19], r[:, 19], np.abs(r[:, 19]).max(), cond_v)
-    ev_ok = _rel_ok(out[:, 21:37], ref[:, 21:37], np.abs(ref[:, 21:37]).max() + 1e-30, cond_e).all(1)
-    epdf_ok = _rel_ok(out[:, 37], ref[:, 37], np.abs(ref[:, 37]).max() + 1e-30, cond_e)
-    bad = {k: int((~v).sum()) for k, v in (("fs", fs_ok), ("pdf", pdf_ok), ("eval", ev_ok), ("eval_pdf", epdf_ok))}
-    # allow at most 0.1% of queries outside the tolerance (sampling near a
-    # branch boundary such as total internal reflection)
-    assert all(v <= max(1, len(ref) // 1000) for v in bad.values()), bad
+    np.testing.assert_array_equal(ok_gpu, ok_ref, err_msg="sampling succeeds on different queries")
+    assert ok_ref.sum() > 0.5 * len(ref)
+    np.testing.assert_array_equal(out[ok_ref, 20], ref[ok_ref, 20], err_msg="sampled direction types differ")
+    if case["kind"] in bsdf_f64.KINDS_RESTATED:
+        k_dir, k_s, k_e = bsdf_f64.conditions(case["kind"], case["spec0"], case.get("spec1", case["spec0"]),
+                                              case.get("ax", 0.0), case.get("ay", 0.0), q)
+    else:
+        k_dir = k_s = k_e = np.ones(len(q))
+    b = ok_ref
+    d_err = np.abs(out[b, 16:19] - ref[b, 16:19]).max(1)
+    s_err = np.maximum(_rel(out[b, 0:16], ref[b, 0:16]).max(1), _rel(out[b, 19], ref[b, 19]))
+    e_err = np.maximum(_rel(out[:, 21:37], ref[:, 21:37]).max(1), _rel(out[:, 37], ref[:, 37]))
+    within = {"direction": float(np.mean(d_err <= TOL)), "sampled": float(np.mean(s_err <= TOL)),
+              "evaluated": float(np.mean(e_err <= TOL))}
+    print(case["name"], "share strictly within 1e-5:", within)
+    bad = {"direction": np.nonzero(d_err > TOL + k_dir[b] * ROUNDING)[0],
+           "sampled": np.nonzero(s_err > TOL + k_s[b] * ROUNDING)[0],
+           "evaluated": np.nonzero(e_err > TOL + k_e * ROUNDING)[0]}
+    assert all(len(v) == 0 for v in bad.values()), {k: v[:5].tolist() for k, v in bad.items()}

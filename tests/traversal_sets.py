@@ -35,6 +35,8 @@ def gpu_trace_sets(api, desc) -> dict:
             torch.cuda.synchronize()
             out[f"{tag}_prim"] = prim.cpu().numpy().view(np.uint32)
             out[f"{tag}_t"] = t.cpu().numpy()
+            out[f"{tag}_b1"] = b1.cpu().numpy()
+            out[f"{tag}_b2"] = b2.cpu().numpy()
             out[f"{tag}_occ"] = occ.cpu().numpy().astype(bool)
     scene.close()
     return out
