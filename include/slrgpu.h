@@ -44,6 +44,7 @@ extern "C" {
 #define SLRGPU_ERR_STATE            (-6)
 #define SLRGPU_ERR_TIMEOUT          (-7)
 #define SLRGPU_ERR_UNSUPPORTED      (-8)   /* a valid request this build does not implement */
+#define SLRGPU_ERR_CANCELLED        (-9)   /* a server request cancelled by slrgpu_server_cancel */
 
 typedef uint64_t slrgpu_handle;
 
@@ -241,7 +242,14 @@ uint64_t slrgpu_render_noalloc_scratch_bytes(void);
  * slrgpu_render.  A request's film is bit-identical in both modes and to
  * slrgpu_render with the same settings: its random numbers depend only on
  * (seed, sample, pixel) and its samples are accumulated in order.  A scene
- * cannot be destroyed while it has unfinished requests. */
+ * cannot be destroyed while it has unfinished requests.
+ *
+ * The HBM budget covers everything the server holds on the device for its
+ * requests: its path-state slots (charged at creation; creation fails if
+ * they alone exceed it), each resident scene an admitted request renders
+ * (charged once while any of its admitted requests is alive) and the
+ * admitted requests' films (released by slrgpu_server_wait).  A request
+ * whose film and scene can never fit is refused at submission. */
 #define SLRGPU_SERVER_PLAIN 0u
 #define SLRGPU_SERVER_BATCHED 1u
 
@@ -254,7 +262,7 @@ typedef struct slrgpu_server_config {
     uint32_t slots;             /* path-state slots = waves in flight; 0: 4 (plain: 1) */
     uint32_t paths_per_slot;    /* 0: 4 Mi paths (about 2 GB per slot) */
     uint32_t max_depth;         /* largest max_depth accepted; 0: 64 */
-    uint64_t hbm_budget_bytes;  /* device bytes for admitted requests' films; 0: 150 GB */
+    uint64_t hbm_budget_bytes;  /* device bytes for slots, scenes and films (above); 0: 150 GB */
 } slrgpu_server_config;
 
 typedef struct slrgpu_request_info {
@@ -272,7 +280,7 @@ typedef struct slrgpu_server_stats {
     uint64_t path_samples_done;
     uint64_t waves;
     uint64_t kernel_launches;
-    uint64_t bytes_in_use;      /* films of admitted requests */
+    uint64_t bytes_in_use;      /* charged to the budget: slots, scenes, admitted films */
     uint32_t queued, active;
     double first_start_seconds;
     double last_done_seconds;
@@ -291,6 +299,27 @@ int slrgpu_server_poll(slrgpu_handle server, uint64_t request, slrgpu_request_in
 int slrgpu_server_wait(slrgpu_handle server, uint64_t request, float* film, slrgpu_request_info* info,
                        double timeout_seconds);
 int slrgpu_server_get_stats(slrgpu_handle server, slrgpu_server_stats* stats);
+/* Cancels a queued or running request (no counterpart in the reference): a
+ * queued request ends at once, a running one gets no more samples and ends
+ * when its waves on the GPU finish; its status becomes SLRGPU_ERR_CANCELLED
+ * and slrgpu_server_wait returns that code and releases it.  A request that
+ * has finished, or whose film is already being converted, is left alone
+ * (SLRGPU_ERR_STATE). */
+int slrgpu_server_cancel(slrgpu_handle server, uint64_t request);
+/* Sets a deadline, seconds from now: a request not finished by then is
+ * cancelled by the server with status SLRGPU_ERR_TIMEOUT (checked at least
+ * every 50 ms). */
+int slrgpu_server_set_deadline(slrgpu_handle server, uint64_t request, double seconds);
+
+/* Host-side fault injection for tests of the serving loop (no counterpart
+ * in the reference): the next `count` film allocations
+ * (SLRGPU_FAULT_SERVER_FILM_ALLOC) or wave launches
+ * (SLRGPU_FAULT_SERVER_WAVE_LAUNCH) of any server in the process fail as if
+ * the CUDA call had failed; nothing is injected on the GPU.  count 0 clears
+ * the site. */
+#define SLRGPU_FAULT_SERVER_FILM_ALLOC 0
+#define SLRGPU_FAULT_SERVER_WAVE_LAUNCH 1
+int slrgpu_debug_inject_fault(int site, uint32_t count);
 
 /* Film output --------------------------------------------------------- *
  * ImageSensor::saveImage (libSLR/Core/ImageSensor.cpp:139-195) on the GPU: the

@@ -38,7 +38,15 @@ _lib = None
 
 
 class SlrGpuError(RuntimeError):
-    pass
+    """A negative status of the C ABI; ``code`` holds it."""
+
+    def __init__(self, msg: str, code: int = 0):
+        super().__init__(msg)
+        self.code = code
+
+
+ERR_TIMEOUT, ERR_CANCELLED = -7, -9
+FAULT_SERVER_FILM_ALLOC, FAULT_SERVER_WAVE_LAUNCH = 0, 1
 
 
 class BvhStats(C.Structure):
@@ -153,6 +161,9 @@ def lib():
             "slrgpu_server_poll": (I, [H, C.c_uint64, C.POINTER(RequestInfo)]),
             "slrgpu_server_wait": (I, [H, C.c_uint64, fp, C.POINTER(RequestInfo), C.c_double]),
             "slrgpu_server_get_stats": (I, [H, C.POINTER(ServerStats)]),
+            "slrgpu_server_cancel": (I, [H, C.c_uint64]),
+            "slrgpu_server_set_deadline": (I, [H, C.c_uint64, C.c_double]),
+            "slrgpu_debug_inject_fault": (I, [I, U]),
             "slrgpu_film_to_bmp": (I, [fp, U, U, I, F, F, C.POINTER(C.c_uint8), C.c_char_p]),
             "slrgpu_film_cmf": (I, [fp, fp]),
             "slrgpu_scene_alias_tables": (I, [H, up, fp, up, fp, up, fp, up]),
@@ -167,7 +178,14 @@ def lib():
 
 def check(rc: int) -> None:
     if rc != 0:
-        raise SlrGpuError(f"slrgpu error {rc}: {lib().slrgpu_last_error().decode()}")
+        raise SlrGpuError(f"slrgpu error {rc}: {lib().slrgpu_last_error().decode()}", rc)
+
+
+def inject_fault(site: int, count: int) -> None:
+    """Host-side fault injection (slrgpu_debug_inject_fault): the next
+    `count` film allocations (FAULT_SERVER_FILM_ALLOC) or wave launches
+    (FAULT_SERVER_WAVE_LAUNCH) of any server fail; 0 clears the site."""
+    check(lib().slrgpu_debug_inject_fault(site, count))
 
 
 def _fp(a):
@@ -489,11 +507,23 @@ class Server:
         return info
 
     def wait(self, request: int, timeout: float = -1.0):
-        h, w = self._shapes.pop(request)
+        """Returns (film, RequestInfo); raises SlrGpuError with the request's
+        status (e.g. ERR_CANCELLED, or ERR_TIMEOUT when `timeout` passes
+        first, in which case the request stays queued or running)."""
+        h, w = self._shapes[request]
         film = np.zeros((h, w, 16), np.float32)
         info = RequestInfo()
-        check(lib().slrgpu_server_wait(self.handle, request, _fp(film), C.byref(info), float(timeout)))
+        rc = lib().slrgpu_server_wait(self.handle, request, _fp(film), C.byref(info), float(timeout))
+        if rc != ERR_TIMEOUT:
+            self._shapes.pop(request, None)
+        check(rc)
         return film, info
+
+    def cancel(self, request: int) -> None:
+        check(lib().slrgpu_server_cancel(self.handle, request))
+
+    def set_deadline(self, request: int, seconds: float) -> None:
+        check(lib().slrgpu_server_set_deadline(self.handle, request, float(seconds)))
 
     def stats(self) -> ServerStats:
         st = ServerStats()

@@ -287,6 +287,11 @@ int slrgpu_scene_add_mesh(slrgpu_handle scene, const float* positions, const flo
     if (!validMaterial(s, material)) return fail(SLRGPU_ERR_INVALID_ARGUMENT, "invalid material id");
     for (uint64_t i = 0; i < 3ull * nt; ++i)
         if (indices[i] >= nv) return fail(SLRGPU_ERR_INVALID_ARGUMENT, "vertex index out of range");
+    // a corrupted mesh (NaN or infinite positions) would poison the BVH's
+    // bounds for every ray of the scene; the reference does not check
+    for (uint64_t i = 0; i < 3ull * nv; ++i)
+        if (!std::isfinite(positions[i]))
+            return fail(SLRGPU_ERR_INVALID_ARGUMENT, "vertex positions must be finite");
     uint64_t total = 0;
     for (const HostMesh &m : s->host.meshes) total += m.idx.size() / 3;
     if (total + nt >= (1ull << 26)) return fail(SLRGPU_ERR_INVALID_ARGUMENT, "too many triangles (limit 2^26)");
@@ -551,6 +556,20 @@ int slrgpu_server_get_stats(slrgpu_handle server, slrgpu_server_stats* stats) {
     rec->server->stats(stats);
     return SLRGPU_OK;
 }
+
+int slrgpu_server_cancel(slrgpu_handle server, uint64_t request) {
+    ServerRec* rec = findServer(server);
+    if (!rec) return fail(SLRGPU_ERR_INVALID_HANDLE, "invalid server handle");
+    return rec->server->cancel(request);
+}
+
+int slrgpu_server_set_deadline(slrgpu_handle server, uint64_t request, double seconds) {
+    ServerRec* rec = findServer(server);
+    if (!rec) return fail(SLRGPU_ERR_INVALID_HANDLE, "invalid server handle");
+    return rec->server->setDeadline(request, seconds);
+}
+
+int slrgpu_debug_inject_fault(int site, uint32_t count) { return injectFault(site, count); }
 
 // ---- film output ---------------------------------------------------------------
 int slrgpu_film_to_bmp(const float* film, uint32_t width, uint32_t height, int film_on_device, float scale,

@@ -1296,6 +1296,9 @@ int RenderEngine::ensure(uint32_t N, uint32_t maxDepth) {
     ws = w;
     capacity = N;
     depthCapacity = maxDepth;
+    stateBytes = (uint64_t)N * (2 * 16 + 16 + 2 * 4 * kNumLambda + sizeof(PathScalars) + 2 * 16 + 4 * kNumLambda +
+                                3 * 4 + 4 * kNumClassQueues) +
+                 4ull * kCtrStride * (maxDepth + 2) + 4 * sizeof(unsigned long long);
     return SLRGPU_OK;
 fail:
     delete w;
@@ -1330,6 +1333,7 @@ void RenderEngine::release() {
     ws = nullptr;
     capacity = 0;
     depthCapacity = 0;
+    stateBytes = 0;
     if (filmSum) { cudaFree(filmSum); filmSum = nullptr; }
     if (filmComp) { cudaFree(filmComp); filmComp = nullptr; }
     if (filmOut) { cudaFree(filmOut); filmOut = nullptr; }
@@ -1953,6 +1957,8 @@ WaveSlot* waveSlotCreate(uint32_t paths, uint32_t maxDepth, std::string* err) {
 void waveSlotDestroy(WaveSlot* slot) { delete slot; }
 
 uint32_t waveSlotCapacity(const WaveSlot* slot) { return slot->engine.capacity; }
+
+uint64_t waveSlotBytes(const WaveSlot* slot) { return slot->engine.stateBytes + sizeof(WaveParams); }
 
 uint32_t sampleGridPositions(uint32_t width, uint32_t height) { return padToTile(width) * padToTile(height); }
 

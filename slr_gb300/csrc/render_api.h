@@ -28,6 +28,14 @@ struct DeviceScene {
     uint64_t uid = 0;        // unique per upload (keys captured wave graphs)
 };
 
+// Device bytes a committed scene holds (BVH, triangles, vertices, materials,
+// spectra, environment and medium tables).
+inline uint64_t deviceSceneBytes(const DeviceScene &ds) {
+    uint64_t b = 0;
+    for (size_t n : ds.buffers.sizes) b += n;
+    return b;
+}
+
 struct WaveState;
 struct BptEngine;   // bidirectional path state (bpt.cu)
 
@@ -38,6 +46,7 @@ struct RenderEngine {
     std::vector<void*> allocs;
     uint32_t capacity = 0;
     uint32_t depthCapacity = 0;
+    uint64_t stateBytes = 0;     // device bytes of the path state (ws)
     float* filmSum = nullptr;
     float* filmComp = nullptr;
     float* filmOut = nullptr;
@@ -75,6 +84,7 @@ struct SegmentDesc {
 WaveSlot* waveSlotCreate(uint32_t paths, uint32_t maxDepth, std::string* err);
 void waveSlotDestroy(WaveSlot* slot);
 uint32_t waveSlotCapacity(const WaveSlot* slot);
+uint64_t waveSlotBytes(const WaveSlot* slot);   // device bytes the slot holds
 uint32_t sampleGridPositions(uint32_t width, uint32_t height);
 // Largest image side any entry point accepts; checkImageSize() also bounds
 // the tile-padded grid to 2^31 - 1 positions (sets the error text).

@@ -14,7 +14,27 @@ constexpr uint64_t kDefaultBudget = 150ull << 30;
 constexpr int kMaxSegmentsPerWave = 32;
 
 uint64_t filmBytes(uint32_t pixels) { return 3ull * pixels * 16 * sizeof(float); }
+
+// Host-side fault injection (slrgpu_debug_inject_fault): the next n film
+// allocations or wave launches of any server fail as if the CUDA call had.
+std::atomic<uint32_t> g_faultFilmAlloc{0}, g_faultWaveLaunch{0};
+bool takeFault(std::atomic<uint32_t> &counter) {
+    uint32_t v = counter.load();
+    while (v > 0)
+        if (counter.compare_exchange_weak(v, v - 1)) return true;
+    return false;
+}
 }  // namespace
+
+int injectFault(int site, uint32_t count) {
+    switch (site) {
+    case SLRGPU_FAULT_SERVER_FILM_ALLOC: g_faultFilmAlloc.store(count); return SLRGPU_OK;
+    case SLRGPU_FAULT_SERVER_WAVE_LAUNCH: g_faultWaveLaunch.store(count); return SLRGPU_OK;
+    default:
+        setError("unknown fault site");
+        return SLRGPU_ERR_INVALID_ARGUMENT;
+    }
+}
 
 Server::Server(int device, const slrgpu_server_config &cfg) : device_(device), cfg_(cfg) {
     if (cfg_.mode != SLRGPU_SERVER_PLAIN) cfg_.mode = SLRGPU_SERVER_BATCHED;
@@ -44,12 +64,18 @@ int Server::init() {
             setError("server: " + err);
             return SLRGPU_ERR_OUT_OF_MEMORY;
         }
+        slotBytes_ += waveSlotBytes(sl.wave);
+        if (slotBytes_ > cfg_.hbm_budget_bytes) {
+            setError("server: the path-state slots alone exceed the HBM budget");
+            return SLRGPU_ERR_INVALID_ARGUMENT;
+        }
         if (cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking) != cudaSuccess ||
             cudaEventCreateWithFlags(&sl.event, cudaEventDisableTiming) != cudaSuccess) {
             setError("server: stream or event creation failed");
             return SLRGPU_ERR_CUDA;
         }
     }
+    usedBytes_ = slotBytes_;
     thread_ = std::thread(&Server::worker, this);
     return SLRGPU_OK;
 }
@@ -100,8 +126,8 @@ int Server::submit(const DeviceScene* ds, std::atomic<int>* pin, const slrgpu_se
         return SLRGPU_ERR_INVALID_ARGUMENT;
     }
     const uint64_t pixels = (uint64_t)s.width * s.height;
-    if (filmBytes((uint32_t)pixels) > cfg_.hbm_budget_bytes) {
-        setError("the request's film exceeds the server's HBM budget");
+    if (slotBytes_ + deviceSceneBytes(*ds) + filmBytes((uint32_t)pixels) > cfg_.hbm_budget_bytes) {
+        setError("the request's film and scene, with the path-state slots, exceed the server's HBM budget");
         return SLRGPU_ERR_INVALID_ARGUMENT;
     }
     std::unique_ptr<Request> r(new Request());
@@ -171,7 +197,7 @@ int Server::wait(uint64_t id, float* filmHost, slrgpu_request_info* info, double
         }
         owned = std::move(it->second);
         requests_.erase(it);
-        if (owned->admitted) usedBytes_ -= owned->footprint;
+        releaseBudgetLocked(owned.get());
     }
     cvWork_.notify_all();   // budget freed
     Request* r = owned.get();
@@ -192,6 +218,119 @@ int Server::wait(uint64_t id, float* filmHost, slrgpu_request_info* info, double
     }
     releaseBuffers(r);
     return rc;
+}
+
+// Gives back the request's film bytes and, with its scene's last admitted
+// request, the scene's bytes.  Holds mu_.
+void Server::releaseBudgetLocked(Request* r) {
+    if (!r->admitted) return;
+    r->admitted = false;
+    usedBytes_ -= r->footprint;
+    auto it = sceneCharge_.find(r->ds);
+    if (it != sceneCharge_.end() && --it->second.first == 0) {
+        usedBytes_ -= it->second.second;
+        sceneCharge_.erase(it);
+    }
+}
+
+// True while a wave holding samples of the request is on the GPU.  Holds mu_.
+bool Server::inFlightLocked(const Request* r) const {
+    for (const Slot &sl : slots_)
+        if (sl.busy)
+            for (const auto &pr : sl.segments)
+                if (pr.first == r) return true;
+    return false;
+}
+
+// Ends a request with a final status.  Holds mu_.
+void Server::retireLocked(Request* r, int status, const std::string &why) {
+    r->status = status;
+    r->error = why;
+    r->tDone = now();
+    if (r->pin) r->pin->fetch_sub(1);
+    r->pin = nullptr;
+    active_.erase(std::remove(active_.begin(), active_.end(), r), active_.end());
+    cvDone_.notify_all();
+}
+
+// Cancels a queued or running request: a queued one ends now, a running one
+// stops getting samples and ends when its waves in flight finish.  A request
+// whose film is already being converted is left to finish.  Holds mu_.
+int Server::cancelLocked(Request* r, int status, const std::string &why) {
+    if (r->status == SLRGPU_REQUEST_DONE || r->status < 0 || r->finishing || r->cancelled) {
+        setError("the request has already finished or is finishing");
+        return SLRGPU_ERR_STATE;
+    }
+    auto q = std::find(pending_.begin(), pending_.end(), r);
+    if (q != pending_.end()) {
+        pending_.erase(q);
+        retireLocked(r, status, why);
+        return SLRGPU_OK;
+    }
+    r->cancelled = true;
+    r->cancelStatus = status;
+    r->error = why;
+    if (!inFlightLocked(r)) retireLocked(r, status, why);
+    return SLRGPU_OK;
+}
+
+void Server::retireCancelledLocked() {
+    for (size_t i = 0; i < active_.size();) {
+        Request* r = active_[i];
+        if (r->cancelled && !inFlightLocked(r)) {
+            retireLocked(r, r->cancelStatus, r->error);   // removes it from active_
+            continue;
+        }
+        ++i;
+    }
+}
+
+void Server::expireDeadlinesLocked() {
+    const double t = now();
+    std::vector<Request*> late;
+    for (Request* r : pending_)
+        if (r->deadline >= 0 && t > r->deadline) late.push_back(r);
+    for (Request* r : active_)
+        if (r->deadline >= 0 && t > r->deadline && !r->finishing && !r->cancelled) late.push_back(r);
+    for (Request* r : late) cancelLocked(r, SLRGPU_ERR_TIMEOUT, "deadline exceeded");
+}
+
+int Server::cancel(uint64_t id) {
+    int rc;
+    {
+        std::lock_guard<std::mutex> lock(mu_);
+        auto it = requests_.find(id);
+        if (it == requests_.end()) {
+            setError("unknown request");
+            return SLRGPU_ERR_INVALID_HANDLE;
+        }
+        rc = cancelLocked(it->second.get(), SLRGPU_ERR_CANCELLED, "cancelled");
+    }
+    cvWork_.notify_all();
+    return rc;
+}
+
+int Server::setDeadline(uint64_t id, double secondsFromNow) {
+    if (!(secondsFromNow >= 0)) {
+        setError("the deadline must be a non-negative number of seconds");
+        return SLRGPU_ERR_INVALID_ARGUMENT;
+    }
+    {
+        std::lock_guard<std::mutex> lock(mu_);
+        auto it = requests_.find(id);
+        if (it == requests_.end()) {
+            setError("unknown request");
+            return SLRGPU_ERR_INVALID_HANDLE;
+        }
+        Request* r = it->second.get();
+        if (r->status == SLRGPU_REQUEST_DONE || r->status < 0) {
+            setError("the request has already finished");
+            return SLRGPU_ERR_STATE;
+        }
+        r->deadline = now() + secondsFromNow;
+    }
+    cvWork_.notify_all();
+    return SLRGPU_OK;
 }
 
 void Server::stats(slrgpu_server_stats* st) {
@@ -222,12 +361,8 @@ void Server::releaseBuffers(Request* r) {
 }
 
 void Server::failRequest(Request* r, const std::string &why) {
-    r->status = SLRGPU_ERR_CUDA;
-    r->error = why;
-    r->tDone = now();
-    if (r->pin) r->pin->fetch_sub(1);
-    r->pin = nullptr;
-    active_.erase(std::remove(active_.begin(), active_.end(), r), active_.end());
+    if (r->status == SLRGPU_REQUEST_DONE || r->status < 0) return;
+    retireLocked(r, SLRGPU_ERR_CUDA, why);
 }
 
 // Moves queued requests into the active set, oldest first, while their films
@@ -236,7 +371,9 @@ void Server::admitLocked() {
     while (!pending_.empty()) {
         if (cfg_.mode == SLRGPU_SERVER_PLAIN && !active_.empty()) return;
         Request* r = pending_.front();
-        if (usedBytes_ + r->footprint > cfg_.hbm_budget_bytes) return;
+        auto charged = sceneCharge_.find(r->ds);
+        const uint64_t sceneBytes = charged == sceneCharge_.end() ? deviceSceneBytes(*r->ds) : 0;
+        if (usedBytes_ + r->footprint + sceneBytes > cfg_.hbm_budget_bytes) return;
         size_t freeB = 0, totalB = 0;
         if (cudaMemGetInfo(&freeB, &totalB) == cudaSuccess && freeB < r->footprint + (256ull << 20)) return;
         pending_.pop_front();
@@ -244,7 +381,8 @@ void Server::admitLocked() {
         // other requests' waves run.
         const size_t planes = (size_t)r->pixels * 16 * sizeof(float);
         cudaStream_t st = allocStream_;
-        bool ok = cudaMallocAsync((void**)&r->filmSum, planes, st) == cudaSuccess &&
+        bool ok = !takeFault(g_faultFilmAlloc) &&
+                  cudaMallocAsync((void**)&r->filmSum, planes, st) == cudaSuccess &&
                   cudaMallocAsync((void**)&r->filmComp, planes, st) == cudaSuccess &&
                   cudaMallocAsync((void**)&r->filmOut, planes, st) == cudaSuccess &&
                   cudaMallocAsync((void**)&r->dropped, sizeof(unsigned long long), st) == cudaSuccess &&
@@ -253,7 +391,9 @@ void Server::admitLocked() {
                   cudaMemsetAsync(r->filmComp, 0, planes, st) == cudaSuccess &&
                   cudaMemsetAsync(r->dropped, 0, sizeof(unsigned long long), st) == cudaSuccess &&
                   cudaStreamSynchronize(st) == cudaSuccess;
-        usedBytes_ += r->footprint;
+        usedBytes_ += r->footprint + sceneBytes;
+        if (charged == sceneCharge_.end()) sceneCharge_[r->ds] = {1, sceneBytes};
+        else ++charged->second.first;
         r->admitted = true;
         if (!ok) {
             r->status = SLRGPU_ERR_OUT_OF_MEMORY;
@@ -281,7 +421,7 @@ bool Server::launchWaves() {
         // wave's scene, integrator and depth
         Request* lead = nullptr;
         for (Request* r : active_)
-            if (r->samplesIssued < r->settings.spp) {
+            if (r->samplesIssued < r->settings.spp && !r->cancelled) {
                 bool taken = false;   // its scene already runs in another slot this round
                 for (const Slot &o : slots_)
                     if (o.busy && o.ds == r->ds) taken = true;
@@ -296,7 +436,7 @@ bool Server::launchWaves() {
         uint64_t paths = 0;
         for (Request* r : active_) {
             if ((int)segs.size() == kMaxSegmentsPerWave) break;
-            if (r->samplesIssued >= r->settings.spp) continue;
+            if (r->samplesIssued >= r->settings.spp || r->cancelled) continue;
             if (r->ds != lead->ds || r->settings.volumetric != lead->settings.volumetric ||
                 r->settings.max_depth != lead->settings.max_depth ||
                 (r->settings.flags & SLRGPU_FLAG_WATERTIGHT) != (lead->settings.flags & SLRGPU_FLAG_WATERTIGHT))
@@ -322,7 +462,11 @@ bool Server::launchWaves() {
         }
         if (segs.empty()) break;
         uint64_t n = 0;
-        int rc = launchWave(*lead->ds, sl.wave, segs.data(), (int)segs.size(), lead->settings.max_depth,
+        int rc = SLRGPU_ERR_CUDA;
+        if (takeFault(g_faultWaveLaunch))
+            setError("injected wave launch failure");
+        else
+            rc = launchWave(*lead->ds, sl.wave, segs.data(), (int)segs.size(), lead->settings.max_depth,
                             lead->settings.volumetric != 0, (lead->settings.flags & SLRGPU_FLAG_WATERTIGHT) != 0,
                             sl.stream, &n, cfg_.mode == SLRGPU_SERVER_BATCHED);
         if (rc != SLRGPU_OK) {
@@ -362,7 +506,7 @@ bool Server::reapSlots(bool block) {
         for (auto &pr : sl.segments) {
             Request* r = pr.first;
             r->samplesDone = std::max(r->samplesDone, pr.second);
-            if (r->samplesDone == r->settings.spp && !r->finishing) {
+            if (r->samplesDone == r->settings.spp && !r->finishing && !r->cancelled && r->status >= 0) {
                 r->finishing = true;
                 launchFilmToPixelMajor(r->filmSum, r->filmOut, r->pixels, sl.stream);
                 cudaMemcpyAsync(&r->droppedHost, r->dropped, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
@@ -402,9 +546,11 @@ void Server::worker() {
     std::unique_lock<std::mutex> lock(mu_);
     while (true) {
         if (stop_) break;
+        expireDeadlinesLocked();
         admitLocked();
         bool launched = launchWaves();
         reapSlots(false);
+        retireCancelledLocked();
         reapFinishing();
         bool busy = false;
         for (const Slot &sl : slots_) busy |= sl.busy;

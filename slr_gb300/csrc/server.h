@@ -11,6 +11,13 @@
 // numbers depend only on (seed, sample, pixel) and its film accumulates its
 // samples in order, so its film is bit-identical in either mode and to
 // slrgpu_render.
+//
+// The HBM budget covers everything the server keeps on the device for its
+// requests: the path-state slots (charged at creation), each resident scene
+// that an admitted request renders (charged once, while any of its admitted
+// requests is alive) and the admitted requests' films.  A request can be
+// cancelled, or given a deadline after which the server cancels it; either
+// stops issuing its samples, and it ends once its waves in flight finish.
 #pragma once
 #include <cuda_runtime.h>
 
@@ -30,6 +37,9 @@
 
 namespace slrgpu {
 
+// slrgpu_debug_inject_fault's sites (host side only).
+int injectFault(int site, uint32_t count);
+
 class Server {
 public:
     Server(int device, const slrgpu_server_config &cfg);
@@ -40,6 +50,8 @@ public:
     int submit(const DeviceScene* ds, std::atomic<int>* pin, const slrgpu_settings &s, uint64_t* id);
     int poll(uint64_t id, slrgpu_request_info* info);
     int wait(uint64_t id, float* filmHost, slrgpu_request_info* info, double timeoutSeconds);
+    int cancel(uint64_t id);
+    int setDeadline(uint64_t id, double secondsFromNow);
     void stats(slrgpu_server_stats* st);
 
 private:
@@ -60,6 +72,9 @@ private:
         unsigned long long droppedHost = 0;
         bool finishing = false;
         bool admitted = false;    // its footprint counts against the budget
+        bool cancelled = false;   // no more samples are issued
+        int cancelStatus = 0;     // the status it ends with once its waves finish
+        double deadline = -1;     // server time after which it is cancelled (< 0: none)
         cudaEvent_t doneEvent = nullptr;
         std::string error;
     };
@@ -80,6 +95,12 @@ private:
     bool reapSlots(bool block);  // returns true when a slot finished
     void reapFinishing();
     void failRequest(Request* r, const std::string &why);
+    void retireLocked(Request* r, int status, const std::string &why);
+    int cancelLocked(Request* r, int status, const std::string &why);
+    bool inFlightLocked(const Request* r) const;
+    void retireCancelledLocked();
+    void expireDeadlinesLocked();
+    void releaseBudgetLocked(Request* r);
     void releaseBuffers(Request* r);
 
     int device_;
@@ -93,7 +114,10 @@ private:
     std::vector<Slot> slots_;
     cudaStream_t allocStream_ = nullptr;   // film allocation, clearing and release
     uint64_t nextId_ = 1;
-    uint64_t usedBytes_ = 0;
+    uint64_t usedBytes_ = 0;      // slots + charged scenes + admitted films
+    uint64_t slotBytes_ = 0;
+    // resident scenes charged to the budget: admitted requests alive, bytes
+    std::unordered_map<const DeviceScene*, std::pair<int, uint64_t>> sceneCharge_;
     bool stop_ = false;
     std::thread thread_;
     // statistics

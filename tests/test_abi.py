@@ -91,3 +91,13 @@ def test_density_grid_file_round_trip(tmp_path, gpu_lib):
     assert b"malformed" in L.slrgpu_last_error()
     assert L.slrgpu_medium_density_grid_file(h.value, path.encode(), fp(lo), fp(hi), sid.value, sid.value, 0.3) == 0
     assert L.slrgpu_scene_destroy(h.value) == 0
+
+
+def test_fault_injection_sites(gpu_lib):
+    """The host-side fault-injection hook takes the two server sites and
+    refuses others (no device work: the counters are armed and cleared)."""
+    L = gpu_lib.lib()
+    assert L.slrgpu_debug_inject_fault(7, 1) == -1
+    for site in (gpu_lib.FAULT_SERVER_FILM_ALLOC, gpu_lib.FAULT_SERVER_WAVE_LAUNCH):
+        assert L.slrgpu_debug_inject_fault(site, 2) == 0
+        assert L.slrgpu_debug_inject_fault(site, 0) == 0

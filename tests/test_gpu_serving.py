@@ -108,11 +108,16 @@ def test_requests_arriving_while_others_run(gpu_lib, served_scenes, standalone):
 
 
 def test_admission_respects_the_budget(gpu_lib, served_scenes, standalone):
-    """A budget that holds one film at a time still serves every request,
-    in order, and never has more than one film admitted."""
+    """A budget that holds the path-state slots, the three scenes and one
+    film at a time still serves every request, in order, and what it
+    charges never exceeds the budget."""
     ctx, scs = served_scenes
+    probe = gpu_lib.Server(ctx, mode=gpu_lib.SERVER_BATCHED, paths_per_slot=1 << 16, max_depth=16)
+    slot_bytes = probe.stats().bytes_in_use
+    probe.close()
+    scene_bytes = sum(sc.reupload() for sc in scs)
     biggest = max(w * h for _, w, h, *_ in REQUESTS)
-    budget = 3 * biggest * 16 * 4              # sum + compensation + output planes of one film
+    budget = slot_bytes + scene_bytes + 3 * biggest * 16 * 4   # sum + compensation + output planes of one film
     srv = gpu_lib.Server(ctx, mode=gpu_lib.SERVER_BATCHED, paths_per_slot=1 << 16, max_depth=16,
                          hbm_budget_bytes=budget)
     try:
