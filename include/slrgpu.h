@@ -199,6 +199,20 @@ int slrgpu_scene_reupload(slrgpu_handle scene, uint64_t* bytes);
 int slrgpu_render(slrgpu_handle scene, const slrgpu_settings* settings, float* film,
                   int film_on_device, slrgpu_render_stats* stats);
 
+/* Checkpointed rendering (no counterpart in the reference, whose renderer
+ * runs all passes in one call): renders samples [sample_base, sample_base +
+ * spp) and adds them, in sample order, to the compensated film sums held in
+ * film_state (host memory, 2 x 16 x width x height floats: the sum planes
+ * [bin][pixel], then the compensation planes; all zeros for a fresh film),
+ * updated in place.  film (host, optional) receives the film
+ * (width*height*16 floats, the layout of slrgpu_render).  A film rendered
+ * over consecutive sample ranges, the state saved and restored between the
+ * calls, equals the one-call film bit for bit: the ranges are additive and
+ * a sample's random numbers depend only on (seed, sample, pixel).  Path
+ * tracers only (SLRGPU_FLAG_BPT: SLRGPU_ERR_UNSUPPORTED). */
+int slrgpu_render_continue(slrgpu_handle scene, const slrgpu_settings* settings, float* film_state, float* film,
+                           slrgpu_render_stats* stats);
+
 /* Render that allocates nothing.  It has no counterpart in the reference.
  *
  * For callers that cannot call cudaMalloc while they run: a real-time loop

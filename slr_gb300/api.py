@@ -146,6 +146,7 @@ def lib():
             "slrgpu_scene_commit": (I, [H, C.POINTER(BvhStats)]),
             "slrgpu_scene_build_host": (I, [H, C.POINTER(BvhStats)]),
             "slrgpu_render": (I, [H, C.POINTER(Settings), P, I, C.POINTER(RenderStats)]),
+            "slrgpu_render_continue": (I, [H, C.POINTER(Settings), fp, fp, C.POINTER(RenderStats)]),
             "slrgpu_trace": (I, [H, P, U, I, P, P, P, P, P]),
             "slrgpu_scene_sbvh_dump": (I, [H, fp, up, up]),
             "slrgpu_spectrum_evaluate": (I, [H, I, fp, U, fp]),
@@ -377,6 +378,21 @@ class Scene:
         check(lib().slrgpu_render(self.handle, C.byref(s), C.c_void_p(ptr), on_device, C.byref(st)))
         return film, st
 
+    def render_continue(self, state: "FilmCheckpoint", spp: int, flags: int = 0):
+        """Renders the next `spp` samples of a checkpointed film
+        (slrgpu_render_continue) and advances the checkpoint; returns
+        (film, RenderStats).  Rendering a frame over several calls, with the
+        checkpoint saved and loaded in between, gives the one-call film bit
+        for bit."""
+        c = state
+        s = Settings(c.width, c.height, spp, c.max_depth, c.seed, int(c.volumetric), 0, flags, c.next_sample)
+        st = RenderStats()
+        film = np.zeros((c.height, c.width, 16), np.float32)
+        check(lib().slrgpu_render_continue(self.handle, C.byref(s), _fp(c.state), _fp(film), C.byref(st)))
+        c.next_sample += spp
+        c.dropped += st.dropped_samples
+        return film, st
+
     def trace(self, rays_dev, any_hit: bool = False, watertight: bool = False):
         """rays_dev: torch CUDA float32 tensor (n, 8).  Returns torch tensors
         (prim, t, b1, b2) on the same device (any hit: prim only); watertight
@@ -477,6 +493,41 @@ def bsdf_query(kind: str, spec0, spec1=None, spec2=None, ax=0.0, ay=0.0, queries
     out = np.zeros((len(q), 40), np.float32)
     check(lib().slrgpu_bsdf_query(BSDF_KINDS[kind], _fp(s0), _fp(s1), _fp(s2), ax, ay, _fp(q), len(q), _fp(out)))
     return out
+
+
+class FilmCheckpoint:
+    """A resumable render: the settings, the next sample index, the dropped
+    sample count and the compensated film sums (2 x 16 x height x width
+    floats), saved to and loaded from an .npz file."""
+
+    def __init__(self, width: int, height: int, max_depth: int, seed: int = 0, volumetric: bool = False):
+        self.width, self.height, self.max_depth = int(width), int(height), int(max_depth)
+        self.seed, self.volumetric = int(seed), bool(volumetric)
+        self.next_sample = 0
+        self.dropped = 0
+        self.state = np.zeros(2 * 16 * self.width * self.height, np.float32)
+
+    def film(self) -> np.ndarray:
+        """The film (height, width, 16) of the samples rendered so far."""
+        return np.ascontiguousarray(self.state[:16 * self.width * self.height].reshape(16, self.height, self.width)
+                                    .transpose(1, 2, 0))
+
+    def save(self, path: str) -> None:
+        np.savez(path, state=self.state, meta=np.array([self.width, self.height, self.max_depth, self.seed,
+                                                         int(self.volumetric), self.next_sample, self.dropped],
+                                                        np.int64))
+
+    @classmethod
+    def load(cls, path: str) -> "FilmCheckpoint":
+        d = np.load(path)
+        w, h, depth, seed, vol, nxt, dropped = (int(v) for v in d["meta"])
+        c = cls(w, h, depth, seed, bool(vol))
+        c.next_sample, c.dropped = nxt, dropped
+        state = np.ascontiguousarray(d["state"], np.float32)
+        if state.shape != c.state.shape:
+            raise ValueError("checkpoint state does not match its settings")
+        c.state = state
+        return c
 
 
 class Server:

@@ -16,6 +16,7 @@
 #include "render_api.h"
 #include "scene_host.h"
 #include "server.h"
+#include "trace_ranges.h"
 
 namespace slrgpu {
 
@@ -91,6 +92,7 @@ int addMaterial(Scene* s, const DevMaterial &m, int* id) {
 
 int ensureHostBuilt(Scene* s) {
     if (s->hostBuilt) return SLRGPU_OK;
+    TraceRange range("scene build: SBVH, wide BVH, light and environment tables");
     std::string err;
     if (!buildScene(s->host, &s->built, &err)) return fail(SLRGPU_ERR_INVALID_ARGUMENT, err);
     s->hostBuilt = true;
@@ -405,6 +407,7 @@ int slrgpu_scene_commit(slrgpu_handle scene, slrgpu_bvh_stats* stats) {
     if (!s->committed) {
         cudaError_t e = cudaSetDevice(s->ctx->device);
         if (e != cudaSuccess) return fail(SLRGPU_ERR_CUDA, cudaGetErrorString(e));
+        TraceRange range("scene upload");
         rc = uploadScene(s->host, s->built, &s->dev);
         if (rc != SLRGPU_OK) return rc;
         s->committed = true;
@@ -437,6 +440,24 @@ int slrgpu_render(slrgpu_handle scene, const slrgpu_settings* settings, float* f
     cudaError_t e = cudaSetDevice(s->ctx->device);
     if (e != cudaSuccess) return fail(SLRGPU_ERR_CUDA, cudaGetErrorString(e));
     return s->ctx->engine.render(s->dev, *settings, film, film_on_device != 0, stats, 0);
+}
+
+int slrgpu_render_continue(slrgpu_handle scene, const slrgpu_settings* settings, float* film_state, float* film,
+                           slrgpu_render_stats* stats) {
+    const bool mutating = false;
+    GET_SCENE(s, scene);
+    if (!settings || !film_state) return fail(SLRGPU_ERR_INVALID_ARGUMENT, "settings and film_state must not be NULL");
+    if (int rc = checkImageSize(settings->width, settings->height)) return rc;
+    if (settings->flags & SLRGPU_FLAG_BPT)
+        return fail(SLRGPU_ERR_UNSUPPORTED, "continuing a film is supported for the path tracers only");
+    if (!s->committed) return fail(SLRGPU_ERR_NOT_COMMITTED, "scene not committed");
+    if (!s->host.cameraPresent) return fail(SLRGPU_ERR_STATE, "scene has no camera");
+    if (settings->volumetric && !s->host.medium.present)
+        return fail(SLRGPU_ERR_INVALID_ARGUMENT, "volumetric render of a scene without medium");
+    std::lock_guard<std::mutex> lock(s->ctx->mu);
+    cudaError_t e = cudaSetDevice(s->ctx->device);
+    if (e != cudaSuccess) return fail(SLRGPU_ERR_CUDA, cudaGetErrorString(e));
+    return s->ctx->engine.render(s->dev, *settings, film, false, stats, 0, film_state);
 }
 
 int slrgpu_render_noalloc(slrgpu_handle scene, const slrgpu_settings* settings, float* film_device, void* stream) {

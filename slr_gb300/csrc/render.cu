@@ -8,6 +8,7 @@
 // reference's PTRenderer::Job::contribution (libSLR/Renderer/PTRenderer.cpp:146-276)
 // and Job::kernel (:103-144); only the random numbers differ (counter-based).
 #include "render_api.h"
+#include "trace_ranges.h"
 
 #include <algorithm>
 #include <atomic>
@@ -1466,6 +1467,7 @@ static int runWave(const DeviceScene &ds0, const WaveState &w, const WaveParams 
     lm.end();
     ++launches;
     for (uint32_t b = 0; b <= D; ++b) {
+        TraceRange range("bounce %u", b);
         uint32_t* ctr = w.counters + (size_t)kCtrStride * b;
         uint32_t* next = ctr + kCtrStride;
         uint32_t* inQueue = w.queue[b & 1];
@@ -1576,6 +1578,7 @@ static int runWave(const DeviceScene &ds0, const WaveState &w, const WaveParams 
 static int runWaves(const DeviceScene &ds, const slrgpu_settings &s, const WavePlan &pl, const WaveState &w,
                     float* filmSum, float* filmComp, cudaStream_t stream, LaunchMarks &lm, uint64_t* launches) {
     for (uint32_t base = 0; base < s.spp; base += pl.S) {
+        TraceRange range("wave: samples %u..%u", s.sample_base + base, s.sample_base + std::min(s.spp, base + pl.S));
         WaveParams wp;
         std::memset(&wp, 0, sizeof(wp));
         WaveSegment &sg = wp.seg[0];
@@ -1603,8 +1606,9 @@ static int runWaves(const DeviceScene &ds, const slrgpu_settings &s, const WaveP
 }
 
 int RenderEngine::render(const DeviceScene &ds, const slrgpu_settings &s, float* film, bool filmOnDevice,
-                         slrgpu_render_stats* stats, cudaStream_t stream) {
+                         slrgpu_render_stats* stats, cudaStream_t stream, float* filmState) {
     auto t0 = std::chrono::steady_clock::now();
+    TraceRange range("render %ux%u, %u spp, depth %u", s.width, s.height, s.spp, s.max_depth);
     if (s.spp == 0) {
         setError("width, height and spp must be positive");
         return SLRGPU_ERR_INVALID_ARGUMENT;
@@ -1628,10 +1632,23 @@ int RenderEngine::render(const DeviceScene &ds, const slrgpu_settings &s, float*
     } else if (!bpt) {
         bpt = bptEngineCreate();
     }
+    if (filmState && bidir) {
+        setError("continuing a film is supported for the path tracers only");
+        return SLRGPU_ERR_UNSUPPORTED;
+    }
     int rc = ensureFilm(P);
     if (rc != SLRGPU_OK) return rc;
-    CUDA_TRY(cudaMemsetAsync(filmSum, 0, (size_t)P * kNumLambda * sizeof(float), stream));
-    CUDA_TRY(cudaMemsetAsync(filmComp, 0, (size_t)P * kNumLambda * sizeof(float), stream));
+    const size_t planeBytes = (size_t)P * kNumLambda * sizeof(float);
+    if (filmState) {
+        // continue the compensated sums of earlier sample ranges: a film
+        // rendered in consecutive ranges equals the one-call film bit for bit
+        CUDA_TRY(cudaMemcpyAsync(filmSum, filmState, planeBytes, cudaMemcpyHostToDevice, stream));
+        CUDA_TRY(cudaMemcpyAsync(filmComp, filmState + (size_t)P * kNumLambda, planeBytes, cudaMemcpyHostToDevice,
+                                 stream));
+    } else {
+        CUDA_TRY(cudaMemsetAsync(filmSum, 0, planeBytes, stream));
+        CUDA_TRY(cudaMemsetAsync(filmComp, 0, planeBytes, stream));
+    }
     if (!bidir) CUDA_TRY(cudaMemsetAsync(ws->stats, 0, 4 * sizeof(unsigned long long), stream));
     // the render's start and end events, destroyed on every return path
     struct EventPair {
@@ -1660,12 +1677,17 @@ int RenderEngine::render(const DeviceScene &ds, const slrgpu_settings &s, float*
         if (rc != SLRGPU_OK) return rc;
     }
     CUDA_TRY(cudaGetLastError());
-    float* dst = filmOnDevice ? film : filmOut;
+    float* dst = filmOnDevice && film ? film : filmOut;
     kFilmToPixelMajor<<<waveGrids(256).accumulate, 256, 0, stream>>>(filmSum, dst, P);
     ++launches;
     CUDA_TRY(cudaEventRecord(e1, stream));
-    if (!filmOnDevice)
-        CUDA_TRY(cudaMemcpyAsync(film, filmOut, (size_t)P * kNumLambda * sizeof(float), cudaMemcpyDeviceToHost, stream));
+    if (!filmOnDevice && film)
+        CUDA_TRY(cudaMemcpyAsync(film, filmOut, planeBytes, cudaMemcpyDeviceToHost, stream));
+    if (filmState) {
+        CUDA_TRY(cudaMemcpyAsync(filmState, filmSum, planeBytes, cudaMemcpyDeviceToHost, stream));
+        CUDA_TRY(cudaMemcpyAsync(filmState + (size_t)P * kNumLambda, filmComp, planeBytes, cudaMemcpyDeviceToHost,
+                                 stream));
+    }
     unsigned long long hstats[4] = {0, 0, 0, 0};
     if (!bidir) CUDA_TRY(cudaMemcpyAsync(hstats, ws->stats, sizeof(hstats), cudaMemcpyDeviceToHost, stream));
     CUDA_TRY(cudaStreamSynchronize(stream));

@@ -56,8 +56,11 @@ struct RenderEngine {
     int ensure(uint32_t paths, uint32_t maxDepth);
     int ensureFilm(uint32_t pixels);
     void release();
+    // filmState (host, optional): the compensated film sums to continue
+    // from (2 x 16 x width x height floats: sum planes, then compensation
+    // planes), updated in place; film may then be null.
     int render(const DeviceScene &ds, const slrgpu_settings &s, float* film, bool filmOnDevice,
-               slrgpu_render_stats* stats, cudaStream_t stream);
+               slrgpu_render_stats* stats, cudaStream_t stream, float* filmState = nullptr);
     ~RenderEngine();
 };
 

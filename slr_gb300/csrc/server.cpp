@@ -1,5 +1,6 @@
 // Serving loop with continuous batching (see server.h).
 #include "server.h"
+#include "trace_ranges.h"
 
 #include <algorithm>
 #include <chrono>
@@ -377,6 +378,7 @@ void Server::admitLocked() {
         size_t freeB = 0, totalB = 0;
         if (cudaMemGetInfo(&freeB, &totalB) == cudaSuccess && freeB < r->footprint + (256ull << 20)) return;
         pending_.pop_front();
+        TraceRange range("admit request %llu", (unsigned long long)r->id);
         // Stream-ordered allocation: no device-wide synchronisation while
         // other requests' waves run.
         const size_t planes = (size_t)r->pixels * 16 * sizeof(float);
@@ -461,6 +463,7 @@ bool Server::launchWaves() {
             paths += (uint64_t)take * r->gridPositions;
         }
         if (segs.empty()) break;
+        TraceRange range("server wave %llu: %d requests", (unsigned long long)wavesLaunched_, (int)segs.size());
         uint64_t n = 0;
         int rc = SLRGPU_ERR_CUDA;
         if (takeFault(g_faultWaveLaunch))

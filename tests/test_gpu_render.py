@@ -118,3 +118,23 @@ def test_degenerate_scenes(gpu_lib):
     assert np.all(film == 0)
     film, _ = gpu_lib.Scene(scenes.box_scene(1, 1)).render(1, 1, 16, 0, seed=2)
     assert film.shape == (1, 1, 16) and np.isfinite(film).all()
+
+
+@pytest.mark.parametrize("volumetric", [False, True])
+def test_checkpointed_render_equals_one_call(gpu_lib, tmp_path, volumetric):
+    """A frame rendered over sample ranges, its compensated film state saved
+    to a file and loaded back between the calls (slrgpu_render_continue),
+    equals the one-call film bit for bit, with the same dropped count."""
+    desc = scenes.medium_box_scene(24, 16, grid=16) if volumetric else scenes.box_scene(24, 16)
+    s = gpu_lib.Scene(desc)
+    whole, st = s.render(24, 16, 13, 8, seed=21, volumetric=volumetric)
+    ck = gpu_lib.FilmCheckpoint(24, 16, 8, seed=21, volumetric=volumetric)
+    for spp in (5, 1, 7):
+        s.render_continue(ck, spp)
+        path = str(tmp_path / "ck.npz")
+        ck.save(path)
+        ck = gpu_lib.FilmCheckpoint.load(path)
+    assert ck.next_sample == 13 and ck.dropped == st.dropped_samples
+    np.testing.assert_array_equal(ck.film().view(np.uint32), whole.view(np.uint32))
+    with pytest.raises(gpu_lib.SlrGpuError):
+        s.render_continue(ck, 1, flags=gpu_lib.FLAG_BPT)
