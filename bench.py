@@ -226,6 +226,17 @@ def run_reference(args):
     return 0
 
 
+def _sub_bench(argv):
+    """Runs this script with argv in a fresh process; returns its JSON line
+    (or the error)."""
+    r = subprocess.run([sys.executable, os.path.abspath(__file__), *argv, "--no-extras"], capture_output=True,
+                       text=True, timeout=900)
+    for ln in reversed(r.stdout.splitlines()):
+        if ln.startswith("{"):
+            return json.loads(ln)
+    return {"error": f"rc {r.returncode}", "stderr_tail": r.stderr[-2000:]}
+
+
 def gpu_config(workload: str, spp: int, world: int, bvh) -> dict:
     """The config object both arms print for a rendering workload."""
     wl = WORKLOADS[workload]
@@ -442,6 +453,10 @@ def main():
                     choices=["ggx_ibl_1m", "small", "box", "bpt_box", "bpt_volumetric", "bpt_box_small", "volumetric",
                              "volumetric_small", "serving", "traversal"])
     ap.add_argument("--requests", type=int, default=512)
+    ap.add_argument("--cpu-seconds", type=float, default=40.0,
+                    help="cap on the CPU baseline's render time (whole passes of the frame)")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the volumetric and serving sub-benchmarks of the default line")
     args = ap.parse_args()
     if args.workload == "serving":
         return run_serving(args)
@@ -588,7 +603,15 @@ def main():
                     "d2h_bytes_per_step": WIDTH * HEIGHT * 16 * 4, "ms_per_step": e2e_total / len(e2e_ms)},
             "clocks": clk}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(desc, os.cpu_count() or 1)
+        line["cpu_baseline"] = cpu_baseline(desc, os.cpu_count() or 1, args.cpu_seconds)
+    if rank == 0 and world == 1 and args.workload == "ggx_ibl_1m" and not args.no_extras:
+        # the other headline configurations, each measured in a process of
+        # its own after this line's timed region
+        del scene, film_dev, l2_flush
+        torch.cuda.empty_cache()
+        line["volumetric"] = _sub_bench(["--workload", "volumetric", "--steps", "2", "--warmup", "1",
+                                         "--cpu-seconds", "8"])
+        line["serving"] = _sub_bench(["--workload", "serving"])
     if rank == 0:
         print(json.dumps(line))
     if world > 1:

@@ -169,6 +169,9 @@ __device__ __forceinline__ void upsWeights(uint32_t adj, float s, float t, int i
 // quotient.  Checked against IEEE division for every float of [2^-20, 2048]
 // (tests/test_division_by_range.py); the inputs here are wavelength offsets,
 // 0 or at least 2^-15.
+#ifndef SLRGPU_FAST_REGULAR
+#define SLRGPU_FAST_REGULAR 0
+#endif
 __device__ __forceinline__ float divRange(float x) {
     constexpr float z = 1.0f / 470.0f;
     const float q = __fmul_rn(x, z);
@@ -207,9 +210,19 @@ static __device__ __noinline__ void evalSpectrum(const DevScene &sc, int id, con
     } else if (sp.kind == kSpecRegular) {
         const float* v = sc.specValues + sp.offset;
         const float nm1 = (float)(sp.count - 1);
+#if SLRGPU_FAST_REGULAR
+        // over the wavelength range itself the quotient is divRange's, the
+        // correctly rounded one, in three operations instead of a division
+        const bool fullRange = sp.p0 == kWavelengthLow && sp.p1 == kWavelengthHigh;
+#endif
 #pragma unroll
         for (int i = 0; i < kNumLambda; ++i) {
+#if SLRGPU_FAST_REGULAR
+            const float x = __fsub_rn(lambdas[i], sp.p0);
+            float binF = __fmul_rn(fullRange ? divRange(x) : __fdiv_rn(x, __fsub_rn(sp.p1, sp.p0)), nm1);
+#else
             float binF = __fmul_rn(__fdiv_rn(__fsub_rn(lambdas[i], sp.p0), __fsub_rn(sp.p1, sp.p0)), nm1);
+#endif
             float r;
             if (binF <= 0.0f) r = v[0];
             else if (binF >= nm1) r = v[sp.count - 1];

@@ -8,7 +8,8 @@
   primitive id and a bit-identical t for every ray (exact ties at equal t
   classified with the restated triangle test), the same occlusion answer for
   every any-hit query; for the 4-wide and the 8-wide BVH.  The watertight
-  option may differ only within rounding of an edge or vertex.
+  option may differ only next to edges, where the reference's own
+  arithmetic is at its limit (classified below, counts printed).
 * The 256 x 256 box at 16 spp and max depth 8, image parity per pixel and bin.
 * The 256^3 fBm medium (16^3 super voxels) at 48 x 48, 8 spp, max depth 32.
 """
@@ -61,30 +62,37 @@ def _check_sets(desc, gpu, ref):
         # reference's, so t is in fact bit-identical (compare_hits)
         assert np.all(np.abs(gpu[f"{name}_mt_t"][same] - r["t"][same]) <= 1e-6 * np.abs(r["t"][same]))
         np.testing.assert_array_equal(gpu[f"{name}_mt_occ"], r["occ"], err_msg=f"{name} any hit")
-        # watertight option: differences only within rounding of an edge or
-        # vertex (smallest barycentric weight of the reference's hit or of
-        # the watertight hit below 1e-5: Moller-Trumbore can slip through a
-        # shared edge to a triangle behind it), where the reference missed
-        # through a crack, or at ties
+        # Watertight option (robust slab tests and Woop-Benthin-Wald edges,
+        # H1): it differs from the reference only where the reference's
+        # arithmetic is at its limit: (a) the reference's hit lies within
+        # 1e-5 (barycentric) of an edge, so the watertight ray may pass on
+        # the neighbour's side; (b) the watertight walk finds a closer
+        # surface, or one where the reference found none, within 1e-4 of an
+        # edge of that triangle: grazing rays whose non-robust slab or edge
+        # tests leaked past it in the reference (and in the default walk,
+        # which rounds like the reference); (c) exact ties.
         wp, wt = gpu[f"{name}_wt_prim"], gpu[f"{name}_wt_t"]
         diff = np.nonzero(wp != r["prim"])[0]
         wmin = np.minimum(np.minimum(r["b1"], r["b2"]), 1 - r["b1"] - r["b2"])
         wb1, wb2 = gpu[f"{name}_wt_b1"], gpu[f"{name}_wt_b2"]
         wtmin = np.minimum(np.minimum(wb1, wb2), 1 - wb1 - wb2)
-        margin = np.where(r["prim"] != MISS, wmin, np.inf)
-        margin = np.minimum(margin, np.where(wp != MISS, wtmin, np.inf))
-        near_edge = margin[diff] < 1e-5
-        crack = r["prim"][diff] == MISS
-        tie = (wp[diff] != MISS) & (r["prim"][diff] != MISS) & (np.abs(wt[diff] - r["t"][diff])
-                                                                  <= 1e-6 * np.abs(r["t"][diff]))
-        unexplained = diff[~(near_edge | crack | tie)]
-        assert len(unexplained) == 0, (name, len(diff), unexplained[:10], margin[unexplained[:10]],
-                                       r["prim"][unexplained[:10]], wp[unexplained[:10]])
+        ref_hit, wt_hit = r["prim"][diff] != MISS, wp[diff] != MISS
+        near_edge = ref_hit & (wmin[diff] < 1e-5)
+        closer = wt_hit & (~ref_hit | (wt[diff] < r["t"][diff]))
+        leak_closed = closer & (wtmin[diff] < 1e-4)
+        tie = wt_hit & ref_hit & (np.abs(wt[diff] - r["t"][diff]) <= 1e-6 * np.abs(r["t"][diff]))
+        unexplained = diff[~(near_edge | leak_closed | tie)]
+        assert len(unexplained) == 0, (name, len(diff), unexplained[:10], wmin[unexplained[:10]],
+                                       wtmin[unexplained[:10]], r["t"][unexplained[:10]], wt[unexplained[:10]])
         occ_diff = int((gpu[f"{name}_wt_occ"] != r["occ"]).sum())
         report[name] = {"hits": res["hits"], "ties": res["ties"], "watertight_id_differences": int(len(diff)),
                         "watertight_rate": len(diff) / len(wp),
-                        "watertight_max_edge_margin": float(margin[diff][near_edge].max()) if near_edge.any() else 0.0,
-                        "watertight_cracks_closed": int(crack.sum()), "watertight_anyhit_differences": occ_diff}
+                        "reference_hit_near_edge": int(near_edge.sum()),
+                        "watertight_closer_hit_near_edge": int((leak_closed & ~near_edge).sum()),
+                        "max_edge_margin": float(np.concatenate([wmin[diff][near_edge],
+                                                                 wtmin[diff][leak_closed]]).max())
+                        if (near_edge | leak_closed).any() else 0.0,
+                        "watertight_anyhit_differences": occ_diff}
         assert len(diff) <= 1e-4 * len(wp) and occ_diff <= 1e-4 * len(wp), report[name]
     print(report)
     return report
