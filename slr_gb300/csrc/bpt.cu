@@ -733,7 +733,7 @@ __global__ void __launch_bounds__(256, 2) kBptBounce(DevScene sc, BptState st, c
 // The BSDF of a surface vertex for its connections: Lambert from the
 // reflectance cached at the vertex, other kinds evaluated again.
 __device__ __forceinline__ void vertexBsdf(const DevScene &sc, const BptState &st, size_t vi, uint32_t material,
-                                           uint32_t flags, const float lambdas[kNumLambda], Bsdf &B) {
+                                           uint32_t flags, const float* lambdas, Bsdf &B) {
     if (((flags >> kVfMatShift) & 0xfu) == kMatMatte) {
         B.kind = kMatMatte;
         B.ax = B.ay = 0.0f;

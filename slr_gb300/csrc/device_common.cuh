@@ -180,8 +180,18 @@ __device__ __forceinline__ float divRange(float x) {
 }
 static_assert(kWavelengthHigh - kWavelengthLow == 470.0f, "divRange divides by the wavelength range");
 
+// The 16 wavelengths of a path computed from its offset where they are
+// used (lambdaAt, the same numbers as a stored array), so that no array of
+// them needs registers or local memory; spectrum functions take either this
+// or a plain array (const float*).
+struct OffsetLambdas {
+    float off;
+    __device__ __forceinline__ float operator[](int i) const { return lambdaAt(i, off); }
+};
+
+template <class LAM>
 __device__ __forceinline__ void evalUpsampled(const float* __restrict__ basis, uint32_t adj, float s, float t, float scale,
-                                              const float lambdas[kNumLambda], Spec &out) {
+                                              LAM lambdas, Spec &out) {
     int idx[4]; float w[4]; int n;
     upsWeights(adj, s, t, idx, w, &n);
 #pragma unroll
@@ -203,7 +213,18 @@ __device__ __forceinline__ void evalUpsampled(const float* __restrict__ basis, u
     }
 }
 
-static __device__ __noinline__ void evalSpectrum(const DevScene &sc, int id, const float lambdas[kNumLambda], Spec &out) {
+// Inlined (SLRGPU_INLINE_SPECTRUM 1), the 16 values can stay in registers;
+// out of line, the callers' spectra live in local memory.
+#ifndef SLRGPU_INLINE_SPECTRUM
+#define SLRGPU_INLINE_SPECTRUM 0
+#endif
+template <class LAM>
+#if SLRGPU_INLINE_SPECTRUM
+static __device__ __forceinline__
+#else
+static __device__ __noinline__
+#endif
+void evalSpectrum(const DevScene &sc, int id, LAM lambdas, Spec &out) {
     const DevSpectrum sp = sc.spectra[id];
     if (sp.kind == kSpecUpsampled) {
         evalUpsampled(sc.upsSpectra, sp.adj, sp.p0, sp.p1, sp.scale, lambdas, out);

@@ -97,8 +97,8 @@ __device__ __forceinline__ void toPolarYUp(V3 d, float* theta, float* phi) {
 
 // Emitted radiance of the environment at texture coordinate (tu, tv):
 // (pi * texel * scale) * (1 / pi) (IBLEmitterSurfaceProperty.cpp:16-18, IBLEDF.cpp:18-21).
-__device__ __forceinline__ void envRadiance(const DevScene &sc, float tu, float tv, const float lambdas[kNumLambda],
-                                            Spec &Le) {
+template <class LAM>
+__device__ __forceinline__ void envRadiance(const DevScene &sc, float tu, float tv, LAM lambdas, Spec &Le) {
     float u = fmodf(tu, 1.0f), v = fmodf(tv, 1.0f);
     u += u < 0 ? 1.0f : 0.0f;
     v += v < 0 ? 1.0f : 0.0f;
@@ -159,7 +159,8 @@ __device__ __forceinline__ float envAreaPdf(const DevScene &sc, float phi, float
 // ---------------------------------------------------------------------------
 // Material -> BSDF (SurfaceMaterial::getBSDF)
 // ---------------------------------------------------------------------------
-static __device__ __noinline__ void makeBsdf(const DevScene &sc, const DevMaterial &m, const float lambdas[kNumLambda],
+template <class LAM>
+static __device__ __noinline__ void makeBsdf(const DevScene &sc, const DevMaterial &m, LAM lambdas,
                                       bool wlSelected, Bsdf &B) {
     B.kind = m.kind;
     B.ax = m.alphaX;
@@ -275,8 +276,8 @@ __device__ __forceinline__ int selectLight3(const DevScene &sc, float u, int* li
     return idx;
 }
 
-template <int K>
-__device__ __forceinline__ void makeBsdfK(const DevScene &sc, const DevMaterial &m, const float lambdas[kNumLambda],
+template <int K, class LAM>
+__device__ __forceinline__ void makeBsdfK(const DevScene &sc, const DevMaterial &m, LAM lambdas,
                                           bool wlSelected, Bsdf &B) {
     B.kind = (uint32_t)K;
     B.ax = m.alphaX;

@@ -56,6 +56,11 @@ static_assert(sizeof(PathScalars) == 32, "one sector per path");
 #ifndef SLRGPU_SURF_RECORD
 #define SLRGPU_SURF_RECORD 0
 #endif
+// The surface shading kernels compute their wavelengths from the path's
+// offset where used (1) instead of keeping an array of 16 (0).
+#ifndef SLRGPU_LAMBDA_OFFSET
+#define SLRGPU_LAMBDA_OFFSET 0
+#endif
 constexpr int kSurfRecordWords = SLRGPU_SURF_RECORD == 2 ? 4 : SLRGPU_SURF_RECORD == 1 ? 2 : 0;
 
 struct WaveState {
@@ -308,9 +313,13 @@ __global__ void kShadeMiss(DevScene sc, WaveState ws, const uint32_t* __restrict
         const uint32_t depth = info >> kInfoDepthShift;
         const bool prevDelta = (info & kInfoPrevDelta) != 0;
         const float wlOff = ws.ps[p].wlOffset;
+#if SLRGPU_LAMBDA_OFFSET
+        const OffsetLambdas lambdas{wlOff};
+#else
         float lambdas[kNumLambda];
 #pragma unroll
         for (int k = 0; k < kNumLambda; ++k) lambdas[k] = lambdaAt(k, wlOff);
+#endif
         float4 rd = ws.ray[2 * (size_t)p + 1];
         V3 dir = V3{rd.x, rd.y, rd.z};
         float theta, phi;
@@ -363,9 +372,13 @@ __global__ void __launch_bounds__(256, K == kMatGGXScattering ? SLRGPU_SHADE_DIE
             const bool prevDelta = (info & kInfoPrevDelta) != 0;
             uint32_t depth = info >> kInfoDepthShift;
             const float wlOff = ws.ps[p].wlOffset;
+#if SLRGPU_LAMBDA_OFFSET
+            const OffsetLambdas lambdas{wlOff};
+#else
             float lambdas[kNumLambda];
 #pragma unroll
             for (int k = 0; k < kNumLambda; ++k) lambdas[k] = lambdaAt(k, wlOff);
+#endif
             Rng rng{loadKey(ws, p), ws.ps[p].rngCounter};
             float4 ro = ws.ray[2 * (size_t)p], rd = ws.ray[2 * (size_t)p + 1];
             V3 org = V3{ro.x, ro.y, ro.z}, dir = V3{rd.x, rd.y, rd.z};

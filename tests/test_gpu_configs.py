@@ -43,7 +43,7 @@ def c1_reference(c1_desc, oracle_lib):
     ref = oracle_lib.RefScene(c1_desc, build=False)
     out = {}
     for name, rays in ray_sets(c1_desc).items():
-        r = rays.cpu().numpy()
+        r = np.ascontiguousarray(rays.cpu().numpy())
         prim, t, b1, b2 = ref.trace(r)
         occ, _, _, _ = ref.trace(r, anyhit=True)
         out[name] = {"rays": r, "prim": prim, "t": t, "b1": b1, "b2": b2, "occ": occ}
@@ -98,8 +98,12 @@ def _check_sets(desc, gpu, ref):
     return report
 
 
+def _sets(ref):
+    return {name: r["rays"] for name, r in ref.items()}
+
+
 def test_traversal_parity_on_benchmark_bvh(gpu_lib, c1_desc, c1_reference):
-    gpu = gpu_trace_sets(gpu_lib, c1_desc)
+    gpu = gpu_trace_sets(gpu_lib, c1_desc, _sets(c1_reference))
     assert gpu["bvh_width"] == 4
     _check_sets(c1_desc, gpu, c1_reference)
 
@@ -110,9 +114,11 @@ def test_traversal_parity_on_benchmark_bvh_8_wide(gpu_lib, c1_desc, c1_reference
     from slr_gb300 import build
     if not build.lib_path("w8").is_file():
         build.build(variants=("w8",))
+    rays = tmp_path / "rays.npz"
+    np.savez(rays, **_sets(c1_reference))
     out = tmp_path / "w8.npz"
     env = dict(os.environ, SLRGPU_LIB_VARIANT="w8")
-    r = subprocess.run([sys.executable, "-m", "tests.traversal_sets", str(out)], cwd=ROOT, env=env,
+    r = subprocess.run([sys.executable, "-m", "tests.traversal_sets", str(rays), str(out)], cwd=ROOT, env=env,
                        capture_output=True, text=True, timeout=900)
     assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-4000:]
     gpu = dict(np.load(out))

@@ -132,8 +132,13 @@ def test_budget_counts_slots_scenes_and_films(gpu_lib, box):
         srv.close()
     with pytest.raises(gpu_lib.SlrGpuError):
         _server(gpu_lib, slots=2, hbm_budget_bytes=1 << 20)
-    small = _server(gpu_lib, slots=1, hbm_budget_bytes=(1 << 14) * 512 + scene_bytes + 32 * 32 * 16 * 12)
+    probe = _server(gpu_lib, slots=1)
+    one_slot = probe.stats().bytes_in_use
+    probe.close()
+    small = _server(gpu_lib, slots=1, hbm_budget_bytes=one_slot + scene_bytes + 32 * 32 * 16 * 12)
     try:
+        ok = small.submit(box, 32, 32, 1, 8)                  # a 32x32 film fits exactly
+        small.wait(ok, timeout=60)
         with pytest.raises(gpu_lib.SlrGpuError):
             small.submit(box, 64, 64, 1, 8)                   # its film can never fit the budget
     finally:

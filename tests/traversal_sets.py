@@ -1,9 +1,10 @@
 """GPU side of the traversal parity test on the 1M-triangle benchmark scene.
 
-Run as a script (``python -m tests.traversal_sets OUT.npz``) it traces the
-ray sets with whichever library variant SLRGPU_LIB_VARIANT selects and saves
-the results, so that a test can check the 8-wide BVH build in a process of
-its own."""
+Run as a script (``python -m tests.traversal_sets RAYS.npz OUT.npz``) it
+traces the saved ray sets with whichever library variant SLRGPU_LIB_VARIANT
+selects and saves the results, so that a test can check the 8-wide BVH build
+in a process of its own.  The ray sets are generated once per test session
+(torch's multinomial sampling on the GPU need not repeat bit for bit)."""
 from __future__ import annotations
 
 import sys
@@ -22,12 +23,14 @@ def ray_sets(desc, device="cuda"):
             "incoherent": raysets.incoherent_rays(desc, N_PER_SET, device, seed=0)}
 
 
-def gpu_trace_sets(api, desc) -> dict:
+def gpu_trace_sets(api, desc, sets: dict) -> dict:
+    """Traces the given ray sets ({name: (n, 8) float32 numpy array})."""
     import torch
     scene = api.Scene(desc)
     out = {"bvh_width": scene.bvh_stats.width}
-    for name, rays in ray_sets(desc).items():
-        out[f"{name}_rays"] = rays.cpu().numpy()
+    for name, host_rays in sets.items():
+        rays = torch.from_numpy(np.ascontiguousarray(host_rays)).cuda()
+        out[f"{name}_rays"] = host_rays
         for wt in (False, True):
             tag = f"{name}_{'wt' if wt else 'mt'}"
             prim, t, b1, b2 = scene.trace(rays, watertight=wt)
@@ -42,14 +45,15 @@ def gpu_trace_sets(api, desc) -> dict:
     return out
 
 
-def main(path: str) -> int:
+def main(rays_path: str, out_path: str) -> int:
     import os
     sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
     from slr_gb300 import api, scenes
-    res = gpu_trace_sets(api, scenes.heightfield_scene(seed=0))
-    np.savez(path, **res)
+    sets = dict(np.load(rays_path))
+    res = gpu_trace_sets(api, scenes.heightfield_scene(seed=0), sets)
+    np.savez(out_path, **res)
     return 0
 
 
 if __name__ == "__main__":
-    sys.exit(main(sys.argv[1]))
+    sys.exit(main(sys.argv[1], sys.argv[2]))
