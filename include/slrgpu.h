@@ -199,6 +199,21 @@ int slrgpu_scene_reupload(slrgpu_handle scene, uint64_t* bytes);
 int slrgpu_render(slrgpu_handle scene, const slrgpu_settings* settings, float* film,
                   int film_on_device, slrgpu_render_stats* stats);
 
+/* Path-level replay (diagnostics; no counterpart in the reference): one
+ * sample per pixel of the surface path tracer in which the path of grid
+ * position i (the tile-padded grid, row-major) draws its uniforms from
+ * tapes[256 i .. 256 i + 256) instead of the renderer's own generator (draws
+ * past 256 read 0.5).  Fed with the uniforms a reference path drew (recorded
+ * in the reference's draw order: time, pixel, wavelength, wavelength
+ * selection, lens; per vertex: Russian roulette after the first, light
+ * selection, light position, BSDF), the GPU traces the same path, so films
+ * can be compared path by path.  spp must be 1, sample_base 0, no
+ * volumetric, watertight or bidirectional flag (SLRGPU_ERR_UNSUPPORTED);
+ * max_depth at most 35 keeps a path's draws within its 256.  Allocates a
+ * device copy of the tapes for the call. */
+int slrgpu_render_replay(slrgpu_handle scene, const slrgpu_settings* settings, const float* tapes, float* film,
+                         slrgpu_render_stats* stats);
+
 /* Checkpointed rendering (no counterpart in the reference, whose renderer
  * runs all passes in one call): renders samples [sample_base, sample_base +
  * spp) and adds them, in sample order, to the compensated film sums held in

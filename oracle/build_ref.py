@@ -67,6 +67,12 @@ Build-only patches (all applied to the copy):
 * P11 ``Renderer/VolumetricBPTRenderer.cpp``: P9 and P10 for the volumetric
   bidirectional renderer (cap before the sample at ``:358``, ``:84``,
   ``:269``, ``:349``).
+* P12 path tapes (test only): ``Core/random_number_generator.cpp:12-15``
+  appends every 32-bit uniform it returns to ``slr_oracle_tape`` when the
+  driver has set it, and ``PTRenderer::Job::kernel`` (``PTRenderer.cpp:107``)
+  calls ``slr_oracle_path_begin()`` before each pixel sample, so that a
+  one-thread render records each path's uniforms in the reference's draw
+  order; nothing changes while no tape is set.
 """
 from __future__ import annotations
 
@@ -88,7 +94,7 @@ FLAVORS = {
     "check": (["-O2", "-ffp-contract=off"], REF_OUT / "obj", LIB),
     "timing": (["-O3", "-DNDEBUG"], REF_OUT / "obj_timing", REF_OUT / "libslr_ref_timing.so"),
 }
-PATCH_SET = "P1 P2 P3 P4 P5 P6 P7 P8 P9 P10 P11\n"
+PATCH_SET = "P1 P2 P3 P4 P5 P6 P7 P8 P9 P10 P11 P12\n"
 
 # Files excluded from the reference's own build (libSLR/CMakeLists.txt:45-51).
 EXCLUDED = {
@@ -165,10 +171,24 @@ def copy_and_patch(ref_root: Path) -> None:
     drop_count = "slr_oracle_dropped_samples.fetch_add(1);"
     def p6_pt(t: str) -> str:
         t = _replace_once(t, "if (pathLength >= 100)", "if (pathLength > slr_oracle_max_depth)", "P6 PT")
+        t = _replace_once(t, "            for (int lx = 0; lx < numPixelX; ++lx) {\n",
+                          "            for (int lx = 0; lx < numPixelX; ++lx) {\n                slr_oracle_path_begin();\n",
+                          "P12 PT path begin")
         t = _replace_once(t, "sensor->saveImage(filename,", "if (0) sensor->saveImage(filename,", "P7 PT")
         t = _replace_once(t, drop_print, drop_count, "P8 PT")
         return t.replace("namespace SLR {", decl + "namespace SLR {", 1)
-    patch("Renderer/PTRenderer.cpp", p6_pt)
+    patch("Renderer/PTRenderer.cpp", lambda t: p6_pt(t).replace(
+        "namespace SLR {", "extern \"C\" void slr_oracle_path_begin();\nnamespace SLR {", 1))
+    def p12_rng(t: str) -> str:
+        t = _replace_once(t, "        Types32bit::UInt fractionBits = (getUInt() >> 9) | 0x3f800000;\n"
+                             "        return *(Types32bit::Float*)&fractionBits - 1.0f;",
+                          "        Types32bit::UInt fractionBits = (getUInt() >> 9) | 0x3f800000;\n"
+                          "        Types32bit::Float v = *(Types32bit::Float*)&fractionBits - 1.0f;\n"
+                          "        if (slr_oracle_tape) slr_oracle_tape->push_back(v);\n"
+                          "        return v;", "P12 rng tape")
+        return t.replace("namespace SLR {", "#include <vector>\nextern std::vector<float>* slr_oracle_tape;\n"
+                                            "namespace SLR {", 1)
+    patch("Core/random_number_generator.cpp", p12_rng)
     def p6_vpt(t: str) -> str:
         t = _replace_once(t, "            ++pathLength;\n",
                           "            ++pathLength;\n            if (pathLength > slr_oracle_max_depth)\n                break;\n",

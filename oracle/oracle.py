@@ -94,6 +94,7 @@ def lib():
             "ora_build": (I, [P]),
             "ora_render": (I, [P, I, I, I, I, I, I, I, fp, dp]),
             "ora_render_bpt": (I, [P, I, I, I, I, I, I, I, fp, dp]),
+            "ora_render_record": (I, [P, I, I, I, I, fp, fp, C.c_uint32, up, C.c_uint32, up, up]),
             "ora_sbvh_build": (I, [P, up, up, fp, up]),
             "ora_sbvh_dump": (I, [P, fp, up, up]),
             "ora_trace": (I, [P, fp, I, I, I, up, fp, fp, fp]),
@@ -222,6 +223,34 @@ class RefScene:
             raise RuntimeError("oracle render failed")
         self.last_dropped = int(lib().ora_dropped_samples())
         return film, sec.value
+
+    def render_record(self, width, height, max_depth, seed=0):
+        """One sample per pixel with one thread, recording every path's
+        uniforms (build patch P12).  Returns (film (h, w, 16), tapes): tapes[k]
+        is the float32 array of the k-th path's draws, paths in the
+        renderer's order (8 x 8 tiles row by row, pixels row by row within a
+        tile)."""
+        film = np.zeros((height, width, 16), np.float32)
+        cap_draws, cap_paths = 1 << 16, 1 << 10
+        while True:
+            tape = np.zeros(cap_draws, np.float32)
+            starts = np.zeros(cap_paths, np.uint32)
+            nd, npaths = C.c_uint32(), C.c_uint32()
+            with _quiet():
+                rc = lib().ora_render_record(self.h, max_depth, width, height, seed,
+                                             film.ctypes.data_as(C.POINTER(C.c_float)),
+                                             tape.ctypes.data_as(C.POINTER(C.c_float)), cap_draws,
+                                             starts.ctypes.data_as(C.POINTER(C.c_uint32)), cap_paths,
+                                             C.byref(nd), C.byref(npaths))
+            if rc == -3:
+                cap_draws, cap_paths = max(cap_draws, nd.value), max(cap_paths, npaths.value)
+                continue
+            if rc != 0:
+                raise RuntimeError("oracle render failed")
+            break
+        bounds = list(starts[:npaths.value]) + [nd.value]
+        tapes = [tape[bounds[k]:bounds[k + 1]].copy() for k in range(npaths.value)]
+        return film, tapes
 
     def render_bpt(self, width, height, spp, max_depth, seed=0, threads=None, volumetric=False):
         """BPTRenderer (VolumetricBPTRenderer with volumetric=True): returns

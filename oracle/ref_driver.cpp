@@ -68,6 +68,14 @@
 
 extern "C" unsigned int slr_oracle_max_depth = 100;
 std::atomic<unsigned long long> slr_oracle_dropped_samples(0);
+// Path tapes (build patch P12): while set, every uniform the reference's RNG
+// returns is appended to slr_oracle_tape, and slr_oracle_path_begin() marks
+// where each pixel sample's draws begin.  Used with one render thread only.
+std::vector<float>* slr_oracle_tape = nullptr;
+static std::vector<uint32_t>* g_pathStarts = nullptr;
+extern "C" void slr_oracle_path_begin() {
+    if (slr_oracle_tape && g_pathStarts) g_pathStarts->push_back((uint32_t)slr_oracle_tape->size());
+}
 
 namespace SLR {
     // Reads the private node arrays of a built SBVH through SBVH's friend
@@ -367,6 +375,30 @@ int ora_render(void* p, int volumetric, int spp, int maxDepth, int w, int h, int
                     film[((size_t)y * w + x) * 16 + b] = v[b];
             }
     }
+    return 0;
+}
+
+// A one-thread, one-sample PTRenderer render that records each path's
+// uniforms in the reference's draw order (Job::kernel, PTRenderer.cpp:103-144,
+// and Job::contribution, :146-276): tape[starts[k] .. starts[k + 1]) are the
+// draws of the k-th pixel sample, in the renderer's tile order.  Returns -3
+// when tapeCap or startsCap is too small (*nDraws, *nPaths then hold the sizes
+// needed).
+int ora_render_record(void* p, int maxDepth, int w, int h, int seed, float* film, float* tape, uint32_t tapeCap,
+                      uint32_t* starts, uint32_t startsCap, uint32_t* nDraws, uint32_t* nPaths) {
+    std::vector<float> t;
+    std::vector<uint32_t> st;
+    slr_oracle_tape = &t;
+    g_pathStarts = &st;
+    int rc = ora_render(p, 0, 1, maxDepth, w, h, 1, seed, film, nullptr);
+    slr_oracle_tape = nullptr;
+    g_pathStarts = nullptr;
+    if (rc != 0) return rc;
+    *nDraws = (uint32_t)t.size();
+    *nPaths = (uint32_t)st.size();
+    if (t.size() > tapeCap || st.size() > startsCap) return -3;
+    std::copy(t.begin(), t.end(), tape);
+    std::copy(st.begin(), st.end(), starts);
     return 0;
 }
 

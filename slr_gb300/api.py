@@ -147,6 +147,7 @@ def lib():
             "slrgpu_scene_build_host": (I, [H, C.POINTER(BvhStats)]),
             "slrgpu_render": (I, [H, C.POINTER(Settings), P, I, C.POINTER(RenderStats)]),
             "slrgpu_render_continue": (I, [H, C.POINTER(Settings), fp, fp, C.POINTER(RenderStats)]),
+            "slrgpu_render_replay": (I, [H, C.POINTER(Settings), fp, fp, C.POINTER(RenderStats)]),
             "slrgpu_trace": (I, [H, P, U, I, P, P, P, P, P]),
             "slrgpu_scene_sbvh_dump": (I, [H, fp, up, up]),
             "slrgpu_spectrum_evaluate": (I, [H, I, fp, U, fp]),
@@ -391,6 +392,18 @@ class Scene:
         check(lib().slrgpu_render_continue(self.handle, C.byref(s), _fp(c.state), _fp(film), C.byref(st)))
         c.next_sample += spp
         c.dropped += st.dropped_samples
+        return film, st
+
+    def render_replay(self, width: int, height: int, max_depth: int, tapes: np.ndarray):
+        """One sample per pixel in which the path of grid position i draws
+        tapes[i] (256 uniforms each, tile-padded grid, row-major) instead of
+        its own random numbers (slrgpu_render_replay).  Returns (film,
+        RenderStats)."""
+        t = np.ascontiguousarray(tapes, np.float32)
+        s = Settings(width, height, 1, max_depth, 0, 0, 0, 0, 0)
+        st = RenderStats()
+        film = np.zeros((height, width, 16), np.float32)
+        check(lib().slrgpu_render_replay(self.handle, C.byref(s), _fp(t), _fp(film), C.byref(st)))
         return film, st
 
     def trace(self, rays_dev, any_hit: bool = False, watertight: bool = False):

@@ -460,6 +460,32 @@ int slrgpu_render_continue(slrgpu_handle scene, const slrgpu_settings* settings,
     return s->ctx->engine.render(s->dev, *settings, film, false, stats, 0, film_state);
 }
 
+int slrgpu_render_replay(slrgpu_handle scene, const slrgpu_settings* settings, const float* tapes, float* film,
+                         slrgpu_render_stats* stats) {
+    const bool mutating = false;
+    GET_SCENE(s, scene);
+    if (!settings || !tapes || !film) return fail(SLRGPU_ERR_INVALID_ARGUMENT, "settings, tapes and film must not be NULL");
+    if (int rc = checkImageSize(settings->width, settings->height)) return rc;
+    if (settings->spp != 1 || settings->sample_base != 0 || settings->volumetric ||
+        (settings->flags & (SLRGPU_FLAG_BPT | SLRGPU_FLAG_WATERTIGHT)))
+        return fail(SLRGPU_ERR_UNSUPPORTED, "replay renders one sample of the surface path tracer");
+    if (!s->committed) return fail(SLRGPU_ERR_NOT_COMMITTED, "scene not committed");
+    if (!s->host.cameraPresent) return fail(SLRGPU_ERR_STATE, "scene has no camera");
+    std::lock_guard<std::mutex> lock(s->ctx->mu);
+    cudaError_t e = cudaSetDevice(s->ctx->device);
+    if (e != cudaSuccess) return fail(SLRGPU_ERR_CUDA, cudaGetErrorString(e));
+    const size_t n = (size_t)sampleGridPositions(settings->width, settings->height) * kRngTapeFloats;
+    float* dev = nullptr;
+    if ((e = cudaMalloc(&dev, n * sizeof(float))) != cudaSuccess) return fail(SLRGPU_ERR_OUT_OF_MEMORY, cudaGetErrorString(e));
+    int rc = SLRGPU_OK;
+    if ((e = cudaMemcpy(dev, tapes, n * sizeof(float), cudaMemcpyHostToDevice)) != cudaSuccess)
+        rc = fail(SLRGPU_ERR_CUDA, cudaGetErrorString(e));
+    else
+        rc = s->ctx->engine.render(s->dev, *settings, film, false, stats, 0, nullptr, dev);
+    cudaFree(dev);
+    return rc;
+}
+
 int slrgpu_render_noalloc(slrgpu_handle scene, const slrgpu_settings* settings, float* film_device, void* stream) {
     const bool mutating = false;
     GET_SCENE(s, scene);

@@ -81,10 +81,21 @@ __device__ __forceinline__ float uniformFloat(uint64_t key, uint32_t counter) {
     return __uint_as_float((u >> 9) | 0x3f800000u) - 1.0f;
 }
 
+// Path-level replay: a path draws its uniforms from tape[key .. key +
+// kRngTapeStride) (a recorded reference path) instead of the counter-based
+// generator; draws past the stride return 0.5.
+constexpr uint32_t kRngTapeStride = 256;   // kRngTapeFloats of render_api.h
 struct Rng {
     uint64_t key;
     uint32_t counter;
-    __device__ float next() { return uniformFloat(key, counter++); }
+    const float* tape = nullptr;
+    __device__ float next() {
+        if (tape) {
+            const uint32_t c = counter++;
+            return c < kRngTapeStride ? tape[key + c] : 0.5f;
+        }
+        return uniformFloat(key, counter++);
+    }
 };
 
 // ---------------------------------------------------------------------------
@@ -169,9 +180,6 @@ __device__ __forceinline__ void upsWeights(uint32_t adj, float s, float t, int i
 // quotient.  Checked against IEEE division for every float of [2^-20, 2048]
 // (tests/test_division_by_range.py); the inputs here are wavelength offsets,
 // 0 or at least 2^-15.
-#ifndef SLRGPU_FAST_REGULAR
-#define SLRGPU_FAST_REGULAR 0
-#endif
 __device__ __forceinline__ float divRange(float x) {
     constexpr float z = 1.0f / 470.0f;
     const float q = __fmul_rn(x, z);
@@ -213,37 +221,21 @@ __device__ __forceinline__ void evalUpsampled(const float* __restrict__ basis, u
     }
 }
 
-// Inlined (SLRGPU_INLINE_SPECTRUM 1), the 16 values can stay in registers;
-// out of line, the callers' spectra live in local memory.
-#ifndef SLRGPU_INLINE_SPECTRUM
-#define SLRGPU_INLINE_SPECTRUM 0
-#endif
 template <class LAM>
-#if SLRGPU_INLINE_SPECTRUM
-static __device__ __forceinline__
-#else
-static __device__ __noinline__
-#endif
-void evalSpectrum(const DevScene &sc, int id, LAM lambdas, Spec &out) {
+static __device__ __noinline__ void evalSpectrum(const DevScene &sc, int id, LAM lambdas, Spec &out) {
     const DevSpectrum sp = sc.spectra[id];
     if (sp.kind == kSpecUpsampled) {
         evalUpsampled(sc.upsSpectra, sp.adj, sp.p0, sp.p1, sp.scale, lambdas, out);
     } else if (sp.kind == kSpecRegular) {
         const float* v = sc.specValues + sp.offset;
         const float nm1 = (float)(sp.count - 1);
-#if SLRGPU_FAST_REGULAR
         // over the wavelength range itself the quotient is divRange's, the
         // correctly rounded one, in three operations instead of a division
         const bool fullRange = sp.p0 == kWavelengthLow && sp.p1 == kWavelengthHigh;
-#endif
 #pragma unroll
         for (int i = 0; i < kNumLambda; ++i) {
-#if SLRGPU_FAST_REGULAR
             const float x = __fsub_rn(lambdas[i], sp.p0);
             float binF = __fmul_rn(fullRange ? divRange(x) : __fdiv_rn(x, __fsub_rn(sp.p1, sp.p0)), nm1);
-#else
-            float binF = __fmul_rn(__fdiv_rn(__fsub_rn(lambdas[i], sp.p0), __fsub_rn(sp.p1, sp.p0)), nm1);
-#endif
             float r;
             if (binF <= 0.0f) r = v[0];
             else if (binF >= nm1) r = v[sp.count - 1];

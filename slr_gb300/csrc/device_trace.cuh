@@ -177,36 +177,9 @@ __device__ __forceinline__ uint32_t testChildren(const BvhNode* __restrict__ nod
 // sorting network on registers (5 comparators for 4 children, Batcher's 19
 // for 8); missed children sort last at +inf.  Pushes all but the nearest,
 // far to near, and returns the nearest.
-#ifndef SLRGPU_ORDER_FASTPATH
-#define SLRGPU_ORDER_FASTPATH 0
-#endif
 __device__ __forceinline__ uint32_t orderChildren(uint32_t mask, const float tn[kBvhWidth],
                                                   const uint32_t ch[kBvhWidth], StackEntry* stack, int &sp,
                                                   bool &ok) {
-#if SLRGPU_ORDER_FASTPATH
-    // One or two hit children, the common cases below the top levels: the
-    // network's order without the network (nearer first; ties to the lower
-    // child index).
-    if (__popc(mask) <= 2) {
-        uint32_t c0 = 0, c1 = 0;
-        float t0 = 0.0f, t1 = 0.0f;
-        bool first = true;
-#pragma unroll
-        for (int i = 0; i < kBvhWidth; ++i) {
-            if ((mask >> i) & 1u) {
-                if (first) { c0 = ch[i]; t0 = tn[i]; first = false; }
-                else { c1 = ch[i]; t1 = tn[i]; }
-            }
-        }
-        if (__popc(mask) == 1) return c0;
-        const bool swap = t1 < t0;
-        const uint32_t cn = swap ? c1 : c0, cf = swap ? c0 : c1;
-        const float tf = swap ? t0 : t1;
-        if (sp < kTraceStack) stack[sp++] = StackEntry{cf, tf};
-        else ok = false;
-        return cn;
-    }
-#endif
     float t[kBvhWidth];
     uint32_t c[kBvhWidth], k[kBvhWidth];
 #pragma unroll

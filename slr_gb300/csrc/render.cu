@@ -49,24 +49,9 @@ struct __align__(16) PathScalars {
 };
 static_assert(sizeof(PathScalars) == 32, "one sector per path");
 
-// The extension kernel's copy of the hit triangle's record for the shading
-// kernels (SLRGPU_SURF_RECORD 1: the 32-byte DevPrim, read beside the hit
-// instead of after it), or the whole surface point (2: position, shading
-// frame, geometric normal, material and 1/area in 64 bytes).
-#ifndef SLRGPU_SURF_RECORD
-#define SLRGPU_SURF_RECORD 0
-#endif
-// The surface shading kernels compute their wavelengths from the path's
-// offset where used (1) instead of keeping an array of 16 (0).
-#ifndef SLRGPU_LAMBDA_OFFSET
-#define SLRGPU_LAMBDA_OFFSET 0
-#endif
-constexpr int kSurfRecordWords = SLRGPU_SURF_RECORD == 2 ? 4 : SLRGPU_SURF_RECORD == 1 ? 2 : 0;
-
 struct WaveState {
     float4* ray;         // [N][2]: origin xyz + tmin, direction xyz + tmax (one sector per path)
     float4* hit;         // t, b1, b2, prim bits
-    float4* surf;        // [N][kSurfRecordWords] (null when 0)
     float* alpha;        // [N][16]: 16 contiguous values per path
     float* L;            // [N][16]
     PathScalars* ps;     // [N]
@@ -180,8 +165,10 @@ __global__ void kRaygen(DevScene sc, WaveState ws, const __grid_constant__ WaveP
         uint32_t s = q / sg.gridPositions;
         uint32_t pixel = q - s * sg.gridPositions;
         uint32_t ix = pixel % sg.gridW, iy = pixel / sg.gridW;
-        const uint64_t key = pathKey(sg.seed, (uint64_t)(sg.sampleBase + s) * sg.gridPositions + pixel);
-        Rng rng{key, 0};
+        // replay: the path's tape slot is its grid position (one sample)
+        const uint64_t key = sc.rngTape ? (uint64_t)pixel * kRngTapeStride
+                                        : pathKey(sg.seed, (uint64_t)(sg.sampleBase + s) * sg.gridPositions + pixel);
+        Rng rng{key, 0, sc.rngTape};
         // Draw order of Job::kernel: time, pixel (2), wavelength offset,
         // wavelength selection, lens (2) (PTRenderer.cpp:108-116).
         (void)rng.next();
@@ -270,28 +257,7 @@ __global__ void __launch_bounds__(256, SLRGPU_TRACE_MIN_BLOCKS) kExtendSort(DevS
             Hit h;
             traceClosest(sc, V3{o.x, o.y, o.z}, V3{d.x, d.y, d.z}, o.w, d.w, &h);
             ws.hit[p] = make_float4(h.t, h.b1, h.b2, __uint_as_float(h.prim));
-#if SLRGPU_SURF_RECORD == 0
             cls = h.prim == kNoHit ? kClassMiss : (int)sc.materials[sc.prims[h.prim].material].kind;
-#else
-            if (h.prim == kNoHit) {
-                cls = kClassMiss;
-            } else {
-                const DevPrim pr = sc.prims[h.prim];
-                cls = (int)sc.materials[pr.material].kind;
-#if SLRGPU_SURF_RECORD == 1
-                ws.surf[2 * (size_t)p] = make_float4(__uint_as_float(pr.v0), __uint_as_float(pr.v1),
-                                                     __uint_as_float(pr.v2), __uint_as_float(pr.material));
-                ws.surf[2 * (size_t)p + 1] = make_float4(pr.ngx, pr.ngy, pr.ngz, pr.invArea);
-#else
-                SurfPoint sp;
-                surfacePoint(sc, pr, V3{o.x, o.y, o.z}, V3{d.x, d.y, d.z}, h.t, h.b1, h.b2, sp);
-                ws.surf[4 * (size_t)p] = make_float4(sp.p.x, sp.p.y, sp.p.z, __uint_as_float(pr.material));
-                ws.surf[4 * (size_t)p + 1] = make_float4(sp.frame.x.x, sp.frame.x.y, sp.frame.x.z, pr.invArea);
-                ws.surf[4 * (size_t)p + 2] = make_float4(sp.frame.z.x, sp.frame.z.y, sp.frame.z.z, 0.0f);
-                ws.surf[4 * (size_t)p + 3] = make_float4(pr.ngx, pr.ngy, pr.ngz, 0.0f);
-#endif
-            }
-#endif
         }
 #pragma unroll
         for (int c = 0; c < kNumShadeClasses; ++c)
@@ -313,13 +279,7 @@ __global__ void kShadeMiss(DevScene sc, WaveState ws, const uint32_t* __restrict
         const uint32_t depth = info >> kInfoDepthShift;
         const bool prevDelta = (info & kInfoPrevDelta) != 0;
         const float wlOff = ws.ps[p].wlOffset;
-#if SLRGPU_LAMBDA_OFFSET
         const OffsetLambdas lambdas{wlOff};
-#else
-        float lambdas[kNumLambda];
-#pragma unroll
-        for (int k = 0; k < kNumLambda; ++k) lambdas[k] = lambdaAt(k, wlOff);
-#endif
         float4 rd = ws.ray[2 * (size_t)p + 1];
         V3 dir = V3{rd.x, rd.y, rd.z};
         float theta, phi;
@@ -372,55 +332,17 @@ __global__ void __launch_bounds__(256, K == kMatGGXScattering ? SLRGPU_SHADE_DIE
             const bool prevDelta = (info & kInfoPrevDelta) != 0;
             uint32_t depth = info >> kInfoDepthShift;
             const float wlOff = ws.ps[p].wlOffset;
-#if SLRGPU_LAMBDA_OFFSET
             const OffsetLambdas lambdas{wlOff};
-#else
-            float lambdas[kNumLambda];
-#pragma unroll
-            for (int k = 0; k < kNumLambda; ++k) lambdas[k] = lambdaAt(k, wlOff);
-#endif
-            Rng rng{loadKey(ws, p), ws.ps[p].rngCounter};
+            Rng rng{loadKey(ws, p), ws.ps[p].rngCounter, sc.rngTape};
             float4 ro = ws.ray[2 * (size_t)p], rd = ws.ray[2 * (size_t)p + 1];
             V3 org = V3{ro.x, ro.y, ro.z}, dir = V3{rd.x, rd.y, rd.z};
-#if SLRGPU_SURF_RECORD == 2
-            const float4 s0 = ws.surf[4 * (size_t)p], s1 = ws.surf[4 * (size_t)p + 1];
-            const float4 s2 = ws.surf[4 * (size_t)p + 2], s3 = ws.surf[4 * (size_t)p + 3];
-            DevPrim pr;
-            pr.material = __float_as_uint(s0.w);
-            pr.invArea = s1.w;
-            SurfPoint sp;
-            sp.p = V3{s0.x, s0.y, s0.z};
-            {
-                const V3 fx{s1.x, s1.y, s1.z}, fz{s2.x, s2.y, s2.z};
-                sp.frame = Frame{fx, cross(fz, fx), fz};
-            }
-            sp.gn = V3{s3.x, s3.y, s3.z};
-            Spec alpha;
-            loadSpec(ws.alpha, p, alpha);
-            bool alive = true;
-#else
-#if SLRGPU_SURF_RECORD == 1
-            float4 hv = ws.hit[p];
-            const float4 r0 = ws.surf[2 * (size_t)p], r1 = ws.surf[2 * (size_t)p + 1];
-            DevPrim pr;
-            pr.v0 = __float_as_uint(r0.x);
-            pr.v1 = __float_as_uint(r0.y);
-            pr.v2 = __float_as_uint(r0.z);
-            pr.material = __float_as_uint(r0.w);
-            pr.ngx = r1.x;
-            pr.ngy = r1.y;
-            pr.ngz = r1.z;
-            pr.invArea = r1.w;
-#else
             float4 hv = ws.hit[p];
             const DevPrim pr = sc.prims[__float_as_uint(hv.w)];
-#endif
             Spec alpha;
             loadSpec(ws.alpha, p, alpha);
             bool alive = true;
             SurfPoint sp;
             surfacePoint(sc, pr, org, dir, hv.x, hv.y, hv.z, sp);
-#endif
             const DevMaterial mat = sc.materials[pr.material];
             V3 dirOut = sp.frame.toLocal(-dir);
             // Emission on hit (PTRenderer.cpp:162-166, :240-263).
@@ -617,9 +539,7 @@ __global__ void __launch_bounds__(256, SLRGPU_VOLINTERACT_MIN_BLOCKS) kVolIntera
                 const int sel = (int)(info & kInfoSelMask);
                 const bool wlSelected = (info & kInfoWlSelected) != 0;
                 const float wlOff = ws.ps[p].wlOffset;
-                float lambdas[kNumLambda];
-#pragma unroll
-                for (int k = 0; k < kNumLambda; ++k) lambdas[k] = lambdaAt(k, wlOff);
+                const OffsetLambdas lambdas{wlOff};
                 Rng rng{loadKey(ws, p), ws.ps[p].rngCounter};
                 const float4 ro = ws.ray[2 * (size_t)p], rd = ws.ray[2 * (size_t)p + 1];
                 const V3 org = V3{ro.x, ro.y, ro.z}, dir = V3{rd.x, rd.y, rd.z};
@@ -673,9 +593,7 @@ __global__ void __launch_bounds__(256, SLRGPU_SHADEVOL_MIN_BLOCKS) kShadeVol(Dev
             const bool prevDelta = (info & kInfoPrevDelta) != 0;
             uint32_t depth = info >> kInfoDepthShift;
             const float wlOff = ws.ps[p].wlOffset;
-            float lambdas[kNumLambda];
-#pragma unroll
-            for (int k = 0; k < kNumLambda; ++k) lambdas[k] = lambdaAt(k, wlOff);
+            const OffsetLambdas lambdas{wlOff};
             Rng rng{loadKey(ws, p), ws.ps[p].rngCounter};
             float4 ro = ws.ray[2 * (size_t)p], rd = ws.ray[2 * (size_t)p + 1];
             V3 org = V3{ro.x, ro.y, ro.z}, dir = V3{rd.x, rd.y, rd.z};
@@ -1359,10 +1277,6 @@ int RenderEngine::ensure(uint32_t N, uint32_t maxDepth) {
     w->N = N;
     w->ray = allocDev<float4>(allocs, 2ull * N, &e); if (!w->ray) goto fail;
     w->hit = allocDev<float4>(allocs, N, &e); if (!w->hit) goto fail;
-    if (kSurfRecordWords) {
-        w->surf = allocDev<float4>(allocs, (size_t)kSurfRecordWords * N, &e);
-        if (!w->surf) goto fail;
-    }
     w->alpha = allocDev<float>(allocs, (size_t)N * kNumLambda, &e); if (!w->alpha) goto fail;
     w->L = allocDev<float>(allocs, (size_t)N * kNumLambda, &e); if (!w->L) goto fail;
     w->ps = allocDev<PathScalars>(allocs, N, &e); if (!w->ps) goto fail;
@@ -1377,7 +1291,7 @@ int RenderEngine::ensure(uint32_t N, uint32_t maxDepth) {
     ws = w;
     capacity = N;
     depthCapacity = maxDepth;
-    stateBytes = (uint64_t)N * (2 * 16 + 16 + 16 * kSurfRecordWords + 2 * 4 * kNumLambda + sizeof(PathScalars) + 2 * 16 + 4 * kNumLambda +
+    stateBytes = (uint64_t)N * (2 * 16 + 16 + 2 * 4 * kNumLambda + sizeof(PathScalars) + 2 * 16 + 4 * kNumLambda +
                                 3 * 4 + 4 * kNumClassQueues) +
                  4ull * kCtrStride * (maxDepth + 2) + 4 * sizeof(unsigned long long);
     return SLRGPU_OK;
@@ -1534,10 +1448,11 @@ static WavePlan planWaves(const slrgpu_settings &s, uint32_t autoPaths) {
 // the counter reset or a launch was rejected.
 static int runWave(const DeviceScene &ds0, const WaveState &w, const WaveParams &wp, uint32_t D, bool volumetric,
                    bool watertight, cudaStream_t stream, LaunchMarks &lm, uint64_t* launchCount,
-                   const WaveParams* wpDev = nullptr) {
+                   const WaveParams* wpDev = nullptr, const float* rngTape = nullptr) {
     // the scene as the kernels see it, with the triangle test chosen
     struct { DevScene sc; uint32_t kindMask; } ds{ds0.sc, ds0.kindMask};
     ds.sc.watertight = watertight ? 1u : 0u;
+    ds.sc.rngTape = rngTape;
     const int block = 256;
     const WaveGrids &g = waveGrids(block);
     uint64_t launches = 0;
@@ -1656,7 +1571,8 @@ static int runWave(const DeviceScene &ds0, const WaveState &w, const WaveParams 
 // The wave loop of one render (slrgpu_render, slrgpu_render_noalloc): waves
 // of pl.S sample indices over the whole sample grid, one segment each.
 static int runWaves(const DeviceScene &ds, const slrgpu_settings &s, const WavePlan &pl, const WaveState &w,
-                    float* filmSum, float* filmComp, cudaStream_t stream, LaunchMarks &lm, uint64_t* launches) {
+                    float* filmSum, float* filmComp, cudaStream_t stream, LaunchMarks &lm, uint64_t* launches,
+                    const float* rngTape = nullptr) {
     for (uint32_t base = 0; base < s.spp; base += pl.S) {
         TraceRange range("wave: samples %u..%u", s.sample_base + base, s.sample_base + std::min(s.spp, base + pl.S));
         WaveParams wp;
@@ -1679,14 +1595,14 @@ static int runWaves(const DeviceScene &ds, const slrgpu_settings &s, const WaveP
         wp.numPaths = sg.samples * pl.gridPositions;
         wp.filmPixels = s.width * s.height;
         int rc = runWave(ds, w, wp, s.max_depth, s.volumetric != 0, (s.flags & SLRGPU_FLAG_WATERTIGHT) != 0,
-                         stream, lm, launches);
+                         stream, lm, launches, nullptr, rngTape);
         if (rc != SLRGPU_OK) return rc;
     }
     return SLRGPU_OK;
 }
 
 int RenderEngine::render(const DeviceScene &ds, const slrgpu_settings &s, float* film, bool filmOnDevice,
-                         slrgpu_render_stats* stats, cudaStream_t stream, float* filmState) {
+                         slrgpu_render_stats* stats, cudaStream_t stream, float* filmState, const float* rngTape) {
     auto t0 = std::chrono::steady_clock::now();
     TraceRange range("render %ux%u, %u spp, depth %u", s.width, s.height, s.spp, s.max_depth);
     if (s.spp == 0) {
@@ -1753,7 +1669,7 @@ int RenderEngine::render(const DeviceScene &ds, const slrgpu_settings &s, float*
         rc = renderBpt(*bpt, ds, s, filmSum, filmComp, stream, &launches, profile ? &eventPool : nullptr, &bst);
         if (rc != SLRGPU_OK) return rc;
     } else {
-        rc = runWaves(ds, s, pl, *ws, filmSum, filmComp, stream, lm, &launches);
+        rc = runWaves(ds, s, pl, *ws, filmSum, filmComp, stream, lm, &launches, rngTape);
         if (rc != SLRGPU_OK) return rc;
     }
     CUDA_TRY(cudaGetLastError());
@@ -1818,8 +1734,7 @@ constexpr uint32_t kNoAllocMaxDepth = 64;
 constexpr size_t naAlign(size_t x) { return (x + 255) & ~(size_t)255; }
 constexpr size_t kNaRay = 0;
 constexpr size_t kNaHit = naAlign(kNaRay + 32ull * kNoAllocMaxPaths);
-constexpr size_t kNaSurf = naAlign(kNaHit + 16ull * kNoAllocMaxPaths);
-constexpr size_t kNaAlpha = naAlign(kNaSurf + 16ull * kSurfRecordWords * kNoAllocMaxPaths);
+constexpr size_t kNaAlpha = naAlign(kNaHit + 16ull * kNoAllocMaxPaths);
 constexpr size_t kNaL = naAlign(kNaAlpha + 4ull * kNumLambda * kNoAllocMaxPaths);
 constexpr size_t kNaScalars = naAlign(kNaL + 4ull * kNumLambda * kNoAllocMaxPaths);
 constexpr size_t kNaShRay = naAlign(kNaScalars + sizeof(PathScalars) * kNoAllocMaxPaths);
@@ -1898,7 +1813,6 @@ int renderNoAlloc(const DeviceScene &ds, const slrgpu_settings &s, float* film, 
     w.N = pl.S * pl.gridPositions;
     w.ray = (float4*)(base + kNaRay);
     w.hit = (float4*)(base + kNaHit);
-    w.surf = kSurfRecordWords ? (float4*)(base + kNaSurf) : nullptr;
     w.alpha = (float*)(base + kNaAlpha);
     w.L = (float*)(base + kNaL);
     w.ps = (PathScalars*)(base + kNaScalars);

@@ -60,7 +60,8 @@ struct RenderEngine {
     // from (2 x 16 x width x height floats: sum planes, then compensation
     // planes), updated in place; film may then be null.
     int render(const DeviceScene &ds, const slrgpu_settings &s, float* film, bool filmOnDevice,
-               slrgpu_render_stats* stats, cudaStream_t stream, float* filmState = nullptr);
+               slrgpu_render_stats* stats, cudaStream_t stream, float* filmState = nullptr,
+               const float* rngTape = nullptr);   // device tape of slrgpu_render_replay
     ~RenderEngine();
 };
 
@@ -92,6 +93,8 @@ uint32_t sampleGridPositions(uint32_t width, uint32_t height);
 // Largest image side any entry point accepts; checkImageSize() also bounds
 // the tile-padded grid to 2^31 - 1 positions (sets the error text).
 constexpr uint32_t kMaxImageSide = 1u << 20;
+// uniforms per grid position of slrgpu_render_replay's tapes
+constexpr uint32_t kRngTapeFloats = 256;
 int checkImageSize(uint32_t width, uint32_t height);
 // useGraph: replay the slot's captured graph for this (scene, depth,
 // integrator), capturing it on first use.

@@ -145,6 +145,10 @@ struct DevScene {
     const TriFrag* frags;
     const float4* wtVerts;  // per fragment: v0 (w = prim id bits), v1, v2 as given (watertight test)
     uint32_t watertight;    // 1: watertight triangle test instead of the reference's
+    // path-level replay (slrgpu_render_replay): kRngTapeStride uniforms per
+    // grid position that the path tracer draws instead of its own; null
+    // otherwise
+    const float* rngTape;
     const DevPrim* prims;
     const float4* vpos;     // xyz, u
     const float4* vnrm;     // xyz, v
