@@ -174,3 +174,19 @@ def test_reference_bpt_agrees_with_pt(oracle_lib):
     tb, tp = np.array(tb), np.array(tp)
     z = (tb.mean() - tp.mean()) / np.sqrt(tb.var(ddof=1) / k + tp.var(ddof=1) / k)
     assert abs(z) < 4.0, (tb.mean(), tp.mean(), z)
+
+
+def test_reference_path_tapes(oracle_lib):
+    """Recording the reference's uniforms (oracle patch P12) changes nothing
+    it renders: the one-thread, one-sample film equals a plain render with
+    the same seed; one tape per pixel sample, each at least the seven camera
+    draws long (time, pixel 2, wavelength, wavelength selection, lens 2)."""
+    from slr_gb300 import scenes
+    desc = scenes.box_scene(16, 8)
+    ref = oracle_lib.RefScene(desc)
+    film, tapes = ref.render_record(16, 8, 8, seed=9)
+    plain, _ = ref.render(16, 8, 1, 8, seed=9, threads=1)
+    np.testing.assert_array_equal(film, plain)
+    assert len(tapes) == 16 * 8
+    assert min(len(t) for t in tapes) >= 7
+    assert all(((t >= 0) & (t < 1)).all() for t in tapes)
