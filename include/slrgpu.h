@@ -211,6 +211,16 @@ int slrgpu_render(slrgpu_handle scene, const slrgpu_settings* settings, float* f
  * volumetric, watertight or bidirectional flag (SLRGPU_ERR_UNSUPPORTED);
  * max_depth at most 35 keeps a path's draws within its 256.  Allocates a
  * device copy of the tapes for the call. */
+/* Diagnostics (no counterpart in the reference): the queue counters of the
+ * last path-tracer wave rendered on the context, one row of 11 per bounce
+ * (rows = max_depth + 2 of the context's path state): [0..4] paths shaded
+ * per material kind, [5] paths that left the scene, [6] medium scattering
+ * points, [7] paths in the bounce's extension queue, [8] shadow rays, [9]
+ * shadow rays waiting for their transmittance, [10] a work counter.  These
+ * are the units of each wave kernel's launch (for profiles).  capacity is
+ * the size of counts in uint32. */
+int slrgpu_context_queue_counts(slrgpu_handle ctx, uint32_t* counts, uint32_t capacity, uint32_t* rows);
+
 int slrgpu_render_replay(slrgpu_handle scene, const slrgpu_settings* settings, const float* tapes, float* film,
                          slrgpu_render_stats* stats);
 

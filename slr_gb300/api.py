@@ -148,6 +148,7 @@ def lib():
             "slrgpu_render": (I, [H, C.POINTER(Settings), P, I, C.POINTER(RenderStats)]),
             "slrgpu_render_continue": (I, [H, C.POINTER(Settings), fp, fp, C.POINTER(RenderStats)]),
             "slrgpu_render_replay": (I, [H, C.POINTER(Settings), fp, fp, C.POINTER(RenderStats)]),
+            "slrgpu_context_queue_counts": (I, [H, up, U, up]),
             "slrgpu_trace": (I, [H, P, U, I, P, P, P, P, P]),
             "slrgpu_scene_sbvh_dump": (I, [H, fp, up, up]),
             "slrgpu_spectrum_evaluate": (I, [H, I, fp, U, fp]),
@@ -230,6 +231,15 @@ class Context:
         h = C.c_uint64()
         check(lib().slrgpu_context_create(device, C.byref(h)))
         self.handle = h.value
+
+    def queue_counts(self) -> np.ndarray:
+        """(rows, 11) queue counters of the last path-tracer wave rendered on
+        this context (slrgpu_context_queue_counts)."""
+        cap = 11 * 4096
+        out = np.zeros(cap, np.uint32)
+        rows = C.c_uint32()
+        check(lib().slrgpu_context_queue_counts(self.handle, _up(out), cap, C.byref(rows)))
+        return out[:11 * rows.value].reshape(rows.value, 11)
 
     def close(self):
         if getattr(self, "handle", 0):

@@ -142,6 +142,16 @@ int slrgpu_context_create(int device, slrgpu_handle* ctx) {
     return SLRGPU_OK;
 }
 
+int slrgpu_context_queue_counts(slrgpu_handle ctx, uint32_t* counts, uint32_t capacity, uint32_t* rows) {
+    if (!counts || !rows) return fail(SLRGPU_ERR_INVALID_ARGUMENT, "counts and rows must not be NULL");
+    Context* c = findContext(ctx);
+    if (!c) return fail(SLRGPU_ERR_INVALID_HANDLE, "invalid context handle");
+    std::lock_guard<std::mutex> lock(c->mu);
+    cudaError_t e = cudaSetDevice(c->device);
+    if (e != cudaSuccess) return fail(SLRGPU_ERR_CUDA, cudaGetErrorString(e));
+    return c->engine.queueCounts(counts, capacity, rows);
+}
+
 int slrgpu_context_destroy(slrgpu_handle ctx) {
     std::unique_ptr<Context> c;
     {

@@ -1307,6 +1307,22 @@ RenderEngine::~RenderEngine() {
     if (bpt) bptEngineDestroy(bpt);
 }
 
+static_assert(kCtrStride == (int)kQueueCountColumns, "queue-count rows are the counter blocks");
+int RenderEngine::queueCounts(uint32_t* out, uint32_t capacity, uint32_t* rows) {
+    if (!ws) {
+        *rows = 0;
+        return SLRGPU_OK;
+    }
+    *rows = depthCapacity + 2;
+    const size_t n = (size_t)kCtrStride * (depthCapacity + 2);
+    if (capacity < n) {
+        setError("capacity below rows x 11 counters");
+        return SLRGPU_ERR_INVALID_ARGUMENT;
+    }
+    CUDA_TRY(cudaMemcpy(out, ws->counters, n * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    return SLRGPU_OK;
+}
+
 int RenderEngine::ensureFilm(uint32_t P) {
     if (filmPixels >= P) return SLRGPU_OK;
     if (filmSum) cudaFree(filmSum);

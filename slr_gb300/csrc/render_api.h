@@ -55,6 +55,8 @@ struct RenderEngine {
 
     int ensure(uint32_t paths, uint32_t maxDepth);
     int ensureFilm(uint32_t pixels);
+    // the last wave's per-bounce queue counters (rows of kQueueCountColumns)
+    int queueCounts(uint32_t* out, uint32_t capacity, uint32_t* rows);
     void release();
     // filmState (host, optional): the compensated film sums to continue
     // from (2 x 16 x width x height floats: sum planes, then compensation
@@ -93,6 +95,8 @@ uint32_t sampleGridPositions(uint32_t width, uint32_t height);
 // Largest image side any entry point accepts; checkImageSize() also bounds
 // the tile-padded grid to 2^31 - 1 positions (sets the error text).
 constexpr uint32_t kMaxImageSide = 1u << 20;
+// columns of slrgpu_context_queue_counts' rows
+constexpr uint32_t kQueueCountColumns = 11;
 // uniforms per grid position of slrgpu_render_replay's tapes
 constexpr uint32_t kRngTapeFloats = 256;
 int checkImageSize(uint32_t width, uint32_t height);
