@@ -274,10 +274,13 @@ uint64_t slrgpu_render_noalloc_scratch_bytes(void);
  * its context, any resolution, spp and max depth) with continuous batching:
  * requests are admitted oldest first while their films fit the HBM budget;
  * in SLRGPU_SERVER_BATCHED mode each wave of launches carries the next
- * samples of several admitted requests of one scene (up to 32), and waves of
- * different scenes run concurrently on separate streams and path-state
- * slots; requests that arrive while others are on the GPU join the next
- * wave.  SLRGPU_SERVER_PLAIN renders one request at a time, like
+ * samples of up to 32 admitted requests with the same integrator and max
+ * depth: for the surface path tracer, requests of up to 8 different scenes,
+ * whose paths share one set of extension, shading and shadow queues (each
+ * path finds its scene in the wave's scene table); for the volumetric path
+ * tracer, requests of one scene.  Several waves run concurrently on separate
+ * streams and path-state slots, a request in one wave at a time; requests
+ * that arrive while others are on the GPU join the next wave.  SLRGPU_SERVER_PLAIN renders one request at a time, like
  * slrgpu_render.  A request's film is bit-identical in both modes and to
  * slrgpu_render with the same settings: its random numbers depend only on
  * (seed, sample, pixel) and its samples are accumulated in order.  A scene
@@ -323,6 +326,7 @@ typedef struct slrgpu_server_stats {
     uint32_t queued, active;
     double first_start_seconds;
     double last_done_seconds;
+    uint64_t mixed_scene_waves; /* waves whose paths came from more than one scene */
 } slrgpu_server_stats;
 
 int slrgpu_server_create(slrgpu_handle ctx, const slrgpu_server_config* config, slrgpu_handle* server);

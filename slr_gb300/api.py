@@ -96,7 +96,8 @@ class RequestInfo(C.Structure):
 class ServerStats(C.Structure):
     _fields_ = [("requests_done", C.c_uint64), ("path_samples_done", C.c_uint64), ("waves", C.c_uint64),
                 ("kernel_launches", C.c_uint64), ("bytes_in_use", C.c_uint64), ("queued", C.c_uint32),
-                ("active", C.c_uint32), ("first_start_seconds", C.c_double), ("last_done_seconds", C.c_double)]
+                ("active", C.c_uint32), ("first_start_seconds", C.c_double), ("last_done_seconds", C.c_double),
+                ("mixed_scene_waves", C.c_uint64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

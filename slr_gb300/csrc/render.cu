@@ -107,6 +107,7 @@ struct WaveSegment {
     uint32_t gridPositions;   // gridW * gridH
     uint32_t sampleBase, samples;
     uint32_t seed;
+    uint32_t scene;           // index in the wave's scene table (waves of several scenes)
     uint32_t filmBegin;       // first pixel of the request in the wave's film enumeration
     float* filmSum;           // [16][width * height], Kahan sum and compensation
     float* filmComp;
@@ -142,7 +143,20 @@ constexpr uint32_t kMediumHit = 0xfffffffeu;
 constexpr uint32_t kInfoSelMask = 0xfu;
 constexpr uint32_t kInfoWlSelected = 1u << 4;
 constexpr uint32_t kInfoPrevDelta = 1u << 5;
-constexpr int kInfoDepthShift = 8;
+constexpr int kInfoSceneShift = 8;    // bits 8-15: the path's scene in a wave of several scenes
+constexpr uint32_t kInfoSceneMask = 0xffu << kInfoSceneShift;
+constexpr int kInfoDepthShift = 16;
+
+// A wave of several scenes (the serving loop's shared queues): the kernels
+// find each path's scene in a table in device memory by the scene index in
+// its info word; single-scene waves take the scene by value (MULTI false).
+constexpr int kMaxWaveScenes = 8;
+template <bool MULTI>
+__device__ __forceinline__ const DevScene &pathScene(const DevScene &scArg, const DevScene* __restrict__ scenes,
+                                                     uint32_t info) {
+    if (MULTI) return scenes[(info & kInfoSceneMask) >> kInfoSceneShift];
+    return scArg;
+}
 
 __device__ __forceinline__ uint64_t loadKey(const WaveState &ws, uint32_t p) {
     return ((uint64_t)ws.ps[p].keyHi << 32) | ws.ps[p].keyLo;
@@ -153,14 +167,16 @@ __device__ __forceinline__ uint64_t loadKey(const WaveState &ws, uint32_t p) {
 // ---------------------------------------------------------------------------
 // wpDev: the wave's parameters in device memory (graph-captured waves, whose
 // launch parameters are fixed at capture), or null to use wpArg.
-__global__ void kRaygen(DevScene sc, WaveState ws, const __grid_constant__ WaveParams wpArg,
-                        const WaveParams* __restrict__ wpDev) {
+template <bool MULTI>
+__global__ void kRaygen(DevScene scArg, WaveState ws, const __grid_constant__ WaveParams wpArg,
+                        const WaveParams* __restrict__ wpDev, const DevScene* __restrict__ scenes) {
     const WaveParams &wp = wpDev ? *wpDev : wpArg;
     if (blockIdx.x == 0 && threadIdx.x == 0) ws.counters[kCtrExt] = wp.numPaths;
     for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < wp.numPaths; p += gridDim.x * blockDim.x) {
         uint32_t k = 0;
         while (k + 1 < wp.numSegments && p >= wp.seg[k + 1].pathBegin) ++k;
         const WaveSegment &sg = wp.seg[k];
+        const DevScene &sc = MULTI ? scenes[sg.scene] : scArg;
         const uint32_t q = p - sg.pathBegin;
         uint32_t s = q / sg.gridPositions;
         uint32_t pixel = q - s * sg.gridPositions;
@@ -185,7 +201,7 @@ __global__ void kRaygen(DevScene sc, WaveState ws, const __grid_constant__ WaveP
         ws.ray[2 * (size_t)p] = make_float4(org.x, org.y, org.z, 0.0f);
         ws.ray[2 * (size_t)p + 1] = make_float4(dir.x, dir.y, dir.z, __int_as_float(0x7f800000));
         PathScalars ps;
-        ps.info = sel;
+        ps.info = sel | (MULTI ? sg.scene << kInfoSceneShift : 0u);
         ps.wlOffset = wlOff;
         ps.prevPdf = 0.0f;
         ps.initY = importance(specConst(1.0f), (int)sel);
@@ -217,12 +233,15 @@ __global__ void kExtend(DevScene sc, WaveState ws, const uint32_t* __restrict__ 
 #ifndef SLRGPU_TRACE_MIN_BLOCKS
 #define SLRGPU_TRACE_MIN_BLOCKS 4
 #endif
-__global__ void __launch_bounds__(256, SLRGPU_TRACE_MIN_BLOCKS) kShadow(DevScene sc, WaveState ws,
+template <bool MULTI>
+__global__ void __launch_bounds__(256, SLRGPU_TRACE_MIN_BLOCKS) kShadow(DevScene scArg, WaveState ws,
                                                                       const uint32_t* __restrict__ queue,
-                                                                      const uint32_t* __restrict__ count) {
+                                                                      const uint32_t* __restrict__ count,
+                                                                      const DevScene* __restrict__ scenes) {
     const uint32_t n = *count;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         uint32_t p = queue[i];
+        const DevScene &sc = pathScene<MULTI>(scArg, scenes, MULTI ? ws.ps[p].info : 0u);
         float4 o = ws.shRay[2 * (size_t)p], d = ws.shRay[2 * (size_t)p + 1];
         if (!traceAny(sc, V3{o.x, o.y, o.z}, V3{d.x, d.y, d.z}, o.w, d.w)) {
             Spec c;
@@ -242,9 +261,11 @@ __global__ void __launch_bounds__(256, SLRGPU_TRACE_MIN_BLOCKS) kShadow(DevScene
 // divergence.  Emission with MIS, Russian roulette, next-event estimation and
 // BSDF sampling follow PTRenderer::Job::contribution (PTRenderer.cpp:145-277).
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256, SLRGPU_TRACE_MIN_BLOCKS) kExtendSort(DevScene sc, WaveState ws,
+template <bool MULTI>
+__global__ void __launch_bounds__(256, SLRGPU_TRACE_MIN_BLOCKS) kExtendSort(DevScene scArg, WaveState ws,
                                                                           const uint32_t* __restrict__ queue,
-                            const uint32_t* __restrict__ count, uint32_t* classCounts) {
+                            const uint32_t* __restrict__ count, uint32_t* classCounts,
+                            const DevScene* __restrict__ scenes) {
     const uint32_t n = *count;
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
         const uint32_t i = base + threadIdx.x;
@@ -253,6 +274,7 @@ __global__ void __launch_bounds__(256, SLRGPU_TRACE_MIN_BLOCKS) kExtendSort(DevS
         uint32_t p = 0;
         if (active) {
             p = queue[i];
+            const DevScene &sc = pathScene<MULTI>(scArg, scenes, MULTI ? ws.ps[p].info : 0u);
             float4 o = ws.ray[2 * (size_t)p], d = ws.ray[2 * (size_t)p + 1];
             Hit h;
             traceClosest(sc, V3{o.x, o.y, o.z}, V3{d.x, d.y, d.z}, o.w, d.w, &h);
@@ -268,14 +290,17 @@ __global__ void __launch_bounds__(256, SLRGPU_TRACE_MIN_BLOCKS) kExtendSort(DevS
 
 // Paths whose ray left the scene: environment emission (with MIS after a
 // non-delta bounce), then the path ends (PTRenderer.cpp:150-152, :234-263).
-__global__ void kShadeMiss(DevScene sc, WaveState ws, const uint32_t* __restrict__ queue,
-                           const uint32_t* __restrict__ count) {
+template <bool MULTI>
+__global__ void kShadeMiss(DevScene scArg, WaveState ws, const uint32_t* __restrict__ queue,
+                           const uint32_t* __restrict__ count, const DevScene* __restrict__ scenes) {
     const uint32_t n = *count;
-    if (!sc.envPresent) return;
+    if (!MULTI && !scArg.envPresent) return;
     const float twoPi = 6.28318530717958647692f;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const uint32_t p = queue[i];
         const uint32_t info = ws.ps[p].info;
+        const DevScene &sc = pathScene<MULTI>(scArg, scenes, info);
+        if (MULTI && !sc.envPresent) continue;     // no environment: the path just ends
         const uint32_t depth = info >> kInfoDepthShift;
         const bool prevDelta = (info & kInfoPrevDelta) != 0;
         const float wlOff = ws.ps[p].wlOffset;
@@ -310,12 +335,13 @@ __global__ void kShadeMiss(DevScene sc, WaveState ws, const uint32_t* __restrict
 #ifndef SLRGPU_SHADE_DIELECTRIC_MIN_BLOCKS
 #define SLRGPU_SHADE_DIELECTRIC_MIN_BLOCKS SLRGPU_SHADE_MIN_BLOCKS
 #endif
-template <int K>
+template <int K, bool MULTI>
 __global__ void __launch_bounds__(256, K == kMatGGXScattering ? SLRGPU_SHADE_DIELECTRIC_MIN_BLOCKS
-                                                               : SLRGPU_SHADE_MIN_BLOCKS) kShadeSurf(DevScene sc, WaveState ws, uint32_t maxDepth,
+                                                               : SLRGPU_SHADE_MIN_BLOCKS) kShadeSurf(DevScene scArg, WaveState ws, uint32_t maxDepth,
                                                   const uint32_t* __restrict__ inQueue,
                                                   const uint32_t* __restrict__ inCount, uint32_t* outQueue,
-                                                  uint32_t* outCount, uint32_t* shQueue, uint32_t* shCount) {
+                                                  uint32_t* outCount, uint32_t* shQueue, uint32_t* shCount,
+                                                  const DevScene* __restrict__ scenes) {
     const uint32_t n = *inCount;
     const uint32_t N = ws.N;
     const float inf = __int_as_float(0x7f800000);
@@ -327,6 +353,8 @@ __global__ void __launch_bounds__(256, K == kMatGGXScattering ? SLRGPU_SHADE_DIE
         uint32_t p = active ? inQueue[i] : 0;
         if (active) {
             uint32_t info = ws.ps[p].info;
+            const DevScene &sc = pathScene<MULTI>(scArg, scenes, info);
+            const uint32_t sceneBits = info & kInfoSceneMask;
             const int sel = (int)(info & kInfoSelMask);
             bool wlSelected = (info & kInfoWlSelected) != 0;
             const bool prevDelta = (info & kInfoPrevDelta) != 0;
@@ -487,7 +515,7 @@ __global__ void __launch_bounds__(256, K == kMatGGXScattering ? SLRGPU_SHADE_DIE
                     ws.ray[2 * (size_t)p + 1] = make_float4(nd.x, nd.y, nd.z, inf);
                     ws.ps[p].prevPdf = bs.pdf;
                     info = (uint32_t)sel | (wlSelected ? kInfoWlSelected : 0u) |
-                           (dirIsDelta(bs.type) ? kInfoPrevDelta : 0u) | (depth << kInfoDepthShift);
+                           (dirIsDelta(bs.type) ? kInfoPrevDelta : 0u) | (depth << kInfoDepthShift) | sceneBits;
                     ws.ps[p].info = info;
                     storeSpec(ws.alpha, p, alpha);
                     extend = true;
@@ -1364,15 +1392,18 @@ static int gridFor(const void* kernel, int block) {
 struct WaveGrids {
     int raygen, extend, shadow, accumulate, volInteract, shadowVol, shadowVolMedium, extendSort, shadeMiss;
     int shadeSurf[kNumShadeClasses - 1];
+    // the multi-scene instances
+    int raygenM, shadowM, extendSortM, shadeMissM;
+    int shadeSurfM[kNumShadeClasses - 1];
     int shadeVol[kNumClassQueues - 1];
 };
 static const WaveGrids &waveGrids(int block) {
     static WaveGrids g;
     static std::once_flag once;
     std::call_once(once, [&]() {
-        g.raygen = gridFor((const void*)kRaygen, block);
+        g.raygen = gridFor((const void*)kRaygen<false>, block);
         g.extend = gridFor((const void*)kExtend, block);
-        g.shadow = gridFor((const void*)kShadow, block);
+        g.shadow = gridFor((const void*)kShadow<false>, block);
         g.accumulate = gridFor((const void*)kAccumulate, block);
         g.volInteract = gridFor((const void*)kVolInteract, block);
         g.shadeVol[0] = gridFor((const void*)kShadeVol<0>, block);
@@ -1384,13 +1415,22 @@ static const WaveGrids &waveGrids(int block) {
         g.shadeVol[6] = gridFor((const void*)kShadeVol<6>, block);
         g.shadowVol = gridFor((const void*)kShadowVol, block);
         g.shadowVolMedium = gridFor((const void*)kShadowVolMedium, block);
-        g.extendSort = gridFor((const void*)kExtendSort, block);
-        g.shadeMiss = gridFor((const void*)kShadeMiss, block);
-        g.shadeSurf[kMatMatte] = gridFor((const void*)kShadeSurf<kMatMatte>, block);
-        g.shadeSurf[kMatSpecularReflection] = gridFor((const void*)kShadeSurf<kMatSpecularReflection>, block);
-        g.shadeSurf[kMatSpecularScattering] = gridFor((const void*)kShadeSurf<kMatSpecularScattering>, block);
-        g.shadeSurf[kMatGGXReflection] = gridFor((const void*)kShadeSurf<kMatGGXReflection>, block);
-        g.shadeSurf[kMatGGXScattering] = gridFor((const void*)kShadeSurf<kMatGGXScattering>, block);
+        g.extendSort = gridFor((const void*)kExtendSort<false>, block);
+        g.shadeMiss = gridFor((const void*)kShadeMiss<false>, block);
+        g.shadeSurf[kMatMatte] = gridFor((const void*)kShadeSurf<kMatMatte, false>, block);
+        g.shadeSurf[kMatSpecularReflection] = gridFor((const void*)kShadeSurf<kMatSpecularReflection, false>, block);
+        g.shadeSurf[kMatSpecularScattering] = gridFor((const void*)kShadeSurf<kMatSpecularScattering, false>, block);
+        g.shadeSurf[kMatGGXReflection] = gridFor((const void*)kShadeSurf<kMatGGXReflection, false>, block);
+        g.shadeSurf[kMatGGXScattering] = gridFor((const void*)kShadeSurf<kMatGGXScattering, false>, block);
+        g.raygenM = gridFor((const void*)kRaygen<true>, block);
+        g.shadowM = gridFor((const void*)kShadow<true>, block);
+        g.extendSortM = gridFor((const void*)kExtendSort<true>, block);
+        g.shadeMissM = gridFor((const void*)kShadeMiss<true>, block);
+        g.shadeSurfM[kMatMatte] = gridFor((const void*)kShadeSurf<kMatMatte, true>, block);
+        g.shadeSurfM[kMatSpecularReflection] = gridFor((const void*)kShadeSurf<kMatSpecularReflection, true>, block);
+        g.shadeSurfM[kMatSpecularScattering] = gridFor((const void*)kShadeSurf<kMatSpecularScattering, true>, block);
+        g.shadeSurfM[kMatGGXReflection] = gridFor((const void*)kShadeSurf<kMatGGXReflection, true>, block);
+        g.shadeSurfM[kMatGGXScattering] = gridFor((const void*)kShadeSurf<kMatGGXScattering, true>, block);
     });
     return g;
 }
@@ -1462,9 +1502,65 @@ static WavePlan planWaves(const slrgpu_settings &s, uint32_t autoPaths) {
 // queues and path state live in w.  Adds the number of kernel launches to
 // *launchCount; returns SLRGPU_OK, or SLRGPU_ERR_CUDA (error text set) when
 // the counter reset or a launch was rejected.
+// The scenes of a wave of several scenes (surface path tracer only): their
+// table in device memory, the union of their material kinds, whether any
+// has an environment.
+struct WaveSceneTable {
+    const DevScene* dev;
+    uint32_t kindMask;
+    bool env;
+};
+
+// One bounce of the surface path tracer: closest hits sorted by shading
+// class, the shading kernels of the classes present, the shadow rays.
+template <bool MULTI>
+static void surfaceBounce(const DevScene &sc, const DevScene* scenes, uint32_t kindMask, bool env, const WaveState &w,
+                          uint32_t D, uint32_t* ctr, uint32_t* next, const uint32_t* inQueue, uint32_t* outQueue,
+                          cudaStream_t stream, LaunchMarks &lm, uint64_t &launches) {
+    const int block = 256;
+    const WaveGrids &g = waveGrids(block);
+    lm.begin(SLRGPU_KERNEL_EXTEND);
+    kExtendSort<MULTI><<<MULTI ? g.extendSortM : g.extendSort, block, 0, stream>>>(sc, w, inQueue, ctr + kCtrExt, ctr,
+                                                                                  scenes);
+    lm.end();
+    ++launches;
+    if (env) {
+        lm.begin(SLRGPU_KERNEL_SHADE);
+        kShadeMiss<MULTI><<<MULTI ? g.shadeMissM : g.shadeMiss, block, 0, stream>>>(
+            sc, w, w.classQueue + (size_t)kClassMiss * w.N, ctr + kClassMiss, scenes);
+        lm.end();
+        ++launches;
+    }
+    // One kernel per material kind present.
+    for (int k = 0; k < kNumShadeClasses - 1; ++k) {
+        if (!(kindMask & (1u << k))) continue;
+        const uint32_t* cq = w.classQueue + (size_t)k * w.N;
+        const int grid = MULTI ? g.shadeSurfM[k] : g.shadeSurf[k];
+        lm.begin(SLRGPU_KERNEL_SHADE);
+#define SLRGPU_SHADESURF(KK)                                                                                   \
+    kShadeSurf<KK, MULTI><<<grid, block, 0, stream>>>(sc, w, D, cq, ctr + k, outQueue, next + kCtrExt, w.shadowQueue, \
+                                                      ctr + kCtrShadow, scenes)
+        switch (k) {
+        case kMatMatte: SLRGPU_SHADESURF(kMatMatte); break;
+        case kMatSpecularReflection: SLRGPU_SHADESURF(kMatSpecularReflection); break;
+        case kMatSpecularScattering: SLRGPU_SHADESURF(kMatSpecularScattering); break;
+        case kMatGGXReflection: SLRGPU_SHADESURF(kMatGGXReflection); break;
+        default: SLRGPU_SHADESURF(kMatGGXScattering); break;
+        }
+#undef SLRGPU_SHADESURF
+        lm.end();
+        ++launches;
+    }
+    lm.begin(SLRGPU_KERNEL_SHADOW);
+    kShadow<MULTI><<<MULTI ? g.shadowM : g.shadow, block, 0, stream>>>(sc, w, w.shadowQueue, ctr + kCtrShadow, scenes);
+    lm.end();
+    ++launches;
+}
+
 static int runWave(const DeviceScene &ds0, const WaveState &w, const WaveParams &wp, uint32_t D, bool volumetric,
                    bool watertight, cudaStream_t stream, LaunchMarks &lm, uint64_t* launchCount,
-                   const WaveParams* wpDev = nullptr, const float* rngTape = nullptr) {
+                   const WaveParams* wpDev = nullptr, const float* rngTape = nullptr,
+                   const WaveSceneTable* multi = nullptr) {
     // the scene as the kernels see it, with the triangle test chosen
     struct { DevScene sc; uint32_t kindMask; } ds{ds0.sc, ds0.kindMask};
     ds.sc.watertight = watertight ? 1u : 0u;
@@ -1473,8 +1569,15 @@ static int runWave(const DeviceScene &ds0, const WaveState &w, const WaveParams 
     const WaveGrids &g = waveGrids(block);
     uint64_t launches = 0;
     CUDA_TRY(cudaMemsetAsync(w.counters, 0, (size_t)kCtrStride * (D + 2) * sizeof(uint32_t), stream));
+    if (multi && volumetric) {
+        setError("waves of several scenes are for the surface path tracer");
+        return SLRGPU_ERR_INVALID_ARGUMENT;
+    }
     lm.begin(SLRGPU_KERNEL_RAYGEN);
-    kRaygen<<<g.raygen, block, 0, stream>>>(ds.sc, w, wp, wpDev);
+    if (multi)
+        kRaygen<true><<<g.raygenM, block, 0, stream>>>(ds.sc, w, wp, wpDev, multi->dev);
+    else
+        kRaygen<false><<<g.raygen, block, 0, stream>>>(ds.sc, w, wp, wpDev, nullptr);
     lm.end();
     ++launches;
     for (uint32_t b = 0; b <= D; ++b) {
@@ -1528,52 +1631,12 @@ static int runWave(const DeviceScene &ds0, const WaveState &w, const WaveParams 
             launches += 2;
             continue;
         }
-        // Closest hits, sorted into one queue per shading class.
-        lm.begin(SLRGPU_KERNEL_EXTEND);
-        kExtendSort<<<g.extendSort, block, 0, stream>>>(ds.sc, w, inQueue, ctr + kCtrExt, ctr);
-        lm.end();
-        ++launches;
-        if (ds.sc.envPresent) {
-            lm.begin(SLRGPU_KERNEL_SHADE);
-            kShadeMiss<<<g.shadeMiss, block, 0, stream>>>(ds.sc, w, w.classQueue + (size_t)kClassMiss * w.N,
-                                                          ctr + kClassMiss);
-            lm.end();
-            ++launches;
-        }
-        // One kernel per material kind present in the scene.
-        for (int k = 0; k < kNumShadeClasses - 1; ++k) {
-            if (!(ds.kindMask & (1u << k))) continue;
-            const uint32_t* cq = w.classQueue + (size_t)k * w.N;
-            lm.begin(SLRGPU_KERNEL_SHADE);
-            switch (k) {
-            case kMatMatte:
-                kShadeSurf<kMatMatte><<<g.shadeSurf[k], block, 0, stream>>>(
-                    ds.sc, w, D, cq, ctr + k, outQueue, next + kCtrExt, w.shadowQueue, ctr + kCtrShadow);
-                break;
-            case kMatSpecularReflection:
-                kShadeSurf<kMatSpecularReflection><<<g.shadeSurf[k], block, 0, stream>>>(
-                    ds.sc, w, D, cq, ctr + k, outQueue, next + kCtrExt, w.shadowQueue, ctr + kCtrShadow);
-                break;
-            case kMatSpecularScattering:
-                kShadeSurf<kMatSpecularScattering><<<g.shadeSurf[k], block, 0, stream>>>(
-                    ds.sc, w, D, cq, ctr + k, outQueue, next + kCtrExt, w.shadowQueue, ctr + kCtrShadow);
-                break;
-            case kMatGGXReflection:
-                kShadeSurf<kMatGGXReflection><<<g.shadeSurf[k], block, 0, stream>>>(
-                    ds.sc, w, D, cq, ctr + k, outQueue, next + kCtrExt, w.shadowQueue, ctr + kCtrShadow);
-                break;
-            default:
-                kShadeSurf<kMatGGXScattering><<<g.shadeSurf[k], block, 0, stream>>>(
-                    ds.sc, w, D, cq, ctr + k, outQueue, next + kCtrExt, w.shadowQueue, ctr + kCtrShadow);
-                break;
-            }
-            lm.end();
-            ++launches;
-        }
-        lm.begin(SLRGPU_KERNEL_SHADOW);
-        kShadow<<<g.shadow, block, 0, stream>>>(ds.sc, w, w.shadowQueue, ctr + kCtrShadow);
-        lm.end();
-        ++launches;
+        if (multi)
+            surfaceBounce<true>(ds.sc, multi->dev, multi->kindMask, multi->env, w, D, ctr, next, inQueue, outQueue,
+                                stream, lm, launches);
+        else
+            surfaceBounce<false>(ds.sc, nullptr, ds.kindMask, ds.sc.envPresent != 0, w, D, ctr, next, inQueue,
+                                 outQueue, stream, lm, launches);
     }
     lm.begin(SLRGPU_KERNEL_ACCUMULATE);
     kAccumulate<<<g.accumulate, block, 0, stream>>>(w, wp, wpDev);
@@ -1956,15 +2019,20 @@ int filmToBmp(const float* film, uint32_t width, uint32_t height, bool filmOnDev
 // depth, integrator) as a CUDA graph and replays it for every later wave of
 // that kind; the wave's segments travel in device memory (copied from pinned
 // staging memory before each replay), so the captured launches never change.
+static_assert(kMaxWaveScenesApi == kMaxWaveScenes, "one scene-table size");
 struct WaveSlot {
     RenderEngine engine;   // path state only; films belong to the requests
     WaveParams* dParams = nullptr;
     WaveParams* hParams = nullptr;   // pinned
+    DevScene* dScenes = nullptr;     // [kMaxWaveScenes]: the scene table of waves of several scenes
+    DevScene* hScenes = nullptr;     // pinned
     struct Graph {
-        uint64_t sceneUid;
+        uint64_t sceneUid;           // 0: a wave of several scenes
         uint32_t depth;
         bool volumetric;
         bool watertight;
+        uint32_t kindMask;           // waves of several scenes: the kinds and the environment
+        bool env;
         cudaGraphExec_t exec;
         uint64_t launches;
     };
@@ -1973,6 +2041,8 @@ struct WaveSlot {
         for (Graph &g : graphs) cudaGraphExecDestroy(g.exec);
         if (dParams) cudaFree(dParams);
         if (hParams) cudaFreeHost(hParams);
+        if (dScenes) cudaFree(dScenes);
+        if (hScenes) cudaFreeHost(hScenes);
     }
 };
 
@@ -1980,7 +2050,9 @@ WaveSlot* waveSlotCreate(uint32_t paths, uint32_t maxDepth, std::string* err) {
     WaveSlot* slot = new WaveSlot();
     if (slot->engine.ensure(paths, maxDepth) != SLRGPU_OK ||
         cudaMalloc(&slot->dParams, sizeof(WaveParams)) != cudaSuccess ||
-        cudaMallocHost(&slot->hParams, sizeof(WaveParams)) != cudaSuccess) {
+        cudaMallocHost(&slot->hParams, sizeof(WaveParams)) != cudaSuccess ||
+        cudaMalloc(&slot->dScenes, kMaxWaveScenes * sizeof(DevScene)) != cudaSuccess ||
+        cudaMallocHost(&slot->hScenes, kMaxWaveScenes * sizeof(DevScene)) != cudaSuccess) {
         if (err) *err = "wave slot allocation failed";
         delete slot;
         return nullptr;
@@ -1992,16 +2064,42 @@ void waveSlotDestroy(WaveSlot* slot) { delete slot; }
 
 uint32_t waveSlotCapacity(const WaveSlot* slot) { return slot->engine.capacity; }
 
-uint64_t waveSlotBytes(const WaveSlot* slot) { return slot->engine.stateBytes + sizeof(WaveParams); }
+uint64_t waveSlotBytes(const WaveSlot* slot) {
+    return slot->engine.stateBytes + sizeof(WaveParams) + kMaxWaveScenes * sizeof(DevScene);
+}
 
 uint32_t sampleGridPositions(uint32_t width, uint32_t height) { return padToTile(width) * padToTile(height); }
 
-int launchWave(const DeviceScene &ds, WaveSlot* slot, const SegmentDesc* segs, int numSegs, uint32_t maxDepth,
-               bool volumetric, bool watertight, cudaStream_t stream, uint64_t* launches, bool useGraph) {
+int launchWave(const DeviceScene* const* scenes, int numScenes, WaveSlot* slot, const SegmentDesc* segs, int numSegs,
+               uint32_t maxDepth, bool volumetric, bool watertight, cudaStream_t stream, uint64_t* launches,
+               bool useGraph) {
     if (numSegs <= 0 || numSegs > kMaxWaveSegments) {
         setError("a wave holds 1 to 32 segments");
         return SLRGPU_ERR_INVALID_ARGUMENT;
     }
+    if (numScenes <= 0 || numScenes > kMaxWaveScenes || (numScenes > 1 && volumetric)) {
+        setError("a wave holds 1 to 8 scenes (one for the volumetric path tracer)");
+        return SLRGPU_ERR_INVALID_ARGUMENT;
+    }
+    const DeviceScene &ds = *scenes[0];
+    // waves of several scenes: the scene table, as the kernels see it
+    WaveSceneTable table{slot->dScenes, 0u, false};
+    const bool multi = numScenes > 1;
+    if (multi) {
+        for (int i = 0; i < numScenes; ++i) {
+            DevScene sc = scenes[i]->sc;
+            sc.watertight = watertight ? 1u : 0u;
+            sc.rngTape = nullptr;
+            slot->hScenes[i] = sc;
+            table.kindMask |= scenes[i]->kindMask;
+            table.env = table.env || sc.envPresent != 0;
+        }
+    }
+    for (int i = 0; i < numSegs; ++i)
+        if ((int)segs[i].scene >= numScenes) {
+            setError("segment scene index out of range");
+            return SLRGPU_ERR_INVALID_ARGUMENT;
+        }
     if (maxDepth > slot->engine.depthCapacity) {
         setError("max_depth exceeds the wave slot's counter capacity");
         return SLRGPU_ERR_INVALID_ARGUMENT;
@@ -2021,6 +2119,7 @@ int launchWave(const DeviceScene &ds, WaveSlot* slot, const SegmentDesc* segs, i
         sg.sampleBase = d.sampleBase;
         sg.samples = d.samples;
         sg.seed = d.seed;
+        sg.scene = d.scene;
         sg.filmBegin = (uint32_t)pixels;
         sg.filmSum = d.filmSum;
         sg.filmComp = d.filmComp;
@@ -2035,16 +2134,24 @@ int launchWave(const DeviceScene &ds, WaveSlot* slot, const SegmentDesc* segs, i
     wp.numSegments = (uint32_t)numSegs;
     wp.numPaths = (uint32_t)paths;
     wp.filmPixels = (uint32_t)pixels;
+    // The previous wave on this slot has completed (the caller waits for it),
+    // so the staging copies are free to overwrite.
+    if (multi)
+        CUDA_TRY(cudaMemcpyAsync(slot->dScenes, slot->hScenes, numScenes * sizeof(DevScene), cudaMemcpyHostToDevice,
+                                 stream));
     if (!useGraph) {
         LaunchMarks lm;
         uint64_t n = 0;
-        int rc = runWave(ds, *slot->engine.ws, wp, maxDepth, volumetric, watertight, stream, lm, &n);
+        int rc = runWave(ds, *slot->engine.ws, wp, maxDepth, volumetric, watertight, stream, lm, &n, nullptr, nullptr,
+                         multi ? &table : nullptr);
         if (launches) *launches += n;
         return rc;
     }
+    const uint64_t uid = multi ? 0 : ds.uid;
     WaveSlot::Graph* graph = nullptr;
     for (WaveSlot::Graph &g : slot->graphs)
-        if (g.sceneUid == ds.uid && g.depth == maxDepth && g.volumetric == volumetric && g.watertight == watertight)
+        if (g.sceneUid == uid && g.depth == maxDepth && g.volumetric == volumetric && g.watertight == watertight &&
+            (!multi || (g.kindMask == table.kindMask && g.env == table.env)))
             graph = &g;
     if (!graph) {
         waveGrids(256);   // occupancy queries stay outside the capture
@@ -2057,7 +2164,7 @@ int launchWave(const DeviceScene &ds, WaveSlot* slot, const SegmentDesc* segs, i
         CUDA_TRY(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
         uint64_t n = 0;
         int rc = runWave(ds, *slot->engine.ws, empty, maxDepth, volumetric, watertight, stream, lm, &n,
-                         slot->dParams);
+                         slot->dParams, nullptr, multi ? &table : nullptr);
         cudaError_t e = cudaStreamEndCapture(stream, &g);
         if (rc != SLRGPU_OK) {
             if (g) cudaGraphDestroy(g);
@@ -2074,11 +2181,10 @@ int launchWave(const DeviceScene &ds, WaveSlot* slot, const SegmentDesc* segs, i
             setError(std::string("wave graph instantiation failed: ") + cudaGetErrorString(e));
             return SLRGPU_ERR_CUDA;
         }
-        slot->graphs.push_back(WaveSlot::Graph{ds.uid, maxDepth, volumetric, watertight, exec, n});
+        slot->graphs.push_back(
+            WaveSlot::Graph{uid, maxDepth, volumetric, watertight, table.kindMask, table.env, exec, n});
         graph = &slot->graphs.back();
     }
-    // The previous wave on this slot has completed (the caller waits for it),
-    // so the staging copy is free to overwrite.
     std::memcpy(slot->hParams, &wp, sizeof(wp));
     CUDA_TRY(cudaMemcpyAsync(slot->dParams, slot->hParams, sizeof(wp), cudaMemcpyHostToDevice, stream));
     CUDA_TRY(cudaGraphLaunch(graph->exec, stream));

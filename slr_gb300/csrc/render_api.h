@@ -83,6 +83,7 @@ struct WaveSlot;
 // (16-bin planes of width * height floats, sum and compensation).
 struct SegmentDesc {
     uint32_t width, height, sampleBase, samples, seed;
+    uint32_t scene;                // index in launchWave's scene list
     float* filmSum;
     float* filmComp;
     unsigned long long* dropped;   // device counter, or null
@@ -102,7 +103,12 @@ constexpr uint32_t kRngTapeFloats = 256;
 int checkImageSize(uint32_t width, uint32_t height);
 // useGraph: replay the slot's captured graph for this (scene, depth,
 // integrator), capturing it on first use.
-int launchWave(const DeviceScene &ds, WaveSlot* slot, const SegmentDesc* segs, int numSegs, uint32_t maxDepth,
+// A wave of up to kMaxWaveScenesApi scenes: with more than one, the surface
+// path tracer's kernels find each path's scene in a table (volumetric waves
+// take one scene).
+constexpr int kMaxWaveScenesApi = 8;
+int launchWave(const DeviceScene* const* scenes, int numScenes, WaveSlot* slot, const SegmentDesc* segs, int numSegs,
+               uint32_t maxDepth,
                bool volumetric, bool watertight, cudaStream_t stream, uint64_t* launches, bool useGraph);
 int launchFilmToPixelMajor(const float* filmSum, float* out, uint32_t pixels, cudaStream_t stream);
 

@@ -344,6 +344,7 @@ void Server::stats(slrgpu_server_stats* st) {
     st->bytes_in_use = usedBytes_;
     st->queued = (uint32_t)pending_.size();
     st->active = (uint32_t)active_.size();
+    st->mixed_scene_waves = mixedWaves_;
     st->first_start_seconds = firstStart_;
     st->last_done_seconds = lastDone_;
 }
@@ -413,39 +414,55 @@ void Server::admitLocked() {
     }
 }
 
-// Fills every idle slot with a wave: the next samples of admitted requests of
-// one scene / integrator / max depth, oldest request first.  Holds mu_.
+// Fills every idle slot with a wave: the next samples of admitted requests,
+// oldest first, that share an integrator, max depth and triangle test.  In
+// the batched mode a surface path-tracer wave takes requests of up to
+// kMaxWaveScenesApi scenes into one set of queues; a volumetric wave takes
+// one scene.  A request is in at most one wave at a time (its film adds its
+// samples in order).  Holds mu_.
 bool Server::launchWaves() {
     bool launched = false;
     for (Slot &sl : slots_) {
         if (sl.busy) continue;
-        // the oldest active request that still has samples to issue picks the
-        // wave's scene, integrator and depth
+        // the oldest active request that still has samples to issue and no
+        // wave in flight picks the wave's integrator and depth
         Request* lead = nullptr;
         for (Request* r : active_)
-            if (r->samplesIssued < r->settings.spp && !r->cancelled) {
-                bool taken = false;   // its scene already runs in another slot this round
-                for (const Slot &o : slots_)
-                    if (o.busy && o.ds == r->ds) taken = true;
-                if (taken && cfg_.mode == SLRGPU_SERVER_BATCHED) continue;
+            if (r->samplesIssued < r->settings.spp && !r->cancelled && !inFlightLocked(r)) {
                 lead = r;
                 break;
             }
         if (!lead) break;
+        const bool mixScenes = cfg_.mode == SLRGPU_SERVER_BATCHED && !lead->settings.volumetric;
         const uint32_t cap = waveSlotCapacity(sl.wave);
         std::vector<SegmentDesc> segs;
+        std::vector<const DeviceScene*> scenes{lead->ds};
         sl.segments.clear();
         uint64_t paths = 0;
         for (Request* r : active_) {
             if ((int)segs.size() == kMaxSegmentsPerWave) break;
-            if (r->samplesIssued >= r->settings.spp || r->cancelled) continue;
-            if (r->ds != lead->ds || r->settings.volumetric != lead->settings.volumetric ||
+            if (r->samplesIssued >= r->settings.spp || r->cancelled || inFlightLocked(r)) continue;
+            if (r->settings.volumetric != lead->settings.volumetric ||
                 r->settings.max_depth != lead->settings.max_depth ||
                 (r->settings.flags & SLRGPU_FLAG_WATERTIGHT) != (lead->settings.flags & SLRGPU_FLAG_WATERTIGHT))
                 continue;
             if (cfg_.mode == SLRGPU_SERVER_PLAIN && r != lead) continue;
+            uint32_t sceneIdx = 0;
+            while (sceneIdx < scenes.size() && scenes[sceneIdx] != r->ds) ++sceneIdx;
+            if (sceneIdx == scenes.size()) {
+                if (!mixScenes || (int)scenes.size() == kMaxWaveScenesApi) continue;
+                scenes.push_back(r->ds);
+            }
             uint64_t room = (cap - paths) / r->gridPositions;
-            if (room == 0) break;
+            if (room == 0) {
+                if (sceneIdx + 1 == scenes.size() && sceneIdx > 0 && scenes.back() == r->ds) {
+                    // nothing of this scene made it in
+                    bool used = false;
+                    for (const SegmentDesc &d : segs) used = used || d.scene == sceneIdx;
+                    if (!used) scenes.pop_back();
+                }
+                break;
+            }
             uint32_t take = (uint32_t)std::min<uint64_t>(room, r->settings.spp - r->samplesIssued);
             if (r->settings.samples_per_wave) take = std::min(take, r->settings.samples_per_wave);
             SegmentDesc d;
@@ -454,6 +471,7 @@ bool Server::launchWaves() {
             d.sampleBase = r->settings.sample_base + r->samplesIssued;
             d.samples = take;
             d.seed = r->settings.seed;
+            d.scene = sceneIdx;
             d.filmSum = r->filmSum;
             d.filmComp = r->filmComp;
             d.dropped = r->dropped;
@@ -469,9 +487,10 @@ bool Server::launchWaves() {
         if (takeFault(g_faultWaveLaunch))
             setError("injected wave launch failure");
         else
-            rc = launchWave(*lead->ds, sl.wave, segs.data(), (int)segs.size(), lead->settings.max_depth,
-                            lead->settings.volumetric != 0, (lead->settings.flags & SLRGPU_FLAG_WATERTIGHT) != 0,
-                            sl.stream, &n, cfg_.mode == SLRGPU_SERVER_BATCHED);
+            rc = launchWave(scenes.data(), (int)scenes.size(), sl.wave, segs.data(), (int)segs.size(),
+                            lead->settings.max_depth, lead->settings.volumetric != 0,
+                            (lead->settings.flags & SLRGPU_FLAG_WATERTIGHT) != 0, sl.stream, &n,
+                            cfg_.mode == SLRGPU_SERVER_BATCHED);
         if (rc != SLRGPU_OK) {
             for (auto &pr : sl.segments) failRequest(pr.first, "wave launch failed");
             sl.segments.clear();
@@ -482,6 +501,7 @@ bool Server::launchWaves() {
         sl.busy = true;
         sl.ds = lead->ds;
         ++wavesLaunched_;
+        if (scenes.size() > 1) ++mixedWaves_;
         kernelLaunches_ += n;
         launched = true;
     }

@@ -3,10 +3,11 @@
 // Requests of any resident scene, resolution and sample count are queued,
 // admitted while their films fit the HBM budget, and rendered in waves.  In
 // the batched mode a wave packs the next samples of several admitted
-// requests of the same scene (and integrator / max depth) into one set of
-// launches, and waves of different scenes run concurrently on their own
-// streams and path-state slots; requests that arrive while others are on the
-// GPU join the next wave.  The plain mode renders one request at a time
+// requests (same integrator and max depth; for the surface path tracer of up
+// to 8 different scenes, whose paths then share one set of queues) into one
+// set of launches, and several waves run concurrently on their own streams
+// and path-state slots; requests that arrive while others are on the GPU
+// join the next wave.  The plain mode renders one request at a time
 // with waves of that request only, as slrgpu_render does.  A request's random
 // numbers depend only on (seed, sample, pixel) and its film accumulates its
 // samples in order, so its film is bit-identical in either mode and to
@@ -121,6 +122,7 @@ private:
     bool stop_ = false;
     std::thread thread_;
     // statistics
+    uint64_t mixedWaves_ = 0;
     uint64_t wavesLaunched_ = 0, kernelLaunches_ = 0, pathSamplesDone_ = 0, requestsDone_ = 0;
     double firstStart_ = -1, lastDone_ = 0;
 };

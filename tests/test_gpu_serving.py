@@ -151,3 +151,25 @@ def test_server_rejects_bad_requests(gpu_lib, served_scenes):
             srv.submit(scs[0], 8, 8, 1, 4, volumetric=True)     # no medium in this scene
     finally:
         srv.close()
+
+
+def test_waves_share_queues_across_scenes(gpu_lib, served_scenes):
+    """Requests of different scenes travel in one wave: their paths share
+    the extension, shading and shadow queues, each path finding its scene in
+    the wave's scene table.  One slot, requests of the box and the GGX scene
+    submitted together: the waves mix the scenes, and every film still
+    equals its standalone render."""
+    ctx, scs = served_scenes
+    srv = gpu_lib.Server(ctx, mode=gpu_lib.SERVER_BATCHED, slots=1, paths_per_slot=1 << 16, max_depth=16)
+    try:
+        reqs = [(0, 48, 48, 8, 8, 31), (1, 40, 24, 8, 8, 32), (0, 21, 13, 16, 8, 33), (1, 64, 64, 4, 8, 34)]
+        ids = [srv.submit(scs[i], w, h, spp, d, seed=seed) for i, w, h, spp, d, seed in reqs]
+        refs = [scs[i].render(w, h, spp, d, seed=seed)[0] for i, w, h, spp, d, seed in reqs]
+        for rid, ref in zip(ids, refs):
+            film, info = srv.wait(rid, timeout=120)
+            assert info.status == gpu_lib.REQUEST_DONE
+            assert np.array_equal(film, ref)
+        st = srv.stats()
+        assert st.mixed_scene_waves > 0, st.as_dict()
+    finally:
+        srv.close()
