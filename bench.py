@@ -77,10 +77,15 @@ BYTES_BPT_BOUNCE = 440
 BYTES_BPT_CONNECT = 390
 BYTES_BPT_SHADOW = 164   # queued connection 100 B in, any-hit query, 64 B atomic add out
 
-# DRAM bytes per unit of the dominant kernel class measured by ncu
-# (dram__bytes_read.sum + dram__bytes_write.sum over the class's launches of
-# the same workload, divided by its units): profiles/dram_ggx_ibl_1m.md.
-MEASURED_DRAM_PER_UNIT = {("ggx_ibl_1m", "shade"): 721.7}
+# DRAM bytes per shaded bounce of the surface shading kernels, measured by
+# ncu (dram__bytes_read.sum + dram__bytes_write.sum, --clock-control none) on
+# the first three kShadeSurf launches of the `small` workload (512 x 512,
+# 4 spp, 176k triangles: 1,048,576 paths, ~0.4 GB of path state) divided by
+# the paths those launches shaded (slrgpu_context_queue_counts): 294.1 MB
+# over 678,107 shaded bounces.  The line scales it by the units per launch of
+# the measured workload (the full-size run is not captured with more than
+# the launch list).
+SHADE_DRAM_BYTES_PER_UNIT = 433.7
 
 
 def load_peaks():
@@ -582,10 +587,15 @@ def main():
                 "bytes_per_unit": per_unit, "units_per_launch": n_units / max(1, kern_n[dom]),
                 "avg_launch_ms": avg_launch_s * 1e3,
                 "kernel_share": {names[k]: kern_ms[k] / max(1e-9, sum(kern_ms)) for k in range(5)}}
-    measured = MEASURED_DRAM_PER_UNIT.get((args.workload, names[dom]))
-    if measured is not None and not BPT:
-        roofline["traffic"] = measured * n_units / max(1, kern_n[dom])
-        roofline["traffic_source"] = "ncu dram bytes per unit (profiles/dram_ggx_ibl_1m.md) x units per launch"
+    if names[dom] == "shade" and not BPT and not VOLUMETRIC:
+        roofline["traffic"] = SHADE_DRAM_BYTES_PER_UNIT * n_units / max(1, kern_n[dom])
+        roofline["traffic_source"] = ("ncu DRAM bytes per shaded bounce of kShadeSurf on the small workload "
+                                      "(three launches, 433.7 B) x shaded bounces per launch of this run")
+    if VOLUMETRIC and names[dom] == "shadow":
+        roofline["note"] = ("the shadow class is dominated by the ratio-tracking transmittance walks, which read the "
+                            "density grid from L2 (64 MiB at 256^3; ~91 % L2 hit rate, ~73 % issue activity with 13 "
+                            "of 32 lanes active per instruction under ncu): issue- and latency-bound, not HBM-bound; "
+                            "bytes_per_unit counts only the shadow ray's 36 B")
     if BPT:   # the bidirectional tracer's kernels behind the classes
         roofline["kernel"] = {0: "kBptInit", 1: "kBptBounce", 2: "kBptConnect", 3: "kBptShadow",
                               4: "kBptAccumulate"}.get(dom, names[dom])
