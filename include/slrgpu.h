@@ -264,7 +264,9 @@ int slrgpu_render_continue(slrgpu_handle scene, const slrgpu_settings* settings,
  * capture.  Every call shares the one array and clears what must start at
  * zero, so calls that overlap on the GPU (concurrent streams or threads)
  * race: serialize them.  With the same settings and samples_per_wave the
- * film equals slrgpu_render's. */
+ * film equals slrgpu_render's.  SLRGPU_FLAG_PROFILE_KERNELS has no effect
+ * here (there are no statistics to fill), and SLRGPU_FLAG_BPT is refused
+ * (SLRGPU_ERR_UNSUPPORTED). */
 int slrgpu_render_noalloc(slrgpu_handle scene, const slrgpu_settings* settings, float* film_device, void* stream);
 uint64_t slrgpu_render_noalloc_scratch_bytes(void);
 
