@@ -26,6 +26,11 @@ struct Bsdf {
     Spec a, b, c;          // see MaterialKind
     float ax, ay;
     bool dispersive;       // SpecularBSDF built while no wavelength is selected
+    // Fresnel-pair kinds (prepareIorPairs): the slot of each wavelength's
+    // index pair, 2 bits each, the number of slots (0: evaluate every
+    // wavelength) and the pairs of the slots
+    uint32_t iorSlots, iorCount;
+    float iorX[4], iorY[4];
 };
 
 struct BsdfQuery {
@@ -110,6 +115,121 @@ __device__ __forceinline__ void fresnelDielectric(const Spec &etaExt, const Spec
     for (int i = 0; i < kNumLambda; ++i) out.v[i] = fresnelDielectric1(etaExt.v[i], etaInt.v[i], cosEnter);
 }
 
+// ---- distinct index pairs of a BSDF's Fresnel spectra ----
+// The Fresnel terms take a pair of spectra per wavelength: (eta, k) of a
+// conductor, (exterior, interior) indices of a dielectric.  A spectrum that
+// is flat in the scene description still differs between the 16 wavelengths
+// by the rounding of its interpolation (one unit in the last place either
+// way), so a path sees two or three distinct pairs.  prepareIorPairs finds
+// them, bit for bit, up to kIorPairSlots, when the BSDF is made;
+// evalIorPairs then evaluates a per-wavelength term once per distinct pair
+// and hands its value to every wavelength of that pair, which is the value
+// that wavelength's own evaluation gives.  With more distinct pairs (a
+// dispersive medium) every wavelength is evaluated on its own.  The pair
+// spectra are (a, b) of the GGX kinds and (b, c) of the specular kinds.
+#ifndef SLRGPU_IOR_PAIRS
+#define SLRGPU_IOR_PAIRS 1
+#endif
+// material kinds that look for pairs (bit = MaterialKind)
+#ifndef SLRGPU_IOR_PAIR_KINDS
+#define SLRGPU_IOR_PAIR_KINDS 0x10u
+#endif
+#ifndef SLRGPU_IOR_PAIR_SLOTS
+#define SLRGPU_IOR_PAIR_SLOTS 4
+#endif
+constexpr int kIorPairSlots = SLRGPU_IOR_PAIR_SLOTS;
+static_assert(kIorPairSlots >= 1 && kIorPairSlots <= 4, "pair slots take 2 bits per wavelength");
+
+__device__ __forceinline__ void prepareIorPairs(Bsdf &B, const Spec &X, const Spec &Y) {
+    uint32_t kx[4] = {0, 0, 0, 0}, ky[4] = {0, 0, 0, 0};
+    uint32_t n = 0, slots = 0;
+    bool fits = SLRGPU_IOR_PAIRS != 0;
+#pragma unroll
+    for (int i = 0; i < kNumLambda; ++i) {
+        const uint32_t x = __float_as_uint(X.v[i]), y = __float_as_uint(Y.v[i]);
+        uint32_t s = kIorPairSlots;
+#pragma unroll
+        for (int k = kIorPairSlots - 1; k >= 0; --k)
+            if ((uint32_t)k < n && kx[k] == x && ky[k] == y) s = (uint32_t)k;
+        if (s == kIorPairSlots) {
+            if (n == kIorPairSlots) {
+                fits = false;
+                s = 0;
+            } else {
+#pragma unroll
+                for (int k = 0; k < kIorPairSlots; ++k)
+                    if ((uint32_t)k == n) { kx[k] = x; ky[k] = y; }
+                s = n++;
+            }
+        }
+        slots |= s << (2 * i);
+    }
+    B.iorSlots = slots;
+    B.iorCount = fits ? n : 0u;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        B.iorX[k] = __uint_as_float(kx[k]);
+        B.iorY[k] = __uint_as_float(ky[k]);
+    }
+}
+
+// The pair spectra of the BSDF's kind, for the kinds where looking for
+// pairs pays (the conductor's Fresnel term costs less than the search).
+__device__ __forceinline__ void prepareIorPairs(Bsdf &B) {
+    B.iorCount = 0u;
+    if (!((SLRGPU_IOR_PAIR_KINDS >> B.kind) & 1u)) return;
+    if (B.kind == kMatGGXReflection || B.kind == kMatGGXScattering) prepareIorPairs(B, B.a, B.b);
+    else if (B.kind == kMatSpecularReflection || B.kind == kMatSpecularScattering) prepareIorPairs(B, B.b, B.c);
+}
+
+// out.v[i] = fn(X.v[i], Y.v[i]) for every wavelength, X and Y the pair
+// spectra B was prepared with.  UNROLL picks the shape of the per-wavelength
+// loop when the pairs did not fit (unrolled for short terms, rolled for
+// long ones).
+template <bool UNROLL, class FN>
+__device__ __forceinline__ void evalIorPairs(const Bsdf &B, const Spec &X, const Spec &Y, FN fn, Spec &out) {
+    const uint32_t n = B.iorCount;
+    if (n == 0) {
+        if constexpr (UNROLL) {
+#pragma unroll
+            for (int i = 0; i < kNumLambda; ++i) out.v[i] = fn(X.v[i], Y.v[i]);
+        } else {
+#pragma unroll 1
+            for (int i = 0; i < kNumLambda; ++i) out.v[i] = fn(X.v[i], Y.v[i]);
+        }
+        return;
+    }
+    float val[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+#pragma unroll 1
+    for (uint32_t j = 0; j < n; ++j) {
+        float x = B.iorX[0], y = B.iorY[0];
+#pragma unroll
+        for (int k = 1; k < kIorPairSlots; ++k)
+            if (j == (uint32_t)k) { x = B.iorX[k]; y = B.iorY[k]; }
+        const float v = fn(x, y);
+#pragma unroll
+        for (int k = 0; k < kIorPairSlots; ++k)
+            if (j == (uint32_t)k) val[k] = v;
+    }
+#pragma unroll
+    for (int i = 0; i < kNumLambda; ++i) {
+        const uint32_t s = (B.iorSlots >> (2 * i)) & 3u;
+        out.v[i] = s == 0 ? val[0] : s == 1 ? val[1] : s == 2 ? val[2] : val[3];
+    }
+}
+
+// fresnelConductor / fresnelDielectric over the pair spectra of B.
+__device__ __forceinline__ void fresnelConductorPairs(const Bsdf &B, const Spec &eta, const Spec &k, float cosEnter,
+                                                      Spec &F) {
+    evalIorPairs<true>(B, eta, k, [cosEnter](float e, float kk) { return fresnelConductor1(e, kk, cosEnter); }, F);
+}
+
+__device__ __forceinline__ void fresnelDielectricPairs(const Bsdf &B, const Spec &etaExt, const Spec &etaInt,
+                                                       float cosEnter, Spec &F) {
+    evalIorPairs<true>(B, etaExt, etaInt,
+                       [cosEnter](float eExt, float eInt) { return fresnelDielectric1(eExt, eInt, cosEnter); }, F);
+}
+
 // ---- GGX (directional_distribution_functions.cpp:247-315) ----
 __device__ __forceinline__ float ggxD(float ax, float ay, V3 m) {
     if (m.z <= 0) return 0.0f;
@@ -125,6 +245,29 @@ __device__ __forceinline__ float ggxG1(float ax, float ay, V3 v, V3 m) {
 
 __device__ __forceinline__ float ggxPdf(float ax, float ay, V3 v, V3 m) {
     return ggxG1(ax, ay, v, m) * absDot(v, m) * ggxD(ax, ay, m) / fabsf(v.z);
+}
+
+// Transmission term of the rough dielectric B between v and l at every
+// wavelength, with each wavelength's own half vector
+// (microfacet_bsdfs.cpp:187-199, :239-250); r = 1 / |v.z l.z|; an adjoint
+// query scales by the exit index squared instead of the entry index's.
+// Rolled when evaluated per wavelength: 16 copies of the half-vector math
+// overflow the instruction cache of the shading kernel.
+__device__ __forceinline__ void ggxTransmitPairs(const Bsdf &B, bool entering, V3 v, V3 l, float r, Spec &fs,
+                                                 bool adjoint = false) {
+    const float ax = B.ax, ay = B.ay;
+    evalIorPairs<false>(B, B.a, B.b, [=](float eExt, float eInt) {
+        float eEnter = entering ? eExt : eInt;
+        float eExit = entering ? eInt : eExt;
+        V3 mw = normalize(-(eEnter * v + eExit * l));
+        float dHV = dot(v, mw), dHL = dot(l, mw);
+        float Fw = fresnelDielectric1(eExt, eInt, dHV);
+        float Gw = ggxG1(ax, ay, v, mw) * ggxG1(ax, ay, l, mw);
+        float Dw = ggxD(ax, ay, mw);
+        float dd = eEnter * dHV + eExit * dHL;
+        float val = fabsf(dHV * dHL) * (1 - Fw) * Gw * Dw / (dd * dd);
+        return (val * r) * (adjoint ? eExit * eExit : eEnter * eEnter);
+    }, fs);
 }
 
 // Visible-normal sampling (Heitz 2017, "A Simpler and Exact Sampling Routine
@@ -184,7 +327,7 @@ __device__ __forceinline__ void bsdfSampleBody(const Bsdf &B, const BsdfQuery &q
         res->pdf = 1.0f;
         res->type = kDirReflection | kDirDelta0D;
         Spec F;
-        fresnelConductor(B.b, B.c, q.dir.z, F);
+        fresnelConductorPairs(B, B.b, B.c, q.dir.z, F);
         float r = 1.0f / fabsf(q.dir.z);
 #pragma unroll
         for (int i = 0; i < kNumLambda; ++i) fs.v[i] = (B.a.v[i] * F.v[i]) * r;
@@ -192,7 +335,7 @@ __device__ __forceinline__ void bsdfSampleBody(const Bsdf &B, const BsdfQuery &q
     }
     case kMatSpecularScattering: {  // basic_bsdfs.cpp:99-150
         Spec F;
-        fresnelDielectric(B.b, B.c, q.dir.z, F);
+        fresnelDielectricPairs(B, B.b, B.c, q.dir.z, F);
         float reflectProb = importance(F, q.wl);
         if (uc < reflectProb) {
             if (q.dir.z == 0.0f) return;
@@ -239,7 +382,7 @@ __device__ __forceinline__ void bsdfSampleBody(const Bsdf &B, const BsdfQuery &q
         res->pdf = common * mPdf;
         res->type = kDirReflection | kDirHighFreq;
         Spec F;
-        fresnelConductor(B.a, B.b, dotHV, F);
+        fresnelConductorPairs(B, B.a, B.b, dotHV, F);
         float G = ggxG1(B.ax, B.ay, q.dir, m) * ggxG1(B.ax, B.ay, d, m);
         float r = 1.0f / (4 * q.dir.z * d.z);
 #pragma unroll
@@ -255,7 +398,7 @@ __device__ __forceinline__ void bsdfSampleBody(const Bsdf &B, const BsdfQuery &q
         float dotHV = dot(q.dir, m);
         if (dotHV * sign <= 0 || isnan(D)) return;
         Spec F;
-        fresnelDielectric(B.a, B.b, dotHV, F);
+        fresnelDielectricPairs(B, B.a, B.b, dotHV, F);
         float reflectProb = importance(F, q.wl);
         if (uc < reflectProb) {
             V3 d = (2 * dotHV) * m - q.dir;
@@ -285,21 +428,7 @@ __device__ __forceinline__ void bsdfSampleBody(const Bsdf &B, const BsdfQuery &q
         res->pdf = common * mPdf * eExitW * eExitW * fabsf(dotHL);
         res->type = kDirTransmission | kDirHighFreq;
         float r = 1.0f / fabsf(q.dir.z * d.z);
-        // Kept rolled: 16 copies of the refraction half-vector math overflow
-        // the instruction cache of the shading kernel.
-#pragma unroll 1
-        for (int i = 0; i < kNumLambda; ++i) {
-            float eEnter = entering ? B.a.v[i] : B.b.v[i];
-            float eExit = entering ? B.b.v[i] : B.a.v[i];
-            V3 mw = normalize(-(eEnter * q.dir + eExit * d));
-            float dHV = dot(q.dir, mw), dHL = dot(d, mw);
-            float Fw = fresnelDielectric1(B.a.v[i], B.b.v[i], dHV);
-            float Gw = ggxG1(B.ax, B.ay, q.dir, mw) * ggxG1(B.ax, B.ay, d, mw);
-            float Dw = ggxD(B.ax, B.ay, mw);
-            float dd = eEnter * dHV + eExit * dHL;
-            float val = fabsf(dHV * dHL) * (1 - Fw) * Gw * Dw / (dd * dd);
-            fs.v[i] = (val * r) * (eEnter * eEnter);
-        }
+        ggxTransmitPairs(B, entering, q.dir, d, r, fs);
         return;
     }
     default:
@@ -323,7 +452,7 @@ __device__ __forceinline__ void bsdfEvalBody(const Bsdf &B, const BsdfQuery &q, 
         float dotHV = dot(q.dir, m);
         float D = ggxD(B.ax, B.ay, m);
         Spec F;
-        fresnelConductor(B.a, B.b, dotHV, F);
+        fresnelConductorPairs(B, B.a, B.b, dotHV, F);
         float G = ggxG1(B.ax, B.ay, q.dir, m) * ggxG1(B.ax, B.ay, dir, m);
         float r = 1.0f / (4 * q.dir.z * dir.z);
 #pragma unroll
@@ -339,26 +468,14 @@ __device__ __forceinline__ void bsdfEvalBody(const Bsdf &B, const BsdfQuery &q, 
             float dotHV = dot(q.dir, m);
             float D = ggxD(B.ax, B.ay, m);
             Spec F;
-            fresnelDielectric(B.a, B.b, dotHV, F);
+            fresnelDielectricPairs(B, B.a, B.b, dotHV, F);
             float G = ggxG1(B.ax, B.ay, q.dir, m) * ggxG1(B.ax, B.ay, dir, m);
             float r = 1.0f / (4 * dNVNL);
 #pragma unroll
             for (int i = 0; i < kNumLambda; ++i) fs.v[i] = ((F.v[i] * D) * G) * r;
         } else if (dNVNL < 0) {
             float r = 1.0f / fabsf(dNVNL);
-#pragma unroll 1
-            for (int i = 0; i < kNumLambda; ++i) {
-                float eEnter = entering ? B.a.v[i] : B.b.v[i];
-                float eExit = entering ? B.b.v[i] : B.a.v[i];
-                V3 mw = normalize(-(eEnter * q.dir + eExit * dir));
-                float dHV = dot(q.dir, mw), dHL = dot(dir, mw);
-                float Fw = fresnelDielectric1(B.a.v[i], B.b.v[i], dHV);
-                float Gw = ggxG1(B.ax, B.ay, q.dir, mw) * ggxG1(B.ax, B.ay, dir, mw);
-                float Dw = ggxD(B.ax, B.ay, mw);
-                float dd = eEnter * dHV + eExit * dHL;
-                float val = fabsf(dHV * dHL) * (1 - Fw) * Gw * Dw / (dd * dd);
-                fs.v[i] = (val * r) * (eEnter * eEnter);
-            }
+            ggxTransmitPairs(B, entering, q.dir, dir, r, fs);
         }
         return;
     }
@@ -397,7 +514,7 @@ __device__ __forceinline__ float bsdfPdfBody(const Bsdf &B, const BsdfQuery &q, 
         if (dotHV * sign <= 0) return 0.0f;
         float mPdf = ggxPdf(B.ax, B.ay, sign * q.dir, m);
         Spec F;
-        fresnelDielectric(B.a, B.b, dotHV, F);
+        fresnelDielectricPairs(B, B.a, B.b, dotHV, F);
         float reflectProb = importance(F, q.wl);
         if (dNVNL > 0) {
             float common = reflectProb / (4 * dotHV * sign);

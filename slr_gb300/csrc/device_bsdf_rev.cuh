@@ -53,7 +53,7 @@ static __device__ __noinline__ void bsdfSampleRev(const Bsdf &B, const RevQuery 
         res->pdf = 1.0f;
         res->type = kDirReflection | kDirDelta0D;
         Spec F;
-        fresnelConductor(B.b, B.c, q.dir.z, F);
+        fresnelConductorPairs(B, B.b, B.c, q.dir.z, F);
         float r = 1.0f / fabsf(q.dir.z);
 #pragma unroll
         for (int i = 0; i < kNumLambda; ++i) fs.v[i] = (B.a.v[i] * F.v[i]) * r;
@@ -63,7 +63,7 @@ static __device__ __noinline__ void bsdfSampleRev(const Bsdf &B, const RevQuery 
     }
     case kMatSpecularScattering: {
         Spec F;
-        fresnelDielectric(B.b, B.c, q.dir.z, F);
+        fresnelDielectricPairs(B, B.b, B.c, q.dir.z, F);
         float reflectProb = importance(F, q.wl);
         if (uc < reflectProb) {
             if (q.dir.z == 0.0f) return;
@@ -118,7 +118,7 @@ static __device__ __noinline__ void bsdfSampleRev(const Bsdf &B, const RevQuery 
         res->pdf = common * mPdf;
         res->type = kDirReflection | kDirHighFreq;
         Spec F;
-        fresnelConductor(B.a, B.b, dotHV, F);
+        fresnelConductorPairs(B, B.a, B.b, dotHV, F);
         float G = ggxG1(B.ax, B.ay, q.dir, m) * ggxG1(B.ax, B.ay, d, m);
         float r = 1.0f / (4 * q.dir.z * d.z);
 #pragma unroll
@@ -136,7 +136,7 @@ static __device__ __noinline__ void bsdfSampleRev(const Bsdf &B, const RevQuery 
         float dotHV = dot(q.dir, m);
         if (dotHV * sign <= 0 || isnan(D)) return;
         Spec F;
-        fresnelDielectric(B.a, B.b, dotHV, F);
+        fresnelDielectricPairs(B, B.a, B.b, dotHV, F);
         float reflectProb = importance(F, q.wl);
         if (uc < reflectProb) {
             V3 d = (2 * dotHV) * m - q.dir;
@@ -168,19 +168,7 @@ static __device__ __noinline__ void bsdfSampleRev(const Bsdf &B, const RevQuery 
         res->pdf = common * mPdf * eExitW * eExitW * fabsf(dotHL);
         res->type = kDirTransmission | kDirHighFreq;
         float r = 1.0f / fabsf(q.dir.z * d.z);
-#pragma unroll 1
-        for (int i = 0; i < kNumLambda; ++i) {
-            float eEnter = entering ? B.a.v[i] : B.b.v[i];
-            float eExit = entering ? B.b.v[i] : B.a.v[i];
-            V3 mw = normalize(-(eEnter * q.dir + eExit * d));
-            float dHV = dot(q.dir, mw), dHL = dot(d, mw);
-            float Fw = fresnelDielectric1(B.a.v[i], B.b.v[i], dHV);
-            float Gw = ggxG1(B.ax, B.ay, q.dir, mw) * ggxG1(B.ax, B.ay, d, mw);
-            float Dw = ggxD(B.ax, B.ay, mw);
-            float dd = eEnter * dHV + eExit * dHL;
-            float val = fabsf(dHV * dHL) * (1 - Fw) * Gw * Dw / (dd * dd);
-            fs.v[i] = (val * r) * (q.adjoint ? eExit * eExit : eEnter * eEnter);
-        }
+        ggxTransmitPairs(B, entering, q.dir, d, r, fs, q.adjoint);
         *revPdf = common * ggxPdf(B.ax, B.ay, -sign * d, m) * eEnterW * eEnterW * fabsf(dotHV);
         revFs = fs;
         break;
@@ -211,7 +199,7 @@ static __device__ __noinline__ void bsdfEvalRev(const Bsdf &B, const RevQuery &q
         float dotHV = dot(q.dir, m);
         float D = ggxD(B.ax, B.ay, m);
         Spec F;
-        fresnelConductor(B.a, B.b, dotHV, F);
+        fresnelConductorPairs(B, B.a, B.b, dotHV, F);
         float G = ggxG1(B.ax, B.ay, q.dir, m) * ggxG1(B.ax, B.ay, dir, m);
         float r = 1.0f / (4 * q.dir.z * dir.z);
 #pragma unroll
@@ -227,26 +215,14 @@ static __device__ __noinline__ void bsdfEvalRev(const Bsdf &B, const RevQuery &q
             float dotHV = dot(q.dir, m);
             float D = ggxD(B.ax, B.ay, m);
             Spec F;
-            fresnelDielectric(B.a, B.b, dotHV, F);
+            fresnelDielectricPairs(B, B.a, B.b, dotHV, F);
             float G = ggxG1(B.ax, B.ay, q.dir, m) * ggxG1(B.ax, B.ay, dir, m);
             float r = 1.0f / (4 * dNVNL);
 #pragma unroll
             for (int i = 0; i < kNumLambda; ++i) fs.v[i] = ((F.v[i] * D) * G) * r;
         } else if (dNVNL < 0) {
             float r = 1.0f / fabsf(dNVNL);
-#pragma unroll 1
-            for (int i = 0; i < kNumLambda; ++i) {
-                float eEnter = entering ? B.a.v[i] : B.b.v[i];
-                float eExit = entering ? B.b.v[i] : B.a.v[i];
-                V3 mw = normalize(-(eEnter * q.dir + eExit * dir));
-                float dHV = dot(q.dir, mw), dHL = dot(dir, mw);
-                float Fw = fresnelDielectric1(B.a.v[i], B.b.v[i], dHV);
-                float Gw = ggxG1(B.ax, B.ay, q.dir, mw) * ggxG1(B.ax, B.ay, dir, mw);
-                float Dw = ggxD(B.ax, B.ay, mw);
-                float dd = eEnter * dHV + eExit * dHL;
-                float val = fabsf(dHV * dHL) * (1 - Fw) * Gw * Dw / (dd * dd);
-                fs.v[i] = (val * r) * (q.adjoint ? eExit * eExit : eEnter * eEnter);
-            }
+            ggxTransmitPairs(B, entering, q.dir, dir, r, fs, q.adjoint);
         }
         break;
     }
@@ -293,7 +269,7 @@ static __device__ __noinline__ float bsdfPdfRev(const Bsdf &B, const RevQuery &q
         if (dotHV * sign <= 0) return 0.0f;
         float mPdf = ggxPdf(B.ax, B.ay, sign * q.dir, m);
         Spec F;
-        fresnelDielectric(B.a, B.b, dotHV, F);
+        fresnelDielectricPairs(B, B.a, B.b, dotHV, F);
         float reflectProb = importance(F, q.wl);
         if (dNVNL > 0) {
             float common = reflectProb / (4 * dotHV * sign);

@@ -184,6 +184,7 @@ static __device__ __noinline__ void makeBsdf(const DevScene &sc, const DevMateri
     default:
         break;
     }
+    prepareIorPairs(B);
 }
 
 struct SurfPoint {
@@ -286,6 +287,12 @@ __device__ __forceinline__ void makeBsdfK(const DevScene &sc, const DevMaterial 
     evalSpectrum(sc, m.spec[0], lambdas, B.a);
     if (K != kMatMatte) evalSpectrum(sc, m.spec[1], lambdas, B.b);
     if (K == kMatSpecularReflection || K == kMatSpecularScattering) evalSpectrum(sc, m.spec[2], lambdas, B.c);
+    if constexpr (((SLRGPU_IOR_PAIR_KINDS >> K) & 1u) != 0) {
+        if (K == kMatGGXReflection || K == kMatGGXScattering) prepareIorPairs(B, B.a, B.b);
+        else prepareIorPairs(B, B.b, B.c);
+    } else {
+        B.iorCount = 0u;
+    }
 }
 
 }  // namespace slrgpu

@@ -1131,6 +1131,7 @@ __global__ void kMediumQuery(DevScene sc, int mode, uint32_t n, const float* __r
 }
 
 __global__ void kBsdfQuery(Bsdf B, const float* __restrict__ q, uint32_t n, float* __restrict__ o) {
+    prepareIorPairs(B);
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const float* qi = q + 16 * (size_t)i;
         float* oi = o + 40 * (size_t)i;
