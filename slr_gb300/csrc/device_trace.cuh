@@ -226,61 +226,98 @@ __device__ __forceinline__ TriFrag loadFrag(const TriFrag* __restrict__ frags, u
     return f;
 }
 
-// Closest hit over [tmin, tmax].  Returns false on stack overflow (the hit
-// found so far is still reported).  WT: the watertight triangle test with
-// conservative box tests, compiled separately so that the default walk
-// carries none of it.
+// A closest-hit walk over [tmin, tmax] that can stop after a number of node
+// or leaf visits and resume later: the wave kernels give a lane a new ray as
+// soon as its walk ends, instead of leaving it idle until the longest walk of
+// its warp is done.  Nodes and triangles are visited in the order of an
+// uninterrupted walk, so the hit is the same.  WT: the watertight triangle
+// test with conservative box tests.
 template <bool WT>
-__device__ __forceinline__ bool traceClosestT(const DevScene &sc, V3 org, V3 dir, float tmin, float tmax, Hit* hit) {
-    hit->prim = kNoHit;
-    hit->t = __int_as_float(0x7f800000);
-    hit->b1 = hit->b2 = 0.0f;
-    V3 inv = V3{__fdiv_rn(1.0f, dir.x), __fdiv_rn(1.0f, dir.y), __fdiv_rn(1.0f, dir.z)};
+struct ClosestWalk {
+    V3 org, dir, inv;
     WtRay wr;
-    if (WT) wr = wtSetup(org, dir);
-    StackEntry stack[kTraceStack];
-    int sp = 0;
-    uint32_t cur = 0;
-    bool ok = true;
-    if (sc.numPrims == 0) return true;
-    for (;;) {
-        if (!(cur & kLeafBit)) {
-            float tn[kBvhWidth];
-            uint32_t ch[kBvhWidth];
-            uint32_t mask = testChildren<WT>(sc.nodes, cur, org, inv, tmin, tmax, tn, ch);
-            if (mask == 0) goto pop;
-            cur = orderChildren(mask, tn, ch, stack, sp, ok);
-            continue;
-        } else {
-            uint32_t first = cur & kLeafFirstMask;
-            uint32_t count = ((cur >> kLeafCountShift) & 0x1f) + 1;
-            for (uint32_t i = 0; i < count; ++i) {
-                float t, b1, b2;
-                uint32_t prim;
-                bool h;
-                if (WT) {
-                    h = wtIntersect(sc.wtVerts, first + i, wr, tmin, tmax, &t, &b1, &b2, &prim);
-                } else {
-                    TriFrag f = loadFrag(sc.frags, first + i);
-                    h = mtIntersect(f, org, dir, tmin, tmax, &t, &b1, &b2);
-                    prim = f.prim;
+    float tmin, tmax;
+    Hit hit;
+    uint32_t cur;
+    int sp;
+    bool ok;   // false after a stack overflow (the hit found so far is kept)
+
+    // Returns true when the walk has already ended (an empty scene).
+    __device__ __forceinline__ bool begin(const DevScene &sc, V3 o, V3 d, float t0, float t1) {
+        hit.prim = kNoHit;
+        hit.t = __int_as_float(0x7f800000);
+        hit.b1 = hit.b2 = 0.0f;
+        org = o;
+        dir = d;
+        inv = V3{__fdiv_rn(1.0f, d.x), __fdiv_rn(1.0f, d.y), __fdiv_rn(1.0f, d.z)};
+        if (WT) wr = wtSetup(o, d);
+        tmin = t0;
+        tmax = t1;
+        cur = 0;
+        sp = 0;
+        ok = true;
+        return sc.numPrims == 0;
+    }
+
+    // At most `visits` node or leaf visits; returns true when the walk has ended.
+    __device__ __forceinline__ bool advance(const DevScene &sc, StackEntry* stack, int visits) {
+        for (int v = 0; v < visits; ++v) {
+            if (!(cur & kLeafBit)) {
+                float tn[kBvhWidth];
+                uint32_t ch[kBvhWidth];
+                const uint32_t mask = testChildren<WT>(sc.nodes, cur, org, inv, tmin, tmax, tn, ch);
+                if (mask != 0) {
+                    cur = orderChildren(mask, tn, ch, stack, sp, ok);
+                    continue;
                 }
-                if (h) {
-                    tmax = t;
-                    hit->t = t;
-                    hit->b1 = b1;
-                    hit->b2 = b2;
-                    hit->prim = prim;
+            } else {
+                const uint32_t first = cur & kLeafFirstMask;
+                const uint32_t count = ((cur >> kLeafCountShift) & 0x1f) + 1;
+                for (uint32_t i = 0; i < count; ++i) {
+                    float t, b1, b2;
+                    uint32_t prim;
+                    bool h;
+                    if (WT) {
+                        h = wtIntersect(sc.wtVerts, first + i, wr, tmin, tmax, &t, &b1, &b2, &prim);
+                    } else {
+                        TriFrag f = loadFrag(sc.frags, first + i);
+                        h = mtIntersect(f, org, dir, tmin, tmax, &t, &b1, &b2);
+                        prim = f.prim;
+                    }
+                    if (h) {
+                        tmax = t;
+                        hit.t = t;
+                        hit.b1 = b1;
+                        hit.b2 = b2;
+                        hit.prim = prim;
+                    }
+                }
+            }
+            // the nearest pushed node the ray can still reach
+            for (;;) {
+                if (sp == 0) return true;
+                const StackEntry e = stack[--sp];
+                if (e.tnear <= tmax) {
+                    cur = e.node;
+                    break;
                 }
             }
         }
-    pop:
-        for (;;) {
-            if (sp == 0) return ok;
-            StackEntry e = stack[--sp];
-            if (e.tnear <= tmax) { cur = e.node; break; }
-        }
+        return false;
     }
+};
+
+// Closest hit over [tmin, tmax] in one go.  Returns false on stack overflow
+// (the hit found so far is still reported).
+template <bool WT>
+__device__ __forceinline__ bool traceClosestT(const DevScene &sc, V3 org, V3 dir, float tmin, float tmax, Hit* hit) {
+    StackEntry stack[kTraceStack];
+    ClosestWalk<WT> w;
+    if (!w.begin(sc, org, dir, tmin, tmax))
+        while (!w.advance(sc, stack, 1 << 30)) {
+        }
+    *hit = w.hit;
+    return w.ok;
 }
 
 __device__ __forceinline__ bool traceClosest(const DevScene &sc, V3 org, V3 dir, float tmin, float tmax, Hit* hit) {
@@ -288,48 +325,84 @@ __device__ __forceinline__ bool traceClosest(const DevScene &sc, V3 org, V3 dir,
                          : traceClosestT<false>(sc, org, dir, tmin, tmax, hit);
 }
 
+// An any-hit walk over [tmin, tmax] that can stop and resume like
+// ClosestWalk; `occluded` holds the answer once the walk has ended.
+template <bool WT>
+struct AnyWalk {
+    V3 org, dir, inv;
+    WtRay wr;
+    float tmin, tmax;
+    uint32_t cur;
+    int sp;
+    bool occluded;
+
+    __device__ __forceinline__ bool begin(const DevScene &sc, V3 o, V3 d, float t0, float t1) {
+        org = o;
+        dir = d;
+        inv = V3{__fdiv_rn(1.0f, d.x), __fdiv_rn(1.0f, d.y), __fdiv_rn(1.0f, d.z)};
+        if (WT) wr = wtSetup(o, d);
+        tmin = t0;
+        tmax = t1;
+        cur = 0;
+        sp = 0;
+        occluded = false;
+        return sc.numPrims == 0;
+    }
+
+    __device__ __forceinline__ bool advance(const DevScene &sc, uint32_t* stack, int visits) {
+        for (int v = 0; v < visits; ++v) {
+            if (!(cur & kLeafBit)) {
+                float tn[kBvhWidth];
+                uint32_t ch[kBvhWidth];
+                const uint32_t mask = testChildren<WT>(sc.nodes, cur, org, inv, tmin, tmax, tn, ch);
+                bool have = false;
+                uint32_t next = 0;
+#pragma unroll
+                for (int k = 0; k < kBvhWidth; ++k) {
+                    if (mask & (1u << k)) {
+                        if (!have) { next = ch[k]; have = true; }
+                        else if (sp < kTraceStack) stack[sp++] = ch[k];
+                    }
+                }
+                if (have) {
+                    cur = next;
+                    continue;
+                }
+            } else {
+                const uint32_t first = cur & kLeafFirstMask;
+                const uint32_t count = ((cur >> kLeafCountShift) & 0x1f) + 1;
+                for (uint32_t i = 0; i < count; ++i) {
+                    float t, b1, b2;
+                    bool h;
+                    if (WT) {
+                        uint32_t prim;
+                        h = wtIntersect(sc.wtVerts, first + i, wr, tmin, tmax, &t, &b1, &b2, &prim);
+                    } else {
+                        TriFrag f = loadFrag(sc.frags, first + i);
+                        h = mtIntersect(f, org, dir, tmin, tmax, &t, &b1, &b2);
+                    }
+                    if (h) {
+                        occluded = true;
+                        return true;
+                    }
+                }
+            }
+            if (sp == 0) return true;
+            cur = stack[--sp];
+        }
+        return false;
+    }
+};
+
 // Any hit over [tmin, tmax]: true when the segment is occluded.
 template <bool WT>
 __device__ __forceinline__ bool traceAnyT(const DevScene &sc, V3 org, V3 dir, float tmin, float tmax) {
-    if (sc.numPrims == 0) return false;
-    V3 inv = V3{__fdiv_rn(1.0f, dir.x), __fdiv_rn(1.0f, dir.y), __fdiv_rn(1.0f, dir.z)};
-    WtRay wr;
-    if (WT) wr = wtSetup(org, dir);
     uint32_t stack[kTraceStack];
-    int sp = 0;
-    uint32_t cur = 0;
-    for (;;) {
-        if (!(cur & kLeafBit)) {
-            float tn[kBvhWidth];
-            uint32_t ch[kBvhWidth];
-            uint32_t mask = testChildren<WT>(sc.nodes, cur, org, inv, tmin, tmax, tn, ch);
-            bool have = false;
-            uint32_t next = 0;
-#pragma unroll
-            for (int k = 0; k < kBvhWidth; ++k) {
-                if (mask & (1u << k)) {
-                    if (!have) { next = ch[k]; have = true; }
-                    else if (sp < kTraceStack) stack[sp++] = ch[k];
-                }
-            }
-            if (have) { cur = next; continue; }
-        } else {
-            uint32_t first = cur & kLeafFirstMask;
-            uint32_t count = ((cur >> kLeafCountShift) & 0x1f) + 1;
-            for (uint32_t i = 0; i < count; ++i) {
-                float t, b1, b2;
-                if (WT) {
-                    uint32_t prim;
-                    if (wtIntersect(sc.wtVerts, first + i, wr, tmin, tmax, &t, &b1, &b2, &prim)) return true;
-                } else {
-                    TriFrag f = loadFrag(sc.frags, first + i);
-                    if (mtIntersect(f, org, dir, tmin, tmax, &t, &b1, &b2)) return true;
-                }
-            }
-        }
-        if (sp == 0) return false;
-        cur = stack[--sp];
+    AnyWalk<WT> w;
+    if (w.begin(sc, org, dir, tmin, tmax)) return false;
+    while (!w.advance(sc, stack, 1 << 30)) {
     }
+    return w.occluded;
 }
 
 __device__ __forceinline__ bool traceAny(const DevScene &sc, V3 org, V3 dir, float tmin, float tmax) {

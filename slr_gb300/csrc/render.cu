@@ -125,17 +125,21 @@ struct WaveParams {
 // Per-bounce counter block: [0, kNumClassQueues - 1) paths per shading
 // class, kCtrExt paths in the extension queue of the bounce, kCtrShadow
 // shadow rays, kCtrMedShadow shadow rays waiting for their transmittance,
-// kCtrMedTake the transmittance kernel's work counter.
+// kCtrMedTake the transmittance kernel's work counter, kCtrExtTake and
+// kCtrShadowTake the work counters of the surface tracer's extension and
+// shadow kernels.  The first kQueueCountColumns are the diagnostics rows.
 constexpr int kNumShadeClasses = 6;   // the five material kinds + environment / miss
 constexpr int kClassMiss = 5;
 constexpr int kClassMedium = 6;       // volumetric: a scattering point in the medium
 constexpr int kQueueMedShadow = 7;    // volumetric: unoccluded shadow rays waiting for their transmittance
 constexpr int kNumClassQueues = 8;
-constexpr int kCtrStride = 11;
+constexpr int kCtrStride = 13;
 constexpr int kCtrExt = 7;
 constexpr int kCtrShadow = 8;
 constexpr int kCtrMedShadow = 9;
 constexpr int kCtrMedTake = 10;
+constexpr int kCtrExtTake = 11;
+constexpr int kCtrShadowTake = 12;
 // hit.w of a path whose ray stopped at a collision in the medium (hit.x = its
 // distance, hit.y = 1 inside the density grid's unit cube)
 constexpr uint32_t kMediumHit = 0xfffffffeu;
@@ -233,12 +237,86 @@ __global__ void kExtend(DevScene sc, WaveState ws, const uint32_t* __restrict__ 
 #ifndef SLRGPU_TRACE_MIN_BLOCKS
 #define SLRGPU_TRACE_MIN_BLOCKS 4
 #endif
+// Dynamic ray fetch in the surface tracer's traversal kernels (Aila and
+// Laine, "Understanding the Efficiency of Ray Traversal on GPUs", HPG 2009):
+// each warp takes rays from the bounce's queue through a work counter, and
+// once SLRGPU_TRACE_REFILL_LANES of its lanes have finished their walks
+// they take new rays while the others go on walking; walks advance
+// SLRGPU_TRACE_REFILL_VISITS node visits between two looks.  0 turns it off
+// (one ray per lane and grid-stride loop).
+#ifndef SLRGPU_TRACE_REFILL
+#define SLRGPU_TRACE_REFILL 1
+#endif
+#ifndef SLRGPU_TRACE_REFILL_LANES
+#define SLRGPU_TRACE_REFILL_LANES 8
+#endif
+#ifndef SLRGPU_TRACE_REFILL_VISITS
+#define SLRGPU_TRACE_REFILL_VISITS 16
+#endif
+static_assert(SLRGPU_TRACE_REFILL_LANES >= 1 && SLRGPU_TRACE_REFILL_LANES <= 32, "a warp has 32 lanes");
+
+// The refill step of a warp: when at least SLRGPU_TRACE_REFILL_LANES lanes
+// are idle and the queue is not drained, the idle lanes take the next queue
+// entries (*slot = entry index, or n when there is none left).  Returns
+// whether this lane got one.  Called by all 32 lanes.
+__device__ __forceinline__ bool refillLanes(bool live, uint32_t* cursor, uint32_t n, bool &drained, uint32_t* slot) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t idle = __ballot_sync(0xffffffffu, !live);
+    if (drained || (uint32_t)__popc(idle) < SLRGPU_TRACE_REFILL_LANES) return false;
+    const int leader = __ffs(idle) - 1;
+    uint32_t base = 0;
+    if ((int)lane == leader) base = atomicAdd(cursor, (uint32_t)__popc(idle));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    drained = base + (uint32_t)__popc(idle) >= n;
+    if (live) return false;
+    *slot = base + (uint32_t)__popc(idle & ((1u << lane) - 1));
+    return *slot < n;
+}
+
+// Shadow rays (PTRenderer.cpp:196-217): an unoccluded ray adds its stored
+// contribution to the path's radiance.
+template <bool MULTI, bool WT>
+__device__ __forceinline__ void shadowRefill(const DevScene &scArg, const WaveState &ws,
+                                             const uint32_t* __restrict__ queue, uint32_t n, uint32_t* cursor,
+                                             const DevScene* __restrict__ scenes) {
+    uint32_t stack[kTraceStack];
+    AnyWalk<WT> walk;
+    uint32_t p = 0, info = 0;
+    bool live = false, drained = false;
+    for (;;) {
+        uint32_t slot;
+        bool fin = false;
+        if (refillLanes(live, cursor, n, drained, &slot)) {
+            p = queue[slot];
+            info = MULTI ? ws.ps[p].info : 0u;
+            const float4 o = ws.shRay[2 * (size_t)p], d = ws.shRay[2 * (size_t)p + 1];
+            fin = walk.begin(pathScene<MULTI>(scArg, scenes, info), V3{o.x, o.y, o.z}, V3{d.x, d.y, d.z}, o.w, d.w);
+            live = true;
+        }
+        if (live && !fin) fin = walk.advance(pathScene<MULTI>(scArg, scenes, info), stack, SLRGPU_TRACE_REFILL_VISITS);
+        if (live && fin) {
+            if (!walk.occluded) {
+                Spec c;
+                loadSpec(ws.shContrib, p, c);
+                addSpec(ws.L, p, c);
+            }
+            live = false;
+        }
+        if (drained && !__any_sync(0xffffffffu, live)) return;
+    }
+}
+
 template <bool MULTI>
 __global__ void __launch_bounds__(256, SLRGPU_TRACE_MIN_BLOCKS) kShadow(DevScene scArg, WaveState ws,
                                                                       const uint32_t* __restrict__ queue,
                                                                       const uint32_t* __restrict__ count,
+                                                                      uint32_t* cursor,
                                                                       const DevScene* __restrict__ scenes) {
     const uint32_t n = *count;
+#if SLRGPU_TRACE_REFILL
+    if (scArg.watertight) shadowRefill<MULTI, true>(scArg, ws, queue, n, cursor, scenes);
+    else shadowRefill<MULTI, false>(scArg, ws, queue, n, cursor, scenes);
+#else
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         uint32_t p = queue[i];
         const DevScene &sc = pathScene<MULTI>(scArg, scenes, MULTI ? ws.ps[p].info : 0u);
@@ -249,6 +327,7 @@ __global__ void __launch_bounds__(256, SLRGPU_TRACE_MIN_BLOCKS) kShadow(DevScene
             addSpec(ws.L, p, c);
         }
     }
+#endif
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&ws.stats[1], (unsigned long long)n);
 }
 
@@ -261,12 +340,57 @@ __global__ void __launch_bounds__(256, SLRGPU_TRACE_MIN_BLOCKS) kShadow(DevScene
 // divergence.  Emission with MIS, Russian roulette, next-event estimation and
 // BSDF sampling follow PTRenderer::Job::contribution (PTRenderer.cpp:145-277).
 // ---------------------------------------------------------------------------
+// Closest hits of the bounce's extension rays, each path pushed to the
+// queue of its shading class (material kind, or miss).
+template <bool MULTI>
+__device__ __forceinline__ void pushByClass(const WaveState &ws, uint32_t* classCounts, uint32_t p, int cls) {
+#pragma unroll
+    for (int c = 0; c < kNumShadeClasses; ++c)
+        queuePush(ws.classQueue + (size_t)c * ws.N, classCounts + c, p, cls == c);
+}
+
+template <bool MULTI, bool WT>
+__device__ __forceinline__ void extendRefill(const DevScene &scArg, const WaveState &ws,
+                                             const uint32_t* __restrict__ queue, uint32_t n, uint32_t* cursor,
+                                             uint32_t* classCounts, const DevScene* __restrict__ scenes) {
+    StackEntry stack[kTraceStack];
+    ClosestWalk<WT> walk;
+    uint32_t p = 0, info = 0;
+    bool live = false, drained = false;
+    for (;;) {
+        uint32_t slot;
+        bool fin = false;
+        if (refillLanes(live, cursor, n, drained, &slot)) {
+            p = queue[slot];
+            info = MULTI ? ws.ps[p].info : 0u;
+            const float4 o = ws.ray[2 * (size_t)p], d = ws.ray[2 * (size_t)p + 1];
+            fin = walk.begin(pathScene<MULTI>(scArg, scenes, info), V3{o.x, o.y, o.z}, V3{d.x, d.y, d.z}, o.w, d.w);
+            live = true;
+        }
+        if (live && !fin) fin = walk.advance(pathScene<MULTI>(scArg, scenes, info), stack, SLRGPU_TRACE_REFILL_VISITS);
+        int cls = -1;
+        if (live && fin) {
+            const DevScene &sc = pathScene<MULTI>(scArg, scenes, info);
+            const Hit &h = walk.hit;
+            ws.hit[p] = make_float4(h.t, h.b1, h.b2, __uint_as_float(h.prim));
+            cls = h.prim == kNoHit ? kClassMiss : (int)sc.materials[sc.prims[h.prim].material].kind;
+            live = false;
+        }
+        if (__any_sync(0xffffffffu, cls >= 0)) pushByClass<MULTI>(ws, classCounts, p, cls);
+        if (drained && !__any_sync(0xffffffffu, live)) return;
+    }
+}
+
 template <bool MULTI>
 __global__ void __launch_bounds__(256, SLRGPU_TRACE_MIN_BLOCKS) kExtendSort(DevScene scArg, WaveState ws,
                                                                           const uint32_t* __restrict__ queue,
-                            const uint32_t* __restrict__ count, uint32_t* classCounts,
+                            const uint32_t* __restrict__ count, uint32_t* classCounts, uint32_t* cursor,
                             const DevScene* __restrict__ scenes) {
     const uint32_t n = *count;
+#if SLRGPU_TRACE_REFILL
+    if (scArg.watertight) extendRefill<MULTI, true>(scArg, ws, queue, n, cursor, classCounts, scenes);
+    else extendRefill<MULTI, false>(scArg, ws, queue, n, cursor, classCounts, scenes);
+#else
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
         const uint32_t i = base + threadIdx.x;
         const bool active = i < n;
@@ -281,10 +405,9 @@ __global__ void __launch_bounds__(256, SLRGPU_TRACE_MIN_BLOCKS) kExtendSort(DevS
             ws.hit[p] = make_float4(h.t, h.b1, h.b2, __uint_as_float(h.prim));
             cls = h.prim == kNoHit ? kClassMiss : (int)sc.materials[sc.prims[h.prim].material].kind;
         }
-#pragma unroll
-        for (int c = 0; c < kNumShadeClasses; ++c)
-            queuePush(ws.classQueue + (size_t)c * ws.N, classCounts + c, p, cls == c);
+        pushByClass<MULTI>(ws, classCounts, p, cls);
     }
+#endif
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&ws.stats[0], (unsigned long long)n);
 }
 
@@ -1336,19 +1459,20 @@ RenderEngine::~RenderEngine() {
     if (bpt) bptEngineDestroy(bpt);
 }
 
-static_assert(kCtrStride == (int)kQueueCountColumns, "queue-count rows are the counter blocks");
+static_assert(kCtrStride >= (int)kQueueCountColumns, "queue-count rows are the first columns of the counter blocks");
 int RenderEngine::queueCounts(uint32_t* out, uint32_t capacity, uint32_t* rows) {
     if (!ws) {
         *rows = 0;
         return SLRGPU_OK;
     }
     *rows = depthCapacity + 2;
-    const size_t n = (size_t)kCtrStride * (depthCapacity + 2);
+    const size_t n = (size_t)kQueueCountColumns * (depthCapacity + 2);
     if (capacity < n) {
         setError("capacity below rows x 11 counters");
         return SLRGPU_ERR_INVALID_ARGUMENT;
     }
-    CUDA_TRY(cudaMemcpy(out, ws->counters, n * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    CUDA_TRY(cudaMemcpy2D(out, kQueueCountColumns * sizeof(uint32_t), ws->counters, kCtrStride * sizeof(uint32_t),
+                          kQueueCountColumns * sizeof(uint32_t), depthCapacity + 2, cudaMemcpyDeviceToHost));
     return SLRGPU_OK;
 }
 
@@ -1522,7 +1646,7 @@ static void surfaceBounce(const DevScene &sc, const DevScene* scenes, uint32_t k
     const WaveGrids &g = waveGrids(block);
     lm.begin(SLRGPU_KERNEL_EXTEND);
     kExtendSort<MULTI><<<MULTI ? g.extendSortM : g.extendSort, block, 0, stream>>>(sc, w, inQueue, ctr + kCtrExt, ctr,
-                                                                                  scenes);
+                                                                                  ctr + kCtrExtTake, scenes);
     lm.end();
     ++launches;
     if (env) {
@@ -1553,7 +1677,8 @@ static void surfaceBounce(const DevScene &sc, const DevScene* scenes, uint32_t k
         ++launches;
     }
     lm.begin(SLRGPU_KERNEL_SHADOW);
-    kShadow<MULTI><<<MULTI ? g.shadowM : g.shadow, block, 0, stream>>>(sc, w, w.shadowQueue, ctr + kCtrShadow, scenes);
+    kShadow<MULTI><<<MULTI ? g.shadowM : g.shadow, block, 0, stream>>>(sc, w, w.shadowQueue, ctr + kCtrShadow,
+                                                                       ctr + kCtrShadowTake, scenes);
     lm.end();
     ++launches;
 }
