@@ -220,26 +220,14 @@ __global__ void kRaygen(DevScene scArg, WaveState ws, const __grid_constant__ Wa
     }
 }
 
-__global__ void kExtend(DevScene sc, WaveState ws, const uint32_t* __restrict__ queue, const uint32_t* __restrict__ count) {
-    const uint32_t n = *count;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        uint32_t p = queue[i];
-        float4 o = ws.ray[2 * (size_t)p], d = ws.ray[2 * (size_t)p + 1];
-        Hit h;
-        traceClosest(sc, V3{o.x, o.y, o.z}, V3{d.x, d.y, d.z}, o.w, d.w, &h);
-        ws.hit[p] = make_float4(h.t, h.b1, h.b2, __uint_as_float(h.prim));
-    }
-    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&ws.stats[0], (unsigned long long)n);
-}
-
 // Resident blocks per SM the traversal kernels are compiled for; a
 // compile-time tuning constant.
 #ifndef SLRGPU_TRACE_MIN_BLOCKS
 #define SLRGPU_TRACE_MIN_BLOCKS 4
 #endif
-// Dynamic ray fetch in the surface tracer's traversal kernels (Aila and
-// Laine, "Understanding the Efficiency of Ray Traversal on GPUs", HPG 2009):
-// each warp takes rays from the bounce's queue through a work counter, and
+// Dynamic ray fetch in the wave's traversal kernels (Aila and Laine,
+// "Understanding the Efficiency of Ray Traversal on GPUs", HPG 2009): each
+// warp takes rays from the bounce's queue through a work counter, and
 // once SLRGPU_TRACE_REFILL_LANES of its lanes have finished their walks
 // they take new rays while the others go on walking; walks advance
 // SLRGPU_TRACE_REFILL_VISITS node visits between two looks.  0 turns it off
@@ -254,6 +242,11 @@ __global__ void kExtend(DevScene sc, WaveState ws, const uint32_t* __restrict__ 
 #define SLRGPU_TRACE_REFILL_VISITS 16
 #endif
 static_assert(SLRGPU_TRACE_REFILL_LANES >= 1 && SLRGPU_TRACE_REFILL_LANES <= 32, "a warp has 32 lanes");
+// The same threshold for the ray-query kernel (slrgpu_trace_rays).
+#ifndef SLRGPU_QUERY_REFILL_LANES
+#define SLRGPU_QUERY_REFILL_LANES SLRGPU_TRACE_REFILL_LANES
+#endif
+static_assert(SLRGPU_QUERY_REFILL_LANES >= 1 && SLRGPU_QUERY_REFILL_LANES <= 32, "a warp has 32 lanes");
 
 // The refill step of a warp: when at least SLRGPU_TRACE_REFILL_LANES lanes
 // are idle and the queue is not drained, the idle lanes take the next queue
@@ -275,10 +268,13 @@ __device__ __forceinline__ bool refillLanes(bool live, uint32_t* cursor, uint32_
 
 // Shadow rays (PTRenderer.cpp:196-217): an unoccluded ray adds its stored
 // contribution to the path's radiance.
-template <bool MULTI, bool WT>
+// VOL: an unoccluded ray of a scene with a medium goes to the transmittance
+// queue (medQueue) instead.
+template <bool MULTI, bool WT, bool VOL = false>
 __device__ __forceinline__ void shadowRefill(const DevScene &scArg, const WaveState &ws,
                                              const uint32_t* __restrict__ queue, uint32_t n, uint32_t* cursor,
-                                             const DevScene* __restrict__ scenes) {
+                                             const DevScene* __restrict__ scenes, uint32_t* medQueue = nullptr,
+                                             uint32_t* medCount = nullptr) {
     uint32_t stack[kTraceStack];
     AnyWalk<WT> walk;
     uint32_t p = 0, info = 0;
@@ -294,14 +290,20 @@ __device__ __forceinline__ void shadowRefill(const DevScene &scArg, const WaveSt
             live = true;
         }
         if (live && !fin) fin = walk.advance(pathScene<MULTI>(scArg, scenes, info), stack, SLRGPU_TRACE_REFILL_VISITS);
+        bool pushMedium = false;
         if (live && fin) {
             if (!walk.occluded) {
-                Spec c;
-                loadSpec(ws.shContrib, p, c);
-                addSpec(ws.L, p, c);
+                if (VOL && scArg.medium.present) {
+                    pushMedium = true;
+                } else {
+                    Spec c;
+                    loadSpec(ws.shContrib, p, c);
+                    addSpec(ws.L, p, c);
+                }
             }
             live = false;
         }
+        if (VOL && __any_sync(0xffffffffu, pushMedium)) queuePush(medQueue, medCount, p, pushMedium);
         if (drained && !__any_sync(0xffffffffu, live)) return;
     }
 }
@@ -349,7 +351,8 @@ __device__ __forceinline__ void pushByClass(const WaveState &ws, uint32_t* class
         queuePush(ws.classQueue + (size_t)c * ws.N, classCounts + c, p, cls == c);
 }
 
-template <bool MULTI, bool WT>
+// SORT: push each path to the queue of its shading class.
+template <bool MULTI, bool WT, bool SORT = true>
 __device__ __forceinline__ void extendRefill(const DevScene &scArg, const WaveState &ws,
                                              const uint32_t* __restrict__ queue, uint32_t n, uint32_t* cursor,
                                              uint32_t* classCounts, const DevScene* __restrict__ scenes) {
@@ -373,10 +376,10 @@ __device__ __forceinline__ void extendRefill(const DevScene &scArg, const WaveSt
             const DevScene &sc = pathScene<MULTI>(scArg, scenes, info);
             const Hit &h = walk.hit;
             ws.hit[p] = make_float4(h.t, h.b1, h.b2, __uint_as_float(h.prim));
-            cls = h.prim == kNoHit ? kClassMiss : (int)sc.materials[sc.prims[h.prim].material].kind;
+            if (SORT) cls = h.prim == kNoHit ? kClassMiss : (int)sc.materials[sc.prims[h.prim].material].kind;
             live = false;
         }
-        if (__any_sync(0xffffffffu, cls >= 0)) pushByClass<MULTI>(ws, classCounts, p, cls);
+        if (SORT && __any_sync(0xffffffffu, cls >= 0)) pushByClass<MULTI>(ws, classCounts, p, cls);
         if (drained && !__any_sync(0xffffffffu, live)) return;
     }
 }
@@ -406,6 +409,28 @@ __global__ void __launch_bounds__(256, SLRGPU_TRACE_MIN_BLOCKS) kExtendSort(DevS
             cls = h.prim == kNoHit ? kClassMiss : (int)sc.materials[sc.prims[h.prim].material].kind;
         }
         pushByClass<MULTI>(ws, classCounts, p, cls);
+    }
+#endif
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&ws.stats[0], (unsigned long long)n);
+}
+
+// Closest hits of the volumetric path tracer's extension rays (the medium
+// interaction comes after, in kVolInteract).
+__global__ void __launch_bounds__(256, SLRGPU_TRACE_MIN_BLOCKS) kExtend(DevScene sc, WaveState ws,
+                                                                      const uint32_t* __restrict__ queue,
+                                                                      const uint32_t* __restrict__ count,
+                                                                      uint32_t* cursor) {
+    const uint32_t n = *count;
+#if SLRGPU_TRACE_REFILL
+    if (sc.watertight) extendRefill<false, true, false>(sc, ws, queue, n, cursor, nullptr, nullptr);
+    else extendRefill<false, false, false>(sc, ws, queue, n, cursor, nullptr, nullptr);
+#else
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        uint32_t p = queue[i];
+        float4 o = ws.ray[2 * (size_t)p], d = ws.ray[2 * (size_t)p + 1];
+        Hit h;
+        traceClosest(sc, V3{o.x, o.y, o.z}, V3{d.x, d.y, d.z}, o.w, d.w, &h);
+        ws.hit[p] = make_float4(h.t, h.b1, h.b2, __uint_as_float(h.prim));
     }
 #endif
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&ws.stats[0], (unsigned long long)n);
@@ -995,9 +1020,16 @@ __global__ void __launch_bounds__(256, SLRGPU_SHADEVOL_MIN_BLOCKS) kShadeVol(Dev
 // Shadow rays of the volumetric integrator (Scene::testVisibility,
 // Scene.cpp:114-135): occlusion by surfaces here; unoccluded rays that may
 // cross the medium go to a second queue for their spectral transmittance.
-__global__ void kShadowVol(DevScene sc, WaveState ws, const uint32_t* __restrict__ queue,
-                           const uint32_t* __restrict__ count, uint32_t* medQueue, uint32_t* medCount) {
+__global__ void __launch_bounds__(256, SLRGPU_TRACE_MIN_BLOCKS) kShadowVol(DevScene sc, WaveState ws,
+                                                                         const uint32_t* __restrict__ queue,
+                                                                         const uint32_t* __restrict__ count,
+                                                                         uint32_t* cursor, uint32_t* medQueue,
+                                                                         uint32_t* medCount) {
     const uint32_t n = *count;
+#if SLRGPU_TRACE_REFILL
+    if (sc.watertight) shadowRefill<false, true, true>(sc, ws, queue, n, cursor, nullptr, medQueue, medCount);
+    else shadowRefill<false, false, true>(sc, ws, queue, n, cursor, nullptr, medQueue, medCount);
+#else
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
         const uint32_t i = base + threadIdx.x;
         bool pushMedium = false;
@@ -1017,6 +1049,7 @@ __global__ void kShadowVol(DevScene sc, WaveState ws, const uint32_t* __restrict
         }
         queuePush(medQueue, medCount, p, pushMedium);
     }
+#endif
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&ws.stats[1], (unsigned long long)n);
 }
 
@@ -1157,21 +1190,70 @@ __global__ void kFilmToPixelMajor(const float* __restrict__ src, float* __restri
     }
 }
 
-__global__ void kTrace(DevScene sc, const float* __restrict__ rays, uint32_t n, int anyHit, uint32_t* prim, float* t,
-                       float* b1, float* b2) {
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const float4* r = reinterpret_cast<const float4*>(rays) + 2 * (size_t)i;
-        float4 o = r[0], d = r[1];
-        if (anyHit) {
-            prim[i] = traceAny(sc, V3{o.x, o.y, o.z}, V3{d.x, d.y, d.z}, o.w, d.w) ? 1u : 0u;
-        } else {
-            Hit h;
-            traceClosest(sc, V3{o.x, o.y, o.z}, V3{d.x, d.y, d.z}, o.w, d.w, &h);
-            prim[i] = h.prim;
-            if (t) t[i] = h.t;
-            if (b1) b1[i] = h.b1;
-            if (b2) b2[i] = h.b2;
+// Ray queries (slrgpu_trace_rays): each warp takes the rays of its own
+// contiguous range, and lanes whose walk has ended take the range's next rays
+// while the others go on walking (the refill of the wave kernels, with the
+// warp's cursor in registers instead of a counter in memory).
+template <bool WT, bool ANY>
+__device__ __forceinline__ void traceQueries(const DevScene &sc, const float4* __restrict__ rays, uint32_t n,
+                                             uint32_t* prim, float* t, float* b1, float* b2) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint64_t chunk = ((uint64_t)n + warps - 1) / warps;
+    const uint64_t first = (uint64_t)warp * chunk;
+    uint32_t cursor = first < n ? (uint32_t)first : n;
+    const uint32_t end = first + chunk < n ? (uint32_t)(first + chunk) : n;
+    StackEntry cstack[ANY ? 1 : kTraceStack];
+    uint32_t astack[ANY ? kTraceStack : 1];
+    ClosestWalk<WT> cw;
+    AnyWalk<WT> aw;
+    uint32_t i = 0;
+    bool live = false;
+    for (;;) {
+        const uint32_t idle = __ballot_sync(0xffffffffu, !live);
+        bool fin = false;
+        if (cursor < end && (uint32_t)__popc(idle) >= SLRGPU_QUERY_REFILL_LANES) {
+            if (!live) {
+                const uint32_t k = cursor + (uint32_t)__popc(idle & ((1u << lane) - 1));
+                if (k < end) {
+                    i = k;
+                    const float4 o = rays[2 * (size_t)i], d = rays[2 * (size_t)i + 1];
+                    const V3 org = V3{o.x, o.y, o.z}, dir = V3{d.x, d.y, d.z};
+                    fin = ANY ? aw.begin(sc, org, dir, o.w, d.w) : cw.begin(sc, org, dir, o.w, d.w);
+                    live = true;
+                }
+            }
+            cursor = end - cursor > (uint32_t)__popc(idle) ? cursor + (uint32_t)__popc(idle) : end;
         }
+        if (live && !fin)
+            fin = ANY ? aw.advance(sc, astack, SLRGPU_TRACE_REFILL_VISITS)
+                      : cw.advance(sc, cstack, SLRGPU_TRACE_REFILL_VISITS);
+        if (live && fin) {
+            if (ANY) {
+                prim[i] = aw.occluded ? 1u : 0u;
+            } else {
+                prim[i] = cw.hit.prim;
+                if (t) t[i] = cw.hit.t;
+                if (b1) b1[i] = cw.hit.b1;
+                if (b2) b2[i] = cw.hit.b2;
+            }
+            live = false;
+        }
+        if (cursor >= end && !__any_sync(0xffffffffu, live)) return;
+    }
+}
+
+__global__ void __launch_bounds__(256, SLRGPU_TRACE_MIN_BLOCKS) kTrace(DevScene sc, const float* __restrict__ rays,
+                                                                     uint32_t n, int anyHit, uint32_t* prim, float* t,
+                                                                     float* b1, float* b2) {
+    const float4* r = reinterpret_cast<const float4*>(rays);
+    if (anyHit) {
+        if (sc.watertight) traceQueries<true, true>(sc, r, n, prim, t, b1, b2);
+        else traceQueries<false, true>(sc, r, n, prim, t, b1, b2);
+    } else {
+        if (sc.watertight) traceQueries<true, false>(sc, r, n, prim, t, b1, b2);
+        else traceQueries<false, false>(sc, r, n, prim, t, b1, b2);
     }
 }
 
@@ -1714,7 +1796,7 @@ static int runWave(const DeviceScene &ds0, const WaveState &w, const WaveParams 
         uint32_t* outQueue = w.queue[(b + 1) & 1];
         if (volumetric) {
             lm.begin(SLRGPU_KERNEL_EXTEND);
-            kExtend<<<g.extend, block, 0, stream>>>(ds.sc, w, inQueue, ctr + kCtrExt);
+            kExtend<<<g.extend, block, 0, stream>>>(ds.sc, w, inQueue, ctr + kCtrExt, ctr + kCtrExtTake);
             lm.end();
             // the medium collision (or not), then one shading kernel per
             // vertex class present
@@ -1747,8 +1829,8 @@ static int runWave(const DeviceScene &ds0, const WaveState &w, const WaveParams 
             // unoccluded shadow rays that cross the medium wait in their own queue
             uint32_t* medQueue = w.classQueue + (size_t)kQueueMedShadow * w.N;
             lm.begin(SLRGPU_KERNEL_SHADOW);
-            kShadowVol<<<g.shadowVol, block, 0, stream>>>(ds.sc, w, w.shadowQueue, ctr + kCtrShadow, medQueue,
-                                                          ctr + kCtrMedShadow);
+            kShadowVol<<<g.shadowVol, block, 0, stream>>>(ds.sc, w, w.shadowQueue, ctr + kCtrShadow,
+                                                          ctr + kCtrShadowTake, medQueue, ctr + kCtrMedShadow);
             lm.end();
             lm.begin(SLRGPU_KERNEL_SHADOW);
             kShadowVolMedium<<<g.shadowVolMedium, block, 0, stream>>>(ds.sc, w, medQueue, ctr + kCtrMedShadow,
