@@ -342,6 +342,44 @@ __global__ void __launch_bounds__(256, SLRGPU_TRACE_MIN_BLOCKS) kShadow(DevScene
 // divergence.  Emission with MIS, Russian roulette, next-event estimation and
 // BSDF sampling follow PTRenderer::Job::contribution (PTRenderer.cpp:145-277).
 // ---------------------------------------------------------------------------
+// Russian roulette at the hit (PTRenderer.cpp:266-272) for materials that do
+// not emit.  A vertex adds its emission before the roulette; with none to add,
+// the roulette is the vertex's first draw from the path's random numbers, so
+// the extension kernel can draw it as soon as the hit is known and a path that
+// ends there never reaches a shading kernel (at depth > 0 about half of them
+// end, and in a shading warp their lanes would idle through next-event
+// estimation and BSDF sampling).  The shading kernel of a surviving path
+// recomputes the same continuation probability from the same inputs and
+// skips the draw.  Returns false when the path ends here (roulette, or the
+// maximum depth reached).
+#ifndef SLRGPU_EARLY_ROULETTE
+#define SLRGPU_EARLY_ROULETTE 1
+#endif
+__device__ __forceinline__ bool rouletteAtHit(const DevScene &sc, const WaveState &ws, uint32_t p, uint32_t maxDepth) {
+    const uint32_t info = ws.ps[p].info;
+    const uint32_t depth = info >> kInfoDepthShift;
+    if (depth + 1 > maxDepth) return false;
+    if (depth == 0) return true;
+    Spec alpha;
+    loadSpec(ws.alpha, p, alpha);
+    const float cp = fminf(importance(alpha, (int)(info & kInfoSelMask)) / ws.ps[p].initY, 1.0f);
+    Rng rng{loadKey(ws, p), ws.ps[p].rngCounter, sc.rngTape};
+    if (!(rng.next() < cp)) return false;
+    ws.ps[p].rngCounter = rng.counter;
+    return true;
+}
+
+// The shading class of a finished extension ray, or -1 when the path ends at
+// the hit's roulette.
+__device__ __forceinline__ int hitClass(const DevScene &sc, const WaveState &ws, uint32_t p, uint32_t prim,
+                                        uint32_t maxDepth) {
+    if (prim == kNoHit) return kClassMiss;
+    const DevMaterial &m = sc.materials[sc.prims[prim].material];
+    const int cls = (int)m.kind;
+    if (SLRGPU_EARLY_ROULETTE && m.emit < 0 && !rouletteAtHit(sc, ws, p, maxDepth)) return -1;
+    return cls;
+}
+
 // Closest hits of the bounce's extension rays, each path pushed to the
 // queue of its shading class (material kind, or miss).
 template <bool MULTI>
@@ -355,7 +393,8 @@ __device__ __forceinline__ void pushByClass(const WaveState &ws, uint32_t* class
 template <bool MULTI, bool WT, bool SORT = true>
 __device__ __forceinline__ void extendRefill(const DevScene &scArg, const WaveState &ws,
                                              const uint32_t* __restrict__ queue, uint32_t n, uint32_t* cursor,
-                                             uint32_t* classCounts, const DevScene* __restrict__ scenes) {
+                                             uint32_t* classCounts, const DevScene* __restrict__ scenes,
+                                             uint32_t maxDepth = 0) {
     StackEntry stack[kTraceStack];
     ClosestWalk<WT> walk;
     uint32_t p = 0, info = 0;
@@ -376,7 +415,7 @@ __device__ __forceinline__ void extendRefill(const DevScene &scArg, const WaveSt
             const DevScene &sc = pathScene<MULTI>(scArg, scenes, info);
             const Hit &h = walk.hit;
             ws.hit[p] = make_float4(h.t, h.b1, h.b2, __uint_as_float(h.prim));
-            if (SORT) cls = h.prim == kNoHit ? kClassMiss : (int)sc.materials[sc.prims[h.prim].material].kind;
+            if (SORT) cls = hitClass(sc, ws, p, h.prim, maxDepth);
             live = false;
         }
         if (SORT && __any_sync(0xffffffffu, cls >= 0)) pushByClass<MULTI>(ws, classCounts, p, cls);
@@ -388,11 +427,11 @@ template <bool MULTI>
 __global__ void __launch_bounds__(256, SLRGPU_TRACE_MIN_BLOCKS) kExtendSort(DevScene scArg, WaveState ws,
                                                                           const uint32_t* __restrict__ queue,
                             const uint32_t* __restrict__ count, uint32_t* classCounts, uint32_t* cursor,
-                            const DevScene* __restrict__ scenes) {
+                            uint32_t maxDepth, const DevScene* __restrict__ scenes) {
     const uint32_t n = *count;
 #if SLRGPU_TRACE_REFILL
-    if (scArg.watertight) extendRefill<MULTI, true>(scArg, ws, queue, n, cursor, classCounts, scenes);
-    else extendRefill<MULTI, false>(scArg, ws, queue, n, cursor, classCounts, scenes);
+    if (scArg.watertight) extendRefill<MULTI, true>(scArg, ws, queue, n, cursor, classCounts, scenes, maxDepth);
+    else extendRefill<MULTI, false>(scArg, ws, queue, n, cursor, classCounts, scenes, maxDepth);
 #else
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
         const uint32_t i = base + threadIdx.x;
@@ -406,7 +445,7 @@ __global__ void __launch_bounds__(256, SLRGPU_TRACE_MIN_BLOCKS) kExtendSort(DevS
             Hit h;
             traceClosest(sc, V3{o.x, o.y, o.z}, V3{d.x, d.y, d.z}, o.w, d.w, &h);
             ws.hit[p] = make_float4(h.t, h.b1, h.b2, __uint_as_float(h.prim));
-            cls = h.prim == kNoHit ? kClassMiss : (int)sc.materials[sc.prims[h.prim].material].kind;
+            cls = hitClass(sc, ws, p, h.prim, maxDepth);
         }
         pushByClass<MULTI>(ws, classCounts, p, cls);
     }
@@ -539,10 +578,12 @@ __global__ void __launch_bounds__(256, K == kMatGGXScattering ? SLRGPU_SHADE_DIE
                 for (int k = 0; k < kNumLambda; ++k) add.v[k] = alpha.v[k] * (M.v[k] * edf) * mis;
                 addSpec(ws.L, p, add);
             }
-            // Russian roulette (PTRenderer.cpp:266-272).
+            // Russian roulette (PTRenderer.cpp:266-272); a material that does
+            // not emit had its draw at the hit (rouletteAtHit), and the path
+            // is here because it continued.
             if (depth > 0) {
                 float cp = fminf(importance(alpha, sel) / ws.ps[p].initY, 1.0f);
-                if (rng.next() < cp) {
+                if ((SLRGPU_EARLY_ROULETTE && mat.emit < 0) || rng.next() < cp) {
                     float r = 1.0f / cp;
 #pragma unroll
                     for (int k = 0; k < kNumLambda; ++k) alpha.v[k] *= r;
@@ -1728,7 +1769,7 @@ static void surfaceBounce(const DevScene &sc, const DevScene* scenes, uint32_t k
     const WaveGrids &g = waveGrids(block);
     lm.begin(SLRGPU_KERNEL_EXTEND);
     kExtendSort<MULTI><<<MULTI ? g.extendSortM : g.extendSort, block, 0, stream>>>(sc, w, inQueue, ctr + kCtrExt, ctr,
-                                                                                  ctr + kCtrExtTake, scenes);
+                                                                                  ctr + kCtrExtTake, D, scenes);
     lm.end();
     ++launches;
     if (env) {
