@@ -77,15 +77,20 @@ BYTES_BPT_BOUNCE = 440
 BYTES_BPT_CONNECT = 390
 BYTES_BPT_SHADOW = 164   # queued connection 100 B in, any-hit query, 64 B atomic add out
 
-# DRAM bytes per shaded bounce of the surface shading kernels, measured by
-# ncu (dram__bytes_read.sum + dram__bytes_write.sum, --clock-control none) on
-# the first three kShadeSurf launches of the `small` workload (512 x 512,
-# 4 spp, 176k triangles: 1,048,576 paths, ~0.4 GB of path state) divided by
-# the paths those launches shaded (slrgpu_context_queue_counts): 294.1 MB
-# over 678,107 shaded bounces.  The line scales it by the units per launch of
-# the measured workload (the full-size run is not captured with more than
-# the launch list).
-SHADE_DRAM_BYTES_PER_UNIT = 433.7
+# DRAM bytes per unit of the surface tracer's kernels, measured by ncu
+# (dram__bytes_read.sum + dram__bytes_write.sum, --clock-control none) on the
+# first three launches of a kernel in the `small` workload (512 x 512, 4 spp,
+# 176k triangles: 1,048,576 paths, ~0.4 GB of path state), divided by the
+# units of those launches (slrgpu_context_queue_counts of the same frame).
+# The line scales them by the units per launch of the measured workload (the
+# full-size run is not captured with more than the launch list).
+# kExtendSort, bounces 0-2: 171.8 MB over 1,604,943 closest-hit queries (the
+# BVH nodes and triangles that miss L2, the path records of the roulette at
+# the hit, the hit records).
+EXTEND_DRAM_BYTES_PER_UNIT = 107.0
+# kShadeSurf, the first three launches (bounce 0 conductor and dielectric,
+# bounce 1 conductor): 258.8 MB over 610,018 shaded paths.
+SHADE_DRAM_BYTES_PER_UNIT = 424.3
 
 
 def load_peaks():
@@ -577,20 +582,30 @@ def main():
     if BPT:
         units.update({1: (ext_rays, BYTES_BPT_BOUNCE), 2: (sh_rays, BYTES_BPT_CONNECT),
                       3: (sh_rays, BYTES_BPT_SHADOW), 0: (samples_per_step * args.steps, 2 * 160 + 96)})
-    n_units, per_unit = units[dom]
-    bytes_per_launch = n_units * per_unit / max(1, kern_n[dom])
-    avg_launch_s = kern_ms[dom] * 1e-3 / max(1, kern_n[dom])
-    achieved = bytes_per_launch / avg_launch_s / 1e9
     peak, peak_kind = load_peaks()
-    roofline = {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "peak_source": peak_kind, "traffic": None,
-                "bytes_per_unit": per_unit, "units_per_launch": n_units / max(1, kern_n[dom]),
-                "avg_launch_ms": avg_launch_s * 1e3,
-                "kernel_share": {names[k]: kern_ms[k] / max(1e-9, sum(kern_ms)) for k in range(5)}}
-    if names[dom] == "shade" and not BPT and not VOLUMETRIC:
-        roofline["traffic"] = SHADE_DRAM_BYTES_PER_UNIT * n_units / max(1, kern_n[dom])
-        roofline["traffic_source"] = ("ncu DRAM bytes per shaded bounce of kShadeSurf on the small workload "
-                                      "(three launches, 433.7 B) x shaded bounces per launch of this run")
+
+    def class_roofline(k):
+        n_units, per_unit = units[k]
+        bytes_per_launch = n_units * per_unit / max(1, kern_n[k])
+        avg_launch_s = kern_ms[k] * 1e-3 / max(1, kern_n[k])
+        achieved = bytes_per_launch / max(1e-12, avg_launch_s) / 1e9
+        r = {"bound": "hbm", "kernel": names[k], "achieved": achieved, "peak": peak, "unit": "GB/s",
+             "frac": achieved / peak, "peak_source": peak_kind, "traffic": None,
+             "bytes_per_unit": per_unit, "units_per_launch": n_units / max(1, kern_n[k]),
+             "avg_launch_ms": avg_launch_s * 1e3}
+        if not BPT and not VOLUMETRIC and names[k] in ("extend", "shade"):
+            dram = EXTEND_DRAM_BYTES_PER_UNIT if names[k] == "extend" else SHADE_DRAM_BYTES_PER_UNIT
+            r["traffic"] = dram * n_units / max(1, kern_n[k])
+            r["traffic_source"] = (f"ncu DRAM bytes per unit of the class's kernel on the small workload (first three "
+                                   f"launches, {dram} B) x units per launch of this run")
+        return r
+
+    roofline = class_roofline(dom)
+    roofline["kernel_share"] = {names[k]: kern_ms[k] / max(1e-9, sum(kern_ms)) for k in range(5)}
+    if names[dom] == "extend" and not BPT and not VOLUMETRIC:
+        roofline["note"] = ("closest-hit BVH walks: bound by the latency of dependent node and triangle loads from L2 "
+                            "and by divergent control flow, not by HBM; bytes_per_unit counts only the query's "
+                            "compulsory 48 B (ray in, hit out)")
     if VOLUMETRIC and names[dom] == "shadow":
         roofline["note"] = ("the shadow class is dominated by the ratio-tracking transmittance walks, which read the "
                             "density grid from L2 (64 MiB at 256^3; ~91 % L2 hit rate, ~73 % issue activity with 13 "
@@ -609,6 +624,7 @@ def main():
             "dropped_samples": dropped,
             "gpu_launches": launches,
             "roofline": roofline,
+            "roofline_shade": class_roofline(2) if not BPT else None,
             "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": WIDTH * HEIGHT * 16 * 4, "ms_per_step": e2e_total / len(e2e_ms)},
             "clocks": clk}
