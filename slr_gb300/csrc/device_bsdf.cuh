@@ -194,8 +194,13 @@ __device__ __forceinline__ void evalIorPairs(const Bsdf &B, const Spec &X, const
 #pragma unroll
             for (int i = 0; i < kNumLambda; ++i) out.v[i] = fn(X.v[i], Y.v[i]);
         } else {
+            // the rolled loop indexes a scratch array, not `out`, so that
+            // `out` itself can stay in registers
+            float tmp[kNumLambda];
 #pragma unroll 1
-            for (int i = 0; i < kNumLambda; ++i) out.v[i] = fn(X.v[i], Y.v[i]);
+            for (int i = 0; i < kNumLambda; ++i) tmp[i] = fn(X.v[i], Y.v[i]);
+#pragma unroll
+            for (int i = 0; i < kNumLambda; ++i) out.v[i] = tmp[i];
         }
         return;
     }
