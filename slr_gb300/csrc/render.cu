@@ -173,7 +173,8 @@ __device__ __forceinline__ uint64_t loadKey(const WaveState &ws, uint32_t p) {
 // launch parameters are fixed at capture), or null to use wpArg.
 template <bool MULTI>
 __global__ void kRaygen(DevScene scArg, WaveState ws, const __grid_constant__ WaveParams wpArg,
-                        const WaveParams* __restrict__ wpDev, const DevScene* __restrict__ scenes) {
+                        const WaveParams* __restrict__ wpDev, const DevScene* __restrict__ scenes,
+                        bool initAlpha) {
     const WaveParams &wp = wpDev ? *wpDev : wpArg;
     if (blockIdx.x == 0 && threadIdx.x == 0) ws.counters[kCtrExt] = wp.numPaths;
     for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < wp.numPaths; p += gridDim.x * blockDim.x) {
@@ -214,7 +215,9 @@ __global__ void kRaygen(DevScene scArg, WaveState ws, const __grid_constant__ Wa
         ps.keyLo = (uint32_t)key;
         ps.keyHi = (uint32_t)(key >> 32);
         ws.ps[p] = ps;
-        storeSpec(ws.alpha, p, specConst(1.0f));
+        // the surface path tracer's kernels take the throughput of a
+        // depth-0 path as 1 without reading it
+        if (initAlpha) storeSpec(ws.alpha, p, specConst(1.0f));
         storeSpec(ws.L, p, specConst(0.0f));
         ws.queue[0][p] = p;
     }
@@ -506,7 +509,8 @@ __global__ void kShadeMiss(DevScene scArg, WaveState ws, const uint32_t* __restr
             mis = (bp * bp) / (lightPdf * lightPdf + bp * bp);
         }
         Spec a;
-        loadSpec(ws.alpha, p, a);
+        if (depth == 0) a = specConst(1.0f);
+        else loadSpec(ws.alpha, p, a);
 #pragma unroll
         for (int k = 0; k < kNumLambda; ++k) a.v[k] = a.v[k] * Le.v[k] * mis;
         addSpec(ws.L, p, a);
@@ -554,7 +558,8 @@ __global__ void __launch_bounds__(256, K == kMatGGXScattering ? SLRGPU_SHADE_DIE
             float4 hv = ws.hit[p];
             const DevPrim pr = sc.prims[__float_as_uint(hv.w)];
             Spec alpha;
-            loadSpec(ws.alpha, p, alpha);
+            if (depth == 0) alpha = specConst(1.0f);
+            else loadSpec(ws.alpha, p, alpha);
             bool alive = true;
             SurfPoint sp;
             surfacePoint(sc, pr, org, dir, hv.x, hv.y, hv.z, sp);
@@ -1824,9 +1829,9 @@ static int runWave(const DeviceScene &ds0, const WaveState &w, const WaveParams 
     }
     lm.begin(SLRGPU_KERNEL_RAYGEN);
     if (multi)
-        kRaygen<true><<<g.raygenM, block, 0, stream>>>(ds.sc, w, wp, wpDev, multi->dev);
+        kRaygen<true><<<g.raygenM, block, 0, stream>>>(ds.sc, w, wp, wpDev, multi->dev, volumetric);
     else
-        kRaygen<false><<<g.raygen, block, 0, stream>>>(ds.sc, w, wp, wpDev, nullptr);
+        kRaygen<false><<<g.raygen, block, 0, stream>>>(ds.sc, w, wp, wpDev, nullptr, volumetric);
     lm.end();
     ++launches;
     for (uint32_t b = 0; b <= D; ++b) {
