@@ -53,6 +53,20 @@ def make_queries(n_per_setup: int, seed: int) -> np.ndarray:
     return np.stack(qs)
 
 
+def _flat_interpolated(v: float, offset: float) -> np.ndarray:
+    """(1 - t) v + t v in float32 at the 16 stratified wavelengths of a path
+    with wavelength offset `offset`, t = (lambda - 360) / 470."""
+    f = np.float32
+    lam = (f(360) + (f(470) * (np.arange(16, dtype=f) + f(offset))).astype(f) * f(0.0625)).astype(f)
+    x = (lam - f(360)).astype(f)
+    # x / 470 correctly rounded, as the renderer computes it (one FMA-refined quotient)
+    z = f(1.0 / 470.0)
+    q = (x * z).astype(f)
+    r = (x.astype(np.float64) - q.astype(np.float64) * 470.0).astype(f)
+    t = (r.astype(np.float64) * np.float64(z) + q.astype(np.float64)).astype(f)
+    return (((f(1) - t).astype(f) * f(v)).astype(f) + (t * f(v)).astype(f)).astype(f)
+
+
 def bsdf_cases(n_per_setup: int = 64):
     eta_al = (1.2 + 0.4 * (WL - 360) / 470).astype(np.float32)
     k_al = (8.0 - 2.0 * (WL - 360) / 470).astype(np.float32)
@@ -60,6 +74,11 @@ def bsdf_cases(n_per_setup: int = 64):
     diamond = (2.38 + 1.5e4 / (WL * WL)).astype(np.float32)  # Cauchy-like dispersion
     glass = (1.5 + 4.0e3 / (WL * WL)).astype(np.float32)
     refl = (0.3 + 0.5 * np.sin(WL / 60.0) ** 2).astype(np.float32)
+    # a flat index spectrum as a path sees it: the two-sample regular spectrum
+    # (v, v) over 360-830 nm interpolated in float32 at one path's 16
+    # wavelengths, which rounds some of them one unit in the last place away
+    # from v (two or three distinct index pairs, the GPU's pair path)
+    flat_ext, flat_int = _flat_interpolated(1.0, 0.03), _flat_interpolated(1.45, 0.03)
     cases = [
         dict(name="lambert", kind="lambert", spec0=refl),
         dict(name="specular_brdf", kind="specular_brdf", spec0=(0.9 * ones).astype(np.float32), spec1=eta_al, spec2=k_al),
@@ -68,6 +87,7 @@ def bsdf_cases(n_per_setup: int = 64):
         dict(name="ggx_brdf_rough", kind="ggx_brdf", spec0=eta_al, spec1=k_al, ax=0.5, ay=0.5),
         dict(name="ggx_bsdf_diamond", kind="ggx_bsdf", spec0=ones, spec1=diamond, ax=0.05, ay=0.2),
         dict(name="ggx_bsdf_glass", kind="ggx_bsdf", spec0=ones, spec1=glass, ax=0.3, ay=0.3),
+        dict(name="ggx_bsdf_flat", kind="ggx_bsdf", spec0=flat_ext, spec1=flat_int, ax=0.3, ay=0.3),
     ]
     for i, c in enumerate(cases):
         c["queries"] = make_queries(n_per_setup, seed=100 + i)

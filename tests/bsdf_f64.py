@@ -191,13 +191,17 @@ def _rel_change(a, b):
 
 def conditions(kind, spec0, spec1, ax, ay, q, eps=1e-7, trials=8, seed=0):
     """Per query: kappa_dir (largest change of the sampled direction per unit
-    perturbation of the query direction, the geometric normal and the
-    uniforms), kappa_s (largest relative change of the sampled value or pdf
-    per unit perturbation) and kappa_e (the same for the evaluated value and
-    pdf, perturbing the query and evaluation directions and the normal).
-    Perturbations cross branch boundaries (total internal reflection, the
-    hemisphere tests) only where a query lies within about eps of one, which
-    then shows as an infinite condition number."""
+    perturbation of the query direction, the geometric normal, the uniforms
+    and the two spectra), kappa_s (largest relative change of the sampled
+    value or pdf per unit perturbation) and kappa_e (the same for the
+    evaluated value and pdf, perturbing the query and evaluation directions,
+    the normal and the spectra).  The spectra are perturbed because an FP32
+    evaluation rounds what it derives from them (the index ratio of the
+    dielectric's Fresnel term and refraction), which near total internal
+    reflection moves the result far more than the rounding of the directions
+    does.  Perturbations cross branch boundaries (total internal reflection,
+    the hemisphere tests) only where a query lies within about eps of one,
+    which then shows as an infinite condition number."""
     q = np.asarray(q, np.float64)
     rng = np.random.default_rng(seed)
     fs0, d0, p0, ok0 = sample(kind, spec0, spec1, ax, ay, q)
@@ -211,8 +215,10 @@ def conditions(kind, spec0, spec1, ax, ay, q, eps=1e-7, trials=8, seed=0):
         qp[:, 3:6] = _perturb_dir(q[:, 3:6], eps, rng)
         qp[:, 8:11] = np.clip(q[:, 8:11] + eps * rng.normal(size=(len(q), 3)), 0.0, np.nextafter(1.0, 0.0))
         qp[:, 11:14] = _perturb_dir(q[:, 11:14], eps, rng)
-        fs1, d1, p1, ok1 = sample(kind, spec0, spec1, ax, ay, qp)
-        fe1, pe1 = evaluate(kind, spec0, spec1, ax, ay, qp)
+        s0p = np.asarray(spec0, np.float64) * (1.0 + eps * rng.normal(size=16))
+        s1p = np.asarray(spec1, np.float64) * (1.0 + eps * rng.normal(size=16))
+        fs1, d1, p1, ok1 = sample(kind, s0p, s1p, ax, ay, qp)
+        fe1, pe1 = evaluate(kind, s0p, s1p, ax, ay, qp)
         flip = ok1 != ok0
         kd = np.maximum(kd, np.where(flip, np.inf, np.nan_to_num(np.abs(d1 - d0).max(1), nan=np.inf) / eps))
         rs = np.maximum(_rel_change(fs1, fs0).max(1), _rel_change(p1, p0))

@@ -40,13 +40,16 @@ def make_images(names):
         print(f"{name}: {st['batches']} batches, image sum {st['sums'].mean():.6g}, dropped {st['dropped']}")
 
 
-def make_rays_and_bsdfs():
+def make_rays():
     for name, d, n in (("trace_box", scenes.box_scene(32, 32), 20000), ("trace_soup", helpers.triangle_soup(3000, 7), 20000)):
         rays = helpers.random_rays(d, n, seed=11)
         ref = O.RefScene(d)
         prim, t, b1, b2 = ref.trace(rays)
         occ, _, _, _ = ref.trace(rays, anyhit=True)
         np.savez_compressed(os.path.join(OUT, name + ".npz"), rays=rays, prim=prim, t=t, b1=b1, b2=b2, occluded=occ)
+
+
+def make_bsdfs():
     kat = {}
     for case in bsdf_cases():
         out = O.bsdf_query(case["kind"], case["spec0"], case.get("spec1"), case.get("spec2"), case.get("ax", 0.0),
@@ -59,11 +62,16 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("images", nargs="*", help="image cases to regenerate (default: every case with a fixture)")
     ap.add_argument("--rays-and-bsdfs", action="store_true", help="also regenerate the ray and BSDF fixtures")
+    ap.add_argument("--bsdfs-only", action="store_true", help="regenerate the BSDF fixture alone")
     a = ap.parse_args()
-    names = a.images or [n for n, c in image_cases.CASES.items() if c.golden]
-    make_images(names)
-    if a.rays_and_bsdfs:
-        make_rays_and_bsdfs()
+    if a.bsdfs_only:
+        make_bsdfs()
+    else:
+        names = a.images or [n for n, c in image_cases.CASES.items() if c.golden]
+        make_images(names)
+        if a.rays_and_bsdfs:
+            make_rays()
+            make_bsdfs()
     print("golden fixtures written to", OUT)
 
 

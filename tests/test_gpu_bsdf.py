@@ -8,9 +8,12 @@ corrections, near-grazing visible-normal sampling, dielectric microfacet
 values near total internal reflection), two FP32 implementations of the same
 formula differ by up to the output's condition number times their rounding.
 The tolerance then grows to 1e-5 + kappa * 16 * 2^-24, with kappa computed in
-float64 from the query alone (tests/bsdf_f64.py: finite differences of a
-float64 restatement of the reference's BSDFs, itself pinned against the
-reference's outputs in test_cpu_parity.py), never from the GPU's result.
+float64 from the query and the BSDF's spectra alone (tests/bsdf_f64.py:
+finite differences of a float64 restatement of the reference's BSDFs, itself
+pinned against the reference's outputs in test_cpu_parity.py), never from
+the GPU's result.  ggx_bsdf_flat gives the dielectric flat index spectra as
+a path sees them (a few values one unit in the last place apart), which
+the GPU evaluates once per distinct index pair.
 Sampling succeeds on exactly the same queries, with the same sampled
 direction types.  The delta BSDFs (specular reflection and refraction) need
 no widening.  Each case prints the share of queries strictly within 1e-5."""
