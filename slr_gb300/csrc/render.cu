@@ -1197,16 +1197,30 @@ __global__ void kAccumulate(WaveState ws, const __grid_constant__ WaveParams wpA
             if (!finite) { ++dropped; continue; }
             float wlOff = ws.ps[p].wlOffset;
             float addend[kNumLambda];
-#pragma unroll
-            for (int b = 0; b < kNumLambda; ++b) addend[b] = 0.0f;
+            // Wavelength i of a path falls in film bin i unless rounding moves
+            // it across a bin edge; then every bin sums its wavelengths in
+            // order.  0 + x keeps the sign of zero the summing loop gives.
+            bool own = true;
+            uint32_t bins[kNumLambda];
 #pragma unroll
             for (int i = 0; i < kNumLambda; ++i) {
                 float lam = lambdaAt(i, wlOff);
                 float f = __fmul_rn(divRange(__fsub_rn(lam, kWavelengthLow)), (float)kNumLambda);
-                uint32_t bin = min((uint32_t)f, (uint32_t)(kNumLambda - 1));
+                bins[i] = min((uint32_t)f, (uint32_t)(kNumLambda - 1));
+                own &= bins[i] == (uint32_t)i;
+            }
+            if (own) {
 #pragma unroll
-                for (int b = 0; b < kNumLambda; ++b)
-                    if (b == (int)bin) addend[b] += c[i] * recBinWidth;
+                for (int b = 0; b < kNumLambda; ++b) addend[b] = __fadd_rn(0.0f, c[b] * recBinWidth);
+            } else {
+#pragma unroll
+                for (int b = 0; b < kNumLambda; ++b) addend[b] = 0.0f;
+#pragma unroll
+                for (int i = 0; i < kNumLambda; ++i) {
+#pragma unroll
+                    for (int b = 0; b < kNumLambda; ++b)
+                        if (b == (int)bins[i]) addend[b] += c[i] * recBinWidth;
+                }
             }
 #pragma unroll
             for (int b = 0; b < kNumLambda; ++b) {
