@@ -137,6 +137,10 @@ __device__ __forceinline__ void fresnelDielectric(const Spec &etaExt, const Spec
 #ifndef SLRGPU_IOR_PAIR_SLOTS
 #define SLRGPU_IOR_PAIR_SLOTS 4
 #endif
+// shape of the dielectric Fresnel loop when the pairs do not fit
+#ifndef SLRGPU_IOR_FRESNEL_UNROLL
+#define SLRGPU_IOR_FRESNEL_UNROLL 1
+#endif
 constexpr int kIorPairSlots = SLRGPU_IOR_PAIR_SLOTS;
 static_assert(kIorPairSlots >= 1 && kIorPairSlots <= 4, "pair slots take 2 bits per wavelength");
 
@@ -223,6 +227,10 @@ __device__ __forceinline__ void evalIorPairs(const Bsdf &B, const Spec &X, const
     }
 }
 
+// Whether material kind KIND looks for index pairs (compile time).
+template <uint32_t KIND>
+constexpr bool kIorPairsFor = SLRGPU_IOR_PAIRS != 0 && ((SLRGPU_IOR_PAIR_KINDS >> KIND) & 1u) != 0;
+
 // fresnelConductor / fresnelDielectric over the pair spectra of B.
 __device__ __forceinline__ void fresnelConductorPairs(const Bsdf &B, const Spec &eta, const Spec &k, float cosEnter,
                                                       Spec &F) {
@@ -231,8 +239,8 @@ __device__ __forceinline__ void fresnelConductorPairs(const Bsdf &B, const Spec 
 
 __device__ __forceinline__ void fresnelDielectricPairs(const Bsdf &B, const Spec &etaExt, const Spec &etaInt,
                                                        float cosEnter, Spec &F) {
-    evalIorPairs<true>(B, etaExt, etaInt,
-                       [cosEnter](float eExt, float eInt) { return fresnelDielectric1(eExt, eInt, cosEnter); }, F);
+    evalIorPairs<SLRGPU_IOR_FRESNEL_UNROLL != 0>(
+        B, etaExt, etaInt, [cosEnter](float eExt, float eInt) { return fresnelDielectric1(eExt, eInt, cosEnter); }, F);
 }
 
 // ---- GGX (directional_distribution_functions.cpp:247-315) ----
@@ -250,6 +258,22 @@ __device__ __forceinline__ float ggxG1(float ax, float ay, V3 v, V3 m) {
 
 __device__ __forceinline__ float ggxPdf(float ax, float ay, V3 v, V3 m) {
     return ggxG1(ax, ay, v, m) * absDot(v, m) * ggxD(ax, ay, m) / fabsf(v.z);
+}
+
+// The Fresnel spectra of a BSDF of kind KIND: once per index pair for the
+// kinds that look for pairs, else per wavelength (no pair code compiled in).
+template <uint32_t KIND>
+__device__ __forceinline__ void fresnelConductorFor(const Bsdf &B, const Spec &eta, const Spec &k, float cosEnter,
+                                                    Spec &F) {
+    if constexpr (kIorPairsFor<KIND>) fresnelConductorPairs(B, eta, k, cosEnter, F);
+    else fresnelConductor(eta, k, cosEnter, F);
+}
+
+template <uint32_t KIND>
+__device__ __forceinline__ void fresnelDielectricFor(const Bsdf &B, const Spec &etaExt, const Spec &etaInt,
+                                                     float cosEnter, Spec &F) {
+    if constexpr (kIorPairsFor<KIND>) fresnelDielectricPairs(B, etaExt, etaInt, cosEnter, F);
+    else fresnelDielectric(etaExt, etaInt, cosEnter, F);
 }
 
 // Transmission term of the rough dielectric B between v and l at every
@@ -332,7 +356,7 @@ __device__ __forceinline__ void bsdfSampleBody(const Bsdf &B, const BsdfQuery &q
         res->pdf = 1.0f;
         res->type = kDirReflection | kDirDelta0D;
         Spec F;
-        fresnelConductorPairs(B, B.b, B.c, q.dir.z, F);
+        fresnelConductorFor<kMatSpecularReflection>(B, B.b, B.c, q.dir.z, F);
         float r = 1.0f / fabsf(q.dir.z);
 #pragma unroll
         for (int i = 0; i < kNumLambda; ++i) fs.v[i] = (B.a.v[i] * F.v[i]) * r;
@@ -340,7 +364,7 @@ __device__ __forceinline__ void bsdfSampleBody(const Bsdf &B, const BsdfQuery &q
     }
     case kMatSpecularScattering: {  // basic_bsdfs.cpp:99-150
         Spec F;
-        fresnelDielectricPairs(B, B.b, B.c, q.dir.z, F);
+        fresnelDielectricFor<kMatSpecularScattering>(B, B.b, B.c, q.dir.z, F);
         float reflectProb = importance(F, q.wl);
         if (uc < reflectProb) {
             if (q.dir.z == 0.0f) return;
@@ -387,7 +411,7 @@ __device__ __forceinline__ void bsdfSampleBody(const Bsdf &B, const BsdfQuery &q
         res->pdf = common * mPdf;
         res->type = kDirReflection | kDirHighFreq;
         Spec F;
-        fresnelConductorPairs(B, B.a, B.b, dotHV, F);
+        fresnelConductorFor<kMatGGXReflection>(B, B.a, B.b, dotHV, F);
         float G = ggxG1(B.ax, B.ay, q.dir, m) * ggxG1(B.ax, B.ay, d, m);
         float r = 1.0f / (4 * q.dir.z * d.z);
 #pragma unroll
@@ -403,7 +427,7 @@ __device__ __forceinline__ void bsdfSampleBody(const Bsdf &B, const BsdfQuery &q
         float dotHV = dot(q.dir, m);
         if (dotHV * sign <= 0 || isnan(D)) return;
         Spec F;
-        fresnelDielectricPairs(B, B.a, B.b, dotHV, F);
+        fresnelDielectricFor<kMatGGXScattering>(B, B.a, B.b, dotHV, F);
         float reflectProb = importance(F, q.wl);
         if (uc < reflectProb) {
             V3 d = (2 * dotHV) * m - q.dir;
@@ -457,7 +481,7 @@ __device__ __forceinline__ void bsdfEvalBody(const Bsdf &B, const BsdfQuery &q, 
         float dotHV = dot(q.dir, m);
         float D = ggxD(B.ax, B.ay, m);
         Spec F;
-        fresnelConductorPairs(B, B.a, B.b, dotHV, F);
+        fresnelConductorFor<kMatGGXReflection>(B, B.a, B.b, dotHV, F);
         float G = ggxG1(B.ax, B.ay, q.dir, m) * ggxG1(B.ax, B.ay, dir, m);
         float r = 1.0f / (4 * q.dir.z * dir.z);
 #pragma unroll
@@ -473,7 +497,7 @@ __device__ __forceinline__ void bsdfEvalBody(const Bsdf &B, const BsdfQuery &q, 
             float dotHV = dot(q.dir, m);
             float D = ggxD(B.ax, B.ay, m);
             Spec F;
-            fresnelDielectricPairs(B, B.a, B.b, dotHV, F);
+            fresnelDielectricFor<kMatGGXScattering>(B, B.a, B.b, dotHV, F);
             float G = ggxG1(B.ax, B.ay, q.dir, m) * ggxG1(B.ax, B.ay, dir, m);
             float r = 1.0f / (4 * dNVNL);
 #pragma unroll
@@ -519,7 +543,7 @@ __device__ __forceinline__ float bsdfPdfBody(const Bsdf &B, const BsdfQuery &q, 
         if (dotHV * sign <= 0) return 0.0f;
         float mPdf = ggxPdf(B.ax, B.ay, sign * q.dir, m);
         Spec F;
-        fresnelDielectricPairs(B, B.a, B.b, dotHV, F);
+        fresnelDielectricFor<kMatGGXScattering>(B, B.a, B.b, dotHV, F);
         float reflectProb = importance(F, q.wl);
         if (dNVNL > 0) {
             float common = reflectProb / (4 * dotHV * sign);

@@ -53,7 +53,7 @@ static __device__ __noinline__ void bsdfSampleRev(const Bsdf &B, const RevQuery 
         res->pdf = 1.0f;
         res->type = kDirReflection | kDirDelta0D;
         Spec F;
-        fresnelConductorPairs(B, B.b, B.c, q.dir.z, F);
+        fresnelConductorFor<kMatSpecularReflection>(B, B.b, B.c, q.dir.z, F);
         float r = 1.0f / fabsf(q.dir.z);
 #pragma unroll
         for (int i = 0; i < kNumLambda; ++i) fs.v[i] = (B.a.v[i] * F.v[i]) * r;
@@ -63,7 +63,7 @@ static __device__ __noinline__ void bsdfSampleRev(const Bsdf &B, const RevQuery 
     }
     case kMatSpecularScattering: {
         Spec F;
-        fresnelDielectricPairs(B, B.b, B.c, q.dir.z, F);
+        fresnelDielectricFor<kMatSpecularScattering>(B, B.b, B.c, q.dir.z, F);
         float reflectProb = importance(F, q.wl);
         if (uc < reflectProb) {
             if (q.dir.z == 0.0f) return;
@@ -118,7 +118,7 @@ static __device__ __noinline__ void bsdfSampleRev(const Bsdf &B, const RevQuery 
         res->pdf = common * mPdf;
         res->type = kDirReflection | kDirHighFreq;
         Spec F;
-        fresnelConductorPairs(B, B.a, B.b, dotHV, F);
+        fresnelConductorFor<kMatGGXReflection>(B, B.a, B.b, dotHV, F);
         float G = ggxG1(B.ax, B.ay, q.dir, m) * ggxG1(B.ax, B.ay, d, m);
         float r = 1.0f / (4 * q.dir.z * d.z);
 #pragma unroll
@@ -136,7 +136,7 @@ static __device__ __noinline__ void bsdfSampleRev(const Bsdf &B, const RevQuery 
         float dotHV = dot(q.dir, m);
         if (dotHV * sign <= 0 || isnan(D)) return;
         Spec F;
-        fresnelDielectricPairs(B, B.a, B.b, dotHV, F);
+        fresnelDielectricFor<kMatGGXScattering>(B, B.a, B.b, dotHV, F);
         float reflectProb = importance(F, q.wl);
         if (uc < reflectProb) {
             V3 d = (2 * dotHV) * m - q.dir;
@@ -199,7 +199,7 @@ static __device__ __noinline__ void bsdfEvalRev(const Bsdf &B, const RevQuery &q
         float dotHV = dot(q.dir, m);
         float D = ggxD(B.ax, B.ay, m);
         Spec F;
-        fresnelConductorPairs(B, B.a, B.b, dotHV, F);
+        fresnelConductorFor<kMatGGXReflection>(B, B.a, B.b, dotHV, F);
         float G = ggxG1(B.ax, B.ay, q.dir, m) * ggxG1(B.ax, B.ay, dir, m);
         float r = 1.0f / (4 * q.dir.z * dir.z);
 #pragma unroll
@@ -215,7 +215,7 @@ static __device__ __noinline__ void bsdfEvalRev(const Bsdf &B, const RevQuery &q
             float dotHV = dot(q.dir, m);
             float D = ggxD(B.ax, B.ay, m);
             Spec F;
-            fresnelDielectricPairs(B, B.a, B.b, dotHV, F);
+            fresnelDielectricFor<kMatGGXScattering>(B, B.a, B.b, dotHV, F);
             float G = ggxG1(B.ax, B.ay, q.dir, m) * ggxG1(B.ax, B.ay, dir, m);
             float r = 1.0f / (4 * dNVNL);
 #pragma unroll
@@ -269,7 +269,7 @@ static __device__ __noinline__ float bsdfPdfRev(const Bsdf &B, const RevQuery &q
         if (dotHV * sign <= 0) return 0.0f;
         float mPdf = ggxPdf(B.ax, B.ay, sign * q.dir, m);
         Spec F;
-        fresnelDielectricPairs(B, B.a, B.b, dotHV, F);
+        fresnelDielectricFor<kMatGGXScattering>(B, B.a, B.b, dotHV, F);
         float reflectProb = importance(F, q.wl);
         if (dNVNL > 0) {
             float common = reflectProb / (4 * dotHV * sign);
