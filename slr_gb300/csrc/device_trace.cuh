@@ -139,6 +139,36 @@ __device__ __forceinline__ float slabTest(float lox, float hix, float loy, float
     return (d0 > d1) ? __int_as_float(0x7f800000) : d0;
 }
 
+// The same slab test as min/max operations, for rays whose inverse direction
+// is finite in every axis: then no product is NaN, the compare-and-swap of
+// each slab's two distances is their min and max, and the running entry and
+// exit distances are a max and a min (the order of the axes does not
+// change a max or a min), so every distance and decision equals slabTest's
+// (up to the sign of a zero, which no comparison sees).  A zero direction
+// component makes (plane - origin) * inv NaN on a plane through the origin,
+// where slabTest's comparisons decide differently from min/max; such rays
+// take slabTest.
+template <bool ROBUST>
+__device__ __forceinline__ float slabTestMinMax(float lox, float hix, float loy, float hiy, float loz, float hiz,
+                                                V3 org, V3 inv, float tmin, float tmax) {
+    const float ax = __fmul_rn(__fsub_rn(lox, org.x), inv.x), bx = __fmul_rn(__fsub_rn(hix, org.x), inv.x);
+    const float ay = __fmul_rn(__fsub_rn(loy, org.y), inv.y), by = __fmul_rn(__fsub_rn(hiy, org.y), inv.y);
+    const float az = __fmul_rn(__fsub_rn(loz, org.z), inv.z), bz = __fmul_rn(__fsub_rn(hiz, org.z), inv.z);
+    float fx = fmaxf(ax, bx), fy = fmaxf(ay, by), fz = fmaxf(az, bz);
+    if (ROBUST) {
+        fx = __fmul_rn(fx, 1.0000008f);
+        fy = __fmul_rn(fy, 1.0000008f);
+        fz = __fmul_rn(fz, 1.0000008f);
+    }
+    const float d0 = fmaxf(fmaxf(fminf(ax, bx), fminf(ay, by)), fmaxf(fminf(az, bz), tmin));
+    const float d1 = fminf(fminf(fx, fy), fminf(fz, tmax));
+    return (d0 > d1) ? __int_as_float(0x7f800000) : d0;
+}
+
+#ifndef SLRGPU_MINMAX_SLABS
+#define SLRGPU_MINMAX_SLABS 1
+#endif
+
 struct StackEntry {
     uint32_t node;
     float tnear;
@@ -148,7 +178,7 @@ struct StackEntry {
 template <bool ROBUST>
 __device__ __forceinline__ uint32_t testChildren(const BvhNode* __restrict__ nodes, uint32_t ni, V3 org, V3 inv,
                                                  float tmin, float tmax, float tn[kBvhWidth],
-                                                 uint32_t ch[kBvhWidth]) {
+                                                 uint32_t ch[kBvhWidth], bool minmax = false) {
     // 128-bit loads: Q float4 per coordinate array, then the child words
     constexpr int Q = kBvhWidth / 4;
     const float4* np = reinterpret_cast<const float4*>(nodes + ni);
@@ -166,7 +196,9 @@ __device__ __forceinline__ uint32_t testChildren(const BvhNode* __restrict__ nod
         for (int k = 0; k < 4; ++k) {
             const int i = 4 * q + k;
             ch[i] = ca[k];
-            tn[i] = slabTest<ROBUST>(lxa[k], hxa[k], lya[k], hya[k], lza[k], hza[k], org, inv, tmin, tmax);
+            tn[i] = (SLRGPU_MINMAX_SLABS && minmax)
+                        ? slabTestMinMax<ROBUST>(lxa[k], hxa[k], lya[k], hya[k], lza[k], hza[k], org, inv, tmin, tmax)
+                        : slabTest<ROBUST>(lxa[k], hxa[k], lya[k], hya[k], lza[k], hza[k], org, inv, tmin, tmax);
             if (ch[i] != kChildEmpty && tn[i] != __int_as_float(0x7f800000)) mask |= 1u << i;
         }
     }
@@ -241,6 +273,7 @@ struct ClosestWalk {
     uint32_t cur;
     int sp;
     bool ok;   // false after a stack overflow (the hit found so far is kept)
+    bool minmax;   // finite inverse direction: slabTestMinMax
 
     // Returns true when the walk has already ended (an empty scene).
     __device__ __forceinline__ bool begin(const DevScene &sc, V3 o, V3 d, float t0, float t1) {
@@ -250,6 +283,7 @@ struct ClosestWalk {
         org = o;
         dir = d;
         inv = V3{__fdiv_rn(1.0f, d.x), __fdiv_rn(1.0f, d.y), __fdiv_rn(1.0f, d.z)};
+        minmax = isfinite(inv.x) && isfinite(inv.y) && isfinite(inv.z);
         if (WT) wr = wtSetup(o, d);
         tmin = t0;
         tmax = t1;
@@ -265,7 +299,7 @@ struct ClosestWalk {
             if (!(cur & kLeafBit)) {
                 float tn[kBvhWidth];
                 uint32_t ch[kBvhWidth];
-                const uint32_t mask = testChildren<WT>(sc.nodes, cur, org, inv, tmin, tmax, tn, ch);
+                const uint32_t mask = testChildren<WT>(sc.nodes, cur, org, inv, tmin, tmax, tn, ch, minmax);
                 if (mask != 0) {
                     cur = orderChildren(mask, tn, ch, stack, sp, ok);
                     continue;
@@ -335,11 +369,13 @@ struct AnyWalk {
     uint32_t cur;
     int sp;
     bool occluded;
+    bool minmax;
 
     __device__ __forceinline__ bool begin(const DevScene &sc, V3 o, V3 d, float t0, float t1) {
         org = o;
         dir = d;
         inv = V3{__fdiv_rn(1.0f, d.x), __fdiv_rn(1.0f, d.y), __fdiv_rn(1.0f, d.z)};
+        minmax = isfinite(inv.x) && isfinite(inv.y) && isfinite(inv.z);
         if (WT) wr = wtSetup(o, d);
         tmin = t0;
         tmax = t1;
@@ -354,7 +390,7 @@ struct AnyWalk {
             if (!(cur & kLeafBit)) {
                 float tn[kBvhWidth];
                 uint32_t ch[kBvhWidth];
-                const uint32_t mask = testChildren<WT>(sc.nodes, cur, org, inv, tmin, tmax, tn, ch);
+                const uint32_t mask = testChildren<WT>(sc.nodes, cur, org, inv, tmin, tmax, tn, ch, minmax);
                 bool have = false;
                 uint32_t next = 0;
 #pragma unroll
