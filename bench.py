@@ -630,7 +630,8 @@ def main():
             "roofline": roofline,
             "roofline_shade": class_roofline(2) if not BPT else None,
             "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": WIDTH * HEIGHT * 16 * 4, "ms_per_step": e2e_total / len(e2e_ms)},
+                    "d2h_bytes_per_step": WIDTH * HEIGHT * 16 * 4, "ms_per_step": e2e_total / len(e2e_ms),
+                    "steps_ms": [round(x, 3) for x in e2e_ms]},
             "clocks": clk}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(desc, os.cpu_count() or 1, args.cpu_seconds)
