@@ -65,3 +65,28 @@ def test_bsdf_matches_reference(gpu_lib, case):
            "sampled": np.nonzero(s_err > TOL + k_s[b] * ROUNDING)[0],
            "evaluated": np.nonzero(e_err > TOL + k_e * ROUNDING)[0]}
     assert all(len(v) == 0 for v in bad.values()), {k: v[:5].tolist() for k, v in bad.items()}
+
+
+def test_index_pairs_give_the_per_wavelength_values(gpu_lib):
+    """The rough dielectric's evaluation once per distinct index pair equals
+    its evaluation per wavelength: for each wavelength i of the flat-index
+    case, a second BSDF whose index spectra keep wavelength i's pair but make
+    every other wavelength distinct (so that the GPU takes the per-wavelength
+    loop) evaluates the same value at i, bit for bit (the evaluated value at
+    a wavelength depends on that wavelength's pair alone)."""
+    from slr_gb300.api import bsdf_query
+    case = [c for c in bsdf_cases() if c["name"] == "ggx_bsdf_flat"][0]
+    q = case["queries"]
+    ext, intr = case["spec0"], case["spec1"]
+    paired = bsdf_query("ggx_bsdf", ext, intr, None, case["ax"], case["ay"], q)
+    checked = 0
+    for i in range(16):
+        dext = (ext * (1.0 + 1e-3 * np.arange(1, 17, dtype=np.float32))).astype(np.float32)
+        dint = (intr * (1.0 + 2e-3 * np.arange(1, 17, dtype=np.float32))).astype(np.float32)
+        dext[i], dint[i] = ext[i], intr[i]
+        assert len(set(zip(dext.view(np.uint32), dint.view(np.uint32)))) == 16
+        single = bsdf_query("ggx_bsdf", dext, dint, None, case["ax"], case["ay"], q)
+        a, b = paired[:, 21 + i], single[:, 21 + i]
+        assert np.array_equal(a.view(np.uint32), b.view(np.uint32)), (i, int((a != b).sum()))
+        checked += int((a != 0).sum())
+    assert checked > 1000
