@@ -138,3 +138,33 @@ def test_checkpointed_render_equals_one_call(gpu_lib, tmp_path, volumetric):
     np.testing.assert_array_equal(ck.film().view(np.uint32), whole.view(np.uint32))
     with pytest.raises(gpu_lib.SlrGpuError):
         s.render_continue(ck, 1, flags=gpu_lib.FLAG_BPT)
+
+
+def test_queue_counts_account_for_every_ray(gpu_lib):
+    """The per-bounce queue counters of a one-wave render
+    (slrgpu_context_queue_counts, 11 columns per bounce) add up to the
+    render's ray statistics: extension queues (column 7) to the extension
+    rays, shadow rays (column 8) to the shadow rays.  At the first bounce,
+    where no roulette is drawn, every extension ray lands in one shading
+    class (columns 0-5); past it, the paths the roulette at the hit ended are
+    in no class, and a bounce's extension rays never exceed the surface
+    paths the previous bounce shaded."""
+    ctx = gpu_lib.Context(0)
+    s = gpu_lib.Scene(scenes.glossy_box_scene(32, 32), context=ctx)
+    try:
+        _, st = s.render(32, 32, 16, 8, seed=3)
+        q = ctx.queue_counts().astype(np.int64)
+        assert q.shape[1] == 11 and q.shape[0] >= 10
+        assert q[0, 7] == 32 * 32 * 16
+        assert q[:, 7].sum() == st.extension_rays
+        assert q[:, 8].sum() == st.shadow_rays
+        assert q[0, 0:6].sum() == q[0, 7]
+        for b in range(1, q.shape[0]):
+            assert q[b, 0:6].sum() <= q[b, 7]
+            assert q[b, 7] <= q[b - 1, 0:5].sum()
+            assert q[b, 8] <= q[b, 0:5].sum()
+        assert q[9:, :].sum() == 0          # bounces past max depth 8
+        assert (q[:, 9:11] == 0).all()      # the volumetric columns of a surface render
+    finally:
+        s.close()
+        ctx.close()
