@@ -606,6 +606,15 @@ def main():
 
     roofline = class_roofline(dom)
     roofline["kernel_share"] = {names[k]: kern_ms[k] / max(1e-9, sum(kern_ms)) for k in range(5)}
+    # the whole wavefront (the survey's sum): 792 B per bounce (which already
+    # counts the extension and shadow queries) plus the film's 256 B per
+    # path sample, over the summed kernel time of the timed frames
+    roofline_wavefront = None
+    if not BPT:
+        step_bytes = ext_rays * BYTES_SHADE + samples_per_step * args.steps * BYTES_FILM
+        step_achieved = step_bytes / max(1e-12, sum(kern_ms) * 1e-3) / 1e9
+        roofline_wavefront = {"bound": "hbm", "achieved": step_achieved, "peak": peak, "unit": "GB/s",
+                              "frac": step_achieved / peak, "bytes_per_step": step_bytes / max(1, args.steps)}
     if names[dom] == "extend" and not BPT and not VOLUMETRIC:
         roofline["note"] = ("closest-hit BVH walks: bound by the latency of dependent node and triangle loads from L2 "
                             "and by divergent control flow, not by HBM; bytes_per_unit counts only the query's "
@@ -629,6 +638,7 @@ def main():
             "gpu_launches": launches,
             "roofline": roofline,
             "roofline_shade": class_roofline(2) if not BPT else None,
+            "roofline_wavefront": roofline_wavefront,
             "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": WIDTH * HEIGHT * 16 * 4, "ms_per_step": e2e_total / len(e2e_ms),
                     "steps_ms": [round(x, 3) for x in e2e_ms]},
