@@ -176,7 +176,7 @@ def _ref_frame(ref_holder, desc, spp, seed, threads):
     return s
 
 
-BASELINE_BUILD = ("the reference renderer built from its own sources with its release flags (-O3 -DNDEBUG, "
+REFERENCE_BUILD_FLAGS = ("the reference renderer built from its own sources with its release flags (-O3 -DNDEBUG, "
                   "default floating-point contraction) and build-only patches P1-P4, P6-P11 (oracle/build_ref.py)")
 
 
@@ -199,7 +199,7 @@ def cpu_baseline(desc, threads: int, seconds_cap: float = 40.0):
         f"{passes} of the frame's {SPP} passes ({WIDTH}x{HEIGHT}"
     return {"value": total / secs, "unit": METRIC, "cores": threads, "kind": "reference",
             "sample": f"{what}, max depth {MAX_DEPTH}): {total} path samples in {secs:.1f} s with {threads} "
-                      f"threads; SBVH build {build_s:.1f} s excluded; {BASELINE_BUILD}"}
+                      f"threads; SBVH build {build_s:.1f} s excluded; {REFERENCE_BUILD_FLAGS}"}
 
 
 def run_reference(args):
@@ -230,7 +230,7 @@ def run_reference(args):
             "cpu_baseline": {"value": value, "unit": METRIC, "cores": threads, "kind": "reference",
                              "sample": f"{args.steps} timed passes (one sample per pixel over all tiles, the "
                                        f"reference's pass loop) of the {WIDTH}x{HEIGHT} frame, max depth "
-                                       f"{MAX_DEPTH}, {threads} threads; {BASELINE_BUILD}"},
+                                       f"{MAX_DEPTH}, {threads} threads; {REFERENCE_BUILD_FLAGS}"},
             "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
     return 0
