@@ -43,7 +43,7 @@ extern "C" {
 #define SLRGPU_ERR_NOT_COMMITTED    (-5)
 #define SLRGPU_ERR_STATE            (-6)
 #define SLRGPU_ERR_TIMEOUT          (-7)
-#define SLRGPU_ERR_UNSUPPORTED      (-8)   /* a valid request this build does not implement */
+#define SLRGPU_ERR_UNSUPPORTED      (-8)   /* a valid request this library does not implement */
 #define SLRGPU_ERR_CANCELLED        (-9)   /* a server request cancelled by slrgpu_server_cancel */
 
 typedef uint64_t slrgpu_handle;

@@ -44,8 +44,8 @@ Build-only patches (all applied to the copy):
   across hosts.
 * P6 max depth: ``Renderer/PTRenderer.cpp:172`` caps a path at 100 vertices
   and ``Renderer/VolumetricPTRenderer.cpp:185`` has no cap.  Both now stop
-  after ``slr_oracle_max_depth`` scattering vertices (a global the driver
-  sets), which is the ``maxDepth`` the GPU renderer implements.
+  after ``slr_oracle_max_depth`` scattering vertices (a global the oracle driver,
+  ``oracle/ref_driver.cpp``, sets), which is the ``maxDepth`` the GPU renderer implements.
 * P7 ``Core/ProgressReporter.cpp`` is replaced by a no-op implementation (the
   stock one blocks up to 250 ms per progressive pass and can hang on a racy
   counter, ``Core/ProgressReporter.cpp:74-81,101-104``), and the progressive
@@ -53,7 +53,7 @@ Build-only patches (all applied to the copy):
   ``VolumetricPTRenderer.cpp:84``) are disabled so rendering writes no BMPs.
 * P8 the message printed for each dropped non-finite sample
   (``PTRenderer.cpp:138``, ``VolumetricPTRenderer.cpp:138``) is replaced by an
-  increment of a counter the driver reports; which samples are dropped does
+  increment of a counter the oracle driver reports; which samples are dropped does
   not change.
 * P9 ``Renderer/BPTRenderer.cpp``: a subpath stops after
   ``slr_oracle_max_depth`` vertices beyond its first (the stock renderer ends
