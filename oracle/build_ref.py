@@ -69,7 +69,7 @@ Build-only patches (all applied to the copy):
   ``:269``, ``:349``).
 * P12 path tapes (test only): ``Core/random_number_generator.cpp:12-15``
   appends every 32-bit uniform it returns to ``slr_oracle_tape`` when the
-  driver has set it, and ``PTRenderer::Job::kernel`` (``PTRenderer.cpp:107``)
+  oracle driver has set it, and ``PTRenderer::Job::kernel`` (``PTRenderer.cpp:107``)
   calls ``slr_oracle_path_begin()`` before each pixel sample, so that a
   one-thread render records each path's uniforms in the reference's draw
   order; nothing changes while no tape is set.
