@@ -520,6 +520,9 @@ __global__ void kShadeMiss(DevScene scArg, WaveState ws, const uint32_t* __restr
 // Resident blocks per SM the shading kernels are compiled for (register cap
 // 65536 / (256 x this)); compile-time tuning constants, the GGX dielectric's
 // (the largest body: per-wavelength refraction) on its own.
+#ifndef SLRGPU_SHADE_SMEM_ALPHA
+#define SLRGPU_SHADE_SMEM_ALPHA 1
+#endif
 #ifndef SLRGPU_SHADE_MIN_BLOCKS
 #define SLRGPU_SHADE_MIN_BLOCKS 3   // 85 registers: +9 % on the 1M-triangle benchmark over 2 (128)
 #endif
@@ -537,6 +540,12 @@ __global__ void __launch_bounds__(256, K == kMatGGXScattering ? SLRGPU_SHADE_DIE
     const uint32_t N = ws.N;
     const float inf = __int_as_float(0x7f800000);
     const float twoPi = 6.28318530717958647692f;
+#if SLRGPU_SHADE_SMEM_ALPHA
+    // the path's throughput in shared memory ([wavelength][thread]), not in
+    // registers, through light and BSDF sampling
+    __shared__ float sAlpha[kNumLambda * 256];
+#define SLRGPU_ALPHA(k) sAlpha[(k) * 256 + threadIdx.x]
+#endif
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
         const uint32_t i = base + threadIdx.x;
         bool active = i < n;
@@ -557,9 +566,20 @@ __global__ void __launch_bounds__(256, K == kMatGGXScattering ? SLRGPU_SHADE_DIE
             V3 org = V3{ro.x, ro.y, ro.z}, dir = V3{rd.x, rd.y, rd.z};
             float4 hv = ws.hit[p];
             const DevPrim pr = sc.prims[__float_as_uint(hv.w)];
+#if SLRGPU_SHADE_SMEM_ALPHA
+            {
+                Spec a0;
+                if (depth == 0) a0 = specConst(1.0f);
+                else loadSpec(ws.alpha, p, a0);
+#pragma unroll
+                for (int k = 0; k < kNumLambda; ++k) SLRGPU_ALPHA(k) = a0.v[k];
+            }
+#else
             Spec alpha;
             if (depth == 0) alpha = specConst(1.0f);
             else loadSpec(ws.alpha, p, alpha);
+#define SLRGPU_ALPHA(k) alpha.v[k]
+#endif
             bool alive = true;
             SurfPoint sp;
             surfacePoint(sc, pr, org, dir, hv.x, hv.y, hv.z, sp);
@@ -580,18 +600,21 @@ __global__ void __launch_bounds__(256, K == kMatGGXScattering ? SLRGPU_SHADE_DIE
                 }
                 Spec add;
 #pragma unroll
-                for (int k = 0; k < kNumLambda; ++k) add.v[k] = alpha.v[k] * (M.v[k] * edf) * mis;
+                for (int k = 0; k < kNumLambda; ++k) add.v[k] = SLRGPU_ALPHA(k) * (M.v[k] * edf) * mis;
                 addSpec(ws.L, p, add);
             }
             // Russian roulette (PTRenderer.cpp:266-272); a material that does
             // not emit had its draw at the hit (rouletteAtHit), and the path
             // is here because it continued.
             if (depth > 0) {
-                float cp = fminf(importance(alpha, sel) / ws.ps[p].initY, 1.0f);
+                Spec a1;
+#pragma unroll
+                for (int k = 0; k < kNumLambda; ++k) a1.v[k] = SLRGPU_ALPHA(k);
+                float cp = fminf(importance(a1, sel) / ws.ps[p].initY, 1.0f);
                 if ((SLRGPU_EARLY_ROULETTE && mat.emit < 0) || rng.next() < cp) {
                     float r = 1.0f / cp;
 #pragma unroll
-                    for (int k = 0; k < kNumLambda; ++k) alpha.v[k] *= r;
+                    for (int k = 0; k < kNumLambda; ++k) SLRGPU_ALPHA(k) *= r;
                 } else {
                     alive = false;
                 }
@@ -666,7 +689,7 @@ __global__ void __launch_bounds__(256, K == kMatGGXScattering ? SLRGPU_SHADE_DIE
                         bool nz = false;
 #pragma unroll
                         for (int k = 0; k < kNumLambda; ++k) {
-                            c.v[k] = ((alpha.v[k] * (M.v[k] * edfVal)) * fs.v[k]) * scale;
+                            c.v[k] = ((SLRGPU_ALPHA(k) * (M.v[k] * edfVal)) * fs.v[k]) * scale;
                             nz |= c.v[k] != 0.0f;
                         }
                         if (nz) {
@@ -703,7 +726,7 @@ __global__ void __launch_bounds__(256, K == kMatGGXScattering ? SLRGPU_SHADE_DIE
                     float cg = absDot(bs.dir, q.gn);
                     float r = 1.0f / bs.pdf;
 #pragma unroll
-                    for (int k = 0; k < kNumLambda; ++k) alpha.v[k] *= (fs.v[k] * cg) * r;
+                    for (int k = 0; k < kNumLambda; ++k) SLRGPU_ALPHA(k) *= (fs.v[k] * cg) * r;
                     V3 nd = sp.frame.fromLocal(bs.dir);
                     ws.ray[2 * (size_t)p] = make_float4(sp.p.x, sp.p.y, sp.p.z, kRayEpsilon);
                     ws.ray[2 * (size_t)p + 1] = make_float4(nd.x, nd.y, nd.z, inf);
@@ -711,7 +734,12 @@ __global__ void __launch_bounds__(256, K == kMatGGXScattering ? SLRGPU_SHADE_DIE
                     info = (uint32_t)sel | (wlSelected ? kInfoWlSelected : 0u) |
                            (dirIsDelta(bs.type) ? kInfoPrevDelta : 0u) | (depth << kInfoDepthShift) | sceneBits;
                     ws.ps[p].info = info;
-                    storeSpec(ws.alpha, p, alpha);
+                    {
+                        Spec a2;
+#pragma unroll
+                        for (int k = 0; k < kNumLambda; ++k) a2.v[k] = SLRGPU_ALPHA(k);
+                        storeSpec(ws.alpha, p, a2);
+                    }
                     extend = true;
                 }
             }
@@ -723,6 +751,7 @@ __global__ void __launch_bounds__(256, K == kMatGGXScattering ? SLRGPU_SHADE_DIE
 }
 
 // ---------------------------------------------------------------------------
+#undef SLRGPU_ALPHA
 // Volumetric path tracing (VolumetricPTRenderer::Job::contribution,
 // libSLR/Renderer/VolumetricPTRenderer.cpp:146-296)
 // ---------------------------------------------------------------------------
