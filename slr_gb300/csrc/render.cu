@@ -523,6 +523,27 @@ __global__ void kShadeMiss(DevScene scArg, WaveState ws, const uint32_t* __restr
 #ifndef SLRGPU_SHADE_SMEM_ALPHA
 #define SLRGPU_SHADE_SMEM_ALPHA 1
 #endif
+#ifndef SLRGPU_SHADE_SMEM_SP
+#define SLRGPU_SHADE_SMEM_SP 1
+#endif
+// A surface point in shared memory, [component][thread] (blocks of 256).
+__device__ __forceinline__ void storeSurfShared(float* s, const SurfPoint &sp) {
+    const float v[15] = {sp.p.x, sp.p.y, sp.p.z, sp.frame.x.x, sp.frame.x.y, sp.frame.x.z, sp.frame.y.x,
+                         sp.frame.y.y, sp.frame.y.z, sp.frame.z.x, sp.frame.z.y, sp.frame.z.z, sp.gn.x, sp.gn.y,
+                         sp.gn.z};
+#pragma unroll
+    for (int k = 0; k < 15; ++k) s[k * 256 + threadIdx.x] = v[k];
+}
+__device__ __forceinline__ SurfPoint loadSurfShared(const float* s) {
+    float v[15];
+#pragma unroll
+    for (int k = 0; k < 15; ++k) v[k] = s[k * 256 + threadIdx.x];
+    SurfPoint sp;
+    sp.p = V3{v[0], v[1], v[2]};
+    sp.frame = Frame{V3{v[3], v[4], v[5]}, V3{v[6], v[7], v[8]}, V3{v[9], v[10], v[11]}};
+    sp.gn = V3{v[12], v[13], v[14]};
+    return sp;
+}
 #ifndef SLRGPU_SHADE_MIN_BLOCKS
 #define SLRGPU_SHADE_MIN_BLOCKS 3   // 85 registers: +9 % on the 1M-triangle benchmark over 2 (128)
 #endif
@@ -545,6 +566,10 @@ __global__ void __launch_bounds__(256, K == kMatGGXScattering ? SLRGPU_SHADE_DIE
     // registers, through light and BSDF sampling
     __shared__ float sAlpha[kNumLambda * 256];
 #define SLRGPU_ALPHA(k) sAlpha[(k) * 256 + threadIdx.x]
+#endif
+#if SLRGPU_SHADE_SMEM_SP
+    // the surface point likewise, from the BSDF query to the new ray
+    __shared__ float sSurf[15 * 256];
 #endif
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
         const uint32_t i = base + threadIdx.x;
@@ -627,8 +652,15 @@ __global__ void __launch_bounds__(256, K == kMatGGXScattering ? SLRGPU_SHADE_DIE
                 Bsdf B;
                 makeBsdfK<K>(sc, mat, lambdas, wlSelected, B);
                 BsdfQuery q{dirOut, sp.frame.toLocal(sp.gn), sel};
+#if SLRGPU_SHADE_SMEM_SP
+                storeSurfShared(sSurf, sp);
+#define SLRGPU_SP() loadSurfShared(sSurf)
+#else
+#define SLRGPU_SP() sp
+#endif
                 // Next-event estimation (PTRenderer.cpp:179-218).
                 if (bsdfHasNonDelta(K) && (sc.numLights > 0 || sc.envPresent)) {
+                    const SurfPoint spN = SLRGPU_SP();
                     float lightProb;
                     int li = selectLight(sc, rng.next(), &lightProb);
                     float lu0 = rng.next(), lu1 = rng.next();
@@ -648,7 +680,7 @@ __global__ void __launch_bounds__(256, K == kMatGGXScattering ? SLRGPU_SHADE_DIE
                         lgn = V3{lpr.ngx, lpr.ngy, lpr.ngz};
                         areaPdf = lpr.invArea;
                         evalSpectrum(sc, sc.materials[lpr.material].emit, lambdas, M);
-                        V3 diff = lp - sp.p;
+                        V3 diff = lp - spN.p;
                         dist2 = sqLength(diff);
                         shadowDir = diff * (1.0f / sqrtf(dist2));
                         edfVal = dot(lz, -shadowDir) > 0.0f ? kInvPiF : 0.0f;
@@ -672,11 +704,11 @@ __global__ void __launch_bounds__(256, K == kMatGGXScattering ? SLRGPU_SHADE_DIE
                         shadowDir = normalize(lp);
                         dist2 = 1.0f;
                     }
-                    float cosShading = absDot(shadowDir, sp.gn);
+                    float cosShading = absDot(shadowDir, spN.gn);
                     float cosLight = absDot(shadowDir, lgn);
                     if (cosShading * cosLight > 0) {
                         float lightPdf = lightProb * areaPdf;
-                        V3 sdl = sp.frame.toLocal(shadowDir);
+                        V3 sdl = spN.frame.toLocal(shadowDir);
                         Spec fs;
                         bsdfEval<K>(B, q, sdl, fs);
                         float bsdfPdfV = bsdfPdf<K>(B, q, sdl) * cosLight / dist2;
@@ -700,12 +732,12 @@ __global__ void __launch_bounds__(256, K == kMatGGXScattering ? SLRGPU_SHADE_DIE
                                 sdir = shadowDir;
                                 tmax = 3.402823466e+38f;
                             } else {
-                                V3 dd = lp - sp.p;
+                                V3 dd = lp - spN.p;
                                 float dist = length(dd);
                                 sdir = dd * (1.0f / dist);
                                 tmax = dist * (1 - kRayEpsilon);
                             }
-                            ws.shRay[2 * (size_t)p] = make_float4(sp.p.x, sp.p.y, sp.p.z, kRayEpsilon);
+                            ws.shRay[2 * (size_t)p] = make_float4(spN.p.x, spN.p.y, spN.p.z, kRayEpsilon);
                             ws.shRay[2 * (size_t)p + 1] = make_float4(sdir.x, sdir.y, sdir.z, tmax);
                             shadow = true;
                         }
@@ -727,8 +759,9 @@ __global__ void __launch_bounds__(256, K == kMatGGXScattering ? SLRGPU_SHADE_DIE
                     float r = 1.0f / bs.pdf;
 #pragma unroll
                     for (int k = 0; k < kNumLambda; ++k) SLRGPU_ALPHA(k) *= (fs.v[k] * cg) * r;
-                    V3 nd = sp.frame.fromLocal(bs.dir);
-                    ws.ray[2 * (size_t)p] = make_float4(sp.p.x, sp.p.y, sp.p.z, kRayEpsilon);
+                    const SurfPoint spS = SLRGPU_SP();
+                    V3 nd = spS.frame.fromLocal(bs.dir);
+                    ws.ray[2 * (size_t)p] = make_float4(spS.p.x, spS.p.y, spS.p.z, kRayEpsilon);
                     ws.ray[2 * (size_t)p + 1] = make_float4(nd.x, nd.y, nd.z, inf);
                     ws.ps[p].prevPdf = bs.pdf;
                     info = (uint32_t)sel | (wlSelected ? kInfoWlSelected : 0u) |
@@ -752,6 +785,7 @@ __global__ void __launch_bounds__(256, K == kMatGGXScattering ? SLRGPU_SHADE_DIE
 
 // ---------------------------------------------------------------------------
 #undef SLRGPU_ALPHA
+#undef SLRGPU_SP
 // Volumetric path tracing (VolumetricPTRenderer::Job::contribution,
 // libSLR/Renderer/VolumetricPTRenderer.cpp:146-296)
 // ---------------------------------------------------------------------------
