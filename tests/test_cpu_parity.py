@@ -190,3 +190,15 @@ def test_reference_path_tapes(oracle_lib):
     assert len(tapes) == 16 * 8
     assert min(len(t) for t in tapes) >= 7
     assert all(((t >= 0) & (t < 1)).all() for t in tapes)
+
+
+def test_flat_index_case_takes_the_pair_path():
+    """The flat-index dielectric case of the BSDF tests holds between two and
+    four distinct (exterior, interior) pairs over its 16 wavelengths, so the
+    GPU evaluates it through its index-pair path, with more than one pair
+    (the per-wavelength loop takes five or more)."""
+    from tests.bsdf_cases import bsdf_cases
+    c = [x for x in bsdf_cases() if x["name"] == "ggx_bsdf_flat"][0]
+    pairs = set(zip(np.asarray(c["spec0"], np.float32).view(np.uint32),
+                    np.asarray(c["spec1"], np.float32).view(np.uint32)))
+    assert 2 <= len(pairs) <= 4
